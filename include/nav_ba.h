@@ -1,0 +1,211 @@
+/*
+ * nav_ba.h - C ABI of the GB300 bundle-adjustment back end.
+ *
+ * This library replaces the arithmetic that nav24's graph back end hands to g2o:
+ *   NAV24::BE::GraphOptim::solve(const ProblemPtr&)      core/backEnd/BE_GraphOptim.cpp:31-77
+ * for a PR_VBA problem (core/backEnd/Problem.hpp:107-113): keyframe poses, map points and the
+ * observation graph go in, optimized poses and points come out.  Everything is plain C: host
+ * pointers, sizes and integer status codes.  No exception crosses this boundary.
+ *
+ * Conventions
+ *  - A pose is T_cw (world -> camera), passed as 12 doubles: the row-major 3x4 block [R | t]
+ *    of nav24's 4x4 PoseSE3 (core/trajectory/pose/Pose.hpp:104, read at BE_GraphOptim.cpp:91-93).
+ *  - Observations are undistorted pixel measurements (KeyPoint2D::getPointUd,
+ *    core/sensorData/observation/Point2D.hpp:23) with the camera and point they link.
+ *    Observation order is the edge order; any order is accepted.
+ *  - The residual of one observation is e = z - pi(T_cw * X_w) (core/dataTypes/optimization/
+ *    OptimizableTypes.hpp:102-107) with the pinhole projection of core/sensor/camera/models/
+ *    Pinhole.cpp:30-36.  The information matrix is the identity (BE_GraphOptim.cpp:188-189).
+ *  - The cost is g2o's robust chi2: sum over active edges of rho(e^T e), rho = identity or Huber.
+ *  - All arithmetic at this boundary is FP64.  nav24 rounds points and measurements to float
+ *    on the way in and points to float on the way out (BE_GraphOptim.cpp:147,239); that rounding
+ *    belongs to the caller's adapter (nav24_gb300/adapter/GraphOptimGpu.cpp does it).
+ *
+ * Threading: one context per host thread.  A context owns one CUDA stream and its device
+ * buffers; every call on it is synchronous (it returns after results are on the host).
+ */
+#ifndef NAV_BA_H
+#define NAV_BA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NAV_BA_ABI_VERSION 1
+
+typedef enum nav_ba_status {
+    NAV_BA_OK = 0,
+    /* No pose, or no point with an edge: nothing is optimized and the outputs are copies of
+     * the inputs.  nav24 logs a warning and returns in this case (BE_GraphOptim.cpp:59-63). */
+    NAV_BA_EMPTY = 1,
+    NAV_BA_ERR_ARGUMENT = -1,          /* null pointer, negative size, index out of range      */
+    NAV_BA_ERR_NONFINITE_INPUT = -2,   /* NaN/Inf in a pose, point, observation or intrinsic   */
+    NAV_BA_ERR_NONFINITE_COST = -3,    /* the initial cost is not finite (e.g. a point at Z=0) */
+    NAV_BA_ERR_CUDA = -4,              /* a CUDA runtime call failed                           */
+    NAV_BA_ERR_OUT_OF_MEMORY = -5,     /* device or pinned-host allocation failed              */
+    NAV_BA_ERR_UNSUPPORTED = -6,       /* size beyond an engine limit or option combination    */
+    NAV_BA_ERR_DEVICE_TIMEOUT = -7,    /* a bounded device-side wait ran out                   */
+    NAV_BA_ERR_NO_DEVICE = -8          /* no CUDA device, or the device index is invalid       */
+} nav_ba_status;
+
+/* Camera models.  PINHOLE is nav24's Pinhole (Pinhole.cpp:30-36,70-80).  PINHOLE_RADIAL adds
+ * the two-coefficient radial factor d = 1 + k1 r^2 + k2 r^4 on normalized coordinates; it has
+ * no counterpart in nav24's BA (nav24 undistorts before BA, Calibration.cpp:135-148). */
+typedef enum nav_ba_camera_model {
+    NAV_BA_CAM_PINHOLE = 0,
+    NAV_BA_CAM_PINHOLE_RADIAL = 1
+} nav_ba_camera_model;
+
+typedef enum nav_ba_precision {
+    NAV_BA_FP64 = 0,   /* plain: every kernel in FP64                                        */
+    NAV_BA_MIXED = 1   /* FP32 residuals/Jacobians/Hessian blocks; FP64 reduced-system
+                          Cholesky, cost, gain ratio and SE(3) update                         */
+} nav_ba_precision;
+
+typedef enum nav_ba_solver {
+    NAV_BA_SOLVER_CHOLESKY = 0,  /* Schur complement + FP64 Cholesky of the reduced system
+                                    (g2o BlockSolver_6_3 + LinearSolverEigen,
+                                    BE_GraphOptim.cpp:41-45)                                  */
+    NAV_BA_SOLVER_PCG = 1        /* matrix-free Schur + block-Jacobi preconditioned CG        */
+} nav_ba_solver;
+
+/* Why the Levenberg-Marquardt loop stopped (g2o OptimizationAlgorithmLevenberg::solve). */
+typedef enum nav_ba_termination {
+    NAV_BA_TERM_ITERATIONS = 0,        /* ran the requested number of iterations           */
+    NAV_BA_TERM_TRIALS_EXHAUSTED = 1,  /* an iteration used all its damping trials          */
+    NAV_BA_TERM_ZERO_GAIN = 2,         /* gain ratio exactly zero (no change in cost)       */
+    NAV_BA_TERM_LAMBDA_NONFINITE = 3,  /* damping overflowed                                */
+    NAV_BA_TERM_NOTHING_TO_DO = 4      /* no free vertex (all fixed) or an empty problem    */
+} nav_ba_termination;
+
+/* One BA problem (nav24: PR_VBA frames + calibration, Problem.hpp:107-113). */
+typedef struct nav_ba_problem {
+    int32_t n_cams;
+    int32_t n_points;
+    int32_t n_obs;
+    const double* cam_pose;       /* [n_cams][12] row-major [R|t] of T_cw                   */
+    const uint8_t* cam_fixed;     /* [n_cams] 1 = fixed (Frame::isOptFixed); NULL: none     */
+    const double* points;         /* [n_points][3] world coordinates                        */
+    const uint8_t* point_fixed;   /* [n_points] 1 = fixed; NULL: none                       */
+    const double* obs_uv;         /* [n_obs][2] measured pixel (u, v)                       */
+    const int32_t* obs_cam;       /* [n_obs] camera index of each observation               */
+    const int32_t* obs_point;     /* [n_obs] point index of each observation                */
+    int32_t camera_model;         /* nav_ba_camera_model                                    */
+    int32_t reserved0;
+    double intrinsics[8];         /* fx, fy, cx, cy, k1, k2, 0, 0                            */
+} nav_ba_problem;
+
+typedef struct nav_ba_options {
+    int32_t iterations;           /* LM iterations (Problem::getNumIter, Problem.hpp:93)   */
+    int32_t precision;            /* nav_ba_precision                                       */
+    int32_t solver;               /* nav_ba_solver                                          */
+    int32_t robust;               /* 1: Huber kernel on every edge (PR_VBA::mbRobust)       */
+    double huber_delta;           /* Huber threshold in pixels (nav24: float(sqrt(5.99)))   */
+    double initial_lambda;        /* > 0: first damping used as given; <= 0: tau*max diag   */
+    double tau;                   /* g2o default 1e-5                                        */
+    int32_t max_trials;           /* damping trials per iteration (g2o default 10)           */
+    int32_t optimize_distortion;  /* 1: k1,k2 shared by all cameras are optimized            */
+    double pcg_tolerance;         /* relative residual for NAV_BA_SOLVER_PCG                 */
+    int32_t pcg_max_iterations;
+    int32_t deterministic;        /* 1 (default): fixed-order reductions, bitwise repeatable */
+    int32_t reserved[8];
+} nav_ba_options;
+
+typedef struct nav_ba_result {
+    /* outputs, each may be NULL */
+    double* cam_pose_out;         /* [n_cams][12] optimized T_cw (fixed cameras: unchanged)   */
+    double* points_out;           /* [n_points][3] optimized points                          */
+    double* intrinsics_out;       /* [8] (k1,k2 change only with optimize_distortion)         */
+    double* cost_trace;           /* [iterations + 1]: cost before iteration 0, then after
+                                     each iteration that ran                                 */
+    /* statistics, always written */
+    double initial_cost;
+    double final_cost;
+    double final_lambda;
+    double time_setup_ms;         /* host-side structure build and upload                   */
+    double time_solve_ms;         /* device LM loop                                          */
+    double time_download_ms;
+    int32_t iterations_done;
+    int32_t trials_accepted;
+    int32_t trials_rejected;
+    int32_t termination;          /* nav_ba_termination                                     */
+    int32_t n_active_edges;       /* edges in the cost (not both vertices fixed)            */
+    int32_t n_free_cams;
+    int32_t n_free_points;
+    int32_t n_schur_blocks;       /* stored lower-triangle 6x6 blocks of the reduced system */
+    int32_t pcg_iterations_total;
+    int32_t status;               /* nav_ba_status of this problem (batched calls)          */
+    int32_t reserved[6];
+} nav_ba_result;
+
+typedef struct nav_ba_ctx nav_ba_ctx;
+
+/* Fill *opt with the defaults of nav24's call: 5 iterations (Problem.hpp:84), FP64, Cholesky,
+ * no robust kernel (PR_VBA::mbRobust = false), Huber delta float(sqrt(5.99)) (BE_GraphOptim.cpp:125),
+ * tau-initialised damping, 10 trials. */
+void nav_ba_options_default(nav_ba_options* opt);
+
+/* Create a context on CUDA device `device`.  Replaces the per-call g2o optimizer construction
+ * (BE_GraphOptim.cpp:40-49); one context may serve many solves. */
+nav_ba_status nav_ba_create(nav_ba_ctx** ctx, int32_t device);
+void nav_ba_destroy(nav_ba_ctx* ctx);
+
+/* Solve one problem: replaces GraphOptim::solve's graph build (BE_GraphOptim.cpp:51-57),
+ * optimizer.initializeOptimization/optimize(n) (:67-68) and the write-back (:73-76).
+ * Synchronous.  On any error status the outputs are left untouched. */
+nav_ba_status nav_ba_solve(nav_ba_ctx* ctx, const nav_ba_problem* problem,
+                           const nav_ba_options* options, nav_ba_result* result);
+
+/* Solve n_windows independent problems (sliding-window BA of FE_SlamMonoV.cpp:143-166, one
+ * window per tracked frame) in one device launch sequence.  results[i] belongs to windows[i].
+ * Each window is solved exactly as nav_ba_solve would solve it alone.  Windows up to
+ * NAV_BA_WINDOW_MAX_CAMS free cameras use the batched window engine. */
+#define NAV_BA_WINDOW_MAX_CAMS 24
+nav_ba_status nav_ba_solve_batched(nav_ba_ctx* ctx, const nav_ba_problem* windows,
+                                   int32_t n_windows, const nav_ba_options* options,
+                                   nav_ba_result* results);
+
+/* Two-phase form of nav_ba_solve for callers that solve the same graph repeatedly:
+ * nav_ba_prepare builds the structure and uploads the initial state; nav_ba_run runs the
+ * LM loop from that uploaded state on the device (no host transfer of the problem), and
+ * nav_ba_fetch copies the last run's results to the host. */
+nav_ba_status nav_ba_prepare(nav_ba_ctx* ctx, const nav_ba_problem* problem,
+                             const nav_ba_options* options);
+nav_ba_status nav_ba_run(nav_ba_ctx* ctx, const nav_ba_options* options, nav_ba_result* stats);
+nav_ba_status nav_ba_fetch(nav_ba_ctx* ctx, nav_ba_result* result);
+
+/* Residuals and Jacobians of every observation at the problem's initial state, computed by
+ * the device linearization kernel in the given precision (EdgeSE3ProjectXYZ::computeError and
+ * ::linearizeOplus, OptimizableTypes.hpp:102-107, OptimizableTypes.cpp:140-161).
+ *   e  [n_obs][2], jc [n_obs][2][6] (pose, rotation first), jp [n_obs][2][3] (point),
+ *   w  [n_obs] robust weight rho'(e^T e) (1 without a robust kernel).  Any may be NULL. */
+nav_ba_status nav_ba_linearize(nav_ba_ctx* ctx, const nav_ba_problem* problem,
+                               const nav_ba_options* options, double* e, double* jc,
+                               double* jp, double* w);
+
+/* Reduced camera system at the initial state for damping `lambda`, assembled on the device:
+ * S = U + lambda I - W (V + lambda I)^-1 W^T and b' (g2o BlockSolver::solve's Schur step).
+ * Free cameras are numbered in input order; s is [6 nf][6 nf] row-major (both triangles), b is
+ * [6 nf], cam_index [n_cams] receives each camera's free index or -1.  *n_free receives nf;
+ * s and b are written only when capacity_free >= nf. */
+nav_ba_status nav_ba_reduced_system(nav_ba_ctx* ctx, const nav_ba_problem* problem,
+                                    const nav_ba_options* options, double lambda,
+                                    int32_t capacity_free, int32_t* n_free, double* s,
+                                    double* b, int32_t* cam_index);
+
+/* Robust chi2 of the problem's initial state, evaluated on the device in FP64. */
+nav_ba_status nav_ba_cost(nav_ba_ctx* ctx, const nav_ba_problem* problem,
+                          const nav_ba_options* options, double* cost);
+
+/* Last error message of the context (empty string if none). */
+const char* nav_ba_last_error(const nav_ba_ctx* ctx);
+const char* nav_ba_status_string(nav_ba_status status);
+int32_t nav_ba_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NAV_BA_H */

@@ -1,0 +1,185 @@
+"""ctypes binding of libnavba.so (the product C ABI, include/nav_ba.h).
+
+The library is built in-tree (nav24_gb300/_build).  Loading fails loudly when it is missing:
+there is no CPU fallback for any entry point.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+from . import abi
+
+LIB_PATH = Path(__file__).resolve().parent / "_build" / "libnavba.so"
+
+# Every entry point declared in include/nav_ba.h.
+EXPORTS = [
+    "nav_ba_options_default", "nav_ba_create", "nav_ba_destroy", "nav_ba_solve",
+    "nav_ba_solve_batched", "nav_ba_prepare", "nav_ba_run", "nav_ba_fetch", "nav_ba_linearize",
+    "nav_ba_reduced_system", "nav_ba_cost", "nav_ba_last_error", "nav_ba_status_string",
+    "nav_ba_abi_version",
+]
+
+_LIB = None
+
+
+class NativeLibraryMissing(RuntimeError):
+    pass
+
+
+def load(path: os.PathLike | None = None) -> C.CDLL:
+    """Load libnavba.so and declare its signatures (raises if the library is absent)."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise NativeLibraryMissing(f"{p} is missing: build it with nav24_gb300.build.build_product()")
+    L = C.CDLL(str(p))
+    P, O, R = C.POINTER(abi.nav_ba_problem), C.POINTER(abi.nav_ba_options), C.POINTER(abi.nav_ba_result)
+    dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int32)
+    ctxp = C.c_void_p
+    L.nav_ba_options_default.argtypes = [O]
+    L.nav_ba_options_default.restype = None
+    L.nav_ba_create.argtypes = [C.POINTER(ctxp), C.c_int32]
+    L.nav_ba_create.restype = C.c_int
+    L.nav_ba_destroy.argtypes = [ctxp]
+    L.nav_ba_destroy.restype = None
+    L.nav_ba_solve.argtypes = [ctxp, P, O, R]
+    L.nav_ba_solve.restype = C.c_int
+    L.nav_ba_solve_batched.argtypes = [ctxp, P, C.c_int32, O, R]
+    L.nav_ba_solve_batched.restype = C.c_int
+    L.nav_ba_prepare.argtypes = [ctxp, P, O]
+    L.nav_ba_prepare.restype = C.c_int
+    L.nav_ba_run.argtypes = [ctxp, O, R]
+    L.nav_ba_run.restype = C.c_int
+    L.nav_ba_fetch.argtypes = [ctxp, R]
+    L.nav_ba_fetch.restype = C.c_int
+    L.nav_ba_linearize.argtypes = [ctxp, P, O, dp, dp, dp, dp]
+    L.nav_ba_linearize.restype = C.c_int
+    L.nav_ba_reduced_system.argtypes = [ctxp, P, O, C.c_double, C.c_int32, ip, dp, dp, ip]
+    L.nav_ba_reduced_system.restype = C.c_int
+    L.nav_ba_cost.argtypes = [ctxp, P, O, dp]
+    L.nav_ba_cost.restype = C.c_int
+    L.nav_ba_last_error.argtypes = [ctxp]
+    L.nav_ba_last_error.restype = C.c_char_p
+    L.nav_ba_status_string.argtypes = [C.c_int]
+    L.nav_ba_status_string.restype = C.c_char_p
+    L.nav_ba_abi_version.argtypes = []
+    L.nav_ba_abi_version.restype = C.c_int32
+    if path is None:
+        _LIB = L
+    return L
+
+
+def _d(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class BAError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"status {status}: {msg}")
+        self.status = status
+
+
+class Context:
+    """One nav_ba_ctx (one CUDA stream on one device)."""
+
+    def __init__(self, device: int = 0):
+        self.L = load()
+        h = C.c_void_p()
+        st = self.L.nav_ba_create(C.byref(h), device)
+        if st != abi.OK:
+            raise BAError(st, self.L.nav_ba_status_string(st).decode())
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.nav_ba_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def last_error(self) -> str:
+        return self.L.nav_ba_last_error(self.h).decode()
+
+    def _check(self, st: int, ok=(abi.OK,)):
+        if st not in ok:
+            raise BAError(st, self.last_error() or self.L.nav_ba_status_string(st).decode())
+        return st
+
+    def solve(self, prob: abi.Problem, opt: abi.nav_ba_options, raise_on_error=True) -> abi.Result:
+        buf = abi.ResultBuffers(prob, opt.iterations)
+        p = prob.as_c()
+        st = self.L.nav_ba_solve(self.h, C.byref(p), C.byref(opt), C.byref(buf.c))
+        if raise_on_error:
+            self._check(st, (abi.OK, abi.EMPTY))
+        return buf.result(st)
+
+    def solve_batched(self, probs: list[abi.Problem], opt: abi.nav_ba_options) -> list[abi.Result]:
+        n = len(probs)
+        cp = (abi.nav_ba_problem * n)(*[p.as_c() for p in probs])
+        bufs = [abi.ResultBuffers(p, opt.iterations) for p in probs]
+        cr = (abi.nav_ba_result * n)(*[b.c for b in bufs])
+        st = self.L.nav_ba_solve_batched(self.h, cp, n, C.byref(opt), cr)
+        self._check(st)
+        out = []
+        for b, r in zip(bufs, cr):
+            b.c = r
+            out.append(b.result(r.status))
+        return out
+
+    def prepare(self, prob: abi.Problem, opt: abi.nav_ba_options):
+        self._prepared = prob  # keep the arrays alive
+        p = prob.as_c()
+        self._check(self.L.nav_ba_prepare(self.h, C.byref(p), C.byref(opt)))
+
+    def run(self, opt: abi.nav_ba_options) -> dict:
+        r = abi.nav_ba_result()
+        self._check(self.L.nav_ba_run(self.h, C.byref(opt), C.byref(r)))
+        return {name: getattr(r, name) for name, _ in abi.nav_ba_result._fields_
+                if name not in ("cam_pose_out", "points_out", "intrinsics_out", "cost_trace", "reserved")}
+
+    def fetch(self, opt: abi.nav_ba_options) -> abi.Result:
+        buf = abi.ResultBuffers(self._prepared, opt.iterations)
+        st = self.L.nav_ba_fetch(self.h, C.byref(buf.c))
+        self._check(st)
+        return buf.result(st)
+
+    def linearize(self, prob: abi.Problem, opt: abi.nav_ba_options):
+        n = prob.n_obs
+        e, jc, jp, w = (np.zeros((n, 2)), np.zeros((n, 2, 6)), np.zeros((n, 2, 3)), np.zeros(n))
+        p = prob.as_c()
+        self._check(self.L.nav_ba_linearize(self.h, C.byref(p), C.byref(opt), _d(e), _d(jc), _d(jp), _d(w)))
+        return e, jc, jp, w
+
+    def reduced_system(self, prob: abi.Problem, opt: abi.nav_ba_options, lam: float):
+        p = prob.as_c()
+        nf = C.c_int32()
+        idx = np.zeros(max(1, prob.n_cams), np.int32)
+        ip = idx.ctypes.data_as(C.POINTER(C.c_int32))
+        self._check(self.L.nav_ba_reduced_system(self.h, C.byref(p), C.byref(opt), lam, 0, C.byref(nf), None, None, ip))
+        n = 6 * nf.value
+        S, b = np.zeros((n, n)), np.zeros(n)
+        self._check(self.L.nav_ba_reduced_system(self.h, C.byref(p), C.byref(opt), lam, nf.value, C.byref(nf),
+                                                 _d(S), _d(b), ip))
+        return S, b, idx[: prob.n_cams]
+
+    def cost(self, prob: abi.Problem, opt: abi.nav_ba_options) -> float:
+        p = prob.as_c()
+        c = C.c_double()
+        self._check(self.L.nav_ba_cost(self.h, C.byref(p), C.byref(opt), C.byref(c)))
+        return c.value

@@ -1,0 +1,276 @@
+// ba_math.cuh - device/host math of the BA edge and the SE(3) vertex.
+//
+// Edge: nav24's EdgeSE3ProjectXYZ (core/dataTypes/optimization/OptimizableTypes.hpp:92-118,
+// OptimizableTypes.cpp:140-161): e = z - pi(T X), J_point = -Jpi R, J_pose = -Jpi [-[Xc]x | I]
+// with the pinhole pi of core/sensor/camera/models/Pinhole.cpp:30-36,70-80.
+// Vertex update: g2o VertexSE3Expmap (T <- exp(d) T, d = [omega; upsilon]) as used through
+// nav24's MyVertexSE3Expmap (OptimizableTypes.hpp:221-227); point update X += d
+// (MyVertexSBAPointXYZ, :229-235).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#define NAVBA_HD __host__ __device__ __forceinline__
+
+namespace navba {
+
+struct Intr {
+    double fx, fy, cx, cy, k1, k2;
+    int model;  // 0 pinhole, 1 pinhole + radial(k1,k2)
+};
+
+// ---- quaternions (x, y, z, w), unit, w >= 0 ---------------------------------------------
+
+NAVBA_HD void q_normalize(double* q) {
+    if (q[3] < 0) {
+        q[0] = -q[0]; q[1] = -q[1]; q[2] = -q[2]; q[3] = -q[3];
+    }
+    const double n = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+    q[0] /= n; q[1] /= n; q[2] /= n; q[3] /= n;
+}
+
+// Shepperd's method: quaternion of a row-major rotation matrix.
+NAVBA_HD void q_from_rot(const double* R, double* q) {
+    const double tr = R[0] + R[4] + R[8];
+    if (tr > 0.0) {
+        double s = sqrt(tr + 1.0);
+        q[3] = 0.5 * s;
+        s = 0.5 / s;
+        q[0] = (R[7] - R[5]) * s;
+        q[1] = (R[2] - R[6]) * s;
+        q[2] = (R[3] - R[1]) * s;
+    } else {
+        int i = 0;
+        if (R[4] > R[0]) i = 1;
+        if (R[8] > R[i * 4]) i = 2;
+        const int j = (i + 1) % 3, k = (j + 1) % 3;
+        double s = sqrt(R[i * 4] - R[j * 4] - R[k * 4] + 1.0);
+        q[i] = 0.5 * s;
+        s = 0.5 / s;
+        q[3] = (R[k * 3 + j] - R[j * 3 + k]) * s;
+        q[j] = (R[j * 3 + i] + R[i * 3 + j]) * s;
+        q[k] = (R[k * 3 + i] + R[i * 3 + k]) * s;
+    }
+}
+
+NAVBA_HD void rot_from_q(const double* q, double* R) {
+    const double tx = 2 * q[0], ty = 2 * q[1], tz = 2 * q[2];
+    const double twx = tx * q[3], twy = ty * q[3], twz = tz * q[3];
+    const double txx = tx * q[0], txy = ty * q[0], txz = tz * q[0];
+    const double tyy = ty * q[1], tyz = tz * q[1], tzz = tz * q[2];
+    R[0] = 1 - (tyy + tzz); R[1] = txy - twz;       R[2] = txz + twy;
+    R[3] = txy + twz;       R[4] = 1 - (txx + tzz); R[5] = tyz - twx;
+    R[6] = txz - twy;       R[7] = tyz + twx;       R[8] = 1 - (txx + tyy);
+}
+
+NAVBA_HD void q_rotate(const double* q, const double* v, double* o) {
+    double uv0 = q[1] * v[2] - q[2] * v[1], uv1 = q[2] * v[0] - q[0] * v[2], uv2 = q[0] * v[1] - q[1] * v[0];
+    uv0 += uv0; uv1 += uv1; uv2 += uv2;
+    o[0] = v[0] + q[3] * uv0 + (q[1] * uv2 - q[2] * uv1);
+    o[1] = v[1] + q[3] * uv1 + (q[2] * uv0 - q[0] * uv2);
+    o[2] = v[2] + q[3] * uv2 + (q[0] * uv1 - q[1] * uv0);
+}
+
+NAVBA_HD void q_mul(const double* a, const double* b, double* r) {
+    r[3] = a[3] * b[3] - a[0] * b[0] - a[1] * b[1] - a[2] * b[2];
+    r[0] = a[3] * b[0] + a[0] * b[3] + a[1] * b[2] - a[2] * b[1];
+    r[1] = a[3] * b[1] + a[1] * b[3] + a[2] * b[0] - a[0] * b[2];
+    r[2] = a[3] * b[2] + a[2] * b[3] + a[0] * b[1] - a[1] * b[0];
+}
+
+// Pose state of one camera: q (4), t (3), pad, R (9) derived from q, pad -> 18 doubles.
+struct CamState {
+    double q[4];
+    double t[3];
+    double pad0;
+    double R[9];
+    double pad1;
+};
+
+NAVBA_HD void cam_from_pose12(const double* P, CamState& c) {
+    const double R[9] = {P[0], P[1], P[2], P[4], P[5], P[6], P[8], P[9], P[10]};
+    q_from_rot(R, c.q);
+    q_normalize(c.q);
+    c.t[0] = P[3]; c.t[1] = P[7]; c.t[2] = P[11];
+    rot_from_q(c.q, c.R);
+    c.pad0 = 0.0;
+    c.pad1 = 0.0;
+}
+
+NAVBA_HD void pose12_from_cam(const CamState& c, double* P) {
+    for (int r = 0; r < 3; ++r) {
+        P[r * 4 + 0] = c.R[r * 3 + 0];
+        P[r * 4 + 1] = c.R[r * 3 + 1];
+        P[r * 4 + 2] = c.R[r * 3 + 2];
+        P[r * 4 + 3] = c.t[r];
+    }
+}
+
+// T <- exp(d) * T with g2o's SE3Quat::exp (small-angle branch R = V = I + W + W^2 for
+// |omega| < 1e-5) and SE3Quat::operator* (t = t_d + q_d t, q = q_d q, normalized).
+NAVBA_HD void se3_left_update(const double* d, const CamState& in, CamState& out) {
+    const double w0 = d[0], w1 = d[1], w2 = d[2];
+    const double th = sqrt(w0 * w0 + w1 * w1 + w2 * w2);
+    const double W[9] = {0, -w2, w1, w2, 0, -w0, -w1, w0, 0};
+    double W2[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            W2[i * 3 + j] = W[i * 3 + 0] * W[0 * 3 + j] + W[i * 3 + 1] * W[1 * 3 + j] + W[i * 3 + 2] * W[2 * 3 + j];
+    double R[9], V[9];
+    if (th < 0.00001) {
+        for (int k = 0; k < 9; ++k) R[k] = ((k % 4) == 0 ? 1.0 : 0.0) + W[k] + W2[k];
+        for (int k = 0; k < 9; ++k) V[k] = R[k];
+    } else {
+        double s, c;
+        sincos(th, &s, &c);
+        const double a = s / th;
+        const double b = (1 - c) / (th * th);
+        const double cc = (th - s) / (th * th * th);
+        for (int k = 0; k < 9; ++k) R[k] = ((k % 4) == 0 ? 1.0 : 0.0) + a * W[k] + b * W2[k];
+        for (int k = 0; k < 9; ++k) V[k] = ((k % 4) == 0 ? 1.0 : 0.0) + b * W[k] + cc * W2[k];
+    }
+    double qd[4];
+    q_from_rot(R, qd);
+    q_normalize(qd);
+    double td[3];
+    for (int i = 0; i < 3; ++i) td[i] = V[i * 3 + 0] * d[3] + V[i * 3 + 1] * d[4] + V[i * 3 + 2] * d[5];
+    double rt[3];
+    q_rotate(qd, in.t, rt);
+    for (int i = 0; i < 3; ++i) out.t[i] = td[i] + rt[i];
+    q_mul(qd, in.q, out.q);
+    q_normalize(out.q);
+    rot_from_q(out.q, out.R);
+    out.pad0 = 0.0;
+    out.pad1 = 0.0;
+}
+
+// ---- edge ------------------------------------------------------------------------------
+
+template <class Real>
+struct EdgeLin {
+    Real e[2];
+    Real jc[12];  // 2x6, rotation first
+    Real jp[6];   // 2x3
+    Real w;       // rho'(e^T e)
+    double rho;   // rho(e^T e)
+};
+
+// Huber (g2o RobustKernelHuber::robustify): rho(s) = s for s <= d^2 else 2 d sqrt(s) - d^2,
+// rho'(s) = 1 or d / sqrt(s).
+template <class Real>
+NAVBA_HD void huber(Real s, bool robust, Real delta, double& rho, Real& w) {
+    if (!robust || s <= delta * delta) {
+        rho = (double)s;
+        w = Real(1);
+    } else {
+        const Real r = sqrt(s);
+        rho = (double)(Real(2) * r * delta - delta * delta);
+        w = delta / r;
+    }
+}
+
+// Camera-frame point Xc = R X + t in precision Real.
+template <class Real>
+NAVBA_HD void transform(const Real* R, const Real* t, const Real* X, Real* Xc) {
+    Xc[0] = R[0] * X[0] + R[1] * X[1] + R[2] * X[2] + t[0];
+    Xc[1] = R[3] * X[0] + R[4] * X[1] + R[5] * X[2] + t[1];
+    Xc[2] = R[6] * X[0] + R[7] * X[1] + R[8] * X[2] + t[2];
+}
+
+// Projection pi(Xc) and, if J != nullptr, d pi / d Xc (2x3).
+template <class Real>
+NAVBA_HD void project(const Intr& in, const Real* Xc, Real* uv, Real* J) {
+    const Real x = Xc[0], y = Xc[1], z = Xc[2];
+    const Real fx = (Real)in.fx, fy = (Real)in.fy, cx = (Real)in.cx, cy = (Real)in.cy;
+    if (in.model == 0) {
+        uv[0] = fx * x / z + cx;
+        uv[1] = fy * y / z + cy;
+        if (J) {
+            J[0] = fx / z; J[1] = Real(0); J[2] = -fx * x / (z * z);
+            J[3] = Real(0); J[4] = fy / z; J[5] = -fy * y / (z * z);
+        }
+    } else {
+        const Real k1 = (Real)in.k1, k2 = (Real)in.k2;
+        const Real xn = x / z, yn = y / z;
+        const Real r2 = xn * xn + yn * yn;
+        const Real d = Real(1) + k1 * r2 + k2 * r2 * r2;
+        uv[0] = fx * d * xn + cx;
+        uv[1] = fy * d * yn + cy;
+        if (J) {
+            const Real c = k1 + Real(2) * k2 * r2;
+            const Real a00 = fx * (d + Real(2) * xn * xn * c), a01 = fx * Real(2) * xn * yn * c;
+            const Real a10 = fy * Real(2) * xn * yn * c, a11 = fy * (d + Real(2) * yn * yn * c);
+            const Real iz = Real(1) / z;
+            J[0] = a00 * iz; J[1] = a01 * iz; J[2] = -(a00 * xn + a01 * yn) * iz;
+            J[3] = a10 * iz; J[4] = a11 * iz; J[5] = -(a10 * xn + a11 * yn) * iz;
+        }
+    }
+}
+
+// Residual, Jacobians and robust weight of one edge (EdgeSE3ProjectXYZ::computeError and
+// ::linearizeOplus).  R, t: camera rotation/translation; X: world point; z: measurement.
+template <class Real>
+NAVBA_HD void edge_linearize(const Intr& in, const Real* R, const Real* t, const Real* X,
+                             const Real* z, bool robust, Real delta, EdgeLin<Real>& L) {
+    Real Xc[3], uv[2], J[6];
+    transform(R, t, X, Xc);
+    project(in, Xc, uv, J);
+    L.e[0] = z[0] - uv[0];
+    L.e[1] = z[1] - uv[1];
+    huber<Real>(L.e[0] * L.e[0] + L.e[1] * L.e[1], robust, delta, L.rho, L.w);
+    Real P[6];
+    for (int k = 0; k < 6; ++k) P[k] = -J[k];
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            L.jp[r * 3 + c] = P[r * 3 + 0] * R[0 * 3 + c] + P[r * 3 + 1] * R[1 * 3 + c] + P[r * 3 + 2] * R[2 * 3 + c];
+    const Real x = Xc[0], y = Xc[1], zc = Xc[2];
+    // J_pose = P * [[0, z, -y, 1, 0, 0], [-z, 0, x, 0, 1, 0], [y, -x, 0, 0, 0, 1]]
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const Real p0 = P[r * 3 + 0], p1 = P[r * 3 + 1], p2 = P[r * 3 + 2];
+        L.jc[r * 6 + 0] = -p1 * zc + p2 * y;
+        L.jc[r * 6 + 1] = p0 * zc - p2 * x;
+        L.jc[r * 6 + 2] = -p0 * y + p1 * x;
+        L.jc[r * 6 + 3] = p0;
+        L.jc[r * 6 + 4] = p1;
+        L.jc[r * 6 + 5] = p2;
+    }
+}
+
+// Robust chi2 of one edge, in precision Real.
+template <class Real>
+NAVBA_HD double edge_cost(const Intr& in, const Real* R, const Real* t, const Real* X,
+                          const Real* z, bool robust, Real delta) {
+    Real Xc[3], uv[2];
+    transform(R, t, X, Xc);
+    project<Real>(in, Xc, uv, nullptr);
+    const Real e0 = z[0] - uv[0], e1 = z[1] - uv[1];
+    double rho;
+    Real w;
+    huber<Real>(e0 * e0 + e1 * e1, robust, delta, rho, w);
+    return rho;
+}
+
+// Inverse of a symmetric 3x3 (packed a00 a01 a02 a11 a12 a22) by its adjugate; returns the
+// packed inverse.  Same formula as Eigen's fixed-size inverse used by g2o's Schur step.
+template <class Real>
+NAVBA_HD void inv_sym3(const Real* v, Real* o) {
+    const Real m00 = v[0], m01 = v[1], m02 = v[2], m11 = v[3], m12 = v[4], m22 = v[5];
+    const Real c00 = m11 * m22 - m12 * m12;
+    const Real c10 = m12 * m02 - m01 * m22;
+    const Real c20 = m01 * m12 - m11 * m02;
+    const Real det = m00 * c00 + m01 * c10 + m02 * c20;
+    const Real id = Real(1) / det;
+    o[0] = c00 * id;
+    o[1] = (m02 * m12 - m01 * m22) * id;
+    o[2] = (m01 * m12 - m02 * m11) * id;
+    o[3] = (m00 * m22 - m02 * m02) * id;
+    o[4] = (m02 * m01 - m00 * m12) * id;
+    o[5] = (m00 * m11 - m01 * m01) * id;
+}
+
+}  // namespace navba

@@ -1,0 +1,109 @@
+// engine.hpp - device engines behind the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/nav_ba.h"
+#include "ba_math.cuh"
+#include "structure.hpp"
+
+namespace navba {
+
+// Limits of the window engine (one CTA solves one window; S lives in shared memory).
+constexpr int kWinMaxFreeCams = NAV_BA_WINDOW_MAX_CAMS;  // 6*24 = 144 reduced unknowns
+constexpr int kWinMaxCams = 64;                          // cameras per window, fixed ones included
+
+struct WinDesc {
+    int32_t cam0, ncam;   // camera range (global)
+    int32_t pt0, npt;     // point range (global)
+    int32_t e0, ne;       // active-edge range (global), point-major
+    int32_t nfc, nfp;     // free cameras / points
+};
+
+struct WinStats {
+    double initial_cost, final_cost, final_lambda;
+    int32_t iterations_done, accepted, rejected, termination;
+    int32_t status, pad0, pad1, pad2;
+};
+
+// Per-launch options of the LM loop.
+struct LmOptions {
+    int32_t iterations;
+    int32_t max_trials;
+    int32_t robust;
+    int32_t pad;
+    double huber_delta;
+    double initial_lambda;
+    double tau;
+};
+
+// A batch of windows resident on the device (inputs, scratch and outputs).
+struct WindowBatch {
+    int32_t n_win = 0;        // windows in the batch (stats/trace rows)
+    int32_t n_queue = 0;      // windows the kernel solves (the work queue)
+    int64_t ncam = 0, npt = 0, ne = 0;
+    int32_t max_m = 0;        // largest 6 * nfc in the batch
+    int32_t max_ncam = 0;
+    int32_t precision = 0;    // buffers sized for this precision
+    int32_t trace_stride = 0; // iterations + 1
+    // device inputs
+    WinDesc* d_win = nullptr;
+    int32_t* d_order = nullptr;
+    int32_t* d_queue = nullptr;
+    CamState* d_cam_init = nullptr;
+    int32_t* d_cam_free = nullptr;
+    double* d_pt_init = nullptr;   // [npt][4]
+    int32_t* d_pt_free = nullptr;
+    int32_t* d_pt_eoff = nullptr;  // [npt + 1] global edge offsets
+    int32_t* d_edge_cam = nullptr; // window-local camera of each edge
+    int32_t* d_edge_pt = nullptr;  // window-local point of each edge
+    double* d_edge_uv = nullptr;   // [ne][2]
+    // device scratch
+    double* d_x[2] = {nullptr, nullptr};  // [npt][4] current / trial points
+    void* d_pt_vg = nullptr;       // [npt][12] Real: V (6 packed) g (3)
+    void* d_pt_vinv = nullptr;     // [npt][8]  Real
+    void* d_edge_jce = nullptr;    // [ne][16]  Real: jc (12) e (2) w (1)
+    void* d_edge_w = nullptr;      // [ne][18]  Real
+    void* d_edge_y = nullptr;      // [ne][18]  Real
+    int32_t* d_cam_list = nullptr; // [ne] camera-major edge list (free cameras only)
+    // device outputs
+    CamState* d_cam_out = nullptr;
+    double* d_pt_out = nullptr;    // [npt][4]
+    double* d_trace = nullptr;     // [n_win][trace_stride]
+    WinStats* d_stats = nullptr;
+    double* d_debug = nullptr;     // reduced-system debug output (optional)
+    size_t bytes = 0;
+};
+
+// Host side of a prepared batch: the built windows and their device copy.
+struct PreparedBatch {
+    std::vector<HostWindow> host;
+    std::vector<int32_t> host_status;  // per window: NAV_BA_OK / NAV_BA_EMPTY / error
+    std::vector<WinDesc> desc;
+    WindowBatch dev;
+    LmOptions lm{};
+    Intr intr{};
+};
+
+// Allocate and upload (stream-ordered, synchronous on return).  Returns a CUDA error or 0.
+cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int precision,
+                                int trace_stride, std::string* why);
+void window_batch_free(WindowBatch& b);
+
+// Launch the persistent window kernel over all windows of the batch.
+// debug_lambda >= 0 stops after assembling the reduced system of window 0 at that damping
+// and writes [S (m*m) | b (m)] to d_debug.
+cudaError_t window_batch_launch(PreparedBatch& pb, cudaStream_t stream, int precision,
+                                int threads, double debug_lambda);
+
+// Linearize every observation of a problem at its initial state (device, precision given);
+// outputs in observation order, FP64.
+cudaError_t linearize_observations(const nav_ba_problem& p, const nav_ba_options& o,
+                                   cudaStream_t stream, double* e, double* jc, double* jp,
+                                   double* w, std::string* why);
+
+}  // namespace navba

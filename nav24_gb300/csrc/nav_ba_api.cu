@@ -1,0 +1,464 @@
+// nav_ba_api.cu - the C ABI of include/nav_ba.h.
+//
+// Replaces nav24's GraphOptim::solve (core/backEnd/BE_GraphOptim.cpp:31-77): graph build
+// (structure.cpp), LM on the device (window_engine.cu), write-back of poses and points.
+#include <chrono>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "engine.hpp"
+
+using namespace navba;
+
+struct nav_ba_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::string last_error;
+    PreparedBatch prepared;
+    std::vector<nav_ba_problem> prepared_problems;  // shapes of the prepared problem (no data)
+    nav_ba_options prepared_opts{};
+    bool has_prepared = false;
+    int threads_fp64 = 256;
+    int threads_mixed = 256;
+};
+
+namespace {
+
+double ms_since(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+nav_ba_status set_err(nav_ba_ctx* ctx, nav_ba_status st, const std::string& msg) {
+    if (ctx) ctx->last_error = msg;
+    return st;
+}
+
+nav_ba_status cuda_status(nav_ba_ctx* ctx, cudaError_t e, const char* where) {
+    if (e == cudaSuccess) return NAV_BA_OK;
+    const nav_ba_status st = (e == cudaErrorMemoryAllocation) ? NAV_BA_ERR_OUT_OF_MEMORY : NAV_BA_ERR_CUDA;
+    return set_err(ctx, st, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+LmOptions lm_options(const nav_ba_options& o) {
+    LmOptions lm{};
+    lm.iterations = o.iterations;
+    lm.max_trials = o.max_trials;
+    lm.robust = o.robust;
+    lm.huber_delta = o.huber_delta;
+    lm.initial_lambda = o.initial_lambda;
+    lm.tau = o.tau;
+    return lm;
+}
+
+Intr intrinsics_of(const nav_ba_problem& p) {
+    return Intr{p.intrinsics[0], p.intrinsics[1], p.intrinsics[2], p.intrinsics[3],
+                p.intrinsics[4], p.intrinsics[5], p.camera_model};
+}
+
+// Outputs of a problem nothing is done to: the round-trip of each pose through its quaternion
+// (as nav24's recoverPose writes every pose vertex back) and the input points.
+void write_passthrough(const nav_ba_problem& p, nav_ba_result* r, bool roundtrip) {
+    if (r->cam_pose_out) {
+        for (int c = 0; c < p.n_cams; ++c) {
+            if (roundtrip) {
+                CamState cs;
+                cam_from_pose12(p.cam_pose + 12LL * c, cs);
+                pose12_from_cam(cs, r->cam_pose_out + 12LL * c);
+            } else {
+                std::memcpy(r->cam_pose_out + 12LL * c, p.cam_pose + 12LL * c, sizeof(double) * 12);
+            }
+        }
+    }
+    if (r->points_out) std::memcpy(r->points_out, p.points, sizeof(double) * 3 * p.n_points);
+    if (r->intrinsics_out) std::memcpy(r->intrinsics_out, p.intrinsics, sizeof(double) * 8);
+}
+
+void clear_stats(nav_ba_result* r) {
+    r->initial_cost = r->final_cost = r->final_lambda = 0.0;
+    r->time_setup_ms = r->time_solve_ms = r->time_download_ms = 0.0;
+    r->iterations_done = r->trials_accepted = r->trials_rejected = 0;
+    r->termination = NAV_BA_TERM_ITERATIONS;
+    r->n_active_edges = r->n_free_cams = r->n_free_points = r->n_schur_blocks = 0;
+    r->pcg_iterations_total = 0;
+    r->status = NAV_BA_OK;
+}
+
+bool fits_window_engine(const HostWindow& h) { return h.nfc <= kWinMaxFreeCams && h.ncam <= kWinMaxCams; }
+
+// Validate and build all windows on the host.  Returns an error (nothing written) or OK.
+nav_ba_status build_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, const nav_ba_options* o,
+                          PreparedBatch& pb) {
+    std::string why;
+    nav_ba_status st = validate_options(o, &why);
+    if (st != NAV_BA_OK) return set_err(ctx, st, why);
+    if (o->solver != NAV_BA_SOLVER_CHOLESKY)
+        return set_err(ctx, NAV_BA_ERR_UNSUPPORTED, "the window engine solves the reduced system by Cholesky");
+    for (int i = 0; i < n; ++i) {
+        st = validate_problem(&probs[i], &why);
+        if (st != NAV_BA_OK) return set_err(ctx, st, "problem " + std::to_string(i) + ": " + why);
+        if (o->optimize_distortion && probs[i].camera_model == NAV_BA_CAM_PINHOLE_RADIAL)
+            return set_err(ctx, NAV_BA_ERR_UNSUPPORTED, "distortion optimization needs the PCG solver");
+        if (i > 0 && std::memcmp(probs[i].intrinsics, probs[0].intrinsics, sizeof(double) * 8) != 0)
+            return set_err(ctx, NAV_BA_ERR_UNSUPPORTED, "a batch shares one calibration");
+        if (i > 0 && probs[i].camera_model != probs[0].camera_model)
+            return set_err(ctx, NAV_BA_ERR_UNSUPPORTED, "a batch shares one camera model");
+    }
+    pb.host.assign(n, HostWindow());
+    pb.host_status.assign(n, NAV_BA_OK);
+    const int nth = std::max(1, std::min<int>(n / 8, (int)std::thread::hardware_concurrency()));
+    auto work = [&](int t) {
+        for (int i = t; i < n; i += nth) {
+            build_window(probs[i], *o, pb.host[i]);
+            const HostWindow& h = pb.host[i];
+            if (probs[i].n_cams == 0 || h.ne == 0) pb.host_status[i] = NAV_BA_EMPTY;
+        }
+    };
+    if (nth == 1) {
+        work(0);
+    } else {
+        std::vector<std::thread> ths;
+        for (int t = 0; t < nth; ++t) ths.emplace_back(work, t);
+        for (auto& th : ths) th.join();
+    }
+    for (int i = 0; i < n; ++i)
+        if (pb.host_status[i] == NAV_BA_OK && !fits_window_engine(pb.host[i]))
+            return set_err(ctx, NAV_BA_ERR_UNSUPPORTED,
+                           "problem " + std::to_string(i) + " has more than " + std::to_string(kWinMaxFreeCams) +
+                               " free cameras or " + std::to_string(kWinMaxCams) + " cameras");
+    pb.lm = lm_options(*o);
+    pb.intr = n > 0 ? intrinsics_of(probs[0]) : Intr{};
+    return NAV_BA_OK;
+}
+
+// Download results of every window into results[] (outputs of EMPTY windows: passthrough).
+nav_ba_status download_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, PreparedBatch& pb,
+                             nav_ba_result* results) {
+    WindowBatch& b = pb.dev;
+    std::vector<CamState> cams(b.ncam);
+    std::vector<double> pts(4 * b.npt);
+    std::vector<double> trace((size_t)b.trace_stride * n);
+    std::vector<WinStats> stats(n);
+    cudaError_t e = cudaSuccess;
+    auto dn = [&](void* dst, const void* src, size_t bytes) {
+        if (e != cudaSuccess || bytes == 0) return;
+        e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+    };
+    dn(cams.data(), b.d_cam_out, sizeof(CamState) * b.ncam);
+    dn(pts.data(), b.d_pt_out, sizeof(double) * 4 * b.npt);
+    dn(trace.data(), b.d_trace, sizeof(double) * trace.size());
+    dn(stats.data(), b.d_stats, sizeof(WinStats) * n);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_status(ctx, e, "download");
+    nav_ba_status overall = NAV_BA_OK;
+    for (int i = 0; i < n; ++i) {
+        nav_ba_result* r = &results[i];
+        const nav_ba_problem& p = probs[i];
+        const HostWindow& h = pb.host[i];
+        const WinDesc& d = pb.desc[i];
+        r->n_active_edges = h.ne;
+        r->n_free_cams = h.nfc;
+        r->n_free_points = h.nfp;
+        r->n_schur_blocks = h.n_schur_blocks;
+        if (pb.host_status[i] == NAV_BA_EMPTY) {
+            write_passthrough(p, r, false);
+            r->termination = NAV_BA_TERM_NOTHING_TO_DO;
+            r->status = NAV_BA_EMPTY;
+            continue;
+        }
+        const WinStats& s = stats[i];
+        r->status = s.status;
+        r->initial_cost = s.initial_cost;
+        r->final_cost = s.final_cost;
+        r->final_lambda = s.final_lambda;
+        r->iterations_done = s.iterations_done;
+        r->trials_accepted = s.accepted;
+        r->trials_rejected = s.rejected;
+        r->termination = s.termination;
+        if (s.status != NAV_BA_OK) {
+            overall = (nav_ba_status)s.status;
+            continue;
+        }
+        if (r->cam_pose_out)
+            for (int c = 0; c < p.n_cams; ++c) pose12_from_cam(cams[d.cam0 + c], r->cam_pose_out + 12LL * c);
+        if (r->points_out)
+            for (int k = 0; k < p.n_points; ++k)
+                for (int j = 0; j < 3; ++j) r->points_out[3LL * k + j] = pts[4LL * (d.pt0 + k) + j];
+        if (r->intrinsics_out) std::memcpy(r->intrinsics_out, p.intrinsics, sizeof(double) * 8);
+        if (r->cost_trace)
+            for (int k = 0; k <= s.iterations_done; ++k) r->cost_trace[k] = trace[(size_t)i * b.trace_stride + k];
+    }
+    return overall;
+}
+
+nav_ba_status solve_impl(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, const nav_ba_options* o,
+                         nav_ba_result* results) {
+    if (!ctx) return NAV_BA_ERR_ARGUMENT;
+    if (!probs || !results || n < 0) return set_err(ctx, NAV_BA_ERR_ARGUMENT, "NULL argument");
+    const auto t0 = std::chrono::steady_clock::now();
+    PreparedBatch pb;
+    nav_ba_status st = build_batch(ctx, probs, n, o, pb);
+    if (st != NAV_BA_OK) return st;
+    std::string why;
+    cudaError_t e = window_batch_upload(pb, ctx->stream, o->precision, o->iterations + 1, &why);
+    if (e != cudaSuccess) {
+        window_batch_free(pb.dev);
+        return cuda_status(ctx, e, "upload");
+    }
+    const double t_setup = ms_since(t0);
+    const int threads = o->precision == NAV_BA_MIXED ? ctx->threads_mixed : ctx->threads_fp64;
+    cudaEventRecord(ctx->ev0, ctx->stream);
+    e = window_batch_launch(pb, ctx->stream, o->precision, threads, -1.0);
+    cudaEventRecord(ctx->ev1, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        window_batch_free(pb.dev);
+        return cuda_status(ctx, e, "window kernel");
+    }
+    float t_solve = 0.f;
+    cudaEventElapsedTime(&t_solve, ctx->ev0, ctx->ev1);
+    const auto t1 = std::chrono::steady_clock::now();
+    std::vector<nav_ba_result> tmp(results, results + n);  // outputs untouched on error
+    for (auto& r : tmp) clear_stats(&r);
+    st = download_batch(ctx, probs, n, pb, tmp.data());
+    window_batch_free(pb.dev);
+    if (st != NAV_BA_OK && st != NAV_BA_EMPTY) return set_err(ctx, st, "a problem has a non-finite initial cost");
+    const double t_down = ms_since(t1);
+    for (int i = 0; i < n; ++i) {
+        tmp[i].time_setup_ms = t_setup;
+        tmp[i].time_solve_ms = t_solve;
+        tmp[i].time_download_ms = t_down;
+        results[i] = tmp[i];
+    }
+    return NAV_BA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void nav_ba_options_default(nav_ba_options* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->iterations = 5;
+    o->precision = NAV_BA_FP64;
+    o->solver = NAV_BA_SOLVER_CHOLESKY;
+    o->robust = 0;
+    o->huber_delta = (double)(float)std::sqrt(5.99);
+    o->initial_lambda = 0.0;
+    o->tau = 1e-5;
+    o->max_trials = 10;
+    o->optimize_distortion = 0;
+    o->pcg_tolerance = 1e-6;
+    o->pcg_max_iterations = 100;
+    o->deterministic = 1;
+}
+
+nav_ba_status nav_ba_create(nav_ba_ctx** out, int32_t device) {
+    if (!out) return NAV_BA_ERR_ARGUMENT;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return NAV_BA_ERR_NO_DEVICE;
+    if (device < 0 || device >= n) return NAV_BA_ERR_NO_DEVICE;
+    if (cudaSetDevice(device) != cudaSuccess) return NAV_BA_ERR_NO_DEVICE;
+    nav_ba_ctx* ctx = new nav_ba_ctx();
+    ctx->device = device;
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess) {
+        delete ctx;
+        return NAV_BA_ERR_CUDA;
+    }
+    *out = ctx;
+    return NAV_BA_OK;
+}
+
+void nav_ba_destroy(nav_ba_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    window_batch_free(ctx->prepared.dev);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+nav_ba_status nav_ba_solve(nav_ba_ctx* ctx, const nav_ba_problem* p, const nav_ba_options* o, nav_ba_result* r) {
+    if (!ctx) return NAV_BA_ERR_ARGUMENT;
+    if (!p || !o || !r) return set_err(ctx, NAV_BA_ERR_ARGUMENT, "NULL argument");
+    cudaSetDevice(ctx->device);
+    ctx->last_error.clear();
+    std::string why;
+    nav_ba_status st = validate_problem(p, &why);
+    if (st != NAV_BA_OK) return set_err(ctx, st, why);
+    nav_ba_result tmp = *r;
+    st = solve_impl(ctx, p, 1, o, &tmp);
+    if (st != NAV_BA_OK) return st;
+    *r = tmp;
+    return (nav_ba_status)(tmp.status == NAV_BA_EMPTY ? NAV_BA_EMPTY : NAV_BA_OK);
+}
+
+nav_ba_status nav_ba_solve_batched(nav_ba_ctx* ctx, const nav_ba_problem* windows, int32_t n,
+                                   const nav_ba_options* o, nav_ba_result* results) {
+    if (!ctx) return NAV_BA_ERR_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    ctx->last_error.clear();
+    return solve_impl(ctx, windows, n, o, results);
+}
+
+nav_ba_status nav_ba_prepare(nav_ba_ctx* ctx, const nav_ba_problem* p, const nav_ba_options* o) {
+    if (!ctx) return NAV_BA_ERR_ARGUMENT;
+    if (!p || !o) return set_err(ctx, NAV_BA_ERR_ARGUMENT, "NULL argument");
+    cudaSetDevice(ctx->device);
+    window_batch_free(ctx->prepared.dev);
+    ctx->has_prepared = false;
+    PreparedBatch& pb = ctx->prepared;
+    pb = PreparedBatch();
+    nav_ba_status st = build_batch(ctx, p, 1, o, pb);
+    if (st != NAV_BA_OK) return st;
+    std::string why;
+    cudaError_t e = window_batch_upload(pb, ctx->stream, o->precision, o->iterations + 1, &why);
+    if (e != cudaSuccess) {
+        window_batch_free(pb.dev);
+        return cuda_status(ctx, e, "upload");
+    }
+    ctx->prepared_problems.assign(1, *p);
+    ctx->prepared_opts = *o;
+    ctx->has_prepared = true;
+    return NAV_BA_OK;
+}
+
+nav_ba_status nav_ba_run(nav_ba_ctx* ctx, const nav_ba_options* o, nav_ba_result* stats) {
+    if (!ctx) return NAV_BA_ERR_ARGUMENT;
+    if (!ctx->has_prepared) return set_err(ctx, NAV_BA_ERR_ARGUMENT, "nothing prepared");
+    const nav_ba_options& po = ctx->prepared_opts;
+    if (o && (o->precision != po.precision || o->iterations != po.iterations))
+        return set_err(ctx, NAV_BA_ERR_ARGUMENT, "run options must match the prepared precision and iterations");
+    cudaSetDevice(ctx->device);
+    const int threads = po.precision == NAV_BA_MIXED ? ctx->threads_mixed : ctx->threads_fp64;
+    if (o) ctx->prepared.lm = lm_options(*o);
+    cudaEventRecord(ctx->ev0, ctx->stream);
+    cudaError_t e = window_batch_launch(ctx->prepared, ctx->stream, po.precision, threads, -1.0);
+    cudaEventRecord(ctx->ev1, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_status(ctx, e, "window kernel");
+    if (stats) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1);
+        WinStats s{};
+        if (ctx->prepared.dev.n_queue > 0) {
+            e = cudaMemcpy(&s, ctx->prepared.dev.d_stats, sizeof(WinStats), cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) return cuda_status(ctx, e, "stats");
+        }
+        stats->time_solve_ms = t;
+        stats->initial_cost = s.initial_cost;
+        stats->final_cost = s.final_cost;
+        stats->final_lambda = s.final_lambda;
+        stats->iterations_done = s.iterations_done;
+        stats->trials_accepted = s.accepted;
+        stats->trials_rejected = s.rejected;
+        stats->termination = s.termination;
+        stats->status = s.status;
+    }
+    return NAV_BA_OK;
+}
+
+nav_ba_status nav_ba_fetch(nav_ba_ctx* ctx, nav_ba_result* r) {
+    if (!ctx) return NAV_BA_ERR_ARGUMENT;
+    if (!ctx->has_prepared || !r) return set_err(ctx, NAV_BA_ERR_ARGUMENT, "nothing prepared");
+    cudaSetDevice(ctx->device);
+    nav_ba_result tmp = *r;
+    clear_stats(&tmp);
+    nav_ba_status st = download_batch(ctx, ctx->prepared_problems.data(), 1, ctx->prepared, &tmp);
+    if (st != NAV_BA_OK && st != NAV_BA_EMPTY) return st;
+    *r = tmp;
+    return NAV_BA_OK;
+}
+
+nav_ba_status nav_ba_linearize(nav_ba_ctx* ctx, const nav_ba_problem* p, const nav_ba_options* o, double* e,
+                               double* jc, double* jp, double* w) {
+    if (!ctx) return NAV_BA_ERR_ARGUMENT;
+    if (!p || !o) return set_err(ctx, NAV_BA_ERR_ARGUMENT, "NULL argument");
+    cudaSetDevice(ctx->device);
+    std::string why;
+    nav_ba_status st = validate_problem(p, &why);
+    if (st != NAV_BA_OK) return set_err(ctx, st, why);
+    st = validate_options(o, &why);
+    if (st != NAV_BA_OK) return set_err(ctx, st, why);
+    cudaError_t err = linearize_observations(*p, *o, ctx->stream, e, jc, jp, w, &why);
+    return cuda_status(ctx, err, "linearize");
+}
+
+nav_ba_status nav_ba_reduced_system(nav_ba_ctx* ctx, const nav_ba_problem* p, const nav_ba_options* o, double lambda,
+                                    int32_t capacity_free, int32_t* n_free, double* s, double* b, int32_t* cam_index) {
+    if (!ctx) return NAV_BA_ERR_ARGUMENT;
+    if (!p || !o || !n_free) return set_err(ctx, NAV_BA_ERR_ARGUMENT, "NULL argument");
+    if (!(lambda >= 0)) return set_err(ctx, NAV_BA_ERR_ARGUMENT, "lambda must be >= 0");
+    cudaSetDevice(ctx->device);
+    PreparedBatch pb;
+    nav_ba_options o1 = *o;
+    o1.iterations = 1;
+    nav_ba_status st = build_batch(ctx, p, 1, &o1, pb);
+    if (st != NAV_BA_OK) return st;
+    const HostWindow& h = pb.host[0];
+    *n_free = h.nfc;
+    if (cam_index) std::memcpy(cam_index, h.cam_free.data(), sizeof(int32_t) * p->n_cams);
+    if (capacity_free < h.nfc || !s || !b) return NAV_BA_OK;
+    if (pb.host_status[0] != NAV_BA_OK || h.nfc == 0) {
+        return NAV_BA_OK;
+    }
+    std::string why;
+    cudaError_t e = window_batch_upload(pb, ctx->stream, o1.precision, 2, &why);
+    if (e == cudaSuccess) e = window_batch_launch(pb, ctx->stream, o1.precision,
+                                                  o1.precision == NAV_BA_MIXED ? ctx->threads_mixed : ctx->threads_fp64,
+                                                  lambda);
+    const int m = 6 * h.nfc;
+    std::vector<double> out((size_t)m * m + m);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out.data(), pb.dev.d_debug, sizeof(double) * out.size(), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    window_batch_free(pb.dev);
+    if (e != cudaSuccess) return cuda_status(ctx, e, "reduced system");
+    std::memcpy(s, out.data(), sizeof(double) * m * m);
+    std::memcpy(b, out.data() + (size_t)m * m, sizeof(double) * m);
+    return NAV_BA_OK;
+}
+
+nav_ba_status nav_ba_cost(nav_ba_ctx* ctx, const nav_ba_problem* p, const nav_ba_options* o, double* cost) {
+    if (!ctx) return NAV_BA_ERR_ARGUMENT;
+    if (!p || !o || !cost) return set_err(ctx, NAV_BA_ERR_ARGUMENT, "NULL argument");
+    nav_ba_options o0 = *o;
+    o0.iterations = 0;
+    nav_ba_result r{};
+    nav_ba_status st = nav_ba_solve(ctx, p, &o0, &r);
+    if (st == NAV_BA_EMPTY) {
+        *cost = 0.0;
+        return NAV_BA_OK;
+    }
+    if (st != NAV_BA_OK) return st;
+    *cost = r.initial_cost;
+    return NAV_BA_OK;
+}
+
+const char* nav_ba_last_error(const nav_ba_ctx* ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+const char* nav_ba_status_string(nav_ba_status s) {
+    switch (s) {
+        case NAV_BA_OK: return "ok";
+        case NAV_BA_EMPTY: return "empty problem: nothing to optimize";
+        case NAV_BA_ERR_ARGUMENT: return "invalid argument";
+        case NAV_BA_ERR_NONFINITE_INPUT: return "non-finite input";
+        case NAV_BA_ERR_NONFINITE_COST: return "non-finite initial cost";
+        case NAV_BA_ERR_CUDA: return "CUDA error";
+        case NAV_BA_ERR_OUT_OF_MEMORY: return "out of memory";
+        case NAV_BA_ERR_UNSUPPORTED: return "unsupported size or option";
+        case NAV_BA_ERR_DEVICE_TIMEOUT: return "device wait timed out";
+        case NAV_BA_ERR_NO_DEVICE: return "no CUDA device";
+    }
+    return "unknown status";
+}
+
+int32_t nav_ba_abi_version(void) { return NAV_BA_ABI_VERSION; }
+
+}  // extern "C"

@@ -1,0 +1,131 @@
+// structure.cpp - host-side graph build (see structure.hpp).
+#include "structure.hpp"
+
+#include <algorithm>
+#include <cmath>
+
+namespace navba {
+
+static bool all_finite(const double* a, long long n) {
+    for (long long i = 0; i < n; ++i)
+        if (!std::isfinite(a[i])) return false;
+    return true;
+}
+
+nav_ba_status validate_problem(const nav_ba_problem* p, std::string* why) {
+    auto fail = [&](nav_ba_status s, const char* msg) {
+        if (why) *why = msg;
+        return s;
+    };
+    if (!p) return fail(NAV_BA_ERR_ARGUMENT, "problem is NULL");
+    if (p->n_cams < 0 || p->n_points < 0 || p->n_obs < 0) return fail(NAV_BA_ERR_ARGUMENT, "negative size");
+    if ((p->n_cams && !p->cam_pose) || (p->n_points && !p->points) ||
+        (p->n_obs && (!p->obs_uv || !p->obs_cam || !p->obs_point)))
+        return fail(NAV_BA_ERR_ARGUMENT, "NULL array with nonzero size");
+    if (p->camera_model != NAV_BA_CAM_PINHOLE && p->camera_model != NAV_BA_CAM_PINHOLE_RADIAL)
+        return fail(NAV_BA_ERR_ARGUMENT, "unknown camera model");
+    for (int o = 0; o < p->n_obs; ++o)
+        if (p->obs_cam[o] < 0 || p->obs_cam[o] >= p->n_cams || p->obs_point[o] < 0 ||
+            p->obs_point[o] >= p->n_points)
+            return fail(NAV_BA_ERR_ARGUMENT, "observation index out of range");
+    if (!all_finite(p->cam_pose, 12LL * p->n_cams) || !all_finite(p->points, 3LL * p->n_points) ||
+        !all_finite(p->obs_uv, 2LL * p->n_obs) || !all_finite(p->intrinsics, 8))
+        return fail(NAV_BA_ERR_NONFINITE_INPUT, "non-finite input value");
+    return NAV_BA_OK;
+}
+
+nav_ba_status validate_options(const nav_ba_options* o, std::string* why) {
+    auto fail = [&](const char* msg) {
+        if (why) *why = msg;
+        return NAV_BA_ERR_ARGUMENT;
+    };
+    if (!o) return fail("options is NULL");
+    if (o->iterations < 0) return fail("iterations < 0");
+    if (o->max_trials < 1) return fail("max_trials < 1");
+    if (o->robust && !(o->huber_delta > 0)) return fail("huber_delta must be > 0");
+    if (o->precision != NAV_BA_FP64 && o->precision != NAV_BA_MIXED) return fail("unknown precision");
+    if (o->solver != NAV_BA_SOLVER_CHOLESKY && o->solver != NAV_BA_SOLVER_PCG) return fail("unknown solver");
+    if (!(o->tau >= 0) || !std::isfinite(o->initial_lambda)) return fail("invalid damping parameters");
+    return NAV_BA_OK;
+}
+
+void build_window(const nav_ba_problem& p, const nav_ba_options& o, HostWindow& w) {
+    const bool free_intr = o.optimize_distortion && p.camera_model == NAV_BA_CAM_PINHOLE_RADIAL;
+    w.ncam = p.n_cams;
+    w.npt = p.n_points;
+    auto cam_fixed = [&](int c) { return p.cam_fixed && p.cam_fixed[c]; };
+    auto pt_fixed = [&](int i) { return p.point_fixed && p.point_fixed[i]; };
+    // active edges, counted per point (counting sort keeps input order within a point)
+    std::vector<int32_t> cnt(w.npt + 1, 0);
+    std::vector<uint8_t> act(p.n_obs, 0);
+    for (int k = 0; k < p.n_obs; ++k) {
+        const int c = p.obs_cam[k], i = p.obs_point[k];
+        act[k] = free_intr || !(cam_fixed(c) && pt_fixed(i));
+        if (act[k]) cnt[i + 1]++;
+    }
+    w.pt_eoff.assign(w.npt + 1, 0);
+    for (int i = 0; i < w.npt; ++i) w.pt_eoff[i + 1] = w.pt_eoff[i] + cnt[i + 1];
+    w.ne = w.pt_eoff[w.npt];
+    w.edge_cam.resize(w.ne);
+    w.edge_obs.resize(w.ne);
+    w.edge_uv.resize(2LL * w.ne);
+    w.edge_pt.resize(w.ne);
+    std::vector<int32_t> fill(w.pt_eoff.begin(), w.pt_eoff.end() - 1);
+    std::vector<uint8_t> cam_has(w.ncam, 0);
+    for (int k = 0; k < p.n_obs; ++k) {
+        if (!act[k]) continue;
+        const int i = p.obs_point[k];
+        const int e = fill[i]++;
+        w.edge_cam[e] = p.obs_cam[k];
+        w.edge_obs[e] = k;
+        w.edge_pt[e] = i;
+        w.edge_uv[2LL * e] = p.obs_uv[2LL * k];
+        w.edge_uv[2LL * e + 1] = p.obs_uv[2LL * k + 1];
+        cam_has[p.obs_cam[k]] = 1;
+    }
+    w.cam_free.assign(w.ncam, -1);
+    w.nfc = 0;
+    for (int c = 0; c < w.ncam; ++c)
+        if (!cam_fixed(c) && cam_has[c]) w.cam_free[c] = w.nfc++;
+    w.pt_free.assign(w.npt, -1);
+    w.nfp = 0;
+    for (int i = 0; i < w.npt; ++i)
+        if (!pt_fixed(i) && w.pt_eoff[i + 1] > w.pt_eoff[i]) w.pt_free[i] = w.nfp++;
+    w.cam.resize(w.ncam);
+    for (int c = 0; c < w.ncam; ++c) cam_from_pose12(p.cam_pose + 12LL * c, w.cam[c]);
+    w.pt.assign(4LL * w.npt, 0.0);
+    for (int i = 0; i < w.npt; ++i)
+        for (int k = 0; k < 3; ++k) w.pt[4LL * i + k] = p.points[3LL * i + k];
+    w.n_schur_blocks = count_schur_blocks(w);
+}
+
+int32_t count_schur_blocks(const HostWindow& w) {
+    if (w.nfc == 0) return 0;
+    // bitset of co-visible free-camera pairs (b <= a)
+    std::vector<uint8_t> seen((size_t)w.nfc * w.nfc, 0);
+    std::vector<int32_t> fc;
+    int32_t n = 0;
+    for (int a = 0; a < w.nfc; ++a) {
+        seen[(size_t)a * w.nfc + a] = 1;
+        ++n;
+    }
+    for (int i = 0; i < w.npt; ++i) {
+        if (w.pt_free[i] < 0) continue;
+        fc.clear();
+        for (int e = w.pt_eoff[i]; e < w.pt_eoff[i + 1]; ++e) {
+            const int a = w.cam_free[w.edge_cam[e]];
+            if (a >= 0) fc.push_back(a);
+        }
+        for (size_t x = 0; x < fc.size(); ++x)
+            for (size_t y = 0; y < fc.size(); ++y) {
+                const int a = fc[x], b = fc[y];
+                if (b < a && !seen[(size_t)a * w.nfc + b]) {
+                    seen[(size_t)a * w.nfc + b] = 1;
+                    ++n;
+                }
+            }
+    }
+    return n;
+}
+
+}  // namespace navba

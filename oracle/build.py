@@ -1,0 +1,31 @@
+"""Build recipe of the CPU oracle (test infrastructure): oracle/_build/libnavba_oracle.so.
+
+The oracle is plain C++17 with no dependencies; it is compiled with g++ directly.  The
+reference's own BA path cannot be compiled here (it needs g2o, Eigen, OpenCV, Boost and glog,
+none of which exist in this environment), so there is no oracle/_ref build.
+"""
+from __future__ import annotations
+
+import subprocess
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+
+
+def build() -> Path:
+    BUILD.mkdir(exist_ok=True)
+    lib = BUILD / "libnavba_oracle.so"
+    srcs = [HERE / "ba_oracle.cpp"]
+    deps = srcs + [HERE / "ba_oracle.h", HERE.parent / "include" / "nav_ba.h"]
+    if not lib.exists() or any(d.stat().st_mtime > lib.stat().st_mtime for d in deps):
+        cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-Wall", "-Wextra", "-pthread",
+               "-o", str(lib), *map(str, srcs)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
+    return lib
+
+
+if __name__ == "__main__":
+    print(build())
