@@ -1,0 +1,339 @@
+"""Benchmark of the GB300 bundle-adjustment back end.
+
+Workload (default, `--workload windows`): batched local BA, 512 independent windows
+(5-20 keyframes, 200-3000 points, 3-8 views per point, 0.8 px noise, first two keyframes fixed,
+10 LM iterations each), seeded synthetic data (family 2, seed 1002).  One step = one solve of
+the whole batch from its initial state (one persistent kernel launch).
+
+Metric: BA observations/s = sum over windows of active edges x LM iterations completed, per
+second of solve; reported for the mixed form (`value`) beside the plain FP64 form, with the
+LM iterations/s of both and the final-cost agreement of the two forms.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl reference` times nav24's BA algorithm on the host cores instead: the reference's own g2o
+path cannot be built here (g2o, Eigen, OpenCV are absent), so the CPU restatement of it
+(oracle/, FP64, one window per thread, all host threads) runs the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+METRIC = "BA obs/s (resid+Jac+Schur) & LM iter/s: mixed vs FP64 GPU at same final cost"
+UNIT = "obs/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["windows"], default="windows")
+    ap.add_argument("--windows", type=int, default=512)
+    ap.add_argument("--cpu-sample", type=int, default=512, help="windows in the CPU baseline sample")
+    ap.add_argument("--profile-case", choices=["mixed", "fp64"], default=None,
+                    help="run only the device-resident solves of one precision (for profiler captures)")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max-reduction over ranks (one process per GPU); no-ops for one rank."""
+
+    def __init__(self, world: int, local: int):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch
+            import torch.distributed as td
+            torch.cuda.set_device(local)
+            td.init_process_group("nccl")
+            self.td, self.torch = td, torch
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        t = self.torch.tensor([x], dtype=self.torch.float64, device="cuda")
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        t = self.torch.tensor([x], dtype=self.torch.float64, device="cuda")
+        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows if len(r) > 8 for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def algorithmic_bytes(wins, results, s_o: int, s_d: int = 8) -> float:
+    """Algorithmic DRAM bytes of one batched solve (per-window sums of the per-iteration model:
+    linearize+reduce, Schur assembly, back-substitution+update, trial cost per damping trial)."""
+    total = 0.0
+    for w, r in zip(wins, results):
+        st = r.stats
+        No, Np, Nc = st["n_active_edges"], st["n_free_points"], st["n_free_cams"]
+        it = st["iterations_done"]
+        trials = st["trials_accepted"] + st["trials_rejected"]
+        nnz = st["n_schur_blocks"]
+        lin = No * (2 * s_o + 8) + Np * 3 * s_o + Nc * 7 * s_d + Np * 9 * s_o + Nc * 27 * s_o
+        schur = No * (2 * s_o + 8) + Np * 9 * s_o + nnz * 36 * s_d + Nc * 6 * s_d
+        upd = No * (2 * s_o + 8) + Np * (3 * s_o * 2 + 9 * s_o) + Nc * (6 + 7 * 2) * s_d
+        cost = No * (2 * s_o + 8) + Np * 3 * s_o + Nc * 7 * s_d
+        total += it * lin + trials * (schur + upd + cost) + cost
+    return total
+
+
+def profile_traffic():
+    """DRAM traffic per launch from the committed ncu summary, if one exists."""
+    p = ROOT / "profiles" / "window_lm_kernel_traffic.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return None
+
+
+def cpu_reference(wins, opt, n_threads):
+    from oracle import oracle
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(n_threads) as ex:
+        res = list(ex.map(lambda w: oracle.solve(w, opt, n_threads=1), wins))
+    dt = time.perf_counter() - t0
+    edge_it = sum(r.stats["n_active_edges"] * r.stats["iterations_done"] for r in res)
+    iters = sum(r.stats["iterations_done"] for r in res)
+    return dt, edge_it, iters, res
+
+
+def run_reference(args, rank, world):
+    from nav24_gb300.synth import Synth, workload_options
+    from nav24_gb300 import abi
+    if rank != 0:
+        return
+    s = Synth(2, n_windows=args.windows)
+    wins = s.windows()[: args.cpu_sample]
+    opt = workload_options(2, abi.FP64)
+    nth = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_reference(wins[: max(1, len(wins) // 8)], opt, nth)
+    times, eis, its = [], 0, 0
+    for _ in range(args.steps):
+        dt, ei, it, _ = cpu_reference(wins, opt, nth)
+        times.append(dt)
+        eis, its = ei, it
+    t = float(np.mean(times))
+    val = eis / t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"batched local BA, {len(wins)} windows of family 2 (seed 1002), FP64 CPU "
+                               f"restatement of nav24 GraphOptim + g2o LM", "windows": len(wins),
+                   "lm_iterations": 10},
+        "lm_iter_per_s": its / t,
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": nth, "kind": "port",
+                         "sample": f"{len(wins)} windows x 10 LM iterations, one window per thread"},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def time_device(ctx, wins, opt, steps, warmup, dist):
+    """Device-resident solves: prepare once, then `steps` launches timed with CUDA events."""
+    ctx.prepare_batched(wins, opt)
+    for _ in range(warmup):
+        ctx.run(opt)
+    dist.barrier()
+    ms, stats = [], None
+    for _ in range(steps):
+        stats = ctx.run(opt)
+        ms.append(stats["time_solve_ms"])
+    dist.barrier()
+    results = ctx.fetch_batched(opt)
+    return ms, stats, results
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    dist = Dist(world, local)
+    from nav24_gb300 import Context, abi
+    from nav24_gb300.build import build_all
+    from nav24_gb300.synth import Synth, workload_options
+    build_all()
+    s = Synth(2, seed=1002 + 7919 * rank, n_windows=args.windows)
+    wins = s.windows()
+    n_obs = s.n_obs
+    ctx = Context(local if world > 1 else 0)
+    om = workload_options(2, abi.MIXED)
+    of = workload_options(2, abi.FP64)
+
+    if args.profile_case:
+        o = om if args.profile_case == "mixed" else of
+        ms, st, _ = time_device(ctx, wins, o, args.steps, args.warmup, dist)
+        print(json.dumps({"profile_case": args.profile_case, "windows": len(wins), "observations": n_obs,
+                          "ms": ms, "edge_iterations": st["edge_iterations"]}), flush=True)
+        ctx.close()
+        dist.close()
+        return
+    with ClockSampler(local) as clk:
+        ms_m, st_m, res_m = time_device(ctx, wins, om, args.steps, args.warmup, dist)
+    clocks = clk.summary()
+    ms_f, st_f, res_f = time_device(ctx, wins, of, args.steps, args.warmup, dist)
+
+    t_m = dist.max(float(np.mean(ms_m)) * 1e-3)
+    t_f = dist.max(float(np.mean(ms_f)) * 1e-3)
+    ei_m = dist.sum(float(st_m["edge_iterations"]))
+    ei_f = dist.sum(float(st_f["edge_iterations"]))
+    it_m = dist.sum(float(st_m["iterations_done"]))
+    it_f = dist.sum(float(st_f["iterations_done"]))
+    value = ei_m / t_m
+    fp64_value = ei_f / t_f
+    cost_rel = max(abs(a.stats["final_cost"] - b.stats["final_cost"]) / b.stats["final_cost"]
+                   for a, b in zip(res_m, res_f) if b.stats["final_cost"] > 0)
+
+    # end to end through the C ABI with host buffers (graph build, H2D, solve, D2H each step)
+    ctx.solve_batched(wins[:8], om)
+    dist.barrier()
+    e2e_t, e2e_ei, h2d, d2h = [], 0, 0, 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        rr = ctx.solve_batched(wins, om)
+        e2e_t.append(time.perf_counter() - t0)
+        e2e_ei = sum(r.stats["edge_iterations"] for r in rr)
+        h2d, d2h = rr[0].stats["h2d_bytes"], rr[0].stats["d2h_bytes"]
+    dist.barrier()
+    e2e_time = dist.max(float(np.mean(e2e_t)))
+    e2e_value = dist.sum(float(e2e_ei)) / e2e_time
+
+    # roofline of the one kernel (window_lm_kernel): algorithmic bytes / launch time
+    peak, peak_kind = measured_peaks()
+    alg = algorithmic_bytes(wins, res_m, s_o=4)
+    achieved = alg / (float(np.mean(ms_m)) * 1e-3) / 1e9
+    prof = profile_traffic()
+    roofline = {"bound": "hbm", "kernel": "window_lm_kernel<float>", "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "peak_kind": f"{peak_kind} hbm_gbs",
+                "algorithmic_bytes_per_launch": alg,
+                "traffic": prof["dram_bytes_per_launch_full"] if prof else None}
+
+    # CPU baseline: the FP64 restatement on this host, all threads, bounded sample
+    cpu = None
+    if rank == 0:
+        nth = os.cpu_count() or 1
+        sample = wins[: args.cpu_sample]
+        dt, ei, its, _ = cpu_reference(sample, of, nth)
+        cpu = {"value": ei / dt, "unit": UNIT, "cores": nth, "kind": "port",
+               "sample": f"{len(sample)} windows x 10 LM iterations (FP64 oracle), one window per thread"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_m * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 bulk / f64 Cholesky+cost+SE3", "data": "synthetic",
+            "config": {"workload": "batched local BA: 512 windows (5-20 keyframes, 200-3000 points, "
+                                   "3-8 views/point, first two keyframes fixed), 10 LM iterations, "
+                                   "family 2 seed 1002 (+7919*rank)",
+                       "windows_per_gpu": len(wins), "observations_per_gpu": n_obs,
+                       "l2": "inputs+scratch > L2 (no flush needed)", "precision": "mixed",
+                       "parallelism": f"replicas x{world}"},
+            "lm_iter_per_s": it_m / t_m,
+            "fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": t_f * 1e3, "lm_iter_per_s": it_f / t_f},
+            "mixed_over_fp64": value / fp64_value,
+            "final_cost_rel_diff_max": cost_rel,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_time * 1e3},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "gpu_launches": args.steps,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -137,7 +137,9 @@ typedef struct nav_ba_result {
     int32_t n_schur_blocks;       /* stored lower-triangle 6x6 blocks of the reduced system */
     int32_t pcg_iterations_total;
     int32_t status;               /* nav_ba_status of this problem (batched calls)          */
-    int32_t reserved[6];
+    int64_t edge_iterations;      /* active edges x LM iterations done (nav_ba_run: summed) */
+    int64_t h2d_bytes;            /* bytes this call copied host -> device                  */
+    int64_t d2h_bytes;            /* bytes this call copied device -> host                  */
 } nav_ba_result;
 
 typedef struct nav_ba_ctx nav_ba_ctx;
@@ -175,6 +177,13 @@ nav_ba_status nav_ba_prepare(nav_ba_ctx* ctx, const nav_ba_problem* problem,
                              const nav_ba_options* options);
 nav_ba_status nav_ba_run(nav_ba_ctx* ctx, const nav_ba_options* options, nav_ba_result* stats);
 nav_ba_status nav_ba_fetch(nav_ba_ctx* ctx, nav_ba_result* result);
+
+/* Batched form of nav_ba_prepare: windows as in nav_ba_solve_batched.  nav_ba_run then solves
+ * all of them in one launch (stats of the whole batch: summed iterations/trials, summed costs,
+ * the launch time); nav_ba_fetch_batched copies every window's results. */
+nav_ba_status nav_ba_prepare_batched(nav_ba_ctx* ctx, const nav_ba_problem* windows,
+                                     int32_t n_windows, const nav_ba_options* options);
+nav_ba_status nav_ba_fetch_batched(nav_ba_ctx* ctx, nav_ba_result* results);
 
 /* Residuals and Jacobians of every observation at the problem's initial state, computed by
  * the device linearization kernel in the given precision (EdgeSE3ProjectXYZ::computeError and

@@ -18,7 +18,8 @@ LIB_PATH = Path(__file__).resolve().parent / "_build" / "libnavba.so"
 # Every entry point declared in include/nav_ba.h.
 EXPORTS = [
     "nav_ba_options_default", "nav_ba_create", "nav_ba_destroy", "nav_ba_solve",
-    "nav_ba_solve_batched", "nav_ba_prepare", "nav_ba_run", "nav_ba_fetch", "nav_ba_linearize",
+    "nav_ba_solve_batched", "nav_ba_prepare", "nav_ba_run", "nav_ba_fetch", "nav_ba_prepare_batched",
+    "nav_ba_fetch_batched", "nav_ba_linearize",
     "nav_ba_reduced_system", "nav_ba_cost", "nav_ba_last_error", "nav_ba_status_string",
     "nav_ba_abi_version",
 ]
@@ -58,6 +59,10 @@ def load(path: os.PathLike | None = None) -> C.CDLL:
     L.nav_ba_run.restype = C.c_int
     L.nav_ba_fetch.argtypes = [ctxp, R]
     L.nav_ba_fetch.restype = C.c_int
+    L.nav_ba_prepare_batched.argtypes = [ctxp, P, C.c_int32, O]
+    L.nav_ba_prepare_batched.restype = C.c_int
+    L.nav_ba_fetch_batched.argtypes = [ctxp, R]
+    L.nav_ba_fetch_batched.restype = C.c_int
     L.nav_ba_linearize.argtypes = [ctxp, P, O, dp, dp, dp, dp]
     L.nav_ba_linearize.restype = C.c_int
     L.nav_ba_reduced_system.argtypes = [ctxp, P, O, C.c_double, C.c_int32, ip, dp, dp, ip]
@@ -147,11 +152,29 @@ class Context:
         p = prob.as_c()
         self._check(self.L.nav_ba_prepare(self.h, C.byref(p), C.byref(opt)))
 
+    def prepare_batched(self, probs: list[abi.Problem], opt: abi.nav_ba_options):
+        self._prepared_batch = probs
+        n = len(probs)
+        self._cp = (abi.nav_ba_problem * n)(*[p.as_c() for p in probs])
+        self._check(self.L.nav_ba_prepare_batched(self.h, self._cp, n, C.byref(opt)))
+
+    def fetch_batched(self, opt: abi.nav_ba_options) -> list[abi.Result]:
+        probs = self._prepared_batch
+        n = len(probs)
+        bufs = [abi.ResultBuffers(p, opt.iterations) for p in probs]
+        cr = (abi.nav_ba_result * n)(*[b.c for b in bufs])
+        self._check(self.L.nav_ba_fetch_batched(self.h, cr))
+        out = []
+        for b, r in zip(bufs, cr):
+            b.c = r
+            out.append(b.result(r.status))
+        return out
+
     def run(self, opt: abi.nav_ba_options) -> dict:
         r = abi.nav_ba_result()
         self._check(self.L.nav_ba_run(self.h, C.byref(opt), C.byref(r)))
         return {name: getattr(r, name) for name, _ in abi.nav_ba_result._fields_
-                if name not in ("cam_pose_out", "points_out", "intrinsics_out", "cost_trace", "reserved")}
+                if name not in ("cam_pose_out", "points_out", "intrinsics_out", "cost_trace")}
 
     def fetch(self, opt: abi.nav_ba_options) -> abi.Result:
         buf = abi.ResultBuffers(self._prepared, opt.iterations)

@@ -100,7 +100,9 @@ class nav_ba_result(C.Structure):
         ("n_schur_blocks", C.c_int32),
         ("pcg_iterations_total", C.c_int32),
         ("status", C.c_int32),
-        ("reserved", C.c_int32 * 6),
+        ("edge_iterations", C.c_int64),
+        ("h2d_bytes", C.c_int64),
+        ("d2h_bytes", C.c_int64),
     ]
 
 
@@ -243,6 +245,6 @@ class ResultBuffers:
     def result(self, status: int) -> Result:
         r = self.c
         stats = {name: getattr(r, name) for name, _ in nav_ba_result._fields_
-                 if name not in ("cam_pose_out", "points_out", "intrinsics_out", "cost_trace", "reserved")}
+                 if name not in ("cam_pose_out", "points_out", "intrinsics_out", "cost_trace")}
         n = max(0, r.iterations_done) + 1
         return Result(status, self.cam_pose, self.points, self.intrinsics, self.cost_trace[:n].copy(), stats)

@@ -77,6 +77,7 @@ struct WindowBatch {
     WinStats* d_stats = nullptr;
     double* d_debug = nullptr;     // reduced-system debug output (optional)
     size_t bytes = 0;
+    int64_t h2d_bytes = 0;    // bytes uploaded by window_batch_upload
 };
 
 // Host side of a prepared batch: the built windows and their device copy.

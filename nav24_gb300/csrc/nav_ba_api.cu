@@ -84,6 +84,7 @@ void clear_stats(nav_ba_result* r) {
     r->n_active_edges = r->n_free_cams = r->n_free_points = r->n_schur_blocks = 0;
     r->pcg_iterations_total = 0;
     r->status = NAV_BA_OK;
+    r->edge_iterations = r->h2d_bytes = r->d2h_bytes = 0;
 }
 
 bool fits_window_engine(const HostWindow& h) { return h.nfc <= kWinMaxFreeCams && h.ncam <= kWinMaxCams; }
@@ -142,9 +143,11 @@ nav_ba_status download_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n
     std::vector<double> trace((size_t)b.trace_stride * n);
     std::vector<WinStats> stats(n);
     cudaError_t e = cudaSuccess;
+    int64_t d2h = 0;
     auto dn = [&](void* dst, const void* src, size_t bytes) {
         if (e != cudaSuccess || bytes == 0) return;
         e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+        d2h += (int64_t)bytes;
     };
     dn(cams.data(), b.d_cam_out, sizeof(CamState) * b.ncam);
     dn(pts.data(), b.d_pt_out, sizeof(double) * 4 * b.npt);
@@ -162,6 +165,8 @@ nav_ba_status download_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n
         r->n_free_cams = h.nfc;
         r->n_free_points = h.nfp;
         r->n_schur_blocks = h.n_schur_blocks;
+        r->h2d_bytes = b.h2d_bytes;
+        r->d2h_bytes = d2h;
         if (pb.host_status[i] == NAV_BA_EMPTY) {
             write_passthrough(p, r, false);
             r->termination = NAV_BA_TERM_NOTHING_TO_DO;
@@ -177,6 +182,7 @@ nav_ba_status download_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n
         r->trials_accepted = s.accepted;
         r->trials_rejected = s.rejected;
         r->termination = s.termination;
+        r->edge_iterations = (int64_t)h.ne * s.iterations_done;
         if (s.status != NAV_BA_OK) {
             overall = (nav_ba_status)s.status;
             continue;
@@ -307,15 +313,15 @@ nav_ba_status nav_ba_solve_batched(nav_ba_ctx* ctx, const nav_ba_problem* window
     return solve_impl(ctx, windows, n, o, results);
 }
 
-nav_ba_status nav_ba_prepare(nav_ba_ctx* ctx, const nav_ba_problem* p, const nav_ba_options* o) {
+nav_ba_status nav_ba_prepare_batched(nav_ba_ctx* ctx, const nav_ba_problem* p, int32_t n, const nav_ba_options* o) {
     if (!ctx) return NAV_BA_ERR_ARGUMENT;
-    if (!p || !o) return set_err(ctx, NAV_BA_ERR_ARGUMENT, "NULL argument");
+    if (!p || !o || n < 0) return set_err(ctx, NAV_BA_ERR_ARGUMENT, "NULL argument");
     cudaSetDevice(ctx->device);
     window_batch_free(ctx->prepared.dev);
     ctx->has_prepared = false;
     PreparedBatch& pb = ctx->prepared;
     pb = PreparedBatch();
-    nav_ba_status st = build_batch(ctx, p, 1, o, pb);
+    nav_ba_status st = build_batch(ctx, p, n, o, pb);
     if (st != NAV_BA_OK) return st;
     std::string why;
     cudaError_t e = window_batch_upload(pb, ctx->stream, o->precision, o->iterations + 1, &why);
@@ -323,16 +329,33 @@ nav_ba_status nav_ba_prepare(nav_ba_ctx* ctx, const nav_ba_problem* p, const nav
         window_batch_free(pb.dev);
         return cuda_status(ctx, e, "upload");
     }
-    ctx->prepared_problems.assign(1, *p);
+    ctx->prepared_problems.assign(p, p + n);
     ctx->prepared_opts = *o;
     ctx->has_prepared = true;
+    return NAV_BA_OK;
+}
+
+nav_ba_status nav_ba_prepare(nav_ba_ctx* ctx, const nav_ba_problem* p, const nav_ba_options* o) {
+    return nav_ba_prepare_batched(ctx, p, 1, o);
+}
+
+nav_ba_status nav_ba_fetch_batched(nav_ba_ctx* ctx, nav_ba_result* results) {
+    if (!ctx) return NAV_BA_ERR_ARGUMENT;
+    if (!ctx->has_prepared || !results) return set_err(ctx, NAV_BA_ERR_ARGUMENT, "nothing prepared");
+    cudaSetDevice(ctx->device);
+    const int n = (int)ctx->prepared_problems.size();
+    std::vector<nav_ba_result> tmp(results, results + n);
+    for (auto& r : tmp) clear_stats(&r);
+    nav_ba_status st = download_batch(ctx, ctx->prepared_problems.data(), n, ctx->prepared, tmp.data());
+    if (st != NAV_BA_OK && st != NAV_BA_EMPTY) return st;
+    std::copy(tmp.begin(), tmp.end(), results);
     return NAV_BA_OK;
 }
 
 nav_ba_status nav_ba_run(nav_ba_ctx* ctx, const nav_ba_options* o, nav_ba_result* stats) {
     if (!ctx) return NAV_BA_ERR_ARGUMENT;
     if (!ctx->has_prepared) return set_err(ctx, NAV_BA_ERR_ARGUMENT, "nothing prepared");
-    const nav_ba_options& po = ctx->prepared_opts;
+    const nav_ba_options po = ctx->prepared_opts;
     if (o && (o->precision != po.precision || o->iterations != po.iterations))
         return set_err(ctx, NAV_BA_ERR_ARGUMENT, "run options must match the prepared precision and iterations");
     cudaSetDevice(ctx->device);
@@ -346,20 +369,32 @@ nav_ba_status nav_ba_run(nav_ba_ctx* ctx, const nav_ba_options* o, nav_ba_result
     if (stats) {
         float t = 0.f;
         cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1);
-        WinStats s{};
+        const int n = ctx->prepared.dev.n_win;
+        std::vector<WinStats> ws(n);
         if (ctx->prepared.dev.n_queue > 0) {
-            e = cudaMemcpy(&s, ctx->prepared.dev.d_stats, sizeof(WinStats), cudaMemcpyDeviceToHost);
+            e = cudaMemcpy(ws.data(), ctx->prepared.dev.d_stats, sizeof(WinStats) * n, cudaMemcpyDeviceToHost);
             if (e != cudaSuccess) return cuda_status(ctx, e, "stats");
         }
+        clear_stats(stats);
         stats->time_solve_ms = t;
-        stats->initial_cost = s.initial_cost;
-        stats->final_cost = s.final_cost;
-        stats->final_lambda = s.final_lambda;
-        stats->iterations_done = s.iterations_done;
-        stats->trials_accepted = s.accepted;
-        stats->trials_rejected = s.rejected;
-        stats->termination = s.termination;
-        stats->status = s.status;
+        int64_t edge_iters = 0;
+        for (int i = 0; i < n; ++i) {
+            if (ctx->prepared.host_status[i] != NAV_BA_OK) continue;
+            const WinStats& s = ws[i];
+            stats->initial_cost += s.initial_cost;
+            stats->final_cost += s.final_cost;
+            stats->final_lambda = s.final_lambda;
+            stats->iterations_done += s.iterations_done;
+            stats->trials_accepted += s.accepted;
+            stats->trials_rejected += s.rejected;
+            stats->termination = s.termination;
+            if (s.status != NAV_BA_OK) stats->status = s.status;
+            stats->n_active_edges += ctx->prepared.host[i].ne;
+            stats->n_free_cams += ctx->prepared.host[i].nfc;
+            stats->n_free_points += ctx->prepared.host[i].nfp;
+            edge_iters += (int64_t)ctx->prepared.host[i].ne * s.iterations_done;
+        }
+        stats->edge_iterations = edge_iters;
     }
     return NAV_BA_OK;
 }

@@ -901,9 +901,11 @@ cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int prec
     alloc(&b.d_trace, sizeof(double) * trace_stride * pb.desc.size());
     alloc(&b.d_stats, sizeof(WinStats) * pb.desc.size());
     alloc(&b.d_debug, sizeof(double) * ((size_t)max_m * max_m + max_m));
+    b.h2d_bytes = 0;
     auto up = [&](void* dst, const void* src, size_t bytes) {
         if (err != cudaSuccess || bytes == 0) return;
         err = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream);
+        b.h2d_bytes += (int64_t)bytes;
     };
     up(b.d_win, pb.desc.data(), sizeof(WinDesc) * pb.desc.size());
     up(b.d_order, order.data(), sizeof(int32_t) * order.size());
