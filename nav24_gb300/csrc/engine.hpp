@@ -22,6 +22,8 @@ struct WinDesc {
     int32_t pt0, npt;     // point range (global)
     int32_t e0, ne;       // active-edge range (global), point-major
     int32_t nfc, nfp;     // free cameras / points
+    int64_t pair0;        // first slot of the window's Schur pair list (global)
+    int64_t npair;        // pair-list length
 };
 
 struct WinStats {
@@ -45,9 +47,9 @@ struct LmOptions {
 struct WindowBatch {
     int32_t n_win = 0;        // windows in the batch (stats/trace rows)
     int32_t n_queue = 0;      // windows the kernel solves (the work queue)
-    int64_t ncam = 0, npt = 0, ne = 0;
+    int64_t ncam = 0, npt = 0, ne = 0, npair = 0;
     int32_t max_m = 0;        // largest 6 * nfc in the batch
-    int32_t max_ncam = 0;
+    int32_t max_ncam = 0;     // largest camera count in the batch
     int32_t precision = 0;    // buffers sized for this precision
     int32_t trace_stride = 0; // iterations + 1
     // device inputs
@@ -65,11 +67,11 @@ struct WindowBatch {
     // device scratch
     double* d_x[2] = {nullptr, nullptr};  // [npt][4] current / trial points
     void* d_pt_vg = nullptr;       // [npt][12] Real: V (6 packed) g (3)
-    void* d_pt_vinv = nullptr;     // [npt][8]  Real
-    void* d_edge_jce = nullptr;    // [ne][16]  Real: jc (12) e (2) w (1)
-    void* d_edge_w = nullptr;      // [ne][18]  Real
-    void* d_edge_y = nullptr;      // [ne][18]  Real
+    void* d_pt_lt = nullptr;       // [npt][12] Real: Linv (6 packed lower) t = Linv g (3)
+    void* d_edge_w = nullptr;      // [ne][18]  Real: W = w Jc^T Jp
+    void* d_edge_a = nullptr;      // [ne][18]  Real: A = W Linv^T
     int32_t* d_cam_list = nullptr; // [ne] camera-major edge list (free cameras only)
+    uint32_t* d_pairs = nullptr;   // [npair] Schur pairs (edge i << 16 | edge j), window-local
     // device outputs
     CamState* d_cam_out = nullptr;
     double* d_pt_out = nullptr;    // [npt][4]
@@ -78,6 +80,12 @@ struct WindowBatch {
     double* d_debug = nullptr;     // reduced-system debug output (optional)
     size_t bytes = 0;
     int64_t h2d_bytes = 0;    // bytes uploaded by window_batch_upload
+};
+
+// Launch shape of the window kernel (picked by the autotuner).
+struct WindowLaunch {
+    int32_t cluster = 4;      // CTAs cooperating on one window (1, 2, 4 or 8)
+    int32_t threads = 256;    // threads per CTA
 };
 
 // Host side of a prepared batch: the built windows and their device copy.
@@ -99,7 +107,10 @@ void window_batch_free(WindowBatch& b);
 // debug_lambda >= 0 stops after assembling the reduced system of window 0 at that damping
 // and writes [S (m*m) | b (m)] to d_debug.
 cudaError_t window_batch_launch(PreparedBatch& pb, cudaStream_t stream, int precision,
-                                int threads, double debug_lambda);
+                                WindowLaunch shape, double debug_lambda);
+
+// Shared memory one CTA of the window kernel needs for a batch (bytes).
+size_t window_smem_bytes(int max_m, int max_ncam, int precision);
 
 // Linearize every observation of a problem at its initial state (device, precision given);
 // outputs in observation order, FP64.

@@ -21,8 +21,8 @@ struct nav_ba_ctx {
     std::vector<nav_ba_problem> prepared_problems;  // shapes of the prepared problem (no data)
     nav_ba_options prepared_opts{};
     bool has_prepared = false;
-    int threads_fp64 = 256;
-    int threads_mixed = 256;
+    WindowLaunch shape[2];        // per precision (autotuned on nav_ba_prepare_batched)
+    bool tuned[2] = {false, false};
 };
 
 namespace {
@@ -87,7 +87,47 @@ void clear_stats(nav_ba_result* r) {
     r->edge_iterations = r->h2d_bytes = r->d2h_bytes = 0;
 }
 
-bool fits_window_engine(const HostWindow& h) { return h.nfc <= kWinMaxFreeCams && h.ncam <= kWinMaxCams; }
+bool fits_window_engine(const HostWindow& h) {
+    return h.nfc <= kWinMaxFreeCams && h.ncam <= kWinMaxCams && h.ne < 65536;
+}
+
+// Autotuner of the window kernel's launch shape: every candidate (cluster size x threads per
+// CTA) solves the prepared batch once; the fastest is kept for the context and precision.
+cudaError_t autotune(nav_ba_ctx* ctx, PreparedBatch& pb, int precision) {
+    const int ths_fp64[] = {256};
+    const int ths_mixed[] = {256, 512};
+    const int* ths = precision == NAV_BA_MIXED ? ths_mixed : ths_fp64;
+    const int nth = precision == NAV_BA_MIXED ? 2 : 1;
+    const int clusters[] = {1, 2, 4, 8};
+    float best = 1e30f;
+    WindowLaunch best_shape = ctx->shape[precision];
+    for (int ci = 0; ci < 4; ++ci) {
+        for (int ti = 0; ti < nth; ++ti) {
+            WindowLaunch sh{clusters[ci], ths[ti]};
+            cudaEventRecord(ctx->ev0, ctx->stream);
+            cudaError_t e = window_batch_launch(pb, ctx->stream, precision, sh, -1.0);
+            cudaEventRecord(ctx->ev1, ctx->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+            if (e != cudaSuccess) {
+                // a shape that cannot launch (occupancy) is skipped; any other error is reported
+                if (e == cudaErrorInvalidConfiguration || e == cudaErrorInvalidValue) {
+                    cudaGetLastError();
+                    continue;
+                }
+                return e;
+            }
+            float t = 0.f;
+            cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1);
+            if (t < best) {
+                best = t;
+                best_shape = sh;
+            }
+        }
+    }
+    ctx->shape[precision] = best_shape;
+    ctx->tuned[precision] = true;
+    return cudaSuccess;
+}
 
 // Validate and build all windows on the host.  Returns an error (nothing written) or OK.
 nav_ba_status build_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, const nav_ba_options* o,
@@ -214,9 +254,8 @@ nav_ba_status solve_impl(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, co
         return cuda_status(ctx, e, "upload");
     }
     const double t_setup = ms_since(t0);
-    const int threads = o->precision == NAV_BA_MIXED ? ctx->threads_mixed : ctx->threads_fp64;
     cudaEventRecord(ctx->ev0, ctx->stream);
-    e = window_batch_launch(pb, ctx->stream, o->precision, threads, -1.0);
+    e = window_batch_launch(pb, ctx->stream, o->precision, ctx->shape[o->precision], -1.0);
     cudaEventRecord(ctx->ev1, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) {
@@ -329,6 +368,11 @@ nav_ba_status nav_ba_prepare_batched(nav_ba_ctx* ctx, const nav_ba_problem* p, i
         window_batch_free(pb.dev);
         return cuda_status(ctx, e, "upload");
     }
+    e = autotune(ctx, pb, o->precision);
+    if (e != cudaSuccess) {
+        window_batch_free(pb.dev);
+        return cuda_status(ctx, e, "autotune");
+    }
     ctx->prepared_problems.assign(p, p + n);
     ctx->prepared_opts = *o;
     ctx->has_prepared = true;
@@ -359,10 +403,9 @@ nav_ba_status nav_ba_run(nav_ba_ctx* ctx, const nav_ba_options* o, nav_ba_result
     if (o && (o->precision != po.precision || o->iterations != po.iterations))
         return set_err(ctx, NAV_BA_ERR_ARGUMENT, "run options must match the prepared precision and iterations");
     cudaSetDevice(ctx->device);
-    const int threads = po.precision == NAV_BA_MIXED ? ctx->threads_mixed : ctx->threads_fp64;
     if (o) ctx->prepared.lm = lm_options(*o);
     cudaEventRecord(ctx->ev0, ctx->stream);
-    cudaError_t e = window_batch_launch(ctx->prepared, ctx->stream, po.precision, threads, -1.0);
+    cudaError_t e = window_batch_launch(ctx->prepared, ctx->stream, po.precision, ctx->shape[po.precision], -1.0);
     cudaEventRecord(ctx->ev1, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_status(ctx, e, "window kernel");
@@ -445,9 +488,7 @@ nav_ba_status nav_ba_reduced_system(nav_ba_ctx* ctx, const nav_ba_problem* p, co
     }
     std::string why;
     cudaError_t e = window_batch_upload(pb, ctx->stream, o1.precision, 2, &why);
-    if (e == cudaSuccess) e = window_batch_launch(pb, ctx->stream, o1.precision,
-                                                  o1.precision == NAV_BA_MIXED ? ctx->threads_mixed : ctx->threads_fp64,
-                                                  lambda);
+    if (e == cudaSuccess) e = window_batch_launch(pb, ctx->stream, o1.precision, ctx->shape[o1.precision], lambda);
     const int m = 6 * h.nfc;
     std::vector<double> out((size_t)m * m + m);
     if (e == cudaSuccess)

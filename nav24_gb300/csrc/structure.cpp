@@ -97,6 +97,18 @@ void build_window(const nav_ba_problem& p, const nav_ba_options& o, HostWindow& 
     for (int i = 0; i < w.npt; ++i)
         for (int k = 0; k < 3; ++k) w.pt[4LL * i + k] = p.points[3LL * i + k];
     w.n_schur_blocks = count_schur_blocks(w);
+    w.n_pairs = 0;
+    for (int i = 0; i < w.npt; ++i) {
+        if (w.pt_free[i] < 0) continue;
+        for (int e = w.pt_eoff[i]; e < w.pt_eoff[i + 1]; ++e) {
+            const int a = w.cam_free[w.edge_cam[e]];
+            if (a < 0) continue;
+            for (int f = w.pt_eoff[i]; f < w.pt_eoff[i + 1]; ++f) {
+                const int b = w.cam_free[w.edge_cam[f]];
+                if (b >= 0 && b <= a) ++w.n_pairs;
+            }
+        }
+    }
 }
 
 int32_t count_schur_blocks(const HostWindow& w) {

@@ -35,6 +35,8 @@ struct HostWindow {
     std::vector<double> edge_uv;      // [ne * 2]
     std::vector<int32_t> edge_pt;     // [ne] point of each active edge
     int32_t n_schur_blocks = 0;       // lower-triangle co-visible free-camera block pairs
+    int64_t n_pairs = 0;              // Schur pairs (i, j): same free point, free cameras,
+                                      // free index of j's camera <= that of i's camera
 };
 
 // Validate a problem exactly like the oracle: pointers, sizes, index ranges, finiteness.

@@ -1,44 +1,78 @@
 // window_engine.cu - batched bundle adjustment: one persistent kernel solves many windows.
 //
-// Each CTA takes windows from a work queue (the host orders it, largest first) and runs the
-// whole Levenberg-Marquardt loop of one window before taking the next, so a batch of uneven
-// windows is a single launch.  Per window the CTA keeps the camera states, the camera blocks
-// of H and the reduced camera system S in shared memory; per-point and per-edge quantities
-// stream through global memory (L2-resident for a window).
+// A thread-block cluster of C CTAs (C = 1, 2, 4 or 8, picked by the autotuner) solves one
+// window at a time: rank 0 takes the next window from a work queue (ordered by the host,
+// largest first) and the cluster runs that window's whole Levenberg-Marquardt loop before taking
+// the next, so a batch of uneven windows is one launch.  Every CTA keeps its own copy of the
+// window's camera states; rank 0 keeps the camera blocks of H and the reduced camera system S
+// (packed lower triangle, FP64) in its shared memory, the other ranks write into it through
+// distributed shared memory.  Per-point and per-edge quantities live in global memory; with C
+// CTAs per window only 1/C as many windows are in flight, which keeps their scratch in L2.
 //
-// One LM iteration (g2o OptimizationAlgorithmLevenberg::solve semantics, as used by nav24's
+// One LM iteration (g2o OptimizationAlgorithmLevenberg::solve semantics as used by nav24's
 // GraphOptim::solve, core/backEnd/BE_GraphOptim.cpp:67-68):
-//   linearize  thread per point: e, J_pose, J_point, Huber weight per edge
-//              (EdgeSE3ProjectXYZ::computeError/linearizeOplus, OptimizableTypes.hpp:102-107,
-//              OptimizableTypes.cpp:140-161); V_p, g_p in registers; W_e = w Jc^T Jp stored;
-//              warp per camera over its edge list: U_c, g_c by warp-shuffle reduction.
-//   trial      Vinv_p = (V_p + lambda I)^-1, Y_e = W_e Vinv_p (thread per point);
-//              S_ab = [a==b](U_a + lambda I) - sum Y_i W_j^T, one warp per 6x6 block, summed
-//              in registers and reduced by shuffles (no atomics, fixed order);
-//              FP64 Cholesky of S in shared memory; dx_p by back-substitution; T <- exp(dx) T;
-//              cost of the trial state; gain ratio, accept/reject, damping update.
-// Real is double (plain FP64 form) or float (mixed form: residuals, Jacobians and Hessian
-// blocks in FP32; S, its Cholesky, the states, the SE(3) update and the cost sums in FP64).
+//   linearize  point-major, thread per point: residual, pose/point Jacobians and Huber weight per
+//              edge (EdgeSE3ProjectXYZ::computeError/linearizeOplus, OptimizableTypes.hpp:102-107,
+//              OptimizableTypes.cpp:140-161); V_p, g_p; W_e = w Jc^T Jp stored per edge.
+//              camera-major, warp per camera: the edges are re-linearized and U_c, g_c summed by
+//              warp shuffles (nothing per edge is stored for them).
+//   trial      point-major: V_p + lambda I = R R^T (3x3 Cholesky), L = R^-1, A_e = W_e L^T,
+//              t_p = L g_p, so that W V^-1 W^T = A A^T and W V^-1 g = A t.
+//              warp per 6x6 block of S over the block's pair list (built once per window,
+//              deterministic order): S_ab = [a==b](U_a + lambda I) - sum A_i A_j^T, summed in
+//              registers and reduced by shuffles, no atomics; b'_a = g_a - sum A_i t_p.
+//              FP64 Cholesky of S (rank 0); dx_p = L^T (t_p - sum A_i^T dx_c); T <- exp(dx) T;
+//              cost of the trial state; gain ratio, accept/reject and damping update.
+// Real is double (plain FP64 form) or float (mixed form: residuals, Jacobians, H blocks and the
+// Schur products in FP32; S, its Cholesky, the states, the SE(3) update and cost sums in FP64).
 #include <algorithm>
 #include <cfloat>
 
+#include <cooperative_groups.h>
+
 #include "engine.hpp"
+
+namespace cg = cooperative_groups;
 
 namespace navba {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
+constexpr int kMaxCluster = 8;
+constexpr int kMaxBlocks = kWinMaxFreeCams * (kWinMaxFreeCams + 1) / 2;
 
 struct SmemHead {
-    CamState cams[2][kWinMaxCams];
-    double U[kWinMaxFreeCams][28];  // packed lower U (21) | g_c (6) | pad
-    double red[66];
-    int32_t fcam[kWinMaxFreeCams];
-    int32_t loff[kWinMaxCams + 1];
-    int32_t lcnt[kWinMaxCams];
-    double lambda, nu, chi, chi_new, scale, maxdiag;
-    int32_t cur, ok, win, pad;
+    double U[kWinMaxFreeCams][28];         // rank 0: packed lower U (21) | g_c (6) | pad
+    double cred[2][kMaxCluster][4];        // rank 0: cluster reduction slots (double-buffered)
+    double red[2 * 16 * 3];                // per CTA: block reduction scratch
+    double bcast[4];                       // per CTA: reduced values
+    int32_t fcam[kWinMaxFreeCams];         // per CTA: free index -> local camera
+    int32_t loff[kWinMaxCams + 1];         // per CTA: camera-major list offsets
+    int32_t lcnt[kWinMaxCams];             // per CTA: edges per camera (free cameras)
+    int32_t poff[kMaxBlocks + 1];          // rank 0: pair-list offsets of the S blocks
+    int32_t pcnt[kMaxBlocks];              // rank 0: pairs per S block
+    int32_t cur, ok, win, slot;
 };
+
+// Offsets of the dynamic part of shared memory (after SmemHead), shared by host and device.
+struct Dyn {
+    size_t cams, camr, camd, dcl, S, bs, total;
+};
+
+NAVBA_HD size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+NAVBA_HD Dyn dyn_layout(int max_m, int max_ncam, int real_size) {
+    Dyn d;
+    size_t o = align16(sizeof(SmemHead));
+    d.cams = o; o = align16(o + sizeof(CamState) * 2 * max_ncam);
+    d.camr = o; o = align16(o + (size_t)real_size * 2 * max_ncam * 12);
+    d.camd = o; o = align16(o + sizeof(double) * max_ncam * 12);
+    d.dcl = o;  o = align16(o + sizeof(double) * max_m);
+    d.S = o;    o = align16(o + sizeof(double) * ((size_t)max_m * (max_m + 1) / 2));
+    d.bs = o;   o = align16(o + sizeof(double) * max_m);
+    d.total = o;
+    return d;
+}
 
 template <class Real>
 struct WinArgs {
@@ -56,11 +90,11 @@ struct WinArgs {
     const double* edge_uv;
     double* x[2];
     Real* pt_vg;
-    Real* pt_vinv;
-    Real* edge_jce;
+    Real* pt_lt;
     Real* edge_w;
-    Real* edge_y;
+    Real* edge_a;
     int32_t* cam_list;
+    uint32_t* pairs;
     CamState* cam_out;
     double* pt_out;
     double* trace;
@@ -70,42 +104,80 @@ struct WinArgs {
     double debug_lambda;
     Intr intr;
     LmOptions lm;
-    int32_t ld;     // leading dimension of S in shared memory
-    int32_t max_m;
+    int32_t max_m, max_ncam;
 };
 
 NAVBA_HD int tri(int r, int c) { return r * (r + 1) / 2 + c; }  // packed lower index, c <= r
 
-__device__ __forceinline__ double block_sum(double v, double* red) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
-    __syncthreads();
-    if (lane == 0) red[wid] = v;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double r = 0.0;
-        for (int i = 0; i < nw; ++i) r += red[i];
-        red[64] = r;
-    }
-    __syncthreads();
-    return red[64];
+// Per-CTA view of the cluster working on a window.
+struct CC {
+    int rank, csize;
+    int gt, CT;   // thread index / count over the cluster
+    int gw, CW;   // warp index / count over the cluster
+    int lane, wid, nw;
+    SmemHead* s;   // this CTA's head
+    SmemHead* s0;  // rank 0's head (distributed shared memory)
+    double* S0;    // rank 0's reduced system
+    double* bs0;   // rank 0's right-hand side / step
+};
+
+__device__ __forceinline__ void csync() { cg::this_cluster().sync(); }
+
+// Decode lower-triangle block index blk = a (a + 1) / 2 + b, b <= a.
+__device__ __forceinline__ void decode_block(int blk, int& a, int& b) {
+    a = (int)((sqrt(8.0 * blk + 1.0) - 1.0) * 0.5);
+    while ((a + 1) * (a + 2) / 2 <= blk) ++a;
+    while (a * (a + 1) / 2 > blk) --a;
+    b = blk - a * (a + 1) / 2;
 }
 
-__device__ __forceinline__ double block_max(double v, double* red) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+// Sums (or a max for the first value when MAX0) of three per-thread values over the whole
+// cluster; every thread of every CTA gets the same result (fixed reduction order).
+template <bool MAX0>
+__device__ double3 cluster_reduce3(CC& c, double a, double b, double d) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(kFull, v, o));
+    for (int o = 16; o > 0; o >>= 1) {
+        const double ta = __shfl_down_sync(kFull, a, o);
+        a = MAX0 ? fmax(a, ta) : a + ta;
+        b += __shfl_down_sync(kFull, b, o);
+        d += __shfl_down_sync(kFull, d, o);
+    }
+    SmemHead& s = *c.s;
     __syncthreads();
-    if (lane == 0) red[wid] = v;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double r = 0.0;
-        for (int i = 0; i < nw; ++i) r = fmax(r, red[i]);
-        red[64] = r;
+    if (c.lane == 0) {
+        s.red[3 * c.wid] = a;
+        s.red[3 * c.wid + 1] = b;
+        s.red[3 * c.wid + 2] = d;
     }
     __syncthreads();
-    return red[64];
+    if (threadIdx.x == 0) {
+        double ra = s.red[0], rb = s.red[1], rd = s.red[2];
+        for (int i = 1; i < c.nw; ++i) {
+            ra = MAX0 ? fmax(ra, s.red[3 * i]) : ra + s.red[3 * i];
+            rb += s.red[3 * i + 1];
+            rd += s.red[3 * i + 2];
+        }
+        double* slot = c.s0->cred[s.slot][c.rank];
+        slot[0] = ra;
+        slot[1] = rb;
+        slot[2] = rd;
+    }
+    csync();
+    if (threadIdx.x == 0) {
+        double ra = c.s0->cred[s.slot][0][0], rb = c.s0->cred[s.slot][0][1], rd = c.s0->cred[s.slot][0][2];
+        for (int r = 1; r < c.csize; ++r) {
+            const double* slot = c.s0->cred[s.slot][r];
+            ra = MAX0 ? fmax(ra, slot[0]) : ra + slot[0];
+            rb += slot[1];
+            rd += slot[2];
+        }
+        s.bcast[0] = ra;
+        s.bcast[1] = rb;
+        s.bcast[2] = rd;
+        s.slot ^= 1;
+    }
+    __syncthreads();
+    return make_double3(s.bcast[0], s.bcast[1], s.bcast[2]);
 }
 
 template <class Real>
@@ -117,14 +189,14 @@ __device__ __forceinline__ void cam_real(const CamState& c, Real* o) {
     o[11] = (Real)c.t[2];
 }
 
-// Robust chi2 of the window for the cameras `camc` (12 values each, precision Cost) and the
-// point buffer X.
+// Cluster-split robust chi2 of the window for cameras `camc` (12 values per camera, precision
+// Cost) and points X; returns this thread's partial sum.
 template <class Cost, class Real>
-__device__ double window_cost(const WinArgs<Real>& A, const WinDesc& D, SmemHead& s, const Cost* camc,
-                              const double* X) {
+__device__ double cost_partial(const WinArgs<Real>& A, const CC& c, const WinDesc& D, const Cost* camc,
+                               const double* X) {
     double acc = 0.0;
     const Cost delta = (Cost)A.lm.huber_delta;
-    for (int p = threadIdx.x; p < D.npt; p += blockDim.x) {
+    for (int p = c.gt; p < D.npt; p += c.CT) {
         const int gp = D.pt0 + p;
         const Cost Xr[3] = {(Cost)X[4LL * gp], (Cost)X[4LL * gp + 1], (Cost)X[4LL * gp + 2]};
         const int e1 = A.pt_eoff[gp + 1];
@@ -134,136 +206,195 @@ __device__ double window_cost(const WinArgs<Real>& A, const WinDesc& D, SmemHead
             acc += edge_cost<Cost>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta);
         }
     }
-    return block_sum(acc, s.red);
+    return acc;
 }
 
-// FP64 camera array (12 values per camera) of camera buffer cb, built in `out` (shared).
+// Camera-major edge lists of the free cameras and the pair lists of the S blocks.
 template <class Real>
-__device__ void cams_fp64(const WinDesc& D, const SmemHead& s, int cb, double* out) {
-    for (int c = threadIdx.x; c < D.ncam; c += blockDim.x) cam_real<double>(s.cams[cb][c], out + 12 * c);
-    __syncthreads();
-}
-
-// Camera-major list of the edges of each free camera (stable: point-major order kept).
-template <class Real>
-__device__ void build_cam_lists(const WinArgs<Real>& A, const WinDesc& D, SmemHead& s) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int c = wid; c < D.ncam; c += nw) {
+__device__ void build_lists(const WinArgs<Real>& A, CC& c, const WinDesc& D) {
+    SmemHead& s = *c.s;
+    cg::cluster_group cl = cg::this_cluster();
+    for (int cam = c.gw; cam < D.ncam; cam += c.CW) {
         int cnt = 0;
-        if (A.cam_free[D.cam0 + c] >= 0) {
+        if (A.cam_free[D.cam0 + cam] >= 0) {
             for (int base = 0; base < D.ne; base += 32) {
-                const int e = base + lane;
-                const bool hit = e < D.ne && A.edge_cam[D.e0 + e] == c;
-                cnt += __popc(__ballot_sync(kFull, hit));
+                const int e = base + c.lane;
+                cnt += __popc(__ballot_sync(kFull, e < D.ne && A.edge_cam[D.e0 + e] == cam));
             }
         }
-        if (lane == 0) s.lcnt[c] = cnt;
+        if (c.lane < c.csize) cl.map_shared_rank(c.s, c.lane)->lcnt[cam] = cnt;
     }
-    __syncthreads();
+    csync();
     if (threadIdx.x == 0) {
         int acc = 0;
-        for (int c = 0; c < D.ncam; ++c) {
-            s.loff[c] = acc;
-            acc += s.lcnt[c];
+        for (int cam = 0; cam < D.ncam; ++cam) {
+            s.loff[cam] = acc;
+            acc += s.lcnt[cam];
+            const int a = A.cam_free[D.cam0 + cam];
+            if (a >= 0) s.fcam[a] = cam;
         }
         s.loff[D.ncam] = acc;
-        for (int c = 0; c < D.ncam; ++c) {
-            const int a = A.cam_free[D.cam0 + c];
-            if (a >= 0) s.fcam[a] = c;
-        }
     }
     __syncthreads();
-    for (int c = wid; c < D.ncam; c += nw) {
-        if (A.cam_free[D.cam0 + c] < 0) continue;
-        int pos = s.loff[c];
+    for (int cam = c.gw; cam < D.ncam; cam += c.CW) {
+        if (A.cam_free[D.cam0 + cam] < 0) continue;
+        int pos = s.loff[cam];
         for (int base = 0; base < D.ne; base += 32) {
-            const int e = base + lane;
-            const bool hit = e < D.ne && A.edge_cam[D.e0 + e] == c;
-            const unsigned m = __ballot_sync(kFull, hit);
-            if (hit) A.cam_list[D.e0 + pos + __popc(m & ((1u << lane) - 1u))] = D.e0 + e;
-            pos += __popc(m);
+            const int e = base + c.lane;
+            const bool hit = e < D.ne && A.edge_cam[D.e0 + e] == cam;
+            const unsigned msk = __ballot_sync(kFull, hit);
+            if (hit) A.cam_list[D.e0 + pos + __popc(msk & ((1u << c.lane) - 1u))] = D.e0 + e;
+            pos += __popc(msk);
         }
     }
-    __syncthreads();
+    csync();  // every camera list is in global memory
+    const int nblk = D.nfc * (D.nfc + 1) / 2;
+    for (int blk = c.gw; blk < nblk; blk += c.CW) {
+        int a, b;
+        decode_block(blk, a, b);
+        const int ca = s.fcam[a], cb = s.fcam[b];
+        const int* list = A.cam_list + D.e0 + s.loff[ca];
+        const int cnt = s.lcnt[ca];
+        int n = 0;
+        for (int i = c.lane; i < cnt; i += 32) {
+            const int ei = list[i];
+            const int gp = D.pt0 + A.edge_pt[ei];
+            if (A.pt_free[gp] < 0) continue;
+            const int e1 = A.pt_eoff[gp + 1];
+            for (int ej = A.pt_eoff[gp]; ej < e1; ++ej) n += A.edge_cam[ej] == cb;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(kFull, n, o);
+        if (c.lane == 0) c.s0->pcnt[blk] = n;
+    }
+    csync();
+    if (c.rank == 0 && threadIdx.x == 0) {
+        int acc = 0;
+        for (int k = 0; k < nblk; ++k) {
+            s.poff[k] = acc;
+            acc += s.pcnt[k];
+        }
+        s.poff[nblk] = acc;
+    }
+    csync();
+    for (int blk = c.gw; blk < nblk; blk += c.CW) {
+        int a, b;
+        decode_block(blk, a, b);
+        const int ca = s.fcam[a], cb = s.fcam[b];
+        const int* list = A.cam_list + D.e0 + s.loff[ca];
+        const int cnt = s.lcnt[ca];
+        int64_t pos = D.pair0 + c.s0->poff[blk];
+        const int64_t end = D.pair0 + D.npair;
+        for (int base = 0; base < cnt; base += 32) {
+            const int i = base + c.lane;
+            int ei = -1, gp = -1, k = 0;
+            if (i < cnt) {
+                ei = list[i];
+                gp = D.pt0 + A.edge_pt[ei];
+                if (A.pt_free[gp] >= 0) {
+                    const int e1 = A.pt_eoff[gp + 1];
+                    for (int ej = A.pt_eoff[gp]; ej < e1; ++ej) k += A.edge_cam[ej] == cb;
+                }
+            }
+            int incl = k;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(kFull, incl, o);
+                if (c.lane >= o) incl += t;
+            }
+            const int total = __shfl_sync(kFull, incl, 31);
+            if (k > 0) {
+                int64_t q = pos + incl - k;
+                const int e1 = A.pt_eoff[gp + 1];
+                for (int ej = A.pt_eoff[gp]; ej < e1; ++ej)
+                    if (A.edge_cam[ej] == cb && q < end)
+                        A.pairs[q++] = ((uint32_t)(ei - D.e0) << 16) | (uint32_t)(ej - D.e0);
+            }
+            pos += total;
+        }
+    }
+    csync();
 }
 
-// Linearize all edges at the current state; fills U, g_c (shared), V_p, g_p, W_e (global).
+// Point-major linearization: V_p, g_p, W_e; returns this thread's max |diag V|.
 template <class Real>
-__device__ void window_linearize(const WinArgs<Real>& A, const WinDesc& D, SmemHead& s, const Real* camr) {
+__device__ double linearize_points(const WinArgs<Real>& A, const CC& c, const WinDesc& D, const Real* camr,
+                                   const double* X) {
     const Real delta = (Real)A.lm.huber_delta;
-    const double* X = A.x[s.cur];
     double mx = 0.0;
-    for (int p = threadIdx.x; p < D.npt; p += blockDim.x) {
+    for (int p = c.gt; p < D.npt; p += c.CT) {
         const int gp = D.pt0 + p;
-        const bool fp = A.pt_free[gp] >= 0;
+        if (A.pt_free[gp] < 0) continue;
         const Real Xr[3] = {(Real)X[4LL * gp], (Real)X[4LL * gp + 1], (Real)X[4LL * gp + 2]};
         Real V[6] = {0, 0, 0, 0, 0, 0}, g[3] = {0, 0, 0};
         const int e1 = A.pt_eoff[gp + 1];
         for (int e = A.pt_eoff[gp]; e < e1; ++e) {
-            const int c = A.edge_cam[e];
-            const Real* cr = camr + 12 * c;
+            const int cam = A.edge_cam[e];
+            const Real* cr = camr + 12 * cam;
             const Real z[2] = {(Real)A.edge_uv[2LL * e], (Real)A.edge_uv[2LL * e + 1]};
             EdgeLin<Real> L;
             edge_linearize<Real>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta, L);
-            Real* jce = A.edge_jce + 16LL * e;
+            const Real w = L.w;
+            const Real* jp = L.jp;
+            V[0] += w * (jp[0] * jp[0] + jp[3] * jp[3]);
+            V[1] += w * (jp[0] * jp[1] + jp[3] * jp[4]);
+            V[2] += w * (jp[0] * jp[2] + jp[3] * jp[5]);
+            V[3] += w * (jp[1] * jp[1] + jp[4] * jp[4]);
+            V[4] += w * (jp[1] * jp[2] + jp[4] * jp[5]);
+            V[5] += w * (jp[2] * jp[2] + jp[5] * jp[5]);
+            const Real we0 = -w * L.e[0], we1 = -w * L.e[1];
+            g[0] += jp[0] * we0 + jp[3] * we1;
+            g[1] += jp[1] * we0 + jp[4] * we1;
+            g[2] += jp[2] * we0 + jp[5] * we1;
+            if (A.cam_free[D.cam0 + cam] >= 0) {
+                Real* W = A.edge_w + 18LL * e;
 #pragma unroll
-            for (int k = 0; k < 12; ++k) jce[k] = L.jc[k];
-            jce[12] = L.e[0];
-            jce[13] = L.e[1];
-            jce[14] = L.w;
-            if (fp) {
-                const Real w = L.w;
-                const Real* jp = L.jp;
-                V[0] += w * (jp[0] * jp[0] + jp[3] * jp[3]);
-                V[1] += w * (jp[0] * jp[1] + jp[3] * jp[4]);
-                V[2] += w * (jp[0] * jp[2] + jp[3] * jp[5]);
-                V[3] += w * (jp[1] * jp[1] + jp[4] * jp[4]);
-                V[4] += w * (jp[1] * jp[2] + jp[4] * jp[5]);
-                V[5] += w * (jp[2] * jp[2] + jp[5] * jp[5]);
-                const Real we0 = -w * L.e[0], we1 = -w * L.e[1];
-                g[0] += jp[0] * we0 + jp[3] * we1;
-                g[1] += jp[1] * we0 + jp[4] * we1;
-                g[2] += jp[2] * we0 + jp[5] * we1;
-                if (A.cam_free[D.cam0 + c] >= 0) {
-                    Real* W = A.edge_w + 18LL * e;
+                for (int r = 0; r < 6; ++r)
 #pragma unroll
-                    for (int r = 0; r < 6; ++r)
-#pragma unroll
-                        for (int k = 0; k < 3; ++k) W[r * 3 + k] = w * (L.jc[r] * jp[k] + L.jc[6 + r] * jp[3 + k]);
-                }
+                    for (int k = 0; k < 3; ++k) W[r * 3 + k] = w * (L.jc[r] * jp[k] + L.jc[6 + r] * jp[3 + k]);
             }
         }
-        if (fp) {
-            Real* vg = A.pt_vg + 12LL * gp;
+        Real* vg = A.pt_vg + 12LL * gp;
 #pragma unroll
-            for (int k = 0; k < 6; ++k) vg[k] = V[k];
-            vg[6] = g[0]; vg[7] = g[1]; vg[8] = g[2];
-            mx = fmax(mx, fmax(fabs((double)V[0]), fmax(fabs((double)V[3]), fabs((double)V[5]))));
-        }
+        for (int k = 0; k < 6; ++k) vg[k] = V[k];
+        vg[6] = g[0];
+        vg[7] = g[1];
+        vg[8] = g[2];
+        mx = fmax(mx, fmax(fabs((double)V[0]), fmax(fabs((double)V[3]), fabs((double)V[5]))));
     }
-    __syncthreads();
-    // camera blocks: warp per free camera, shuffle reduction
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int a = wid; a < D.nfc; a += nw) {
-        const int c = s.fcam[a];
-        const int* list = A.cam_list + D.e0 + s.loff[c];
-        const int cnt = s.lcnt[c];
+    return mx;
+}
+
+// Camera-major linearization: U_c, g_c (warp per free camera) into rank 0; returns max |diag U|.
+template <class Real>
+__device__ double linearize_cameras(const WinArgs<Real>& A, const CC& c, const WinDesc& D, const Real* camr,
+                                    const double* X) {
+    const Real delta = (Real)A.lm.huber_delta;
+    const SmemHead& s = *c.s;
+    double mx = 0.0;
+    for (int a = c.gw; a < D.nfc; a += c.CW) {
+        const int cam = s.fcam[a];
+        const int* list = A.cam_list + D.e0 + s.loff[cam];
+        const int cnt = s.lcnt[cam];
+        const Real* cr = camr + 12 * cam;
         Real u[27];
 #pragma unroll
         for (int k = 0; k < 27; ++k) u[k] = Real(0);
-        for (int i = lane; i < cnt; i += 32) {
-            const Real* jce = A.edge_jce + 16LL * list[i];
-            Real jc[12];
-#pragma unroll
-            for (int k = 0; k < 12; ++k) jc[k] = jce[k];
-            const Real e0 = jce[12], e1 = jce[13], w = jce[14];
+        for (int i = c.lane; i < cnt; i += 32) {
+            const int e = list[i];
+            const int gp = D.pt0 + A.edge_pt[e];
+            const Real Xr[3] = {(Real)X[4LL * gp], (Real)X[4LL * gp + 1], (Real)X[4LL * gp + 2]};
+            const Real z[2] = {(Real)A.edge_uv[2LL * e], (Real)A.edge_uv[2LL * e + 1]};
+            EdgeLin<Real> L;
+            edge_linearize<Real>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta, L);
+            const Real w = L.w;
 #pragma unroll
             for (int r = 0; r < 6; ++r)
 #pragma unroll
-                for (int q = 0; q <= r; ++q) u[tri(r, q)] += w * (jc[r] * jc[q] + jc[6 + r] * jc[6 + q]);
-            const Real we0 = -w * e0, we1 = -w * e1;
+                for (int q = 0; q <= r; ++q) u[tri(r, q)] += w * (L.jc[r] * L.jc[q] + L.jc[6 + r] * L.jc[6 + q]);
+            const Real we0 = -w * L.e[0], we1 = -w * L.e[1];
 #pragma unroll
-            for (int r = 0; r < 6; ++r) u[21 + r] += jc[r] * we0 + jc[6 + r] * we1;
+            for (int r = 0; r < 6; ++r) u[21 + r] += L.jc[r] * we0 + L.jc[6 + r] * we1;
         }
 #pragma unroll
         for (int k = 0; k < 27; ++k)
@@ -271,92 +402,93 @@ __device__ void window_linearize(const WinArgs<Real>& A, const WinDesc& D, SmemH
             for (int o = 16; o > 0; o >>= 1) u[k] += __shfl_xor_sync(kFull, u[k], o);
 #pragma unroll
         for (int k = 0; k < 27; ++k)
-            if ((k & 31) == lane) s.U[a][k] = (double)u[k];
-        if (lane == 0) {
-            double m = 0.0;
+            if ((k & 31) == c.lane) c.s0->U[a][k] = (double)u[k];
 #pragma unroll
-            for (int r = 0; r < 6; ++r) m = fmax(m, fabs((double)u[tri(r, r)]));
-            mx = fmax(mx, m);
-        }
+        for (int r = 0; r < 6; ++r) mx = fmax(mx, fabs((double)u[tri(r, r)]));
     }
-    const double m = block_max(mx, s.red);
-    if (threadIdx.x == 0) s.maxdiag = m;
-    __syncthreads();
+    return mx;
 }
 
-// Reduced camera system for damping lambda: S (lower blocks, shared) and b' (shared).
+// Per free point: R R^T = V + lambda I, L = R^-1, t = L g, A_e = W_e L^T.  Returns the number of
+// points whose damped block was not positive definite (treated like a failed factorization).
 template <class Real>
-__device__ void window_schur(const WinArgs<Real>& A, const WinDesc& D, SmemHead& s, double lambda,
-                             double* S, double* bs) {
+__device__ int schur_points(const WinArgs<Real>& A, const CC& c, const WinDesc& D, double lambda) {
     const Real lam = (Real)lambda;
-    for (int p = threadIdx.x; p < D.npt; p += blockDim.x) {
+    int bad = 0;
+    for (int p = c.gt; p < D.npt; p += c.CT) {
         const int gp = D.pt0 + p;
         if (A.pt_free[gp] < 0) continue;
         const Real* vg = A.pt_vg + 12LL * gp;
-        Real V[6] = {vg[0] + lam, vg[1], vg[2], vg[3] + lam, vg[4], vg[5] + lam};
-        Real Vi[6];
-        inv_sym3<Real>(V, Vi);
-        Real* vi = A.pt_vinv + 8LL * gp;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) vi[k] = Vi[k];
-        const Real M[9] = {Vi[0], Vi[1], Vi[2], Vi[1], Vi[3], Vi[4], Vi[2], Vi[4], Vi[5]};
+        const Real v00 = vg[0] + lam, v01 = vg[1], v02 = vg[2], v11 = vg[3] + lam, v12 = vg[4], v22 = vg[5] + lam;
+        const Real r00 = sqrt(v00);
+        const Real r10 = v01 / r00, r20 = v02 / r00;
+        const Real d11 = v11 - r10 * r10;
+        const Real r11 = sqrt(d11);
+        const Real r21 = (v12 - r20 * r10) / r11;
+        const Real d22 = v22 - r20 * r20 - r21 * r21;
+        const Real r22 = sqrt(d22);
+        if (!(v00 > Real(0)) || !(d11 > Real(0)) || !(d22 > Real(0))) ++bad;
+        const Real l00 = Real(1) / r00, l11 = Real(1) / r11, l22 = Real(1) / r22;
+        const Real l10 = -r10 * l00 * l11;
+        const Real l21 = -r21 * l11 * l22;
+        const Real l20 = -(r20 * l00 + r21 * l10) * l22;
+        Real* lt = A.pt_lt + 12LL * gp;
+        lt[0] = l00; lt[1] = l10; lt[2] = l11; lt[3] = l20; lt[4] = l21; lt[5] = l22;
+        lt[6] = l00 * vg[6];
+        lt[7] = l10 * vg[6] + l11 * vg[7];
+        lt[8] = l20 * vg[6] + l21 * vg[7] + l22 * vg[8];
         const int e1 = A.pt_eoff[gp + 1];
         for (int e = A.pt_eoff[gp]; e < e1; ++e) {
             if (A.cam_free[D.cam0 + A.edge_cam[e]] < 0) continue;
             const Real* W = A.edge_w + 18LL * e;
-            Real* Y = A.edge_y + 18LL * e;
+            Real* Ae = A.edge_a + 18LL * e;
 #pragma unroll
             for (int r = 0; r < 6; ++r) {
                 const Real w0 = W[r * 3 + 0], w1 = W[r * 3 + 1], w2 = W[r * 3 + 2];
-#pragma unroll
-                for (int k = 0; k < 3; ++k) Y[r * 3 + k] = w0 * M[k] + w1 * M[3 + k] + w2 * M[6 + k];
+                Ae[r * 3 + 0] = w0 * l00;
+                Ae[r * 3 + 1] = w0 * l10 + w1 * l11;
+                Ae[r * 3 + 2] = w0 * l20 + w1 * l21 + w2 * l22;
             }
         }
     }
-    __syncthreads();
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    return bad;
+}
+
+// S blocks (warp per block over its pair list) into rank 0's packed S, and b'.
+template <class Real>
+__device__ void schur_blocks(const WinArgs<Real>& A, const CC& c, const WinDesc& D, double lambda) {
     const int nblk = D.nfc * (D.nfc + 1) / 2;
-    const int ld = A.ld;
-    for (int blk = wid; blk < nblk; blk += nw) {
-        int a = (int)((sqrt(8.0 * blk + 1.0) - 1.0) * 0.5);
-        while ((a + 1) * (a + 2) / 2 <= blk) ++a;
-        while (a * (a + 1) / 2 > blk) --a;
-        const int b = blk - a * (a + 1) / 2;
-        const int ca = s.fcam[a], cb = s.fcam[b];
-        const int* list = A.cam_list + D.e0 + s.loff[ca];
-        const int cnt = s.lcnt[ca];
+    for (int blk = c.gw; blk < nblk; blk += c.CW) {
+        int a, b;
+        decode_block(blk, a, b);
+        const int64_t base = D.pair0 + c.s0->poff[blk];
+        const int n = c.s0->pcnt[blk];
         Real acc[36];
         Real accb[6];
 #pragma unroll
         for (int k = 0; k < 36; ++k) acc[k] = Real(0);
 #pragma unroll
         for (int k = 0; k < 6; ++k) accb[k] = Real(0);
-        for (int i = lane; i < cnt; i += 32) {
-            const int ei = list[i];
-            const int gp = D.pt0 + A.edge_pt[ei];
-            if (A.pt_free[gp] < 0) continue;
-            const Real* Y = A.edge_y + 18LL * ei;
-            Real y[18];
+        for (int k = c.lane; k < n; k += 32) {
+            const uint32_t pr = A.pairs[base + k];
+            const int ei = D.e0 + (int)(pr >> 16), ej = D.e0 + (int)(pr & 0xffffu);
+            const Real* Ai = A.edge_a + 18LL * ei;
+            const Real* Aj = A.edge_a + 18LL * ej;
+            Real ai[18], aj[18];
 #pragma unroll
-            for (int k = 0; k < 18; ++k) y[k] = Y[k];
-            if (a == b) {
-                const Real* g = A.pt_vg + 12LL * gp + 6;
-                const Real g0 = g[0], g1 = g[1], g2 = g[2];
+            for (int q = 0; q < 18; ++q) ai[q] = Ai[q];
 #pragma unroll
-                for (int r = 0; r < 6; ++r) accb[r] += y[r * 3 + 0] * g0 + y[r * 3 + 1] * g1 + y[r * 3 + 2] * g2;
-            }
-            const int e1 = A.pt_eoff[gp + 1];
-            for (int ej = A.pt_eoff[gp]; ej < e1; ++ej) {
-                if (A.edge_cam[ej] != cb) continue;
-                const Real* W = A.edge_w + 18LL * ej;
-                Real wv[18];
+            for (int q = 0; q < 18; ++q) aj[q] = Aj[q];
 #pragma unroll
-                for (int k = 0; k < 18; ++k) wv[k] = W[k];
+            for (int r = 0; r < 6; ++r)
 #pragma unroll
-                for (int r = 0; r < 6; ++r)
+                for (int q = 0; q < 6; ++q)
+                    acc[r * 6 + q] += ai[r * 3 + 0] * aj[q * 3 + 0] + ai[r * 3 + 1] * aj[q * 3 + 1] + ai[r * 3 + 2] * aj[q * 3 + 2];
+            if (a == b && ei == ej) {
+                const Real* t = A.pt_lt + 12LL * (D.pt0 + A.edge_pt[ei]) + 6;
+                const Real t0 = t[0], t1 = t[1], t2 = t[2];
 #pragma unroll
-                    for (int q = 0; q < 6; ++q)
-                        acc[r * 6 + q] += y[r * 3 + 0] * wv[q * 3 + 0] + y[r * 3 + 1] * wv[q * 3 + 1] + y[r * 3 + 2] * wv[q * 3 + 2];
+                for (int r = 0; r < 6; ++r) accb[r] += ai[r * 3 + 0] * t0 + ai[r * 3 + 1] * t1 + ai[r * 3 + 2] * t2;
             }
         }
 #pragma unroll
@@ -371,140 +503,142 @@ __device__ void window_schur(const WinArgs<Real>& A, const WinDesc& D, SmemHead&
         }
 #pragma unroll
         for (int k = 0; k < 36; ++k) {
-            if ((k & 31) != lane) continue;
+            if ((k & 31) != c.lane) continue;
             const int r = k / 6, q = k % 6;
+            if (a == b && q > r) continue;
             double v = -(double)acc[k];
             if (a == b) {
-                v += s.U[a][r >= q ? tri(r, q) : tri(q, r)];
+                v += c.s0->U[a][tri(r, q)];
                 if (r == q) v += lambda;
             }
-            S[(6 * a + r) * ld + 6 * b + q] = v;
+            c.S0[tri(6 * a + r, 6 * b + q)] = v;
         }
-        if (a == b && lane < 6) {
+        if (a == b && c.lane < 6) {
 #pragma unroll
             for (int k = 0; k < 6; ++k)
-                if (k == lane) bs[6 * a + k] = s.U[a][21 + k] - (double)accb[k];
+                if (k == c.lane) c.bs0[6 * a + k] = c.s0->U[a][21 + k] - (double)accb[k];
         }
     }
-    __syncthreads();
 }
 
-// In-place Cholesky (LL^T) of the lower triangle of S (m x m, leading dimension ld), FP64.
-// Returns false (to all threads) when a pivot is not positive and finite.
-__device__ bool smem_cholesky(double* S, int m, int ld, SmemHead& s) {
+// In-place Cholesky (LL^T) of packed lower S (m x m) in this CTA's shared memory, FP64.
+__device__ bool smem_cholesky(double* S, int m, SmemHead& s) {
     if (threadIdx.x == 0) s.ok = 1;
     __syncthreads();
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int j = 0; j < m; ++j) {
         if (threadIdx.x == 0) {
-            const double d = S[j * ld + j];
+            const double d = S[tri(j, j)];
             if (!(d > 0.0) || !isfinite(d)) {
                 s.ok = 0;
-                S[j * ld + j] = 1.0;
+                S[tri(j, j)] = 1.0;
             } else {
-                S[j * ld + j] = sqrt(d);
+                S[tri(j, j)] = sqrt(d);
             }
         }
         __syncthreads();
-        const double piv = S[j * ld + j];
-        for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) S[i * ld + j] = S[i * ld + j] / piv;
+        const double piv = S[tri(j, j)];
+        for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) S[tri(i, j)] = S[tri(i, j)] / piv;
         __syncthreads();
         for (int i = j + 1 + wid; i < m; i += nw) {
-            const double lij = S[i * ld + j];
-            for (int k = j + 1 + lane; k <= i; k += 32) S[i * ld + k] -= lij * S[k * ld + j];
+            const double lij = S[tri(i, j)];
+            double* Si = S + tri(i, 0);
+            for (int k = j + 1 + lane; k <= i; k += 32) Si[k] -= lij * S[tri(k, j)];
         }
         __syncthreads();
     }
     return s.ok != 0;
 }
 
-// Solve L L^T x = b in place (warp 0), FP64.
-__device__ void smem_chol_solve(const double* L, int m, int ld, double* x) {
+// Solve L L^T x = b in place (warp 0), FP64, packed L.
+__device__ void smem_chol_solve(const double* L, int m, double* x) {
     if (threadIdx.x < 32) {
         const int lane = threadIdx.x;
         for (int i = 0; i < m; ++i) {
             double sum = 0.0;
-            for (int k = lane; k < i; k += 32) sum += L[i * ld + k] * x[k];
+            const double* Li = L + tri(i, 0);
+            for (int k = lane; k < i; k += 32) sum += Li[k] * x[k];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
-            if (lane == 0) x[i] = (x[i] - sum) / L[i * ld + i];
+            if (lane == 0) x[i] = (x[i] - sum) / Li[i];
             __syncwarp();
         }
         for (int i = m - 1; i >= 0; --i) {
             double sum = 0.0;
-            for (int k = i + 1 + lane; k < m; k += 32) sum += L[k * ld + i] * x[k];
+            for (int k = i + 1 + lane; k < m; k += 32) sum += L[tri(k, i)] * x[k];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
-            if (lane == 0) x[i] = (x[i] - sum) / L[i * ld + i];
+            if (lane == 0) x[i] = (x[i] - sum) / L[tri(i, i)];
             __syncwarp();
         }
     }
     __syncthreads();
 }
 
-// Apply the step: trial cameras (shared) and trial points (global); returns dx^T(lambda dx + b).
+// Trial points dx_p = L^T (t_p - sum A_e^T dx_c); returns this thread's dx^T(lambda dx + g) part.
 template <class Real>
-__device__ double window_update(const WinArgs<Real>& A, const WinDesc& D, SmemHead& s, double lambda,
-                                const double* dc, Real* camr_trial) {
-    const int cur = s.cur, tr = cur ^ 1;
-    double sc = 0.0;
-    for (int c = threadIdx.x; c < D.ncam; c += blockDim.x) {
-        const int a = A.cam_free[D.cam0 + c];
-        if (a >= 0) {
-            se3_left_update(dc + 6 * a, s.cams[cur][c], s.cams[tr][c]);
-#pragma unroll
-            for (int r = 0; r < 6; ++r) sc += dc[6 * a + r] * (lambda * dc[6 * a + r] + s.U[a][21 + r]);
-        }
-        cam_real<Real>(s.cams[tr][c], camr_trial + 12 * c);
-    }
+__device__ double update_points(const WinArgs<Real>& A, const CC& c, const WinDesc& D, double lambda,
+                                const double* dcl, int cur) {
     const double* Xc = A.x[cur];
-    double* Xt = A.x[tr];
-    for (int p = threadIdx.x; p < D.npt; p += blockDim.x) {
+    double* Xt = A.x[cur ^ 1];
+    double sc = 0.0;
+    for (int p = c.gt; p < D.npt; p += c.CT) {
         const int gp = D.pt0 + p;
         if (A.pt_free[gp] < 0) continue;
-        const Real* vg = A.pt_vg + 12LL * gp;
-        Real c3[3] = {vg[6], vg[7], vg[8]};
+        const Real* lt = A.pt_lt + 12LL * gp;
+        Real u0 = lt[6], u1 = lt[7], u2 = lt[8];
         const int e1 = A.pt_eoff[gp + 1];
         for (int e = A.pt_eoff[gp]; e < e1; ++e) {
             const int a = A.cam_free[D.cam0 + A.edge_cam[e]];
             if (a < 0) continue;
-            const Real* W = A.edge_w + 18LL * e;
+            const Real* Ae = A.edge_a + 18LL * e;
 #pragma unroll
             for (int r = 0; r < 6; ++r) {
-                const Real d = (Real)dc[6 * a + r];
-                c3[0] -= W[r * 3 + 0] * d;
-                c3[1] -= W[r * 3 + 1] * d;
-                c3[2] -= W[r * 3 + 2] * d;
+                const Real d = (Real)dcl[6 * a + r];
+                u0 -= Ae[r * 3 + 0] * d;
+                u1 -= Ae[r * 3 + 1] * d;
+                u2 -= Ae[r * 3 + 2] * d;
             }
         }
-        const Real* vi = A.pt_vinv + 8LL * gp;
-        const Real d0 = vi[0] * c3[0] + vi[1] * c3[1] + vi[2] * c3[2];
-        const Real d1 = vi[1] * c3[0] + vi[3] * c3[1] + vi[4] * c3[2];
-        const Real d2 = vi[2] * c3[0] + vi[4] * c3[1] + vi[5] * c3[2];
+        // dx = L^T u
+        const Real d0 = lt[0] * u0 + lt[1] * u1 + lt[3] * u2;
+        const Real d1 = lt[2] * u1 + lt[4] * u2;
+        const Real d2 = lt[5] * u2;
         Xt[4LL * gp + 0] = Xc[4LL * gp + 0] + (double)d0;
         Xt[4LL * gp + 1] = Xc[4LL * gp + 1] + (double)d1;
         Xt[4LL * gp + 2] = Xc[4LL * gp + 2] + (double)d2;
+        const Real* vg = A.pt_vg + 12LL * gp;
         sc += (double)d0 * (lambda * (double)d0 + (double)vg[6]) + (double)d1 * (lambda * (double)d1 + (double)vg[7]) +
               (double)d2 * (lambda * (double)d2 + (double)vg[8]);
     }
-    return block_sum(sc, s.red);
+    return sc;
 }
 
 template <class Real>
-__device__ void solve_window(const WinArgs<Real>& A, int w, SmemHead& s, double* S, double* bs, Real* camr,
-                             double* camd) {
+__device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char* smem) {
+    SmemHead& s = *c.s;
     const WinDesc D = A.win[w];
     const int m = 6 * D.nfc;
-    const int ld = A.ld;
+    const Dyn dl = dyn_layout(A.max_m, A.max_ncam, (int)sizeof(Real));
+    CamState* cams0 = reinterpret_cast<CamState*>(smem + dl.cams);
+    CamState* cams1 = cams0 + A.max_ncam;
+    Real* camr = reinterpret_cast<Real*>(smem + dl.camr);
+    Real* camr_tr = camr + 12 * A.max_ncam;
+    double* camd = reinterpret_cast<double*>(smem + dl.camd);
+    double* dcl = reinterpret_cast<double*>(smem + dl.dcl);
+    double* S = reinterpret_cast<double*>(smem + dl.S);
+    double* bs = reinterpret_cast<double*>(smem + dl.bs);
     WinStats* st = A.stats + w;
     double* trace = A.trace + (long long)w * A.trace_stride;
-    // initial state: both camera and point buffers hold the initial values
-    for (int c = threadIdx.x; c < D.ncam; c += blockDim.x) {
-        s.cams[0][c] = A.cam_init[D.cam0 + c];
-        s.cams[1][c] = A.cam_init[D.cam0 + c];
-        cam_real<Real>(s.cams[0][c], camr + 12 * c);
+    const bool mixed = sizeof(Real) == 4;
+
+    for (int k = threadIdx.x; k < D.ncam; k += blockDim.x) {
+        cams0[k] = A.cam_init[D.cam0 + k];
+        cams1[k] = A.cam_init[D.cam0 + k];
+        cam_real<Real>(cams0[k], camr + 12 * k);
+        cam_real<Real>(cams0[k], camr_tr + 12 * k);
     }
-    for (int p = threadIdx.x; p < D.npt; p += blockDim.x) {
+    for (int p = c.gt; p < D.npt; p += c.CT) {
         const long long gp = D.pt0 + p;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -514,105 +648,130 @@ __device__ void solve_window(const WinArgs<Real>& A, int w, SmemHead& s, double*
     }
     if (threadIdx.x == 0) s.cur = 0;
     __syncthreads();
-    build_cam_lists(A, D, s);
-    const bool mixed = sizeof(Real) == 4;
-    double chi = window_cost<Real, Real>(A, D, s, camr, A.x[0]);
+    build_lists(A, c, D);  // ends with a cluster barrier: points are initialized everywhere
+
+    double chi = cluster_reduce3<false>(c, cost_partial<Real, Real>(A, c, D, camr, A.x[0]), 0.0, 0.0).x;
     double chi0_fp64 = chi;
     if (mixed) {
-        cams_fp64<Real>(D, s, 0, camd);
-        chi0_fp64 = window_cost<double, Real>(A, D, s, camd, A.x[0]);
+        for (int k = threadIdx.x; k < D.ncam; k += blockDim.x) cam_real<double>(cams0[k], camd + 12 * k);
+        __syncthreads();
+        chi0_fp64 = cluster_reduce3<false>(c, cost_partial<double, Real>(A, c, D, camd, A.x[0]), 0.0, 0.0).x;
     }
     int iters_done = 0, acc = 0, rej = 0, term = NAV_BA_TERM_ITERATIONS;
     double lambda = 0.0, nu = 2.0;
-    if (threadIdx.x == 0) trace[0] = chi;
-    bool bad = !isfinite(chi);
+    if (c.rank == 0 && threadIdx.x == 0) trace[0] = chi;
+    const bool bad = !isfinite(chi);
     if (!bad && D.nfc + D.nfp == 0) term = NAV_BA_TERM_NOTHING_TO_DO;
     if (!bad && term == NAV_BA_TERM_ITERATIONS) {
-        Real* camr_tr = camr + 12 * kWinMaxCams;
         for (int it = 0; it < A.lm.iterations; ++it) {
-            window_linearize(A, D, s, camr);
+            const int cur = s.cur;
+            Real* cr_cur = cur == 0 ? camr : camr_tr;
+            const double mxp = linearize_points<Real>(A, c, D, cr_cur, A.x[cur]);
+            const double mxc = linearize_cameras<Real>(A, c, D, cr_cur, A.x[cur]);
+            const double maxdiag = cluster_reduce3<true>(c, fmax(mxp, mxc), 0.0, 0.0).x;
             if (it == 0) {
-                lambda = A.lm.initial_lambda > 0 ? A.lm.initial_lambda : A.lm.tau * s.maxdiag;
+                lambda = A.lm.initial_lambda > 0 ? A.lm.initial_lambda : A.lm.tau * maxdiag;
                 nu = 2.0;
             }
             double rho = 0.0;
             int q = 0;
             do {
                 const double lam_use = (A.debug && it == 0 && q == 0) ? A.debug_lambda : lambda;
-                for (int k = threadIdx.x; k < m * ld; k += blockDim.x) S[k] = 0.0;
-                __syncthreads();
-                window_schur(A, D, s, lam_use, S, bs);
+                if (c.rank == 0)
+                    for (int k = threadIdx.x; k < m * (m + 1) / 2; k += blockDim.x) S[k] = 0.0;
+                const int npd = schur_points<Real>(A, c, D, lam_use);
+                const double3 r0 = cluster_reduce3<false>(c, (double)npd, 0.0, 0.0);  // also orders S zeroing
+                schur_blocks<Real>(A, c, D, lam_use);
+                csync();
                 if (A.debug) {
-                    // reduced-system output of window 0: full symmetric S then b'
-                    for (int k = threadIdx.x; k < m * m; k += blockDim.x) {
-                        const int r = k / m, c = k % m;
-                        A.debug[k] = r >= c ? S[r * ld + c] : S[c * ld + r];
+                    if (c.rank == 0) {
+                        for (int k = threadIdx.x; k < m * m; k += blockDim.x) {
+                            const int r = k / m, cc = k % m;
+                            A.debug[k] = r >= cc ? S[tri(r, cc)] : S[tri(cc, r)];
+                        }
+                        for (int k = threadIdx.x; k < m; k += blockDim.x) A.debug[m * m + k] = bs[k];
                     }
-                    for (int k = threadIdx.x; k < m; k += blockDim.x) A.debug[m * m + k] = bs[k];
-                    __syncthreads();
+                    csync();
                     return;
                 }
-                const bool ok = smem_cholesky(S, m, ld, s);
-                if (ok) {
-                    smem_chol_solve(S, m, ld, bs);
-                } else {
-                    for (int k = threadIdx.x; k < m; k += blockDim.x) bs[k] = 0.0;
+                if (c.rank == 0) {
+                    bool okc = smem_cholesky(S, m, s) && r0.x == 0.0;
+                    if (okc) {
+                        smem_chol_solve(S, m, bs);
+                    } else {
+                        for (int k = threadIdx.x; k < m; k += blockDim.x) bs[k] = 0.0;
+                    }
                     __syncthreads();
+                    if (threadIdx.x == 0) s.ok = okc ? 1 : 0;
                 }
-                double scale = window_update(A, D, s, lambda, bs, camr_tr);
-                double chi_new = window_cost<Real, Real>(A, D, s, camr_tr, A.x[s.cur ^ 1]);
+                csync();
+                // every CTA takes the camera step from rank 0 and updates all cameras itself
+                for (int k = threadIdx.x; k < m; k += blockDim.x) dcl[k] = c.bs0[k];
+                __syncthreads();
+                const bool ok = c.s0->ok != 0;
+                CamState* ccur = cur == 0 ? cams0 : cams1;
+                CamState* ctr = cur == 0 ? cams1 : cams0;
+                Real* crt = cur == 0 ? camr_tr : camr;
+                double sc = 0.0;
+                for (int k = threadIdx.x; k < D.ncam; k += blockDim.x) {
+                    const int a = A.cam_free[D.cam0 + k];
+                    if (a >= 0) {
+                        se3_left_update(dcl + 6 * a, ccur[k], ctr[k]);
+                        if (c.rank == 0)
+#pragma unroll
+                            for (int r = 0; r < 6; ++r) sc += dcl[6 * a + r] * (lambda * dcl[6 * a + r] + s.U[a][21 + r]);
+                    }
+                    cam_real<Real>(ctr[k], crt + 12 * k);
+                }
+                __syncthreads();
+                sc += update_points<Real>(A, c, D, lambda, dcl, cur);
+                const double3 red = cluster_reduce3<false>(
+                    c, cost_partial<Real, Real>(A, c, D, crt, A.x[cur ^ 1]), sc, 0.0);
+                double chi_new = red.x;
+                double scale = red.y;
                 if (!ok) chi_new = DBL_MAX;
                 rho = chi - chi_new;
                 scale += 1e-3;
                 rho /= scale;
-                const bool accept = rho > 0 && isfinite(chi_new);
-                if (accept) {
+                if (rho > 0 && isfinite(chi_new)) {
                     double alpha = 1.0 - pow(2 * rho - 1, 3.0);
                     alpha = fmin(alpha, 2.0 / 3.0);
-                    const double sf = fmax(1.0 / 3.0, alpha);
-                    lambda *= sf;
+                    lambda *= fmax(1.0 / 3.0, alpha);
                     nu = 2.0;
                     chi = chi_new;
                     ++acc;
-                    __syncthreads();
-                    if (threadIdx.x == 0) s.cur ^= 1;
-                    // the accepted trial cameras become current: swap the FP32/FP64 copies
-                    for (int k = threadIdx.x; k < 12 * D.ncam; k += blockDim.x) {
-                        const Real t = camr[k];
-                        camr[k] = camr_tr[k];
-                        camr_tr[k] = t;
-                    }
-                    __syncthreads();
-                    // keep the non-current buffers equal for cameras (fixed ones never change)
+                    if (threadIdx.x == 0) s.cur = cur ^ 1;
                 } else {
                     lambda *= nu;
                     nu *= 2;
                     ++rej;
                 }
+                __syncthreads();
                 ++q;
             } while (rho < 0 && q < A.lm.max_trials);
             iters_done = it + 1;
-            if (threadIdx.x == 0) trace[it + 1] = chi;
+            if (c.rank == 0 && threadIdx.x == 0) trace[it + 1] = chi;
             if (q == A.lm.max_trials) { term = NAV_BA_TERM_TRIALS_EXHAUSTED; break; }
             if (rho == 0) { term = NAV_BA_TERM_ZERO_GAIN; break; }
             if (!isfinite(lambda)) { term = NAV_BA_TERM_LAMBDA_NONFINITE; break; }
         }
     }
     const int cur = s.cur;
+    CamState* cfin = cur == 0 ? cams0 : cams1;
     double chi_final = chi;
     if (mixed && !bad) {
-        // the mixed form reports FP64 costs of its initial and final states; its trace holds the
-        // FP32-residual costs the damping decisions used
-        cams_fp64<Real>(D, s, cur, camd);
-        chi_final = window_cost<double, Real>(A, D, s, camd, A.x[cur]);
+        for (int k = threadIdx.x; k < D.ncam; k += blockDim.x) cam_real<double>(cfin[k], camd + 12 * k);
+        __syncthreads();
+        chi_final = cluster_reduce3<false>(c, cost_partial<double, Real>(A, c, D, camd, A.x[cur]), 0.0, 0.0).x;
     }
-    for (int c = threadIdx.x; c < D.ncam; c += blockDim.x) A.cam_out[D.cam0 + c] = s.cams[cur][c];
-    for (int p = threadIdx.x; p < D.npt; p += blockDim.x) {
+    if (c.rank == 0)
+        for (int k = threadIdx.x; k < D.ncam; k += blockDim.x) A.cam_out[D.cam0 + k] = cfin[k];
+    for (int p = c.gt; p < D.npt; p += c.CT) {
         const long long gp = D.pt0 + p;
 #pragma unroll
         for (int k = 0; k < 4; ++k) A.pt_out[4 * gp + k] = A.x[cur][4 * gp + k];
     }
-    if (threadIdx.x == 0) {
+    if (c.rank == 0 && threadIdx.x == 0) {
         st->initial_cost = chi0_fp64;
         st->final_cost = chi_final;
         st->final_lambda = lambda;
@@ -622,39 +781,47 @@ __device__ void solve_window(const WinArgs<Real>& A, int w, SmemHead& s, double*
         st->termination = term;
         st->status = bad ? NAV_BA_ERR_NONFINITE_COST : NAV_BA_OK;
     }
-    __syncthreads();
+    csync();
 }
 
 template <class Real>
 __global__ void __launch_bounds__(sizeof(Real) == 8 ? 256 : 512) window_lm_kernel(WinArgs<Real> A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    SmemHead& s = *reinterpret_cast<SmemHead*>(smem_raw);
-    Real* camr = reinterpret_cast<Real*>(smem_raw + sizeof(SmemHead));  // [2][kWinMaxCams][12]
-    double* camd = reinterpret_cast<double*>(smem_raw + sizeof(SmemHead) + 2 * kWinMaxCams * 12 * sizeof(double));
-    double* S = camd + kWinMaxCams * 12;
-    double* bs = S + (size_t)A.max_m * A.ld;
+    cg::cluster_group cl = cg::this_cluster();
+    CC c;
+    c.rank = (int)cl.block_rank();
+    c.csize = (int)cl.num_blocks();
+    c.lane = threadIdx.x & 31;
+    c.wid = threadIdx.x >> 5;
+    c.nw = blockDim.x >> 5;
+    c.gt = c.rank * blockDim.x + threadIdx.x;
+    c.CT = c.csize * blockDim.x;
+    c.gw = c.rank * c.nw + c.wid;
+    c.CW = c.csize * c.nw;
+    c.s = reinterpret_cast<SmemHead*>(smem_raw);
+    c.s0 = cl.map_shared_rank(c.s, 0);
+    const Dyn dl = dyn_layout(A.max_m, A.max_ncam, (int)sizeof(Real));
+    c.S0 = cl.map_shared_rank(reinterpret_cast<double*>(smem_raw + dl.S), 0);
+    c.bs0 = cl.map_shared_rank(reinterpret_cast<double*>(smem_raw + dl.bs), 0);
+    if (threadIdx.x == 0) c.s->slot = 0;
+    __syncthreads();
     for (;;) {
-        if (threadIdx.x == 0) {
+        if (c.rank == 0 && threadIdx.x == 0) {
             const int k = atomicAdd(A.queue, 1);
-            s.win = k < A.n_win ? A.order[k] : -1;
+            c.s->win = k < A.n_win ? A.order[k] : -1;
         }
-        __syncthreads();
-        const int w = s.win;
-        __syncthreads();
+        csync();
+        const int w = c.s0->win;
+        csync();  // every rank has read rank 0's window index
         if (w < 0) break;
-        solve_window<Real>(A, w, s, S, bs, camr, camd);
+        solve_window<Real>(A, c, w, smem_raw);
         if (A.debug) break;
     }
-}
-
-size_t window_smem_bytes(int max_m) {
-    const int ld = max_m + 1;
-    return sizeof(SmemHead) + 3 * kWinMaxCams * 12 * sizeof(double) + (size_t)max_m * ld * sizeof(double) +
-           (size_t)max_m * sizeof(double);
+    csync();
 }
 
 template <class Real>
-cudaError_t launch_typed(PreparedBatch& pb, cudaStream_t stream, int threads, double debug_lambda) {
+cudaError_t launch_typed(PreparedBatch& pb, cudaStream_t stream, WindowLaunch shape, double debug_lambda) {
     WindowBatch& b = pb.dev;
     WinArgs<Real> A;
     A.win = b.d_win;
@@ -672,11 +839,11 @@ cudaError_t launch_typed(PreparedBatch& pb, cudaStream_t stream, int threads, do
     A.x[0] = b.d_x[0];
     A.x[1] = b.d_x[1];
     A.pt_vg = (Real*)b.d_pt_vg;
-    A.pt_vinv = (Real*)b.d_pt_vinv;
-    A.edge_jce = (Real*)b.d_edge_jce;
+    A.pt_lt = (Real*)b.d_pt_lt;
     A.edge_w = (Real*)b.d_edge_w;
-    A.edge_y = (Real*)b.d_edge_y;
+    A.edge_a = (Real*)b.d_edge_a;
     A.cam_list = b.d_cam_list;
+    A.pairs = b.d_pairs;
     A.cam_out = b.d_cam_out;
     A.pt_out = b.d_pt_out;
     A.trace = b.d_trace;
@@ -687,32 +854,48 @@ cudaError_t launch_typed(PreparedBatch& pb, cudaStream_t stream, int threads, do
     A.intr = pb.intr;
     A.lm = pb.lm;
     A.max_m = b.max_m;
-    A.ld = b.max_m + 1;
-    const size_t smem = window_smem_bytes(b.max_m);
+    A.max_ncam = std::max(1, b.max_ncam);
+    const int C = std::max(1, std::min(kMaxCluster, shape.cluster));
+    const int T = shape.threads;
+    if (T % 32 != 0 || T < 64 || T > (sizeof(Real) == 8 ? 256 : 512)) return cudaErrorInvalidConfiguration;
+    const size_t smem = dyn_layout(A.max_m, A.max_ncam, (int)sizeof(Real)).total;
     cudaError_t err = cudaFuncSetAttribute(window_lm_kernel<Real>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
-    int dev = 0, nsm = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, window_lm_kernel<Real>, threads, smem);
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.blockDim = dim3(T);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    int max_clusters = 0;
+    cfg.gridDim = dim3(C);
+    err = cudaOccupancyMaxActiveClusters(&max_clusters, window_lm_kernel<Real>, &cfg);
     if (err != cudaSuccess) return err;
-    if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    int grid = nsm * per_sm;
-    if (grid > b.n_queue) grid = b.n_queue;
-    if (debug_lambda >= 0) grid = 1;
+    if (max_clusters < 1) return cudaErrorInvalidConfiguration;
+    int clusters = std::min(max_clusters, b.n_queue);
+    if (debug_lambda >= 0) clusters = 1;
+    cfg.gridDim = dim3(clusters * C);
     err = cudaMemsetAsync(b.d_queue, 0, sizeof(int32_t), stream);
     if (err != cudaSuccess) return err;
-    window_lm_kernel<Real><<<grid, threads, smem, stream>>>(A);
-    return cudaGetLastError();
+    return cudaLaunchKernelEx(&cfg, window_lm_kernel<Real>, A);
 }
 
 }  // namespace
 
-cudaError_t window_batch_launch(PreparedBatch& pb, cudaStream_t stream, int precision, int threads,
+size_t window_smem_bytes(int max_m, int max_ncam, int precision) {
+    return dyn_layout(max_m, std::max(1, max_ncam), precision == NAV_BA_MIXED ? 4 : 8).total;
+}
+
+cudaError_t window_batch_launch(PreparedBatch& pb, cudaStream_t stream, int precision, WindowLaunch shape,
                                 double debug_lambda) {
     if (pb.dev.n_queue == 0) return cudaSuccess;
-    if (precision == NAV_BA_MIXED) return launch_typed<float>(pb, stream, threads, debug_lambda);
-    return launch_typed<double>(pb, stream, threads, debug_lambda);
+    if (precision == NAV_BA_MIXED) return launch_typed<float>(pb, stream, shape, debug_lambda);
+    return launch_typed<double>(pb, stream, shape, debug_lambda);
 }
 
 // ---- per-observation linearization (parity entry point) ---------------------------------
@@ -804,7 +987,7 @@ static size_t real_size(int precision) { return precision == NAV_BA_MIXED ? size
 void window_batch_free(WindowBatch& b) {
     void* ptrs[] = {b.d_win, b.d_order, b.d_queue, b.d_cam_init, b.d_cam_free, b.d_pt_init, b.d_pt_free,
                     b.d_pt_eoff, b.d_edge_cam, b.d_edge_pt, b.d_edge_uv, b.d_x[0], b.d_x[1], b.d_pt_vg,
-                    b.d_pt_vinv, b.d_edge_jce, b.d_edge_w, b.d_edge_y, b.d_cam_list, b.d_cam_out, b.d_pt_out,
+                    b.d_pt_lt, b.d_edge_w, b.d_edge_a, b.d_cam_list, b.d_pairs, b.d_cam_out, b.d_pt_out,
                     b.d_trace, b.d_stats, b.d_debug};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -815,12 +998,11 @@ cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int prec
                                 std::string* why) {
     window_batch_free(pb.dev);
     WindowBatch& b = pb.dev;
-    // windows that need the engine (others were resolved on the host)
     std::vector<int32_t> idx;
     for (size_t i = 0; i < pb.host.size(); ++i)
         if (pb.host_status[i] == NAV_BA_OK) idx.push_back((int32_t)i);
     pb.desc.assign(pb.host.size(), WinDesc{});
-    int64_t nc = 0, np = 0, ne = 0;
+    int64_t nc = 0, np = 0, ne = 0, npair = 0;
     int max_m = 0, max_nc = 0;
     for (size_t i = 0; i < pb.host.size(); ++i) {
         const HostWindow& h = pb.host[i];
@@ -829,7 +1011,8 @@ cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int prec
         d.pt0 = (int32_t)np; d.npt = h.npt;
         d.e0 = (int32_t)ne; d.ne = h.ne;
         d.nfc = h.nfc; d.nfp = h.nfp;
-        nc += h.ncam; np += h.npt; ne += h.ne;
+        d.pair0 = npair; d.npair = h.n_pairs;
+        nc += h.ncam; np += h.npt; ne += h.ne; npair += h.n_pairs;
         if (pb.host_status[i] == NAV_BA_OK) {
             max_m = std::max(max_m, 6 * h.nfc);
             max_nc = std::max(max_nc, h.ncam);
@@ -840,12 +1023,11 @@ cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int prec
         return cudaErrorInvalidValue;
     }
     b.n_win = (int32_t)pb.host.size();
-    b.ncam = nc; b.npt = np; b.ne = ne;
+    b.ncam = nc; b.npt = np; b.ne = ne; b.npair = npair;
     b.max_m = max_m;
     b.max_ncam = max_nc;
     b.precision = precision;
     b.trace_stride = trace_stride;
-    // host staging
     std::vector<CamState> cam(nc);
     std::vector<int32_t> cam_free(nc), pt_free(np), pt_eoff(np + 1), edge_cam(ne), edge_pt(ne);
     std::vector<double> pt(4 * np), uv(2 * ne);
@@ -862,11 +1044,13 @@ cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int prec
         std::copy(h.edge_uv.begin(), h.edge_uv.end(), uv.begin() + 2LL * d.e0);
     }
     pt_eoff[np] = (int32_t)ne;
-    // schedule: largest windows first (the most edges), engine windows only
+    // schedule: largest windows first (edges, pairs and a Cholesky-size term)
     std::vector<int32_t> order = idx;
     std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
-        const double wx = (double)pb.host[x].ne + 50.0 * pb.host[x].nfc * pb.host[x].nfc;
-        const double wy = (double)pb.host[y].ne + 50.0 * pb.host[y].nfc * pb.host[y].nfc;
+        const HostWindow& hx = pb.host[x];
+        const HostWindow& hy = pb.host[y];
+        const double wx = (double)hx.ne + (double)hx.n_pairs + 2.0 * hx.nfc * hx.nfc * hx.nfc;
+        const double wy = (double)hy.ne + (double)hy.n_pairs + 2.0 * hy.nfc * hy.nfc * hy.nfc;
         return wx > wy;
     });
     const size_t rs = real_size(precision);
@@ -891,11 +1075,11 @@ cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int prec
     alloc(&b.d_x[0], sizeof(double) * 4 * np);
     alloc(&b.d_x[1], sizeof(double) * 4 * np);
     alloc(&b.d_pt_vg, rs * 12 * np);
-    alloc(&b.d_pt_vinv, rs * 8 * np);
-    alloc(&b.d_edge_jce, rs * 16 * ne);
+    alloc(&b.d_pt_lt, rs * 12 * np);
     alloc(&b.d_edge_w, rs * 18 * ne);
-    alloc(&b.d_edge_y, rs * 18 * ne);
+    alloc(&b.d_edge_a, rs * 18 * ne);
     alloc(&b.d_cam_list, sizeof(int32_t) * ne);
+    alloc(&b.d_pairs, sizeof(uint32_t) * npair);
     alloc(&b.d_cam_out, sizeof(CamState) * nc);
     alloc(&b.d_pt_out, sizeof(double) * 4 * np);
     alloc(&b.d_trace, sizeof(double) * trace_stride * pb.desc.size());
