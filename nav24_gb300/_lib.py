@@ -147,6 +147,11 @@ class Context:
             out.append(b.result(r.status))
         return out
 
+    def batched_call(self, probs: list[abi.Problem], opt: abi.nav_ba_options) -> "BatchedCall":
+        """A nav_ba_solve_batched call with its C structs and host output buffers built once, so
+        that repeated calls time the C ABI alone."""
+        return BatchedCall(self, probs, opt)
+
     def prepare(self, prob: abi.Problem, opt: abi.nav_ba_options):
         self._prepared = prob  # keep the arrays alive
         p = prob.as_c()
@@ -206,3 +211,23 @@ class Context:
         c = C.c_double()
         self._check(self.L.nav_ba_cost(self.h, C.byref(p), C.byref(opt), C.byref(c)))
         return c.value
+
+
+class BatchedCall:
+    def __init__(self, ctx: Context, probs: list[abi.Problem], opt: abi.nav_ba_options):
+        self.ctx, self.probs, self.opt = ctx, probs, opt
+        n = len(probs)
+        self.n = n
+        self.cp = (abi.nav_ba_problem * n)(*[p.as_c() for p in probs])
+        self.bufs = [abi.ResultBuffers(p, opt.iterations) for p in probs]
+        self.cr = (abi.nav_ba_result * n)(*[b.c for b in self.bufs])
+
+    def __call__(self) -> int:
+        return self.ctx._check(self.ctx.L.nav_ba_solve_batched(self.ctx.h, self.cp, self.n, C.byref(self.opt), self.cr))
+
+    def results(self) -> list[abi.Result]:
+        out = []
+        for b, r in zip(self.bufs, self.cr):
+            b.c = r
+            out.append(b.result(r.status))
+        return out

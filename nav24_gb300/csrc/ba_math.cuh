@@ -184,16 +184,18 @@ template <class Real>
 NAVBA_HD void project(const Intr& in, const Real* Xc, Real* uv, Real* J) {
     const Real x = Xc[0], y = Xc[1], z = Xc[2];
     const Real fx = (Real)in.fx, fy = (Real)in.fy, cx = (Real)in.cx, cy = (Real)in.cy;
+    const Real iz = Real(1) / z;  // one division per edge; the rest are products
     if (in.model == 0) {
-        uv[0] = fx * x / z + cx;
-        uv[1] = fy * y / z + cy;
+        const Real xn = x * iz, yn = y * iz;
+        uv[0] = fx * xn + cx;
+        uv[1] = fy * yn + cy;
         if (J) {
-            J[0] = fx / z; J[1] = Real(0); J[2] = -fx * x / (z * z);
-            J[3] = Real(0); J[4] = fy / z; J[5] = -fy * y / (z * z);
+            J[0] = fx * iz; J[1] = Real(0); J[2] = -fx * xn * iz;
+            J[3] = Real(0); J[4] = fy * iz; J[5] = -fy * yn * iz;
         }
     } else {
         const Real k1 = (Real)in.k1, k2 = (Real)in.k2;
-        const Real xn = x / z, yn = y / z;
+        const Real xn = x * iz, yn = y * iz;
         const Real r2 = xn * xn + yn * yn;
         const Real d = Real(1) + k1 * r2 + k2 * r2 * r2;
         uv[0] = fx * d * xn + cx;
@@ -202,7 +204,6 @@ NAVBA_HD void project(const Intr& in, const Real* Xc, Real* uv, Real* J) {
             const Real c = k1 + Real(2) * k2 * r2;
             const Real a00 = fx * (d + Real(2) * xn * xn * c), a01 = fx * Real(2) * xn * yn * c;
             const Real a10 = fy * Real(2) * xn * yn * c, a11 = fy * (d + Real(2) * yn * yn * c);
-            const Real iz = Real(1) / z;
             J[0] = a00 * iz; J[1] = a01 * iz; J[2] = -(a00 * xn + a01 * yn) * iz;
             J[3] = a10 * iz; J[4] = a11 * iz; J[5] = -(a10 * xn + a11 * yn) * iz;
         }

@@ -62,14 +62,15 @@ struct WindowBatch {
     int32_t* d_pt_free = nullptr;
     int32_t* d_pt_eoff = nullptr;  // [npt + 1] global edge offsets
     int32_t* d_edge_cam = nullptr; // window-local camera of each edge
+    int32_t* d_edge_fc = nullptr;  // free index of each edge's camera, or -1
     int32_t* d_edge_pt = nullptr;  // window-local point of each edge
     double* d_edge_uv = nullptr;   // [ne][2]
     // device scratch
     double* d_x[2] = {nullptr, nullptr};  // [npt][4] current / trial points
     void* d_pt_vg = nullptr;       // [npt][12] Real: V (6 packed) g (3)
     void* d_pt_lt = nullptr;       // [npt][12] Real: Linv (6 packed lower) t = Linv g (3)
-    void* d_edge_w = nullptr;      // [ne][18]  Real: W = w Jc^T Jp
-    void* d_edge_a = nullptr;      // [ne][18]  Real: A = W Linv^T
+    void* d_edge_w = nullptr;      // [ne][20 f32 | 18 f64] Real: W = w Jc^T Jp
+    void* d_edge_a = nullptr;      // [ne][20 f32 | 18 f64] Real: A = W Linv^T
     int32_t* d_cam_list = nullptr; // [ne] camera-major edge list (free cameras only)
     uint32_t* d_pairs = nullptr;   // [npair] Schur pairs (edge i << 16 | edge j), window-local
     // device outputs
@@ -78,6 +79,8 @@ struct WindowBatch {
     double* d_trace = nullptr;     // [n_win][trace_stride]
     WinStats* d_stats = nullptr;
     double* d_debug = nullptr;     // reduced-system debug output (optional)
+    unsigned long long* d_phase = nullptr;  // per-phase cycle totals (NAVBA_PHASE_TIMING=1)
+    size_t cap[32] = {};      // allocated bytes of each buffer (buffers are reused across calls)
     size_t bytes = 0;
     int64_t h2d_bytes = 0;    // bytes uploaded by window_batch_upload
 };
@@ -86,6 +89,14 @@ struct WindowBatch {
 struct WindowLaunch {
     int32_t cluster = 4;      // CTAs cooperating on one window (1, 2, 4 or 8)
     int32_t threads = 256;    // threads per CTA
+};
+
+// Pinned host buffers reused across calls (inputs staged for upload, outputs for download).
+struct HostStaging {
+    void* buf[16] = {};
+    size_t cap[16] = {};
+    void* get(int id, size_t bytes);  // grows buffer `id` to at least `bytes`; null on failure
+    void release();
 };
 
 // Host side of a prepared batch: the built windows and their device copy.
@@ -98,9 +109,10 @@ struct PreparedBatch {
     Intr intr{};
 };
 
-// Allocate and upload (stream-ordered, synchronous on return).  Returns a CUDA error or 0.
+// Allocate (reusing pb.dev's buffers when large enough) and upload through pinned staging
+// (synchronous on return).  Returns a CUDA error or 0.
 cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int precision,
-                                int trace_stride, std::string* why);
+                                int trace_stride, HostStaging& stg, std::string* why);
 void window_batch_free(WindowBatch& b);
 
 // Launch the persistent window kernel over all windows of the batch.
@@ -108,6 +120,11 @@ void window_batch_free(WindowBatch& b);
 // and writes [S (m*m) | b (m)] to d_debug.
 cudaError_t window_batch_launch(PreparedBatch& pb, cudaStream_t stream, int precision,
                                 WindowLaunch shape, double debug_lambda);
+
+// Print the per-phase cycle breakdown of the last launch to stderr (NAVBA_PHASE_TIMING=1).
+constexpr int kWinPhases = 10;
+struct WindowLaunch;
+void window_phase_report(const PreparedBatch& pb, const WindowLaunch& shape, int precision);
 
 // Shared memory one CTA of the window kernel needs for a batch (bytes).
 size_t window_smem_bytes(int max_m, int max_ncam, int precision);

@@ -3,6 +3,8 @@
 // Replaces nav24's GraphOptim::solve (core/backEnd/BE_GraphOptim.cpp:31-77): graph build
 // (structure.cpp), LM on the device (window_engine.cu), write-back of poses and points.
 #include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <thread>
@@ -23,6 +25,8 @@ struct nav_ba_ctx {
     bool has_prepared = false;
     WindowLaunch shape[2];        // per precision (autotuned on nav_ba_prepare_batched)
     bool tuned[2] = {false, false};
+    WindowBatch solve_dev;        // device buffers of nav_ba_solve / _batched, reused across calls
+    HostStaging stg;              // pinned staging reused across calls
 };
 
 namespace {
@@ -126,6 +130,10 @@ cudaError_t autotune(nav_ba_ctx* ctx, PreparedBatch& pb, int precision) {
     }
     ctx->shape[precision] = best_shape;
     ctx->tuned[precision] = true;
+    const char* env = getenv("NAVBA_VERBOSE");
+    if (env && env[0] == '1')
+        fprintf(stderr, "[navba autotune] precision=%d cluster=%d threads=%d %.3f ms\n", precision, best_shape.cluster,
+                best_shape.threads, best);
     return cudaSuccess;
 }
 
@@ -178,10 +186,11 @@ nav_ba_status build_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, c
 nav_ba_status download_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, PreparedBatch& pb,
                              nav_ba_result* results) {
     WindowBatch& b = pb.dev;
-    std::vector<CamState> cams(b.ncam);
-    std::vector<double> pts(4 * b.npt);
-    std::vector<double> trace((size_t)b.trace_stride * n);
-    std::vector<WinStats> stats(n);
+    CamState* cams = (CamState*)ctx->stg.get(10, sizeof(CamState) * b.ncam);
+    double* pts = (double*)ctx->stg.get(11, sizeof(double) * 4 * b.npt);
+    double* trace = (double*)ctx->stg.get(12, sizeof(double) * (size_t)b.trace_stride * n);
+    WinStats* stats = (WinStats*)ctx->stg.get(13, sizeof(WinStats) * n);
+    if (!cams || !pts || !trace || !stats) return set_err(ctx, NAV_BA_ERR_OUT_OF_MEMORY, "pinned host allocation failed");
     cudaError_t e = cudaSuccess;
     int64_t d2h = 0;
     auto dn = [&](void* dst, const void* src, size_t bytes) {
@@ -189,14 +198,14 @@ nav_ba_status download_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n
         e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream);
         d2h += (int64_t)bytes;
     };
-    dn(cams.data(), b.d_cam_out, sizeof(CamState) * b.ncam);
-    dn(pts.data(), b.d_pt_out, sizeof(double) * 4 * b.npt);
-    dn(trace.data(), b.d_trace, sizeof(double) * trace.size());
-    dn(stats.data(), b.d_stats, sizeof(WinStats) * n);
+    dn(cams, b.d_cam_out, sizeof(CamState) * b.ncam);
+    dn(pts, b.d_pt_out, sizeof(double) * 4 * b.npt);
+    dn(trace, b.d_trace, sizeof(double) * (size_t)b.trace_stride * n);
+    dn(stats, b.d_stats, sizeof(WinStats) * n);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_status(ctx, e, "download");
-    nav_ba_status overall = NAV_BA_OK;
-    for (int i = 0; i < n; ++i) {
+    std::vector<int32_t> st_out(n, NAV_BA_OK);
+    auto one = [&](int i) {
         nav_ba_result* r = &results[i];
         const nav_ba_problem& p = probs[i];
         const HostWindow& h = pb.host[i];
@@ -211,7 +220,7 @@ nav_ba_status download_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n
             write_passthrough(p, r, false);
             r->termination = NAV_BA_TERM_NOTHING_TO_DO;
             r->status = NAV_BA_EMPTY;
-            continue;
+            return;
         }
         const WinStats& s = stats[i];
         r->status = s.status;
@@ -224,8 +233,8 @@ nav_ba_status download_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n
         r->termination = s.termination;
         r->edge_iterations = (int64_t)h.ne * s.iterations_done;
         if (s.status != NAV_BA_OK) {
-            overall = (nav_ba_status)s.status;
-            continue;
+            st_out[i] = s.status;
+            return;
         }
         if (r->cam_pose_out)
             for (int c = 0; c < p.n_cams; ++c) pose12_from_cam(cams[d.cam0 + c], r->cam_pose_out + 12LL * c);
@@ -235,8 +244,21 @@ nav_ba_status download_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n
         if (r->intrinsics_out) std::memcpy(r->intrinsics_out, p.intrinsics, sizeof(double) * 8);
         if (r->cost_trace)
             for (int k = 0; k <= s.iterations_done; ++k) r->cost_trace[k] = trace[(size_t)i * b.trace_stride + k];
+    };
+    const int nth = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), n / 8));
+    if (nth <= 1) {
+        for (int i = 0; i < n; ++i) one(i);
+    } else {
+        std::vector<std::thread> th;
+        for (int t = 0; t < nth; ++t)
+            th.emplace_back([&, t] {
+                for (int i = (int)((long long)n * t / nth); i < (int)((long long)n * (t + 1) / nth); ++i) one(i);
+            });
+        for (auto& x : th) x.join();
     }
-    return overall;
+    for (int i = 0; i < n; ++i)
+        if (st_out[i] != NAV_BA_OK) return (nav_ba_status)st_out[i];
+    return NAV_BA_OK;
 }
 
 nav_ba_status solve_impl(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, const nav_ba_options* o,
@@ -248,27 +270,26 @@ nav_ba_status solve_impl(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, co
     nav_ba_status st = build_batch(ctx, probs, n, o, pb);
     if (st != NAV_BA_OK) return st;
     std::string why;
-    cudaError_t e = window_batch_upload(pb, ctx->stream, o->precision, o->iterations + 1, &why);
-    if (e != cudaSuccess) {
-        window_batch_free(pb.dev);
-        return cuda_status(ctx, e, "upload");
-    }
+    std::swap(pb.dev, ctx->solve_dev);  // reuse the context's device buffers
+    struct SwapBack {
+        PreparedBatch& pb;
+        nav_ba_ctx* ctx;
+        ~SwapBack() { std::swap(pb.dev, ctx->solve_dev); }
+    } swap_back{pb, ctx};
+    cudaError_t e = window_batch_upload(pb, ctx->stream, o->precision, o->iterations + 1, ctx->stg, &why);
+    if (e != cudaSuccess) return cuda_status(ctx, e, "upload");
     const double t_setup = ms_since(t0);
     cudaEventRecord(ctx->ev0, ctx->stream);
     e = window_batch_launch(pb, ctx->stream, o->precision, ctx->shape[o->precision], -1.0);
     cudaEventRecord(ctx->ev1, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) {
-        window_batch_free(pb.dev);
-        return cuda_status(ctx, e, "window kernel");
-    }
+    if (e != cudaSuccess) return cuda_status(ctx, e, "window kernel");
     float t_solve = 0.f;
     cudaEventElapsedTime(&t_solve, ctx->ev0, ctx->ev1);
     const auto t1 = std::chrono::steady_clock::now();
     std::vector<nav_ba_result> tmp(results, results + n);  // outputs untouched on error
     for (auto& r : tmp) clear_stats(&r);
     st = download_batch(ctx, probs, n, pb, tmp.data());
-    window_batch_free(pb.dev);
     if (st != NAV_BA_OK && st != NAV_BA_EMPTY) return set_err(ctx, st, "a problem has a non-finite initial cost");
     const double t_down = ms_since(t1);
     for (int i = 0; i < n; ++i) {
@@ -323,6 +344,8 @@ void nav_ba_destroy(nav_ba_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     window_batch_free(ctx->prepared.dev);
+    window_batch_free(ctx->solve_dev);
+    ctx->stg.release();
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -356,23 +379,18 @@ nav_ba_status nav_ba_prepare_batched(nav_ba_ctx* ctx, const nav_ba_problem* p, i
     if (!ctx) return NAV_BA_ERR_ARGUMENT;
     if (!p || !o || n < 0) return set_err(ctx, NAV_BA_ERR_ARGUMENT, "NULL argument");
     cudaSetDevice(ctx->device);
-    window_batch_free(ctx->prepared.dev);
     ctx->has_prepared = false;
     PreparedBatch& pb = ctx->prepared;
-    pb = PreparedBatch();
+    pb.host.clear();
+    pb.host_status.clear();
+    pb.desc.clear();
     nav_ba_status st = build_batch(ctx, p, n, o, pb);
     if (st != NAV_BA_OK) return st;
     std::string why;
-    cudaError_t e = window_batch_upload(pb, ctx->stream, o->precision, o->iterations + 1, &why);
-    if (e != cudaSuccess) {
-        window_batch_free(pb.dev);
-        return cuda_status(ctx, e, "upload");
-    }
+    cudaError_t e = window_batch_upload(pb, ctx->stream, o->precision, o->iterations + 1, ctx->stg, &why);
+    if (e != cudaSuccess) return cuda_status(ctx, e, "upload");
     e = autotune(ctx, pb, o->precision);
-    if (e != cudaSuccess) {
-        window_batch_free(pb.dev);
-        return cuda_status(ctx, e, "autotune");
-    }
+    if (e != cudaSuccess) return cuda_status(ctx, e, "autotune");
     ctx->prepared_problems.assign(p, p + n);
     ctx->prepared_opts = *o;
     ctx->has_prepared = true;
@@ -409,6 +427,7 @@ nav_ba_status nav_ba_run(nav_ba_ctx* ctx, const nav_ba_options* o, nav_ba_result
     cudaEventRecord(ctx->ev1, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_status(ctx, e, "window kernel");
+    window_phase_report(ctx->prepared, ctx->shape[po.precision], po.precision);
     if (stats) {
         float t = 0.f;
         cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1);
@@ -487,14 +506,15 @@ nav_ba_status nav_ba_reduced_system(nav_ba_ctx* ctx, const nav_ba_problem* p, co
         return NAV_BA_OK;
     }
     std::string why;
-    cudaError_t e = window_batch_upload(pb, ctx->stream, o1.precision, 2, &why);
+    std::swap(pb.dev, ctx->solve_dev);
+    cudaError_t e = window_batch_upload(pb, ctx->stream, o1.precision, 2, ctx->stg, &why);
     if (e == cudaSuccess) e = window_batch_launch(pb, ctx->stream, o1.precision, ctx->shape[o1.precision], lambda);
     const int m = 6 * h.nfc;
     std::vector<double> out((size_t)m * m + m);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(out.data(), pb.dev.d_debug, sizeof(double) * out.size(), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-    window_batch_free(pb.dev);
+    std::swap(pb.dev, ctx->solve_dev);
     if (e != cudaSuccess) return cuda_status(ctx, e, "reduced system");
     std::memcpy(s, out.data(), sizeof(double) * m * m);
     std::memcpy(b, out.data() + (size_t)m * m, sizeof(double) * m);

@@ -27,6 +27,9 @@
 // Schur products in FP32; S, its Cholesky, the states, the SE(3) update and cost sums in FP64).
 #include <algorithm>
 #include <cfloat>
+#include <cstdio>
+#include <cstdlib>
+#include <thread>
 
 #include <cooperative_groups.h>
 
@@ -56,7 +59,7 @@ struct SmemHead {
 
 // Offsets of the dynamic part of shared memory (after SmemHead), shared by host and device.
 struct Dyn {
-    size_t cams, camr, camd, dcl, S, bs, total;
+    size_t cams, camr, camd, dcl, S, bs, rinv, total;
 };
 
 NAVBA_HD size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -70,6 +73,7 @@ NAVBA_HD Dyn dyn_layout(int max_m, int max_ncam, int real_size) {
     d.dcl = o;  o = align16(o + sizeof(double) * max_m);
     d.S = o;    o = align16(o + sizeof(double) * ((size_t)max_m * (max_m + 1) / 2));
     d.bs = o;   o = align16(o + sizeof(double) * max_m);
+    d.rinv = o; o = align16(o + sizeof(double) * max_m);
     d.total = o;
     return d;
 }
@@ -86,6 +90,7 @@ struct WinArgs {
     const int32_t* pt_free;
     const int32_t* pt_eoff;
     const int32_t* edge_cam;
+    const int32_t* edge_fc;   // free index of each edge's camera, or -1
     const int32_t* edge_pt;
     const double* edge_uv;
     double* x[2];
@@ -105,6 +110,7 @@ struct WinArgs {
     Intr intr;
     LmOptions lm;
     int32_t max_m, max_ncam;
+    unsigned long long* phase;  // optional per-phase SM-cycle totals (rank 0 view), or null
 };
 
 NAVBA_HD int tri(int r, int c) { return r * (r + 1) / 2 + c; }  // packed lower index, c <= r
@@ -125,7 +131,7 @@ __device__ __forceinline__ void csync() { cg::this_cluster().sync(); }
 
 // Decode lower-triangle block index blk = a (a + 1) / 2 + b, b <= a.
 __device__ __forceinline__ void decode_block(int blk, int& a, int& b) {
-    a = (int)((sqrt(8.0 * blk + 1.0) - 1.0) * 0.5);
+    a = (int)((sqrtf(8.0f * (float)blk + 1.0f) - 1.0f) * 0.5f);
     while ((a + 1) * (a + 2) / 2 <= blk) ++a;
     while (a * (a + 1) / 2 > blk) --a;
     b = blk - a * (a + 1) / 2;
@@ -188,6 +194,79 @@ __device__ __forceinline__ void cam_real(const CamState& c, Real* o) {
     o[10] = (Real)c.t[1];
     o[11] = (Real)c.t[2];
 }
+
+// Per-edge 18-value records (W, A) and per-point 12-value records (V|g, L|t), moved with
+// 16-byte vector accesses: FP32 records are padded to 20 floats (80 B), FP64 ones are 144 B.
+template <class Real>
+struct Rec;
+
+template <>
+struct Rec<float> {
+    static constexpr int kEdge = 20;
+    static __device__ __forceinline__ void load18(const float* p, float* v) {
+        const float4* q = reinterpret_cast<const float4*>(p);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float4 t = q[k];
+            v[4 * k] = t.x; v[4 * k + 1] = t.y; v[4 * k + 2] = t.z; v[4 * k + 3] = t.w;
+        }
+        const float2 t = reinterpret_cast<const float2*>(p)[8];
+        v[16] = t.x;
+        v[17] = t.y;
+    }
+    static __device__ __forceinline__ void store18(float* p, const float* v) {
+        float4* q = reinterpret_cast<float4*>(p);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) q[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+        reinterpret_cast<float2*>(p)[8] = make_float2(v[16], v[17]);
+    }
+    static __device__ __forceinline__ void load12(const float* p, float* v) {
+        const float4* q = reinterpret_cast<const float4*>(p);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float4 t = q[k];
+            v[4 * k] = t.x; v[4 * k + 1] = t.y; v[4 * k + 2] = t.z; v[4 * k + 3] = t.w;
+        }
+    }
+    static __device__ __forceinline__ void store12(float* p, const float* v) {
+        float4* q = reinterpret_cast<float4*>(p);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) q[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+    }
+};
+
+template <>
+struct Rec<double> {
+    static constexpr int kEdge = 18;
+    static __device__ __forceinline__ void load18(const double* p, double* v) {
+        const double2* q = reinterpret_cast<const double2*>(p);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            const double2 t = q[k];
+            v[2 * k] = t.x;
+            v[2 * k + 1] = t.y;
+        }
+    }
+    static __device__ __forceinline__ void store18(double* p, const double* v) {
+        double2* q = reinterpret_cast<double2*>(p);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) q[k] = make_double2(v[2 * k], v[2 * k + 1]);
+    }
+    static __device__ __forceinline__ void load12(const double* p, double* v) {
+        const double2* q = reinterpret_cast<const double2*>(p);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const double2 t = q[k];
+            v[2 * k] = t.x;
+            v[2 * k + 1] = t.y;
+        }
+    }
+    static __device__ __forceinline__ void store12(double* p, const double* v) {
+        double2* q = reinterpret_cast<double2*>(p);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) q[k] = make_double2(v[2 * k], v[2 * k + 1]);
+    }
+};
 
 // Cluster-split robust chi2 of the window for cameras `camc` (12 values per camera, precision
 // Cost) and points X; returns this thread's partial sum.
@@ -346,20 +425,17 @@ __device__ double linearize_points(const WinArgs<Real>& A, const CC& c, const Wi
             g[0] += jp[0] * we0 + jp[3] * we1;
             g[1] += jp[1] * we0 + jp[4] * we1;
             g[2] += jp[2] * we0 + jp[5] * we1;
-            if (A.cam_free[D.cam0 + cam] >= 0) {
-                Real* W = A.edge_w + 18LL * e;
+            if (A.edge_fc[e] >= 0) {
+                Real W[18];
 #pragma unroll
                 for (int r = 0; r < 6; ++r)
 #pragma unroll
                     for (int k = 0; k < 3; ++k) W[r * 3 + k] = w * (L.jc[r] * jp[k] + L.jc[6 + r] * jp[3 + k]);
+                Rec<Real>::store18(A.edge_w + (long long)Rec<Real>::kEdge * e, W);
             }
         }
-        Real* vg = A.pt_vg + 12LL * gp;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) vg[k] = V[k];
-        vg[6] = g[0];
-        vg[7] = g[1];
-        vg[8] = g[2];
+        const Real vgv[12] = {V[0], V[1], V[2], V[3], V[4], V[5], g[0], g[1], g[2], Real(0), Real(0), Real(0)};
+        Rec<Real>::store12(A.pt_vg + 12LL * gp, vgv);
         mx = fmax(mx, fmax(fabs((double)V[0]), fmax(fabs((double)V[3]), fabs((double)V[5]))));
     }
     return mx;
@@ -418,7 +494,8 @@ __device__ int schur_points(const WinArgs<Real>& A, const CC& c, const WinDesc& 
     for (int p = c.gt; p < D.npt; p += c.CT) {
         const int gp = D.pt0 + p;
         if (A.pt_free[gp] < 0) continue;
-        const Real* vg = A.pt_vg + 12LL * gp;
+        Real vg[12];
+        Rec<Real>::load12(A.pt_vg + 12LL * gp, vg);
         const Real v00 = vg[0] + lam, v01 = vg[1], v02 = vg[2], v11 = vg[3] + lam, v12 = vg[4], v22 = vg[5] + lam;
         const Real r00 = sqrt(v00);
         const Real r10 = v01 / r00, r20 = v02 / r00;
@@ -432,16 +509,14 @@ __device__ int schur_points(const WinArgs<Real>& A, const CC& c, const WinDesc& 
         const Real l10 = -r10 * l00 * l11;
         const Real l21 = -r21 * l11 * l22;
         const Real l20 = -(r20 * l00 + r21 * l10) * l22;
-        Real* lt = A.pt_lt + 12LL * gp;
-        lt[0] = l00; lt[1] = l10; lt[2] = l11; lt[3] = l20; lt[4] = l21; lt[5] = l22;
-        lt[6] = l00 * vg[6];
-        lt[7] = l10 * vg[6] + l11 * vg[7];
-        lt[8] = l20 * vg[6] + l21 * vg[7] + l22 * vg[8];
+        const Real ltv[12] = {l00, l10, l11, l20, l21, l22, l00 * vg[6], l10 * vg[6] + l11 * vg[7],
+                              l20 * vg[6] + l21 * vg[7] + l22 * vg[8], Real(0), Real(0), Real(0)};
+        Rec<Real>::store12(A.pt_lt + 12LL * gp, ltv);
         const int e1 = A.pt_eoff[gp + 1];
         for (int e = A.pt_eoff[gp]; e < e1; ++e) {
-            if (A.cam_free[D.cam0 + A.edge_cam[e]] < 0) continue;
-            const Real* W = A.edge_w + 18LL * e;
-            Real* Ae = A.edge_a + 18LL * e;
+            if (A.edge_fc[e] < 0) continue;
+            Real W[18], Ae[18];
+            Rec<Real>::load18(A.edge_w + (long long)Rec<Real>::kEdge * e, W);
 #pragma unroll
             for (int r = 0; r < 6; ++r) {
                 const Real w0 = W[r * 3 + 0], w1 = W[r * 3 + 1], w2 = W[r * 3 + 2];
@@ -449,6 +524,7 @@ __device__ int schur_points(const WinArgs<Real>& A, const CC& c, const WinDesc& 
                 Ae[r * 3 + 1] = w0 * l10 + w1 * l11;
                 Ae[r * 3 + 2] = w0 * l20 + w1 * l21 + w2 * l22;
             }
+            Rec<Real>::store18(A.edge_a + (long long)Rec<Real>::kEdge * e, Ae);
         }
     }
     return bad;
@@ -469,16 +545,14 @@ __device__ void schur_blocks(const WinArgs<Real>& A, const CC& c, const WinDesc&
         for (int k = 0; k < 36; ++k) acc[k] = Real(0);
 #pragma unroll
         for (int k = 0; k < 6; ++k) accb[k] = Real(0);
+        uint32_t pr_next = c.lane < n ? A.pairs[base + c.lane] : 0u;
         for (int k = c.lane; k < n; k += 32) {
-            const uint32_t pr = A.pairs[base + k];
+            const uint32_t pr = pr_next;
+            pr_next = k + 32 < n ? A.pairs[base + k + 32] : 0u;  // prefetch the next pair index
             const int ei = D.e0 + (int)(pr >> 16), ej = D.e0 + (int)(pr & 0xffffu);
-            const Real* Ai = A.edge_a + 18LL * ei;
-            const Real* Aj = A.edge_a + 18LL * ej;
             Real ai[18], aj[18];
-#pragma unroll
-            for (int q = 0; q < 18; ++q) ai[q] = Ai[q];
-#pragma unroll
-            for (int q = 0; q < 18; ++q) aj[q] = Aj[q];
+            Rec<Real>::load18(A.edge_a + (long long)Rec<Real>::kEdge * ei, ai);
+            Rec<Real>::load18(A.edge_a + (long long)Rec<Real>::kEdge * ej, aj);
 #pragma unroll
             for (int r = 0; r < 6; ++r)
 #pragma unroll
@@ -521,8 +595,10 @@ __device__ void schur_blocks(const WinArgs<Real>& A, const CC& c, const WinDesc&
     }
 }
 
-// In-place Cholesky (LL^T) of packed lower S (m x m) in this CTA's shared memory, FP64.
-__device__ bool smem_cholesky(double* S, int m, SmemHead& s) {
+// In-place Cholesky (LL^T) of packed lower S (m x m) in this CTA's shared memory, FP64; rinv
+// receives 1/L_jj.  One reciprocal square root per column (FP64 divides and square roots are
+// long instruction sequences on GB300's FP64 pipe, so the column is scaled by a product).
+__device__ bool smem_cholesky(double* S, double* rinv, int m, SmemHead& s) {
     if (threadIdx.x == 0) s.ok = 1;
     __syncthreads();
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -532,13 +608,16 @@ __device__ bool smem_cholesky(double* S, int m, SmemHead& s) {
             if (!(d > 0.0) || !isfinite(d)) {
                 s.ok = 0;
                 S[tri(j, j)] = 1.0;
+                rinv[j] = 1.0;
             } else {
-                S[tri(j, j)] = sqrt(d);
+                const double r = rsqrt(d);
+                S[tri(j, j)] = d * r;
+                rinv[j] = r;
             }
         }
         __syncthreads();
-        const double piv = S[tri(j, j)];
-        for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) S[tri(i, j)] = S[tri(i, j)] / piv;
+        const double ri = rinv[j];
+        for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) S[tri(i, j)] *= ri;
         __syncthreads();
         for (int i = j + 1 + wid; i < m; i += nw) {
             const double lij = S[tri(i, j)];
@@ -550,29 +629,33 @@ __device__ bool smem_cholesky(double* S, int m, SmemHead& s) {
     return s.ok != 0;
 }
 
-// Solve L L^T x = b in place (warp 0), FP64, packed L.
-__device__ void smem_chol_solve(const double* L, int m, double* x) {
-    if (threadIdx.x < 32) {
-        const int lane = threadIdx.x;
-        for (int i = 0; i < m; ++i) {
-            double sum = 0.0;
-            const double* Li = L + tri(i, 0);
-            for (int k = lane; k < i; k += 32) sum += Li[k] * x[k];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
-            if (lane == 0) x[i] = (x[i] - sum) / Li[i];
-            __syncwarp();
-        }
-        for (int i = m - 1; i >= 0; --i) {
-            double sum = 0.0;
-            for (int k = i + 1 + lane; k < m; k += 32) sum += L[tri(k, i)] * x[k];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
-            if (lane == 0) x[i] = (x[i] - sum) / L[tri(i, i)];
-            __syncwarp();
-        }
-    }
+// Solve L L^T x = b in place, FP64, packed L, rinv = 1/diag(L); column-oriented substitution
+// with one barrier per column (the owner of the next row finalizes it).
+__device__ void smem_chol_solve(const double* L, const double* rinv, int m, double* x) {
+    if (m == 0) return;
+    if (threadIdx.x == 0) x[0] *= rinv[0];
     __syncthreads();
+    for (int j = 0; j < m - 1; ++j) {
+        const double xj = x[j];
+        for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) {
+            double v = x[i] - L[tri(i, j)] * xj;
+            if (i == j + 1) v *= rinv[i];
+            x[i] = v;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) x[m - 1] *= rinv[m - 1];
+    __syncthreads();
+    for (int j = m - 1; j > 0; --j) {
+        const double xj = x[j];
+        const double* Lj = L + tri(j, 0);
+        for (int i = threadIdx.x; i < j; i += blockDim.x) {
+            double v = x[i] - Lj[i] * xj;
+            if (i == j - 1) v *= rinv[i];
+            x[i] = v;
+        }
+        __syncthreads();
+    }
 }
 
 // Trial points dx_p = L^T (t_p - sum A_e^T dx_c); returns this thread's dx^T(lambda dx + g) part.
@@ -585,13 +668,15 @@ __device__ double update_points(const WinArgs<Real>& A, const CC& c, const WinDe
     for (int p = c.gt; p < D.npt; p += c.CT) {
         const int gp = D.pt0 + p;
         if (A.pt_free[gp] < 0) continue;
-        const Real* lt = A.pt_lt + 12LL * gp;
+        Real lt[12];
+        Rec<Real>::load12(A.pt_lt + 12LL * gp, lt);
         Real u0 = lt[6], u1 = lt[7], u2 = lt[8];
         const int e1 = A.pt_eoff[gp + 1];
         for (int e = A.pt_eoff[gp]; e < e1; ++e) {
-            const int a = A.cam_free[D.cam0 + A.edge_cam[e]];
+            const int a = A.edge_fc[e];
             if (a < 0) continue;
-            const Real* Ae = A.edge_a + 18LL * e;
+            Real Ae[18];
+            Rec<Real>::load18(A.edge_a + (long long)Rec<Real>::kEdge * e, Ae);
 #pragma unroll
             for (int r = 0; r < 6; ++r) {
                 const Real d = (Real)dcl[6 * a + r];
@@ -607,16 +692,33 @@ __device__ double update_points(const WinArgs<Real>& A, const CC& c, const WinDe
         Xt[4LL * gp + 0] = Xc[4LL * gp + 0] + (double)d0;
         Xt[4LL * gp + 1] = Xc[4LL * gp + 1] + (double)d1;
         Xt[4LL * gp + 2] = Xc[4LL * gp + 2] + (double)d2;
-        const Real* vg = A.pt_vg + 12LL * gp;
+        Real vg[12];
+        Rec<Real>::load12(A.pt_vg + 12LL * gp, vg);
         sc += (double)d0 * (lambda * (double)d0 + (double)vg[6]) + (double)d1 * (lambda * (double)d1 + (double)vg[7]) +
               (double)d2 * (lambda * (double)d2 + (double)vg[8]);
     }
     return sc;
 }
 
+// Phase timer: thread 0 of rank 0 adds the SM cycles since the previous mark to phase `ph`.
+struct PhaseClock {
+    unsigned long long* acc;
+    long long last;
+    __device__ PhaseClock(unsigned long long* a, const CC& c) : acc(c.rank == 0 && threadIdx.x == 0 ? a : nullptr) {
+        last = clock64();
+    }
+    __device__ __forceinline__ void mark(int ph) {
+        if (!acc) return;
+        const long long now = clock64();
+        atomicAdd(acc + ph, (unsigned long long)(now - last));
+        last = now;
+    }
+};
+
 template <class Real>
 __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char* smem) {
     SmemHead& s = *c.s;
+    PhaseClock pc(A.phase, c);
     const WinDesc D = A.win[w];
     const int m = 6 * D.nfc;
     const Dyn dl = dyn_layout(A.max_m, A.max_ncam, (int)sizeof(Real));
@@ -628,6 +730,7 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
     double* dcl = reinterpret_cast<double*>(smem + dl.dcl);
     double* S = reinterpret_cast<double*>(smem + dl.S);
     double* bs = reinterpret_cast<double*>(smem + dl.bs);
+    double* rinv = reinterpret_cast<double*>(smem + dl.rinv);
     WinStats* st = A.stats + w;
     double* trace = A.trace + (long long)w * A.trace_stride;
     const bool mixed = sizeof(Real) == 4;
@@ -649,6 +752,7 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
     if (threadIdx.x == 0) s.cur = 0;
     __syncthreads();
     build_lists(A, c, D);  // ends with a cluster barrier: points are initialized everywhere
+    pc.mark(0);
 
     double chi = cluster_reduce3<false>(c, cost_partial<Real, Real>(A, c, D, camr, A.x[0]), 0.0, 0.0).x;
     double chi0_fp64 = chi;
@@ -659,6 +763,7 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
     }
     int iters_done = 0, acc = 0, rej = 0, term = NAV_BA_TERM_ITERATIONS;
     double lambda = 0.0, nu = 2.0;
+    pc.mark(1);
     if (c.rank == 0 && threadIdx.x == 0) trace[0] = chi;
     const bool bad = !isfinite(chi);
     if (!bad && D.nfc + D.nfp == 0) term = NAV_BA_TERM_NOTHING_TO_DO;
@@ -667,8 +772,10 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
             const int cur = s.cur;
             Real* cr_cur = cur == 0 ? camr : camr_tr;
             const double mxp = linearize_points<Real>(A, c, D, cr_cur, A.x[cur]);
+            pc.mark(2);
             const double mxc = linearize_cameras<Real>(A, c, D, cr_cur, A.x[cur]);
             const double maxdiag = cluster_reduce3<true>(c, fmax(mxp, mxc), 0.0, 0.0).x;
+            pc.mark(3);
             if (it == 0) {
                 lambda = A.lm.initial_lambda > 0 ? A.lm.initial_lambda : A.lm.tau * maxdiag;
                 nu = 2.0;
@@ -681,8 +788,10 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
                     for (int k = threadIdx.x; k < m * (m + 1) / 2; k += blockDim.x) S[k] = 0.0;
                 const int npd = schur_points<Real>(A, c, D, lam_use);
                 const double3 r0 = cluster_reduce3<false>(c, (double)npd, 0.0, 0.0);  // also orders S zeroing
+                pc.mark(4);
                 schur_blocks<Real>(A, c, D, lam_use);
                 csync();
+                pc.mark(5);
                 if (A.debug) {
                     if (c.rank == 0) {
                         for (int k = threadIdx.x; k < m * m; k += blockDim.x) {
@@ -695,9 +804,9 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
                     return;
                 }
                 if (c.rank == 0) {
-                    bool okc = smem_cholesky(S, m, s) && r0.x == 0.0;
+                    bool okc = smem_cholesky(S, rinv, m, s) && r0.x == 0.0;
                     if (okc) {
-                        smem_chol_solve(S, m, bs);
+                        smem_chol_solve(S, rinv, m, bs);
                     } else {
                         for (int k = threadIdx.x; k < m; k += blockDim.x) bs[k] = 0.0;
                     }
@@ -705,6 +814,7 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
                     if (threadIdx.x == 0) s.ok = okc ? 1 : 0;
                 }
                 csync();
+                pc.mark(6);
                 // every CTA takes the camera step from rank 0 and updates all cameras itself
                 for (int k = threadIdx.x; k < m; k += blockDim.x) dcl[k] = c.bs0[k];
                 __syncthreads();
@@ -725,6 +835,7 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
                 }
                 __syncthreads();
                 sc += update_points<Real>(A, c, D, lambda, dcl, cur);
+                pc.mark(7);
                 const double3 red = cluster_reduce3<false>(
                     c, cost_partial<Real, Real>(A, c, D, crt, A.x[cur ^ 1]), sc, 0.0);
                 double chi_new = red.x;
@@ -747,6 +858,7 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
                     ++rej;
                 }
                 __syncthreads();
+                pc.mark(8);
                 ++q;
             } while (rho < 0 && q < A.lm.max_trials);
             iters_done = it + 1;
@@ -782,6 +894,7 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
         st->status = bad ? NAV_BA_ERR_NONFINITE_COST : NAV_BA_OK;
     }
     csync();
+    pc.mark(9);
 }
 
 template <class Real>
@@ -834,6 +947,7 @@ cudaError_t launch_typed(PreparedBatch& pb, cudaStream_t stream, WindowLaunch sh
     A.pt_free = b.d_pt_free;
     A.pt_eoff = b.d_pt_eoff;
     A.edge_cam = b.d_edge_cam;
+    A.edge_fc = b.d_edge_fc;
     A.edge_pt = b.d_edge_pt;
     A.edge_uv = b.d_edge_uv;
     A.x[0] = b.d_x[0];
@@ -855,6 +969,8 @@ cudaError_t launch_typed(PreparedBatch& pb, cudaStream_t stream, WindowLaunch sh
     A.lm = pb.lm;
     A.max_m = b.max_m;
     A.max_ncam = std::max(1, b.max_ncam);
+    A.phase = b.d_phase;
+    if (b.d_phase) cudaMemsetAsync(b.d_phase, 0, sizeof(unsigned long long) * kWinPhases, stream);
     const int C = std::max(1, std::min(kMaxCluster, shape.cluster));
     const int T = shape.threads;
     if (T % 32 != 0 || T < 64 || T > (sizeof(Real) == 8 ? 256 : 512)) return cudaErrorInvalidConfiguration;
@@ -984,19 +1100,62 @@ cudaError_t linearize_observations(const nav_ba_problem& p, const nav_ba_options
 
 static size_t real_size(int precision) { return precision == NAV_BA_MIXED ? sizeof(float) : sizeof(double); }
 
+void* HostStaging::get(int id, size_t bytes) {
+    bytes = std::max<size_t>(bytes, 64);
+    if (cap[id] >= bytes) return buf[id];
+    if (buf[id]) cudaFreeHost(buf[id]);
+    buf[id] = nullptr;
+    cap[id] = 0;
+    const size_t want = bytes + bytes / 4;
+    if (cudaHostAlloc(&buf[id], want, cudaHostAllocDefault) != cudaSuccess) {
+        buf[id] = nullptr;
+        return nullptr;
+    }
+    cap[id] = want;
+    return buf[id];
+}
+
+void HostStaging::release() {
+    for (int i = 0; i < 16; ++i) {
+        if (buf[i]) cudaFreeHost(buf[i]);
+        buf[i] = nullptr;
+        cap[i] = 0;
+    }
+}
+
 void window_batch_free(WindowBatch& b) {
     void* ptrs[] = {b.d_win, b.d_order, b.d_queue, b.d_cam_init, b.d_cam_free, b.d_pt_init, b.d_pt_free,
-                    b.d_pt_eoff, b.d_edge_cam, b.d_edge_pt, b.d_edge_uv, b.d_x[0], b.d_x[1], b.d_pt_vg,
+                    b.d_pt_eoff, b.d_edge_cam, b.d_edge_fc, b.d_edge_pt, b.d_edge_uv, b.d_x[0], b.d_x[1], b.d_pt_vg,
                     b.d_pt_lt, b.d_edge_w, b.d_edge_a, b.d_cam_list, b.d_pairs, b.d_cam_out, b.d_pt_out,
-                    b.d_trace, b.d_stats, b.d_debug};
+                    b.d_trace, b.d_stats, b.d_debug, b.d_phase};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     b = WindowBatch();
 }
 
+namespace {
+
+// Run fn(i) for i in [0, n) on up to hardware_concurrency threads (contiguous chunks).
+template <class Fn>
+void parallel_for(int n, Fn fn) {
+    const int nth = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), n / 4));
+    if (nth <= 1) {
+        for (int i = 0; i < n; ++i) fn(i);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int t = 0; t < nth; ++t)
+        th.emplace_back([&, t] {
+            const int lo = (int)((long long)n * t / nth), hi = (int)((long long)n * (t + 1) / nth);
+            for (int i = lo; i < hi; ++i) fn(i);
+        });
+    for (auto& x : th) x.join();
+}
+
+}  // namespace
+
 cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int precision, int trace_stride,
-                                std::string* why) {
-    window_batch_free(pb.dev);
+                                HostStaging& stg, std::string* why) {
     WindowBatch& b = pb.dev;
     std::vector<int32_t> idx;
     for (size_t i = 0; i < pb.host.size(); ++i)
@@ -1022,28 +1181,6 @@ cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int prec
         if (why) *why = "batch too large for 32-bit indices";
         return cudaErrorInvalidValue;
     }
-    b.n_win = (int32_t)pb.host.size();
-    b.ncam = nc; b.npt = np; b.ne = ne; b.npair = npair;
-    b.max_m = max_m;
-    b.max_ncam = max_nc;
-    b.precision = precision;
-    b.trace_stride = trace_stride;
-    std::vector<CamState> cam(nc);
-    std::vector<int32_t> cam_free(nc), pt_free(np), pt_eoff(np + 1), edge_cam(ne), edge_pt(ne);
-    std::vector<double> pt(4 * np), uv(2 * ne);
-    for (size_t i = 0; i < pb.host.size(); ++i) {
-        const HostWindow& h = pb.host[i];
-        const WinDesc& d = pb.desc[i];
-        std::copy(h.cam.begin(), h.cam.end(), cam.begin() + d.cam0);
-        std::copy(h.cam_free.begin(), h.cam_free.end(), cam_free.begin() + d.cam0);
-        std::copy(h.pt_free.begin(), h.pt_free.end(), pt_free.begin() + d.pt0);
-        std::copy(h.pt.begin(), h.pt.end(), pt.begin() + 4LL * d.pt0);
-        for (int k = 0; k < h.npt; ++k) pt_eoff[d.pt0 + k] = d.e0 + h.pt_eoff[k];
-        std::copy(h.edge_cam.begin(), h.edge_cam.end(), edge_cam.begin() + d.e0);
-        std::copy(h.edge_pt.begin(), h.edge_pt.end(), edge_pt.begin() + d.e0);
-        std::copy(h.edge_uv.begin(), h.edge_uv.end(), uv.begin() + 2LL * d.e0);
-    }
-    pt_eoff[np] = (int32_t)ne;
     // schedule: largest windows first (edges, pairs and a Cholesky-size term)
     std::vector<int32_t> order = idx;
     std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
@@ -1054,57 +1191,134 @@ cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int prec
         return wx > wy;
     });
     const size_t rs = real_size(precision);
+    const size_t nw = pb.desc.size();
     cudaError_t err = cudaSuccess;
-    auto alloc = [&](auto** p, size_t bytes) {
+    int slot = 0;
+    b.bytes = 0;
+    auto ensure = [&](auto** p, size_t bytes) {
+        const int id = slot++;
         if (err != cudaSuccess) return;
         bytes = std::max<size_t>(bytes, 16);
-        err = cudaMalloc((void**)p, bytes);
         b.bytes += bytes;
+        if (*p && b.cap[id] >= bytes) return;
+        if (*p) cudaFree(*p);
+        *p = nullptr;
+        b.cap[id] = 0;
+        err = cudaMalloc((void**)p, bytes);
+        if (err == cudaSuccess) b.cap[id] = bytes;
     };
-    alloc(&b.d_win, sizeof(WinDesc) * pb.desc.size());
-    alloc(&b.d_order, sizeof(int32_t) * order.size());
-    alloc(&b.d_queue, sizeof(int32_t));
-    alloc(&b.d_cam_init, sizeof(CamState) * nc);
-    alloc(&b.d_cam_free, sizeof(int32_t) * nc);
-    alloc(&b.d_pt_init, sizeof(double) * 4 * np);
-    alloc(&b.d_pt_free, sizeof(int32_t) * np);
-    alloc(&b.d_pt_eoff, sizeof(int32_t) * (np + 1));
-    alloc(&b.d_edge_cam, sizeof(int32_t) * ne);
-    alloc(&b.d_edge_pt, sizeof(int32_t) * ne);
-    alloc(&b.d_edge_uv, sizeof(double) * 2 * ne);
-    alloc(&b.d_x[0], sizeof(double) * 4 * np);
-    alloc(&b.d_x[1], sizeof(double) * 4 * np);
-    alloc(&b.d_pt_vg, rs * 12 * np);
-    alloc(&b.d_pt_lt, rs * 12 * np);
-    alloc(&b.d_edge_w, rs * 18 * ne);
-    alloc(&b.d_edge_a, rs * 18 * ne);
-    alloc(&b.d_cam_list, sizeof(int32_t) * ne);
-    alloc(&b.d_pairs, sizeof(uint32_t) * npair);
-    alloc(&b.d_cam_out, sizeof(CamState) * nc);
-    alloc(&b.d_pt_out, sizeof(double) * 4 * np);
-    alloc(&b.d_trace, sizeof(double) * trace_stride * pb.desc.size());
-    alloc(&b.d_stats, sizeof(WinStats) * pb.desc.size());
-    alloc(&b.d_debug, sizeof(double) * ((size_t)max_m * max_m + max_m));
+    ensure(&b.d_win, sizeof(WinDesc) * nw);
+    ensure(&b.d_order, sizeof(int32_t) * order.size());
+    ensure(&b.d_queue, sizeof(int32_t));
+    ensure(&b.d_cam_init, sizeof(CamState) * nc);
+    ensure(&b.d_cam_free, sizeof(int32_t) * nc);
+    ensure(&b.d_pt_init, sizeof(double) * 4 * np);
+    ensure(&b.d_pt_free, sizeof(int32_t) * np);
+    ensure(&b.d_pt_eoff, sizeof(int32_t) * (np + 1));
+    ensure(&b.d_edge_cam, sizeof(int32_t) * ne);
+    ensure(&b.d_edge_fc, sizeof(int32_t) * ne);
+    ensure(&b.d_edge_pt, sizeof(int32_t) * ne);
+    ensure(&b.d_edge_uv, sizeof(double) * 2 * ne);
+    ensure(&b.d_x[0], sizeof(double) * 4 * np);
+    ensure(&b.d_x[1], sizeof(double) * 4 * np);
+    ensure(&b.d_pt_vg, rs * 12 * np);
+    ensure(&b.d_pt_lt, rs * 12 * np);
+    const size_t rec = precision == NAV_BA_MIXED ? 20 : 18;  // per-edge record stride (Reals)
+    ensure(&b.d_edge_w, rs * rec * ne);
+    ensure(&b.d_edge_a, rs * rec * ne);
+    ensure(&b.d_cam_list, sizeof(int32_t) * ne);
+    ensure(&b.d_pairs, sizeof(uint32_t) * npair);
+    ensure(&b.d_cam_out, sizeof(CamState) * nc);
+    ensure(&b.d_pt_out, sizeof(double) * 4 * np);
+    ensure(&b.d_trace, sizeof(double) * trace_stride * nw);
+    ensure(&b.d_stats, sizeof(WinStats) * nw);
+    ensure(&b.d_debug, sizeof(double) * ((size_t)max_m * max_m + max_m));
+    const char* pt_env = getenv("NAVBA_PHASE_TIMING");
+    if (pt_env && pt_env[0] == '1') {
+        ensure(&b.d_phase, sizeof(unsigned long long) * kWinPhases);
+    } else {
+        if (b.d_phase) cudaFree(b.d_phase);
+        b.d_phase = nullptr;
+        b.cap[slot++] = 0;
+    }
+    if (err != cudaSuccess) {
+        if (why) *why = cudaGetErrorString(err);
+        return err;
+    }
+    b.n_win = (int32_t)nw;
+    b.ncam = nc; b.npt = np; b.ne = ne; b.npair = npair;
+    b.max_m = max_m;
+    b.max_ncam = max_nc;
+    b.precision = precision;
+    b.trace_stride = trace_stride;
+    // stage the concatenated inputs in pinned memory (parallel over windows), then copy
+    CamState* cam = (CamState*)stg.get(0, sizeof(CamState) * nc);
+    int32_t* cam_free = (int32_t*)stg.get(1, sizeof(int32_t) * nc);
+    double* pt = (double*)stg.get(2, sizeof(double) * 4 * np);
+    int32_t* pt_free = (int32_t*)stg.get(3, sizeof(int32_t) * np);
+    int32_t* pt_eoff = (int32_t*)stg.get(4, sizeof(int32_t) * (np + 1));
+    int32_t* edge_cam = (int32_t*)stg.get(5, sizeof(int32_t) * ne);
+    int32_t* edge_fc = (int32_t*)stg.get(14, sizeof(int32_t) * ne);
+    int32_t* edge_pt = (int32_t*)stg.get(6, sizeof(int32_t) * ne);
+    double* uv = (double*)stg.get(7, sizeof(double) * 2 * ne);
+    WinDesc* desc = (WinDesc*)stg.get(8, sizeof(WinDesc) * nw);
+    int32_t* ord = (int32_t*)stg.get(9, sizeof(int32_t) * order.size());
+    if (!cam || !cam_free || !pt || !pt_free || !pt_eoff || !edge_cam || !edge_fc || !edge_pt || !uv || !desc || !ord) {
+        if (why) *why = "pinned host allocation failed";
+        return cudaErrorMemoryAllocation;
+    }
+    std::copy(pb.desc.begin(), pb.desc.end(), desc);
+    std::copy(order.begin(), order.end(), ord);
+    parallel_for((int)nw, [&](int i) {
+        const HostWindow& h = pb.host[i];
+        const WinDesc& d = pb.desc[i];
+        std::copy(h.cam.begin(), h.cam.end(), cam + d.cam0);
+        std::copy(h.cam_free.begin(), h.cam_free.end(), cam_free + d.cam0);
+        std::copy(h.pt_free.begin(), h.pt_free.end(), pt_free + d.pt0);
+        std::copy(h.pt.begin(), h.pt.end(), pt + 4LL * d.pt0);
+        for (int k = 0; k < h.npt; ++k) pt_eoff[d.pt0 + k] = d.e0 + h.pt_eoff[k];
+        std::copy(h.edge_cam.begin(), h.edge_cam.end(), edge_cam + d.e0);
+        for (int k = 0; k < h.ne; ++k) edge_fc[d.e0 + k] = h.cam_free[h.edge_cam[k]];
+        std::copy(h.edge_pt.begin(), h.edge_pt.end(), edge_pt + d.e0);
+        std::copy(h.edge_uv.begin(), h.edge_uv.end(), uv + 2LL * d.e0);
+    });
+    pt_eoff[np] = (int32_t)ne;
     b.h2d_bytes = 0;
     auto up = [&](void* dst, const void* src, size_t bytes) {
         if (err != cudaSuccess || bytes == 0) return;
         err = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream);
         b.h2d_bytes += (int64_t)bytes;
     };
-    up(b.d_win, pb.desc.data(), sizeof(WinDesc) * pb.desc.size());
-    up(b.d_order, order.data(), sizeof(int32_t) * order.size());
-    up(b.d_cam_init, cam.data(), sizeof(CamState) * nc);
-    up(b.d_cam_free, cam_free.data(), sizeof(int32_t) * nc);
-    up(b.d_pt_init, pt.data(), sizeof(double) * 4 * np);
-    up(b.d_pt_free, pt_free.data(), sizeof(int32_t) * np);
-    up(b.d_pt_eoff, pt_eoff.data(), sizeof(int32_t) * (np + 1));
-    up(b.d_edge_cam, edge_cam.data(), sizeof(int32_t) * ne);
-    up(b.d_edge_pt, edge_pt.data(), sizeof(int32_t) * ne);
-    up(b.d_edge_uv, uv.data(), sizeof(double) * 2 * ne);
+    up(b.d_win, desc, sizeof(WinDesc) * nw);
+    up(b.d_order, ord, sizeof(int32_t) * order.size());
+    up(b.d_cam_init, cam, sizeof(CamState) * nc);
+    up(b.d_cam_free, cam_free, sizeof(int32_t) * nc);
+    up(b.d_pt_init, pt, sizeof(double) * 4 * np);
+    up(b.d_pt_free, pt_free, sizeof(int32_t) * np);
+    up(b.d_pt_eoff, pt_eoff, sizeof(int32_t) * (np + 1));
+    up(b.d_edge_cam, edge_cam, sizeof(int32_t) * ne);
+    up(b.d_edge_fc, edge_fc, sizeof(int32_t) * ne);
+    up(b.d_edge_pt, edge_pt, sizeof(int32_t) * ne);
+    up(b.d_edge_uv, uv, sizeof(double) * 2 * ne);
     if (err == cudaSuccess) err = cudaStreamSynchronize(stream);
     b.n_queue = (int32_t)order.size();
     if (err != cudaSuccess && why) *why = cudaGetErrorString(err);
     return err;
+}
+
+void window_phase_report(const PreparedBatch& pb, const WindowLaunch& shape, int precision) {
+    if (!pb.dev.d_phase) return;
+    unsigned long long h[kWinPhases] = {};
+    if (cudaMemcpy(h, pb.dev.d_phase, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return;
+    static const char* names[kWinPhases] = {"init+lists", "initial cost", "linearize points", "linearize cameras",
+                                            "schur points", "schur blocks", "cholesky", "update", "trial cost",
+                                            "outputs"};
+    unsigned long long tot = 0;
+    for (int k = 0; k < kWinPhases; ++k) tot += h[k];
+    fprintf(stderr, "[navba phases] precision=%d cluster=%d threads=%d total=%llu cycles (rank-0 CTAs, summed)\n",
+            precision, shape.cluster, shape.threads, tot);
+    for (int k = 0; k < kWinPhases; ++k)
+        fprintf(stderr, "[navba phases] %-18s %14llu  %5.1f%%\n", names[k], h[k], tot ? 100.0 * h[k] / tot : 0.0);
 }
 
 }  // namespace navba
