@@ -208,6 +208,28 @@ nav_ba_status nav_ba_reduced_system(nav_ba_ctx* ctx, const nav_ba_problem* probl
 nav_ba_status nav_ba_cost(nav_ba_ctx* ctx, const nav_ba_problem* problem,
                           const nav_ba_options* options, double* cost);
 
+/* No counterpart in the reference (nav24 builds a g2o optimizer on the heap for every call).
+ * nav_ba_solve for callers that must not allocate device memory while solving: a tracking
+ * thread with a real-time budget (cudaMalloc/cudaFree can block, cudaFree synchronizes the
+ * device), or a process whose device memory is reserved by another framework's allocator.
+ * It solves one window with the window engine, and every device buffer it uses lives in one
+ * static device array of NAV_BA_NOALLOC_ARENA_BYTES that each GPU loading the library holds until
+ * the process exits.  No cudaMalloc, cudaFree or other allocating routine is called.
+ * Limits: NAV_BA_NOALLOC_MAX_CAMS cameras (at most NAV_BA_WINDOW_MAX_CAMS free),
+ * NAV_BA_NOALLOC_MAX_POINTS points, NAV_BA_NOALLOC_MAX_OBS observations and
+ * NAV_BA_NOALLOC_MAX_PAIRS Schur pairs, and the whole layout must fit the array; larger problems
+ * are rejected with NAV_BA_ERR_UNSUPPORTED and a message.  Cholesky solver only, no distortion
+ * optimization.  The first call on a device looks up the array's device address (make that first
+ * call before any stream capture).  All calls on a device share the array; calls whose GPU work
+ * overlaps (e.g. from two contexts on one device) race on it. */
+#define NAV_BA_NOALLOC_MAX_CAMS 64
+#define NAV_BA_NOALLOC_MAX_POINTS 4096
+#define NAV_BA_NOALLOC_MAX_OBS 32768
+#define NAV_BA_NOALLOC_MAX_PAIRS 262144
+#define NAV_BA_NOALLOC_ARENA_BYTES (16u * 1024u * 1024u)
+nav_ba_status nav_ba_solve_noalloc(nav_ba_ctx* ctx, const nav_ba_problem* problem,
+                                   const nav_ba_options* options, nav_ba_result* result);
+
 /* Last error message of the context (empty string if none). */
 const char* nav_ba_last_error(const nav_ba_ctx* ctx);
 const char* nav_ba_status_string(nav_ba_status status);

@@ -21,7 +21,7 @@ EXPORTS = [
     "nav_ba_solve_batched", "nav_ba_prepare", "nav_ba_run", "nav_ba_fetch", "nav_ba_prepare_batched",
     "nav_ba_fetch_batched", "nav_ba_linearize",
     "nav_ba_reduced_system", "nav_ba_cost", "nav_ba_last_error", "nav_ba_status_string",
-    "nav_ba_abi_version",
+    "nav_ba_abi_version", "nav_ba_solve_noalloc",
 ]
 
 _LIB = None
@@ -73,6 +73,8 @@ def load(path: os.PathLike | None = None) -> C.CDLL:
     L.nav_ba_last_error.restype = C.c_char_p
     L.nav_ba_status_string.argtypes = [C.c_int]
     L.nav_ba_status_string.restype = C.c_char_p
+    L.nav_ba_solve_noalloc.argtypes = [ctxp, P, O, R]
+    L.nav_ba_solve_noalloc.restype = C.c_int
     L.nav_ba_abi_version.argtypes = []
     L.nav_ba_abi_version.restype = C.c_int32
     if path is None:
@@ -130,6 +132,15 @@ class Context:
         buf = abi.ResultBuffers(prob, opt.iterations)
         p = prob.as_c()
         st = self.L.nav_ba_solve(self.h, C.byref(p), C.byref(opt), C.byref(buf.c))
+        if raise_on_error:
+            self._check(st, (abi.OK, abi.EMPTY))
+        return buf.result(st)
+
+    def solve_noalloc(self, prob: abi.Problem, opt: abi.nav_ba_options, raise_on_error=True) -> abi.Result:
+        """nav_ba_solve_noalloc: one window solved in the library's static device array."""
+        buf = abi.ResultBuffers(prob, opt.iterations)
+        p = prob.as_c()
+        st = self.L.nav_ba_solve_noalloc(self.h, C.byref(p), C.byref(opt), C.byref(buf.c))
         if raise_on_error:
             self._check(st, (abi.OK, abi.EMPTY))
         return buf.result(st)

@@ -135,4 +135,8 @@ cudaError_t linearize_observations(const nav_ba_problem& p, const nav_ba_options
                                    cudaStream_t stream, double* e, double* jc, double* jp,
                                    double* w, std::string* why);
 
+// One-window solve in the library's static device array (no device allocation), noalloc.cu.
+nav_ba_status solve_window_noalloc(int device, cudaStream_t stream, const nav_ba_problem& p,
+                                   const nav_ba_options& o, nav_ba_result& r, std::string* why);
+
 }  // namespace navba

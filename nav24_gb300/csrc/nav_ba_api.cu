@@ -537,6 +537,31 @@ nav_ba_status nav_ba_cost(nav_ba_ctx* ctx, const nav_ba_problem* p, const nav_ba
     return NAV_BA_OK;
 }
 
+nav_ba_status nav_ba_solve_noalloc(nav_ba_ctx* ctx, const nav_ba_problem* p, const nav_ba_options* o,
+                                   nav_ba_result* r) {
+    if (!ctx) return NAV_BA_ERR_ARGUMENT;
+    if (!p || !o || !r) return set_err(ctx, NAV_BA_ERR_ARGUMENT, "NULL argument");
+    cudaSetDevice(ctx->device);
+    ctx->last_error.clear();
+    std::string why;
+    nav_ba_status st = validate_problem(p, &why);
+    if (st == NAV_BA_OK) st = validate_options(o, &why);
+    if (st != NAV_BA_OK) return set_err(ctx, st, why);
+    nav_ba_result tmp = *r;
+    clear_stats(&tmp);
+    st = solve_window_noalloc(ctx->device, ctx->stream, *p, *o, tmp, &why);
+    if (st == NAV_BA_EMPTY) {
+        write_passthrough(*p, &tmp, false);
+        tmp.termination = NAV_BA_TERM_NOTHING_TO_DO;
+        tmp.status = NAV_BA_EMPTY;
+        *r = tmp;
+        return NAV_BA_EMPTY;
+    }
+    if (st != NAV_BA_OK) return set_err(ctx, st, why);
+    *r = tmp;
+    return NAV_BA_OK;
+}
+
 const char* nav_ba_last_error(const nav_ba_ctx* ctx) { return ctx ? ctx->last_error.c_str() : ""; }
 
 const char* nav_ba_status_string(nav_ba_status s) {
