@@ -25,7 +25,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-r
               "-Xptxas", "-warn-spills"]
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-Wextra"]
 
-PRODUCT_CU = ["nav_ba_api.cu", "window_engine.cu", "noalloc.cu"]
+PRODUCT_CU = ["nav_ba_api.cu", "window_engine.cu", "grid_engine.cu", "noalloc.cu"]
 PRODUCT_CPP = ["structure.cpp"]
 SYNTH_CPP = ["synth.cpp"]
 

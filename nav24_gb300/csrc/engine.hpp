@@ -135,6 +135,22 @@ cudaError_t linearize_observations(const nav_ba_problem& p, const nav_ba_options
                                    cudaStream_t stream, double* e, double* jc, double* jp,
                                    double* w, std::string* why);
 
+// Result of one grid-engine solve (grid_engine.cu).
+struct GridResult {
+    int32_t status = 0;
+    double initial_cost = 0, final_cost = 0, final_lambda = 0;
+    int32_t iterations_done = 0, accepted = 0, rejected = 0, termination = 0;
+    std::vector<double> trace;
+    std::vector<CamState> cams;
+    std::vector<double> points;  // [npt][4]
+};
+
+// Solve one large problem on the whole GPU.  debug_S != nullptr: stop after assembling the
+// reduced system at damping debug_lambda and return [S (m*m, row-major, lower part) | b'].
+cudaError_t grid_solve(const HostWindow& h, const LmOptions& lm, const Intr& intr, int precision,
+                       cudaStream_t stream, int cluster, GridResult& out, double debug_lambda,
+                       std::vector<double>* debug_S);
+
 // One-window solve in the library's static device array (no device allocation), noalloc.cu.
 nav_ba_status solve_window_noalloc(int device, cudaStream_t stream, const nav_ba_problem& p,
                                    const nav_ba_options& o, nav_ba_result& r, std::string* why);

@@ -1,0 +1,300 @@
+// lm_device.cuh - device code shared by the window engine and the grid engine: the argument
+// block, the thread-range view, the per-point / per-edge phases of one LM iteration (point-major
+// linearization, damped point blocks and A = W L^T, back-substitution) and the robust cost.
+// Each phase loops over points p = gt, gt + CT, ... so it runs unchanged over one window (a CTA
+// cluster) or over a whole problem (a grid).
+#pragma once
+
+#include "engine.hpp"
+
+namespace navba {
+namespace {
+
+struct SmemHead;  // the window engine's shared-memory head (window_engine.cu)
+
+template <class Real>
+struct WinArgs {
+    const WinDesc* win;
+    int32_t n_win;
+    const int32_t* order;
+    int32_t* queue;
+    const CamState* cam_init;
+    const int32_t* cam_free;
+    const double* pt_init;
+    const int32_t* pt_free;
+    const int32_t* pt_eoff;
+    const int32_t* edge_cam;
+    const int32_t* edge_fc;   // free index of each edge's camera, or -1
+    const int32_t* edge_pt;
+    const double* edge_uv;
+    double* x[2];
+    Real* pt_vg;
+    Real* pt_lt;
+    Real* edge_w;
+    Real* edge_a;
+    int32_t* cam_list;
+    uint32_t* pairs;
+    CamState* cam_out;
+    double* pt_out;
+    double* trace;
+    int32_t trace_stride;
+    WinStats* stats;
+    double* debug;
+    double debug_lambda;
+    Intr intr;
+    LmOptions lm;
+    int32_t max_m, max_ncam;
+    unsigned long long* phase;  // optional per-phase SM-cycle totals (rank 0 view), or null
+};
+
+NAVBA_HD int tri(int r, int c) { return r * (r + 1) / 2 + c; }  // packed lower index, c <= r
+
+// Per-CTA view of the cluster working on a window.
+struct CC {
+    int rank, csize;
+    int gt, CT;   // thread index / count over the cluster
+    int gw, CW;   // warp index / count over the cluster
+    int lane, wid, nw;
+    SmemHead* s;   // this CTA's head
+    SmemHead* s0;  // rank 0's head (distributed shared memory)
+    double* S0;    // rank 0's reduced system
+    double* bs0;   // rank 0's right-hand side / step
+};
+
+template <class Real>
+__device__ __forceinline__ void cam_real(const CamState& c, Real* o) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) o[k] = (Real)c.R[k];
+    o[9] = (Real)c.t[0];
+    o[10] = (Real)c.t[1];
+    o[11] = (Real)c.t[2];
+}
+
+// Per-edge 18-value records (W, A) and per-point 12-value records (V|g, L|t), moved with
+// 16-byte vector accesses: FP32 records are padded to 20 floats (80 B), FP64 ones are 144 B.
+template <class Real>
+struct Rec;
+
+template <>
+struct Rec<float> {
+    static constexpr int kEdge = 20;
+    static __device__ __forceinline__ void load18(const float* p, float* v) {
+        const float4* q = reinterpret_cast<const float4*>(p);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float4 t = q[k];
+            v[4 * k] = t.x; v[4 * k + 1] = t.y; v[4 * k + 2] = t.z; v[4 * k + 3] = t.w;
+        }
+        const float2 t = reinterpret_cast<const float2*>(p)[8];
+        v[16] = t.x;
+        v[17] = t.y;
+    }
+    static __device__ __forceinline__ void store18(float* p, const float* v) {
+        float4* q = reinterpret_cast<float4*>(p);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) q[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+        reinterpret_cast<float2*>(p)[8] = make_float2(v[16], v[17]);
+    }
+    static __device__ __forceinline__ void load12(const float* p, float* v) {
+        const float4* q = reinterpret_cast<const float4*>(p);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float4 t = q[k];
+            v[4 * k] = t.x; v[4 * k + 1] = t.y; v[4 * k + 2] = t.z; v[4 * k + 3] = t.w;
+        }
+    }
+    static __device__ __forceinline__ void store12(float* p, const float* v) {
+        float4* q = reinterpret_cast<float4*>(p);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) q[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+    }
+};
+
+template <>
+struct Rec<double> {
+    static constexpr int kEdge = 18;
+    static __device__ __forceinline__ void load18(const double* p, double* v) {
+        const double2* q = reinterpret_cast<const double2*>(p);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            const double2 t = q[k];
+            v[2 * k] = t.x;
+            v[2 * k + 1] = t.y;
+        }
+    }
+    static __device__ __forceinline__ void store18(double* p, const double* v) {
+        double2* q = reinterpret_cast<double2*>(p);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) q[k] = make_double2(v[2 * k], v[2 * k + 1]);
+    }
+    static __device__ __forceinline__ void load12(const double* p, double* v) {
+        const double2* q = reinterpret_cast<const double2*>(p);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const double2 t = q[k];
+            v[2 * k] = t.x;
+            v[2 * k + 1] = t.y;
+        }
+    }
+    static __device__ __forceinline__ void store12(double* p, const double* v) {
+        double2* q = reinterpret_cast<double2*>(p);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) q[k] = make_double2(v[2 * k], v[2 * k + 1]);
+    }
+};
+
+// Cluster-split robust chi2 of the window for cameras `camc` (12 values per camera, precision
+// Cost) and points X; returns this thread's partial sum.
+template <class Cost, class Real>
+__device__ double cost_partial(const WinArgs<Real>& A, const CC& c, const WinDesc& D, const Cost* camc,
+                               const double* X) {
+    double acc = 0.0;
+    const Cost delta = (Cost)A.lm.huber_delta;
+    for (int p = c.gt; p < D.npt; p += c.CT) {
+        const int gp = D.pt0 + p;
+        const Cost Xr[3] = {(Cost)X[4LL * gp], (Cost)X[4LL * gp + 1], (Cost)X[4LL * gp + 2]};
+        const int e1 = A.pt_eoff[gp + 1];
+        for (int e = A.pt_eoff[gp]; e < e1; ++e) {
+            const Cost* cr = camc + 12 * A.edge_cam[e];
+            const Cost z[2] = {(Cost)A.edge_uv[2LL * e], (Cost)A.edge_uv[2LL * e + 1]};
+            acc += edge_cost<Cost>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta);
+        }
+    }
+    return acc;
+}
+
+// Point-major linearization: V_p, g_p, W_e; returns this thread's max |diag V|.
+template <class Real>
+__device__ double linearize_points(const WinArgs<Real>& A, const CC& c, const WinDesc& D, const Real* camr,
+                                   const double* X) {
+    const Real delta = (Real)A.lm.huber_delta;
+    double mx = 0.0;
+    for (int p = c.gt; p < D.npt; p += c.CT) {
+        const int gp = D.pt0 + p;
+        if (A.pt_free[gp] < 0) continue;
+        const Real Xr[3] = {(Real)X[4LL * gp], (Real)X[4LL * gp + 1], (Real)X[4LL * gp + 2]};
+        Real V[6] = {0, 0, 0, 0, 0, 0}, g[3] = {0, 0, 0};
+        const int e1 = A.pt_eoff[gp + 1];
+        for (int e = A.pt_eoff[gp]; e < e1; ++e) {
+            const int cam = A.edge_cam[e];
+            const Real* cr = camr + 12 * cam;
+            const Real z[2] = {(Real)A.edge_uv[2LL * e], (Real)A.edge_uv[2LL * e + 1]};
+            EdgeLin<Real> L;
+            edge_linearize<Real>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta, L);
+            const Real w = L.w;
+            const Real* jp = L.jp;
+            V[0] += w * (jp[0] * jp[0] + jp[3] * jp[3]);
+            V[1] += w * (jp[0] * jp[1] + jp[3] * jp[4]);
+            V[2] += w * (jp[0] * jp[2] + jp[3] * jp[5]);
+            V[3] += w * (jp[1] * jp[1] + jp[4] * jp[4]);
+            V[4] += w * (jp[1] * jp[2] + jp[4] * jp[5]);
+            V[5] += w * (jp[2] * jp[2] + jp[5] * jp[5]);
+            const Real we0 = -w * L.e[0], we1 = -w * L.e[1];
+            g[0] += jp[0] * we0 + jp[3] * we1;
+            g[1] += jp[1] * we0 + jp[4] * we1;
+            g[2] += jp[2] * we0 + jp[5] * we1;
+            if (A.edge_fc[e] >= 0) {
+                Real W[18];
+#pragma unroll
+                for (int r = 0; r < 6; ++r)
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) W[r * 3 + k] = w * (L.jc[r] * jp[k] + L.jc[6 + r] * jp[3 + k]);
+                Rec<Real>::store18(A.edge_w + (long long)Rec<Real>::kEdge * e, W);
+            }
+        }
+        const Real vgv[12] = {V[0], V[1], V[2], V[3], V[4], V[5], g[0], g[1], g[2], Real(0), Real(0), Real(0)};
+        Rec<Real>::store12(A.pt_vg + 12LL * gp, vgv);
+        mx = fmax(mx, fmax(fabs((double)V[0]), fmax(fabs((double)V[3]), fabs((double)V[5]))));
+    }
+    return mx;
+}
+
+// Per free point: R R^T = V + lambda I, L = R^-1, t = L g, A_e = W_e L^T.  Returns the number of
+// points whose damped block was not positive definite (treated like a failed factorization).
+template <class Real>
+__device__ int schur_points(const WinArgs<Real>& A, const CC& c, const WinDesc& D, double lambda) {
+    const Real lam = (Real)lambda;
+    int bad = 0;
+    for (int p = c.gt; p < D.npt; p += c.CT) {
+        const int gp = D.pt0 + p;
+        if (A.pt_free[gp] < 0) continue;
+        Real vg[12];
+        Rec<Real>::load12(A.pt_vg + 12LL * gp, vg);
+        const Real v00 = vg[0] + lam, v01 = vg[1], v02 = vg[2], v11 = vg[3] + lam, v12 = vg[4], v22 = vg[5] + lam;
+        const Real r00 = sqrt(v00);
+        const Real r10 = v01 / r00, r20 = v02 / r00;
+        const Real d11 = v11 - r10 * r10;
+        const Real r11 = sqrt(d11);
+        const Real r21 = (v12 - r20 * r10) / r11;
+        const Real d22 = v22 - r20 * r20 - r21 * r21;
+        const Real r22 = sqrt(d22);
+        if (!(v00 > Real(0)) || !(d11 > Real(0)) || !(d22 > Real(0))) ++bad;
+        const Real l00 = Real(1) / r00, l11 = Real(1) / r11, l22 = Real(1) / r22;
+        const Real l10 = -r10 * l00 * l11;
+        const Real l21 = -r21 * l11 * l22;
+        const Real l20 = -(r20 * l00 + r21 * l10) * l22;
+        const Real ltv[12] = {l00, l10, l11, l20, l21, l22, l00 * vg[6], l10 * vg[6] + l11 * vg[7],
+                              l20 * vg[6] + l21 * vg[7] + l22 * vg[8], Real(0), Real(0), Real(0)};
+        Rec<Real>::store12(A.pt_lt + 12LL * gp, ltv);
+        const int e1 = A.pt_eoff[gp + 1];
+        for (int e = A.pt_eoff[gp]; e < e1; ++e) {
+            if (A.edge_fc[e] < 0) continue;
+            Real W[18], Ae[18];
+            Rec<Real>::load18(A.edge_w + (long long)Rec<Real>::kEdge * e, W);
+#pragma unroll
+            for (int r = 0; r < 6; ++r) {
+                const Real w0 = W[r * 3 + 0], w1 = W[r * 3 + 1], w2 = W[r * 3 + 2];
+                Ae[r * 3 + 0] = w0 * l00;
+                Ae[r * 3 + 1] = w0 * l10 + w1 * l11;
+                Ae[r * 3 + 2] = w0 * l20 + w1 * l21 + w2 * l22;
+            }
+            Rec<Real>::store18(A.edge_a + (long long)Rec<Real>::kEdge * e, Ae);
+        }
+    }
+    return bad;
+}
+
+// Trial points dx_p = L^T (t_p - sum A_e^T dx_c); returns this thread's dx^T(lambda dx + g) part.
+template <class Real>
+__device__ double update_points(const WinArgs<Real>& A, const CC& c, const WinDesc& D, double lambda,
+                                const double* dcl, int cur) {
+    const double* Xc = A.x[cur];
+    double* Xt = A.x[cur ^ 1];
+    double sc = 0.0;
+    for (int p = c.gt; p < D.npt; p += c.CT) {
+        const int gp = D.pt0 + p;
+        if (A.pt_free[gp] < 0) continue;
+        Real lt[12];
+        Rec<Real>::load12(A.pt_lt + 12LL * gp, lt);
+        Real u0 = lt[6], u1 = lt[7], u2 = lt[8];
+        const int e1 = A.pt_eoff[gp + 1];
+        for (int e = A.pt_eoff[gp]; e < e1; ++e) {
+            const int a = A.edge_fc[e];
+            if (a < 0) continue;
+            Real Ae[18];
+            Rec<Real>::load18(A.edge_a + (long long)Rec<Real>::kEdge * e, Ae);
+#pragma unroll
+            for (int r = 0; r < 6; ++r) {
+                const Real d = (Real)dcl[6 * a + r];
+                u0 -= Ae[r * 3 + 0] * d;
+                u1 -= Ae[r * 3 + 1] * d;
+                u2 -= Ae[r * 3 + 2] * d;
+            }
+        }
+        // dx = L^T u
+        const Real d0 = lt[0] * u0 + lt[1] * u1 + lt[3] * u2;
+        const Real d1 = lt[2] * u1 + lt[4] * u2;
+        const Real d2 = lt[5] * u2;
+        Xt[4LL * gp + 0] = Xc[4LL * gp + 0] + (double)d0;
+        Xt[4LL * gp + 1] = Xc[4LL * gp + 1] + (double)d1;
+        Xt[4LL * gp + 2] = Xc[4LL * gp + 2] + (double)d2;
+        Real vg[12];
+        Rec<Real>::load12(A.pt_vg + 12LL * gp, vg);
+        sc += (double)d0 * (lambda * (double)d0 + (double)vg[6]) + (double)d1 * (lambda * (double)d1 + (double)vg[7]) +
+              (double)d2 * (lambda * (double)d2 + (double)vg[8]);
+    }
+    return sc;
+}
+
+}  // namespace
+}  // namespace navba

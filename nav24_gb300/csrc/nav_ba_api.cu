@@ -26,6 +26,7 @@ struct nav_ba_ctx {
     WindowLaunch shape[2];        // per precision (autotuned on nav_ba_prepare_batched)
     bool tuned[2] = {false, false};
     WindowBatch solve_dev;        // device buffers of nav_ba_solve / _batched, reused across calls
+    int grid_cluster = 8;         // CTAs of the grid engine's Cholesky cluster
     HostStaging stg;              // pinned staging reused across calls
 };
 
@@ -90,6 +91,9 @@ void clear_stats(nav_ba_result* r) {
     r->status = NAV_BA_OK;
     r->edge_iterations = r->h2d_bytes = r->d2h_bytes = 0;
 }
+
+// host_status of a window that goes to the grid engine (too large for the window engine)
+constexpr int32_t kGridWindow = 2;
 
 bool fits_window_engine(const HostWindow& h) {
     return h.nfc <= kWinMaxFreeCams && h.ncam <= kWinMaxCams && h.ne < 65536;
@@ -173,10 +177,7 @@ nav_ba_status build_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, c
         for (auto& th : ths) th.join();
     }
     for (int i = 0; i < n; ++i)
-        if (pb.host_status[i] == NAV_BA_OK && !fits_window_engine(pb.host[i]))
-            return set_err(ctx, NAV_BA_ERR_UNSUPPORTED,
-                           "problem " + std::to_string(i) + " has more than " + std::to_string(kWinMaxFreeCams) +
-                               " free cameras or " + std::to_string(kWinMaxCams) + " cameras");
+        if (pb.host_status[i] == NAV_BA_OK && !fits_window_engine(pb.host[i])) pb.host_status[i] = kGridWindow;
     pb.lm = lm_options(*o);
     pb.intr = n > 0 ? intrinsics_of(probs[0]) : Intr{};
     return NAV_BA_OK;
@@ -222,6 +223,7 @@ nav_ba_status download_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n
             r->status = NAV_BA_EMPTY;
             return;
         }
+        if (pb.host_status[i] == kGridWindow) return;  // solved by the grid engine
         const WinStats& s = stats[i];
         r->status = s.status;
         r->initial_cost = s.initial_cost;
@@ -261,6 +263,44 @@ nav_ba_status download_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n
     return NAV_BA_OK;
 }
 
+// One problem beyond the window engine's limits, on the grid engine; fills r (outputs and stats).
+nav_ba_status solve_grid_window(nav_ba_ctx* ctx, const nav_ba_problem& p, const HostWindow& h, const nav_ba_options& o,
+                                nav_ba_result& r) {
+    GridResult g;
+    cudaEventRecord(ctx->ev0, ctx->stream);
+    cudaError_t e = grid_solve(h, lm_options(o), intrinsics_of(p), o.precision, ctx->stream, ctx->grid_cluster, g, -1.0,
+                               nullptr);
+    cudaEventRecord(ctx->ev1, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev1);
+    if (e != cudaSuccess) return cuda_status(ctx, e, "grid engine");
+    if (g.status != NAV_BA_OK) return set_err(ctx, (nav_ba_status)g.status, "non-finite initial cost");
+    float t = 0.f;
+    cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1);
+    r.status = NAV_BA_OK;
+    r.initial_cost = g.initial_cost;
+    r.final_cost = g.final_cost;
+    r.final_lambda = g.final_lambda;
+    r.iterations_done = g.iterations_done;
+    r.trials_accepted = g.accepted;
+    r.trials_rejected = g.rejected;
+    r.termination = g.termination;
+    r.n_active_edges = h.ne;
+    r.n_free_cams = h.nfc;
+    r.n_free_points = h.nfp;
+    r.n_schur_blocks = h.n_schur_blocks;
+    r.edge_iterations = (int64_t)h.ne * g.iterations_done;
+    r.time_solve_ms += t;
+    if (r.cam_pose_out)
+        for (int c = 0; c < p.n_cams; ++c) pose12_from_cam(g.cams[c], r.cam_pose_out + 12LL * c);
+    if (r.points_out)
+        for (int k = 0; k < p.n_points; ++k)
+            for (int j = 0; j < 3; ++j) r.points_out[3LL * k + j] = g.points[4LL * k + j];
+    if (r.intrinsics_out) std::memcpy(r.intrinsics_out, p.intrinsics, sizeof(double) * 8);
+    if (r.cost_trace)
+        for (int k = 0; k <= g.iterations_done; ++k) r.cost_trace[k] = g.trace[k];
+    return NAV_BA_OK;
+}
+
 nav_ba_status solve_impl(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, const nav_ba_options* o,
                          nav_ba_result* results) {
     if (!ctx) return NAV_BA_ERR_ARGUMENT;
@@ -291,6 +331,11 @@ nav_ba_status solve_impl(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, co
     for (auto& r : tmp) clear_stats(&r);
     st = download_batch(ctx, probs, n, pb, tmp.data());
     if (st != NAV_BA_OK && st != NAV_BA_EMPTY) return set_err(ctx, st, "a problem has a non-finite initial cost");
+    for (int i = 0; i < n; ++i) {
+        if (pb.host_status[i] != kGridWindow) continue;
+        st = solve_grid_window(ctx, probs[i], pb.host[i], *o, tmp[i]);
+        if (st != NAV_BA_OK) return st;
+    }
     const double t_down = ms_since(t1);
     for (int i = 0; i < n; ++i) {
         tmp[i].time_setup_ms = t_setup;
@@ -386,6 +431,11 @@ nav_ba_status nav_ba_prepare_batched(nav_ba_ctx* ctx, const nav_ba_problem* p, i
     pb.desc.clear();
     nav_ba_status st = build_batch(ctx, p, n, o, pb);
     if (st != NAV_BA_OK) return st;
+    for (int i = 0; i < n; ++i)
+        if (pb.host_status[i] == kGridWindow)
+            return set_err(ctx, NAV_BA_ERR_UNSUPPORTED,
+                           "nav_ba_prepare: problem " + std::to_string(i) + " exceeds the window engine (" +
+                               std::to_string(kWinMaxFreeCams) + " free cameras); use nav_ba_solve");
     std::string why;
     cudaError_t e = window_batch_upload(pb, ctx->stream, o->precision, o->iterations + 1, ctx->stg, &why);
     if (e != cudaSuccess) return cuda_status(ctx, e, "upload");
@@ -502,7 +552,19 @@ nav_ba_status nav_ba_reduced_system(nav_ba_ctx* ctx, const nav_ba_problem* p, co
     *n_free = h.nfc;
     if (cam_index) std::memcpy(cam_index, h.cam_free.data(), sizeof(int32_t) * p->n_cams);
     if (capacity_free < h.nfc || !s || !b) return NAV_BA_OK;
-    if (pb.host_status[0] != NAV_BA_OK || h.nfc == 0) {
+    if ((pb.host_status[0] != NAV_BA_OK && pb.host_status[0] != kGridWindow) || h.nfc == 0) {
+        return NAV_BA_OK;
+    }
+    if (pb.host_status[0] == kGridWindow) {
+        GridResult g;
+        std::vector<double> dbg;
+        cudaError_t e = grid_solve(h, lm_options(o1), intrinsics_of(*p), o1.precision, ctx->stream, ctx->grid_cluster, g,
+                                   lambda, &dbg);
+        if (e != cudaSuccess) return cuda_status(ctx, e, "reduced system");
+        const int m = 6 * h.nfc;
+        for (int r = 0; r < m; ++r)
+            for (int c = 0; c < m; ++c) s[(size_t)r * m + c] = r >= c ? dbg[(size_t)r * m + c] : dbg[(size_t)c * m + r];
+        std::memcpy(b, dbg.data() + (size_t)m * m, sizeof(double) * m);
         return NAV_BA_OK;
     }
     std::string why;

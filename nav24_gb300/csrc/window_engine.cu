@@ -34,6 +34,7 @@
 #include <cooperative_groups.h>
 
 #include "engine.hpp"
+#include "lm_device.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -69,7 +70,7 @@ NAVBA_HD Dyn dyn_layout(int max_m, int max_ncam, int real_size) {
     size_t o = align16(sizeof(SmemHead));
     d.cams = o; o = align16(o + sizeof(CamState) * 2 * max_ncam);
     d.camr = o; o = align16(o + (size_t)real_size * 2 * max_ncam * 12);
-    d.camd = o; o = align16(o + sizeof(double) * max_ncam * 12);
+    d.camd = o; o = align16(o + sizeof(double) * 2 * max_ncam * 12);
     d.dcl = o;  o = align16(o + sizeof(double) * max_m);
     d.S = o;    o = align16(o + sizeof(double) * ((size_t)max_m * (max_m + 1) / 2));
     d.bs = o;   o = align16(o + sizeof(double) * max_m);
@@ -77,55 +78,6 @@ NAVBA_HD Dyn dyn_layout(int max_m, int max_ncam, int real_size) {
     d.total = o;
     return d;
 }
-
-template <class Real>
-struct WinArgs {
-    const WinDesc* win;
-    int32_t n_win;
-    const int32_t* order;
-    int32_t* queue;
-    const CamState* cam_init;
-    const int32_t* cam_free;
-    const double* pt_init;
-    const int32_t* pt_free;
-    const int32_t* pt_eoff;
-    const int32_t* edge_cam;
-    const int32_t* edge_fc;   // free index of each edge's camera, or -1
-    const int32_t* edge_pt;
-    const double* edge_uv;
-    double* x[2];
-    Real* pt_vg;
-    Real* pt_lt;
-    Real* edge_w;
-    Real* edge_a;
-    int32_t* cam_list;
-    uint32_t* pairs;
-    CamState* cam_out;
-    double* pt_out;
-    double* trace;
-    int32_t trace_stride;
-    WinStats* stats;
-    double* debug;
-    double debug_lambda;
-    Intr intr;
-    LmOptions lm;
-    int32_t max_m, max_ncam;
-    unsigned long long* phase;  // optional per-phase SM-cycle totals (rank 0 view), or null
-};
-
-NAVBA_HD int tri(int r, int c) { return r * (r + 1) / 2 + c; }  // packed lower index, c <= r
-
-// Per-CTA view of the cluster working on a window.
-struct CC {
-    int rank, csize;
-    int gt, CT;   // thread index / count over the cluster
-    int gw, CW;   // warp index / count over the cluster
-    int lane, wid, nw;
-    SmemHead* s;   // this CTA's head
-    SmemHead* s0;  // rank 0's head (distributed shared memory)
-    double* S0;    // rank 0's reduced system
-    double* bs0;   // rank 0's right-hand side / step
-};
 
 __device__ __forceinline__ void csync() { cg::this_cluster().sync(); }
 
@@ -184,108 +136,6 @@ __device__ double3 cluster_reduce3(CC& c, double a, double b, double d) {
     }
     __syncthreads();
     return make_double3(s.bcast[0], s.bcast[1], s.bcast[2]);
-}
-
-template <class Real>
-__device__ __forceinline__ void cam_real(const CamState& c, Real* o) {
-#pragma unroll
-    for (int k = 0; k < 9; ++k) o[k] = (Real)c.R[k];
-    o[9] = (Real)c.t[0];
-    o[10] = (Real)c.t[1];
-    o[11] = (Real)c.t[2];
-}
-
-// Per-edge 18-value records (W, A) and per-point 12-value records (V|g, L|t), moved with
-// 16-byte vector accesses: FP32 records are padded to 20 floats (80 B), FP64 ones are 144 B.
-template <class Real>
-struct Rec;
-
-template <>
-struct Rec<float> {
-    static constexpr int kEdge = 20;
-    static __device__ __forceinline__ void load18(const float* p, float* v) {
-        const float4* q = reinterpret_cast<const float4*>(p);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const float4 t = q[k];
-            v[4 * k] = t.x; v[4 * k + 1] = t.y; v[4 * k + 2] = t.z; v[4 * k + 3] = t.w;
-        }
-        const float2 t = reinterpret_cast<const float2*>(p)[8];
-        v[16] = t.x;
-        v[17] = t.y;
-    }
-    static __device__ __forceinline__ void store18(float* p, const float* v) {
-        float4* q = reinterpret_cast<float4*>(p);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) q[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
-        reinterpret_cast<float2*>(p)[8] = make_float2(v[16], v[17]);
-    }
-    static __device__ __forceinline__ void load12(const float* p, float* v) {
-        const float4* q = reinterpret_cast<const float4*>(p);
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const float4 t = q[k];
-            v[4 * k] = t.x; v[4 * k + 1] = t.y; v[4 * k + 2] = t.z; v[4 * k + 3] = t.w;
-        }
-    }
-    static __device__ __forceinline__ void store12(float* p, const float* v) {
-        float4* q = reinterpret_cast<float4*>(p);
-#pragma unroll
-        for (int k = 0; k < 3; ++k) q[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
-    }
-};
-
-template <>
-struct Rec<double> {
-    static constexpr int kEdge = 18;
-    static __device__ __forceinline__ void load18(const double* p, double* v) {
-        const double2* q = reinterpret_cast<const double2*>(p);
-#pragma unroll
-        for (int k = 0; k < 9; ++k) {
-            const double2 t = q[k];
-            v[2 * k] = t.x;
-            v[2 * k + 1] = t.y;
-        }
-    }
-    static __device__ __forceinline__ void store18(double* p, const double* v) {
-        double2* q = reinterpret_cast<double2*>(p);
-#pragma unroll
-        for (int k = 0; k < 9; ++k) q[k] = make_double2(v[2 * k], v[2 * k + 1]);
-    }
-    static __device__ __forceinline__ void load12(const double* p, double* v) {
-        const double2* q = reinterpret_cast<const double2*>(p);
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-            const double2 t = q[k];
-            v[2 * k] = t.x;
-            v[2 * k + 1] = t.y;
-        }
-    }
-    static __device__ __forceinline__ void store12(double* p, const double* v) {
-        double2* q = reinterpret_cast<double2*>(p);
-#pragma unroll
-        for (int k = 0; k < 6; ++k) q[k] = make_double2(v[2 * k], v[2 * k + 1]);
-    }
-};
-
-// Cluster-split robust chi2 of the window for cameras `camc` (12 values per camera, precision
-// Cost) and points X; returns this thread's partial sum.
-template <class Cost, class Real>
-__device__ double cost_partial(const WinArgs<Real>& A, const CC& c, const WinDesc& D, const Cost* camc,
-                               const double* X) {
-    double acc = 0.0;
-    const Cost delta = (Cost)A.lm.huber_delta;
-    for (int p = c.gt; p < D.npt; p += c.CT) {
-        const int gp = D.pt0 + p;
-        const Cost Xr[3] = {(Cost)X[4LL * gp], (Cost)X[4LL * gp + 1], (Cost)X[4LL * gp + 2]};
-        const int e1 = A.pt_eoff[gp + 1];
-        for (int e = A.pt_eoff[gp]; e < e1; ++e) {
-            const Cost* cr = camc + 12 * A.edge_cam[e];
-            const Cost z[2] = {(Cost)A.edge_uv[2LL * e], (Cost)A.edge_uv[2LL * e + 1]};
-            acc += edge_cost<Cost>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta);
-        }
-    }
-    return acc;
 }
 
 // Camera-major edge lists of the free cameras and the pair lists of the S blocks.
@@ -395,52 +245,6 @@ __device__ void build_lists(const WinArgs<Real>& A, CC& c, const WinDesc& D) {
     csync();
 }
 
-// Point-major linearization: V_p, g_p, W_e; returns this thread's max |diag V|.
-template <class Real>
-__device__ double linearize_points(const WinArgs<Real>& A, const CC& c, const WinDesc& D, const Real* camr,
-                                   const double* X) {
-    const Real delta = (Real)A.lm.huber_delta;
-    double mx = 0.0;
-    for (int p = c.gt; p < D.npt; p += c.CT) {
-        const int gp = D.pt0 + p;
-        if (A.pt_free[gp] < 0) continue;
-        const Real Xr[3] = {(Real)X[4LL * gp], (Real)X[4LL * gp + 1], (Real)X[4LL * gp + 2]};
-        Real V[6] = {0, 0, 0, 0, 0, 0}, g[3] = {0, 0, 0};
-        const int e1 = A.pt_eoff[gp + 1];
-        for (int e = A.pt_eoff[gp]; e < e1; ++e) {
-            const int cam = A.edge_cam[e];
-            const Real* cr = camr + 12 * cam;
-            const Real z[2] = {(Real)A.edge_uv[2LL * e], (Real)A.edge_uv[2LL * e + 1]};
-            EdgeLin<Real> L;
-            edge_linearize<Real>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta, L);
-            const Real w = L.w;
-            const Real* jp = L.jp;
-            V[0] += w * (jp[0] * jp[0] + jp[3] * jp[3]);
-            V[1] += w * (jp[0] * jp[1] + jp[3] * jp[4]);
-            V[2] += w * (jp[0] * jp[2] + jp[3] * jp[5]);
-            V[3] += w * (jp[1] * jp[1] + jp[4] * jp[4]);
-            V[4] += w * (jp[1] * jp[2] + jp[4] * jp[5]);
-            V[5] += w * (jp[2] * jp[2] + jp[5] * jp[5]);
-            const Real we0 = -w * L.e[0], we1 = -w * L.e[1];
-            g[0] += jp[0] * we0 + jp[3] * we1;
-            g[1] += jp[1] * we0 + jp[4] * we1;
-            g[2] += jp[2] * we0 + jp[5] * we1;
-            if (A.edge_fc[e] >= 0) {
-                Real W[18];
-#pragma unroll
-                for (int r = 0; r < 6; ++r)
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) W[r * 3 + k] = w * (L.jc[r] * jp[k] + L.jc[6 + r] * jp[3 + k]);
-                Rec<Real>::store18(A.edge_w + (long long)Rec<Real>::kEdge * e, W);
-            }
-        }
-        const Real vgv[12] = {V[0], V[1], V[2], V[3], V[4], V[5], g[0], g[1], g[2], Real(0), Real(0), Real(0)};
-        Rec<Real>::store12(A.pt_vg + 12LL * gp, vgv);
-        mx = fmax(mx, fmax(fabs((double)V[0]), fmax(fabs((double)V[3]), fabs((double)V[5]))));
-    }
-    return mx;
-}
-
 // Camera-major linearization: U_c, g_c (warp per free camera) into rank 0; returns max |diag U|.
 template <class Real>
 __device__ double linearize_cameras(const WinArgs<Real>& A, const CC& c, const WinDesc& D, const Real* camr,
@@ -483,51 +287,6 @@ __device__ double linearize_cameras(const WinArgs<Real>& A, const CC& c, const W
         for (int r = 0; r < 6; ++r) mx = fmax(mx, fabs((double)u[tri(r, r)]));
     }
     return mx;
-}
-
-// Per free point: R R^T = V + lambda I, L = R^-1, t = L g, A_e = W_e L^T.  Returns the number of
-// points whose damped block was not positive definite (treated like a failed factorization).
-template <class Real>
-__device__ int schur_points(const WinArgs<Real>& A, const CC& c, const WinDesc& D, double lambda) {
-    const Real lam = (Real)lambda;
-    int bad = 0;
-    for (int p = c.gt; p < D.npt; p += c.CT) {
-        const int gp = D.pt0 + p;
-        if (A.pt_free[gp] < 0) continue;
-        Real vg[12];
-        Rec<Real>::load12(A.pt_vg + 12LL * gp, vg);
-        const Real v00 = vg[0] + lam, v01 = vg[1], v02 = vg[2], v11 = vg[3] + lam, v12 = vg[4], v22 = vg[5] + lam;
-        const Real r00 = sqrt(v00);
-        const Real r10 = v01 / r00, r20 = v02 / r00;
-        const Real d11 = v11 - r10 * r10;
-        const Real r11 = sqrt(d11);
-        const Real r21 = (v12 - r20 * r10) / r11;
-        const Real d22 = v22 - r20 * r20 - r21 * r21;
-        const Real r22 = sqrt(d22);
-        if (!(v00 > Real(0)) || !(d11 > Real(0)) || !(d22 > Real(0))) ++bad;
-        const Real l00 = Real(1) / r00, l11 = Real(1) / r11, l22 = Real(1) / r22;
-        const Real l10 = -r10 * l00 * l11;
-        const Real l21 = -r21 * l11 * l22;
-        const Real l20 = -(r20 * l00 + r21 * l10) * l22;
-        const Real ltv[12] = {l00, l10, l11, l20, l21, l22, l00 * vg[6], l10 * vg[6] + l11 * vg[7],
-                              l20 * vg[6] + l21 * vg[7] + l22 * vg[8], Real(0), Real(0), Real(0)};
-        Rec<Real>::store12(A.pt_lt + 12LL * gp, ltv);
-        const int e1 = A.pt_eoff[gp + 1];
-        for (int e = A.pt_eoff[gp]; e < e1; ++e) {
-            if (A.edge_fc[e] < 0) continue;
-            Real W[18], Ae[18];
-            Rec<Real>::load18(A.edge_w + (long long)Rec<Real>::kEdge * e, W);
-#pragma unroll
-            for (int r = 0; r < 6; ++r) {
-                const Real w0 = W[r * 3 + 0], w1 = W[r * 3 + 1], w2 = W[r * 3 + 2];
-                Ae[r * 3 + 0] = w0 * l00;
-                Ae[r * 3 + 1] = w0 * l10 + w1 * l11;
-                Ae[r * 3 + 2] = w0 * l20 + w1 * l21 + w2 * l22;
-            }
-            Rec<Real>::store18(A.edge_a + (long long)Rec<Real>::kEdge * e, Ae);
-        }
-    }
-    return bad;
 }
 
 // S blocks (warp per block over its pair list) into rank 0's packed S, and b'.
@@ -658,48 +417,6 @@ __device__ void smem_chol_solve(const double* L, const double* rinv, int m, doub
     }
 }
 
-// Trial points dx_p = L^T (t_p - sum A_e^T dx_c); returns this thread's dx^T(lambda dx + g) part.
-template <class Real>
-__device__ double update_points(const WinArgs<Real>& A, const CC& c, const WinDesc& D, double lambda,
-                                const double* dcl, int cur) {
-    const double* Xc = A.x[cur];
-    double* Xt = A.x[cur ^ 1];
-    double sc = 0.0;
-    for (int p = c.gt; p < D.npt; p += c.CT) {
-        const int gp = D.pt0 + p;
-        if (A.pt_free[gp] < 0) continue;
-        Real lt[12];
-        Rec<Real>::load12(A.pt_lt + 12LL * gp, lt);
-        Real u0 = lt[6], u1 = lt[7], u2 = lt[8];
-        const int e1 = A.pt_eoff[gp + 1];
-        for (int e = A.pt_eoff[gp]; e < e1; ++e) {
-            const int a = A.edge_fc[e];
-            if (a < 0) continue;
-            Real Ae[18];
-            Rec<Real>::load18(A.edge_a + (long long)Rec<Real>::kEdge * e, Ae);
-#pragma unroll
-            for (int r = 0; r < 6; ++r) {
-                const Real d = (Real)dcl[6 * a + r];
-                u0 -= Ae[r * 3 + 0] * d;
-                u1 -= Ae[r * 3 + 1] * d;
-                u2 -= Ae[r * 3 + 2] * d;
-            }
-        }
-        // dx = L^T u
-        const Real d0 = lt[0] * u0 + lt[1] * u1 + lt[3] * u2;
-        const Real d1 = lt[2] * u1 + lt[4] * u2;
-        const Real d2 = lt[5] * u2;
-        Xt[4LL * gp + 0] = Xc[4LL * gp + 0] + (double)d0;
-        Xt[4LL * gp + 1] = Xc[4LL * gp + 1] + (double)d1;
-        Xt[4LL * gp + 2] = Xc[4LL * gp + 2] + (double)d2;
-        Real vg[12];
-        Rec<Real>::load12(A.pt_vg + 12LL * gp, vg);
-        sc += (double)d0 * (lambda * (double)d0 + (double)vg[6]) + (double)d1 * (lambda * (double)d1 + (double)vg[7]) +
-              (double)d2 * (lambda * (double)d2 + (double)vg[8]);
-    }
-    return sc;
-}
-
 // Phase timer: thread 0 of rank 0 adds the SM cycles since the previous mark to phase `ph`.
 struct PhaseClock {
     unsigned long long* acc;
@@ -726,7 +443,8 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
     CamState* cams1 = cams0 + A.max_ncam;
     Real* camr = reinterpret_cast<Real*>(smem + dl.camr);
     Real* camr_tr = camr + 12 * A.max_ncam;
-    double* camd = reinterpret_cast<double*>(smem + dl.camd);
+    double* camd = reinterpret_cast<double*>(smem + dl.camd);  // FP64 copies for the cost (mixed form)
+    double* camd_tr = camd + 12 * A.max_ncam;
     double* dcl = reinterpret_cast<double*>(smem + dl.dcl);
     double* S = reinterpret_cast<double*>(smem + dl.S);
     double* bs = reinterpret_cast<double*>(smem + dl.bs);
@@ -740,6 +458,8 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
         cams1[k] = A.cam_init[D.cam0 + k];
         cam_real<Real>(cams0[k], camr + 12 * k);
         cam_real<Real>(cams0[k], camr_tr + 12 * k);
+        cam_real<double>(cams0[k], camd + 12 * k);
+        cam_real<double>(cams0[k], camd_tr + 12 * k);
     }
     for (int p = c.gt; p < D.npt; p += c.CT) {
         const long long gp = D.pt0 + p;
@@ -754,13 +474,9 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
     build_lists(A, c, D);  // ends with a cluster barrier: points are initialized everywhere
     pc.mark(0);
 
-    double chi = cluster_reduce3<false>(c, cost_partial<Real, Real>(A, c, D, camr, A.x[0]), 0.0, 0.0).x;
-    double chi0_fp64 = chi;
-    if (mixed) {
-        for (int k = threadIdx.x; k < D.ncam; k += blockDim.x) cam_real<double>(cams0[k], camd + 12 * k);
-        __syncthreads();
-        chi0_fp64 = cluster_reduce3<false>(c, cost_partial<double, Real>(A, c, D, camd, A.x[0]), 0.0, 0.0).x;
-    }
+    // costs (initial, every trial) are evaluated in FP64 in both forms: they drive the gain ratio
+    double chi = cluster_reduce3<false>(c, cost_partial<double, Real>(A, c, D, camd, A.x[0]), 0.0, 0.0).x;
+    const double chi0_fp64 = chi;
     int iters_done = 0, acc = 0, rej = 0, term = NAV_BA_TERM_ITERATIONS;
     double lambda = 0.0, nu = 2.0;
     pc.mark(1);
@@ -822,6 +538,7 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
                 CamState* ccur = cur == 0 ? cams0 : cams1;
                 CamState* ctr = cur == 0 ? cams1 : cams0;
                 Real* crt = cur == 0 ? camr_tr : camr;
+                double* cdt = cur == 0 ? camd_tr : camd;
                 double sc = 0.0;
                 for (int k = threadIdx.x; k < D.ncam; k += blockDim.x) {
                     const int a = A.cam_free[D.cam0 + k];
@@ -832,12 +549,13 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
                             for (int r = 0; r < 6; ++r) sc += dcl[6 * a + r] * (lambda * dcl[6 * a + r] + s.U[a][21 + r]);
                     }
                     cam_real<Real>(ctr[k], crt + 12 * k);
+                    cam_real<double>(ctr[k], cdt + 12 * k);
                 }
                 __syncthreads();
                 sc += update_points<Real>(A, c, D, lambda, dcl, cur);
                 pc.mark(7);
                 const double3 red = cluster_reduce3<false>(
-                    c, cost_partial<Real, Real>(A, c, D, crt, A.x[cur ^ 1]), sc, 0.0);
+                    c, cost_partial<double, Real>(A, c, D, cdt, A.x[cur ^ 1]), sc, 0.0);
                 double chi_new = red.x;
                 double scale = red.y;
                 if (!ok) chi_new = DBL_MAX;
@@ -870,12 +588,8 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
     }
     const int cur = s.cur;
     CamState* cfin = cur == 0 ? cams0 : cams1;
-    double chi_final = chi;
-    if (mixed && !bad) {
-        for (int k = threadIdx.x; k < D.ncam; k += blockDim.x) cam_real<double>(cfin[k], camd + 12 * k);
-        __syncthreads();
-        chi_final = cluster_reduce3<false>(c, cost_partial<double, Real>(A, c, D, camd, A.x[cur]), 0.0, 0.0).x;
-    }
+    const double chi_final = chi;
+    (void)mixed;
     if (c.rank == 0)
         for (int k = threadIdx.x; k < D.ncam; k += blockDim.x) A.cam_out[D.cam0 + k] = cfin[k];
     for (int p = c.gt; p < D.npt; p += c.CT) {

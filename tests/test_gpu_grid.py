@@ -1,0 +1,75 @@
+"""GPU parity tests of the grid engine (one large problem on the whole GPU: more than 24 free
+cameras) against the CPU oracle, with the same tolerances as the window engine: reduced-system
+pattern bit-exact and values within 1e-10 relative (FP64), final cost within 1e-6 relative after
+a fixed number of LM iterations, and the mixed form within 1e-6 of the FP64 oracle."""
+import numpy as np
+import pytest
+
+from nav24_gb300 import abi
+from nav24_gb300.synth import Synth, workload_options
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return abs(a - b) / abs(b)
+
+
+def grid_problem():
+    return Synth(1, n_cams=50, n_points=4000, seed=77).window(0)  # 49 free cameras
+
+
+def test_grid_reduced_system_matches_oracle(ctx):
+    p = grid_problem()
+    o = abi.default_options(robust=1, huber_delta=2.0)
+    gS, gb, gidx = ctx.reduced_system(p, o, 1e-2)
+    oS, ob, oidx = oracle.reduced_system(p, o, 1e-2)
+    assert np.array_equal(gidx, oidx)
+    nf = oS.shape[0] // 6
+    blk = lambda S: np.array([[np.any(S[6 * a:6 * a + 6, 6 * b:6 * b + 6] != 0) for b in range(nf)] for a in range(nf)])
+    assert np.array_equal(blk(gS), blk(oS))
+    assert np.max(np.abs(gS - oS)) / np.max(np.abs(oS)) < 1e-10
+    assert np.max(np.abs(gb - ob)) / np.max(np.abs(ob)) < 1e-10
+
+
+@pytest.mark.parametrize("robust", [0, 1])
+def test_grid_fp64_solve_matches_oracle(ctx, robust):
+    p = grid_problem()
+    o = abi.default_options(iterations=10, robust=robust, huber_delta=2.0)
+    g = ctx.solve(p, o)
+    r = oracle.solve(p, o, n_threads=8)
+    assert g.status == abi.OK and g.stats["n_free_cams"] == 49
+    assert rel(g.stats["initial_cost"], r.stats["initial_cost"]) < 1e-12
+    assert rel(g.stats["final_cost"], r.stats["final_cost"]) < 1e-6
+    n = min(len(g.cost_trace), len(r.cost_trace))
+    assert np.max(np.abs(g.cost_trace[:n] - r.cost_trace[:n]) / r.cost_trace[:n]) < 1e-6
+    assert np.allclose(g.points, r.points, rtol=0, atol=1e-6)
+
+
+def test_grid_mixed_reaches_fp64_cost(ctx):
+    p = grid_problem()
+    o = abi.default_options(iterations=20, robust=1, huber_delta=2.0)
+    r = oracle.solve(p, o, n_threads=8)
+    o.precision = abi.MIXED
+    g = ctx.solve(p, o)
+    assert rel(g.stats["final_cost"], r.stats["final_cost"]) < 1e-6
+
+
+def test_cap_workload_fp64(ctx):
+    p = Synth(3, n_points=3000).window(0)  # 50 cameras on a sphere cap, dense reduced system
+    o = workload_options(3)
+    g = ctx.solve(p, o)
+    r = oracle.solve(p, o, n_threads=8)
+    assert rel(g.stats["final_cost"], r.stats["final_cost"]) < 1e-6
+
+
+def test_grid_workload_full_size(ctx):
+    """The 200-camera grid workload (family 1): FP64 and mixed forms against the FP64 oracle."""
+    p = Synth(1).window(0)
+    o = workload_options(1)
+    r = oracle.solve(p, o, n_threads=16)
+    g = ctx.solve(p, o)
+    assert rel(g.stats["final_cost"], r.stats["final_cost"]) < 1e-6
+    g = ctx.solve(p, workload_options(1, abi.MIXED))
+    assert rel(g.stats["final_cost"], r.stats["final_cost"]) < 1e-6
