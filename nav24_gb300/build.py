@@ -21,9 +21,12 @@ BUILD = PKG / "_build"
 INCLUDE = ROOT / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-              "-Xptxas", "-warn-spills"]
-CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-Wextra"]
+# Host code is compiled without floating-point contraction (-ffp-contract=off) so that the synthetic
+# problems and every host-side floating-point result are the same on x86-64 and aarch64 (gcc fuses
+# a*b+c into an FMA by default on aarch64 only).
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
+CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra"]
 
 PRODUCT_CU = ["nav_ba_api.cu", "window_engine.cu", "grid_engine.cu", "noalloc.cu"]
 PRODUCT_CPP = ["structure.cpp"]
@@ -48,7 +51,9 @@ def _newer(target: Path, deps: list[Path]) -> bool:
 
 
 def _headers() -> list[Path]:
-    return sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.hpp")) + sorted(INCLUDE.glob("*.h"))
+    # this file is a dependency too: a change of flags rebuilds everything
+    return (sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.hpp")) + sorted(INCLUDE.glob("*.h")) +
+            [Path(__file__).resolve()])
 
 
 def _run(cmd: list[str]) -> None:

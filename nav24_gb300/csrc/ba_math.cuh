@@ -153,6 +153,7 @@ struct EdgeLin {
     Real e[2];
     Real jc[12];  // 2x6, rotation first
     Real jp[6];   // 2x3
+    Real jk[4];   // 2x2 d e / d (k1, k2) (radial model; zero for the pinhole)
     Real w;       // rho'(e^T e)
     double rho;   // rho(e^T e)
 };
@@ -179,9 +180,10 @@ NAVBA_HD void transform(const Real* R, const Real* t, const Real* X, Real* Xc) {
     Xc[2] = R[6] * X[0] + R[7] * X[1] + R[8] * X[2] + t[2];
 }
 
-// Projection pi(Xc) and, if J != nullptr, d pi / d Xc (2x3).
+// Projection pi(Xc) and, if J != nullptr, d pi / d Xc (2x3); if Jk != nullptr (radial model),
+// d pi / d (k1, k2) (2x2).
 template <class Real>
-NAVBA_HD void project(const Intr& in, const Real* Xc, Real* uv, Real* J) {
+NAVBA_HD void project(const Intr& in, const Real* Xc, Real* uv, Real* J, Real* Jk = nullptr) {
     const Real x = Xc[0], y = Xc[1], z = Xc[2];
     const Real fx = (Real)in.fx, fy = (Real)in.fy, cx = (Real)in.cx, cy = (Real)in.cy;
     const Real iz = Real(1) / z;  // one division per edge; the rest are products
@@ -207,6 +209,10 @@ NAVBA_HD void project(const Intr& in, const Real* Xc, Real* uv, Real* J) {
             J[0] = a00 * iz; J[1] = a01 * iz; J[2] = -(a00 * xn + a01 * yn) * iz;
             J[3] = a10 * iz; J[4] = a11 * iz; J[5] = -(a10 * xn + a11 * yn) * iz;
         }
+        if (Jk) {
+            Jk[0] = fx * xn * r2; Jk[1] = fx * xn * r2 * r2;
+            Jk[2] = fy * yn * r2; Jk[3] = fy * yn * r2 * r2;
+        }
     }
 }
 
@@ -215,11 +221,12 @@ NAVBA_HD void project(const Intr& in, const Real* Xc, Real* uv, Real* J) {
 template <class Real>
 NAVBA_HD void edge_linearize(const Intr& in, const Real* R, const Real* t, const Real* X,
                              const Real* z, bool robust, Real delta, EdgeLin<Real>& L) {
-    Real Xc[3], uv[2], J[6];
+    Real Xc[3], uv[2], J[6], Jk[4] = {Real(0), Real(0), Real(0), Real(0)};
     transform(R, t, X, Xc);
-    project(in, Xc, uv, J);
+    project(in, Xc, uv, J, in.model == 1 ? Jk : nullptr);
     L.e[0] = z[0] - uv[0];
     L.e[1] = z[1] - uv[1];
+    L.jk[0] = -Jk[0]; L.jk[1] = -Jk[1]; L.jk[2] = -Jk[2]; L.jk[3] = -Jk[3];
     huber<Real>(L.e[0] * L.e[0] + L.e[1] * L.e[1], robust, delta, L.rho, L.w);
     Real P[6];
     for (int k = 0; k < 6; ++k) P[k] = -J[k];

@@ -37,10 +37,13 @@ struct LmOptions {
     int32_t iterations;
     int32_t max_trials;
     int32_t robust;
-    int32_t pad;
+    int32_t solver;          // NAV_BA_SOLVER_CHOLESKY / NAV_BA_SOLVER_PCG
     double huber_delta;
     double initial_lambda;
     double tau;
+    int32_t optimize_k;      // shared radial k1, k2 are free (PCG only)
+    int32_t pcg_max_iterations;
+    double pcg_tolerance;
 };
 
 // A batch of windows resident on the device (inputs, scratch and outputs).
@@ -143,6 +146,8 @@ struct GridResult {
     std::vector<double> trace;
     std::vector<CamState> cams;
     std::vector<double> points;  // [npt][4]
+    double k1 = 0, k2 = 0;       // final distortion (optimize_k)
+    int32_t pcg_iterations = 0;
 };
 
 // Solve one large problem on the whole GPU.  debug_S != nullptr: stop after assembling the

@@ -421,6 +421,440 @@ __global__ void k_init_points(const double* init, double* x0, double* x1, int np
     }
 }
 
+
+// ---- shared radial distortion (k1, k2) and the PCG solver ---------------------------------
+
+// Block sums of N per-thread values; thread 0 writes out[N * blockIdx.x + k].
+template <int N>
+__device__ void block_partials(double (&v)[N], double* out) {
+    __shared__ double red[32 * N];
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(kFullG, v[k], o);
+    if ((threadIdx.x & 31) == 0)
+#pragma unroll
+        for (int k = 0; k < N; ++k) red[N * (threadIdx.x >> 5) + k] = v[k];
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int k = 0; k < N; ++k) {
+            double r = 0.0;
+            for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r += red[N * i + k];
+            out[N * blockIdx.x + k] = r;
+        }
+}
+
+// Intrinsics rows of H: per free point Kp = sum w Jk^T Jp (2x3); block sums of H_kk (3 unique)
+// and g_k (2) over every edge (the shared intrinsics are a free vertex of every edge).
+template <class Real>
+__global__ void k_lin_intr_points(WinArgs<Real> A, WinDesc D, const Real* camr, const double* X, Real* pt_kp,
+                                  double* part) {
+    const CC c = grid_view();
+    const Real delta = (Real)A.lm.huber_delta;
+    double acc[5] = {0, 0, 0, 0, 0};
+    for (int p = c.gt; p < D.npt; p += c.CT) {
+        const bool fp = A.pt_free[p] >= 0;
+        const Real Xr[3] = {(Real)X[4LL * p], (Real)X[4LL * p + 1], (Real)X[4LL * p + 2]};
+        Real kp[6] = {0, 0, 0, 0, 0, 0};
+        for (int e = A.pt_eoff[p]; e < A.pt_eoff[p + 1]; ++e) {
+            const Real* cr = camr + 12 * A.edge_cam[e];
+            const Real z[2] = {(Real)A.edge_uv[2LL * e], (Real)A.edge_uv[2LL * e + 1]};
+            EdgeLin<Real> L;
+            edge_linearize<Real>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta, L);
+            const Real w = L.w;
+            const Real* jk = L.jk;  // rows: residual u, v; columns: k1, k2
+            acc[0] += (double)(w * (jk[0] * jk[0] + jk[2] * jk[2]));
+            acc[1] += (double)(w * (jk[0] * jk[1] + jk[2] * jk[3]));
+            acc[2] += (double)(w * (jk[1] * jk[1] + jk[3] * jk[3]));
+            acc[3] += (double)(-w * (jk[0] * L.e[0] + jk[2] * L.e[1]));
+            acc[4] += (double)(-w * (jk[1] * L.e[0] + jk[3] * L.e[1]));
+            if (fp)
+#pragma unroll
+                for (int r = 0; r < 2; ++r)
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) kp[r * 3 + q] += w * (jk[r] * L.jp[q] + jk[2 + r] * L.jp[3 + q]);
+        }
+        if (fp) {
+            const Real v[12] = {kp[0], kp[1], kp[2], kp[3], kp[4], kp[5], 0, 0, 0, 0, 0, 0};
+            Rec<Real>::store12(pt_kp + 12LL * p, v);
+        }
+    }
+    block_partials<5>(acc, part);
+}
+
+// Camera-intrinsics blocks: per work item sum w Jc^T Jk (6x2) -> hpart[item] (12 values).
+template <class Real>
+__global__ void k_lin_intr_cams(WinArgs<Real> A, const int4* items, int n_items, const int32_t* cam_list,
+                                const int32_t* fcam, const Real* camr, const double* X, double* hpart) {
+    const CC c = grid_view();
+    const Real delta = (Real)A.lm.huber_delta;
+    for (int it = c.gw; it < n_items; it += c.CW) {
+        const int4 wi = items[it];
+        const Real* cr = camr + 12 * fcam[wi.x];
+        Real h[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) h[k] = Real(0);
+        for (int i = c.lane; i < wi.z; i += 32) {
+            const int e = cam_list[wi.y + i];
+            const int gp = A.edge_pt[e];
+            const Real Xr[3] = {(Real)X[4LL * gp], (Real)X[4LL * gp + 1], (Real)X[4LL * gp + 2]};
+            const Real z[2] = {(Real)A.edge_uv[2LL * e], (Real)A.edge_uv[2LL * e + 1]};
+            EdgeLin<Real> L;
+            edge_linearize<Real>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta, L);
+#pragma unroll
+            for (int r = 0; r < 6; ++r)
+#pragma unroll
+                for (int q = 0; q < 2; ++q) h[r * 2 + q] += L.w * (L.jc[r] * L.jk[q] + L.jc[6 + r] * L.jk[2 + q]);
+        }
+#pragma unroll
+        for (int k = 0; k < 12; ++k)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) h[k] += __shfl_xor_sync(kFullG, h[k], o);
+#pragma unroll
+        for (int k = 0; k < 12; ++k)
+            if ((k & 31) == c.lane) hpart[12LL * it + k] = (double)h[k];
+    }
+}
+
+// Per-camera sums of item partials (stride `stride`, first `nval` values) in item order.
+__global__ void k_reduce_items(const double* part, int stride, int nval, const int32_t* item_off, int nfc, double* out,
+                               int out_stride) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nfc * nval) return;
+    const int a = idx / nval, k = idx % nval;
+    double s = 0.0;
+    for (int it = item_off[a]; it < item_off[a + 1]; ++it) s += part[(long long)stride * it + k];
+    out[(long long)out_stride * a + k] = s;
+}
+
+// Per free point: B = Kp L^T (2x3); block sums of B B^T (3 unique) and B t (2).
+template <class Real>
+__global__ void k_schur_intr_points(WinArgs<Real> A, WinDesc D, const Real* pt_kp, Real* pt_b, double* part) {
+    const CC c = grid_view();
+    double acc[5] = {0, 0, 0, 0, 0};
+    for (int p = c.gt; p < D.npt; p += c.CT) {
+        if (A.pt_free[p] < 0) continue;
+        Real kp[12], lt[12];
+        Rec<Real>::load12(pt_kp + 12LL * p, kp);
+        Rec<Real>::load12(A.pt_lt + 12LL * p, lt);
+        // L packed lower: l00 lt[0], l10 lt[1], l11 lt[2], l20 lt[3], l21 lt[4], l22 lt[5]; B = Kp L^T
+        Real b[6];
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const Real k0 = kp[r * 3], k1 = kp[r * 3 + 1], k2 = kp[r * 3 + 2];
+            b[r * 3 + 0] = k0 * lt[0];
+            b[r * 3 + 1] = k0 * lt[1] + k1 * lt[2];
+            b[r * 3 + 2] = k0 * lt[3] + k1 * lt[4] + k2 * lt[5];
+        }
+        const Real v[12] = {b[0], b[1], b[2], b[3], b[4], b[5], 0, 0, 0, 0, 0, 0};
+        Rec<Real>::store12(pt_b + 12LL * p, v);
+        acc[0] += (double)(b[0] * b[0] + b[1] * b[1] + b[2] * b[2]);
+        acc[1] += (double)(b[0] * b[3] + b[1] * b[4] + b[2] * b[5]);
+        acc[2] += (double)(b[3] * b[3] + b[4] * b[4] + b[5] * b[5]);
+        acc[3] += (double)(b[0] * lt[6] + b[1] * lt[7] + b[2] * lt[8]);
+        acc[4] += (double)(b[3] * lt[6] + b[4] * lt[7] + b[5] * lt[8]);
+    }
+    block_partials<5>(acc, part);
+}
+
+// Preconditioner and right-hand side, per work item over the camera lists: sum A A^T (21) and
+// sum A t (6) -> part[28 * item].
+template <class Real>
+__global__ void k_pcg_diag_items(WinArgs<Real> A, const int4* items, int n_items, const int32_t* cam_list, double* part) {
+    const CC c = grid_view();
+    for (int it = c.gw; it < n_items; it += c.CW) {
+        const int4 wi = items[it];
+        Real u[27];
+#pragma unroll
+        for (int k = 0; k < 27; ++k) u[k] = Real(0);
+        for (int i = c.lane; i < wi.z; i += 32) {
+            const int e = cam_list[wi.y + i];
+            const int gp = A.edge_pt[e];
+            if (A.pt_free[gp] < 0) continue;
+            Real a[18], lt[12];
+            Rec<Real>::load18(A.edge_a + (long long)Rec<Real>::kEdge * e, a);
+            Rec<Real>::load12(A.pt_lt + 12LL * gp, lt);
+#pragma unroll
+            for (int r = 0; r < 6; ++r) {
+#pragma unroll
+                for (int q = 0; q <= r; ++q) u[tri(r, q)] += a[r * 3] * a[q * 3] + a[r * 3 + 1] * a[q * 3 + 1] + a[r * 3 + 2] * a[q * 3 + 2];
+                u[21 + r] += a[r * 3] * lt[6] + a[r * 3 + 1] * lt[7] + a[r * 3 + 2] * lt[8];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 27; ++k)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) u[k] += __shfl_xor_sync(kFullG, u[k], o);
+#pragma unroll
+        for (int k = 0; k < 27; ++k)
+            if ((k & 31) == c.lane) part[28LL * it + k] = (double)u[k];
+    }
+}
+
+// Per free camera: P_a = U_a + lambda I - sum A A^T, FP64 Cholesky (packed lower L, with 1/L_jj in
+// the diagonal slots of pinv); b'_a = g_a - sum A t.  pc[28 a]: 21 L entries + 6 inverse diagonal.
+__global__ void k_pcg_precond(const double* U, const double* aat, int nfc, double lambda, double* pc, double* b,
+                              int32_t* ok) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nfc) return;
+    double P[21];
+    for (int k = 0; k < 21; ++k) P[k] = U[28LL * a + k] - aat[28LL * a + k];
+    for (int r = 0; r < 6; ++r) P[tri(r, r)] += lambda;
+    double rinv[6];
+    bool good = true;
+    for (int j = 0; j < 6; ++j) {
+        double d = P[tri(j, j)];
+        for (int k = 0; k < j; ++k) d -= P[tri(j, k)] * P[tri(j, k)];
+        if (!(d > 0.0) || !isfinite(d)) {
+            good = false;
+            d = 1.0;
+        }
+        const double r = rsqrt(d);
+        P[tri(j, j)] = d * r;
+        rinv[j] = r;
+        for (int i = j + 1; i < 6; ++i) {
+            double v = P[tri(i, j)];
+            for (int k = 0; k < j; ++k) v -= P[tri(i, k)] * P[tri(j, k)];
+            P[tri(i, j)] = v * r;
+        }
+    }
+    for (int k = 0; k < 21; ++k) pc[28LL * a + k] = P[k];
+    for (int k = 0; k < 6; ++k) pc[28LL * a + 21 + k] = rinv[k];
+    for (int k = 0; k < 6; ++k) b[6 * a + k] = U[28LL * a + 21 + k] - aat[28LL * a + 21 + k];
+    if (!good) ok[0] = 0;
+}
+
+// t2_p = sum_{edges with a free camera} A^T x_c + B^T x_k (free points); block sums of B t2 (2).
+template <class Real>
+__global__ void k_pcg_points(WinArgs<Real> A, WinDesc D, const double* x, int nk, const Real* pt_b, Real* pt_t2,
+                             double* part) {
+    const CC c = grid_view();
+    const int kb = 6 * D.nfc;
+    double acc[2] = {0, 0};
+    for (int p = c.gt; p < D.npt; p += c.CT) {
+        if (A.pt_free[p] < 0) continue;
+        Real t0 = 0, t1 = 0, t2 = 0;
+        for (int e = A.pt_eoff[p]; e < A.pt_eoff[p + 1]; ++e) {
+            const int a = A.edge_fc[e];
+            if (a < 0) continue;
+            Real ae[18];
+            Rec<Real>::load18(A.edge_a + (long long)Rec<Real>::kEdge * e, ae);
+#pragma unroll
+            for (int r = 0; r < 6; ++r) {
+                const Real xv = (Real)x[6 * a + r];
+                t0 += ae[r * 3] * xv;
+                t1 += ae[r * 3 + 1] * xv;
+                t2 += ae[r * 3 + 2] * xv;
+            }
+        }
+        if (nk) {
+            Real b[12];
+            Rec<Real>::load12(pt_b + 12LL * p, b);
+            const Real k1 = (Real)x[kb], k2 = (Real)x[kb + 1];
+            t0 += b[0] * k1 + b[3] * k2;
+            t1 += b[1] * k1 + b[4] * k2;
+            t2 += b[2] * k1 + b[5] * k2;
+            acc[0] += (double)(b[0] * t0 + b[1] * t1 + b[2] * t2);
+            acc[1] += (double)(b[3] * t0 + b[4] * t1 + b[5] * t2);
+        }
+        pt_t2[4LL * p] = t0;
+        pt_t2[4LL * p + 1] = t1;
+        pt_t2[4LL * p + 2] = t2;
+    }
+    block_partials<2>(acc, part);
+}
+
+// Per work item: sum A_i t2_{p(i)} (6) -> part[8 * item].
+template <class Real>
+__global__ void k_pcg_cams(WinArgs<Real> A, const int4* items, int n_items, const int32_t* cam_list, const Real* pt_t2,
+                           double* part) {
+    const CC c = grid_view();
+    for (int it = c.gw; it < n_items; it += c.CW) {
+        const int4 wi = items[it];
+        Real y[6] = {0, 0, 0, 0, 0, 0};
+        for (int i = c.lane; i < wi.z; i += 32) {
+            const int e = cam_list[wi.y + i];
+            const int gp = A.edge_pt[e];
+            if (A.pt_free[gp] < 0) continue;
+            Real ae[18];
+            Rec<Real>::load18(A.edge_a + (long long)Rec<Real>::kEdge * e, ae);
+            const Real t0 = pt_t2[4LL * gp], t1 = pt_t2[4LL * gp + 1], t2 = pt_t2[4LL * gp + 2];
+#pragma unroll
+            for (int r = 0; r < 6; ++r) y[r] += ae[r * 3] * t0 + ae[r * 3 + 1] * t1 + ae[r * 3 + 2] * t2;
+        }
+#pragma unroll
+        for (int k = 0; k < 6; ++k)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) y[k] += __shfl_xor_sync(kFullG, y[k], o);
+        if (c.lane < 6)
+#pragma unroll
+            for (int k = 0; k < 6; ++k)
+                if (k == c.lane) part[8LL * it + k] = (double)y[k];
+    }
+}
+
+// PCG state in one device block: vectors x r z p q of length mt, scalars.
+struct PcgVec {
+    double *x, *r, *z, *p, *q;
+    double* sc;  // [0] rz, [1] r.r, [2] b.b
+};
+
+__device__ double cta_sum(double v) {
+    __shared__ double red[33];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFullG, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double r = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r += red[i];
+        red[32] = r;
+    }
+    __syncthreads();
+    return red[32];
+}
+
+// z = M^-1 r: per camera the 6x6 Cholesky solve, the 2x2 intrinsics block (host-factored pk).
+__device__ void pcg_precond_apply(const double* pc, int nfc, int nk, const double* pk, const double* r, double* z) {
+    for (int a = threadIdx.x; a < nfc; a += blockDim.x) {
+        const double* L = pc + 28LL * a;
+        const double* ri = L + 21;
+        double v[6];
+        for (int i = 0; i < 6; ++i) {
+            double s = r[6 * a + i];
+            for (int k = 0; k < i; ++k) s -= L[tri(i, k)] * v[k];
+            v[i] = s * ri[i];
+        }
+        for (int i = 5; i >= 0; --i) {
+            double s = v[i];
+            for (int k = i + 1; k < 6; ++k) s -= L[tri(k, i)] * v[k];
+            v[i] = s * ri[i];
+        }
+        for (int i = 0; i < 6; ++i) z[6 * a + i] = v[i];
+    }
+    if (nk && threadIdx.x == 0) {
+        // pk: 2x2 lower Cholesky l00 l10 l11 of the intrinsics block
+        const int kb = 6 * nfc;
+        const double y0 = r[kb] / pk[0];
+        const double y1 = (r[kb + 1] - pk[1] * y0) / pk[2];
+        const double x1 = y1 / pk[2];
+        const double x0 = (y0 - pk[1] * x1) / pk[0];
+        z[kb] = x0;
+        z[kb + 1] = x1;
+    }
+}
+
+// x = 0, r = b, z = M^-1 r, p = z, rz = r.z, r.r, b.b (one CTA).
+__global__ void k_pcg_init(PcgVec v, const double* b, int mt, const double* pc, int nfc, int nk, const double* pk) {
+    for (int i = threadIdx.x; i < mt; i += blockDim.x) {
+        v.x[i] = 0.0;
+        v.r[i] = b[i];
+    }
+    __syncthreads();
+    pcg_precond_apply(pc, nfc, nk, pk, v.r, v.z);
+    __syncthreads();
+    double rz = 0.0, rr = 0.0;
+    for (int i = threadIdx.x; i < mt; i += blockDim.x) {
+        v.p[i] = v.z[i];
+        rz += v.r[i] * v.z[i];
+        rr += v.r[i] * v.r[i];
+    }
+    rz = cta_sum(rz);
+    rr = cta_sum(rr);
+    if (threadIdx.x == 0) {
+        v.sc[0] = rz;
+        v.sc[1] = rr;
+        v.sc[2] = rr;
+    }
+}
+
+// q = S p from the item / point partials, then one PCG update (one CTA).
+__global__ void k_pcg_step(PcgVec v, int mt, int nfc, int nk, const double* U, const double* Hck, const double* kk,
+                           double lambda, const double* cam_part, const int32_t* item_off, const double* pt_part,
+                           int n_pt_blocks, const double* pc, const double* pk) {
+    const int kb = 6 * nfc;
+    double pk0 = 0.0, pk1 = 0.0;
+    if (nk) {
+        pk0 = v.p[kb];
+        pk1 = v.p[kb + 1];
+    }
+    for (int a = threadIdx.x; a < nfc; a += blockDim.x) {
+        const double* Ua = U + 28LL * a;
+        double pa[6];
+        for (int r = 0; r < 6; ++r) pa[r] = v.p[6 * a + r];
+        for (int r = 0; r < 6; ++r) {
+            double s = lambda * pa[r];
+            for (int q = 0; q < 6; ++q) s += Ua[r >= q ? tri(r, q) : tri(q, r)] * pa[q];
+            for (int it = item_off[a]; it < item_off[a + 1]; ++it) s -= cam_part[8LL * it + r];
+            if (nk) s += Hck[12LL * a + r * 2] * pk0 + Hck[12LL * a + r * 2 + 1] * pk1;
+            v.q[6 * a + r] = s;
+        }
+    }
+    if (nk) {
+        // q_k = (Kk + lambda) p_k + sum_a Hck_a^T p_a - sum_p B t2
+        double s0 = 0.0, s1 = 0.0;
+        for (int a = threadIdx.x; a < nfc; a += blockDim.x)
+            for (int r = 0; r < 6; ++r) {
+                s0 += Hck[12LL * a + r * 2] * v.p[6 * a + r];
+                s1 += Hck[12LL * a + r * 2 + 1] * v.p[6 * a + r];
+            }
+        s0 = cta_sum(s0);
+        s1 = cta_sum(s1);
+        if (threadIdx.x == 0) {
+            double b0 = 0.0, b1 = 0.0;
+            for (int k = 0; k < n_pt_blocks; ++k) {
+                b0 += pt_part[2 * k];
+                b1 += pt_part[2 * k + 1];
+            }
+            v.q[kb] = (kk[0] + lambda) * pk0 + kk[1] * pk1 + s0 - b0;
+            v.q[kb + 1] = kk[1] * pk0 + (kk[2] + lambda) * pk1 + s1 - b1;
+        }
+    }
+    __syncthreads();
+    double pq = 0.0;
+    for (int i = threadIdx.x; i < mt; i += blockDim.x) pq += v.p[i] * v.q[i];
+    pq = cta_sum(pq);
+    const double rz = v.sc[0];
+    const double alpha = pq != 0.0 ? rz / pq : 0.0;
+    for (int i = threadIdx.x; i < mt; i += blockDim.x) {
+        v.x[i] += alpha * v.p[i];
+        v.r[i] -= alpha * v.q[i];
+    }
+    __syncthreads();
+    pcg_precond_apply(pc, nfc, nk, pk, v.r, v.z);
+    __syncthreads();
+    double rzn = 0.0, rr = 0.0;
+    for (int i = threadIdx.x; i < mt; i += blockDim.x) {
+        rzn += v.r[i] * v.z[i];
+        rr += v.r[i] * v.r[i];
+    }
+    rzn = cta_sum(rzn);
+    rr = cta_sum(rr);
+    const double beta = rz != 0.0 ? rzn / rz : 0.0;
+    for (int i = threadIdx.x; i < mt; i += blockDim.x) v.p[i] = v.z[i] + beta * v.p[i];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        v.sc[0] = rzn;
+        v.sc[1] = rr;
+    }
+}
+
+// t_p -= B_p^T dk before the point back-substitution (the distortion part of the step).
+template <class Real>
+__global__ void k_fold_intr(WinArgs<Real> A, WinDesc D, const Real* pt_b, double dk1, double dk2) {
+    const CC c = grid_view();
+    for (int p = c.gt; p < D.npt; p += c.CT) {
+        if (A.pt_free[p] < 0) continue;
+        Real b[12];
+        Rec<Real>::load12(pt_b + 12LL * p, b);
+        Real* lt = A.pt_lt + 12LL * p;
+        lt[6] -= b[0] * (Real)dk1 + b[3] * (Real)dk2;
+        lt[7] -= b[1] * (Real)dk1 + b[4] * (Real)dk2;
+        lt[8] -= b[2] * (Real)dk1 + b[5] * (Real)dk2;
+    }
+}
+
 // ---- host side ---------------------------------------------------------------------------
 
 struct GridHost {
@@ -591,16 +1025,31 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     int32_t* d_boff = dv.alloc<int32_t>(g.boff.size());
     int2* d_pairs = dv.alloc<int2>(g.pairs.size());
     int32_t* d_tfirst = dv.alloc<int32_t>(g.tfirst.size());
-    double* d_S = dv.alloc<double>((size_t)std::max(1, m) * std::max(1, m));
-    double* d_bs = dv.alloc<double>(std::max(1, m));
+    const bool pcg = lm.solver == NAV_BA_SOLVER_PCG && !debug_S;
+    const int nk = (lm.optimize_k && intr.model == 1) ? 2 : 0;
+    const int mt = m + nk;
+    double* d_S = dv.alloc<double>(pcg ? 1 : (size_t)std::max(1, m) * std::max(1, m));
+    double* d_bs = dv.alloc<double>(std::max(1, mt));
     double* d_rinv = dv.alloc<double>(std::max(1, m));
     int32_t* d_ok = dv.alloc<int32_t>(1);
     const int TB = 256;
     const int nsm_blocks = 152 * 4;
     const int pblocks = std::max(1, std::min(nsm_blocks, (np + TB - 1) / TB));
     const int cblocks = std::max(1, (nc + TB - 1) / TB);
-    const int npart = std::max(pblocks, std::max(cblocks, (nfc * 27 + TB - 1) / TB + 1));
+    const int npart = std::max(5 * pblocks, std::max(cblocks, (nfc * 27 + TB - 1) / TB + 1));
     double* d_part = dv.alloc<double>(npart);
+    // PCG and distortion buffers
+    const int n_items = (int)g.items.size();
+    Real* d_kp = nk ? dv.alloc<Real>(12LL * np) : nullptr;
+    Real* d_pb = nk ? dv.alloc<Real>(12LL * np) : nullptr;
+    double* d_hpart = nk ? dv.alloc<double>(12LL * n_items) : nullptr;
+    double* d_Hck = dv.alloc<double>(12LL * std::max(1, nfc));
+    Real* d_t2 = pcg ? dv.alloc<Real>(4LL * np) : nullptr;
+    double* d_aat = pcg ? dv.alloc<double>(28LL * std::max(1, nfc)) : nullptr;
+    double* d_pc = pcg ? dv.alloc<double>(28LL * std::max(1, nfc)) : nullptr;
+    double* d_camp = pcg ? dv.alloc<double>(8LL * n_items) : nullptr;
+    double* d_vec = pcg ? dv.alloc<double>(5LL * std::max(1, mt) + 8) : nullptr;
+    double* d_kvals = dv.alloc<double>(8);  // [0..2] H_kk + lambda-free, [3..5] pk (2x2 Cholesky)
     if (dv.err != cudaSuccess) return dv.err;
     std::vector<int32_t> edge_fc(ne);
     for (int e = 0; e < ne; ++e) edge_fc[e] = h.cam_free[h.edge_cam[e]];
@@ -648,6 +1097,10 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     CamState* cams[2] = {d_cams0, d_cams1};
     Real* camr[2] = {d_camr0, d_camr1};
     const bool mixed = sizeof(Real) == 4;
+    (void)mixed;
+    double kcur[2] = {intr.k1, intr.k2};  // current shared distortion (free when nk == 2)
+    double Kk[3] = {0, 0, 0}, gk[2] = {0, 0};
+    int pcg_total = 0;
     std::vector<double> hpart(npart);
     auto sum_part = [&](int n, bool mx) -> double {
         if (e != cudaSuccess) return 0.0;
@@ -675,6 +1128,14 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     // costs (initial, every trial) are evaluated in FP64 in both forms: they drive the gain ratio
     double chi = cost_of(0, true);
     out.initial_cost = chi;
+    auto sum_parts = [&](int nblocks, int nval, double* outv) {
+        if (e != cudaSuccess) return;
+        e = cudaMemcpyAsync(hpart.data(), d_part, sizeof(double) * nblocks * nval, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        for (int k = 0; k < nval; ++k) outv[k] = 0.0;
+        for (int bI = 0; bI < nblocks; ++bI)
+            for (int k = 0; k < nval; ++k) outv[k] += hpart[(size_t)nval * bI + k];
+    };
     out.trace.assign(lm.iterations + 1, 0.0);
     out.trace[0] = chi;
     out.termination = NAV_BA_TERM_ITERATIONS;
@@ -699,7 +1160,21 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             k_reduce_cams<<<rb, TB, 0, st>>>(d_upart, d_item_off, nfc, d_U, d_part);
             chk(cudaGetLastError());
         }
-        const double mxc = nfc > 0 ? sum_part((nfc * 27 + TB - 1) / TB, true) : 0.0;
+        double mxc = nfc > 0 ? sum_part((nfc * 27 + TB - 1) / TB, true) : 0.0;
+        if (nk) {
+            k_lin_intr_points<Real><<<pblocks, TB, 0, st>>>(A, D, camr[cur], A.x[cur], d_kp, d_part);
+            double v5[5];
+            sum_parts(pblocks, 5, v5);
+            Kk[0] = v5[0]; Kk[1] = v5[1]; Kk[2] = v5[2];
+            gk[0] = v5[3]; gk[1] = v5[4];
+            mxc = std::max(mxc, std::max(std::fabs(Kk[0]), std::fabs(Kk[2])));
+            if (nfc > 0) {
+                k_lin_intr_cams<Real><<<std::max(1, std::min(nsm_blocks, (n_items * 32 + TB - 1) / TB)), TB, 0, st>>>(
+                    A, d_items, n_items, d_list, d_fcam, camr[cur], A.x[cur], d_hpart);
+                k_reduce_items<<<(nfc * 12 + TB - 1) / TB, TB, 0, st>>>(d_hpart, 12, 12, d_item_off, nfc, d_Hck, 12);
+                chk(cudaGetLastError());
+            }
+        }
         if (e != cudaSuccess) return e;
         if (it == 0) {
             lambda = lm.initial_lambda > 0 ? lm.initial_lambda : lm.tau * std::max(mxp, mxc);
@@ -712,7 +1187,79 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             k_schur_points<Real><<<pblocks, TB, 0, st>>>(A, D, lam_use, d_part);
             const double npd = sum_part(pblocks, false);
             bool ok = npd == 0.0;
-            if (nfc > 0) {
+            double dk[2] = {0.0, 0.0};
+            if (pcg && mt > 0) {
+                // right-hand side and block-Jacobi preconditioner of the reduced system [cameras; k]
+                const int32_t one = 1;
+                chk(cudaMemcpyAsync(d_ok, &one, sizeof(int32_t), cudaMemcpyHostToDevice, st));
+                if (nfc > 0) {
+                    k_pcg_diag_items<Real><<<std::max(1, std::min(nsm_blocks, (n_items * 32 + TB - 1) / TB)), TB, 0, st>>>(
+                        A, d_items, n_items, d_list, d_upart);
+                    k_reduce_items<<<(nfc * 27 + TB - 1) / TB, TB, 0, st>>>(d_upart, 28, 27, d_item_off, nfc, d_aat, 28);
+                    k_pcg_precond<<<(nfc + TB - 1) / TB, TB, 0, st>>>(d_U, d_aat, nfc, lam_use, d_pc, d_bs, d_ok);
+                    chk(cudaGetLastError());
+                }
+                double pkh[3] = {1.0, 0.0, 1.0};
+                if (nk) {
+                    k_schur_intr_points<Real><<<pblocks, TB, 0, st>>>(A, D, d_kp, d_pb, d_part);
+                    double v5[5];
+                    sum_parts(pblocks, 5, v5);
+                    // P_k = H_kk + lambda I - sum B B^T (2x2 Cholesky on the host); b'_k = g_k - sum B t
+                    const double p00 = Kk[0] + lam_use - v5[0], p01 = Kk[1] - v5[1], p11 = Kk[2] + lam_use - v5[2];
+                    const double l00 = p00 > 0 ? std::sqrt(p00) : 1.0;
+                    const double l10 = p01 / l00;
+                    const double d11 = p11 - l10 * l10;
+                    const double l11 = d11 > 0 ? std::sqrt(d11) : 1.0;
+                    if (!(p00 > 0) || !(d11 > 0)) ok = false;
+                    pkh[0] = l00; pkh[1] = l10; pkh[2] = l11;
+                    const double bk[2] = {gk[0] - v5[3], gk[1] - v5[4]};
+                    const double kv[6] = {Kk[0], Kk[1], Kk[2], pkh[0], pkh[1], pkh[2]};
+                    chk(cudaMemcpyAsync(d_kvals, kv, sizeof(kv), cudaMemcpyHostToDevice, st));
+                    chk(cudaMemcpyAsync(d_bs + m, bk, sizeof(bk), cudaMemcpyHostToDevice, st));
+                } else {
+                    chk(cudaMemcpyAsync(d_kvals + 3, pkh, sizeof(pkh), cudaMemcpyHostToDevice, st));
+                }
+                PcgVec v;
+                v.x = d_vec;
+                v.r = d_vec + mt;
+                v.z = d_vec + 2LL * mt;
+                v.p = d_vec + 3LL * mt;
+                v.q = d_vec + 4LL * mt;
+                v.sc = d_vec + 5LL * mt;
+                k_pcg_init<<<1, 1024, 0, st>>>(v, d_bs, mt, d_pc, nfc, nk, d_kvals + 3);
+                chk(cudaGetLastError());
+                double scv[3] = {0, 0, 0};
+                int pit = 0;
+                const double tol2 = lm.pcg_tolerance * lm.pcg_tolerance;
+                for (; pit < lm.pcg_max_iterations; ++pit) {
+                    if (pit % 4 == 0) {
+                        chk(cudaMemcpyAsync(scv, v.sc, sizeof(scv), cudaMemcpyDeviceToHost, st));
+                        chk(cudaStreamSynchronize(st));
+                        if (e != cudaSuccess) return e;
+                        if (!(scv[1] > tol2 * scv[2])) break;
+                    }
+                    k_pcg_points<Real><<<pblocks, TB, 0, st>>>(A, D, v.p, nk, d_pb, d_t2, d_part);
+                    if (nfc > 0)
+                        k_pcg_cams<Real><<<std::max(1, std::min(nsm_blocks, (n_items * 32 + TB - 1) / TB)), TB, 0, st>>>(
+                            A, d_items, n_items, d_list, d_t2, d_camp);
+                    k_pcg_step<<<1, 1024, 0, st>>>(v, mt, nfc, nk, d_U, d_Hck, d_kvals, lam_use, d_camp, d_item_off,
+                                                   d_part, pblocks, d_pc, d_kvals + 3);
+                    chk(cudaGetLastError());
+                }
+                pcg_total += pit;
+                chk(cudaMemcpyAsync(d_bs, v.x, sizeof(double) * mt, cudaMemcpyDeviceToDevice, st));
+                int32_t okh = 1;
+                chk(cudaMemcpyAsync(&okh, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+                if (nk) chk(cudaMemcpyAsync(dk, v.x + m, sizeof(dk), cudaMemcpyDeviceToHost, st));
+                chk(cudaStreamSynchronize(st));
+                if (e != cudaSuccess) return e;
+                ok = ok && okh != 0;
+                if (!ok) {
+                    chk(cudaMemsetAsync(d_bs, 0, sizeof(double) * mt, st));
+                    dk[0] = dk[1] = 0.0;
+                }
+                if (nk) k_fold_intr<Real><<<pblocks, TB, 0, st>>>(A, D, d_pb, dk[0], dk[1]);
+            } else if (nfc > 0) {
                 chk(cudaMemsetAsync(d_S, 0, sizeof(double) * (size_t)m * m, st));
                 const int nb = (int)g.blocks.size();
                 k_schur_blocks<Real><<<std::max(1, std::min(nsm_blocks, (nb * 32 + TB - 1) / TB)), TB, 0, st>>>(
@@ -756,6 +1303,9 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             double scale = sum_part(cblocks, false);
             k_update_points<Real><<<pblocks, TB, 0, st>>>(A, D, lambda, d_bs, cur, d_part);
             scale += sum_part(pblocks, false);
+            scale += dk[0] * (lambda * dk[0] + gk[0]) + dk[1] * (lambda * dk[1] + gk[1]);
+            A.intr.k1 = kcur[0] + dk[0];
+            A.intr.k2 = kcur[1] + dk[1];
             double chi_new = cost_of(cur ^ 1, true);
             if (e != cudaSuccess) return e;
             if (!ok) chi_new = DBL_MAX;
@@ -770,10 +1320,14 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                 chi = chi_new;
                 ++out.accepted;
                 cur ^= 1;
+                kcur[0] = A.intr.k1;
+                kcur[1] = A.intr.k2;
             } else {
                 lambda *= nu;
                 nu *= 2;
                 ++out.rejected;
+                A.intr.k1 = kcur[0];
+                A.intr.k2 = kcur[1];
             }
             ++q;
         } while (rho < 0 && q < lm.max_trials);
@@ -787,6 +1341,9 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     if (out.termination == NAV_BA_TERM_ITERATIONS && out.iterations_done < lm.iterations) out.termination = NAV_BA_TERM_ITERATIONS;
     out.final_cost = chi;
     out.final_lambda = lambda;
+    out.k1 = kcur[0];
+    out.k2 = kcur[1];
+    out.pcg_iterations = pcg_total;
     out.trace.resize(out.iterations_done + 1);
     out.cams.resize(nc);
     out.points.resize(4LL * np);

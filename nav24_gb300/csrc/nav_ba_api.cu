@@ -55,6 +55,10 @@ LmOptions lm_options(const nav_ba_options& o) {
     lm.huber_delta = o.huber_delta;
     lm.initial_lambda = o.initial_lambda;
     lm.tau = o.tau;
+    lm.solver = o.solver;
+    lm.optimize_k = o.optimize_distortion;
+    lm.pcg_max_iterations = o.pcg_max_iterations;
+    lm.pcg_tolerance = o.pcg_tolerance;
     return lm;
 }
 
@@ -147,12 +151,13 @@ nav_ba_status build_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, c
     std::string why;
     nav_ba_status st = validate_options(o, &why);
     if (st != NAV_BA_OK) return set_err(ctx, st, why);
-    if (o->solver != NAV_BA_SOLVER_CHOLESKY)
-        return set_err(ctx, NAV_BA_ERR_UNSUPPORTED, "the window engine solves the reduced system by Cholesky");
+    if (o->solver == NAV_BA_SOLVER_PCG && o->pcg_max_iterations < 1)
+        return set_err(ctx, NAV_BA_ERR_ARGUMENT, "pcg_max_iterations < 1");
     for (int i = 0; i < n; ++i) {
         st = validate_problem(&probs[i], &why);
         if (st != NAV_BA_OK) return set_err(ctx, st, "problem " + std::to_string(i) + ": " + why);
-        if (o->optimize_distortion && probs[i].camera_model == NAV_BA_CAM_PINHOLE_RADIAL)
+        if (o->optimize_distortion && probs[i].camera_model == NAV_BA_CAM_PINHOLE_RADIAL &&
+            o->solver != NAV_BA_SOLVER_PCG)
             return set_err(ctx, NAV_BA_ERR_UNSUPPORTED, "distortion optimization needs the PCG solver");
         if (i > 0 && std::memcmp(probs[i].intrinsics, probs[0].intrinsics, sizeof(double) * 8) != 0)
             return set_err(ctx, NAV_BA_ERR_UNSUPPORTED, "a batch shares one calibration");
@@ -177,7 +182,8 @@ nav_ba_status build_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, c
         for (auto& th : ths) th.join();
     }
     for (int i = 0; i < n; ++i)
-        if (pb.host_status[i] == NAV_BA_OK && !fits_window_engine(pb.host[i])) pb.host_status[i] = kGridWindow;
+        if (pb.host_status[i] == NAV_BA_OK && (o->solver == NAV_BA_SOLVER_PCG || !fits_window_engine(pb.host[i])))
+            pb.host_status[i] = kGridWindow;  // the window engine is Cholesky-only
     pb.lm = lm_options(*o);
     pb.intr = n > 0 ? intrinsics_of(probs[0]) : Intr{};
     return NAV_BA_OK;
@@ -295,7 +301,14 @@ nav_ba_status solve_grid_window(nav_ba_ctx* ctx, const nav_ba_problem& p, const 
     if (r.points_out)
         for (int k = 0; k < p.n_points; ++k)
             for (int j = 0; j < 3; ++j) r.points_out[3LL * k + j] = g.points[4LL * k + j];
-    if (r.intrinsics_out) std::memcpy(r.intrinsics_out, p.intrinsics, sizeof(double) * 8);
+    if (r.intrinsics_out) {
+        std::memcpy(r.intrinsics_out, p.intrinsics, sizeof(double) * 8);
+        if (o.optimize_distortion && p.camera_model == NAV_BA_CAM_PINHOLE_RADIAL) {
+            r.intrinsics_out[4] = g.k1;
+            r.intrinsics_out[5] = g.k2;
+        }
+    }
+    r.pcg_iterations_total = g.pcg_iterations;
     if (r.cost_trace)
         for (int k = 0; k <= g.iterations_done; ++k) r.cost_trace[k] = g.trace[k];
     return NAV_BA_OK;

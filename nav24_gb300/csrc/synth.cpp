@@ -24,6 +24,61 @@ constexpr double kWidth = 640.0, kHeight = 480.0;
 using Vec3 = std::array<double, 3>;
 using Mat3 = std::array<double, 9>;  // row-major
 
+// Host-independent elementary functions.  The platform libm may pick a different sin/cos/log per
+// CPU (glibc on x86-64 selects an FMA variant at run time), which changes last bits and, through
+// the visibility tests, the whole random stream.  These use only +, -, *, / and sqrt, all
+// correctly rounded in IEEE double, and the file is compiled without contraction, so every host
+// produces the same bits.  Accuracy is a few ulp, which is all the generator needs.
+//
+// sin/cos: Cody-Waite reduction x = k*pi/2 + r with pi/2 split into a 32-bit head (k*head exact for
+// |k| < 2^21) and a tail, then the Taylor series of sin and cos on |r| <= pi/4 to order 17/18
+// (remainder below 1e-19), nested so each step divides by the next factorial ratio.
+struct PiHalf {
+    double head, tail;
+    PiHalf() {
+        const double ph = 1.5707963267948966;  // pi/2 rounded to double
+        uint64_t b;
+        std::memcpy(&b, &ph, 8);
+        b &= ~((uint64_t(1) << 21) - 1);       // keep 32 significant bits
+        std::memcpy(&head, &b, 8);
+        tail = (ph - head) + 6.123233995736766e-17;  // pi/2 - double(pi/2) = 6.1232339957367658e-17
+    }
+};
+const PiHalf kPiHalf;
+
+void dsincos(double x, double* s, double* c) {
+    const double kd = std::nearbyint(x * (2.0 / kPi));
+    const double r = (x - kd * kPiHalf.head) - kd * kPiHalf.tail;
+    const double r2 = r * r;
+    double ps = 1.0, pc = 1.0;
+    for (int n = 9; n >= 1; --n) {  // sin: 1 - r2/(2n(2n+1)) (...);  cos: 1 - r2/((2n-1)2n) (...)
+        ps = 1.0 - r2 / (double)((2 * n) * (2 * n + 1)) * ps;
+        pc = 1.0 - r2 / (double)((2 * n - 1) * (2 * n)) * pc;
+    }
+    const double sr = r * ps, cr = pc;
+    switch (((long long)kd % 4 + 4) % 4) {
+        case 0: *s = sr; *c = cr; break;
+        case 1: *s = cr; *c = -sr; break;
+        case 2: *s = -sr; *c = -cr; break;
+        default: *s = -cr; *c = sr; break;
+    }
+}
+double dsin(double x) { double s, c; dsincos(x, &s, &c); return s; }
+double dcos(double x) { double s, c; dsincos(x, &s, &c); return c; }
+
+// log for x > 0: x = m 2^e with m in [sqrt(1/2), sqrt(2)) (frexp is exact), log m = 2 atanh(t) with
+// t = (m-1)/(m+1), |t| <= 0.1716, by its series t + t^3/3 + ... to t^25 (remainder below 1e-20);
+// ln 2 as a double plus its rounding error.
+double dlog(double x) {
+    int e;
+    double m = std::frexp(x, &e);
+    if (m < 0.70710678118654752) { m *= 2.0; e -= 1; }
+    const double t = (m - 1.0) / (m + 1.0), t2 = t * t;
+    double p = 1.0 / 25.0;
+    for (int k = 11; k >= 0; --k) p = 1.0 / (double)(2 * k + 1) + t2 * p;
+    return (double)e * 0.6931471805599453 + ((double)e * 2.3190468138462996e-17 + 2.0 * t * p);
+}
+
 // Deterministic random source: mt19937_64 bits, uniform from the top 53 bits, normal by the
 // Box-Muller transform (Box & Muller 1958).
 struct Rng {
@@ -41,10 +96,10 @@ struct Rng {
         double u1 = uniform();
         while (u1 <= 1e-300) u1 = uniform();
         const double u2 = uniform();
-        const double r = std::sqrt(-2.0 * std::log(u1));
-        spare = r * std::sin(2.0 * kPi * u2);
+        const double r = std::sqrt(-2.0 * dlog(u1));
+        spare = r * dsin(2.0 * kPi * u2);
         has_spare = true;
-        return r * std::cos(2.0 * kPi * u2);
+        return r * dcos(2.0 * kPi * u2);
     }
 };
 
@@ -76,7 +131,7 @@ Mat3 expso3(const Vec3& w) {
     const double th = std::sqrt(dot(w, w));
     if (th < 1e-15) return {1, 0, 0, 0, 1, 0, 0, 0, 1};
     const Vec3 k = scale(w, 1.0 / th);
-    const double c = std::cos(th), s = std::sin(th), v = 1.0 - c;
+    const double c = dcos(th), s = dsin(th), v = 1.0 - c;
     return {c + k[0] * k[0] * v,        k[0] * k[1] * v - k[2] * s, k[0] * k[2] * v + k[1] * s,
             k[1] * k[0] * v + k[2] * s, c + k[1] * k[1] * v,        k[1] * k[2] * v - k[0] * s,
             k[2] * k[0] * v - k[1] * s, k[2] * k[1] * v + k[0] * s, c + k[2] * k[2] * v};
@@ -271,7 +326,7 @@ extern "C" nav_synth* nav_synth_create(const nav_synth_params* prm) {
         const int np = prm->n_points > 0 ? prm->n_points : 500;
         for (int c = 0; c < nc; ++c) {
             const double a = 2.0 * kPi * c / nc;
-            const Vec3 C = {5.0 * std::cos(a), 5.0 * std::sin(a), 0.0};
+            const Vec3 C = {5.0 * dcos(a), 5.0 * dsin(a), 0.0};
             w.cams.push_back(look_along(C, scale(C, -1.0), up));
             w.cam_fixed.push_back(c == 0);
         }
@@ -370,12 +425,12 @@ extern "C" nav_synth* nav_synth_create(const nav_synth_params* prm) {
         const int nc = prm->n_cams > 0 ? prm->n_cams : 50;
         const int np = prm->n_points > 0 ? prm->n_points : 10000;
         const double golden = kPi * (3.0 - std::sqrt(5.0));
-        const double cos_min = std::cos(60.0 * kPi / 180.0);
+        const double cos_min = dcos(60.0 * kPi / 180.0);
         for (int c = 0; c < nc; ++c) {
             const double z = 1.0 - (1.0 - cos_min) * (c + 0.5) / nc;
             const double r = std::sqrt(std::max(0.0, 1.0 - z * z));
             const double a = golden * c;
-            const Vec3 C = {6.0 * r * std::cos(a), 6.0 * r * std::sin(a), 6.0 * z};
+            const Vec3 C = {6.0 * r * dcos(a), 6.0 * r * dsin(a), 6.0 * z};
             w.cams.push_back(look_along(C, scale(C, -1.0), Vec3{0, 1, 0}));
             w.cam_fixed.push_back(c == 0);
         }
@@ -401,7 +456,7 @@ extern "C" nav_synth* nav_synth_create(const nav_synth_params* prm) {
         // arc-length table of the base curve
         const int nt = 20000;
         std::vector<double> arc(nt + 1, 0.0);
-        auto curve = [](double s) { return Vec3{150.0 * std::sin(s), 100.0 * std::sin(s) * std::cos(s), 0.0}; };
+        auto curve = [](double s) { return Vec3{150.0 * dsin(s), 100.0 * dsin(s) * dcos(s), 0.0}; };
         for (int k = 1; k <= nt; ++k) {
             const Vec3 a = curve(2 * kPi * (k - 1) / nt), b = curve(2 * kPi * k / nt);
             arc[k] = arc[k - 1] + std::sqrt(dot(sub(b, a), sub(b, a)));
@@ -431,8 +486,8 @@ extern "C" nav_synth* nav_synth_create(const nav_synth_params* prm) {
             const Vec3 C = pos(s, 0.6 * (loop - 1), 1.5);
             const Vec3 d = normalize(sub(curve(s + 1e-4), curve(s - 1e-4)));
             const double yaw = rng.normal() * 0.05;
-            const Vec3 f = {d[0] * std::cos(yaw) - d[1] * std::sin(yaw),
-                            d[0] * std::sin(yaw) + d[1] * std::cos(yaw), 0.0};
+            const Vec3 f = {d[0] * dcos(yaw) - d[1] * dsin(yaw),
+                            d[0] * dsin(yaw) + d[1] * dcos(yaw), 0.0};
             w.cams.push_back(look_along(C, f, up));
             w.cam_fixed.push_back(c == 0);
             centres.push_back(C);

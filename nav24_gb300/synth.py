@@ -10,6 +10,7 @@ Workload families and the seeds of the five named workloads (seed = 1000 + famil
 from __future__ import annotations
 
 import ctypes as C
+import hashlib
 from pathlib import Path
 
 import numpy as np
@@ -98,6 +99,16 @@ class Synth:
         self.win_obs = arrs[11]
         self.intrinsics = arrs[12]
         self.intrinsics_init = arrs[13]
+
+    def digest(self) -> str:
+        """SHA-256 of every generated array: the generator is host-independent (no platform libm,
+        no floating-point contraction), so a workload has the same digest on every machine."""
+        h = hashlib.sha256()
+        for a in (self.cam_pose, self.cam_pose_true, self.cam_fixed, self.points, self.points_true,
+                  self.point_fixed, self.obs_uv, self.obs_cam, self.obs_point, self.win_cam, self.win_pt,
+                  self.win_obs, self.intrinsics, self.intrinsics_init):
+            h.update(np.ascontiguousarray(a).tobytes())
+        return h.hexdigest()
 
     @property
     def n_windows(self) -> int:

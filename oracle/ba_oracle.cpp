@@ -682,12 +682,103 @@ public:
         }
     }
 
+    // Block-Jacobi preconditioned conjugate gradients on the reduced system (NAV_BA_SOLVER_PCG):
+    // preconditioner = the 6x6 camera blocks and the 2x2 distortion block of S, each factored by
+    // Cholesky; x0 = 0; stop when ||r|| <= tol ||b|| (tested every 4 iterations) or after the
+    // maximum number of iterations.  Returns false when a preconditioner block is not positive
+    // definite.  The solution replaces bs.
+    int pcg_iterations = 0;
+    bool pcg_solve(const std::vector<double>& S, std::vector<double>& bs) {
+        const int m = dim_s();
+        auto Sij = [&](int i, int j) { return j <= i ? S[(size_t)i * m + j] : S[(size_t)j * m + i]; };
+        // diagonal blocks: cameras (6x6) then the distortion pair (2x2)
+        std::vector<int> bstart, bsize;
+        for (int a = 0; a < nfc; ++a) { bstart.push_back(6 * a); bsize.push_back(6); }
+        if (nk) { bstart.push_back(6 * nfc); bsize.push_back(nk); }
+        std::vector<std::vector<double>> Lb(bstart.size());
+        bool ok = true;
+        for (size_t k = 0; k < bstart.size(); ++k) {
+            const int s0 = bstart[k], n = bsize[k];
+            std::vector<double>& L = Lb[k];
+            L.assign(n * n, 0.0);
+            for (int i = 0; i < n; ++i)
+                for (int j = 0; j <= i; ++j) L[i * n + j] = Sij(s0 + i, s0 + j);
+            for (int j = 0; j < n; ++j) {
+                double d = L[j * n + j];
+                for (int q = 0; q < j; ++q) d -= L[j * n + q] * L[j * n + q];
+                if (!(d > 0.0) || !std::isfinite(d)) { ok = false; d = 1.0; }
+                L[j * n + j] = std::sqrt(d);
+                for (int i = j + 1; i < n; ++i) {
+                    double v = L[i * n + j];
+                    for (int q = 0; q < j; ++q) v -= L[i * n + q] * L[j * n + q];
+                    L[i * n + j] = v / L[j * n + j];
+                }
+            }
+        }
+        auto precond = [&](const std::vector<double>& r, std::vector<double>& z) {
+            z.assign(m, 0.0);
+            for (size_t k = 0; k < bstart.size(); ++k) {
+                const int s0 = bstart[k], n = bsize[k];
+                const std::vector<double>& L = Lb[k];
+                double v[6];
+                for (int i = 0; i < n; ++i) {
+                    double t = r[s0 + i];
+                    for (int q = 0; q < i; ++q) t -= L[i * n + q] * v[q];
+                    v[i] = t / L[i * n + i];
+                }
+                for (int i = n - 1; i >= 0; --i) {
+                    double t = v[i];
+                    for (int q = i + 1; q < n; ++q) t -= L[q * n + i] * v[q];
+                    v[i] = t / L[i * n + i];
+                }
+                for (int i = 0; i < n; ++i) z[s0 + i] = v[i];
+            }
+        };
+        std::vector<double> x(m, 0.0), r = bs, z, p, q(m);
+        precond(r, z);
+        p = z;
+        double rz = 0.0, rr = 0.0;
+        for (int i = 0; i < m; ++i) { rz += r[i] * z[i]; rr += r[i] * r[i]; }
+        const double bb = rr;
+        const double tol2 = O.pcg_tolerance * O.pcg_tolerance;
+        int it = 0;
+        for (; it < O.pcg_max_iterations; ++it) {
+            if (it % 4 == 0 && !(rr > tol2 * bb)) break;
+            for (int i = 0; i < m; ++i) {
+                double t = 0.0;
+                for (int j = 0; j < m; ++j) t += Sij(i, j) * p[j];
+                q[i] = t;
+            }
+            double pq = 0.0;
+            for (int i = 0; i < m; ++i) pq += p[i] * q[i];
+            const double alpha = pq != 0.0 ? rz / pq : 0.0;
+            for (int i = 0; i < m; ++i) { x[i] += alpha * p[i]; r[i] -= alpha * q[i]; }
+            precond(r, z);
+            double rzn = 0.0;
+            rr = 0.0;
+            for (int i = 0; i < m; ++i) { rzn += r[i] * z[i]; rr += r[i] * r[i]; }
+            const double beta = rz != 0.0 ? rzn / rz : 0.0;
+            for (int i = 0; i < m; ++i) p[i] = z[i] + beta * p[i];
+            rz = rzn;
+        }
+        pcg_iterations += it;
+        bs = x;
+        return ok;
+    }
+
     // BlockSolver::solve with the damping applied (setLambda .. restoreDiagonal).
     bool compute_step(double lambda) {
         std::vector<double> S, bs, Vinv;
         reduced_system(lambda, S, bs, Vinv);
-        bool ok = cholesky(S);
-        if (ok) chol_solve(S, bs);
+        bool ok;
+        if (O.solver == NAV_BA_SOLVER_PCG) {
+            ok = pcg_solve(S, bs);
+            if (!ok) std::fill(bs.begin(), bs.end(), 0.0);
+        } else {
+            ok = cholesky(S);
+            if (ok) chol_solve(S, bs);
+            else std::fill(bs.begin(), bs.end(), 0.0);
+        }
         const int m = dim_s();
         dc.assign(6LL * nfc, 0.0);
         for (int j = 0; j < 6 * nfc; ++j) dc[j] = bs[j];
@@ -808,6 +899,7 @@ public:
             if (!std::isfinite(lambda)) { res->termination = NAV_BA_TERM_LAMBDA_NONFINITE; ++it; break; }
         }
         res->iterations_done = it;
+        res->pcg_iterations_total = pcg_iterations;
         res->trials_accepted = acc;
         res->trials_rejected = rej;
         res->final_cost = chi;

@@ -14,6 +14,10 @@ known_answer.json
 ring_fixture.npz
     The ring workload (family 0, seed 1000: 10 cameras, 500 points, camera 0 fixed) as input
     arrays, with the oracle's 10-iteration solve (lambda0 = 1e-3) as a regression pin.
+
+synth_digests.json
+    SHA-256 digests of small instances of every workload family (SYNTH_CASES): the generator is
+    host-independent, so the same digests must come out on x86-64 and aarch64.
 """
 from __future__ import annotations
 
@@ -116,7 +120,23 @@ def make_ring_fixture():
         out_iterations=np.int32(r.stats["iterations_done"]), out_termination=np.int32(r.stats["termination"]))
 
 
+SYNTH_CASES = [
+    {"family": 0},
+    {"family": 1, "n_cams": 40, "n_points": 3000},
+    {"family": 2, "n_windows": 8},
+    {"family": 3, "n_windows": 4},
+    {"family": 4, "n_cams": 60, "n_points": 6000, "seed": 8},
+]
+
+
+def make_synth_digests():
+    from nav24_gb300.synth import Synth
+    out = [dict(case, digest=Synth(**case).digest()) for case in SYNTH_CASES]
+    (HERE / "synth_digests.json").write_text(json.dumps(out, indent=1))
+
+
 if __name__ == "__main__":
     make_known_answer()
     make_ring_fixture()
+    make_synth_digests()
     print("written", sorted(x.name for x in HERE.iterdir()))

@@ -283,3 +283,26 @@ def test_reduced_system_is_symmetric_positive_definite_with_covisibility_pattern
             shared = np.any(vis[a] & vis[c])
             assert (np.abs(blk).max() > 0) == (shared or a == c)
     assert nf == int(np.sum(idx >= 0))
+
+
+def test_pcg_reaches_the_cholesky_step():
+    p = Synth(1, n_cams=30, n_points=2000, seed=3).window(0)
+    o = abi.default_options(iterations=8, robust=1, huber_delta=2.0)
+    rc = oracle.solve(p, o)
+    op = abi.default_options(iterations=8, robust=1, huber_delta=2.0, solver=abi.SOLVER_PCG,
+                             pcg_tolerance=1e-12, pcg_max_iterations=2000)
+    rp = oracle.solve(p, op)
+    assert rp.stats["pcg_iterations_total"] > 0
+    assert abs(rp.stats["final_cost"] - rc.stats["final_cost"]) / rc.stats["final_cost"] < 1e-9
+
+
+def test_distortion_is_recovered():
+    """Shared radial k1, k2 (family 4, no outliers): started off the truth, the solve recovers them."""
+    s = Synth(4, n_cams=40, n_points=4000, outlier_frac=0.0, seed=9)
+    p = s.window(0)
+    o = abi.default_options(iterations=15, robust=1, huber_delta=1.5, solver=abi.SOLVER_PCG,
+                            optimize_distortion=1, pcg_tolerance=1e-8, pcg_max_iterations=500)
+    r = oracle.solve(p, o, n_threads=4)
+    assert r.status == abi.OK
+    assert abs(r.intrinsics[4] - s.intrinsics[4]) < 2e-3 and abs(r.intrinsics[5] - s.intrinsics[5]) < 2e-3
+    assert r.cost_trace[-1] < 0.05 * r.cost_trace[0]
