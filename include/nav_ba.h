@@ -230,6 +230,56 @@ nav_ba_status nav_ba_cost(nav_ba_ctx* ctx, const nav_ba_problem* problem,
 nav_ba_status nav_ba_solve_noalloc(nav_ba_ctx* ctx, const nav_ba_problem* problem,
                                    const nav_ba_options* options, nav_ba_result* result);
 
+/* ---- differentiation through the LM steps (no counterpart in the reference) ----------------
+ *
+ * The differentiable function is the LM solve with its damping schedule frozen: the steps that
+ * the solve accepted, each x <- x [+] dx with (H(x) + lambda I) dx = b(x) at its recorded lambda.
+ * Rejected trials leave the state unchanged and so are not part of the function.  Outputs are the
+ * final robust cost, the poses and the points; inputs whose gradients are given are the
+ * observations, the intrinsics (fx, fy, cx, cy) and the initial poses and points.
+ *
+ * nav_ba_vjp runs the forward and, when `cot` and `grads` are both non-NULL, the backward:
+ *   - schedule->replay == 0: the forward is the LM solve of nav_ba_solve (same semantics, run by
+ *     the whole-GPU engine, so it agrees with nav_ba_solve to rounding) and schedule receives the
+ *     damping of each accepted step;
+ *   - schedule->replay == 1: the forward applies the schedule's n_steps steps unconditionally
+ *     (result->iterations_done = n_steps).  Replaying a recorded schedule on the same inputs
+ *     reproduces the recorded solve, and is the function that finite differences check.
+ * The backward is the adjoint of the unrolled steps: per step (last first) it re-linearizes at
+ * the stored state (Jacobians are recomputed, not stored), refactors H + lambda I, solves the
+ * adjoint system with that factorization, and accumulates per-observation adjoints of the
+ * residual, Jacobian and Huber weight.  L = cot->cost * final_cost + <cot->cam_pose, cam_pose_out>
+ * + <cot->points, points_out>.
+ * Supported: FP64 precision, the Cholesky solver, the pinhole model, no distortion optimization;
+ * other options return NAV_BA_ERR_UNSUPPORTED.  An EMPTY problem writes the inputs as outputs and
+ * zero gradients. */
+#define NAV_BA_VJP_MAX_STEPS 64
+typedef struct nav_ba_schedule {
+    int32_t replay;                        /* 0: run LM and record; 1: apply the given steps   */
+    int32_t n_steps;                       /* accepted steps (<= NAV_BA_VJP_MAX_STEPS)          */
+    double lambda[NAV_BA_VJP_MAX_STEPS];   /* damping of each accepted step                     */
+} nav_ba_schedule;
+
+typedef struct nav_ba_cotangent {
+    double cost;                  /* dL / d final cost                                         */
+    const double* cam_pose;       /* [n_cams][12] dL / d cam_pose_out entries, or NULL (zero)  */
+    const double* points;         /* [n_points][3] dL / d points_out, or NULL (zero)           */
+} nav_ba_cotangent;
+
+typedef struct nav_ba_grads {
+    double* obs_uv;               /* [n_obs][2] dL / d obs_uv, or NULL                         */
+    double intrinsics[8];         /* dL / d (fx, fy, cx, cy); entries 4..7 are 0               */
+    /* The next two are gradients with respect to the initial values of the optimized vertices
+     * (cameras and points that are free and have an active edge); 0 for the other vertices. */
+    double* cam_tangent;          /* [n_cams][6] dL / d (left perturbation [omega; upsilon] of
+                                     each input pose: T -> exp(eps) T), or NULL                  */
+    double* points;               /* [n_points][3] dL / d input points, or NULL                */
+} nav_ba_grads;
+
+nav_ba_status nav_ba_vjp(nav_ba_ctx* ctx, const nav_ba_problem* problem,
+                         const nav_ba_options* options, nav_ba_schedule* schedule,
+                         const nav_ba_cotangent* cot, nav_ba_result* result, nav_ba_grads* grads);
+
 /* Last error message of the context (empty string if none). */
 const char* nav_ba_last_error(const nav_ba_ctx* ctx);
 const char* nav_ba_status_string(nav_ba_status status);

@@ -21,7 +21,7 @@ EXPORTS = [
     "nav_ba_solve_batched", "nav_ba_prepare", "nav_ba_run", "nav_ba_fetch", "nav_ba_prepare_batched",
     "nav_ba_fetch_batched", "nav_ba_linearize",
     "nav_ba_reduced_system", "nav_ba_cost", "nav_ba_last_error", "nav_ba_status_string",
-    "nav_ba_abi_version", "nav_ba_solve_noalloc",
+    "nav_ba_abi_version", "nav_ba_solve_noalloc", "nav_ba_vjp",
 ]
 
 _LIB = None
@@ -75,6 +75,9 @@ def load(path: os.PathLike | None = None) -> C.CDLL:
     L.nav_ba_status_string.restype = C.c_char_p
     L.nav_ba_solve_noalloc.argtypes = [ctxp, P, O, R]
     L.nav_ba_solve_noalloc.restype = C.c_int
+    L.nav_ba_vjp.argtypes = [ctxp, P, O, C.POINTER(abi.nav_ba_schedule), C.POINTER(abi.nav_ba_cotangent), R,
+                             C.POINTER(abi.nav_ba_grads)]
+    L.nav_ba_vjp.restype = C.c_int
     L.nav_ba_abi_version.argtypes = []
     L.nav_ba_abi_version.restype = C.c_int32
     if path is None:
@@ -144,6 +147,46 @@ class Context:
         if raise_on_error:
             self._check(st, (abi.OK, abi.EMPTY))
         return buf.result(st)
+
+    def vjp(self, prob: abi.Problem, opt: abi.nav_ba_options, lambdas=None, cost_bar: float | None = None,
+            pose_bar: np.ndarray | None = None, point_bar: np.ndarray | None = None):
+        """nav_ba_vjp.  lambdas None: run LM and record the accepted steps' damping; else replay
+        those steps.  With any cotangent given (cost_bar, pose_bar [n_cams, 12], point_bar
+        [n_points, 3]) the backward runs too.  Returns (Result, lambdas, grads or None), grads a
+        dict of obs_uv [n_obs, 2], intrinsics [4] (fx, fy, cx, cy), cam_tangent [n_cams, 6] and
+        points [n_points, 3]."""
+        replay = lambdas is not None
+        sched = abi.nav_ba_schedule.of(lambdas if replay else [], replay)
+        buf = abi.ResultBuffers(prob, max(opt.iterations, len(lambdas) if replay else 0))
+        p = prob.as_c()
+        bwd = cost_bar is not None or pose_bar is not None or point_bar is not None
+        cot = grads = None
+        keep = []
+        if bwd:
+            cot = abi.nav_ba_cotangent()
+            cot.cost = 0.0 if cost_bar is None else float(cost_bar)
+            if pose_bar is not None:
+                pb = np.ascontiguousarray(pose_bar, np.float64).reshape(prob.n_cams, 12)
+                keep.append(pb)
+                cot.cam_pose = _d(pb)
+            if point_bar is not None:
+                qb = np.ascontiguousarray(point_bar, np.float64).reshape(prob.n_points, 3)
+                keep.append(qb)
+                cot.points = _d(qb)
+            g = {"obs_uv": np.zeros((prob.n_obs, 2)), "cam_tangent": np.zeros((prob.n_cams, 6)),
+                 "points": np.zeros((prob.n_points, 3))}
+            grads = abi.nav_ba_grads()
+            grads.obs_uv = _d(g["obs_uv"])
+            grads.cam_tangent = _d(g["cam_tangent"])
+            grads.points = _d(g["points"])
+        st = self.L.nav_ba_vjp(self.h, C.byref(p), C.byref(opt), C.byref(sched),
+                               C.byref(cot) if bwd else None, C.byref(buf.c), C.byref(grads) if bwd else None)
+        self._check(st, (abi.OK, abi.EMPTY))
+        out = None
+        if bwd:
+            g["intrinsics"] = np.array([grads.intrinsics[i] for i in range(4)])
+            out = g
+        return buf.result(st), sched.lambdas, out
 
     def solve_batched(self, probs: list[abi.Problem], opt: abi.nav_ba_options) -> list[abi.Result]:
         n = len(probs)

@@ -106,6 +106,35 @@ class nav_ba_result(C.Structure):
     ]
 
 
+VJP_MAX_STEPS = 64
+
+
+class nav_ba_schedule(C.Structure):
+    _fields_ = [("replay", C.c_int32), ("n_steps", C.c_int32), ("lam", C.c_double * VJP_MAX_STEPS)]
+
+    @property
+    def lambdas(self) -> list[float]:
+        return [self.lam[i] for i in range(self.n_steps)]
+
+    @staticmethod
+    def of(lambdas, replay: bool = True) -> "nav_ba_schedule":
+        s = nav_ba_schedule()
+        s.replay = 1 if replay else 0
+        s.n_steps = len(lambdas)
+        for i, v in enumerate(lambdas):
+            s.lam[i] = float(v)
+        return s
+
+
+class nav_ba_cotangent(C.Structure):
+    _fields_ = [("cost", C.c_double), ("cam_pose", C.POINTER(C.c_double)), ("points", C.POINTER(C.c_double))]
+
+
+class nav_ba_grads(C.Structure):
+    _fields_ = [("obs_uv", C.POINTER(C.c_double)), ("intrinsics", C.c_double * 8),
+                ("cam_tangent", C.POINTER(C.c_double)), ("points", C.POINTER(C.c_double))]
+
+
 class nav_synth_params(C.Structure):
     _fields_ = [
         ("family", C.c_int32),

@@ -150,11 +150,31 @@ struct GridResult {
     int32_t pcg_iterations = 0;
 };
 
+// Differentiation through the accepted LM steps (grid engine, FP64, Cholesky, pinhole).
+struct GridVjp {
+    // replay: apply the steps of `lambdas` unconditionally; else run LM and record the damping of
+    // every accepted step into `lambdas`
+    bool replay = false;
+    std::vector<double> lambdas;
+    // backward: run it with these cotangents of the outputs (problem order; null = zero)
+    bool backward = false;
+    double cost_bar = 0.0;
+    const double* pose_bar = nullptr;   // [ncam][12]
+    const double* point_bar = nullptr;  // [npt][3]
+    // results of the backward
+    std::vector<double> uv_bar;         // [ne][2], active-edge order
+    double intr_bar[4] = {0, 0, 0, 0};  // fx, fy, cx, cy
+    std::vector<double> cam_bar;        // [ncam][6] left-tangent adjoint of the input poses
+    std::vector<double> pt_bar;         // [npt][3]
+    std::string why;                    // reason of a non-OK status
+};
+
 // Solve one large problem on the whole GPU.  debug_S != nullptr: stop after assembling the
 // reduced system at damping debug_lambda and return [S (m*m, row-major, lower part) | b'].
+// vjp != nullptr (FP64 only): record or replay the damping schedule and run the backward.
 cudaError_t grid_solve(const HostWindow& h, const LmOptions& lm, const Intr& intr, int precision,
                        cudaStream_t stream, int cluster, GridResult& out, double debug_lambda,
-                       std::vector<double>* debug_S);
+                       std::vector<double>* debug_S, GridVjp* vjp = nullptr);
 
 // One-window solve in the library's static device array (no device allocation), noalloc.cu.
 nav_ba_status solve_window_noalloc(int device, cudaStream_t stream, const nav_ba_problem& p,

@@ -17,15 +17,19 @@
 //   solve         one CTA, tile-blocked forward/back substitution inside the envelope
 //   update        thread per point (dx_p = L^T (t - sum A^T dx_c), shared) and per camera (SE(3))
 //   cost          thread per point, per-block partial sums reduced on the host in a fixed order
+// With a GridVjp, the accepted steps' states and damping are taped (or a given damping schedule
+// is replayed) and the backward pass of vjp_device.cuh runs over the taped steps, last first.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 
 #include <cooperative_groups.h>
 
 #include "engine.hpp"
 #include "lm_device.cuh"
+#include "vjp_device.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -987,7 +991,8 @@ cudaError_t up(T* d, const std::vector<T>& h, cudaStream_t s) {
 
 template <class Real>
 cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Intr& intr, cudaStream_t st,
-                             int cluster, GridResult& out, double debug_lambda, std::vector<double>* debug_S) {
+                             int cluster, GridResult& out, double debug_lambda, std::vector<double>* debug_S,
+                             GridVjp* vjp) {
     GridHost g;
     build_grid_host(h, g);
     const int nc = h.ncam, np = h.npt, ne = h.ne, nfc = h.nfc;
@@ -1050,6 +1055,25 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     double* d_camp = pcg ? dv.alloc<double>(8LL * n_items) : nullptr;
     double* d_vec = pcg ? dv.alloc<double>(5LL * std::max(1, mt) + 8) : nullptr;
     double* d_kvals = dv.alloc<double>(8);  // [0..2] H_kk + lambda-free, [3..5] pk (2x2 Cholesky)
+    // tape of the accepted steps (state before each step) and the backward's vectors
+    const int tape_cap = vjp ? (vjp->replay ? (int)vjp->lambdas.size() : lm.iterations) : 0;
+    CamState* d_tape_c = vjp ? dv.alloc<CamState>((size_t)std::max(1, tape_cap) * nc) : nullptr;
+    double* d_tape_x = vjp ? dv.alloc<double>((size_t)std::max(1, tape_cap) * 4 * np) : nullptr;
+    const bool bwd = vjp && vjp->backward;
+    const int nfc1 = std::max(1, nfc);
+    double* d_cb[2] = {bwd ? dv.alloc<double>(6LL * nfc1) : nullptr, bwd ? dv.alloc<double>(6LL * nfc1) : nullptr};
+    double* d_rc = bwd ? dv.alloc<double>(6LL * nfc1) : nullptr;
+    double* d_uc = bwd ? dv.alloc<double>(6LL * nfc1) : nullptr;
+    double* d_ctmp = bwd ? dv.alloc<double>(6LL * nfc1) : nullptr;
+    double* d_pbar = bwd ? dv.alloc<double>(4LL * np) : nullptr;
+    double* d_up = bwd ? dv.alloc<double>(4LL * np) : nullptr;
+    double* d_dp = bwd ? dv.alloc<double>(4LL * np) : nullptr;
+    double* d_tr = bwd ? dv.alloc<double>(4LL * np) : nullptr;
+    double* d_eadj = bwd ? dv.alloc<double>(8LL * ne) : nullptr;  // per-edge camera adjoints
+    double* d_uvbar = bwd ? dv.alloc<double>(2LL * ne) : nullptr;
+    double* d_ipart = bwd ? dv.alloc<double>(8LL * g.items.size()) : nullptr;
+    double* d_posebar = (bwd && vjp->pose_bar) ? dv.alloc<double>(12LL * nc) : nullptr;
+    double* d_ptbar = (bwd && vjp->point_bar) ? dv.alloc<double>(3LL * np) : nullptr;
     if (dv.err != cudaSuccess) return dv.err;
     std::vector<int32_t> edge_fc(ne);
     for (int e = 0; e < ne; ++e) edge_fc[e] = h.cam_free[h.edge_cam[e]];
@@ -1075,6 +1099,8 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     chk(up(d_boff, g.boff, st));
     chk(up(d_pairs, g.pairs, st));
     chk(up(d_tfirst, g.tfirst, st));
+    if (d_posebar) chk(cudaMemcpyAsync(d_posebar, vjp->pose_bar, sizeof(double) * 12 * nc, cudaMemcpyHostToDevice, st));
+    if (d_ptbar) chk(cudaMemcpyAsync(d_ptbar, vjp->point_bar, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, st));
     if (e != cudaSuccess) return e;
 
     WinArgs<Real> A{};
@@ -1136,7 +1162,58 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         for (int bI = 0; bI < nblocks; ++bI)
             for (int k = 0; k < nval; ++k) outv[k] += hpart[(size_t)nval * bI + k];
     };
-    out.trace.assign(lm.iterations + 1, 0.0);
+    const int iblocks = std::max(1, std::min(nsm_blocks, (n_items * 32 + TB - 1) / TB));
+    // linearization at state c: V_p, g_p, W_e (point-major), U_a, g_a (camera-major); the max
+    // |diag| of the point and camera blocks (g2o's initial damping)
+    auto linearize = [&](int c, double& mxp, double& mxc) {
+        k_lin_points<Real><<<pblocks, TB, 0, st>>>(A, D, camr[c], A.x[c], d_part);
+        mxp = sum_part(pblocks, true);
+        if (nfc > 0) {
+            k_lin_cams<Real><<<iblocks, TB, 0, st>>>(A, d_items, n_items, d_list, d_fcam, camr[c], A.x[c], d_upart);
+            k_reduce_cams<<<(nfc * 27 + TB - 1) / TB, TB, 0, st>>>(d_upart, d_item_off, nfc, d_U, d_part);
+            chk(cudaGetLastError());
+        }
+        mxc = nfc > 0 ? sum_part((nfc * 27 + TB - 1) / TB, true) : 0.0;
+    };
+    // dense reduced system S = U + lam I - sum A A^T (lower part) and b'
+    auto assemble_S = [&](double lam) {
+        chk(cudaMemsetAsync(d_S, 0, sizeof(double) * (size_t)m * m, st));
+        const int nb = (int)g.blocks.size();
+        k_schur_blocks<Real><<<std::max(1, std::min(nsm_blocks, (nb * 32 + TB - 1) / TB)), TB, 0, st>>>(
+            A, d_blocks, d_boff, (int)(g.boff.size() - 1), d_pairs, d_U, lam, d_S, m, d_bs);
+        chk(cudaGetLastError());
+    };
+    int cl = std::max(1, std::min(8, cluster));
+    // Cholesky of S in place (one thread-block cluster); false if S is not positive definite
+    auto factor_S = [&]() -> bool {
+        const int32_t one = 1;
+        chk(cudaMemcpyAsync(d_ok, &one, sizeof(int32_t), cudaMemcpyHostToDevice, st));
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = cl;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cfg.gridDim = dim3(cl);
+        cfg.blockDim = dim3(256);
+        cfg.stream = st;
+        chk(cudaLaunchKernelEx(&cfg, k_cholesky, d_S, m, (const int32_t*)d_tfirst, d_rinv, d_ok));
+        int32_t okh = 1;
+        chk(cudaMemcpyAsync(&okh, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        chk(cudaStreamSynchronize(st));
+        return e == cudaSuccess && okh != 0;
+    };
+    // state c -> tape slot s
+    auto save_state = [&](int c, int s) {
+        chk(cudaMemcpyAsync(d_tape_c + (size_t)s * nc, cams[c], sizeof(CamState) * nc, cudaMemcpyDeviceToDevice, st));
+        chk(cudaMemcpyAsync(d_tape_x + (size_t)s * 4 * np, A.x[c], sizeof(double) * 4 * np, cudaMemcpyDeviceToDevice, st));
+    };
+    if (vjp && !vjp->replay) vjp->lambdas.clear();
+    const bool replay = vjp && vjp->replay;
+    const int n_out = replay ? (int)vjp->lambdas.size() : lm.iterations;
+    out.trace.assign(n_out + 1, 0.0);
     out.trace[0] = chi;
     out.termination = NAV_BA_TERM_ITERATIONS;
     out.iterations_done = out.accepted = out.rejected = 0;
@@ -1148,19 +1225,42 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     out.status = NAV_BA_OK;
     if (nfc + h.nfp == 0) out.termination = NAV_BA_TERM_NOTHING_TO_DO;
     double lambda = 0.0, nu = 2.0;
-    int cl = std::max(1, std::min(8, cluster));
-    for (int it = 0; out.termination == NAV_BA_TERM_ITERATIONS && it < lm.iterations; ++it) {
-        k_lin_points<Real><<<pblocks, TB, 0, st>>>(A, D, camr[cur], A.x[cur], d_part);
-        const double mxp = sum_part(pblocks, true);
-        if (nfc > 0) {
-            const int ni = (int)g.items.size();
-            k_lin_cams<Real><<<std::max(1, std::min(nsm_blocks, (ni * 32 + TB - 1) / TB)), TB, 0, st>>>(
-                A, d_items, ni, d_list, d_fcam, camr[cur], A.x[cur], d_upart);
-            const int rb = (nfc * 27 + TB - 1) / TB;
-            k_reduce_cams<<<rb, TB, 0, st>>>(d_upart, d_item_off, nfc, d_U, d_part);
+    if (replay) {
+        // the given steps, each accepted: x <- x [+] (H + lambda_s I)^-1 b at the current state
+        for (int s = 0; s < n_out; ++s) {
+            const double lam = vjp->lambdas[s];
+            save_state(cur, s);
+            double mxp, mxc;
+            linearize(cur, mxp, mxc);
+            k_schur_points<Real><<<pblocks, TB, 0, st>>>(A, D, lam, d_part);
+            bool ok = sum_part(pblocks, false) == 0.0;
+            if (nfc > 0) {
+                assemble_S(lam);
+                ok = factor_S() && ok;
+                if (ok) k_chol_solve<<<1, 256, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_bs);
+                chk(cudaGetLastError());
+            }
+            if (e != cudaSuccess) return e;
+            if (!ok) {
+                out.status = NAV_BA_ERR_UNSUPPORTED;
+                vjp->why = "replayed step " + std::to_string(s) + ": the damped system is not positive definite";
+                return cudaSuccess;
+            }
+            k_update_cams<Real><<<cblocks, TB, 0, st>>>(cams[cur], cams[cur ^ 1], camr[cur ^ 1], d_cam_free, nc, d_bs, d_U,
+                                                         lam, d_part);
+            k_update_points<Real><<<pblocks, TB, 0, st>>>(A, D, lam, d_bs, cur, d_part);
             chk(cudaGetLastError());
+            cur ^= 1;
+            chi = cost_of(cur, true);
+            if (e != cudaSuccess) return e;
+            out.trace[s + 1] = chi;
+            lambda = lam;
         }
-        double mxc = nfc > 0 ? sum_part((nfc * 27 + TB - 1) / TB, true) : 0.0;
+        out.iterations_done = out.accepted = n_out;
+    }
+    for (int it = 0; !replay && out.termination == NAV_BA_TERM_ITERATIONS && it < lm.iterations; ++it) {
+        double mxp, mxc;
+        linearize(cur, mxp, mxc);
         if (nk) {
             k_lin_intr_points<Real><<<pblocks, TB, 0, st>>>(A, D, camr[cur], A.x[cur], d_kp, d_part);
             double v5[5];
@@ -1169,8 +1269,8 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             gk[0] = v5[3]; gk[1] = v5[4];
             mxc = std::max(mxc, std::max(std::fabs(Kk[0]), std::fabs(Kk[2])));
             if (nfc > 0) {
-                k_lin_intr_cams<Real><<<std::max(1, std::min(nsm_blocks, (n_items * 32 + TB - 1) / TB)), TB, 0, st>>>(
-                    A, d_items, n_items, d_list, d_fcam, camr[cur], A.x[cur], d_hpart);
+                k_lin_intr_cams<Real><<<iblocks, TB, 0, st>>>(A, d_items, n_items, d_list, d_fcam, camr[cur], A.x[cur],
+                                                              d_hpart);
                 k_reduce_items<<<(nfc * 12 + TB - 1) / TB, TB, 0, st>>>(d_hpart, 12, 12, d_item_off, nfc, d_Hck, 12);
                 chk(cudaGetLastError());
             }
@@ -1193,8 +1293,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                 const int32_t one = 1;
                 chk(cudaMemcpyAsync(d_ok, &one, sizeof(int32_t), cudaMemcpyHostToDevice, st));
                 if (nfc > 0) {
-                    k_pcg_diag_items<Real><<<std::max(1, std::min(nsm_blocks, (n_items * 32 + TB - 1) / TB)), TB, 0, st>>>(
-                        A, d_items, n_items, d_list, d_upart);
+                    k_pcg_diag_items<Real><<<iblocks, TB, 0, st>>>(A, d_items, n_items, d_list, d_upart);
                     k_reduce_items<<<(nfc * 27 + TB - 1) / TB, TB, 0, st>>>(d_upart, 28, 27, d_item_off, nfc, d_aat, 28);
                     k_pcg_precond<<<(nfc + TB - 1) / TB, TB, 0, st>>>(d_U, d_aat, nfc, lam_use, d_pc, d_bs, d_ok);
                     chk(cudaGetLastError());
@@ -1240,8 +1339,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                     }
                     k_pcg_points<Real><<<pblocks, TB, 0, st>>>(A, D, v.p, nk, d_pb, d_t2, d_part);
                     if (nfc > 0)
-                        k_pcg_cams<Real><<<std::max(1, std::min(nsm_blocks, (n_items * 32 + TB - 1) / TB)), TB, 0, st>>>(
-                            A, d_items, n_items, d_list, d_t2, d_camp);
+                        k_pcg_cams<Real><<<iblocks, TB, 0, st>>>(A, d_items, n_items, d_list, d_t2, d_camp);
                     k_pcg_step<<<1, 1024, 0, st>>>(v, mt, nfc, nk, d_U, d_Hck, d_kvals, lam_use, d_camp, d_item_off,
                                                    d_part, pblocks, d_pc, d_kvals + 3);
                     chk(cudaGetLastError());
@@ -1260,11 +1358,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                 }
                 if (nk) k_fold_intr<Real><<<pblocks, TB, 0, st>>>(A, D, d_pb, dk[0], dk[1]);
             } else if (nfc > 0) {
-                chk(cudaMemsetAsync(d_S, 0, sizeof(double) * (size_t)m * m, st));
-                const int nb = (int)g.blocks.size();
-                k_schur_blocks<Real><<<std::max(1, std::min(nsm_blocks, (nb * 32 + TB - 1) / TB)), TB, 0, st>>>(
-                    A, d_blocks, d_boff, (int)(g.boff.size() - 1), d_pairs, d_U, lam_use, d_S, m, d_bs);
-                chk(cudaGetLastError());
+                assemble_S(lam_use);
                 if (debug_S) {
                     debug_S->assign((size_t)m * m + m, 0.0);
                     chk(cudaMemcpyAsync(debug_S->data(), d_S, sizeof(double) * m * m, cudaMemcpyDeviceToHost, st));
@@ -1272,25 +1366,8 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                     chk(cudaStreamSynchronize(st));
                     return e;
                 }
-                const int32_t one = 1;
-                chk(cudaMemcpyAsync(d_ok, &one, sizeof(int32_t), cudaMemcpyHostToDevice, st));
-                cudaLaunchConfig_t cfg = {};
-                cudaLaunchAttribute attr[1];
-                attr[0].id = cudaLaunchAttributeClusterDimension;
-                attr[0].val.clusterDim.x = cl;
-                attr[0].val.clusterDim.y = 1;
-                attr[0].val.clusterDim.z = 1;
-                cfg.attrs = attr;
-                cfg.numAttrs = 1;
-                cfg.gridDim = dim3(cl);
-                cfg.blockDim = dim3(256);
-                cfg.stream = st;
-                chk(cudaLaunchKernelEx(&cfg, k_cholesky, d_S, m, (const int32_t*)d_tfirst, d_rinv, d_ok));
-                int32_t okh = 1;
-                chk(cudaMemcpyAsync(&okh, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-                chk(cudaStreamSynchronize(st));
+                ok = factor_S() && ok;
                 if (e != cudaSuccess) return e;
-                ok = ok && okh != 0;
                 if (ok) {
                     k_chol_solve<<<1, 256, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_bs);
                 } else {
@@ -1313,6 +1390,10 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             scale += 1e-3;
             rho /= scale;
             if (rho > 0 && std::isfinite(chi_new)) {
+                if (vjp) {  // tape: the state before this step and its damping
+                    save_state(cur, (int)vjp->lambdas.size());
+                    vjp->lambdas.push_back(lam_use);
+                }
                 double alpha = 1.0 - std::pow(2 * rho - 1, 3.0);
                 alpha = std::min(alpha, 2.0 / 3.0);
                 lambda *= std::max(1.0 / 3.0, alpha);
@@ -1338,7 +1419,6 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         else if (!std::isfinite(lambda)) out.termination = NAV_BA_TERM_LAMBDA_NONFINITE;
         if (out.termination != NAV_BA_TERM_ITERATIONS) break;
     }
-    if (out.termination == NAV_BA_TERM_ITERATIONS && out.iterations_done < lm.iterations) out.termination = NAV_BA_TERM_ITERATIONS;
     out.final_cost = chi;
     out.final_lambda = lambda;
     out.k1 = kcur[0];
@@ -1350,16 +1430,115 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     chk(cudaMemcpyAsync(out.cams.data(), cams[cur], sizeof(CamState) * nc, cudaMemcpyDeviceToHost, st));
     chk(cudaMemcpyAsync(out.points.data(), A.x[cur], sizeof(double) * 4 * np, cudaMemcpyDeviceToHost, st));
     chk(cudaStreamSynchronize(st));
+    if constexpr (std::is_same<Real, double>::value) {
+        if (bwd && e == cudaSuccess && out.status == NAV_BA_OK) {
+            // ---- backward over the taped steps (vjp_device.cuh) ----
+            const int ns = (int)vjp->lambdas.size();
+            const int rblocks = (nfc * 6 + TB - 1) / TB;
+            // per free camera: sum of the edge vectors (edge adjoints, or A_e t_p with lt) over its items
+            auto cam_sum = [&](const double* src, bool lt) {
+                k_vjp_cam_items<<<iblocks, TB, 0, st>>>(A, d_items, n_items, d_list, src, lt, d_ipart);
+                k_reduce_items<<<rblocks, TB, 0, st>>>(d_ipart, 8, 6, d_item_off, nfc, d_ctmp, 6);
+                chk(cudaGetLastError());
+            };
+            double kb[4] = {0, 0, 0, 0};
+            auto add_k = [&]() {
+                double v4[4];
+                sum_parts(pblocks, 4, v4);
+                for (int k = 0; k < 4; ++k) kb[k] += v4[k];
+            };
+            double* xb = d_cb[0];  // left-tangent adjoint of the current step's output cameras
+            double* xa = d_cb[1];
+            chk(cudaMemsetAsync(d_uvbar, 0, sizeof(double) * 2 * ne, st));
+            if (nfc > 0) {
+                chk(cudaMemsetAsync(xb, 0, sizeof(double) * 6 * nfc, st));
+                k_vjp_seed_cams<<<cblocks, TB, 0, st>>>(cams[cur], d_cam_free, nc, d_posebar, xb);
+            }
+            k_vjp_seed_points<<<(np + TB - 1) / TB, TB, 0, st>>>(d_ptbar, np, d_pbar);
+            // the final cost's term at the final state
+            k_vjp_edges<<<pblocks, TB, 0, st>>>(A, np, camr[cur], A.x[cur], nullptr, nullptr, nullptr, nullptr,
+                                                vjp->cost_bar, d_pbar, d_eadj, d_uvbar, d_part);
+            chk(cudaGetLastError());
+            add_k();
+            if (nfc > 0) {
+                cam_sum(d_eadj, false);
+                k_vjp_axpy<<<rblocks, TB, 0, st>>>(xb, d_ctmp, 1.0, 6 * nfc);
+            }
+            for (int s = ns - 1; s >= 0 && e == cudaSuccess; --s) {
+                const double lam = vjp->lambdas[s];
+                // the state before step s, its linearization and factorization (recomputed)
+                chk(cudaMemcpyAsync(cams[0], d_tape_c + (size_t)s * nc, sizeof(CamState) * nc, cudaMemcpyDeviceToDevice, st));
+                chk(cudaMemcpyAsync(A.x[0], d_tape_x + (size_t)s * 4 * np, sizeof(double) * 4 * np,
+                                    cudaMemcpyDeviceToDevice, st));
+                k_cams_real<double><<<cblocks, TB, 0, st>>>(cams[0], nc, camr[0]);
+                double mxp, mxc;
+                linearize(0, mxp, mxc);
+                k_schur_points<double><<<pblocks, TB, 0, st>>>(A, D, lam, d_part);
+                bool ok = sum_part(pblocks, false) == 0.0;
+                if (nfc > 0) {
+                    assemble_S(lam);
+                    ok = factor_S() && ok;
+                }
+                if (e != cudaSuccess) break;
+                if (!ok) {
+                    out.status = NAV_BA_ERR_UNSUPPORTED;
+                    vjp->why = "backward step " + std::to_string(s) + ": the damped system is not positive definite";
+                    return cudaSuccess;
+                }
+                // the step: dx_c (in d_bs), dx_p
+                if (nfc > 0) k_chol_solve<<<1, 256, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_bs);
+                k_vjp_point_solve<<<pblocks, TB, 0, st>>>(A, np, d_lt, 12, 6, d_bs, d_dp);
+                // adjoint through [+]: rc = J_l^T xbar'_c, xa = Ad^T xbar'_c; r_p = xbar'_p
+                if (nfc > 0) k_vjp_cams_step<<<(nfc + 127) / 128, 128, 0, st>>>(d_bs, xb, d_rc, xa, nfc);
+                // adjoint solve u = (H + lambda I)^-1 r with the same factorization
+                k_vjp_lt_points<<<pblocks, TB, 0, st>>>(A, np, d_pbar, d_tr);
+                if (nfc > 0) {
+                    cam_sum(d_tr, true);
+                    chk(cudaMemcpyAsync(d_uc, d_rc, sizeof(double) * m, cudaMemcpyDeviceToDevice, st));
+                    k_vjp_axpy<<<rblocks, TB, 0, st>>>(d_uc, d_ctmp, -1.0, m);
+                    k_chol_solve<<<1, 256, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_uc);
+                }
+                k_vjp_point_solve<<<pblocks, TB, 0, st>>>(A, np, d_tr, 4, 0, d_uc, d_up);
+                // grad psi at the state: points into d_pbar, cameras into xa, observations, intrinsics
+                k_vjp_edges<<<pblocks, TB, 0, st>>>(A, np, camr[0], A.x[0], nfc > 0 ? d_uc : nullptr, d_up,
+                                                    nfc > 0 ? d_bs : nullptr, d_dp, 0.0, d_pbar, d_eadj, d_uvbar, d_part);
+                chk(cudaGetLastError());
+                add_k();
+                if (nfc > 0) {
+                    cam_sum(d_eadj, false);
+                    k_vjp_axpy<<<rblocks, TB, 0, st>>>(xa, d_ctmp, 1.0, 6 * nfc);
+                }
+                std::swap(xa, xb);
+            }
+            if (e != cudaSuccess) return e;
+            vjp->uv_bar.assign(2LL * ne, 0.0);
+            std::vector<double> pb(4LL * np), cb(6LL * nfc1, 0.0);
+            chk(cudaMemcpyAsync(vjp->uv_bar.data(), d_uvbar, sizeof(double) * 2 * ne, cudaMemcpyDeviceToHost, st));
+            chk(cudaMemcpyAsync(pb.data(), d_pbar, sizeof(double) * 4 * np, cudaMemcpyDeviceToHost, st));
+            if (nfc > 0) chk(cudaMemcpyAsync(cb.data(), xb, sizeof(double) * 6 * nfc, cudaMemcpyDeviceToHost, st));
+            chk(cudaStreamSynchronize(st));
+            if (e != cudaSuccess) return e;
+            for (int k = 0; k < 4; ++k) vjp->intr_bar[k] = kb[k];
+            vjp->pt_bar.assign(3LL * np, 0.0);
+            for (int p = 0; p < np; ++p)
+                if (h.pt_free[p] >= 0)
+                    for (int j = 0; j < 3; ++j) vjp->pt_bar[3LL * p + j] = pb[4LL * p + j];
+            vjp->cam_bar.assign(6LL * nc, 0.0);
+            for (int c = 0; c < nc; ++c)
+                if (h.cam_free[c] >= 0)
+                    for (int j = 0; j < 6; ++j) vjp->cam_bar[6LL * c + j] = cb[6LL * h.cam_free[c] + j];
+        }
+    }
     return e;
 }
 
 }  // namespace
 
 cudaError_t grid_solve(const HostWindow& h, const LmOptions& lm, const Intr& intr, int precision, cudaStream_t stream,
-                       int cluster, GridResult& out, double debug_lambda, std::vector<double>* debug_S) {
+                       int cluster, GridResult& out, double debug_lambda, std::vector<double>* debug_S, GridVjp* vjp) {
     if (precision == NAV_BA_MIXED)
-        return grid_solve_typed<float>(h, lm, intr, stream, cluster, out, debug_lambda, debug_S);
-    return grid_solve_typed<double>(h, lm, intr, stream, cluster, out, debug_lambda, debug_S);
+        return grid_solve_typed<float>(h, lm, intr, stream, cluster, out, debug_lambda, debug_S, vjp && !vjp->backward ? vjp : nullptr);
+    return grid_solve_typed<double>(h, lm, intr, stream, cluster, out, debug_lambda, debug_S, vjp);
 }
 
 }  // namespace navba

@@ -3,6 +3,7 @@
 // Replaces nav24's GraphOptim::solve (core/backEnd/BE_GraphOptim.cpp:31-77): graph build
 // (structure.cpp), LM on the device (window_engine.cu), write-back of poses and points.
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -269,19 +270,9 @@ nav_ba_status download_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n
     return NAV_BA_OK;
 }
 
-// One problem beyond the window engine's limits, on the grid engine; fills r (outputs and stats).
-nav_ba_status solve_grid_window(nav_ba_ctx* ctx, const nav_ba_problem& p, const HostWindow& h, const nav_ba_options& o,
-                                nav_ba_result& r) {
-    GridResult g;
-    cudaEventRecord(ctx->ev0, ctx->stream);
-    cudaError_t e = grid_solve(h, lm_options(o), intrinsics_of(p), o.precision, ctx->stream, ctx->grid_cluster, g, -1.0,
-                               nullptr);
-    cudaEventRecord(ctx->ev1, ctx->stream);
-    if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev1);
-    if (e != cudaSuccess) return cuda_status(ctx, e, "grid engine");
-    if (g.status != NAV_BA_OK) return set_err(ctx, (nav_ba_status)g.status, "non-finite initial cost");
-    float t = 0.f;
-    cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1);
+// Outputs and statistics of a grid-engine solve.
+void fill_grid_result(const nav_ba_problem& p, const HostWindow& h, const nav_ba_options& o, const GridResult& g,
+                      nav_ba_result& r) {
     r.status = NAV_BA_OK;
     r.initial_cost = g.initial_cost;
     r.final_cost = g.final_cost;
@@ -295,7 +286,6 @@ nav_ba_status solve_grid_window(nav_ba_ctx* ctx, const nav_ba_problem& p, const 
     r.n_free_points = h.nfp;
     r.n_schur_blocks = h.n_schur_blocks;
     r.edge_iterations = (int64_t)h.ne * g.iterations_done;
-    r.time_solve_ms += t;
     if (r.cam_pose_out)
         for (int c = 0; c < p.n_cams; ++c) pose12_from_cam(g.cams[c], r.cam_pose_out + 12LL * c);
     if (r.points_out)
@@ -311,6 +301,23 @@ nav_ba_status solve_grid_window(nav_ba_ctx* ctx, const nav_ba_problem& p, const 
     r.pcg_iterations_total = g.pcg_iterations;
     if (r.cost_trace)
         for (int k = 0; k <= g.iterations_done; ++k) r.cost_trace[k] = g.trace[k];
+}
+
+// One problem beyond the window engine's limits, on the grid engine; fills r (outputs and stats).
+nav_ba_status solve_grid_window(nav_ba_ctx* ctx, const nav_ba_problem& p, const HostWindow& h, const nav_ba_options& o,
+                                nav_ba_result& r) {
+    GridResult g;
+    cudaEventRecord(ctx->ev0, ctx->stream);
+    cudaError_t e = grid_solve(h, lm_options(o), intrinsics_of(p), o.precision, ctx->stream, ctx->grid_cluster, g, -1.0,
+                               nullptr);
+    cudaEventRecord(ctx->ev1, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev1);
+    if (e != cudaSuccess) return cuda_status(ctx, e, "grid engine");
+    if (g.status != NAV_BA_OK) return set_err(ctx, (nav_ba_status)g.status, "non-finite initial cost");
+    float t = 0.f;
+    cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1);
+    fill_grid_result(p, h, o, g, r);
+    r.time_solve_ms += t;
     return NAV_BA_OK;
 }
 
@@ -352,7 +359,7 @@ nav_ba_status solve_impl(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, co
     const double t_down = ms_since(t1);
     for (int i = 0; i < n; ++i) {
         tmp[i].time_setup_ms = t_setup;
-        tmp[i].time_solve_ms = t_solve;
+        tmp[i].time_solve_ms += t_solve;  // grid-engine problems already hold their own solve time
         tmp[i].time_download_ms = t_down;
         results[i] = tmp[i];
     }
@@ -634,6 +641,92 @@ nav_ba_status nav_ba_solve_noalloc(nav_ba_ctx* ctx, const nav_ba_problem* p, con
     }
     if (st != NAV_BA_OK) return set_err(ctx, st, why);
     *r = tmp;
+    return NAV_BA_OK;
+}
+
+nav_ba_status nav_ba_vjp(nav_ba_ctx* ctx, const nav_ba_problem* p, const nav_ba_options* o, nav_ba_schedule* sched,
+                         const nav_ba_cotangent* cot, nav_ba_result* r, nav_ba_grads* grads) {
+    if (!ctx) return NAV_BA_ERR_ARGUMENT;
+    if (!p || !o || !sched || !r) return set_err(ctx, NAV_BA_ERR_ARGUMENT, "NULL argument");
+    cudaSetDevice(ctx->device);
+    std::string why;
+    nav_ba_status st = validate_options(o, &why);
+    if (st == NAV_BA_OK) st = validate_problem(p, &why);
+    if (st != NAV_BA_OK) return set_err(ctx, st, why);
+    if (o->precision != NAV_BA_FP64 || o->solver != NAV_BA_SOLVER_CHOLESKY || p->camera_model != NAV_BA_CAM_PINHOLE ||
+        o->optimize_distortion)
+        return set_err(ctx, NAV_BA_ERR_UNSUPPORTED,
+                       "the VJP needs FP64 precision, the Cholesky solver and the pinhole model without distortion");
+    GridVjp v;
+    v.replay = sched->replay != 0;
+    if (v.replay) {
+        if (sched->n_steps < 0 || sched->n_steps > NAV_BA_VJP_MAX_STEPS)
+            return set_err(ctx, NAV_BA_ERR_ARGUMENT, "schedule n_steps out of range");
+        for (int s = 0; s < sched->n_steps; ++s)
+            if (!std::isfinite(sched->lambda[s]) || sched->lambda[s] < 0.0)
+                return set_err(ctx, NAV_BA_ERR_ARGUMENT, "schedule damping must be finite and >= 0");
+        v.lambdas.assign(sched->lambda, sched->lambda + sched->n_steps);
+    } else if (o->iterations > NAV_BA_VJP_MAX_STEPS) {
+        return set_err(ctx, NAV_BA_ERR_UNSUPPORTED, "more LM iterations than NAV_BA_VJP_MAX_STEPS");
+    }
+    const bool bwd = cot && grads;
+    v.backward = bwd;
+    if (bwd) {
+        if (!std::isfinite(cot->cost)) return set_err(ctx, NAV_BA_ERR_NONFINITE_INPUT, "non-finite cost cotangent");
+        v.cost_bar = cot->cost;
+        v.pose_bar = cot->cam_pose;
+        v.point_bar = cot->points;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    HostWindow h;
+    build_window(*p, *o, h);
+    if (p->n_cams == 0 || h.ne == 0) {  // nothing is optimized: outputs are the inputs
+        write_passthrough(*p, r, false);
+        clear_stats(r);
+        r->termination = NAV_BA_TERM_NOTHING_TO_DO;
+        r->status = NAV_BA_EMPTY;
+        if (!v.replay) sched->n_steps = 0;
+        if (bwd) {
+            if (grads->obs_uv) std::memset(grads->obs_uv, 0, sizeof(double) * 2 * p->n_obs);
+            std::memset(grads->intrinsics, 0, sizeof(grads->intrinsics));
+            if (grads->cam_tangent) std::memset(grads->cam_tangent, 0, sizeof(double) * 6 * p->n_cams);
+            if (grads->points) std::memset(grads->points, 0, sizeof(double) * 3 * p->n_points);
+        }
+        return NAV_BA_EMPTY;
+    }
+    const double t_setup = ms_since(t0);
+    GridResult g;
+    cudaEventRecord(ctx->ev0, ctx->stream);
+    cudaError_t e = grid_solve(h, lm_options(*o), intrinsics_of(*p), NAV_BA_FP64, ctx->stream, ctx->grid_cluster, g, -1.0,
+                               nullptr, &v);
+    cudaEventRecord(ctx->ev1, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev1);
+    if (e != cudaSuccess) return cuda_status(ctx, e, "grid engine (vjp)");
+    if (g.status != NAV_BA_OK)
+        return set_err(ctx, (nav_ba_status)g.status, v.why.empty() ? std::string("non-finite initial cost") : v.why);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1);
+    clear_stats(r);
+    fill_grid_result(*p, h, *o, g, *r);
+    r->time_setup_ms = t_setup;
+    r->time_solve_ms = t;
+    if (!v.replay) {
+        sched->n_steps = (int32_t)v.lambdas.size();
+        for (int s = 0; s < sched->n_steps; ++s) sched->lambda[s] = v.lambdas[s];
+    }
+    if (bwd) {
+        if (grads->obs_uv) {
+            std::memset(grads->obs_uv, 0, sizeof(double) * 2 * p->n_obs);
+            for (int k = 0; k < h.ne; ++k) {
+                grads->obs_uv[2LL * h.edge_obs[k]] = v.uv_bar[2LL * k];
+                grads->obs_uv[2LL * h.edge_obs[k] + 1] = v.uv_bar[2LL * k + 1];
+            }
+        }
+        std::memset(grads->intrinsics, 0, sizeof(grads->intrinsics));
+        for (int k = 0; k < 4; ++k) grads->intrinsics[k] = v.intr_bar[k];
+        if (grads->cam_tangent) std::memcpy(grads->cam_tangent, v.cam_bar.data(), sizeof(double) * 6 * p->n_cams);
+        if (grads->points) std::memcpy(grads->points, v.pt_bar.data(), sizeof(double) * 3 * p->n_points);
+    }
     return NAV_BA_OK;
 }
 

@@ -404,8 +404,10 @@ extern "C" nav_synth* nav_synth_create(const nav_synth_params* prm) {
                 Rwc = matmul(Rwc, expso3(om));
                 const Vec3 xc = {Rwc[0], Rwc[3], Rwc[6]}, yc = {Rwc[1], Rwc[4], Rwc[7]},
                            zc = {Rwc[2], Rwc[5], Rwc[8]};
-                const Vec3 d = normalize(add(xc, add(scale(zc, 0.3 * rng.normal()),
-                                                     scale(yc, 0.3 * rng.normal()))));
+                // draws sequenced explicitly: function arguments have no evaluation order
+                const double jz = rng.normal();
+                const double jy = rng.normal();
+                const Vec3 d = normalize(add(xc, add(scale(zc, 0.3 * jz), scale(yc, 0.3 * jy))));
                 C = add(C, scale(d, 0.3));
             }
             const Vec3 box_c = add(scale(csum, 1.0 / nc), scale(normalize(zsum), 6.0));
@@ -510,7 +512,9 @@ extern "C" nav_synth* nav_synth_create(const nav_synth_params* prm) {
             w, rng, np, truth, 1.0, 40.0, 2,
             [&] {
                 const double L = rng.uniform(0.0, arc[nt] * sc);
-                return pos(at_arc(L), rng.uniform(-5.0, 5.0), rng.uniform(0.0, 3.0));
+                const double lateral = rng.uniform(-5.0, 5.0);
+                const double height = rng.uniform(0.0, 3.0);
+                return pos(at_arc(L), lateral, height);
             },
             [&] { return rng.uniform_int(6, 10); }, cands);
         emit_window(S, rng, w, truth, noise, outl, rot_p, trans_p, pt_p);

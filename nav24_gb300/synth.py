@@ -23,10 +23,8 @@ _LIB = None
 def _lib():
     global _LIB
     if _LIB is None:
-        path = Path(__file__).resolve().parent / "_build" / "libnavsynth.so"
-        if not path.exists():
-            from .build import build_synth
-            build_synth()
+        from .build import build_synth
+        path = build_synth()  # rebuilds only when a source or header is newer than the library
         lib = C.CDLL(str(path))
         lib.nav_synth_create.restype = C.c_void_p
         lib.nav_synth_create.argtypes = [C.POINTER(abi.nav_synth_params)]

@@ -836,7 +836,10 @@ public:
         kn[1] = k[1] + dk[1];
     }
 
-    int32_t solve(nav_ba_result* res) {
+    // record != null: the damping of every accepted step is appended.  replay != null: those
+    // steps are applied unconditionally instead of the LM control (the frozen-schedule function
+    // that the product's nav_ba_vjp differentiates).
+    int32_t solve(nav_ba_result* res, std::vector<double>* record = nullptr, const std::vector<double>* replay = nullptr) {
         const int iters = O.iterations;
         double chi = cost(T, X, k);
         res->initial_cost = chi;
@@ -854,6 +857,30 @@ public:
         double lambda = 0.0, nu = 2.0;
         int it = 0;
         int acc = 0, rej = 0;
+        if (replay) {
+            for (const double lam : *replay) {
+                linearize();
+                if (!compute_step(lam)) return NAV_BA_ERR_UNSUPPORTED;
+                std::vector<SE3> Tn;
+                std::vector<double> Xn;
+                double kn[2];
+                apply_step(Tn, Xn, kn);
+                T.swap(Tn);
+                X.swap(Xn);
+                k[0] = kn[0];
+                k[1] = kn[1];
+                chi = cost(T, X, k);
+                ++it;
+                if (res->cost_trace) res->cost_trace[it] = chi;
+                lambda = lam;
+            }
+            res->iterations_done = it;
+            res->trials_accepted = it;
+            res->trials_rejected = 0;
+            res->final_cost = chi;
+            res->final_lambda = lambda;
+            return NAV_BA_OK;
+        }
         for (; it < iters; ++it) {
             linearize();
             if (it == 0) {
@@ -875,6 +902,7 @@ public:
                 scale += 1e-3;
                 rho /= scale;
                 if (rho > 0 && std::isfinite(chi_new)) {
+                    if (record) record->push_back(lambda);
                     double alpha = 1.0 - std::pow(2 * rho - 1, 3);
                     alpha = std::min(alpha, 2.0 / 3.0);
                     const double sf = std::max(1.0 / 3.0, alpha);
@@ -943,8 +971,8 @@ int count_schur_blocks(const Solver& s) {
 
 }  // namespace
 
-extern "C" int32_t oracle_solve(const nav_ba_problem* p, const nav_ba_options* o, nav_ba_result* r,
-                                int32_t n_threads) {
+extern "C" int32_t oracle_solve_schedule(const nav_ba_problem* p, const nav_ba_options* o, nav_ba_result* r,
+                                         int32_t n_threads, nav_ba_schedule* sched) {
     if (!o || !r) return NAV_BA_ERR_ARGUMENT;
     int32_t st = validate(p);
     if (st != NAV_BA_OK) return st;
@@ -960,11 +988,25 @@ extern "C" int32_t oracle_solve(const nav_ba_problem* p, const nav_ba_options* o
         r->iterations_done = 0;
         return NAV_BA_EMPTY;
     }
-    st = s.solve(r);
+    std::vector<double> rec, rep;
+    if (sched && sched->replay) {
+        if (sched->n_steps < 0 || sched->n_steps > NAV_BA_VJP_MAX_STEPS) return NAV_BA_ERR_ARGUMENT;
+        rep.assign(sched->lambda, sched->lambda + sched->n_steps);
+    }
+    st = s.solve(r, sched && !sched->replay ? &rec : nullptr, sched && sched->replay ? &rep : nullptr);
     if (st != NAV_BA_OK) return st;
+    if (sched && !sched->replay) {
+        sched->n_steps = (int32_t)rec.size();
+        for (size_t i = 0; i < rec.size() && i < NAV_BA_VJP_MAX_STEPS; ++i) sched->lambda[i] = rec[i];
+    }
     r->n_schur_blocks = count_schur_blocks(s);
     s.write_outputs(r);
     return NAV_BA_OK;
+}
+
+extern "C" int32_t oracle_solve(const nav_ba_problem* p, const nav_ba_options* o, nav_ba_result* r,
+                                int32_t n_threads) {
+    return oracle_solve_schedule(p, o, r, n_threads, nullptr);
 }
 
 extern "C" int32_t oracle_linearize(const nav_ba_problem* p, const nav_ba_options* o, double* e,

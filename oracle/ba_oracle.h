@@ -20,6 +20,12 @@ extern "C" {
 int32_t oracle_solve(const nav_ba_problem* p, const nav_ba_options* o, nav_ba_result* r,
                      int32_t n_threads);
 
+/* oracle_solve with a damping schedule (the twin of nav_ba_vjp's forward): sched->replay == 0
+ * records the damping of every accepted step; sched->replay == 1 applies the given steps
+ * unconditionally (x <- x [+] (H + lambda I)^-1 b at the current state, for each lambda). */
+int32_t oracle_solve_schedule(const nav_ba_problem* p, const nav_ba_options* o, nav_ba_result* r,
+                              int32_t n_threads, nav_ba_schedule* sched);
+
 /* Twin of nav_ba_linearize (FP64). */
 int32_t oracle_linearize(const nav_ba_problem* p, const nav_ba_options* o, double* e,
                          double* jc, double* jp, double* w);

@@ -20,6 +20,8 @@ def lib():
         dp = C.POINTER(C.c_double)
         L.oracle_solve.argtypes = [P, O, R, C.c_int32]
         L.oracle_solve.restype = C.c_int32
+        L.oracle_solve_schedule.argtypes = [P, O, R, C.c_int32, C.POINTER(abi.nav_ba_schedule)]
+        L.oracle_solve_schedule.restype = C.c_int32
         L.oracle_linearize.argtypes = [P, O, dp, dp, dp, dp]
         L.oracle_linearize.restype = C.c_int32
         L.oracle_distortion_jacobian.argtypes = [P, dp]
@@ -44,6 +46,16 @@ def solve(prob: abi.Problem, opt: abi.nav_ba_options, n_threads: int = 1) -> abi
     p = prob.as_c()
     st = lib().oracle_solve(C.byref(p), C.byref(opt), C.byref(buf.c), n_threads)
     return buf.result(st)
+
+
+def solve_schedule(prob: abi.Problem, opt: abi.nav_ba_options, lambdas=None, n_threads: int = 1):
+    """Record (lambdas None) or replay the damping schedule; returns (Result, lambdas)."""
+    replay = lambdas is not None
+    sched = abi.nav_ba_schedule.of(lambdas if replay else [], replay)
+    buf = abi.ResultBuffers(prob, max(opt.iterations, len(lambdas) if replay else 0))
+    p = prob.as_c()
+    st = lib().oracle_solve_schedule(C.byref(p), C.byref(opt), C.byref(buf.c), n_threads, C.byref(sched))
+    return buf.result(st), sched.lambdas
 
 
 def linearize(prob: abi.Problem, opt: abi.nav_ba_options):

@@ -43,6 +43,8 @@ int main(void) {{
          sizeof(nav_synth_params));
   printf("%zu %zu %zu %zu\\n", offsetof(nav_ba_problem, intrinsics), offsetof(nav_ba_options, pcg_tolerance),
          offsetof(nav_ba_result, status), offsetof(nav_synth_params, min_points));
+  printf("%zu %zu %zu %zu %zu\\n", sizeof(nav_ba_schedule), sizeof(nav_ba_cotangent), sizeof(nav_ba_grads),
+         offsetof(nav_ba_schedule, lambda), offsetof(nav_ba_grads, cam_tangent));
   return 0;
 }}
 """)
@@ -53,7 +55,9 @@ int main(void) {{
     want = [C.sizeof(abi.nav_ba_problem), C.sizeof(abi.nav_ba_options), C.sizeof(abi.nav_ba_result),
             C.sizeof(abi.nav_synth_params), abi.nav_ba_problem.intrinsics.offset,
             abi.nav_ba_options.pcg_tolerance.offset, abi.nav_ba_result.status.offset,
-            abi.nav_synth_params.min_points.offset]
+            abi.nav_synth_params.min_points.offset,
+            C.sizeof(abi.nav_ba_schedule), C.sizeof(abi.nav_ba_cotangent), C.sizeof(abi.nav_ba_grads),
+            abi.nav_ba_schedule.lam.offset, abi.nav_ba_grads.cam_tangent.offset]
     assert got == want
 
 

@@ -304,5 +304,28 @@ def test_distortion_is_recovered():
                             optimize_distortion=1, pcg_tolerance=1e-8, pcg_max_iterations=500)
     r = oracle.solve(p, o, n_threads=4)
     assert r.status == abi.OK
-    assert abs(r.intrinsics[4] - s.intrinsics[4]) < 2e-3 and abs(r.intrinsics[5] - s.intrinsics[5]) < 2e-3
+    # k1 and k2 are strongly anti-correlated; the radial factor d(r) = 1 + k1 r^2 + k2 r^4 they
+    # define is what the data determine.  Over the image (r^2 <= 0.64 at the corners) it is
+    # recovered to 1e-3 (0.4 px at the corner), from a start 10x further off.
+    r2 = np.linspace(0.0, 0.64, 65)
+    dd = lambda k: k[4] * r2 + k[5] * r2 * r2
+    assert np.max(np.abs(dd(r.intrinsics) - dd(s.intrinsics))) < 1e-3
+    assert np.max(np.abs(dd(p.intrinsics) - dd(s.intrinsics))) > 1e-2
     assert r.cost_trace[-1] < 0.05 * r.cost_trace[0]
+
+
+def test_schedule_replay_reproduces_the_solve():
+    """Replaying the recorded damping of the accepted steps reproduces the LM solve exactly: the
+    frozen-schedule function that the backward differentiates agrees with the solve at the
+    recorded inputs."""
+    from nav24_gb300.synth import Synth
+    p = Synth(3, n_cams=12, n_points=600, seed=3).window(0)
+    o = abi.default_options(iterations=5, robust=1, huber_delta=2.0)
+    r, lam = oracle.solve_schedule(p, o)
+    assert r.status == abi.OK and len(lam) == r.stats["trials_accepted"] >= 1
+    r2, _ = oracle.solve_schedule(p, o, lam)
+    assert r2.status == abi.OK
+    assert r2.stats["final_cost"] == r.stats["final_cost"]
+    assert np.array_equal(r2.cam_pose, r.cam_pose) and np.array_equal(r2.points, r.points)
+    r0 = oracle.solve(p, o)
+    assert r0.stats["final_cost"] == r.stats["final_cost"]
