@@ -14,6 +14,11 @@ LM iterations/s of both and the final-cost agreement of the two forms.
 `--impl reference` times nav24's BA algorithm on the host cores instead: the reference's own g2o
 path cannot be built here (g2o, Eigen, OpenCV are absent), so the CPU restatement of it
 (oracle/, FP64, one window per thread, all host threads) runs the same workload.
+
+The line also carries, under "workloads", one solve of each other named workload on the same GPU
+(after one warm-up solve): the 200-camera grid (mixed vs FP64), the differentiable sphere cap
+(forward and backward through K = 5 LM steps) and the large robust figure-eight with shared
+distortion (PCG, mixed vs FP64).  `--no-secondary` skips them.
 """
 from __future__ import annotations
 
@@ -46,8 +51,10 @@ def parse():
     ap.add_argument("--workload", choices=["windows"], default="windows")
     ap.add_argument("--windows", type=int, default=512)
     ap.add_argument("--cpu-sample", type=int, default=512, help="windows in the CPU baseline sample")
-    ap.add_argument("--profile-case", choices=["mixed", "fp64"], default=None,
-                    help="run only the device-resident solves of one precision (for profiler captures)")
+    ap.add_argument("--profile-case", choices=["mixed", "fp64", "grid", "pcg", "vjp"], default=None,
+                    help="run only the device-resident solves of one precision (mixed, fp64), or one solve of a "
+                         "secondary workload (for profiler captures)")
+    ap.add_argument("--no-secondary", action="store_true", help="skip the secondary workloads")
     return ap.parse_args()
 
 
@@ -233,6 +240,58 @@ def time_device(ctx, wins, opt, steps, warmup, dist):
     return ms, stats, results
 
 
+def solve_pair(ctx, p, family):
+    """One warm-up and one timed solve of problem p in each precision; device time per solve."""
+    from nav24_gb300 import abi
+    from nav24_gb300.synth import workload_options
+    out = {}
+    for name, prec in (("fp64", abi.FP64), ("mixed", abi.MIXED)):
+        o = workload_options(family, prec)
+        ctx.solve(p, o)
+        r = ctx.solve(p, o)
+        t = r.stats["time_solve_ms"] * 1e-3
+        out[name] = {"obs_per_s": r.stats["edge_iterations"] / t, "lm_iter_per_s": r.stats["iterations_done"] / t,
+                     "ms": t * 1e3, "final_cost": r.stats["final_cost"], "initial_cost": r.stats["initial_cost"],
+                     "iterations": r.stats["iterations_done"], "pcg_iterations": r.stats["pcg_iterations_total"]}
+    out["mixed_over_fp64"] = out["mixed"]["obs_per_s"] / out["fp64"]["obs_per_s"]
+    out["final_cost_rel_diff"] = abs(out["mixed"]["final_cost"] - out["fp64"]["final_cost"]) / out["fp64"]["final_cost"]
+    return out
+
+
+def secondary_workloads(ctx, only=None):
+    """One solve of each other named workload (device time, including the per-solve upload)."""
+    from nav24_gb300 import abi
+    from nav24_gb300.synth import Synth, workload_options
+    out = {}
+    if only in (None, "grid"):
+        p = Synth(1).window(0)
+        out["grid_200cams"] = {"workload": "200 cameras on a 20x10 grid facing down, 50,000 points, Huber 2 px, "
+                                           "20 LM iterations (family 1, seed 1001), grid engine, Cholesky",
+                               "observations": p.n_obs, **solve_pair(ctx, p, 1)}
+    if only in (None, "vjp"):
+        p = Synth(3).window(0)
+        o = workload_options(3)
+        ctx.vjp(p, o)
+        t0 = time.perf_counter()
+        r, lam, _ = ctx.vjp(p, o)
+        t1 = time.perf_counter()
+        _, _, g = ctx.vjp(p, o, lam, cost_bar=1.0)
+        t2 = time.perf_counter()
+        out["differentiable_cap"] = {
+            "workload": "50 cameras on a sphere cap, 10,000 points, Huber 2 px, K = 5 LM iterations (family 3, "
+                        "seed 1003); VJP w.r.t. observations and intrinsics", "observations": p.n_obs,
+            "forward_ms": (t1 - t0) * 1e3, "replay_and_backward_ms": (t2 - t1) * 1e3, "steps": len(lam),
+            "forward_obs_per_s": r.stats["edge_iterations"] / (t1 - t0), "final_cost": r.stats["final_cost"],
+            "timing": "wall clock of the C-ABI call (host graph build, upload, device work, download)"}
+    if only in (None, "pcg"):
+        p = Synth(4).window(0)
+        out["figure_eight_pcg"] = {
+            "workload": "1000 cameras on a 2 km figure-eight, 500,000 points, shared radial k1/k2 optimized, 5% "
+                        "outliers, Huber 1.5 px, 30 LM iterations, PCG (block-Jacobi, tol 1e-6, <= 100 iterations) "
+                        "(family 4, seed 1004), grid engine", "observations": p.n_obs, **solve_pair(ctx, p, 4)}
+    return out
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -251,6 +310,11 @@ def main():
     om = workload_options(2, abi.MIXED)
     of = workload_options(2, abi.FP64)
 
+    if args.profile_case in ("grid", "pcg", "vjp"):
+        print(json.dumps(secondary_workloads(ctx, args.profile_case)), flush=True)
+        ctx.close()
+        dist.close()
+        return
     if args.profile_case:
         o = om if args.profile_case == "mixed" else of
         ms, st, _ = time_device(ctx, wins, o, args.steps, args.warmup, dist)
@@ -305,12 +369,22 @@ def main():
 
     # CPU baseline: the FP64 restatement on this host, all threads, bounded sample
     cpu = None
+    oracle_diff = None
     if rank == 0:
         nth = os.cpu_count() or 1
         sample = wins[: args.cpu_sample]
-        dt, ei, its, _ = cpu_reference(sample, of, nth)
+        dt, ei, its, res_o = cpu_reference(sample, of, nth)
         cpu = {"value": ei / dt, "unit": UNIT, "cores": nth, "kind": "port",
                "sample": f"{len(sample)} windows x 10 LM iterations (FP64 oracle), one window per thread"}
+        # "same final cost": both GPU forms against the FP64 oracle, per window
+        oracle_diff = {
+            name: max(abs(a.stats["final_cost"] - b.stats["final_cost"]) / b.stats["final_cost"]
+                      for a, b in zip(res, res_o) if b.stats["final_cost"] > 0)
+            for name, res in (("mixed", res_m), ("fp64", res_f))}
+
+    secondary = None
+    if rank == 0 and not args.no_secondary:
+        secondary = secondary_workloads(ctx)
 
     if rank == 0:
         line = {
@@ -327,12 +401,14 @@ def main():
             "fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": t_f * 1e3, "lm_iter_per_s": it_f / t_f},
             "mixed_over_fp64": value / fp64_value,
             "final_cost_rel_diff_max": cost_rel,
+            "final_cost_rel_diff_vs_oracle_max": oracle_diff,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_time * 1e3},
             "roofline": roofline,
             "cpu_baseline": cpu,
             "clocks": clocks,
             "gpu_launches": args.steps,
+            "workloads": secondary,
         }
         print(json.dumps(line), flush=True)
     ctx.close()

@@ -106,7 +106,17 @@ bool fits_window_engine(const HostWindow& h) {
 
 // Autotuner of the window kernel's launch shape: every candidate (cluster size x threads per
 // CTA) solves the prepared batch once; the fastest is kept for the context and precision.
+// NAVBA_WINDOW_SHAPE="<cluster>,<threads>" fixes the shape instead (no tuning launches), e.g. to
+// profile one known launch.
 cudaError_t autotune(nav_ba_ctx* ctx, PreparedBatch& pb, int precision) {
+    const char* fixed = getenv("NAVBA_WINDOW_SHAPE");
+    int fc = 0, ft = 0;
+    if (fixed && sscanf(fixed, "%d,%d", &fc, &ft) == 2 && (fc == 1 || fc == 2 || fc == 4 || fc == 8) &&
+        (ft == 256 || (ft == 512 && precision == NAV_BA_MIXED))) {
+        ctx->shape[precision] = WindowLaunch{fc, ft};
+        ctx->tuned[precision] = true;
+        return cudaSuccess;
+    }
     const int ths_fp64[] = {256};
     const int ths_mixed[] = {256, 512};
     const int* ths = precision == NAV_BA_MIXED ? ths_mixed : ths_fp64;

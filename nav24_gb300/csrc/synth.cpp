@@ -224,10 +224,13 @@ void emit_window(nav_synth* S, Rng& rng, const Window& w, const Intr& truth, dou
         const Pose& p = w.cams[c];
         Pose q = p;
         if (!w.cam_fixed[c]) {
+            // orientation perturbed by exp(om) and the camera centre C = -R^T t by a translation
+            // (perturbing t directly would also move the centre by |t| * |om|, metres on a 2 km path)
             const Vec3 om = {rng.normal() * rot_p, rng.normal() * rot_p, rng.normal() * rot_p};
+            const Vec3 dC = {rng.normal() * trans_p, rng.normal() * trans_p, rng.normal() * trans_p};
+            const Vec3 C = add(scale(matvec(transpose(p.R), p.t), -1.0), dC);
             q.R = matmul(expso3(om), p.R);
-            q.t = {p.t[0] + rng.normal() * trans_p, p.t[1] + rng.normal() * trans_p,
-                   p.t[2] + rng.normal() * trans_p};
+            q.t = scale(matvec(q.R, C), -1.0);
         }
         for (int r = 0; r < 3; ++r) {
             for (int k = 0; k < 3; ++k) {
