@@ -146,6 +146,35 @@ NAVBA_HD void se3_left_update(const double* d, const CamState& in, CamState& out
     out.pad1 = 0.0;
 }
 
+// The step exp(d) of se3_left_update as E - I (row-major 3x3) and E_t = V upsilon, with the same
+// branches, without forming I + (small term): the change of a transformed point under the step,
+// (E - I) y + E_t, keeps its relative precision when rounded to FP32.
+NAVBA_HD void se3_exp_delta(const double* d, double* EmI, double* Et) {
+    const double w0 = d[0], w1 = d[1], w2 = d[2];
+    const double th = sqrt(w0 * w0 + w1 * w1 + w2 * w2);
+    const double W[9] = {0, -w2, w1, w2, 0, -w0, -w1, w0, 0};
+    double W2[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            W2[i * 3 + j] = W[i * 3 + 0] * W[0 * 3 + j] + W[i * 3 + 1] * W[1 * 3 + j] + W[i * 3 + 2] * W[2 * 3 + j];
+    double a = 1.0, b = 1.0, cc = 1.0, vb = 1.0;  // small-angle branch: R = V = I + W + W^2
+    if (!(th < 0.00001)) {
+        double s, c;
+        sincos(th, &s, &c);
+        a = s / th;
+        b = (1 - c) / (th * th);
+        cc = (th - s) / (th * th * th);
+        vb = b;
+    }
+    for (int k = 0; k < 9; ++k) EmI[k] = a * W[k] + b * W2[k];
+    // V - I = vb W + cc W^2 (small-angle: W + W^2)
+    for (int i = 0; i < 3; ++i) {
+        double v = d[3 + i];
+        for (int j = 0; j < 3; ++j) v += (vb * W[i * 3 + j] + cc * W2[i * 3 + j]) * d[3 + j];
+        Et[i] = v;
+    }
+}
+
 // ---- edge ------------------------------------------------------------------------------
 
 template <class Real>

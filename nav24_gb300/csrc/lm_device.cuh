@@ -32,6 +32,7 @@ struct WinArgs {
     Real* pt_lt;
     Real* edge_w;
     Real* edge_a;
+    Real* edge_e[2];          // mixed form: residual (u, v) of each edge at the current / trial state
     int32_t* cam_list;
     uint32_t* pairs;
     CamState* cam_out;
@@ -144,10 +145,11 @@ struct Rec<double> {
 };
 
 // Cluster-split robust chi2 of the window for cameras `camc` (12 values per camera, precision
-// Cost) and points X; returns this thread's partial sum.
+// Cost) and points X; returns this thread's partial sum.  e_out != null: each edge's residual is
+// also written there (2 values per edge, rounded to Real).
 template <class Cost, class Real>
 __device__ double cost_partial(const WinArgs<Real>& A, const CC& c, const WinDesc& D, const Cost* camc,
-                               const double* X) {
+                               const double* X, Real* e_out = nullptr) {
     double acc = 0.0;
     const Cost delta = (Cost)A.lm.huber_delta;
     for (int p = c.gt; p < D.npt; p += c.CT) {
@@ -157,7 +159,20 @@ __device__ double cost_partial(const WinArgs<Real>& A, const CC& c, const WinDes
         for (int e = A.pt_eoff[gp]; e < e1; ++e) {
             const Cost* cr = camc + 12 * A.edge_cam[e];
             const Cost z[2] = {(Cost)A.edge_uv[2LL * e], (Cost)A.edge_uv[2LL * e + 1]};
-            acc += edge_cost<Cost>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta);
+            if (e_out) {
+                Cost Xc[3], uv[2];
+                transform(cr, cr + 9, Xr, Xc);
+                project<Cost>(A.intr, Xc, uv, nullptr);
+                const Cost e0 = z[0] - uv[0], e1v = z[1] - uv[1];
+                double rho;
+                Cost w;
+                huber<Cost>(e0 * e0 + e1v * e1v, A.lm.robust != 0, delta, rho, w);
+                acc += rho;
+                e_out[2LL * e] = (Real)e0;
+                e_out[2LL * e + 1] = (Real)e1v;
+            } else {
+                acc += edge_cost<Cost>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta);
+            }
         }
     }
     return acc;
@@ -294,6 +309,102 @@ __device__ double update_points(const WinArgs<Real>& A, const CC& c, const WinDe
               (double)d2 * (lambda * (double)d2 + (double)vg[8]);
     }
     return sc;
+}
+
+// Mixed form: the trial points of update_points fused with the trial cost change.  For every edge
+// of the window's points the residual change is formed from the state change, in Real, without
+// cancellation against the pixel coordinates:
+//   Xc' - Xc = (E - I)(Xc + R dX) + R dX + E_t     (E, E_t: the camera's step exp(dx_c), camdel)
+//   dpi = pi(Xc') - pi(Xc) = f (dx z - x dz) / (z z'),   e' = e - dpi,
+//   d rho = ds = -dpi . (e + e')  (both quadratic),  2 delta ds / (sqrt s' + sqrt s)  (both Huber),
+// so each d rho carries Real's relative precision of the change itself, not of the pixel values.
+// e of the current state is read from edge_e[cur], e' written to edge_e[cur ^ 1].  Pinhole model.
+// Returns (this thread's dx^T(lambda dx + g) part, its Kahan-compensated d chi part).
+template <class Real>
+__device__ double2 update_points_dcost(const WinArgs<Real>& A, const CC& c, const WinDesc& D, double lambda,
+                                       const double* dcl, int cur, const Real* camr, const Real* camdel) {
+    const double* Xc = A.x[cur];
+    double* Xt = A.x[cur ^ 1];
+    const Real* ecur = A.edge_e[cur];
+    Real* etr = A.edge_e[cur ^ 1];
+    const Real fx = (Real)A.intr.fx, fy = (Real)A.intr.fy;
+    const bool robust = A.lm.robust != 0;
+    const Real hd = (Real)A.lm.huber_delta, hd2 = hd * hd;
+    double sc = 0.0;
+    Real ks = Real(0), kc = Real(0);
+    for (int p = c.gt; p < D.npt; p += c.CT) {
+        const int gp = D.pt0 + p;
+        const bool fp = A.pt_free[gp] >= 0;
+        Real d0 = Real(0), d1 = Real(0), d2 = Real(0);
+        const int e0i = A.pt_eoff[gp], e1i = A.pt_eoff[gp + 1];
+        if (fp) {
+            Real lt[12];
+            Rec<Real>::load12(A.pt_lt + 12LL * gp, lt);
+            Real u0 = lt[6], u1 = lt[7], u2 = lt[8];
+            for (int e = e0i; e < e1i; ++e) {
+                const int a = A.edge_fc[e];
+                if (a < 0) continue;
+                Real Ae[18];
+                Rec<Real>::load18(A.edge_a + (long long)Rec<Real>::kEdge * e, Ae);
+#pragma unroll
+                for (int r = 0; r < 6; ++r) {
+                    const Real d = (Real)dcl[6 * a + r];
+                    u0 -= Ae[r * 3 + 0] * d;
+                    u1 -= Ae[r * 3 + 1] * d;
+                    u2 -= Ae[r * 3 + 2] * d;
+                }
+            }
+            d0 = lt[0] * u0 + lt[1] * u1 + lt[3] * u2;
+            d1 = lt[2] * u1 + lt[4] * u2;
+            d2 = lt[5] * u2;
+            Xt[4LL * gp + 0] = Xc[4LL * gp + 0] + (double)d0;
+            Xt[4LL * gp + 1] = Xc[4LL * gp + 1] + (double)d1;
+            Xt[4LL * gp + 2] = Xc[4LL * gp + 2] + (double)d2;
+            Real vg[12];
+            Rec<Real>::load12(A.pt_vg + 12LL * gp, vg);
+            sc += (double)d0 * (lambda * (double)d0 + (double)vg[6]) + (double)d1 * (lambda * (double)d1 + (double)vg[7]) +
+                  (double)d2 * (lambda * (double)d2 + (double)vg[8]);
+        }
+        const Real X[3] = {(Real)Xc[4LL * gp], (Real)Xc[4LL * gp + 1], (Real)Xc[4LL * gp + 2]};
+        for (int e = e0i; e < e1i; ++e) {
+            const int cam = A.edge_cam[e];
+            const Real* cr = camr + 12 * cam;
+            const Real* cd = camdel + 12 * cam;
+            Real xc[3];
+            transform(cr, cr + 9, X, xc);
+            const Real rd[3] = {cr[0] * d0 + cr[1] * d1 + cr[2] * d2, cr[3] * d0 + cr[4] * d1 + cr[5] * d2,
+                                cr[6] * d0 + cr[7] * d1 + cr[8] * d2};
+            const Real q[3] = {xc[0] + rd[0], xc[1] + rd[1], xc[2] + rd[2]};
+            Real dx[3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) dx[i] = cd[3 * i] * q[0] + cd[3 * i + 1] * q[1] + cd[3 * i + 2] * q[2] + rd[i] + cd[9 + i];
+            const Real z = xc[2], zt = z + dx[2];
+            const Real inv = Real(1) / (z * zt);
+            const Real dpu = fx * (dx[0] * z - xc[0] * dx[2]) * inv;
+            const Real dpv = fy * (dx[1] * z - xc[1] * dx[2]) * inv;
+            const Real r0 = ecur[2LL * e], r1 = ecur[2LL * e + 1];
+            const Real n0 = r0 - dpu, n1 = r1 - dpv;
+            etr[2LL * e] = n0;
+            etr[2LL * e + 1] = n1;
+            const Real ds = -(dpu * (r0 + n0) + dpv * (r1 + n1));
+            Real dr = ds;
+            if (robust) {
+                const Real s = r0 * r0 + r1 * r1, sn = n0 * n0 + n1 * n1;
+                if (s > hd2 && sn > hd2) {
+                    dr = Real(2) * hd * ds / (sqrt(sn) + sqrt(s));
+                } else if (s > hd2 || sn > hd2) {
+                    const Real rho_o = s > hd2 ? Real(2) * hd * sqrt(s) - hd2 : s;
+                    const Real rho_n = sn > hd2 ? Real(2) * hd * sqrt(sn) - hd2 : sn;
+                    dr = rho_n - rho_o;
+                }
+            }
+            const Real y = dr - kc;
+            const Real t = ks + y;
+            kc = (t - ks) - y;
+            ks = t;
+        }
+    }
+    return make_double2(sc, (double)ks - (double)kc);
 }
 
 }  // namespace

@@ -103,6 +103,8 @@ nav_ba_status solve_window_noalloc(int device, cudaStream_t stream, const nav_ba
     const size_t o_x0 = carve(sizeof(double) * 4 * np), o_x1 = carve(sizeof(double) * 4 * np);
     const size_t o_vg = carve(rs * 12 * np), o_lt = carve(rs * 12 * np);
     const size_t o_w = carve(rs * rec * ne), o_a = carve(rs * rec * ne);
+    const size_t eb = o.precision == NAV_BA_MIXED ? rs * 2 * ne : 16;
+    const size_t o_e0 = carve(eb), o_e1 = carve(eb);
     const size_t o_list = carve(sizeof(int32_t) * ne), o_pairs = carve(sizeof(uint32_t) * npair);
     const size_t o_cout = carve(sizeof(CamState) * nc), o_pout = carve(sizeof(double) * 4 * np);
     const size_t o_trace = carve(sizeof(double) * trace_stride), o_stats = carve(sizeof(WinStats));
@@ -129,6 +131,8 @@ nav_ba_status solve_window_noalloc(int device, cudaStream_t stream, const nav_ba
     b.d_pt_lt = arena + o_lt;
     b.d_edge_w = arena + o_w;
     b.d_edge_a = arena + o_a;
+    b.d_edge_e[0] = arena + o_e0;
+    b.d_edge_e[1] = arena + o_e1;
     b.d_cam_list = reinterpret_cast<int32_t*>(arena + o_list);
     b.d_pairs = reinterpret_cast<uint32_t*>(arena + o_pairs);
     b.d_cam_out = reinterpret_cast<CamState*>(arena + o_cout);

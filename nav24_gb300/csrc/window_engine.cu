@@ -60,7 +60,7 @@ struct SmemHead {
 
 // Offsets of the dynamic part of shared memory (after SmemHead), shared by host and device.
 struct Dyn {
-    size_t cams, camr, camd, dcl, S, bs, rinv, total;
+    size_t cams, camr, camd, camdel, dcl, S, bs, rinv, total;
 };
 
 NAVBA_HD size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -71,6 +71,7 @@ NAVBA_HD Dyn dyn_layout(int max_m, int max_ncam, int real_size) {
     d.cams = o; o = align16(o + sizeof(CamState) * 2 * max_ncam);
     d.camr = o; o = align16(o + (size_t)real_size * 2 * max_ncam * 12);
     d.camd = o; o = align16(o + sizeof(double) * 2 * max_ncam * 12);
+    d.camdel = o; o = align16(o + (size_t)real_size * max_ncam * 12);
     d.dcl = o;  o = align16(o + sizeof(double) * max_m);
     d.S = o;    o = align16(o + sizeof(double) * ((size_t)max_m * (max_m + 1) / 2));
     d.bs = o;   o = align16(o + sizeof(double) * max_m);
@@ -445,6 +446,7 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
     Real* camr_tr = camr + 12 * A.max_ncam;
     double* camd = reinterpret_cast<double*>(smem + dl.camd);  // FP64 copies for the cost (mixed form)
     double* camd_tr = camd + 12 * A.max_ncam;
+    Real* camdel = reinterpret_cast<Real*>(smem + dl.camdel);  // trial step per camera: E - I, E_t
     double* dcl = reinterpret_cast<double*>(smem + dl.dcl);
     double* S = reinterpret_cast<double*>(smem + dl.S);
     double* bs = reinterpret_cast<double*>(smem + dl.bs);
@@ -452,6 +454,9 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
     WinStats* st = A.stats + w;
     double* trace = A.trace + (long long)w * A.trace_stride;
     const bool mixed = sizeof(Real) == 4;
+    // mixed form, pinhole model: trial costs as the FP64 current cost plus FP32 residual changes
+    // (update_points_dcost); otherwise every trial cost is evaluated in FP64
+    const bool dcost = mixed && A.edge_e[0] != nullptr && A.intr.model == 0;
 
     for (int k = threadIdx.x; k < D.ncam; k += blockDim.x) {
         cams0[k] = A.cam_init[D.cam0 + k];
@@ -474,8 +479,10 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
     build_lists(A, c, D);  // ends with a cluster barrier: points are initialized everywhere
     pc.mark(0);
 
-    // costs (initial, every trial) are evaluated in FP64 in both forms: they drive the gain ratio
-    double chi = cluster_reduce3<false>(c, cost_partial<double, Real>(A, c, D, camd, A.x[0]), 0.0, 0.0).x;
+    // the initial cost is FP64 in both forms; the FP64 form evaluates every trial cost in FP64, the
+    // mixed form tracks FP32 residuals from these FP64 ones and sums the residual changes
+    double chi = cluster_reduce3<false>(
+        c, cost_partial<double, Real>(A, c, D, camd, A.x[0], dcost ? A.edge_e[0] : nullptr), 0.0, 0.0).x;
     const double chi0_fp64 = chi;
     int iters_done = 0, acc = 0, rej = 0, term = NAV_BA_TERM_ITERATIONS;
     double lambda = 0.0, nu = 2.0;
@@ -548,16 +555,33 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
 #pragma unroll
                             for (int r = 0; r < 6; ++r) sc += dcl[6 * a + r] * (lambda * dcl[6 * a + r] + s.U[a][21 + r]);
                     }
+                    if (dcost) {
+                        double emi[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, et[3] = {0, 0, 0};
+                        if (a >= 0) se3_exp_delta(dcl + 6 * a, emi, et);
+#pragma unroll
+                        for (int r = 0; r < 9; ++r) camdel[12 * k + r] = (Real)emi[r];
+#pragma unroll
+                        for (int r = 0; r < 3; ++r) camdel[12 * k + 9 + r] = (Real)et[r];
+                    }
                     cam_real<Real>(ctr[k], crt + 12 * k);
                     cam_real<double>(ctr[k], cdt + 12 * k);
                 }
                 __syncthreads();
-                sc += update_points<Real>(A, c, D, lambda, dcl, cur);
-                pc.mark(7);
-                const double3 red = cluster_reduce3<false>(
-                    c, cost_partial<double, Real>(A, c, D, cdt, A.x[cur ^ 1]), sc, 0.0);
-                double chi_new = red.x;
-                double scale = red.y;
+                double chi_new, scale;
+                if (dcost) {
+                    const double2 ud = update_points_dcost<Real>(A, c, D, lambda, dcl, cur, cr_cur, camdel);
+                    pc.mark(7);
+                    const double3 red = cluster_reduce3<false>(c, ud.y, sc + ud.x, 0.0);
+                    chi_new = chi + red.x;
+                    scale = red.y;
+                } else {
+                    sc += update_points<Real>(A, c, D, lambda, dcl, cur);
+                    pc.mark(7);
+                    const double3 red = cluster_reduce3<false>(
+                        c, cost_partial<double, Real>(A, c, D, cdt, A.x[cur ^ 1]), sc, 0.0);
+                    chi_new = red.x;
+                    scale = red.y;
+                }
                 if (!ok) chi_new = DBL_MAX;
                 rho = chi - chi_new;
                 scale += 1e-3;
@@ -588,8 +612,13 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
     }
     const int cur = s.cur;
     CamState* cfin = cur == 0 ? cams0 : cams1;
-    const double chi_final = chi;
-    (void)mixed;
+    double chi_final = chi;
+    if (dcost && !bad) {
+        // the final cost reported is the FP64 cost of the final state
+        chi_final = cluster_reduce3<false>(c, cost_partial<double, Real>(A, c, D, cur == 0 ? camd : camd_tr, A.x[cur]),
+                                           0.0, 0.0).x;
+        if (c.rank == 0 && threadIdx.x == 0) trace[iters_done] = chi_final;
+    }
     if (c.rank == 0)
         for (int k = threadIdx.x; k < D.ncam; k += blockDim.x) A.cam_out[D.cam0 + k] = cfin[k];
     for (int p = c.gt; p < D.npt; p += c.CT) {
@@ -670,6 +699,8 @@ cudaError_t launch_typed(PreparedBatch& pb, cudaStream_t stream, WindowLaunch sh
     A.pt_lt = (Real*)b.d_pt_lt;
     A.edge_w = (Real*)b.d_edge_w;
     A.edge_a = (Real*)b.d_edge_a;
+    A.edge_e[0] = sizeof(Real) == 4 ? (Real*)b.d_edge_e[0] : nullptr;
+    A.edge_e[1] = sizeof(Real) == 4 ? (Real*)b.d_edge_e[1] : nullptr;
     A.cam_list = b.d_cam_list;
     A.pairs = b.d_pairs;
     A.cam_out = b.d_cam_out;
@@ -840,7 +871,8 @@ void HostStaging::release() {
 void window_batch_free(WindowBatch& b) {
     void* ptrs[] = {b.d_win, b.d_order, b.d_queue, b.d_cam_init, b.d_cam_free, b.d_pt_init, b.d_pt_free,
                     b.d_pt_eoff, b.d_edge_cam, b.d_edge_fc, b.d_edge_pt, b.d_edge_uv, b.d_x[0], b.d_x[1], b.d_pt_vg,
-                    b.d_pt_lt, b.d_edge_w, b.d_edge_a, b.d_cam_list, b.d_pairs, b.d_cam_out, b.d_pt_out,
+                    b.d_pt_lt, b.d_edge_w, b.d_edge_a, b.d_edge_e[0], b.d_edge_e[1], b.d_cam_list, b.d_pairs,
+                    b.d_cam_out, b.d_pt_out,
                     b.d_trace, b.d_stats, b.d_debug, b.d_phase};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -940,6 +972,8 @@ cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int prec
     const size_t rec = precision == NAV_BA_MIXED ? 20 : 18;  // per-edge record stride (Reals)
     ensure(&b.d_edge_w, rs * rec * ne);
     ensure(&b.d_edge_a, rs * rec * ne);
+    ensure(&b.d_edge_e[0], precision == NAV_BA_MIXED ? rs * 2 * ne : 16);
+    ensure(&b.d_edge_e[1], precision == NAV_BA_MIXED ? rs * 2 * ne : 16);
     ensure(&b.d_cam_list, sizeof(int32_t) * ne);
     ensure(&b.d_pairs, sizeof(uint32_t) * npair);
     ensure(&b.d_cam_out, sizeof(CamState) * nc);
