@@ -55,6 +55,8 @@ def parse():
                     help="run only the device-resident solves of one precision (mixed, fp64), or one solve of a "
                          "secondary workload (for profiler captures)")
     ap.add_argument("--no-secondary", action="store_true", help="skip the secondary workloads")
+    ap.add_argument("--pcg-cams", type=int, default=1000, help="cameras of the figure-eight PCG workload")
+    ap.add_argument("--pcg-points", type=int, default=500000, help="points of the figure-eight PCG workload")
     return ap.parse_args()
 
 
@@ -258,7 +260,7 @@ def solve_pair(ctx, p, family):
     return out
 
 
-def secondary_workloads(ctx, only=None):
+def secondary_workloads(ctx, only=None, pcg_cams=1000, pcg_points=500000):
     """One solve of each other named workload (device time, including the per-solve upload)."""
     from nav24_gb300 import abi
     from nav24_gb300.synth import Synth, workload_options
@@ -284,11 +286,12 @@ def secondary_workloads(ctx, only=None):
             "forward_obs_per_s": r.stats["edge_iterations"] / (t1 - t0), "final_cost": r.stats["final_cost"],
             "timing": "wall clock of the C-ABI call (host graph build, upload, device work, download)"}
     if only in (None, "pcg"):
-        p = Synth(4).window(0)
+        p = Synth(4, n_cams=pcg_cams, n_points=pcg_points).window(0)
         out["figure_eight_pcg"] = {
-            "workload": "1000 cameras on a 2 km figure-eight, 500,000 points, shared radial k1/k2 optimized, 5% "
-                        "outliers, Huber 1.5 px, 30 LM iterations, PCG (block-Jacobi, tol 1e-6, <= 100 iterations) "
-                        "(family 4, seed 1004), grid engine", "observations": p.n_obs, **solve_pair(ctx, p, 4)}
+            "workload": f"{pcg_cams} cameras on a {2 * pcg_cams} m figure-eight, {pcg_points} points, shared radial "
+                        "k1/k2 optimized, 5% outliers, Huber 1.5 px, 30 LM iterations, PCG (block-Jacobi, tol 1e-6, "
+                        "<= 100 iterations) (family 4, seed 1004), grid engine", "observations": p.n_obs,
+            **solve_pair(ctx, p, 4)}
     return out
 
 
@@ -311,7 +314,7 @@ def main():
     of = workload_options(2, abi.FP64)
 
     if args.profile_case in ("grid", "pcg", "vjp"):
-        print(json.dumps(secondary_workloads(ctx, args.profile_case)), flush=True)
+        print(json.dumps(secondary_workloads(ctx, args.profile_case, args.pcg_cams, args.pcg_points)), flush=True)
         ctx.close()
         dist.close()
         return
@@ -384,7 +387,7 @@ def main():
 
     secondary = None
     if rank == 0 and not args.no_secondary:
-        secondary = secondary_workloads(ctx)
+        secondary = secondary_workloads(ctx, None, args.pcg_cams, args.pcg_points)
 
     if rank == 0:
         line = {

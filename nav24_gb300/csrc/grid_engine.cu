@@ -628,220 +628,334 @@ __global__ void k_pcg_precond(const double* U, const double* aat, int nfc, doubl
     if (!good) ok[0] = 0;
 }
 
-// t2_p = sum_{edges with a free camera} A^T x_c + B^T x_k (free points); block sums of B t2 (2).
+// Structure-of-arrays copies of A_e for the PCG products (18 arrays of Real each): point-major in
+// edge order (apm[k * ne + e]) and camera-major in camera-list order (acm[k * ncl + s]), packed
+// once per damping trial from the per-edge records and read by every PCG iteration with
+// contiguous (coalesced) accesses.  Entries of edges without a free camera or a free point are
+// not written and never read.
 template <class Real>
-__global__ void k_pcg_points(WinArgs<Real> A, WinDesc D, const double* x, int nk, const Real* pt_b, Real* pt_t2,
-                             double* part) {
-    const CC c = grid_view();
-    const int kb = 6 * D.nfc;
-    double acc[2] = {0, 0};
-    for (int p = c.gt; p < D.npt; p += c.CT) {
-        if (A.pt_free[p] < 0) continue;
-        Real t0 = 0, t1 = 0, t2 = 0;
-        for (int e = A.pt_eoff[p]; e < A.pt_eoff[p + 1]; ++e) {
-            const int a = A.edge_fc[e];
-            if (a < 0) continue;
-            Real ae[18];
-            Rec<Real>::load18(A.edge_a + (long long)Rec<Real>::kEdge * e, ae);
+__global__ void k_pcg_pack(WinArgs<Real> A, int ne, const int32_t* cam_list, int ncl, Real* apm, Real* acm) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += stride) {
+        if (A.edge_fc[e] < 0 || A.pt_free[A.edge_pt[e]] < 0) continue;
+        Real a[18];
+        Rec<Real>::load18(A.edge_a + (long long)Rec<Real>::kEdge * e, a);
 #pragma unroll
-            for (int r = 0; r < 6; ++r) {
-                const Real xv = (Real)x[6 * a + r];
-                t0 += ae[r * 3] * xv;
-                t1 += ae[r * 3 + 1] * xv;
-                t2 += ae[r * 3 + 2] * xv;
-            }
-        }
-        if (nk) {
-            Real b[12];
-            Rec<Real>::load12(pt_b + 12LL * p, b);
-            const Real k1 = (Real)x[kb], k2 = (Real)x[kb + 1];
-            t0 += b[0] * k1 + b[3] * k2;
-            t1 += b[1] * k1 + b[4] * k2;
-            t2 += b[2] * k1 + b[5] * k2;
-            acc[0] += (double)(b[0] * t0 + b[1] * t1 + b[2] * t2);
-            acc[1] += (double)(b[3] * t0 + b[4] * t1 + b[5] * t2);
-        }
-        pt_t2[4LL * p] = t0;
-        pt_t2[4LL * p + 1] = t1;
-        pt_t2[4LL * p + 2] = t2;
+        for (int k = 0; k < 18; ++k) apm[(long long)k * ne + e] = a[k];
     }
-    block_partials<2>(acc, part);
-}
-
-// Per work item: sum A_i t2_{p(i)} (6) -> part[8 * item].
-template <class Real>
-__global__ void k_pcg_cams(WinArgs<Real> A, const int4* items, int n_items, const int32_t* cam_list, const Real* pt_t2,
-                           double* part) {
-    const CC c = grid_view();
-    for (int it = c.gw; it < n_items; it += c.CW) {
-        const int4 wi = items[it];
-        Real y[6] = {0, 0, 0, 0, 0, 0};
-        for (int i = c.lane; i < wi.z; i += 32) {
-            const int e = cam_list[wi.y + i];
-            const int gp = A.edge_pt[e];
-            if (A.pt_free[gp] < 0) continue;
-            Real ae[18];
-            Rec<Real>::load18(A.edge_a + (long long)Rec<Real>::kEdge * e, ae);
-            const Real t0 = pt_t2[4LL * gp], t1 = pt_t2[4LL * gp + 1], t2 = pt_t2[4LL * gp + 2];
+    for (int sl = blockIdx.x * blockDim.x + threadIdx.x; sl < ncl; sl += stride) {
+        const int e = cam_list[sl];
+        if (A.pt_free[A.edge_pt[e]] < 0) continue;
+        Real a[18];
+        Rec<Real>::load18(A.edge_a + (long long)Rec<Real>::kEdge * e, a);
 #pragma unroll
-            for (int r = 0; r < 6; ++r) y[r] += ae[r * 3] * t0 + ae[r * 3 + 1] * t1 + ae[r * 3 + 2] * t2;
-        }
-#pragma unroll
-        for (int k = 0; k < 6; ++k)
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) y[k] += __shfl_xor_sync(kFullG, y[k], o);
-        if (c.lane < 6)
-#pragma unroll
-            for (int k = 0; k < 6; ++k)
-                if (k == c.lane) part[8LL * it + k] = (double)y[k];
+        for (int k = 0; k < 18; ++k) acm[(long long)k * ncl + sl] = a[k];
     }
 }
 
-// PCG state in one device block: vectors x r z p q of length mt, scalars.
+// PCG vectors x r z p q of length mt and scalars.
 struct PcgVec {
     double *x, *r, *z, *p, *q;
     double* sc;  // [0] rz, [1] r.r, [2] b.b
+    float* pf;   // FP32 copy of the camera part of p (mixed form), or null
+    int npf;     // its length (6 * free cameras)
 };
 
-__device__ double cta_sum(double v) {
-    __shared__ double red[33];
+// ---- PCG as one cooperative persistent kernel ------------------------------------------------
+//
+// One launch per damped system: every phase of every CG iteration runs grid-wide with grid
+// synchronizations in between (no host round trip, no per-iteration launches).  Reductions go
+// through per-block partials that every block sums in the same fixed order, so every block holds
+// the same scalars and the iteration is bitwise repeatable.  The convergence test (r.r <= tol^2
+// b.b) is made every 4 iterations, as in the oracle.
+
+template <class Real>
+struct PcgArgs {
+    WinArgs<Real> A;
+    int np, ne, ncl, nfc, nk, mt;
+    const Real* apm;
+    const Real* acm;
+    const int32_t* cm_pt;
+    const int4* items;
+    int n_items;
+    const int32_t* item_off;
+    const Real* pt_b;
+    Real* pt_t2;
+    double* camp;           // [n_items][8]
+    const double* U;        // [nfc][28]
+    const double* Hck;      // [nfc][12]
+    const double* kk;       // [0..2] H_kk (lambda-free), [3..5] 2x2 Cholesky of the k block
+    const double* pc;       // [nfc][28] block-Jacobi factors
+    const double* b;        // right-hand side [mt]
+    double lambda;
+    PcgVec v;
+    double* part;           // [7][gridDim.x] partials
+    int max_it;
+    double tol2;
+    int32_t* iters;         // out: iterations run
+};
+
+// Sum of n per-block partials (stride `stride`) in a fixed order; every thread gets the result.
+__device__ double grid_partials_sum(const double* part, int n, int stride) {
+    __shared__ double red[32];
+    double v = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) v += part[(long long)i * stride];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFullG, v, o);
     __syncthreads();
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double r = 0.0;
-        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r += red[i];
-        red[32] = r;
-    }
+    double r = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r += red[i];
     __syncthreads();
-    return red[32];
+    return r;
 }
 
-// z = M^-1 r: per camera the 6x6 Cholesky solve, the 2x2 intrinsics block (host-factored pk).
-__device__ void pcg_precond_apply(const double* pc, int nfc, int nk, const double* pk, const double* r, double* z) {
-    for (int a = threadIdx.x; a < nfc; a += blockDim.x) {
-        const double* L = pc + 28LL * a;
-        const double* ri = L + 21;
-        double v[6];
-        for (int i = 0; i < 6; ++i) {
-            double s = r[6 * a + i];
-            for (int k = 0; k < i; ++k) s -= L[tri(i, k)] * v[k];
-            v[i] = s * ri[i];
-        }
-        for (int i = 5; i >= 0; --i) {
-            double s = v[i];
-            for (int k = i + 1; k < 6; ++k) s -= L[tri(k, i)] * v[k];
-            v[i] = s * ri[i];
-        }
-        for (int i = 0; i < 6; ++i) z[6 * a + i] = v[i];
+// z = P_a^-1 r for camera a (6x6 Cholesky factors with inverse diagonal).
+__device__ __forceinline__ void precond_cam(const double* pc, int a, const double* r, double* z) {
+    const double* L = pc + 28LL * a;
+    const double* ri = L + 21;
+    double v[6];
+    for (int i = 0; i < 6; ++i) {
+        double s = r[i];
+        for (int k = 0; k < i; ++k) s -= L[tri(i, k)] * v[k];
+        v[i] = s * ri[i];
     }
-    if (nk && threadIdx.x == 0) {
-        // pk: 2x2 lower Cholesky l00 l10 l11 of the intrinsics block
-        const int kb = 6 * nfc;
-        const double y0 = r[kb] / pk[0];
-        const double y1 = (r[kb + 1] - pk[1] * y0) / pk[2];
-        const double x1 = y1 / pk[2];
-        const double x0 = (y0 - pk[1] * x1) / pk[0];
-        z[kb] = x0;
-        z[kb + 1] = x1;
+    for (int i = 5; i >= 0; --i) {
+        double s = v[i];
+        for (int k = i + 1; k < 6; ++k) s -= L[tri(k, i)] * v[k];
+        v[i] = s * ri[i];
     }
+    for (int i = 0; i < 6; ++i) z[i] = v[i];
 }
 
-// x = 0, r = b, z = M^-1 r, p = z, rz = r.z, r.r, b.b (one CTA).
-__global__ void k_pcg_init(PcgVec v, const double* b, int mt, const double* pc, int nfc, int nk, const double* pk) {
-    for (int i = threadIdx.x; i < mt; i += blockDim.x) {
-        v.x[i] = 0.0;
-        v.r[i] = b[i];
-    }
-    __syncthreads();
-    pcg_precond_apply(pc, nfc, nk, pk, v.r, v.z);
-    __syncthreads();
+// z = P_k^-1 r for the 2x2 intrinsics block (lower Cholesky l00 l10 l11 in pk).
+__device__ __forceinline__ void precond_k(const double* pk, const double* r, double* z) {
+    const double y0 = r[0] / pk[0];
+    const double y1 = (r[1] - pk[1] * y0) / pk[2];
+    const double x1 = y1 / pk[2];
+    const double x0 = (y0 - pk[1] * x1) / pk[0];
+    z[0] = x0;
+    z[1] = x1;
+}
+
+template <class Real>
+__global__ void __launch_bounds__(256) k_pcg_solve(PcgArgs<Real> P) {
+    cg::grid_group grid = cg::this_grid();
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    const int nb = gridDim.x;
+    const int lane = threadIdx.x & 31;
+    const int gw = tid >> 5, nwarp = nth >> 5;
+    const int kb = 6 * P.nfc;
+    PcgVec& v = P.v;
+    double* pk_part = P.part;               // phase 1: B t2 (2 per block)
+    double* hk_part = P.part + 2LL * nb;    // phase 2: Hck^T p (2 per block)
+    double* pq_part = P.part + 4LL * nb;    // phase 3: p.q
+    double* rz_part = P.part + 5LL * nb;    // phase 4: r.z, r.r (2 per block)
+    const double* pkc = P.kk + 3;
+    // init: x = 0, r = b, z = M^-1 r, p = z
     double rz = 0.0, rr = 0.0;
-    for (int i = threadIdx.x; i < mt; i += blockDim.x) {
-        v.p[i] = v.z[i];
-        rz += v.r[i] * v.z[i];
-        rr += v.r[i] * v.r[i];
-    }
-    rz = cta_sum(rz);
-    rr = cta_sum(rr);
-    if (threadIdx.x == 0) {
-        v.sc[0] = rz;
-        v.sc[1] = rr;
-        v.sc[2] = rr;
-    }
-}
-
-// q = S p from the item / point partials, then one PCG update (one CTA).
-__global__ void k_pcg_step(PcgVec v, int mt, int nfc, int nk, const double* U, const double* Hck, const double* kk,
-                           double lambda, const double* cam_part, const int32_t* item_off, const double* pt_part,
-                           int n_pt_blocks, const double* pc, const double* pk) {
-    const int kb = 6 * nfc;
-    double pk0 = 0.0, pk1 = 0.0;
-    if (nk) {
-        pk0 = v.p[kb];
-        pk1 = v.p[kb + 1];
-    }
-    for (int a = threadIdx.x; a < nfc; a += blockDim.x) {
-        const double* Ua = U + 28LL * a;
-        double pa[6];
-        for (int r = 0; r < 6; ++r) pa[r] = v.p[6 * a + r];
-        for (int r = 0; r < 6; ++r) {
-            double s = lambda * pa[r];
-            for (int q = 0; q < 6; ++q) s += Ua[r >= q ? tri(r, q) : tri(q, r)] * pa[q];
-            for (int it = item_off[a]; it < item_off[a + 1]; ++it) s -= cam_part[8LL * it + r];
-            if (nk) s += Hck[12LL * a + r * 2] * pk0 + Hck[12LL * a + r * 2 + 1] * pk1;
-            v.q[6 * a + r] = s;
+    for (int a = tid; a < P.nfc; a += nth) {
+        double* r = v.r + 6 * a;
+        for (int i = 0; i < 6; ++i) {
+            v.x[6 * a + i] = 0.0;
+            r[i] = P.b[6 * a + i];
+        }
+        precond_cam(P.pc, a, r, v.z + 6 * a);
+        for (int i = 0; i < 6; ++i) {
+            const double z = v.z[6 * a + i];
+            v.p[6 * a + i] = z;
+            if (v.pf) v.pf[6 * a + i] = (float)z;
+            rz += r[i] * z;
+            rr += r[i] * r[i];
         }
     }
-    if (nk) {
-        // q_k = (Kk + lambda) p_k + sum_a Hck_a^T p_a - sum_p B t2
-        double s0 = 0.0, s1 = 0.0;
-        for (int a = threadIdx.x; a < nfc; a += blockDim.x)
-            for (int r = 0; r < 6; ++r) {
-                s0 += Hck[12LL * a + r * 2] * v.p[6 * a + r];
-                s1 += Hck[12LL * a + r * 2 + 1] * v.p[6 * a + r];
-            }
-        s0 = cta_sum(s0);
-        s1 = cta_sum(s1);
-        if (threadIdx.x == 0) {
-            double b0 = 0.0, b1 = 0.0;
-            for (int k = 0; k < n_pt_blocks; ++k) {
-                b0 += pt_part[2 * k];
-                b1 += pt_part[2 * k + 1];
-            }
-            v.q[kb] = (kk[0] + lambda) * pk0 + kk[1] * pk1 + s0 - b0;
-            v.q[kb + 1] = kk[1] * pk0 + (kk[2] + lambda) * pk1 + s1 - b1;
+    if (P.nk && tid == 0) {
+        for (int i = 0; i < 2; ++i) {
+            v.x[kb + i] = 0.0;
+            v.r[kb + i] = P.b[kb + i];
+        }
+        precond_k(pkc, v.r + kb, v.z + kb);
+        for (int i = 0; i < 2; ++i) {
+            v.p[kb + i] = v.z[kb + i];
+            rz += v.r[kb + i] * v.z[kb + i];
+            rr += v.r[kb + i] * v.r[kb + i];
         }
     }
-    __syncthreads();
-    double pq = 0.0;
-    for (int i = threadIdx.x; i < mt; i += blockDim.x) pq += v.p[i] * v.q[i];
-    pq = cta_sum(pq);
-    const double rz = v.sc[0];
-    const double alpha = pq != 0.0 ? rz / pq : 0.0;
-    for (int i = threadIdx.x; i < mt; i += blockDim.x) {
-        v.x[i] += alpha * v.p[i];
-        v.r[i] -= alpha * v.q[i];
+    {
+        double two[2] = {rz, rr};
+        block_partials<2>(two, rz_part);
     }
-    __syncthreads();
-    pcg_precond_apply(pc, nfc, nk, pk, v.r, v.z);
-    __syncthreads();
-    double rzn = 0.0, rr = 0.0;
-    for (int i = threadIdx.x; i < mt; i += blockDim.x) {
-        rzn += v.r[i] * v.z[i];
-        rr += v.r[i] * v.r[i];
+    grid.sync();
+    rz = grid_partials_sum(rz_part, nb, 2);
+    rr = grid_partials_sum(rz_part + 1, nb, 2);
+    const double bb = rr;
+    const Real* xr = reinterpret_cast<const Real*>(sizeof(Real) == 4 ? (const void*)v.pf : (const void*)v.p);
+    int pit = 0;
+    for (; pit < P.max_it; ++pit) {
+        if (pit % 4 == 0 && !(rr > P.tol2 * bb)) break;
+        // phase 1: t2_p = sum A_e^T p_c + B_p^T p_k (8 lanes per point, warp-uniform loop)
+        {
+            constexpr int G = 8, GPW = 32 / G;
+            const int gl = lane % G, gi = lane / G;
+            double acc[2] = {0, 0};
+            const Real k1 = P.nk ? (Real)v.p[kb] : Real(0), k2 = P.nk ? (Real)v.p[kb + 1] : Real(0);
+            for (int p0 = gw * GPW; p0 < P.np; p0 += nwarp * GPW) {
+                const int p = p0 + gi;
+                const bool valid = p < P.np && P.A.pt_free[p] >= 0;
+                Real t0 = 0, t1 = 0, t2 = 0;
+                if (valid) {
+                    const int e1 = P.A.pt_eoff[p + 1];
+                    for (int e = P.A.pt_eoff[p] + gl; e < e1; e += G) {
+                        const int a = P.A.edge_fc[e];
+                        if (a < 0) continue;
+                        const Real* xa = xr + 6 * a;
+#pragma unroll
+                        for (int r = 0; r < 6; ++r) {
+                            const Real xv = xa[r];
+                            t0 += P.apm[(long long)(r * 3) * P.ne + e] * xv;
+                            t1 += P.apm[(long long)(r * 3 + 1) * P.ne + e] * xv;
+                            t2 += P.apm[(long long)(r * 3 + 2) * P.ne + e] * xv;
+                        }
+                    }
+                }
+#pragma unroll
+                for (int o = G / 2; o > 0; o >>= 1) {
+                    t0 += __shfl_xor_sync(kFullG, t0, o);
+                    t1 += __shfl_xor_sync(kFullG, t1, o);
+                    t2 += __shfl_xor_sync(kFullG, t2, o);
+                }
+                if (valid && gl == 0) {
+                    if (P.nk) {
+                        Real bp[12];
+                        Rec<Real>::load12(P.pt_b + 12LL * p, bp);
+                        t0 += bp[0] * k1 + bp[3] * k2;
+                        t1 += bp[1] * k1 + bp[4] * k2;
+                        t2 += bp[2] * k1 + bp[5] * k2;
+                        acc[0] += (double)(bp[0] * t0 + bp[1] * t1 + bp[2] * t2);
+                        acc[1] += (double)(bp[3] * t0 + bp[4] * t1 + bp[5] * t2);
+                    }
+                    P.pt_t2[4LL * p] = t0;
+                    P.pt_t2[4LL * p + 1] = t1;
+                    P.pt_t2[4LL * p + 2] = t2;
+                }
+            }
+            block_partials<2>(acc, pk_part);
+        }
+        grid.sync();
+        // phase 2: per camera item sum A_s t2 (warp per item); Hck_a^T p_a partials
+        for (int it = gw; it < P.n_items; it += nwarp) {
+            const int4 wi = P.items[it];
+            Real y[6] = {0, 0, 0, 0, 0, 0};
+            for (int i = lane; i < wi.z; i += 32) {
+                const int sl = wi.y + i;
+                const int gp = P.cm_pt[sl];
+                if (gp < 0) continue;
+                const Real t0 = P.pt_t2[4LL * gp], t1 = P.pt_t2[4LL * gp + 1], t2 = P.pt_t2[4LL * gp + 2];
+#pragma unroll
+                for (int r = 0; r < 6; ++r)
+                    y[r] += P.acm[(long long)(r * 3) * P.ncl + sl] * t0 + P.acm[(long long)(r * 3 + 1) * P.ncl + sl] * t1 +
+                            P.acm[(long long)(r * 3 + 2) * P.ncl + sl] * t2;
+            }
+#pragma unroll
+            for (int k = 0; k < 6; ++k)
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) y[k] += __shfl_xor_sync(kFullG, y[k], o);
+            if (lane < 6)
+#pragma unroll
+                for (int k = 0; k < 6; ++k)
+                    if (k == lane) P.camp[8LL * it + k] = (double)y[k];
+        }
+        {
+            double hk[2] = {0, 0};
+            if (P.nk)
+                for (int a = tid; a < P.nfc; a += nth)
+                    for (int r = 0; r < 6; ++r) {
+                        hk[0] += P.Hck[12LL * a + r * 2] * v.p[6 * a + r];
+                        hk[1] += P.Hck[12LL * a + r * 2 + 1] * v.p[6 * a + r];
+                    }
+            block_partials<2>(hk, hk_part);
+        }
+        grid.sync();
+        // phase 3: q = S p per camera (and the k block), p.q partials
+        {
+            double pq = 0.0;
+            const double pk0 = P.nk ? v.p[kb] : 0.0, pk1 = P.nk ? v.p[kb + 1] : 0.0;
+            for (int a = tid; a < P.nfc; a += nth) {
+                const double* Ua = P.U + 28LL * a;
+                double pa[6];
+                for (int r = 0; r < 6; ++r) pa[r] = v.p[6 * a + r];
+                for (int r = 0; r < 6; ++r) {
+                    double s = P.lambda * pa[r];
+                    for (int q = 0; q < 6; ++q) s += Ua[r >= q ? tri(r, q) : tri(q, r)] * pa[q];
+                    for (int it = P.item_off[a]; it < P.item_off[a + 1]; ++it) s -= P.camp[8LL * it + r];
+                    if (P.nk) s += P.Hck[12LL * a + r * 2] * pk0 + P.Hck[12LL * a + r * 2 + 1] * pk1;
+                    v.q[6 * a + r] = s;
+                    pq += pa[r] * s;
+                }
+            }
+            if (P.nk) {
+                // q_k = (H_kk + lambda) p_k + sum_a Hck_a^T p_a - sum_p B t2 (block 0 writes it)
+                const double h0 = grid_partials_sum(hk_part, nb, 2), h1 = grid_partials_sum(hk_part + 1, nb, 2);
+                const double b0 = grid_partials_sum(pk_part, nb, 2), b1 = grid_partials_sum(pk_part + 1, nb, 2);
+                if (blockIdx.x == 0 && threadIdx.x == 0) {
+                    const double q0 = (P.kk[0] + P.lambda) * pk0 + P.kk[1] * pk1 + h0 - b0;
+                    const double q1 = P.kk[1] * pk0 + (P.kk[2] + P.lambda) * pk1 + h1 - b1;
+                    v.q[kb] = q0;
+                    v.q[kb + 1] = q1;
+                    pq += pk0 * q0 + pk1 * q1;
+                }
+            }
+            block_partial<false>(pq, pq_part);
+        }
+        grid.sync();
+        // phase 4: x += alpha p, r -= alpha q, z = M^-1 r, r.z and r.r partials
+        {
+            const double pq = grid_partials_sum(pq_part, nb, 1);
+            const double alpha = pq != 0.0 ? rz / pq : 0.0;
+            double rzn = 0.0, rrn = 0.0;
+            for (int a = tid; a < P.nfc; a += nth) {
+                double* r = v.r + 6 * a;
+                for (int i = 0; i < 6; ++i) {
+                    v.x[6 * a + i] += alpha * v.p[6 * a + i];
+                    r[i] -= alpha * v.q[6 * a + i];
+                }
+                precond_cam(P.pc, a, r, v.z + 6 * a);
+                for (int i = 0; i < 6; ++i) {
+                    rzn += r[i] * v.z[6 * a + i];
+                    rrn += r[i] * r[i];
+                }
+            }
+            if (P.nk && tid == 0) {
+                for (int i = 0; i < 2; ++i) {
+                    v.x[kb + i] += alpha * v.p[kb + i];
+                    v.r[kb + i] -= alpha * v.q[kb + i];
+                }
+                precond_k(pkc, v.r + kb, v.z + kb);
+                for (int i = 0; i < 2; ++i) {
+                    rzn += v.r[kb + i] * v.z[kb + i];
+                    rrn += v.r[kb + i] * v.r[kb + i];
+                }
+            }
+            double two[2] = {rzn, rrn};
+            block_partials<2>(two, rz_part);
+        }
+        grid.sync();
+        // phase 5: p = z + beta p
+        {
+            const double rzn = grid_partials_sum(rz_part, nb, 2);
+            rr = grid_partials_sum(rz_part + 1, nb, 2);
+            const double beta = rz != 0.0 ? rzn / rz : 0.0;
+            for (int i = tid; i < P.mt; i += nth) {
+                const double pn = v.z[i] + beta * v.p[i];
+                v.p[i] = pn;
+                if (v.pf && i < kb) v.pf[i] = (float)pn;
+            }
+            rz = rzn;
+        }
+        grid.sync();
     }
-    rzn = cta_sum(rzn);
-    rr = cta_sum(rr);
-    const double beta = rz != 0.0 ? rzn / rz : 0.0;
-    for (int i = threadIdx.x; i < mt; i += blockDim.x) v.p[i] = v.z[i] + beta * v.p[i];
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        v.sc[0] = rzn;
-        v.sc[1] = rr;
-    }
+    if (tid == 0) P.iters[0] = pit;
 }
 
 // t_p -= B_p^T dk before the point back-substitution (the distortion part of the step).
@@ -1074,6 +1188,23 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     double* d_ipart = bwd ? dv.alloc<double>(8LL * g.items.size()) : nullptr;
     double* d_posebar = (bwd && vjp->pose_bar) ? dv.alloc<double>(12LL * nc) : nullptr;
     double* d_ptbar = (bwd && vjp->point_bar) ? dv.alloc<double>(3LL * np) : nullptr;
+    // PCG: structure-of-arrays copies of A (point-major, camera-major) and the camera list's points
+    const int ncl = (int)g.cam_list.size();
+    Real* d_apm = pcg ? dv.alloc<Real>(18LL * ne) : nullptr;
+    Real* d_acm = pcg ? dv.alloc<Real>(18LL * ncl) : nullptr;
+    int32_t* d_cmpt = pcg ? dv.alloc<int32_t>(ncl) : nullptr;
+    float* d_pf = (pcg && sizeof(Real) == 4) ? dv.alloc<float>(6LL * nfc1) : nullptr;
+    // cooperative PCG grid: every block resident (the occupancy bound of the kernel)
+    int pcg_grid = 1;
+    if (pcg) {
+        int dev = 0, nsm = 0, bps = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_pcg_solve<Real>, 256, 0);
+        pcg_grid = std::max(1, nsm * std::max(1, std::min(bps, 4)));
+    }
+    double* d_ppart = pcg ? dv.alloc<double>(7LL * pcg_grid) : nullptr;
+    int32_t* d_pit = pcg ? dv.alloc<int32_t>(1) : nullptr;
     if (dv.err != cudaSuccess) return dv.err;
     std::vector<int32_t> edge_fc(ne);
     for (int e = 0; e < ne; ++e) edge_fc[e] = h.cam_free[h.edge_cam[e]];
@@ -1099,6 +1230,15 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     chk(up(d_boff, g.boff, st));
     chk(up(d_pairs, g.pairs, st));
     chk(up(d_tfirst, g.tfirst, st));
+    std::vector<int32_t> cm_pt;
+    if (pcg) {
+        cm_pt.resize(ncl);
+        for (int sl = 0; sl < ncl; ++sl) {
+            const int pt = h.edge_pt[g.cam_list[sl]];
+            cm_pt[sl] = h.pt_free[pt] >= 0 ? pt : -1;
+        }
+        chk(up(d_cmpt, cm_pt, st));
+    }
     if (d_posebar) chk(cudaMemcpyAsync(d_posebar, vjp->pose_bar, sizeof(double) * 12 * nc, cudaMemcpyHostToDevice, st));
     if (d_ptbar) chk(cudaMemcpyAsync(d_ptbar, vjp->point_bar, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, st));
     if (e != cudaSuccess) return e;
@@ -1289,6 +1429,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             bool ok = npd == 0.0;
             double dk[2] = {0.0, 0.0};
             if (pcg && mt > 0) {
+                k_pcg_pack<Real><<<nsm_blocks, TB, 0, st>>>(A, ne, d_list, ncl, d_apm, d_acm);
                 // right-hand side and block-Jacobi preconditioner of the reduced system [cameras; k]
                 const int32_t one = 1;
                 chk(cudaMemcpyAsync(d_ok, &one, sizeof(int32_t), cudaMemcpyHostToDevice, st));
@@ -1325,32 +1466,47 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                 v.p = d_vec + 3LL * mt;
                 v.q = d_vec + 4LL * mt;
                 v.sc = d_vec + 5LL * mt;
-                k_pcg_init<<<1, 1024, 0, st>>>(v, d_bs, mt, d_pc, nfc, nk, d_kvals + 3);
-                chk(cudaGetLastError());
-                double scv[3] = {0, 0, 0};
-                int pit = 0;
-                const double tol2 = lm.pcg_tolerance * lm.pcg_tolerance;
-                for (; pit < lm.pcg_max_iterations; ++pit) {
-                    if (pit % 4 == 0) {
-                        chk(cudaMemcpyAsync(scv, v.sc, sizeof(scv), cudaMemcpyDeviceToHost, st));
-                        chk(cudaStreamSynchronize(st));
-                        if (e != cudaSuccess) return e;
-                        if (!(scv[1] > tol2 * scv[2])) break;
-                    }
-                    k_pcg_points<Real><<<pblocks, TB, 0, st>>>(A, D, v.p, nk, d_pb, d_t2, d_part);
-                    if (nfc > 0)
-                        k_pcg_cams<Real><<<iblocks, TB, 0, st>>>(A, d_items, n_items, d_list, d_t2, d_camp);
-                    k_pcg_step<<<1, 1024, 0, st>>>(v, mt, nfc, nk, d_U, d_Hck, d_kvals, lam_use, d_camp, d_item_off,
-                                                   d_part, pblocks, d_pc, d_kvals + 3);
-                    chk(cudaGetLastError());
-                }
-                pcg_total += pit;
+                v.pf = d_pf;
+                v.npf = 6 * nfc;
+                PcgArgs<Real> PA;
+                PA.A = A;
+                PA.np = np;
+                PA.ne = ne;
+                PA.ncl = ncl;
+                PA.nfc = nfc;
+                PA.nk = nk;
+                PA.mt = mt;
+                PA.apm = d_apm;
+                PA.acm = d_acm;
+                PA.cm_pt = d_cmpt;
+                PA.items = d_items;
+                PA.n_items = n_items;
+                PA.item_off = d_item_off;
+                PA.pt_b = d_pb;
+                PA.pt_t2 = d_t2;
+                PA.camp = d_camp;
+                PA.U = d_U;
+                PA.Hck = d_Hck;
+                PA.kk = d_kvals;
+                PA.pc = d_pc;
+                PA.b = d_bs;
+                PA.lambda = lam_use;
+                PA.v = v;
+                PA.part = d_ppart;
+                PA.max_it = lm.pcg_max_iterations;
+                PA.tol2 = lm.pcg_tolerance * lm.pcg_tolerance;
+                PA.iters = d_pit;
+                void* kargs[] = {&PA};
+                chk(cudaLaunchCooperativeKernel((const void*)k_pcg_solve<Real>, dim3(pcg_grid), dim3(256), kargs, 0, st));
+                int32_t pit = 0;
+                chk(cudaMemcpyAsync(&pit, d_pit, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
                 chk(cudaMemcpyAsync(d_bs, v.x, sizeof(double) * mt, cudaMemcpyDeviceToDevice, st));
                 int32_t okh = 1;
                 chk(cudaMemcpyAsync(&okh, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
                 if (nk) chk(cudaMemcpyAsync(dk, v.x + m, sizeof(dk), cudaMemcpyDeviceToHost, st));
                 chk(cudaStreamSynchronize(st));
                 if (e != cudaSuccess) return e;
+                pcg_total += pit;
                 ok = ok && okh != 0;
                 if (!ok) {
                     chk(cudaMemsetAsync(d_bs, 0, sizeof(double) * mt, st));
