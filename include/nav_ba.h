@@ -52,10 +52,15 @@ typedef enum nav_ba_status {
 
 /* Camera models.  PINHOLE is nav24's Pinhole (Pinhole.cpp:30-36,70-80).  PINHOLE_RADIAL adds
  * the two-coefficient radial factor d = 1 + k1 r^2 + k2 r^4 on normalized coordinates; it has
- * no counterpart in nav24's BA (nav24 undistorts before BA, Calibration.cpp:135-148). */
+ * no counterpart in nav24's BA (nav24 undistorts before BA, Calibration.cpp:135-148).
+ * KANNALA_BRANDT8 is nav24's fisheye model (core/sensor/camera/models/KannalaBrandt8.cpp:80-107,
+ * Jacobian :195-226, selected at Calibration.cpp:81-82) with intrinsics fx, fy, cx, cy, k1..k4:
+ * pi = f r(theta) (x, y)/rho + c, theta = atan2(rho, z), r = theta + k1 theta^3 + ... + k4 theta^9,
+ * evaluated in the engine's precision (the reference rounds theta and psi to float). */
 typedef enum nav_ba_camera_model {
     NAV_BA_CAM_PINHOLE = 0,
-    NAV_BA_CAM_PINHOLE_RADIAL = 1
+    NAV_BA_CAM_PINHOLE_RADIAL = 1,
+    NAV_BA_CAM_KANNALA_BRANDT8 = 2
 } nav_ba_camera_model;
 
 typedef enum nav_ba_precision {
@@ -94,7 +99,7 @@ typedef struct nav_ba_problem {
     const int32_t* obs_point;     /* [n_obs] point index of each observation                */
     int32_t camera_model;         /* nav_ba_camera_model                                    */
     int32_t reserved0;
-    double intrinsics[8];         /* fx, fy, cx, cy, k1, k2, 0, 0                            */
+    double intrinsics[8];         /* fx, fy, cx, cy, k1, k2, 0, 0 (KANNALA_BRANDT8: k1..k4)  */
 } nav_ba_problem;
 
 typedef struct nav_ba_options {
@@ -229,6 +234,41 @@ nav_ba_status nav_ba_cost(nav_ba_ctx* ctx, const nav_ba_problem* problem,
 #define NAV_BA_NOALLOC_ARENA_BYTES (16u * 1024u * 1024u)
 nav_ba_status nav_ba_solve_noalloc(nav_ba_ctx* ctx, const nav_ba_problem* problem,
                                    const nav_ba_options* options, nav_ba_result* result);
+
+/* ---- motion-only BA (per-frame tracking) ------------------------------------------------------
+ *
+ * One free pose against fixed world points: nav24's EdgeSE3ProjectXYZOnlyPose (declared, commented
+ * out, in core/dataTypes/optimization/OptimizableTypes.hpp:34-60; linearizeOplus at
+ * OptimizableTypes.cpp:50-64: e = z - pi(T Xw), J = -Jpi [-[Xc]x | I]), the problem of the tracking call
+ * core/frontEnd/FE_SlamMonoV.cpp:153-165 when the current frame is optimized against a fixed map.
+ * The LM is the one of nav_ba_solve (iterations, robust kernel, damping, trials, precision), on the
+ * 6x6 normal equations.  nav_ba_solve_pose_batched solves n problems in one launch (one warp each).
+ * Statuses per problem as in nav_ba_solve_batched; a problem with no observation is EMPTY. */
+typedef struct nav_ba_pose_problem {
+    int32_t n_obs;
+    int32_t camera_model;         /* NAV_BA_CAM_PINHOLE or NAV_BA_CAM_PINHOLE_RADIAL (k1, k2 fixed) */
+    const double* pose;           /* [12] initial T_cw                                          */
+    const double* points;         /* [n_obs][3] fixed world point of each observation          */
+    const double* obs_uv;         /* [n_obs][2]                                                 */
+    double intrinsics[8];         /* fx, fy, cx, cy, k1, k2, 0, 0                               */
+} nav_ba_pose_problem;
+
+typedef struct nav_ba_pose_result {
+    double* pose_out;             /* [12] optimized T_cw, or NULL                              */
+    double initial_cost;
+    double final_cost;
+    double final_lambda;
+    int32_t iterations_done;
+    int32_t trials_accepted;
+    int32_t trials_rejected;
+    int32_t termination;          /* nav_ba_termination                                         */
+    int32_t status;               /* nav_ba_status of this problem                              */
+    int32_t reserved;
+} nav_ba_pose_result;
+
+nav_ba_status nav_ba_solve_pose_batched(nav_ba_ctx* ctx, const nav_ba_pose_problem* problems,
+                                        int32_t n_problems, const nav_ba_options* options,
+                                        nav_ba_pose_result* results);
 
 /* ---- differentiation through the LM steps (no counterpart in the reference) ----------------
  *

@@ -21,7 +21,7 @@ EXPORTS = [
     "nav_ba_solve_batched", "nav_ba_prepare", "nav_ba_run", "nav_ba_fetch", "nav_ba_prepare_batched",
     "nav_ba_fetch_batched", "nav_ba_linearize",
     "nav_ba_reduced_system", "nav_ba_cost", "nav_ba_last_error", "nav_ba_status_string",
-    "nav_ba_abi_version", "nav_ba_solve_noalloc", "nav_ba_vjp",
+    "nav_ba_abi_version", "nav_ba_solve_noalloc", "nav_ba_vjp", "nav_ba_solve_pose_batched",
 ]
 
 _LIB = None
@@ -78,6 +78,9 @@ def load(path: os.PathLike | None = None) -> C.CDLL:
     L.nav_ba_vjp.argtypes = [ctxp, P, O, C.POINTER(abi.nav_ba_schedule), C.POINTER(abi.nav_ba_cotangent), R,
                              C.POINTER(abi.nav_ba_grads)]
     L.nav_ba_vjp.restype = C.c_int
+    L.nav_ba_solve_pose_batched.argtypes = [ctxp, C.POINTER(abi.nav_ba_pose_problem), C.c_int32, O,
+                                            C.POINTER(abi.nav_ba_pose_result)]
+    L.nav_ba_solve_pose_batched.restype = C.c_int
     L.nav_ba_abi_version.argtypes = []
     L.nav_ba_abi_version.restype = C.c_int32
     if path is None:
@@ -187,6 +190,20 @@ class Context:
             g["intrinsics"] = np.array([grads.intrinsics[i] for i in range(4)])
             out = g
         return buf.result(st), sched.lambdas, out
+
+    def solve_pose_batched(self, probs: list[abi.PoseProblem], opt: abi.nav_ba_options):
+        """nav_ba_solve_pose_batched: motion-only BA of every problem in one launch.  Returns
+        [(pose [12], stats dict)]."""
+        n = len(probs)
+        cp = (abi.nav_ba_pose_problem * max(n, 1))(*[p.as_c() for p in probs])
+        outs = [np.zeros(12) for _ in probs]
+        cr = (abi.nav_ba_pose_result * max(n, 1))()
+        for i in range(n):
+            cr[i].pose_out = _d(outs[i])
+        st = self.L.nav_ba_solve_pose_batched(self.h, cp, n, C.byref(opt), cr)
+        self._check(st)
+        return [(outs[i], {f: getattr(cr[i], f) for f, _ in abi.nav_ba_pose_result._fields_ if f != "pose_out"})
+                for i in range(n)]
 
     def solve_batched(self, probs: list[abi.Problem], opt: abi.nav_ba_options) -> list[abi.Result]:
         n = len(probs)

@@ -24,6 +24,7 @@ ERR_NO_DEVICE = -8
 
 CAM_PINHOLE = 0
 CAM_PINHOLE_RADIAL = 1
+CAM_KANNALA_BRANDT8 = 2
 FP64 = 0
 MIXED = 1
 SOLVER_CHOLESKY = 0
@@ -104,6 +105,54 @@ class nav_ba_result(C.Structure):
         ("h2d_bytes", C.c_int64),
         ("d2h_bytes", C.c_int64),
     ]
+
+
+class nav_ba_pose_problem(C.Structure):
+    _fields_ = [("n_obs", C.c_int32), ("camera_model", C.c_int32), ("pose", C.POINTER(C.c_double)),
+                ("points", C.POINTER(C.c_double)), ("obs_uv", C.POINTER(C.c_double)), ("intrinsics", C.c_double * 8)]
+
+
+class nav_ba_pose_result(C.Structure):
+    _fields_ = [("pose_out", C.POINTER(C.c_double)), ("initial_cost", C.c_double), ("final_cost", C.c_double),
+                ("final_lambda", C.c_double), ("iterations_done", C.c_int32), ("trials_accepted", C.c_int32),
+                ("trials_rejected", C.c_int32), ("termination", C.c_int32), ("status", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+@dataclass
+class PoseProblem:
+    """One motion-only problem: a pose against fixed world points (nav_ba_pose_problem)."""
+
+    pose: np.ndarray          # (12,) row-major [R|t] of T_cw
+    points: np.ndarray        # (n_obs, 3) world point of each observation
+    obs_uv: np.ndarray        # (n_obs, 2)
+    intrinsics: np.ndarray    # (8,)
+    camera_model: int = CAM_PINHOLE
+
+    def __post_init__(self):
+        self.pose = np.ascontiguousarray(self.pose, np.float64).reshape(12)
+        self.points = np.ascontiguousarray(self.points, np.float64).reshape(-1, 3)
+        self.obs_uv = np.ascontiguousarray(self.obs_uv, np.float64).reshape(-1, 2)
+        self.intrinsics = np.ascontiguousarray(self.intrinsics, np.float64).reshape(8)
+
+    def as_c(self) -> nav_ba_pose_problem:
+        p = nav_ba_pose_problem()
+        p.n_obs = self.obs_uv.shape[0]
+        p.camera_model = int(self.camera_model)
+        p.pose = _ptr(self.pose, C.c_double)
+        p.points = _ptr(self.points, C.c_double)
+        p.obs_uv = _ptr(self.obs_uv, C.c_double)
+        for i in range(8):
+            p.intrinsics[i] = float(self.intrinsics[i])
+        return p
+
+    def as_problem(self) -> "Problem":
+        """The same problem as a general one: one free camera, every point fixed."""
+        n = self.obs_uv.shape[0]
+        return Problem(cam_pose=self.pose.reshape(1, 12), points=self.points, obs_uv=self.obs_uv,
+                       obs_cam=np.zeros(n, np.int32), obs_point=np.arange(n, dtype=np.int32),
+                       intrinsics=self.intrinsics, cam_fixed=np.zeros(1, np.uint8),
+                       point_fixed=np.ones(n, np.uint8), camera_model=self.camera_model)
 
 
 VJP_MAX_STEPS = 64

@@ -17,9 +17,14 @@
 namespace navba {
 
 struct Intr {
-    double fx, fy, cx, cy, k1, k2;
-    int model;  // 0 pinhole, 1 pinhole + radial(k1,k2)
+    double fx, fy, cx, cy, k1, k2, k3, k4;
+    int model;  // 0 pinhole, 1 pinhole + radial (k1, k2), 2 Kannala-Brandt (k1..k4)
 };
+
+// Intrinsics from the 8 values of nav_ba_problem::intrinsics and the camera model.
+NAVBA_HD Intr make_intr(const double* k8, int model) {
+    return Intr{k8[0], k8[1], k8[2], k8[3], k8[4], k8[5], k8[6], k8[7], model};
+}
 
 // ---- quaternions (x, y, z, w), unit, w >= 0 ---------------------------------------------
 
@@ -215,6 +220,45 @@ template <class Real>
 NAVBA_HD void project(const Intr& in, const Real* Xc, Real* uv, Real* J, Real* Jk = nullptr) {
     const Real x = Xc[0], y = Xc[1], z = Xc[2];
     const Real fx = (Real)in.fx, fy = (Real)in.fy, cx = (Real)in.cx, cy = (Real)in.cy;
+    if (in.model == 2) {
+        // Kannala-Brandt (KannalaBrandt8.cpp:80-107 projection, :195-226 Jacobian), in Real throughout:
+        // pi = f r(theta) (x, y) / rho + c, theta = atan2(rho, z), r = theta + k1 theta^3 + .. + k4 theta^9.
+        // (The reference rounds theta and psi to float in project; here they keep Real precision.)
+        // With A = r'(theta) z / (rho^2 + z^2) and B = r / rho the Jacobian is
+        //   [[fx (x^2 A + y^2 B), fx x y (A - B)] / rho^2, -fx r' x / (rho^2 + z^2)], likewise for v;
+        // on the optical axis (rho <= 1e-9 |z|) both reduce to the pinhole values (B -> 1/z).
+        const Real fx = (Real)in.fx, fy = (Real)in.fy, cx = (Real)in.cx, cy = (Real)in.cy;
+        const Real k1 = (Real)in.k1, k2 = (Real)in.k2, k3 = (Real)in.k3, k4 = (Real)in.k4;
+        const Real rho2 = x * x + y * y, rho = sqrt(rho2);
+        const Real rz2 = rho2 + z * z;
+        if (rho <= Real(1e-9) * fabs(z)) {
+            const Real iz = Real(1) / z;
+            uv[0] = fx * x * iz + cx;
+            uv[1] = fy * y * iz + cy;
+            if (J) {
+                J[0] = fx * iz; J[1] = Real(0); J[2] = -fx * x * iz * iz;
+                J[3] = Real(0); J[4] = fy * iz; J[5] = -fy * y * iz * iz;
+            }
+        } else {
+            const Real th = atan2(rho, z), t2 = th * th;
+            const Real r = th * (Real(1) + t2 * (k1 + t2 * (k2 + t2 * (k3 + t2 * k4))));
+            const Real B = r / rho;
+            uv[0] = fx * B * x + cx;
+            uv[1] = fy * B * y + cy;
+            if (J) {
+                const Real rd = Real(1) + t2 * (Real(3) * k1 + t2 * (Real(5) * k2 + t2 * (Real(7) * k3 + t2 * Real(9) * k4)));
+                const Real A = rd * z / rz2;
+                const Real ir2 = Real(1) / rho2;
+                J[0] = fx * (x * x * A + y * y * B) * ir2;
+                J[1] = fx * x * y * (A - B) * ir2;
+                J[2] = -fx * rd * x / rz2;
+                J[3] = fy * x * y * (A - B) * ir2;
+                J[4] = fy * (y * y * A + x * x * B) * ir2;
+                J[5] = -fy * rd * y / rz2;
+            }
+        }
+        return;
+    }
     const Real iz = Real(1) / z;  // one division per edge; the rest are products
     if (in.model == 0) {
         const Real xn = x * iz, yn = y * iz;

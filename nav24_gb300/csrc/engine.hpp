@@ -177,6 +177,30 @@ cudaError_t grid_solve(const HostWindow& h, const LmOptions& lm, const Intr& int
                        cudaStream_t stream, int cluster, GridResult& out, double debug_lambda,
                        std::vector<double>* debug_S, GridVjp* vjp = nullptr);
 
+// Motion-only BA (pose_engine.cu): per problem descriptor, statistics, and the reused device buffers.
+struct PoseDesc {
+    int64_t o0;       // first observation (global)
+    int32_t n;        // observations
+    int32_t model;    // camera model
+    double intr[8];   // fx fy cx cy k1 k2 k3 k4
+};
+struct PoseStat {
+    double initial_cost, final_cost, final_lambda;
+    int32_t iters, acc, rej, term, status, pad;
+};
+struct PoseBatch {
+    PoseDesc* d_desc = nullptr;
+    CamState* d_cam_in = nullptr;
+    CamState* d_cam_out = nullptr;
+    double* d_pts = nullptr;   // [no][4]
+    double* d_uv = nullptr;    // [no][2]
+    PoseStat* d_stats = nullptr;
+    size_t cap[6] = {};
+    void release();
+};
+nav_ba_status solve_pose_batch(cudaStream_t stream, PoseBatch& B, const nav_ba_pose_problem* probs, int n,
+                               const nav_ba_options& o, nav_ba_pose_result* res, float* ms, std::string* why);
+
 // One-window solve in the library's static device array (no device allocation), noalloc.cu.
 nav_ba_status solve_window_noalloc(int device, cudaStream_t stream, const nav_ba_problem& p,
                                    const nav_ba_options& o, nav_ba_result& r, std::string* why);

@@ -23,6 +23,7 @@ struct nav_ba_ctx {
     PreparedBatch prepared;
     std::vector<nav_ba_problem> prepared_problems;  // shapes of the prepared problem (no data)
     nav_ba_options prepared_opts{};
+    PoseBatch pose;  // device buffers of nav_ba_solve_pose_batched (reused)
     bool has_prepared = false;
     WindowLaunch shape[2];        // per precision (autotuned on nav_ba_prepare_batched)
     bool tuned[2] = {false, false};
@@ -64,8 +65,7 @@ LmOptions lm_options(const nav_ba_options& o) {
 }
 
 Intr intrinsics_of(const nav_ba_problem& p) {
-    return Intr{p.intrinsics[0], p.intrinsics[1], p.intrinsics[2], p.intrinsics[3],
-                p.intrinsics[4], p.intrinsics[5], p.camera_model};
+    return make_intr(p.intrinsics, p.camera_model);
 }
 
 // Outputs of a problem nothing is done to: the round-trip of each pose through its quaternion
@@ -420,6 +420,7 @@ void nav_ba_destroy(nav_ba_ctx* ctx) {
     cudaSetDevice(ctx->device);
     window_batch_free(ctx->prepared.dev);
     window_batch_free(ctx->solve_dev);
+    ctx->pose.release();
     ctx->stg.release();
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -651,6 +652,25 @@ nav_ba_status nav_ba_solve_noalloc(nav_ba_ctx* ctx, const nav_ba_problem* p, con
     }
     if (st != NAV_BA_OK) return set_err(ctx, st, why);
     *r = tmp;
+    return NAV_BA_OK;
+}
+
+nav_ba_status nav_ba_solve_pose_batched(nav_ba_ctx* ctx, const nav_ba_pose_problem* probs, int32_t n,
+                                        const nav_ba_options* o, nav_ba_pose_result* results) {
+    if (!ctx) return NAV_BA_ERR_ARGUMENT;
+    if ((!probs && n > 0) || !o || (!results && n > 0) || n < 0) return set_err(ctx, NAV_BA_ERR_ARGUMENT, "NULL argument");
+    cudaSetDevice(ctx->device);
+    std::string why;
+    nav_ba_status st = validate_options(o, &why);
+    if (st != NAV_BA_OK) return set_err(ctx, st, why);
+    if (o->solver != NAV_BA_SOLVER_CHOLESKY || o->optimize_distortion)
+        return set_err(ctx, NAV_BA_ERR_UNSUPPORTED, "motion-only BA solves its 6x6 system by Cholesky, without distortion");
+    std::vector<nav_ba_pose_result> tmp(results, results + n);  // outputs untouched on error
+    float ms = 0.f;
+    st = solve_pose_batch(ctx->stream, ctx->pose, probs, n, *o, tmp.data(), &ms, &why);
+    if (st != NAV_BA_OK) return set_err(ctx, st, why);
+    for (int i = 0; i < n; ++i) results[i] = tmp[i];
+    (void)ms;
     return NAV_BA_OK;
 }
 

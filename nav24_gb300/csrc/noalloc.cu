@@ -163,8 +163,7 @@ nav_ba_status solve_window_noalloc(int device, cudaStream_t stream, const nav_ba
     pb.lm.huber_delta = o.huber_delta;
     pb.lm.initial_lambda = o.initial_lambda;
     pb.lm.tau = o.tau;
-    pb.intr = Intr{p.intrinsics[0], p.intrinsics[1], p.intrinsics[2], p.intrinsics[3], p.intrinsics[4],
-                   p.intrinsics[5], p.camera_model};
+    pb.intr = make_intr(p.intrinsics, p.camera_model);
     auto up = [&](void* dst, const void* src, size_t bytes) {
         if (e != cudaSuccess || bytes == 0) return;
         e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream);

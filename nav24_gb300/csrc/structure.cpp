@@ -22,7 +22,8 @@ nav_ba_status validate_problem(const nav_ba_problem* p, std::string* why) {
     if ((p->n_cams && !p->cam_pose) || (p->n_points && !p->points) ||
         (p->n_obs && (!p->obs_uv || !p->obs_cam || !p->obs_point)))
         return fail(NAV_BA_ERR_ARGUMENT, "NULL array with nonzero size");
-    if (p->camera_model != NAV_BA_CAM_PINHOLE && p->camera_model != NAV_BA_CAM_PINHOLE_RADIAL)
+    if (p->camera_model != NAV_BA_CAM_PINHOLE && p->camera_model != NAV_BA_CAM_PINHOLE_RADIAL &&
+        p->camera_model != NAV_BA_CAM_KANNALA_BRANDT8)
         return fail(NAV_BA_ERR_ARGUMENT, "unknown camera model");
     for (int o = 0; o < p->n_obs; ++o)
         if (p->obs_cam[o] < 0 || p->obs_cam[o] >= p->n_cams || p->obs_point[o] < 0 ||

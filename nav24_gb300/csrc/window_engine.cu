@@ -811,8 +811,7 @@ cudaError_t linearize_observations(const nav_ba_problem& p, const nav_ba_options
         chk(cudaMemcpyAsync(d_op, p.obs_point, sizeof(int32_t) * n, cudaMemcpyHostToDevice, stream));
     }
     if (err == cudaSuccess) {
-        Intr in{p.intrinsics[0], p.intrinsics[1], p.intrinsics[2], p.intrinsics[3], p.intrinsics[4],
-                p.intrinsics[5], p.camera_model};
+        const Intr in = make_intr(p.intrinsics, p.camera_model);
         double* oe = d_out;
         double* ojc = oe + 2LL * n;
         double* ojp = ojc + 12LL * n;

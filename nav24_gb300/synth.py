@@ -131,6 +131,22 @@ class Synth:
     def windows(self) -> list[abi.Problem]:
         return [self.window(w) for w in range(self.n_windows)]
 
+    def pose_problems(self) -> list[abi.PoseProblem]:
+        """Tracking problems: per window, its last camera (perturbed initial pose) against the window's
+        points seen by it, held fixed at their initial positions (the current frame optimized against
+        a fixed map, as in FE_SlamMonoV.cpp:153-165)."""
+        out = []
+        for w in range(self.n_windows):
+            c0, c1 = self.win_cam[w], self.win_cam[w + 1]
+            p0 = self.win_pt[w]
+            o0, o1 = self.win_obs[w], self.win_obs[w + 1]
+            cam = c1 - c0 - 1
+            sel = np.nonzero(self.obs_cam[o0:o1] == cam)[0] + o0
+            out.append(abi.PoseProblem(pose=self.cam_pose[c1 - 1], points=self.points[p0 + self.obs_point[sel]],
+                                       obs_uv=self.obs_uv[sel], intrinsics=self.intrinsics_init,
+                                       camera_model=self.camera_model))
+        return out
+
 
 # Named workloads (one per family) with their solver options.
 def workload_options(family: int, precision: int = abi.FP64) -> abi.nav_ba_options:

@@ -212,7 +212,7 @@ struct EdgeLin {
 
 struct Model {
     int model;
-    double fx, fy, cx, cy, k1, k2;
+    double fx, fy, cx, cy, k1, k2, k3 = 0.0, k4 = 0.0;
 };
 
 // Residual and Jacobians of one edge.  Returns false when the edge cannot be evaluated
@@ -227,7 +227,35 @@ void linearize_edge(const Model& m, const SE3& T, const double* X, const double*
     double u, v;
     double J[6];  // d pi / d Xc, 2x3
     double jk[4] = {0, 0, 0, 0};
-    if (m.model == NAV_BA_CAM_PINHOLE) {
+    if (m.model == NAV_BA_CAM_KANNALA_BRANDT8) {
+        // KannalaBrandt8::project (KannalaBrandt8.cpp:80-107) and ::projectJac (:195-226), in FP64
+        // (the reference's project rounds theta and psi to float; its projectJac is FP64):
+        //   theta = atan2(rho, z), r = theta + k1 theta^3 + k2 theta^5 + k3 theta^7 + k4 theta^9,
+        //   (u, v) = (fx r cos psi + cx, fy r sin psi + cy) with cos psi = x / rho, sin psi = y / rho.
+        // On the optical axis the limit is the pinhole projection.
+        const double rho2 = x * x + y * y, rho = std::sqrt(rho2), z2 = zc * zc;
+        if (rho <= 1e-9 * std::fabs(zc)) {
+            u = m.fx * x / zc + m.cx;
+            v = m.fy * y / zc + m.cy;
+            J[0] = m.fx / zc; J[1] = 0.0; J[2] = -m.fx * x / z2;
+            J[3] = 0.0; J[4] = m.fy / zc; J[5] = -m.fy * y / z2;
+        } else {
+            const double th = std::atan2(rho, zc);
+            const double t2 = th * th, t3 = t2 * th, t4 = t2 * t2, t5 = t4 * th, t6 = t4 * t2, t7 = t6 * th,
+                         t8 = t4 * t4, t9 = t8 * th;
+            const double f = th + m.k1 * t3 + m.k2 * t5 + m.k3 * t7 + m.k4 * t9;
+            const double fd = 1.0 + 3.0 * m.k1 * t2 + 5.0 * m.k2 * t4 + 7.0 * m.k3 * t6 + 9.0 * m.k4 * t8;
+            u = m.fx * f * x / rho + m.cx;
+            v = m.fy * f * y / rho + m.cy;
+            const double rho3 = rho2 * rho, x2 = x * x, y2 = y * y;
+            J[0] = m.fx * (fd * zc * x2 / (rho2 * (rho2 + z2)) + f * y2 / rho3);
+            J[1] = m.fx * (fd * zc * y * x / (rho2 * (rho2 + z2)) - f * y * x / rho3);
+            J[2] = -m.fx * fd * x / (rho2 + z2);
+            J[3] = m.fy * (fd * zc * y * x / (rho2 * (rho2 + z2)) - f * y * x / rho3);
+            J[4] = m.fy * (fd * zc * y2 / (rho2 * (rho2 + z2)) + f * x2 / rho3);
+            J[5] = -m.fy * fd * y / (rho2 + z2);
+        }
+    } else if (m.model == NAV_BA_CAM_PINHOLE) {
         // Pinhole::project (Pinhole.cpp:30-36) and Pinhole::projectJac (Pinhole.cpp:70-80)
         u = m.fx * x / zc + m.cx;
         v = m.fy * y / zc + m.cy;
@@ -312,7 +340,8 @@ int32_t validate(const nav_ba_problem* p) {
     if ((p->n_cams && !p->cam_pose) || (p->n_points && !p->points) ||
         (p->n_obs && (!p->obs_uv || !p->obs_cam || !p->obs_point)))
         return NAV_BA_ERR_ARGUMENT;
-    if (p->camera_model != NAV_BA_CAM_PINHOLE && p->camera_model != NAV_BA_CAM_PINHOLE_RADIAL)
+    if (p->camera_model != NAV_BA_CAM_PINHOLE && p->camera_model != NAV_BA_CAM_PINHOLE_RADIAL &&
+        p->camera_model != NAV_BA_CAM_KANNALA_BRANDT8)
         return NAV_BA_ERR_ARGUMENT;
     for (int o = 0; o < p->n_obs; ++o)
         if (p->obs_cam[o] < 0 || p->obs_cam[o] >= p->n_cams || p->obs_point[o] < 0 ||
@@ -356,6 +385,7 @@ public:
         M.fx = p.intrinsics[0]; M.fy = p.intrinsics[1];
         M.cx = p.intrinsics[2]; M.cy = p.intrinsics[3];
         M.k1 = p.intrinsics[4]; M.k2 = p.intrinsics[5];
+        M.k3 = p.intrinsics[6]; M.k4 = p.intrinsics[7];
         k[0] = M.k1; k[1] = M.k2;
         nc = p.n_cams;
         np = p.n_points;
@@ -1018,6 +1048,7 @@ extern "C" int32_t oracle_linearize(const nav_ba_problem* p, const nav_ba_option
     m.model = p->camera_model;
     m.fx = p->intrinsics[0]; m.fy = p->intrinsics[1]; m.cx = p->intrinsics[2]; m.cy = p->intrinsics[3];
     m.k1 = p->intrinsics[4]; m.k2 = p->intrinsics[5];
+    m.k3 = p->intrinsics[6]; m.k4 = p->intrinsics[7];
     EdgeLin L;
     for (int k = 0; k < p->n_obs; ++k) {
         const SE3 T = se3_from_pose12(p->cam_pose + 12LL * p->obs_cam[k]);
@@ -1038,6 +1069,7 @@ extern "C" int32_t oracle_distortion_jacobian(const nav_ba_problem* p, double* j
     m.model = p->camera_model;
     m.fx = p->intrinsics[0]; m.fy = p->intrinsics[1]; m.cx = p->intrinsics[2]; m.cy = p->intrinsics[3];
     m.k1 = p->intrinsics[4]; m.k2 = p->intrinsics[5];
+    m.k3 = p->intrinsics[6]; m.k4 = p->intrinsics[7];
     EdgeLin L;
     for (int k = 0; k < p->n_obs; ++k) {
         const SE3 T = se3_from_pose12(p->cam_pose + 12LL * p->obs_cam[k]);

@@ -45,6 +45,8 @@ int main(void) {{
          offsetof(nav_ba_result, status), offsetof(nav_synth_params, min_points));
   printf("%zu %zu %zu %zu %zu\\n", sizeof(nav_ba_schedule), sizeof(nav_ba_cotangent), sizeof(nav_ba_grads),
          offsetof(nav_ba_schedule, lambda), offsetof(nav_ba_grads, cam_tangent));
+  printf("%zu %zu %zu %zu\\n", sizeof(nav_ba_pose_problem), sizeof(nav_ba_pose_result),
+         offsetof(nav_ba_pose_problem, intrinsics), offsetof(nav_ba_pose_result, status));
   return 0;
 }}
 """)
@@ -57,7 +59,9 @@ int main(void) {{
             abi.nav_ba_options.pcg_tolerance.offset, abi.nav_ba_result.status.offset,
             abi.nav_synth_params.min_points.offset,
             C.sizeof(abi.nav_ba_schedule), C.sizeof(abi.nav_ba_cotangent), C.sizeof(abi.nav_ba_grads),
-            abi.nav_ba_schedule.lam.offset, abi.nav_ba_grads.cam_tangent.offset]
+            abi.nav_ba_schedule.lam.offset, abi.nav_ba_grads.cam_tangent.offset,
+            C.sizeof(abi.nav_ba_pose_problem), C.sizeof(abi.nav_ba_pose_result),
+            abi.nav_ba_pose_problem.intrinsics.offset, abi.nav_ba_pose_result.status.offset]
     assert got == want
 
 

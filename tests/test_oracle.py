@@ -329,3 +329,55 @@ def test_schedule_replay_reproduces_the_solve():
     assert np.array_equal(r2.cam_pose, r.cam_pose) and np.array_equal(r2.points, r.points)
     r0 = oracle.solve(p, o)
     assert r0.stats["final_cost"] == r.stats["final_cost"]
+
+
+def test_kb8_projection_matches_reference_formula():
+    """The oracle's Kannala-Brandt residual equals z - pi of the reference's formula (FP64 angles);
+    the reference's float rounding of theta and psi moves a projection by far less than a pixel."""
+    from kb8_util import kb8_problem, kb8_project, transform
+    p = kb8_problem(n_cams=10, n_points=400)
+    e, jc, jp, w = oracle.linearize(p, abi.default_options())
+    pi = kb8_project(p.intrinsics, transform(p))
+    assert rel_err(e, p.obs_uv - pi) < 1e-12
+    assert np.max(np.abs(kb8_project(p.intrinsics, transform(p), float_angles=True) - pi)) < 1e-3
+
+
+def test_kb8_jacobians_central_differences():
+    from kb8_util import kb8_problem
+    p = kb8_problem(n_cams=10, n_points=60)
+    o = abi.default_options()
+    e0, jc, jp, _ = oracle.linearize(p, o)
+    h = 1e-6
+    for k in range(0, p.n_obs, 5):
+        c, i = p.obs_cam[k], p.obs_point[k]
+        sub = abi.Problem(cam_pose=p.cam_pose[c], points=p.points[i], obs_uv=p.obs_uv[k], obs_cam=[0], obs_point=[0],
+                          intrinsics=p.intrinsics, camera_model=p.camera_model)
+        fd_c = np.zeros((2, 6))
+        for j in range(6):
+            d = np.zeros(6)
+            d[j] = h
+            sp_, sm_ = sub.copy(), sub.copy()
+            sp_.cam_pose[0] = _pose_apply(sub.cam_pose[0], d)
+            sm_.cam_pose[0] = _pose_apply(sub.cam_pose[0], -d)
+            fd_c[:, j] = (oracle.linearize(sp_, o)[0][0] - oracle.linearize(sm_, o)[0][0]) / (2 * h)
+        fd_p = np.zeros((2, 3))
+        for j in range(3):
+            sp_, sm_ = sub.copy(), sub.copy()
+            sp_.points[0, j] += h
+            sm_.points[0, j] -= h
+            fd_p[:, j] = (oracle.linearize(sp_, o)[0][0] - oracle.linearize(sm_, o)[0][0]) / (2 * h)
+        assert rel_err(jc[k], fd_c) < 1e-6
+        assert rel_err(jp[k], fd_p) < 1e-6
+
+
+def test_kb8_on_the_optical_axis():
+    """A point on the optical axis: the reference's Jacobian divides by rho = 0; the limit (the
+    pinhole values) is used, and it is the limit of the off-axis Jacobian."""
+    from kb8_util import KB8
+    pose = np.array([1.0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0])
+    mk = lambda X: abi.Problem(cam_pose=pose, points=np.array(X, float), obs_uv=np.array([320.0, 240.0]),
+                               obs_cam=[0], obs_point=[0], intrinsics=KB8, camera_model=abi.CAM_KANNALA_BRANDT8)
+    e, jc, jp, _ = oracle.linearize(mk([0.0, 0.0, 2.0]), abi.default_options())
+    assert np.all(np.isfinite(jp)) and np.allclose(e, 0.0)
+    _, _, jp_off, _ = oracle.linearize(mk([1e-6, 2e-6, 2.0]), abi.default_options())
+    assert rel_err(jp_off, jp) < 1e-6
