@@ -270,6 +270,58 @@ nav_ba_status nav_ba_solve_pose_batched(nav_ba_ctx* ctx, const nav_ba_pose_probl
                                         int32_t n_problems, const nav_ba_options* options,
                                         nav_ba_pose_result* results);
 
+/* ---- two-view triangulation and hypothesis check (map initialization) --------------------------
+ *
+ * The per-match work of TwoViewReconstruction::CheckRT (core/operators/mapInit/
+ * OP_2ViewReconstruction.cpp:1244-1353) with Triangulate (:1179-1193), for n_hyp relative-pose
+ * hypotheses (R, t of camera 2 with respect to camera 1, e.g. the 4 of ReconstructF or the 8 of
+ * ReconstructH) and n_matches matches at once.  Per hypothesis and match: the DLT point of
+ * A = [x1 P1_3 - P1_1; y1 P1_3 - P1_2; x2 P2_3 - P2_1; y2 P2_3 - P2_2] (P1 = K[I|0], P2 = K[R|t]) as the
+ * right singular vector of A's smallest singular value (one-sided Jacobi SVD, FP64), then the checks
+ * in CheckRT's order:
+ * finite, depth > 0 in camera 1 and camera 2 unless the parallax is below the minimum, squared
+ * reprojection error <= th2 in both images.  A match that passes is "triangulated" (counted in
+ * n_good); it is also "good" (vbGood) when cos(parallax) < min_parallax_cos.  parallax_deg is
+ * CheckRT's statistic: acos of the sorted cos-parallax values at index min(min_triangulated, n - 1),
+ * in degrees (0 when no match passes). */
+typedef struct nav_ba_twoview {
+    int32_t n_matches;
+    int32_t n_hyp;
+    double K[4];                  /* fx, fy, cx, cy                                             */
+    const double* kp1;            /* [n_matches][2] pixel in image 1                            */
+    const double* kp2;            /* [n_matches][2] pixel in image 2                            */
+    const uint8_t* inlier;        /* [n_matches] vbMatchesInliers, or NULL (all)                */
+    const double* R;              /* [n_hyp][9] row-major                                       */
+    const double* t;              /* [n_hyp][3]                                                 */
+    double th2;                   /* squared reprojection threshold (CheckRT: 4 sigma^2)        */
+    double min_parallax_cos;      /* mMinParallaxCRT                                            */
+    int32_t min_triangulated;     /* mMinTriangulated                                           */
+    int32_t reserved;
+} nav_ba_twoview;
+
+typedef struct nav_ba_twoview_result {
+    double* points;               /* [n_hyp][n_matches][3] point in camera 1 (of every match
+                                     whose DLT point is finite; NaN otherwise), or NULL         */
+    uint8_t* triangulated;        /* [n_hyp][n_matches] passed every check, or NULL            */
+    uint8_t* good;                /* [n_hyp][n_matches] vbGood, or NULL                        */
+    int32_t* n_good;              /* [n_hyp] nGood                                              */
+    double* parallax_deg;         /* [n_hyp]                                                    */
+} nav_ba_twoview_result;
+
+nav_ba_status nav_ba_twoview_check(nav_ba_ctx* ctx, const nav_ba_twoview* in, nav_ba_twoview_result* out);
+
+/* ---- keypoint undistortion (the measurements BA consumes) ------------------------------------
+ *
+ * Calibration::undistort (core/sensor/camera/Calibration.cpp:135-148) -> PinholeRadTan::
+ * UndistortKeyPoints (core/sensor/camera/models/PinholeRadTan.cpp:11-24) -> cv::undistortPoints
+ * with R = I and P = K: the fixed-point inversion of the radial-tangential model on normalized
+ * coordinates, x <- (x_d - dx(x)) / (1 + k1 r^2 + k2 r^4), `iterations` times (OpenCV's default: 5),
+ * mapped back through K; FP64.  K = fx, fy, cx, cy; dist = k1, k2, p1, p2 (the 4-coefficient order
+ * of mD_cv).  uv_in and uv_out are [n][2] and may be the same array. */
+nav_ba_status nav_ba_undistort_points(nav_ba_ctx* ctx, const double* K, const double* dist,
+                                      int32_t iterations, int32_t n, const double* uv_in,
+                                      double* uv_out);
+
 /* ---- differentiation through the LM steps (no counterpart in the reference) ----------------
  *
  * The differentiable function is the LM solve with its damping schedule frozen: the steps that

@@ -22,6 +22,7 @@ EXPORTS = [
     "nav_ba_fetch_batched", "nav_ba_linearize",
     "nav_ba_reduced_system", "nav_ba_cost", "nav_ba_last_error", "nav_ba_status_string",
     "nav_ba_abi_version", "nav_ba_solve_noalloc", "nav_ba_vjp", "nav_ba_solve_pose_batched",
+    "nav_ba_twoview_check", "nav_ba_undistort_points",
 ]
 
 _LIB = None
@@ -81,6 +82,10 @@ def load(path: os.PathLike | None = None) -> C.CDLL:
     L.nav_ba_solve_pose_batched.argtypes = [ctxp, C.POINTER(abi.nav_ba_pose_problem), C.c_int32, O,
                                             C.POINTER(abi.nav_ba_pose_result)]
     L.nav_ba_solve_pose_batched.restype = C.c_int
+    L.nav_ba_twoview_check.argtypes = [ctxp, C.POINTER(abi.nav_ba_twoview), C.POINTER(abi.nav_ba_twoview_result)]
+    L.nav_ba_twoview_check.restype = C.c_int
+    L.nav_ba_undistort_points.argtypes = [ctxp, dp, dp, C.c_int32, C.c_int32, dp, dp]
+    L.nav_ba_undistort_points.restype = C.c_int
     L.nav_ba_abi_version.argtypes = []
     L.nav_ba_abi_version.restype = C.c_int32
     if path is None:
@@ -204,6 +209,47 @@ class Context:
         self._check(st)
         return [(outs[i], {f: getattr(cr[i], f) for f, _ in abi.nav_ba_pose_result._fields_ if f != "pose_out"})
                 for i in range(n)]
+
+    def twoview_check(self, K, kp1, kp2, R, t, th2: float, min_parallax_cos: float, min_triangulated: int = 50,
+                      inlier=None):
+        """nav_ba_twoview_check for hypotheses R [n_hyp, 3, 3], t [n_hyp, 3].  Returns a dict of points
+        [n_hyp, n, 3], triangulated / good [n_hyp, n] (bool), n_good [n_hyp], parallax_deg [n_hyp]."""
+        kp1 = np.ascontiguousarray(kp1, np.float64).reshape(-1, 2)
+        kp2 = np.ascontiguousarray(kp2, np.float64).reshape(-1, 2)
+        R = np.ascontiguousarray(R, np.float64).reshape(-1, 9)
+        t = np.ascontiguousarray(t, np.float64).reshape(-1, 3)
+        n, nh = kp1.shape[0], R.shape[0]
+        tv = abi.nav_ba_twoview()
+        tv.n_matches, tv.n_hyp = n, nh
+        for i in range(4):
+            tv.K[i] = float(K[i])
+        tv.kp1, tv.kp2, tv.R, tv.t = _d(kp1), _d(kp2), _d(R), _d(t)
+        inl = None
+        if inlier is not None:
+            inl = np.ascontiguousarray(inlier, np.uint8)
+            tv.inlier = inl.ctypes.data_as(C.POINTER(C.c_uint8))
+        tv.th2, tv.min_parallax_cos, tv.min_triangulated = th2, min_parallax_cos, min_triangulated
+        out = {"points": np.zeros((nh, n, 3)), "triangulated": np.zeros((nh, n), np.uint8),
+               "good": np.zeros((nh, n), np.uint8), "n_good": np.zeros(nh, np.int32), "parallax_deg": np.zeros(nh)}
+        r = abi.nav_ba_twoview_result()
+        r.points = _d(out["points"])
+        r.triangulated = out["triangulated"].ctypes.data_as(C.POINTER(C.c_uint8))
+        r.good = out["good"].ctypes.data_as(C.POINTER(C.c_uint8))
+        r.n_good = out["n_good"].ctypes.data_as(C.POINTER(C.c_int32))
+        r.parallax_deg = _d(out["parallax_deg"])
+        self._check(self.L.nav_ba_twoview_check(self.h, C.byref(tv), C.byref(r)))
+        out["triangulated"] = out["triangulated"].astype(bool)
+        out["good"] = out["good"].astype(bool)
+        return out
+
+    def undistort_points(self, K, dist, uv, iterations: int = 5) -> np.ndarray:
+        """nav_ba_undistort_points: radial-tangential keypoint undistortion (returns [n, 2])."""
+        Kd = np.ascontiguousarray(K, np.float64).reshape(4)
+        dd = np.ascontiguousarray(dist, np.float64).reshape(4)
+        uv = np.ascontiguousarray(uv, np.float64).reshape(-1, 2)
+        out = np.empty_like(uv)
+        self._check(self.L.nav_ba_undistort_points(self.h, _d(Kd), _d(dd), iterations, uv.shape[0], _d(uv), _d(out)))
+        return out
 
     def solve_batched(self, probs: list[abi.Problem], opt: abi.nav_ba_options) -> list[abi.Result]:
         n = len(probs)

@@ -155,6 +155,19 @@ class PoseProblem:
                        point_fixed=np.ones(n, np.uint8), camera_model=self.camera_model)
 
 
+class nav_ba_twoview(C.Structure):
+    _fields_ = [("n_matches", C.c_int32), ("n_hyp", C.c_int32), ("K", C.c_double * 4),
+                ("kp1", C.POINTER(C.c_double)), ("kp2", C.POINTER(C.c_double)), ("inlier", C.POINTER(C.c_uint8)),
+                ("R", C.POINTER(C.c_double)), ("t", C.POINTER(C.c_double)), ("th2", C.c_double),
+                ("min_parallax_cos", C.c_double), ("min_triangulated", C.c_int32), ("reserved", C.c_int32)]
+
+
+class nav_ba_twoview_result(C.Structure):
+    _fields_ = [("points", C.POINTER(C.c_double)), ("triangulated", C.POINTER(C.c_uint8)),
+                ("good", C.POINTER(C.c_uint8)), ("n_good", C.POINTER(C.c_int32)),
+                ("parallax_deg", C.POINTER(C.c_double))]
+
+
 VJP_MAX_STEPS = 64
 
 

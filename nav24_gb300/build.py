@@ -28,7 +28,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra"]
 
-PRODUCT_CU = ["nav_ba_api.cu", "window_engine.cu", "grid_engine.cu", "noalloc.cu", "pose_engine.cu"]
+PRODUCT_CU = ["nav_ba_api.cu", "window_engine.cu", "grid_engine.cu", "noalloc.cu", "pose_engine.cu", "twoview.cu", "undistort.cu"]
 PRODUCT_CPP = ["structure.cpp"]
 SYNTH_CPP = ["synth.cpp"]
 

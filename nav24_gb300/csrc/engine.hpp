@@ -201,6 +201,13 @@ struct PoseBatch {
 nav_ba_status solve_pose_batch(cudaStream_t stream, PoseBatch& B, const nav_ba_pose_problem* probs, int n,
                                const nav_ba_options& o, nav_ba_pose_result* res, float* ms, std::string* why);
 
+// Two-view triangulation and hypothesis checks (twoview.cu).
+nav_ba_status twoview_check(cudaStream_t stream, const nav_ba_twoview& in, nav_ba_twoview_result& out, std::string* why);
+
+// Keypoint undistortion (undistort.cu).
+nav_ba_status undistort_points(cudaStream_t stream, const double* K, const double* dist, int iters, int n,
+                               const double* uv_in, double* uv_out, std::string* why);
+
 // One-window solve in the library's static device array (no device allocation), noalloc.cu.
 nav_ba_status solve_window_noalloc(int device, cudaStream_t stream, const nav_ba_problem& p,
                                    const nav_ba_options& o, nav_ba_result& r, std::string* why);

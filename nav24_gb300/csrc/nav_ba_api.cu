@@ -674,6 +674,26 @@ nav_ba_status nav_ba_solve_pose_batched(nav_ba_ctx* ctx, const nav_ba_pose_probl
     return NAV_BA_OK;
 }
 
+nav_ba_status nav_ba_twoview_check(nav_ba_ctx* ctx, const nav_ba_twoview* in, nav_ba_twoview_result* out) {
+    if (!ctx) return NAV_BA_ERR_ARGUMENT;
+    if (!in || !out) return set_err(ctx, NAV_BA_ERR_ARGUMENT, "NULL argument");
+    cudaSetDevice(ctx->device);
+    std::string why;
+    const nav_ba_status st = twoview_check(ctx->stream, *in, *out, &why);
+    if (st != NAV_BA_OK) return set_err(ctx, st, why);
+    return NAV_BA_OK;
+}
+
+nav_ba_status nav_ba_undistort_points(nav_ba_ctx* ctx, const double* K, const double* dist, int32_t iterations,
+                                      int32_t n, const double* uv_in, double* uv_out) {
+    if (!ctx) return NAV_BA_ERR_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    std::string why;
+    const nav_ba_status st = undistort_points(ctx->stream, K, dist, iterations, n, uv_in, uv_out, &why);
+    if (st != NAV_BA_OK) return set_err(ctx, st, why);
+    return NAV_BA_OK;
+}
+
 nav_ba_status nav_ba_vjp(nav_ba_ctx* ctx, const nav_ba_problem* p, const nav_ba_options* o, nav_ba_schedule* sched,
                          const nav_ba_cotangent* cot, nav_ba_result* r, nav_ba_grads* grads) {
     if (!ctx) return NAV_BA_ERR_ARGUMENT;

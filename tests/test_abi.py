@@ -47,6 +47,8 @@ int main(void) {{
          offsetof(nav_ba_schedule, lambda), offsetof(nav_ba_grads, cam_tangent));
   printf("%zu %zu %zu %zu\\n", sizeof(nav_ba_pose_problem), sizeof(nav_ba_pose_result),
          offsetof(nav_ba_pose_problem, intrinsics), offsetof(nav_ba_pose_result, status));
+  printf("%zu %zu %zu\\n", sizeof(nav_ba_twoview), sizeof(nav_ba_twoview_result),
+         offsetof(nav_ba_twoview, min_triangulated));
   return 0;
 }}
 """)
@@ -61,7 +63,9 @@ int main(void) {{
             C.sizeof(abi.nav_ba_schedule), C.sizeof(abi.nav_ba_cotangent), C.sizeof(abi.nav_ba_grads),
             abi.nav_ba_schedule.lam.offset, abi.nav_ba_grads.cam_tangent.offset,
             C.sizeof(abi.nav_ba_pose_problem), C.sizeof(abi.nav_ba_pose_result),
-            abi.nav_ba_pose_problem.intrinsics.offset, abi.nav_ba_pose_result.status.offset]
+            abi.nav_ba_pose_problem.intrinsics.offset, abi.nav_ba_pose_result.status.offset,
+            C.sizeof(abi.nav_ba_twoview), C.sizeof(abi.nav_ba_twoview_result),
+            abi.nav_ba_twoview.min_triangulated.offset]
     assert got == want
 
 

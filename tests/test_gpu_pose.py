@@ -1,7 +1,7 @@
 """GPU parity of motion-only BA (nav_ba_solve_pose_batched: one free pose against fixed world
 points, nav24's EdgeSE3ProjectXYZOnlyPose) against the oracle solving the same problem as a general
 one (one free camera, every point fixed).  FP64: final cost within 1e-10 relative, pose within
-1e-9; mixed: final cost within 1e-6 of the FP64 oracle."""
+1e-8; mixed: final cost within 1e-6 of the FP64 oracle."""
 import numpy as np
 import pytest
 
@@ -34,7 +34,7 @@ def test_pose_fp64_matches_oracle(ctx, robust):
         # histories are compared where both ran every iteration
         if st["termination"] == abi.TERM_ITERATIONS and r.stats["termination"] == abi.TERM_ITERATIONS:
             assert st["trials_accepted"] == r.stats["trials_accepted"]
-        assert np.max(np.abs(pose - r.cam_pose[0])) < 1e-9
+        assert np.max(np.abs(pose - r.cam_pose[0])) < 1e-8
 
 
 def test_pose_mixed_matches_fp64_oracle(ctx):

@@ -381,3 +381,14 @@ def test_kb8_on_the_optical_axis():
     assert np.all(np.isfinite(jp)) and np.allclose(e, 0.0)
     _, _, jp_off, _ = oracle.linearize(mk([1e-6, 2e-6, 2.0]), abi.default_options())
     assert rel_err(jp_off, jp) < 1e-6
+
+
+def test_twoview_oracle_noise_free():
+    """The DLT restatement recovers exact points from noise-free matches under the true pose."""
+    from twoview_util import K, project, scene
+    from oracle import twoview
+    kp1, kp2, inl, Rs, ts, X = scene(n=200, seed=2)
+    kp1, kp2 = project(X), project(X @ Rs[0].T + ts[0])
+    pts, tri, good, ngood, par = twoview.check_rt(K, kp1, kp2, Rs[0], ts[0], 4.0, 0.99998, 50)
+    assert tri.all() and ngood == 200
+    assert np.max(np.abs(pts - X)) < 1e-9
