@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--workload", choices=["windows"], default="windows")
     ap.add_argument("--windows", type=int, default=512)
     ap.add_argument("--cpu-sample", type=int, default=512, help="windows in the CPU baseline sample")
-    ap.add_argument("--profile-case", choices=["mixed", "fp64", "grid", "pcg", "vjp"], default=None,
+    ap.add_argument("--profile-case", choices=["mixed", "fp64", "grid", "pcg", "vjp", "pose"], default=None,
                     help="run only the device-resident solves of one precision (mixed, fp64), or one solve of a "
                          "secondary workload (for profiler captures)")
     ap.add_argument("--no-secondary", action="store_true", help="skip the secondary workloads")
@@ -285,6 +285,21 @@ def secondary_workloads(ctx, only=None, pcg_cams=1000, pcg_points=500000):
             "forward_ms": (t1 - t0) * 1e3, "replay_and_backward_ms": (t2 - t1) * 1e3, "steps": len(lam),
             "forward_obs_per_s": r.stats["edge_iterations"] / (t1 - t0), "final_cost": r.stats["final_cost"],
             "timing": "wall clock of the C-ABI call (host graph build, upload, device work, download)"}
+    if only in (None, "pose"):
+        probs = Synth(2, n_windows=2048, seed=1102).pose_problems()
+        o = workload_options(2, abi.MIXED)
+        ctx.solve_pose_batched(probs, o)
+        nobs = sum(p.obs_uv.shape[0] for p in probs)
+        t0 = time.perf_counter()
+        res = ctx.solve_pose_batched(probs, o)
+        dt = time.perf_counter() - t0
+        its = sum(st["iterations_done"] for _, st in res)
+        out["tracking_pose_only"] = {
+            "workload": "2048 motion-only problems (the last keyframe of each family-2 window against its fixed "
+                        "points), 10 LM iterations, mixed form, one launch", "problems": len(probs),
+            "observations": nobs, "ms": dt * 1e3, "frames_per_s": len(probs) / dt,
+            "obs_per_s": sum(p.obs_uv.shape[0] * st["iterations_done"] for p, (_, st) in zip(probs, res)) / dt,
+            "lm_iterations": its, "timing": "wall clock of the C-ABI call (host layout, upload, kernel, download)"}
     if only in (None, "pcg"):
         p = Synth(4, n_cams=pcg_cams, n_points=pcg_points).window(0)
         out["figure_eight_pcg"] = {
@@ -313,7 +328,7 @@ def main():
     om = workload_options(2, abi.MIXED)
     of = workload_options(2, abi.FP64)
 
-    if args.profile_case in ("grid", "pcg", "vjp"):
+    if args.profile_case in ("grid", "pcg", "vjp", "pose"):
         print(json.dumps(secondary_workloads(ctx, args.profile_case, args.pcg_cams, args.pcg_points)), flush=True)
         ctx.close()
         dist.close()
@@ -356,6 +371,8 @@ def main():
     rr = call.results()
     e2e_ei = sum(r.stats["edge_iterations"] for r in rr)
     h2d, d2h = rr[0].stats["h2d_bytes"], rr[0].stats["d2h_bytes"]
+    e2e_split = {"host_setup_and_upload_ms": rr[0].stats["time_setup_ms"], "device_ms": rr[0].stats["time_solve_ms"],
+                 "download_ms": rr[0].stats["time_download_ms"]}
     dist.barrier()
     e2e_time = dist.max(float(np.mean(e2e_t)))
     e2e_value = dist.sum(float(e2e_ei)) / e2e_time
@@ -406,7 +423,7 @@ def main():
             "final_cost_rel_diff_max": cost_rel,
             "final_cost_rel_diff_vs_oracle_max": oracle_diff,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_time * 1e3},
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_time * 1e3, "last_call": e2e_split},
             "roofline": roofline,
             "cpu_baseline": cpu,
             "clocks": clocks,

@@ -164,22 +164,31 @@ nav_ba_status build_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, c
     if (st != NAV_BA_OK) return set_err(ctx, st, why);
     if (o->solver == NAV_BA_SOLVER_PCG && o->pcg_max_iterations < 1)
         return set_err(ctx, NAV_BA_ERR_ARGUMENT, "pcg_max_iterations < 1");
-    for (int i = 0; i < n; ++i) {
-        st = validate_problem(&probs[i], &why);
-        if (st != NAV_BA_OK) return set_err(ctx, st, "problem " + std::to_string(i) + ": " + why);
-        if (o->optimize_distortion && probs[i].camera_model == NAV_BA_CAM_PINHOLE_RADIAL &&
-            o->solver != NAV_BA_SOLVER_PCG)
-            return set_err(ctx, NAV_BA_ERR_UNSUPPORTED, "distortion optimization needs the PCG solver");
-        if (i > 0 && std::memcmp(probs[i].intrinsics, probs[0].intrinsics, sizeof(double) * 8) != 0)
-            return set_err(ctx, NAV_BA_ERR_UNSUPPORTED, "a batch shares one calibration");
-        if (i > 0 && probs[i].camera_model != probs[0].camera_model)
-            return set_err(ctx, NAV_BA_ERR_UNSUPPORTED, "a batch shares one camera model");
-    }
+    // validation and graph build of every problem spread over host threads; the first failing
+    // problem (lowest index) is reported, as a sequential pass would
     pb.host.assign(n, HostWindow());
     pb.host_status.assign(n, NAV_BA_OK);
+    std::vector<nav_ba_status> vst(n, NAV_BA_OK);
+    std::vector<std::string> vwhy(n);
     const int nth = std::max(1, std::min<int>(n / 8, (int)std::thread::hardware_concurrency()));
     auto work = [&](int t) {
         for (int i = t; i < n; i += nth) {
+            nav_ba_status s = validate_problem(&probs[i], &vwhy[i]);
+            if (s == NAV_BA_OK && o->optimize_distortion && probs[i].camera_model == NAV_BA_CAM_PINHOLE_RADIAL &&
+                o->solver != NAV_BA_SOLVER_PCG) {
+                s = NAV_BA_ERR_UNSUPPORTED;
+                vwhy[i] = "distortion optimization needs the PCG solver";
+            }
+            if (s == NAV_BA_OK && i > 0 && std::memcmp(probs[i].intrinsics, probs[0].intrinsics, sizeof(double) * 8) != 0) {
+                s = NAV_BA_ERR_UNSUPPORTED;
+                vwhy[i] = "a batch shares one calibration";
+            }
+            if (s == NAV_BA_OK && i > 0 && probs[i].camera_model != probs[0].camera_model) {
+                s = NAV_BA_ERR_UNSUPPORTED;
+                vwhy[i] = "a batch shares one camera model";
+            }
+            vst[i] = s;
+            if (s != NAV_BA_OK) continue;
             build_window(probs[i], *o, pb.host[i]);
             const HostWindow& h = pb.host[i];
             if (probs[i].n_cams == 0 || h.ne == 0) pb.host_status[i] = NAV_BA_EMPTY;
@@ -192,6 +201,8 @@ nav_ba_status build_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, c
         for (int t = 0; t < nth; ++t) ths.emplace_back(work, t);
         for (auto& th : ths) th.join();
     }
+    for (int i = 0; i < n; ++i)
+        if (vst[i] != NAV_BA_OK) return set_err(ctx, vst[i], "problem " + std::to_string(i) + ": " + vwhy[i]);
     for (int i = 0; i < n; ++i)
         if (pb.host_status[i] == NAV_BA_OK && (o->solver == NAV_BA_SOLVER_PCG || !fits_window_engine(pb.host[i])))
             pb.host_status[i] = kGridWindow;  // the window engine is Cholesky-only
