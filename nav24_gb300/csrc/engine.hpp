@@ -72,7 +72,7 @@ struct WindowBatch {
     double* d_x[2] = {nullptr, nullptr};  // [npt][4] current / trial points
     void* d_pt_vg = nullptr;       // [npt][12] Real: V (6 packed) g (3)
     void* d_pt_lt = nullptr;       // [npt][12] Real: Linv (6 packed lower) t = Linv g (3)
-    void* d_edge_w = nullptr;      // [ne][20 f32 | 18 f64] Real: W = w Jc^T Jp
+    void* d_edge_w = nullptr;      // FP64 form: [ne][18] W = w Jc^T Jp (the mixed form recomputes W)
     void* d_edge_a = nullptr;      // [ne][20 f32 | 18 f64] Real: A = W Linv^T
     void* d_edge_e[2] = {nullptr, nullptr};  // mixed: [ne][2] f32 residuals, current / trial state
     int32_t* d_cam_list = nullptr; // [ne] camera-major edge list (free cameras only)

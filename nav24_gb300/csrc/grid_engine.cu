@@ -5,10 +5,10 @@
 // Levenberg-Marquardt control (g2o OptimizationAlgorithmLevenberg::solve semantics, as in the
 // window engine) runs on the host, which reads the two reduced scalars of each damping trial
 // (cost and dx^T(lambda dx + b)) and decides.  Phases:
-//   lin_points    thread per point: e, J, Huber weight, V_p, g_p, W_e (shared with the window engine)
+//   lin_points    thread per point: e, J, Huber weight, V_p, g_p (shared with the window engine)
 //   lin_cameras   warp per chunk of <= 256 edges of one camera (camera-major list), U/g_c partial
 //                 sums reduced per camera in a fixed order (no atomics)
-//   schur_points  thread per point: chol(V + lambda I), L, t, A_e = W_e L^T (shared)
+//   schur_points  thread per point: chol(V + lambda I), L, t, A_e = W_e L^T with W_e recomputed (shared)
 //   schur_blocks  warp per nonzero 6x6 block of S over its pair list: S_ab = [a==b](U_a + lambda I)
 //                 - sum A_i A_j^T into a dense FP64 S; b'
 //   cholesky      one thread-block cluster, right-looking 32x32 tiles inside the envelope of S
@@ -141,9 +141,9 @@ __global__ void k_reduce_cams(const double* upart, const int32_t* item_off, int 
 }
 
 template <class Real>
-__global__ void k_schur_points(WinArgs<Real> A, WinDesc D, double lambda, double* part) {
+__global__ void k_schur_points(WinArgs<Real> A, WinDesc D, double lambda, const Real* camr, const double* X, double* part) {
     const CC c = grid_view();
-    block_partial<false>((double)schur_points<Real>(A, c, D, lambda), part);
+    block_partial<false>((double)schur_points<Real>(A, c, D, lambda, camr, X), part);
 }
 
 // Warp per nonzero block (a >= b) of S over its pair list; dense row-major S (m x m, lower part).
@@ -1129,7 +1129,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     double* d_x1 = dv.alloc<double>(4LL * np);
     Real* d_vg = dv.alloc<Real>(12LL * np);
     Real* d_lt = dv.alloc<Real>(12LL * np);
-    Real* d_w = dv.alloc<Real>(rec * ne);
+    Real* d_w = sizeof(Real) == 8 ? dv.alloc<Real>(rec * ne) : nullptr;  // FP64 form: stored W
     Real* d_a = dv.alloc<Real>(rec * ne);
     Real* d_camr0 = dv.alloc<Real>(12LL * nc);
     Real* d_camr1 = dv.alloc<Real>(12LL * nc);
@@ -1303,7 +1303,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             for (int k = 0; k < nval; ++k) outv[k] += hpart[(size_t)nval * bI + k];
     };
     const int iblocks = std::max(1, std::min(nsm_blocks, (n_items * 32 + TB - 1) / TB));
-    // linearization at state c: V_p, g_p, W_e (point-major), U_a, g_a (camera-major); the max
+    // linearization at state c: V_p, g_p (point-major), U_a, g_a (camera-major); the max
     // |diag| of the point and camera blocks (g2o's initial damping)
     auto linearize = [&](int c, double& mxp, double& mxc) {
         k_lin_points<Real><<<pblocks, TB, 0, st>>>(A, D, camr[c], A.x[c], d_part);
@@ -1372,7 +1372,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             save_state(cur, s);
             double mxp, mxc;
             linearize(cur, mxp, mxc);
-            k_schur_points<Real><<<pblocks, TB, 0, st>>>(A, D, lam, d_part);
+            k_schur_points<Real><<<pblocks, TB, 0, st>>>(A, D, lam, camr[cur], A.x[cur], d_part);
             bool ok = sum_part(pblocks, false) == 0.0;
             if (nfc > 0) {
                 assemble_S(lam);
@@ -1424,7 +1424,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         int q = 0;
         do {
             const double lam_use = (debug_S && it == 0 && q == 0) ? debug_lambda : lambda;
-            k_schur_points<Real><<<pblocks, TB, 0, st>>>(A, D, lam_use, d_part);
+            k_schur_points<Real><<<pblocks, TB, 0, st>>>(A, D, lam_use, camr[cur], A.x[cur], d_part);
             const double npd = sum_part(pblocks, false);
             bool ok = npd == 0.0;
             double dk[2] = {0.0, 0.0};
@@ -1629,7 +1629,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                 k_cams_real<double><<<cblocks, TB, 0, st>>>(cams[0], nc, camr[0]);
                 double mxp, mxc;
                 linearize(0, mxp, mxc);
-                k_schur_points<double><<<pblocks, TB, 0, st>>>(A, D, lam, d_part);
+                k_schur_points<double><<<pblocks, TB, 0, st>>>(A, D, lam, camr[0], A.x[0], d_part);
                 bool ok = sum_part(pblocks, false) == 0.0;
                 if (nfc > 0) {
                     assemble_S(lam);

@@ -30,7 +30,7 @@ struct WinArgs {
     double* x[2];
     Real* pt_vg;
     Real* pt_lt;
-    Real* edge_w;
+    Real* edge_w;             // FP64 form: W_e = w J_c^T J_p per edge; null: recomputed (mixed form)
     Real* edge_a;
     Real* edge_e[2];          // mixed form: residual (u, v) of each edge at the current / trial state
     int32_t* cam_list;
@@ -178,7 +178,7 @@ __device__ double cost_partial(const WinArgs<Real>& A, const CC& c, const WinDes
     return acc;
 }
 
-// Point-major linearization: V_p, g_p, W_e; returns this thread's max |diag V|.
+// Point-major linearization: V_p, g_p and, when edge_w is set, W_e; returns this thread's max |diag V|.
 template <class Real>
 __device__ double linearize_points(const WinArgs<Real>& A, const CC& c, const WinDesc& D, const Real* camr,
                                    const double* X) {
@@ -208,7 +208,7 @@ __device__ double linearize_points(const WinArgs<Real>& A, const CC& c, const Wi
             g[0] += jp[0] * we0 + jp[3] * we1;
             g[1] += jp[1] * we0 + jp[4] * we1;
             g[2] += jp[2] * we0 + jp[5] * we1;
-            if (A.edge_fc[e] >= 0) {
+            if (A.edge_w && A.edge_fc[e] >= 0) {
                 Real W[18];
 #pragma unroll
                 for (int r = 0; r < 6; ++r)
@@ -224,11 +224,16 @@ __device__ double linearize_points(const WinArgs<Real>& A, const CC& c, const Wi
     return mx;
 }
 
-// Per free point: R R^T = V + lambda I, L = R^-1, t = L g, A_e = W_e L^T.  Returns the number of
-// points whose damped block was not positive definite (treated like a failed factorization).
+// Per free point: R R^T = V + lambda I, L = R^-1, t = L g, A_e = W_e L^T.  W_e = w J_c^T J_p is read
+// from edge_w (FP64 form, where recomputing costs FP64-pipe time) or recomputed from the edge's
+// Jacobians at the current state (mixed form: camr, X are the state the point blocks were
+// linearized at, the same arithmetic gives the same W, and no per-edge record round-trips through
+// memory).  Returns the number of points whose damped block was not positive definite.
 template <class Real>
-__device__ int schur_points(const WinArgs<Real>& A, const CC& c, const WinDesc& D, double lambda) {
+__device__ int schur_points(const WinArgs<Real>& A, const CC& c, const WinDesc& D, double lambda, const Real* camr,
+                            const double* X) {
     const Real lam = (Real)lambda;
+    const Real delta = (Real)A.lm.huber_delta;
     int bad = 0;
     for (int p = c.gt; p < D.npt; p += c.CT) {
         const int gp = D.pt0 + p;
@@ -251,11 +256,24 @@ __device__ int schur_points(const WinArgs<Real>& A, const CC& c, const WinDesc& 
         const Real ltv[12] = {l00, l10, l11, l20, l21, l22, l00 * vg[6], l10 * vg[6] + l11 * vg[7],
                               l20 * vg[6] + l21 * vg[7] + l22 * vg[8], Real(0), Real(0), Real(0)};
         Rec<Real>::store12(A.pt_lt + 12LL * gp, ltv);
+        const Real Xr[3] = {(Real)X[4LL * gp], (Real)X[4LL * gp + 1], (Real)X[4LL * gp + 2]};
         const int e1 = A.pt_eoff[gp + 1];
         for (int e = A.pt_eoff[gp]; e < e1; ++e) {
             if (A.edge_fc[e] < 0) continue;
-            Real W[18], Ae[18];
-            Rec<Real>::load18(A.edge_w + (long long)Rec<Real>::kEdge * e, W);
+            Real W[18];
+            if (A.edge_w) {
+                Rec<Real>::load18(A.edge_w + (long long)Rec<Real>::kEdge * e, W);
+            } else {
+                const Real* cr = camr + 12 * A.edge_cam[e];
+                const Real z[2] = {(Real)A.edge_uv[2LL * e], (Real)A.edge_uv[2LL * e + 1]};
+                EdgeLin<Real> L;
+                edge_linearize<Real>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta, L);
+#pragma unroll
+                for (int r = 0; r < 6; ++r)
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) W[r * 3 + k] = L.w * (L.jc[r] * L.jp[k] + L.jc[6 + r] * L.jp[3 + k]);
+            }
+            Real Ae[18];
 #pragma unroll
             for (int r = 0; r < 6; ++r) {
                 const Real w0 = W[r * 3 + 0], w1 = W[r * 3 + 1], w2 = W[r * 3 + 2];

@@ -350,6 +350,7 @@ nav_ba_status solve_impl(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, co
     PreparedBatch pb;
     nav_ba_status st = build_batch(ctx, probs, n, o, pb);
     if (st != NAV_BA_OK) return st;
+    const double t_build = ms_since(t0);
     std::string why;
     std::swap(pb.dev, ctx->solve_dev);  // reuse the context's device buffers
     struct SwapBack {
@@ -378,6 +379,10 @@ nav_ba_status solve_impl(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, co
         if (st != NAV_BA_OK) return st;
     }
     const double t_down = ms_since(t1);
+    const char* verbose = getenv("NAVBA_VERBOSE");
+    if (verbose && verbose[0] == '1')
+        fprintf(stderr, "[navba host] %d problems: build %.2f ms, stage+upload %.2f ms, device %.2f ms, download %.2f ms\n", n,
+                t_build, t_setup - t_build, t_solve, t_down);
     for (int i = 0; i < n; ++i) {
         tmp[i].time_setup_ms = t_setup;
         tmp[i].time_solve_ms += t_solve;  // grid-engine problems already hold their own solve time

@@ -102,7 +102,7 @@ nav_ba_status solve_window_noalloc(int device, cudaStream_t stream, const nav_ba
     const size_t o_ept = carve(sizeof(int32_t) * ne), o_euv = carve(sizeof(double) * 2 * ne);
     const size_t o_x0 = carve(sizeof(double) * 4 * np), o_x1 = carve(sizeof(double) * 4 * np);
     const size_t o_vg = carve(rs * 12 * np), o_lt = carve(rs * 12 * np);
-    const size_t o_w = carve(rs * rec * ne), o_a = carve(rs * rec * ne);
+    const size_t o_w = carve(o.precision == NAV_BA_MIXED ? 16 : rs * rec * ne), o_a = carve(rs * rec * ne);
     const size_t eb = o.precision == NAV_BA_MIXED ? rs * 2 * ne : 16;
     const size_t o_e0 = carve(eb), o_e1 = carve(eb);
     const size_t o_list = carve(sizeof(int32_t) * ne), o_pairs = carve(sizeof(uint32_t) * npair);

@@ -97,48 +97,32 @@ void build_window(const nav_ba_problem& p, const nav_ba_options& o, HostWindow& 
     w.pt.assign(4LL * w.npt, 0.0);
     for (int i = 0; i < w.npt; ++i)
         for (int k = 0; k < 3; ++k) w.pt[4LL * i + k] = p.points[3LL * i + k];
-    w.n_schur_blocks = count_schur_blocks(w);
+    // Schur pairs (same free point, free cameras, b <= a) and the distinct lower blocks they touch,
+    // in one pass over each point's free-camera edges
     w.n_pairs = 0;
-    for (int i = 0; i < w.npt; ++i) {
-        if (w.pt_free[i] < 0) continue;
-        for (int e = w.pt_eoff[i]; e < w.pt_eoff[i + 1]; ++e) {
-            const int a = w.cam_free[w.edge_cam[e]];
-            if (a < 0) continue;
-            for (int f = w.pt_eoff[i]; f < w.pt_eoff[i + 1]; ++f) {
-                const int b = w.cam_free[w.edge_cam[f]];
-                if (b >= 0 && b <= a) ++w.n_pairs;
+    w.n_schur_blocks = w.nfc;  // the diagonal blocks
+    if (w.nfc > 0) {
+        std::vector<uint8_t> seen((size_t)w.nfc * w.nfc, 0);
+        std::vector<int32_t> fc;
+        for (int i = 0; i < w.npt; ++i) {
+            if (w.pt_free[i] < 0) continue;
+            fc.clear();
+            for (int e = w.pt_eoff[i]; e < w.pt_eoff[i + 1]; ++e) {
+                const int a = w.cam_free[w.edge_cam[e]];
+                if (a >= 0) fc.push_back(a);
             }
-        }
-    }
-}
-
-int32_t count_schur_blocks(const HostWindow& w) {
-    if (w.nfc == 0) return 0;
-    // bitset of co-visible free-camera pairs (b <= a)
-    std::vector<uint8_t> seen((size_t)w.nfc * w.nfc, 0);
-    std::vector<int32_t> fc;
-    int32_t n = 0;
-    for (int a = 0; a < w.nfc; ++a) {
-        seen[(size_t)a * w.nfc + a] = 1;
-        ++n;
-    }
-    for (int i = 0; i < w.npt; ++i) {
-        if (w.pt_free[i] < 0) continue;
-        fc.clear();
-        for (int e = w.pt_eoff[i]; e < w.pt_eoff[i + 1]; ++e) {
-            const int a = w.cam_free[w.edge_cam[e]];
-            if (a >= 0) fc.push_back(a);
-        }
-        for (size_t x = 0; x < fc.size(); ++x)
-            for (size_t y = 0; y < fc.size(); ++y) {
-                const int a = fc[x], b = fc[y];
-                if (b < a && !seen[(size_t)a * w.nfc + b]) {
-                    seen[(size_t)a * w.nfc + b] = 1;
-                    ++n;
+            for (size_t x = 0; x < fc.size(); ++x)
+                for (size_t y = 0; y < fc.size(); ++y) {
+                    const int a = fc[x], b = fc[y];
+                    if (b > a) continue;
+                    ++w.n_pairs;
+                    if (b < a && !seen[(size_t)a * w.nfc + b]) {
+                        seen[(size_t)a * w.nfc + b] = 1;
+                        ++w.n_schur_blocks;
+                    }
                 }
-            }
+        }
     }
-    return n;
 }
 
 }  // namespace navba

@@ -46,7 +46,4 @@ nav_ba_status validate_options(const nav_ba_options* o, std::string* why);
 // Build the device layout of one problem (assumes validate_problem passed).
 void build_window(const nav_ba_problem& p, const nav_ba_options& o, HostWindow& w);
 
-// Count the lower-triangle 6x6 blocks of the reduced camera system (diagonal included).
-int32_t count_schur_blocks(const HostWindow& w);
-
 }  // namespace navba

@@ -13,16 +13,18 @@
 // GraphOptim::solve, core/backEnd/BE_GraphOptim.cpp:67-68):
 //   linearize  point-major, thread per point: residual, pose/point Jacobians and Huber weight per
 //              edge (EdgeSE3ProjectXYZ::computeError/linearizeOplus, OptimizableTypes.hpp:102-107,
-//              OptimizableTypes.cpp:140-161); V_p, g_p; W_e = w Jc^T Jp stored per edge.
+//              OptimizableTypes.cpp:140-161); V_p, g_p; the FP64 form stores W_e = w Jc^T Jp.
 //              camera-major, warp per camera: the edges are re-linearized and U_c, g_c summed by
 //              warp shuffles (nothing per edge is stored for them).
-//   trial      point-major: V_p + lambda I = R R^T (3x3 Cholesky), L = R^-1, A_e = W_e L^T,
-//              t_p = L g_p, so that W V^-1 W^T = A A^T and W V^-1 g = A t.
+//   trial      point-major: V_p + lambda I = R R^T (3x3 Cholesky), L = R^-1, A_e = W_e L^T (the
+//              mixed form recomputes W_e from the edge's Jacobians), t_p = L g_p, so that
+//              W V^-1 W^T = A A^T and W V^-1 g = A t.
 //              warp per 6x6 block of S over the block's pair list (built once per window,
 //              deterministic order): S_ab = [a==b](U_a + lambda I) - sum A_i A_j^T, summed in
 //              registers and reduced by shuffles, no atomics; b'_a = g_a - sum A_i t_p.
 //              FP64 Cholesky of S (rank 0); dx_p = L^T (t_p - sum A_i^T dx_c); T <- exp(dx) T;
-//              cost of the trial state; gain ratio, accept/reject and damping update.
+//              cost of the trial state (mixed form: FP32 residual changes, fused with the point
+//              update); gain ratio, accept/reject and damping update.
 // Real is double (plain FP64 form) or float (mixed form: residuals, Jacobians, H blocks and the
 // Schur products in FP32; S, its Cholesky, the states, the SE(3) update and cost sums in FP64).
 #include <algorithm>
@@ -509,7 +511,7 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
                 const double lam_use = (A.debug && it == 0 && q == 0) ? A.debug_lambda : lambda;
                 if (c.rank == 0)
                     for (int k = threadIdx.x; k < m * (m + 1) / 2; k += blockDim.x) S[k] = 0.0;
-                const int npd = schur_points<Real>(A, c, D, lam_use);
+                const int npd = schur_points<Real>(A, c, D, lam_use, cr_cur, A.x[cur]);
                 const double3 r0 = cluster_reduce3<false>(c, (double)npd, 0.0, 0.0);  // also orders S zeroing
                 pc.mark(4);
                 schur_blocks<Real>(A, c, D, lam_use);
@@ -697,7 +699,7 @@ cudaError_t launch_typed(PreparedBatch& pb, cudaStream_t stream, WindowLaunch sh
     A.x[1] = b.d_x[1];
     A.pt_vg = (Real*)b.d_pt_vg;
     A.pt_lt = (Real*)b.d_pt_lt;
-    A.edge_w = (Real*)b.d_edge_w;
+    A.edge_w = sizeof(Real) == 8 ? (Real*)b.d_edge_w : nullptr;
     A.edge_a = (Real*)b.d_edge_a;
     A.edge_e[0] = sizeof(Real) == 4 ? (Real*)b.d_edge_e[0] : nullptr;
     A.edge_e[1] = sizeof(Real) == 4 ? (Real*)b.d_edge_e[1] : nullptr;
@@ -969,7 +971,7 @@ cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int prec
     ensure(&b.d_pt_vg, rs * 12 * np);
     ensure(&b.d_pt_lt, rs * 12 * np);
     const size_t rec = precision == NAV_BA_MIXED ? 20 : 18;  // per-edge record stride (Reals)
-    ensure(&b.d_edge_w, rs * rec * ne);
+    ensure(&b.d_edge_w, precision == NAV_BA_MIXED ? 16 : rs * rec * ne);  // FP64 form only
     ensure(&b.d_edge_a, rs * rec * ne);
     ensure(&b.d_edge_e[0], precision == NAV_BA_MIXED ? rs * 2 * ne : 16);
     ensure(&b.d_edge_e[1], precision == NAV_BA_MIXED ? rs * 2 * ne : 16);
