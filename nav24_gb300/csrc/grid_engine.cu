@@ -21,6 +21,9 @@
 // is replayed) and the backward pass of vjp_device.cuh runs over the taped steps, last first.
 #include <algorithm>
 #include <cfloat>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <type_traits>
@@ -207,133 +210,153 @@ __global__ void k_schur_blocks(WinArgs<Real> A, const int2* blocks, const int32_
     }
 }
 
-// ---- FP64 tiled Cholesky inside the envelope (one thread-block cluster) ------------------
-
-__device__ __forceinline__ void gsync() { cg::this_cluster().sync(); }
+// ---- FP64 tiled Cholesky inside the envelope -------------------------------------------
 
 // tfirst[I]: first tile column of tile row I that may be nonzero (the envelope, at tile level).
-__global__ void k_cholesky(double* S, int m, const int32_t* tfirst, double* rinv, int32_t* ok) {
+// FP64 Cholesky of the envelope over the whole GPU (cooperative launch, every block resident).
+// Per tile column K: each block owning a panel tile (tile row I > K whose envelope reaches K)
+// factors the diagonal tile L_KK in its own shared memory (block 0 also stores it and 1/L_jj), then
+// solves its panel tiles L_IK = A_IK L_KK^-T; after a grid synchronization block 0 stores L_KK and the
+// trailing tiles
+// (I, J), K < J <= I inside the envelope, are updated A_IJ -= L_IK L_JK^T in quarter-tile work items
+// (8 rows x 32 columns, one output per thread) spread over all blocks; a grid synchronization ends
+// the column.  Every block runs the same loops, so all reach every synchronization; a non-positive
+// pivot is replaced by 1 and reported through ok.
+__device__ void factor_diag_tile(double (*tk)[kTile + 1], double* rv, const double* S, int m, int k0, int kb, int& bad) {
+    const int tid = threadIdx.x, nth = blockDim.x;
+    for (int idx = tid; idx < kTile * kTile; idx += nth) {
+        const int i = idx / kTile, j = idx % kTile;
+        tk[i][j] = (i < kb && j <= i) ? S[(size_t)(k0 + i) * m + k0 + j] : 0.0;
+    }
+    __syncthreads();
+    for (int j = 0; j < kb; ++j) {
+        if (tid == 0) {
+            const double d = tk[j][j];
+            double r;
+            if (!(d > 0.0) || !isfinite(d)) {
+                bad = 1;
+                r = 1.0;
+                tk[j][j] = 1.0;
+            } else {
+                r = rsqrt(d);
+                tk[j][j] = d * r;
+            }
+            rv[j] = r;
+        }
+        __syncthreads();
+        for (int i = j + 1 + tid; i < kb; i += nth) tk[i][j] *= rv[j];
+        __syncthreads();
+        const int w = kb - j - 1;
+        for (int idx = tid; idx < w * w; idx += nth) {
+            const int i = j + 1 + idx / w, l = j + 1 + idx % w;
+            if (l <= i) tk[i][l] -= tk[i][j] * tk[l][j];
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(256) k_cholesky_coop(double* S, int m, const int32_t* tfirst, double* rinv,
+                                                       int32_t* ok) {
+    cg::grid_group grid = cg::this_grid();
     __shared__ double tk[kTile][kTile + 1];
     __shared__ double ta[kTile][kTile + 1];
     __shared__ double tb[kTile][kTile + 1];
     __shared__ double rv[kTile];
-    __shared__ int sok;
-    cg::cluster_group cl = cg::this_cluster();
-    const int rank = (int)cl.block_rank(), cs = (int)cl.num_blocks();
-    const int tid = threadIdx.x, nth = blockDim.x;
+    __shared__ int sbad;
+    const int tid = threadIdx.x, nth = blockDim.x, nb = gridDim.x, bid = blockIdx.x;
     const int nt = (m + kTile - 1) / kTile;
-    if (tid == 0) sok = 1;
+    if (tid == 0) sbad = 0;
     __syncthreads();
     for (int K = 0; K < nt; ++K) {
         const int k0 = K * kTile, kb = min(kTile, m - k0);
-        if (rank == 0) {
-            for (int idx = tid; idx < kTile * kTile; idx += nth) {
-                const int i = idx / kTile, j = idx % kTile;
-                tk[i][j] = (i < kb && j <= i) ? S[(size_t)(k0 + i) * m + k0 + j] : 0.0;
-            }
-            __syncthreads();
-            for (int j = 0; j < kb; ++j) {
-                if (tid == 0) {
-                    const double d = tk[j][j];
-                    double r;
-                    if (!(d > 0.0) || !isfinite(d)) {
-                        sok = 0;
-                        r = 1.0;
-                        tk[j][j] = 1.0;
-                    } else {
-                        r = rsqrt(d);
-                        tk[j][j] = d * r;
+        int npan = 0;
+        for (int I = K + 1; I < nt; ++I) npan += tfirst[I] <= K;
+        if (bid == 0 || bid < npan) {
+            factor_diag_tile(tk, rv, S, m, k0, kb, sbad);
+            // this block's panel tiles: the (bid + c nb)-th tile rows below K inside the envelope
+            int pidx = 0;
+            for (int I = K + 1; I < nt; ++I) {
+                if (tfirst[I] > K) continue;
+                if ((pidx++ % nb) != bid) continue;
+                const int i0 = I * kTile, ib = min(kTile, m - i0);
+                __syncthreads();
+                for (int idx = tid; idx < kTile * kTile; idx += nth) {
+                    const int i = idx / kTile, j = idx % kTile;
+                    ta[i][j] = (i < ib && j < kb) ? S[(size_t)(i0 + i) * m + k0 + j] : 0.0;
+                }
+                __syncthreads();
+                if (tid < ib) {
+                    // x_c = (a_c - sum_{j<c} x_j L_cj) / L_cc; the sum in four independent partial sums
+                    for (int cc = 0; cc < kb; ++cc) {
+                        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+                        int j = 0;
+                        for (; j + 3 < cc; j += 4) {
+                            s0 += ta[tid][j] * tk[cc][j];
+                            s1 += ta[tid][j + 1] * tk[cc][j + 1];
+                            s2 += ta[tid][j + 2] * tk[cc][j + 2];
+                            s3 += ta[tid][j + 3] * tk[cc][j + 3];
+                        }
+                        for (; j < cc; ++j) s0 += ta[tid][j] * tk[cc][j];
+                        ta[tid][cc] = (ta[tid][cc] - ((s0 + s1) + (s2 + s3))) * rv[cc];
                     }
-                    rv[j] = r;
-                    rinv[k0 + j] = r;
                 }
                 __syncthreads();
-                for (int i = j + 1 + tid; i < kb; i += nth) tk[i][j] *= rv[j];
-                __syncthreads();
-                const int w = kb - j - 1;
-                for (int idx = tid; idx < w * w; idx += nth) {
-                    const int i = j + 1 + idx / w, l = j + 1 + idx % w;
-                    if (l <= i) tk[i][l] -= tk[i][j] * tk[l][j];
+                for (int idx = tid; idx < ib * kb; idx += nth) {
+                    const int i = idx / kb, j = idx % kb;
+                    S[(size_t)(i0 + i) * m + k0 + j] = ta[i][j];
                 }
-                __syncthreads();
             }
+        }
+        grid.sync();
+        // block 0 stores L_KK now that every block has read A_KK (the trailing tiles do not touch it)
+        if (bid == 0) {
             for (int idx = tid; idx < kb * kb; idx += nth) {
                 const int i = idx / kb, j = idx % kb;
                 if (j <= i) S[(size_t)(k0 + i) * m + k0 + j] = tk[i][j];
             }
-            if (tid == 0 && !sok) ok[0] = 0;
+            for (int j = tid; j < kb; j += nth) rinv[k0 + j] = rv[j];
         }
-        gsync();
-        // panel: L_IK = A_IK L_KK^-T for the tile rows below whose envelope reaches column K
-        int cnt = 0;
-        bool loaded = false;
-        for (int I = K + 1; I < nt; ++I) {
-            if (tfirst[I] > K) continue;
-            if ((cnt++ % cs) != rank) continue;
-            if (!loaded) {
-                for (int idx = tid; idx < kTile * kTile; idx += nth) {
-                    const int i = idx / kTile, j = idx % kTile;
-                    tk[i][j] = (i < kb && j <= i) ? S[(size_t)(k0 + i) * m + k0 + j] : 0.0;
-                }
-                for (int j = tid; j < kb; j += nth) rv[j] = rinv[k0 + j];
-                loaded = true;
-            }
-            const int i0 = I * kTile, ib = min(kTile, m - i0);
-            __syncthreads();
-            for (int idx = tid; idx < kTile * kTile; idx += nth) {
-                const int i = idx / kTile, j = idx % kTile;
-                ta[i][j] = (i < ib && j < kb) ? S[(size_t)(i0 + i) * m + k0 + j] : 0.0;
-            }
-            __syncthreads();
-            // forward substitution, row-parallel: x_c = (a_c - sum_{j<c} x_j L_cj) / L_cc
-            if (tid < ib) {
-                for (int cc = 0; cc < kb; ++cc) {
-                    double x = ta[tid][cc];
-                    for (int j = 0; j < cc; ++j) x -= ta[tid][j] * tk[cc][j];
-                    ta[tid][cc] = x * rv[cc];
-                }
-            }
-            __syncthreads();
-            for (int idx = tid; idx < ib * kb; idx += nth) {
-                const int i = idx / kb, j = idx % kb;
-                S[(size_t)(i0 + i) * m + k0 + j] = ta[i][j];
-            }
-            __syncthreads();
-        }
-        gsync();
-        // trailing update A_IJ -= L_IK L_JK^T for K < J <= I inside the envelope
-        cnt = 0;
+        // trailing update in quarter-tile work items
+        int widx = 0;
         for (int I = K + 1; I < nt; ++I) {
             if (tfirst[I] > K) continue;
             const int i0 = I * kTile, ib = min(kTile, m - i0);
             for (int J = K + 1; J <= I; ++J) {
                 if (tfirst[J] > K) continue;
-                if ((cnt++ % cs) != rank) continue;
                 const int j0 = J * kTile, jb = min(kTile, m - j0);
-                __syncthreads();
-                for (int idx = tid; idx < kTile * kTile; idx += nth) {
-                    const int i = idx / kTile, j = idx % kTile;
-                    ta[i][j] = (i < ib && j < kb) ? S[(size_t)(i0 + i) * m + k0 + j] : 0.0;
-                    tb[i][j] = (i < jb && j < kb) ? S[(size_t)(j0 + i) * m + k0 + j] : 0.0;
-                }
-                __syncthreads();
-                for (int idx = tid; idx < ib * jb; idx += nth) {
-                    const int i = idx / jb, j = idx % jb;
-                    if (I == J && j > i) continue;
-                    double s = 0.0;
+                for (int q = 0; q < 4; ++q) {
+                    if ((widx++ % nb) != bid) continue;
+                    const int r0 = 8 * q;
+                    if (r0 >= ib) continue;  // uniform per block
+                    __syncthreads();
+                    for (int idx = tid; idx < kTile * kTile; idx += nth) {
+                        const int i = idx / kTile, j = idx % kTile;
+                        tb[i][j] = (i < jb && j < kb) ? S[(size_t)(j0 + i) * m + k0 + j] : 0.0;
+                        if (i < 8) ta[i][j] = (r0 + i < ib && j < kb) ? S[(size_t)(i0 + r0 + i) * m + k0 + j] : 0.0;
+                    }
+                    __syncthreads();
+                    const int r = tid / kTile, c = tid % kTile;  // 256 threads: 8 rows x 32 columns
+                    if (r < 8 && r0 + r < ib && c < jb && !(I == J && c > r0 + r)) {
+                        double sum = 0.0;
 #pragma unroll 8
-                    for (int t = 0; t < kTile; ++t) s += ta[i][t] * tb[j][t];
-                    S[(size_t)(i0 + i) * m + j0 + j] -= s;
+                        for (int t = 0; t < kTile; ++t) sum += ta[r][t] * tb[c][t];
+                        S[(size_t)(i0 + r0 + r) * m + j0 + c] -= sum;
+                    }
                 }
             }
         }
-        gsync();
+        grid.sync();
     }
+    if (tid == 0 && sbad) ok[0] = 0;
 }
 
-// Solve L L^T x = b in place (one CTA), tile-blocked, inside the envelope.
+// Solve L L^T x = b in place (one CTA), tile-blocked, inside the envelope.  Per tile column K:
+// warp 0 solves the diagonal tile; the rows below (those whose tile row reaches column K) are
+// spread over the warps with the lanes over the tile's columns, so every load of L is a
+// contiguous 256-byte row segment; sums are shuffle trees and a fixed-order sum over warps.
 __global__ void k_chol_solve(const double* L, int m, const int32_t* tfirst, const double* rinv, double* x) {
-    const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31;
+    __shared__ double red[32][kTile];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
     const int nt = (m + kTile - 1) / kTile;
     // forward: L y = b
     for (int K = 0; K < nt; ++K) {
@@ -348,29 +371,31 @@ __global__ void k_chol_solve(const double* L, int m, const int32_t* tfirst, cons
             if (lane < kb) x[k0 + lane] = v;
         }
         __syncthreads();
-        for (int r = k0 + kb + tid; r < m; r += nth) {
-            if (tfirst[r / kTile] > K) continue;
-            double s = 0.0;
-            const double* Lr = L + (size_t)r * m + k0;
-            for (int j = 0; j < kb; ++j) s += Lr[j] * x[k0 + j];
-            x[r] -= s;
+        const double xk = lane < kb ? x[k0 + lane] : 0.0;
+        for (int r = k0 + kb + wid; r < m; r += nw) {
+            if (tfirst[r / kTile] > K) continue;  // uniform per warp
+            double s = lane < kb ? L[(size_t)r * m + k0 + lane] * xk : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(kFullG, s, o);
+            if (lane == 0) x[r] -= s;
         }
         __syncthreads();
     }
     // backward: L^T x = y
     for (int K = nt - 1; K >= 0; --K) {
         const int k0 = K * kTile, kb = min(kTile, m - k0);
-        // x_K -= sum over rows below of L_rK x_r (rows r > tile K whose envelope reaches K)
-        for (int j = tid; j < kb; j += nth) {
+        // x_K -= sum over the rows below of L_rK x_r (rows whose tile row reaches column K)
+        double acc = 0.0;
+        for (int r = k0 + kb + wid; r < m; r += nw) {
+            if (tfirst[r / kTile] > K) continue;
+            if (lane < kb) acc += L[(size_t)r * m + k0 + lane] * x[r];
+        }
+        red[wid][lane] = acc;
+        __syncthreads();
+        if (tid < kb) {
             double s = 0.0;
-            for (int r = k0 + kb; r < m; ++r) {
-                if (tfirst[r / kTile] > K) {
-                    r = (r / kTile + 1) * kTile - 1;
-                    continue;
-                }
-                s += L[(size_t)r * m + k0 + j] * x[r];
-            }
-            x[k0 + j] -= s;
+            for (int w = 0; w < nw; ++w) s += red[w][tid];
+            x[k0 + tid] -= s;
         }
         __syncthreads();
         if (tid < 32) {
@@ -1107,8 +1132,13 @@ template <class Real>
 cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Intr& intr, cudaStream_t st,
                              int cluster, GridResult& out, double debug_lambda, std::vector<double>* debug_S,
                              GridVjp* vjp) {
+    const auto tg0 = std::chrono::steady_clock::now();
+    auto ms_from = [](std::chrono::steady_clock::time_point a) {
+        return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
+    };
     GridHost g;
     build_grid_host(h, g);
+    const double t_host = ms_from(tg0);
     const int nc = h.ncam, np = h.npt, ne = h.ne, nfc = h.nfc;
     const int m = 6 * nfc;
     GridDev dv;
@@ -1290,6 +1320,21 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     k_cams_real<Real><<<cblocks, TB, 0, st>>>(d_cams0, nc, d_camr0);
     k_cams_real<Real><<<cblocks, TB, 0, st>>>(d_cams0, nc, d_camr1);
     chk(cudaGetLastError());
+    chk(cudaStreamSynchronize(st));
+    const double t_setup = ms_from(tg0);
+    struct LoopTimer {
+        std::chrono::steady_clock::time_point t0;
+        double host, setup;
+        double (*ms)(std::chrono::steady_clock::time_point);
+        ~LoopTimer() {
+            const char* v = getenv("NAVBA_VERBOSE");
+            if (v && v[0] == '1')
+                fprintf(stderr, "[navba grid] host structure %.2f ms, allocation + upload %.2f ms, LM loop %.2f ms\n", host,
+                        setup - host, ms(t0));
+        }
+    } loop_timer{std::chrono::steady_clock::now(), t_host, t_setup, +[](std::chrono::steady_clock::time_point a) {
+                     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
+                 }};
     int cur = 0;
     // costs (initial, every trial) are evaluated in FP64 in both forms: they drive the gain ratio
     double chi = cost_of(0, true);
@@ -1323,23 +1368,26 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             A, d_blocks, d_boff, (int)(g.boff.size() - 1), d_pairs, d_U, lam, d_S, m, d_bs);
         chk(cudaGetLastError());
     };
-    int cl = std::max(1, std::min(8, cluster));
-    // Cholesky of S in place (one thread-block cluster); false if S is not positive definite
+    (void)cluster;
+    // Cholesky of S in place (cooperative, whole GPU); false if S is not positive definite
+    int chol_grid = 1;
+    {
+        int dev = 0, nsm = 0, bps = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_cholesky_coop, 256, 0);
+        chol_grid = std::max(1, nsm * std::max(1, std::min(bps, 2)));
+    }
     auto factor_S = [&]() -> bool {
         const int32_t one = 1;
         chk(cudaMemcpyAsync(d_ok, &one, sizeof(int32_t), cudaMemcpyHostToDevice, st));
-        cudaLaunchConfig_t cfg = {};
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = cl;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        cfg.gridDim = dim3(cl);
-        cfg.blockDim = dim3(256);
-        cfg.stream = st;
-        chk(cudaLaunchKernelEx(&cfg, k_cholesky, d_S, m, (const int32_t*)d_tfirst, d_rinv, d_ok));
+        double* Sp = d_S;
+        int mm = m;
+        const int32_t* tf = d_tfirst;
+        double* ri = d_rinv;
+        int32_t* okp = d_ok;
+        void* kargs[] = {&Sp, &mm, &tf, &ri, &okp};
+        chk(cudaLaunchCooperativeKernel((const void*)k_cholesky_coop, dim3(chol_grid), dim3(256), kargs, 0, st));
         int32_t okh = 1;
         chk(cudaMemcpyAsync(&okh, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
         chk(cudaStreamSynchronize(st));
@@ -1377,7 +1425,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             if (nfc > 0) {
                 assemble_S(lam);
                 ok = factor_S() && ok;
-                if (ok) k_chol_solve<<<1, 256, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_bs);
+                if (ok) k_chol_solve<<<1, 1024, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_bs);
                 chk(cudaGetLastError());
             }
             if (e != cudaSuccess) return e;
@@ -1525,7 +1573,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                 ok = factor_S() && ok;
                 if (e != cudaSuccess) return e;
                 if (ok) {
-                    k_chol_solve<<<1, 256, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_bs);
+                    k_chol_solve<<<1, 1024, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_bs);
                 } else {
                     chk(cudaMemsetAsync(d_bs, 0, sizeof(double) * m, st));
                 }
@@ -1642,7 +1690,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                     return cudaSuccess;
                 }
                 // the step: dx_c (in d_bs), dx_p
-                if (nfc > 0) k_chol_solve<<<1, 256, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_bs);
+                if (nfc > 0) k_chol_solve<<<1, 1024, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_bs);
                 k_vjp_point_solve<<<pblocks, TB, 0, st>>>(A, np, d_lt, 12, 6, d_bs, d_dp);
                 // adjoint through [+]: rc = J_l^T xbar'_c, xa = Ad^T xbar'_c; r_p = xbar'_p
                 if (nfc > 0) k_vjp_cams_step<<<(nfc + 127) / 128, 128, 0, st>>>(d_bs, xb, d_rc, xa, nfc);
@@ -1652,7 +1700,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                     cam_sum(d_tr, true);
                     chk(cudaMemcpyAsync(d_uc, d_rc, sizeof(double) * m, cudaMemcpyDeviceToDevice, st));
                     k_vjp_axpy<<<rblocks, TB, 0, st>>>(d_uc, d_ctmp, -1.0, m);
-                    k_chol_solve<<<1, 256, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_uc);
+                    k_chol_solve<<<1, 1024, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_uc);
                 }
                 k_vjp_point_solve<<<pblocks, TB, 0, st>>>(A, np, d_tr, 4, 0, d_uc, d_up);
                 // grad psi at the state: points into d_pbar, cameras into xa, observations, intrinsics
