@@ -219,9 +219,11 @@ __global__ void k_schur_blocks(WinArgs<Real> A, const int2* blocks, const int32_
 // solves its panel tiles L_IK = A_IK L_KK^-T; after a grid synchronization block 0 stores L_KK and the
 // trailing tiles
 // (I, J), K < J <= I inside the envelope, are updated A_IJ -= L_IK L_JK^T in quarter-tile work items
-// (8 rows x 32 columns, one output per thread) spread over all blocks; a grid synchronization ends
-// the column.  Every block runs the same loops, so all reach every synchronization; a non-positive
-// pivot is replaced by 1 and reported through ok.
+// (8 rows x 32 columns, one output per thread) spread over the blocks; a grid synchronization ends
+// the column.  The per-column panel rows and trailing tiles come from host-built lists, and the grid
+// is sized to the largest column's work (a grid synchronization costs more with more blocks).
+// Every block runs the same loops, so all reach every synchronization; a non-positive pivot is
+// replaced by 1 and reported through ok.
 __device__ void factor_diag_tile(double (*tk)[kTile + 1], double* rv, const double* S, int m, int k0, int kb, int& bad) {
     const int tid = threadIdx.x, nth = blockDim.x;
     for (int idx = tid; idx < kTile * kTile; idx += nth) {
@@ -255,7 +257,8 @@ __device__ void factor_diag_tile(double (*tk)[kTile + 1], double* rv, const doub
     }
 }
 
-__global__ void __launch_bounds__(256) k_cholesky_coop(double* S, int m, const int32_t* tfirst, double* rinv,
+__global__ void __launch_bounds__(256) k_cholesky_coop(double* S, int m, const int32_t* pan_off, const int32_t* pan_row,
+                                                       const int32_t* tr_off, const int2* tr_ij, double* rinv,
                                                        int32_t* ok) {
     cg::grid_group grid = cg::this_grid();
     __shared__ double tk[kTile][kTile + 1];
@@ -269,15 +272,11 @@ __global__ void __launch_bounds__(256) k_cholesky_coop(double* S, int m, const i
     __syncthreads();
     for (int K = 0; K < nt; ++K) {
         const int k0 = K * kTile, kb = min(kTile, m - k0);
-        int npan = 0;
-        for (int I = K + 1; I < nt; ++I) npan += tfirst[I] <= K;
+        const int p0 = pan_off[K], npan = pan_off[K + 1] - p0;
         if (bid == 0 || bid < npan) {
             factor_diag_tile(tk, rv, S, m, k0, kb, sbad);
-            // this block's panel tiles: the (bid + c nb)-th tile rows below K inside the envelope
-            int pidx = 0;
-            for (int I = K + 1; I < nt; ++I) {
-                if (tfirst[I] > K) continue;
-                if ((pidx++ % nb) != bid) continue;
+            for (int pi = bid; pi < npan; pi += nb) {  // this block's panel tiles
+                const int I = pan_row[p0 + pi];
                 const int i0 = I * kTile, ib = min(kTile, m - i0);
                 __syncthreads();
                 for (int idx = tid; idx < kTile * kTile; idx += nth) {
@@ -316,33 +315,26 @@ __global__ void __launch_bounds__(256) k_cholesky_coop(double* S, int m, const i
             }
             for (int j = tid; j < kb; j += nth) rinv[k0 + j] = rv[j];
         }
-        // trailing update in quarter-tile work items
-        int widx = 0;
-        for (int I = K + 1; I < nt; ++I) {
-            if (tfirst[I] > K) continue;
-            const int i0 = I * kTile, ib = min(kTile, m - i0);
-            for (int J = K + 1; J <= I; ++J) {
-                if (tfirst[J] > K) continue;
-                const int j0 = J * kTile, jb = min(kTile, m - j0);
-                for (int q = 0; q < 4; ++q) {
-                    if ((widx++ % nb) != bid) continue;
-                    const int r0 = 8 * q;
-                    if (r0 >= ib) continue;  // uniform per block
-                    __syncthreads();
-                    for (int idx = tid; idx < kTile * kTile; idx += nth) {
-                        const int i = idx / kTile, j = idx % kTile;
-                        tb[i][j] = (i < jb && j < kb) ? S[(size_t)(j0 + i) * m + k0 + j] : 0.0;
-                        if (i < 8) ta[i][j] = (r0 + i < ib && j < kb) ? S[(size_t)(i0 + r0 + i) * m + k0 + j] : 0.0;
-                    }
-                    __syncthreads();
-                    const int r = tid / kTile, c = tid % kTile;  // 256 threads: 8 rows x 32 columns
-                    if (r < 8 && r0 + r < ib && c < jb && !(I == J && c > r0 + r)) {
-                        double sum = 0.0;
+        // trailing update: work item w = 4 * tile + quarter over the column's tile list
+        const int t0 = tr_off[K], nitems = 4 * (tr_off[K + 1] - t0);
+        for (int w = bid; w < nitems; w += nb) {
+            const int2 ij = tr_ij[t0 + w / 4];
+            const int I = ij.x, J = ij.y, r0 = 8 * (w % 4);
+            const int i0 = I * kTile, ib = min(kTile, m - i0), j0 = J * kTile, jb = min(kTile, m - j0);
+            if (r0 >= ib) continue;  // uniform per block
+            __syncthreads();
+            for (int idx = tid; idx < kTile * kTile; idx += nth) {
+                const int i = idx / kTile, j = idx % kTile;
+                tb[i][j] = (i < jb && j < kb) ? S[(size_t)(j0 + i) * m + k0 + j] : 0.0;
+                if (i < 8) ta[i][j] = (r0 + i < ib && j < kb) ? S[(size_t)(i0 + r0 + i) * m + k0 + j] : 0.0;
+            }
+            __syncthreads();
+            const int r = tid / kTile, c = tid % kTile;  // 256 threads: 8 rows x 32 columns
+            if (r < 8 && r0 + r < ib && c < jb && !(I == J && c > r0 + r)) {
+                double sum = 0.0;
 #pragma unroll 8
-                        for (int t = 0; t < kTile; ++t) sum += ta[r][t] * tb[c][t];
-                        S[(size_t)(i0 + r0 + r) * m + j0 + c] -= sum;
-                    }
-                }
+                for (int t = 0; t < kTile; ++t) sum += ta[r][t] * tb[c][t];
+                S[(size_t)(i0 + r0 + r) * m + j0 + c] -= sum;
             }
         }
         grid.sync();
@@ -356,17 +348,28 @@ __global__ void __launch_bounds__(256) k_cholesky_coop(double* S, int m, const i
 // contiguous 256-byte row segment; sums are shuffle trees and a fixed-order sum over warps.
 __global__ void k_chol_solve(const double* L, int m, const int32_t* tfirst, const double* rinv, double* x) {
     __shared__ double red[32][kTile];
+    __shared__ double dt[kTile][kTile + 1];  // the diagonal tile, staged for the serial chain
+    __shared__ double dr[kTile];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
     const int nt = (m + kTile - 1) / kTile;
+    auto stage = [&](int k0, int kb) {
+        for (int idx = tid; idx < kTile * kTile; idx += blockDim.x) {
+            const int i = idx / kTile, j = idx % kTile;
+            dt[i][j] = (i < kb && j < kb) ? L[(size_t)(k0 + i) * m + k0 + j] : 0.0;
+        }
+        for (int j = tid; j < kTile; j += blockDim.x) dr[j] = j < kb ? rinv[k0 + j] : 1.0;
+        __syncthreads();
+    };
     // forward: L y = b
     for (int K = 0; K < nt; ++K) {
         const int k0 = K * kTile, kb = min(kTile, m - k0);
+        stage(k0, kb);
         if (tid < 32) {  // warp 0 solves the diagonal tile
             double v = lane < kb ? x[k0 + lane] : 0.0;
             for (int j = 0; j < kb; ++j) {
-                const double xj = __shfl_sync(kFullG, v * (lane == j ? rinv[k0 + j] : 1.0), j);
+                const double xj = __shfl_sync(kFullG, v * (lane == j ? dr[j] : 1.0), j);
                 if (lane == j) v = xj;
-                if (lane > j && lane < kb) v -= L[(size_t)(k0 + lane) * m + k0 + j] * xj;
+                if (lane > j && lane < kb) v -= dt[lane][j] * xj;
             }
             if (lane < kb) x[k0 + lane] = v;
         }
@@ -398,12 +401,13 @@ __global__ void k_chol_solve(const double* L, int m, const int32_t* tfirst, cons
             x[k0 + tid] -= s;
         }
         __syncthreads();
+        stage(k0, kb);
         if (tid < 32) {
             double v = lane < kb ? x[k0 + lane] : 0.0;
             for (int j = kb - 1; j >= 0; --j) {
-                const double xj = __shfl_sync(kFullG, v * (lane == j ? rinv[k0 + j] : 1.0), j);
+                const double xj = __shfl_sync(kFullG, v * (lane == j ? dr[j] : 1.0), j);
                 if (lane == j) v = xj;
-                if (lane < j) v -= L[(size_t)(k0 + j) * m + k0 + lane] * xj;
+                if (lane < j) v -= dt[j][lane] * xj;
             }
             if (lane < kb) x[k0 + lane] = v;
         }
@@ -1004,6 +1008,10 @@ struct GridHost {
     std::vector<int32_t> cam_list, item_off, fcam, boff, tfirst;
     std::vector<int4> items;
     std::vector<int2> blocks, pairs;
+    // Cholesky work per tile column K: panel tile rows and trailing tiles (I, J), K < J <= I
+    std::vector<int32_t> pan_off, pan_row, tr_off;
+    std::vector<int2> tr_ij;
+    int max_col_work = 1;  // largest per-column count of panel tiles or trailing quarter items
 };
 
 void build_grid_host(const HostWindow& h, GridHost& g) {
@@ -1102,6 +1110,24 @@ void build_grid_host(const HostWindow& h, GridHost& g) {
         }
         g.tfirst[I] = first;
     }
+    g.pan_off.assign(nt + 1, 0);
+    g.tr_off.assign(nt + 1, 0);
+    g.pan_row.clear();
+    g.tr_ij.clear();
+    g.max_col_work = 1;
+    for (int K = 0; K < nt; ++K) {
+        std::vector<int32_t> rows;
+        for (int I = K + 1; I < nt; ++I)
+            if (g.tfirst[I] <= K) rows.push_back(I);
+        for (int I : rows) g.pan_row.push_back(I);
+        for (size_t x = 0; x < rows.size(); ++x)
+            for (size_t y = 0; y <= x; ++y) g.tr_ij.push_back(make_int2(rows[x], rows[y]));
+        g.pan_off[K + 1] = (int32_t)g.pan_row.size();
+        g.tr_off[K + 1] = (int32_t)g.tr_ij.size();
+        g.max_col_work = std::max(g.max_col_work, std::max((int)rows.size(), 4 * (g.tr_off[K + 1] - g.tr_off[K])));
+    }
+    if (g.pan_row.empty()) g.pan_row.push_back(0);
+    if (g.tr_ij.empty()) g.tr_ij.push_back(make_int2(0, 0));
 }
 
 // Device buffers of one grid solve (allocated per call; problems here are large, so the
@@ -1174,6 +1200,10 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     int32_t* d_boff = dv.alloc<int32_t>(g.boff.size());
     int2* d_pairs = dv.alloc<int2>(g.pairs.size());
     int32_t* d_tfirst = dv.alloc<int32_t>(g.tfirst.size());
+    int32_t* d_pan_off = dv.alloc<int32_t>(g.pan_off.size());
+    int32_t* d_pan_row = dv.alloc<int32_t>(g.pan_row.size());
+    int32_t* d_tr_off = dv.alloc<int32_t>(g.tr_off.size());
+    int2* d_tr_ij = dv.alloc<int2>(g.tr_ij.size());
     const bool pcg = lm.solver == NAV_BA_SOLVER_PCG && !debug_S;
     const int nk = (lm.optimize_k && intr.model == 1) ? 2 : 0;
     const int mt = m + nk;
@@ -1260,6 +1290,10 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     chk(up(d_boff, g.boff, st));
     chk(up(d_pairs, g.pairs, st));
     chk(up(d_tfirst, g.tfirst, st));
+    chk(up(d_pan_off, g.pan_off, st));
+    chk(up(d_pan_row, g.pan_row, st));
+    chk(up(d_tr_off, g.tr_off, st));
+    chk(up(d_tr_ij, g.tr_ij, st));
     std::vector<int32_t> cm_pt;
     if (pcg) {
         cm_pt.resize(ncl);
@@ -1376,17 +1410,20 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_cholesky_coop, 256, 0);
-        chol_grid = std::max(1, nsm * std::max(1, std::min(bps, 2)));
+        chol_grid = std::max(1, std::min(nsm * std::max(1, std::min(bps, 2)), g.max_col_work));
     }
     auto factor_S = [&]() -> bool {
         const int32_t one = 1;
         chk(cudaMemcpyAsync(d_ok, &one, sizeof(int32_t), cudaMemcpyHostToDevice, st));
         double* Sp = d_S;
         int mm = m;
-        const int32_t* tf = d_tfirst;
+        const int32_t* po = d_pan_off;
+        const int32_t* pr = d_pan_row;
+        const int32_t* to = d_tr_off;
+        const int2* tij = d_tr_ij;
         double* ri = d_rinv;
         int32_t* okp = d_ok;
-        void* kargs[] = {&Sp, &mm, &tf, &ri, &okp};
+        void* kargs[] = {&Sp, &mm, &po, &pr, &to, &tij, &ri, &okp};
         chk(cudaLaunchCooperativeKernel((const void*)k_cholesky_coop, dim3(chol_grid), dim3(256), kargs, 0, st));
         int32_t okh = 1;
         chk(cudaMemcpyAsync(&okh, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
