@@ -57,6 +57,7 @@ struct SmemHead {
     int32_t lcnt[kWinMaxCams];             // per CTA: edges per camera (free cameras)
     int32_t poff[kMaxBlocks + 1];          // rank 0: pair-list offsets of the S blocks
     int32_t pcnt[kMaxBlocks];              // rank 0: pairs per S block
+    int32_t whist[16][kWinMaxFreeCams];    // per warp: pair counts / cursors of one block row
     int32_t cur, ok, win, slot;
 };
 
@@ -180,24 +181,28 @@ __device__ void build_lists(const WinArgs<Real>& A, CC& c, const WinDesc& D) {
         }
     }
     csync();  // every camera list is in global memory
+    // Schur pairs by block row: the warp of free camera a walks a's edges i and, for each, the other
+    // edges j of i's free point whose free camera b <= a; pair (i, j) belongs to block (a, b).
     const int nblk = D.nfc * (D.nfc + 1) / 2;
-    for (int blk = c.gw; blk < nblk; blk += c.CW) {
-        int a, b;
-        decode_block(blk, a, b);
-        const int ca = s.fcam[a], cb = s.fcam[b];
+    int* hist = c.s->whist[c.wid];
+    for (int a = c.gw; a < D.nfc; a += c.CW) {
+        for (int b = c.lane; b <= a; b += 32) hist[b] = 0;
+        __syncwarp();
+        const int ca = s.fcam[a];
         const int* list = A.cam_list + D.e0 + s.loff[ca];
         const int cnt = s.lcnt[ca];
-        int n = 0;
         for (int i = c.lane; i < cnt; i += 32) {
-            const int ei = list[i];
-            const int gp = D.pt0 + A.edge_pt[ei];
+            const int gp = D.pt0 + A.edge_pt[list[i]];
             if (A.pt_free[gp] < 0) continue;
             const int e1 = A.pt_eoff[gp + 1];
-            for (int ej = A.pt_eoff[gp]; ej < e1; ++ej) n += A.edge_cam[ej] == cb;
+            for (int ej = A.pt_eoff[gp]; ej < e1; ++ej) {
+                const int bb = A.edge_fc[ej];
+                if (bb >= 0 && bb <= a) atomicAdd(&hist[bb], 1);  // integer counts: order-independent
+            }
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(kFull, n, o);
-        if (c.lane == 0) c.s0->pcnt[blk] = n;
+        __syncwarp();
+        for (int b = c.lane; b <= a; b += 32) c.s0->pcnt[a * (a + 1) / 2 + b] = hist[b];
+        __syncwarp();
     }
     csync();
     if (c.rank == 0 && threadIdx.x == 0) {
@@ -209,40 +214,47 @@ __device__ void build_lists(const WinArgs<Real>& A, CC& c, const WinDesc& D) {
         s.poff[nblk] = acc;
     }
     csync();
-    for (int blk = c.gw; blk < nblk; blk += c.CW) {
-        int a, b;
-        decode_block(blk, a, b);
-        const int ca = s.fcam[a], cb = s.fcam[b];
+    // fill: lanes take 32 consecutive edges of a's list; in warp-uniform rounds every lane emits its
+    // next pair; lanes of one round with the same block are placed in lane order (match + rank) and
+    // the block's cursor advances, so each block's list is in (list position, point-edge) order
+    const int64_t end = D.pair0 + D.npair;
+    for (int a = c.gw; a < D.nfc; a += c.CW) {
+        for (int b = c.lane; b <= a; b += 32) hist[b] = c.s0->poff[a * (a + 1) / 2 + b];
+        __syncwarp();
+        const int ca = s.fcam[a];
         const int* list = A.cam_list + D.e0 + s.loff[ca];
         const int cnt = s.lcnt[ca];
-        int64_t pos = D.pair0 + c.s0->poff[blk];
-        const int64_t end = D.pair0 + D.npair;
         for (int base = 0; base < cnt; base += 32) {
             const int i = base + c.lane;
-            int ei = -1, gp = -1, k = 0;
+            int ei = -1, ej = 0, e1 = 0;
             if (i < cnt) {
                 ei = list[i];
-                gp = D.pt0 + A.edge_pt[ei];
+                const int gp = D.pt0 + A.edge_pt[ei];
                 if (A.pt_free[gp] >= 0) {
-                    const int e1 = A.pt_eoff[gp + 1];
-                    for (int ej = A.pt_eoff[gp]; ej < e1; ++ej) k += A.edge_cam[ej] == cb;
+                    ej = A.pt_eoff[gp];
+                    e1 = A.pt_eoff[gp + 1];
                 }
             }
-            int incl = k;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int t = __shfl_up_sync(kFull, incl, o);
-                if (c.lane >= o) incl += t;
+            for (;;) {
+                int b = -1;
+                for (; ej < e1; ++ej) {
+                    const int bb = A.edge_fc[ej];
+                    if (bb >= 0 && bb <= a) {
+                        b = bb;
+                        break;
+                    }
+                }
+                if (__ballot_sync(kFull, b >= 0) == 0u) break;
+                const unsigned grp = __match_any_sync(kFull, b);
+                if (b >= 0) {
+                    const int64_t q = D.pair0 + hist[b] + __popc(grp & ((1u << c.lane) - 1u));
+                    if (q < end) A.pairs[q] = ((uint32_t)(ei - D.e0) << 16) | (uint32_t)(ej - D.e0);
+                }
+                __syncwarp();
+                if (b >= 0 && (grp >> c.lane) == 1u) hist[b] += __popc(grp);  // the group's highest lane
+                __syncwarp();
+                if (b >= 0) ++ej;
             }
-            const int total = __shfl_sync(kFull, incl, 31);
-            if (k > 0) {
-                int64_t q = pos + incl - k;
-                const int e1 = A.pt_eoff[gp + 1];
-                for (int ej = A.pt_eoff[gp]; ej < e1; ++ej)
-                    if (A.edge_cam[ej] == cb && q < end)
-                        A.pairs[q++] = ((uint32_t)(ei - D.e0) << 16) | (uint32_t)(ej - D.e0);
-            }
-            pos += total;
         }
     }
     csync();
