@@ -19,11 +19,27 @@ namespace navba {
 struct Intr {
     double fx, fy, cx, cy, k1, k2, k3, k4;
     int model;  // 0 pinhole, 1 pinhole + radial (k1, k2), 2 Kannala-Brandt (k1..k4)
+    float f[8];  // the same eight values rounded to float once (the mixed form's arithmetic)
 };
 
 // Intrinsics from the 8 values of nav_ba_problem::intrinsics and the camera model.
 NAVBA_HD Intr make_intr(const double* k8, int model) {
-    return Intr{k8[0], k8[1], k8[2], k8[3], k8[4], k8[5], k8[6], k8[7], model};
+    Intr in{k8[0], k8[1], k8[2], k8[3], k8[4], k8[5], k8[6], k8[7], model, {}};
+    for (int k = 0; k < 8; ++k) in.f[k] = (float)k8[k];
+    return in;
+}
+
+// The intrinsics in precision Real: the FP64 values, or their float copies (no conversion per use).
+template <class Real>
+struct IntrV {
+    Real fx, fy, cx, cy, k1, k2, k3, k4;
+};
+template <class Real>
+NAVBA_HD IntrV<Real> intr_in(const Intr& in) {
+    if constexpr (sizeof(Real) == 4)
+        return IntrV<Real>{in.f[0], in.f[1], in.f[2], in.f[3], in.f[4], in.f[5], in.f[6], in.f[7]};
+    else
+        return IntrV<Real>{in.fx, in.fy, in.cx, in.cy, in.k1, in.k2, in.k3, in.k4};
 }
 
 // ---- quaternions (x, y, z, w), unit, w >= 0 ---------------------------------------------
@@ -190,6 +206,7 @@ struct EdgeLin {
     Real jk[4];   // 2x2 d e / d (k1, k2) (radial model; zero for the pinhole)
     Real w;       // rho'(e^T e)
     double rho;   // rho(e^T e)
+    Real xc[3];   // the point in the camera
 };
 
 // Huber (g2o RobustKernelHuber::robustify): rho(s) = s for s <= d^2 else 2 d sqrt(s) - d^2,
@@ -219,7 +236,8 @@ NAVBA_HD void transform(const Real* R, const Real* t, const Real* X, Real* Xc) {
 template <class Real>
 NAVBA_HD void project(const Intr& in, const Real* Xc, Real* uv, Real* J, Real* Jk = nullptr) {
     const Real x = Xc[0], y = Xc[1], z = Xc[2];
-    const Real fx = (Real)in.fx, fy = (Real)in.fy, cx = (Real)in.cx, cy = (Real)in.cy;
+    const IntrV<Real> kv = intr_in<Real>(in);
+    const Real fx = kv.fx, fy = kv.fy, cx = kv.cx, cy = kv.cy;
     if (in.model == 2) {
         // Kannala-Brandt (KannalaBrandt8.cpp:80-107 projection, :195-226 Jacobian), in Real throughout:
         // pi = f r(theta) (x, y) / rho + c, theta = atan2(rho, z), r = theta + k1 theta^3 + .. + k4 theta^9.
@@ -227,8 +245,7 @@ NAVBA_HD void project(const Intr& in, const Real* Xc, Real* uv, Real* J, Real* J
         // With A = r'(theta) z / (rho^2 + z^2) and B = r / rho the Jacobian is
         //   [[fx (x^2 A + y^2 B), fx x y (A - B)] / rho^2, -fx r' x / (rho^2 + z^2)], likewise for v;
         // on the optical axis (rho <= 1e-9 |z|) both reduce to the pinhole values (B -> 1/z).
-        const Real fx = (Real)in.fx, fy = (Real)in.fy, cx = (Real)in.cx, cy = (Real)in.cy;
-        const Real k1 = (Real)in.k1, k2 = (Real)in.k2, k3 = (Real)in.k3, k4 = (Real)in.k4;
+        const Real k1 = kv.k1, k2 = kv.k2, k3 = kv.k3, k4 = kv.k4;
         const Real rho2 = x * x + y * y, rho = sqrt(rho2);
         const Real rz2 = rho2 + z * z;
         if (rho <= Real(1e-9) * fabs(z)) {
@@ -269,7 +286,7 @@ NAVBA_HD void project(const Intr& in, const Real* Xc, Real* uv, Real* J, Real* J
             J[3] = Real(0); J[4] = fy * iz; J[5] = -fy * yn * iz;
         }
     } else {
-        const Real k1 = (Real)in.k1, k2 = (Real)in.k2;
+        const Real k1 = kv.k1, k2 = kv.k2;
         const Real xn = x * iz, yn = y * iz;
         const Real r2 = xn * xn + yn * yn;
         const Real d = Real(1) + k1 * r2 + k2 * r2 * r2;
@@ -296,6 +313,9 @@ NAVBA_HD void edge_linearize(const Intr& in, const Real* R, const Real* t, const
                              const Real* z, bool robust, Real delta, EdgeLin<Real>& L) {
     Real Xc[3], uv[2], J[6], Jk[4] = {Real(0), Real(0), Real(0), Real(0)};
     transform(R, t, X, Xc);
+    L.xc[0] = Xc[0];
+    L.xc[1] = Xc[1];
+    L.xc[2] = Xc[2];
     project(in, Xc, uv, J, in.model == 1 ? Jk : nullptr);
     L.e[0] = z[0] - uv[0];
     L.e[1] = z[1] - uv[1];
@@ -320,6 +340,27 @@ NAVBA_HD void edge_linearize(const Intr& in, const Real* R, const Real* t, const
         L.jc[r * 6 + 4] = p1;
         L.jc[r * 6 + 5] = p2;
     }
+}
+
+// Pinhole pose Jacobian d e / d (omega, upsilon) (edge_linearize's jc, rotation first) from the
+// normalized camera coordinates u = x / z, v = y / z and iz = 1 / z of the point in the camera:
+// -Jpi [-[Xc]x | I] with Jpi = iz [[fx, 0, -fx u], [0, fy, -fy v]]; the rotation block does not
+// depend on the depth.
+template <class Real>
+NAVBA_HD void pinhole_jc(Real fx, Real fy, Real u, Real v, Real iz, Real* jc) {
+    const Real uv = u * v;
+    jc[0] = fx * uv;
+    jc[1] = -fx * (Real(1) + u * u);
+    jc[2] = fx * v;
+    jc[3] = -fx * iz;
+    jc[4] = Real(0);
+    jc[5] = fx * u * iz;
+    jc[6] = fy * (Real(1) + v * v);
+    jc[7] = -fy * uv;
+    jc[8] = -fy * u;
+    jc[9] = Real(0);
+    jc[10] = -fy * iz;
+    jc[11] = fy * v * iz;
 }
 
 // Robust chi2 of one edge, in precision Real.

@@ -77,6 +77,8 @@ struct WindowBatch {
     void* d_edge_e[2] = {nullptr, nullptr};  // mixed: [ne][2] f32 residuals, current / trial state
     int32_t* d_cam_list = nullptr; // [ne] camera-major edge list (free cameras only)
     uint32_t* d_pairs = nullptr;   // [npair] Schur pairs (edge i << 16 | edge j), window-local
+    void* d_edge_uvr = nullptr;    // mixed: [ne][2] f32 observations
+    void* d_xr[2] = {nullptr, nullptr};  // mixed: [npt][4] f32 copies of d_x
     // device outputs
     CamState* d_cam_out = nullptr;
     double* d_pt_out = nullptr;    // [npt][4]
@@ -84,7 +86,7 @@ struct WindowBatch {
     WinStats* d_stats = nullptr;
     double* d_debug = nullptr;     // reduced-system debug output (optional)
     unsigned long long* d_phase = nullptr;  // per-phase cycle totals (NAVBA_PHASE_TIMING=1)
-    size_t cap[32] = {};      // allocated bytes of each buffer (buffers are reused across calls)
+    size_t cap[48] = {};      // allocated bytes of each buffer (buffers are reused across calls)
     size_t bytes = 0;
     int64_t h2d_bytes = 0;    // bytes uploaded by window_batch_upload
 };

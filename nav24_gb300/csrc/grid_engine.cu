@@ -1014,7 +1014,9 @@ struct GridHost {
     int max_col_work = 1;  // largest per-column count of panel tiles or trailing quarter items
 };
 
-void build_grid_host(const HostWindow& h, GridHost& g) {
+// schur: also the reduced system's block structure, pair lists and Cholesky work lists (the dense
+// Cholesky path; the PCG path forms S only implicitly and needs none of them).
+void build_grid_host(const HostWindow& h, GridHost& g, bool schur) {
     const int nfc = h.nfc;
     g.fcam.assign(std::max(1, nfc), 0);
     for (int c = 0; c < h.ncam; ++c)
@@ -1040,26 +1042,51 @@ void build_grid_host(const HostWindow& h, GridHost& g) {
         g.item_off[a + 1] = (int32_t)g.items.size();
     }
     if (g.items.empty()) g.items.push_back(make_int4(0, 0, 0, 0));
+    if (!schur) {
+        g.blocks.assign(1, make_int2(0, 0));
+        g.boff.assign(2, 0);
+        g.pairs.assign(1, make_int2(0, 0));
+        g.tfirst.assign(1, 0);
+        g.pan_off.assign(2, 0);
+        g.tr_off.assign(2, 0);
+        g.pan_row.assign(1, 0);
+        g.tr_ij.assign(1, make_int2(0, 0));
+        g.max_col_work = 1;
+        return;
+    }
     // nonzero lower blocks and their pair lists (per block: pairs in camera-major, point order)
-    std::vector<std::vector<int2>> per_block_rows(nfc);
-    std::vector<int> mark(nfc, -1);
+    // (up to 4096 free cameras through a dense nfc x nfc index, beyond that by sorted rows)
+    const bool dense = (size_t)nfc * nfc <= ((size_t)1 << 24);
+    std::vector<int32_t> bidx;  // dense: block index of (a, b), b <= a, or -1
     std::vector<std::vector<int32_t>> rowcols(nfc);
-    for (int i = 0; i < h.npt; ++i) {
-        if (h.pt_free[i] < 0) continue;
-        for (int e = h.pt_eoff[i]; e < h.pt_eoff[i + 1]; ++e) {
-            const int a = h.cam_free[h.edge_cam[e]];
-            if (a < 0) continue;
-            for (int f = h.pt_eoff[i]; f < h.pt_eoff[i + 1]; ++f) {
-                const int b = h.cam_free[h.edge_cam[f]];
-                if (b >= 0 && b <= a) rowcols[a].push_back(b);
+    auto for_each_block = [&](auto fn) {  // fn(a, b) for every co-observing pair, b <= a
+        for (int i = 0; i < h.npt; ++i) {
+            if (h.pt_free[i] < 0) continue;
+            for (int e = h.pt_eoff[i]; e < h.pt_eoff[i + 1]; ++e) {
+                const int a = h.cam_free[h.edge_cam[e]];
+                if (a < 0) continue;
+                for (int f = h.pt_eoff[i]; f < h.pt_eoff[i + 1]; ++f) {
+                    const int b = h.cam_free[h.edge_cam[f]];
+                    if (b >= 0 && b <= a) fn(a, b);
+                }
             }
         }
-    }
-    std::vector<std::vector<int32_t>> cols(nfc);
-    for (int a = 0; a < nfc; ++a) {
-        rowcols[a].push_back(a);
-        std::sort(rowcols[a].begin(), rowcols[a].end());
-        rowcols[a].erase(std::unique(rowcols[a].begin(), rowcols[a].end()), rowcols[a].end());
+    };
+    if (dense) {
+        bidx.assign((size_t)nfc * nfc, -1);
+        for_each_block([&](int a, int b) { bidx[(size_t)a * nfc + b] = 0; });
+        for (int a = 0; a < nfc; ++a) {
+            bidx[(size_t)a * nfc + a] = 0;
+            for (int b = 0; b <= a; ++b)
+                if (bidx[(size_t)a * nfc + b] == 0) rowcols[a].push_back(b);
+        }
+    } else {
+        for_each_block([&](int a, int b) { rowcols[a].push_back(b); });
+        for (int a = 0; a < nfc; ++a) {
+            rowcols[a].push_back(a);
+            std::sort(rowcols[a].begin(), rowcols[a].end());
+            rowcols[a].erase(std::unique(rowcols[a].begin(), rowcols[a].end()), rowcols[a].end());
+        }
     }
     // block index of (a, b)
     std::vector<int32_t> row_start(nfc + 1, 0);
@@ -1067,8 +1094,12 @@ void build_grid_host(const HostWindow& h, GridHost& g) {
     const int nblk = row_start[nfc];
     g.blocks.resize(std::max(1, nblk));
     for (int a = 0; a < nfc; ++a)
-        for (size_t k = 0; k < rowcols[a].size(); ++k) g.blocks[row_start[a] + k] = make_int2(a, rowcols[a][k]);
+        for (size_t k = 0; k < rowcols[a].size(); ++k) {
+            g.blocks[row_start[a] + k] = make_int2(a, rowcols[a][k]);
+            if (dense) bidx[(size_t)a * nfc + rowcols[a][k]] = row_start[a] + (int32_t)k;
+        }
     auto block_of = [&](int a, int b) {
+        if (dense) return bidx[(size_t)a * nfc + b];
         const auto& rc = rowcols[a];
         return row_start[a] + (int32_t)(std::lower_bound(rc.begin(), rc.end(), b) - rc.begin());
     };
@@ -1162,8 +1193,9 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     auto ms_from = [](std::chrono::steady_clock::time_point a) {
         return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
     };
+    const bool pcg = lm.solver == NAV_BA_SOLVER_PCG && !debug_S;
     GridHost g;
-    build_grid_host(h, g);
+    build_grid_host(h, g, !pcg || vjp != nullptr);
     const double t_host = ms_from(tg0);
     const int nc = h.ncam, np = h.npt, ne = h.ne, nfc = h.nfc;
     const int m = 6 * nfc;
@@ -1204,7 +1236,6 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     int32_t* d_pan_row = dv.alloc<int32_t>(g.pan_row.size());
     int32_t* d_tr_off = dv.alloc<int32_t>(g.tr_off.size());
     int2* d_tr_ij = dv.alloc<int2>(g.tr_ij.size());
-    const bool pcg = lm.solver == NAV_BA_SOLVER_PCG && !debug_S;
     const int nk = (lm.optimize_k && intr.model == 1) ? 2 : 0;
     const int mt = m + nk;
     double* d_S = dv.alloc<double>(pcg ? 1 : (size_t)std::max(1, m) * std::max(1, m));

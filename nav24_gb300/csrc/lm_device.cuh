@@ -27,11 +27,15 @@ struct WinArgs {
     const int32_t* edge_fc;   // free index of each edge's camera, or -1
     const int32_t* edge_pt;
     const double* edge_uv;
+    Real* edge_uvr;           // window engine, mixed form: edge_uv rounded to Real (null: rounded per use)
     double* x[2];
+    Real* xr[2];              // window engine, mixed form: x rounded to Real, kept with x (null: per use)
     Real* pt_vg;
     Real* pt_lt;
     Real* edge_w;             // FP64 form: W_e = w J_c^T J_p per edge; null: recomputed (mixed form)
     Real* edge_a;
+    int32_t jfact;            // window engine, mixed form, pinhole: edge_a holds Jacobian-factored
+                              // records (JRec) instead of A
     Real* edge_e[2];          // mixed form: residual (u, v) of each edge at the current / trial state
     int32_t* cam_list;
     uint32_t* pairs;
@@ -144,6 +148,94 @@ struct Rec<double> {
     }
 };
 
+// Point gp's state and edge e's observation in Real, from the Real copies where they are kept
+// (XR, A.edge_uvr), else rounded from FP64 here: both give the same values.
+template <class Real>
+__device__ __forceinline__ void point_real(const double* X, const Real* XR, long long gp, Real* o) {
+    if constexpr (sizeof(Real) == 4) {
+        if (XR) {
+            const float4 t = *reinterpret_cast<const float4*>(XR + 4 * gp);
+            o[0] = t.x;
+            o[1] = t.y;
+            o[2] = t.z;
+            return;
+        }
+    }
+    o[0] = (Real)X[4 * gp];
+    o[1] = (Real)X[4 * gp + 1];
+    o[2] = (Real)X[4 * gp + 2];
+}
+
+template <class Real>
+__device__ __forceinline__ void obs_real(const WinArgs<Real>& A, long long e, Real* z) {
+    if constexpr (sizeof(Real) == 4) {
+        if (A.edge_uvr) {
+            const float2 t = *reinterpret_cast<const float2*>(A.edge_uvr + 2 * e);
+            z[0] = t.x;
+            z[1] = t.y;
+            return;
+        }
+    }
+    z[0] = (Real)A.edge_uv[2 * e];
+    z[1] = (Real)A.edge_uv[2 * e + 1];
+}
+
+// Trial point gp = X + d: the FP64 state, and its Real copy where one is kept.
+template <class Real>
+__device__ __forceinline__ void store_trial_point(const double* Xc, double* Xt, Real* XRt, long long gp, Real d0,
+                                                  Real d1, Real d2) {
+    const double x0 = Xc[4 * gp + 0] + (double)d0, x1 = Xc[4 * gp + 1] + (double)d1, x2 = Xc[4 * gp + 2] + (double)d2;
+    Xt[4 * gp + 0] = x0;
+    Xt[4 * gp + 1] = x1;
+    Xt[4 * gp + 2] = x2;
+    if constexpr (sizeof(Real) == 4) {
+        if (XRt) *reinterpret_cast<float4*>(XRt + 4 * gp) = make_float4((float)x0, (float)x1, (float)x2, 0.f);
+    }
+}
+
+// Jacobian-factored edge record (mixed form, pinhole model), 12 floats: u = x / z, v = y / z,
+// iz = 1 / z of the point in the camera at the linearization state, B = w J_p L^T (2x3, row-major)
+// and the point's t = L g.  A = W L^T = w J_c^T J_p L^T = J_c^T B, and J_c follows from (u, v, iz)
+// (pinhole_jc), so the record carries A in 48 bytes instead of 80: A_i A_j^T = J_ci^T (B_i B_j^T)
+// J_cj and A^T d = B^T (J_c d).
+struct JRec {
+    static constexpr int kEdge = 12;
+    static __device__ __forceinline__ void load(const float* p, float* v) { Rec<float>::load12(p, v); }
+};
+
+// u -= A_e^T d for edge e and its camera's step d (6 values).
+template <class Real, class DC>
+__device__ __forceinline__ void sub_at_d(const WinArgs<Real>& A, long long e, const DC* d, Real fx, Real fy, Real& u0,
+                                         Real& u1, Real& u2) {
+    if constexpr (sizeof(Real) == 4) {
+        if (A.jfact) {
+            Real rec[12], jc[12];
+            JRec::load(A.edge_a + (long long)JRec::kEdge * e, rec);
+            pinhole_jc(fx, fy, rec[0], rec[1], rec[2], jc);
+            Real j0 = Real(0), j1 = Real(0);
+#pragma unroll
+            for (int r = 0; r < 6; ++r) {
+                const Real dr = (Real)d[r];
+                j0 += jc[r] * dr;
+                j1 += jc[6 + r] * dr;
+            }
+            u0 -= rec[3] * j0 + rec[6] * j1;
+            u1 -= rec[4] * j0 + rec[7] * j1;
+            u2 -= rec[5] * j0 + rec[8] * j1;
+            return;
+        }
+    }
+    Real Ae[18];
+    Rec<Real>::load18(A.edge_a + (long long)Rec<Real>::kEdge * e, Ae);
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+        const Real dr = (Real)d[r];
+        u0 -= Ae[r * 3 + 0] * dr;
+        u1 -= Ae[r * 3 + 1] * dr;
+        u2 -= Ae[r * 3 + 2] * dr;
+    }
+}
+
 // Cluster-split robust chi2 of the window for cameras `camc` (12 values per camera, precision
 // Cost) and points X; returns this thread's partial sum.  e_out != null: each edge's residual is
 // also written there (2 values per edge, rounded to Real).
@@ -181,19 +273,21 @@ __device__ double cost_partial(const WinArgs<Real>& A, const CC& c, const WinDes
 // Point-major linearization: V_p, g_p and, when edge_w is set, W_e; returns this thread's max |diag V|.
 template <class Real>
 __device__ double linearize_points(const WinArgs<Real>& A, const CC& c, const WinDesc& D, const Real* camr,
-                                   const double* X) {
+                                   const double* X, const Real* XR = nullptr) {
     const Real delta = (Real)A.lm.huber_delta;
     double mx = 0.0;
     for (int p = c.gt; p < D.npt; p += c.CT) {
         const int gp = D.pt0 + p;
         if (A.pt_free[gp] < 0) continue;
-        const Real Xr[3] = {(Real)X[4LL * gp], (Real)X[4LL * gp + 1], (Real)X[4LL * gp + 2]};
+        Real Xr[3];
+        point_real(X, XR, gp, Xr);
         Real V[6] = {0, 0, 0, 0, 0, 0}, g[3] = {0, 0, 0};
         const int e1 = A.pt_eoff[gp + 1];
         for (int e = A.pt_eoff[gp]; e < e1; ++e) {
             const int cam = A.edge_cam[e];
             const Real* cr = camr + 12 * cam;
-            const Real z[2] = {(Real)A.edge_uv[2LL * e], (Real)A.edge_uv[2LL * e + 1]};
+            Real z[2];
+            obs_real(A, e, z);
             EdgeLin<Real> L;
             edge_linearize<Real>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta, L);
             const Real w = L.w;
@@ -219,7 +313,7 @@ __device__ double linearize_points(const WinArgs<Real>& A, const CC& c, const Wi
         }
         const Real vgv[12] = {V[0], V[1], V[2], V[3], V[4], V[5], g[0], g[1], g[2], Real(0), Real(0), Real(0)};
         Rec<Real>::store12(A.pt_vg + 12LL * gp, vgv);
-        mx = fmax(mx, fmax(fabs((double)V[0]), fmax(fabs((double)V[3]), fabs((double)V[5]))));
+        mx = fmax(mx, (double)fmax(fabs(V[0]), fmax(fabs(V[3]), fabs(V[5]))));
     }
     return mx;
 }
@@ -231,7 +325,7 @@ __device__ double linearize_points(const WinArgs<Real>& A, const CC& c, const Wi
 // memory).  Returns the number of points whose damped block was not positive definite.
 template <class Real>
 __device__ int schur_points(const WinArgs<Real>& A, const CC& c, const WinDesc& D, double lambda, const Real* camr,
-                            const double* X) {
+                            const double* X, const Real* XR = nullptr) {
     const Real lam = (Real)lambda;
     const Real delta = (Real)A.lm.huber_delta;
     int bad = 0;
@@ -256,16 +350,44 @@ __device__ int schur_points(const WinArgs<Real>& A, const CC& c, const WinDesc& 
         const Real ltv[12] = {l00, l10, l11, l20, l21, l22, l00 * vg[6], l10 * vg[6] + l11 * vg[7],
                               l20 * vg[6] + l21 * vg[7] + l22 * vg[8], Real(0), Real(0), Real(0)};
         Rec<Real>::store12(A.pt_lt + 12LL * gp, ltv);
-        const Real Xr[3] = {(Real)X[4LL * gp], (Real)X[4LL * gp + 1], (Real)X[4LL * gp + 2]};
+        Real Xr[3];
+        point_real(X, XR, gp, Xr);
         const int e1 = A.pt_eoff[gp + 1];
         for (int e = A.pt_eoff[gp]; e < e1; ++e) {
             if (A.edge_fc[e] < 0) continue;
+            if constexpr (sizeof(Real) == 4) {
+                if (A.jfact) {  // Jacobian-factored record
+                    const Real* cr = camr + 12 * A.edge_cam[e];
+                    Real z[2];
+                    obs_real(A, e, z);
+                    EdgeLin<Real> L;
+                    edge_linearize<Real>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta, L);
+                    const Real iz = Real(1) / L.xc[2];
+                    Real rec[12];
+                    rec[0] = L.xc[0] * iz;
+                    rec[1] = L.xc[1] * iz;
+                    rec[2] = iz;
+#pragma unroll
+                    for (int s2 = 0; s2 < 2; ++s2) {
+                        const Real j0 = L.w * L.jp[s2 * 3 + 0], j1 = L.w * L.jp[s2 * 3 + 1], j2 = L.w * L.jp[s2 * 3 + 2];
+                        rec[3 + s2 * 3 + 0] = j0 * l00;
+                        rec[3 + s2 * 3 + 1] = j0 * l10 + j1 * l11;
+                        rec[3 + s2 * 3 + 2] = j0 * l20 + j1 * l21 + j2 * l22;
+                    }
+                    rec[9] = ltv[6];
+                    rec[10] = ltv[7];
+                    rec[11] = ltv[8];
+                    Rec<Real>::store12(A.edge_a + (long long)JRec::kEdge * e, rec);
+                    continue;
+                }
+            }
             Real W[18];
             if (A.edge_w) {
                 Rec<Real>::load18(A.edge_w + (long long)Rec<Real>::kEdge * e, W);
             } else {
                 const Real* cr = camr + 12 * A.edge_cam[e];
-                const Real z[2] = {(Real)A.edge_uv[2LL * e], (Real)A.edge_uv[2LL * e + 1]};
+                Real z[2];
+                obs_real(A, e, z);
                 EdgeLin<Real> L;
                 edge_linearize<Real>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta, L);
 #pragma unroll
@@ -288,11 +410,13 @@ __device__ int schur_points(const WinArgs<Real>& A, const CC& c, const WinDesc& 
 }
 
 // Trial points dx_p = L^T (t_p - sum A_e^T dx_c); returns this thread's dx^T(lambda dx + g) part.
-template <class Real>
+template <class Real, class DC>
 __device__ double update_points(const WinArgs<Real>& A, const CC& c, const WinDesc& D, double lambda,
-                                const double* dcl, int cur) {
+                                const DC* dcl, int cur) {
     const double* Xc = A.x[cur];
     double* Xt = A.x[cur ^ 1];
+    Real* XRt = A.xr[cur ^ 1];
+    const Real fx = (Real)A.intr.fx, fy = (Real)A.intr.fy;
     double sc = 0.0;
     for (int p = c.gt; p < D.npt; p += c.CT) {
         const int gp = D.pt0 + p;
@@ -303,24 +427,13 @@ __device__ double update_points(const WinArgs<Real>& A, const CC& c, const WinDe
         const int e1 = A.pt_eoff[gp + 1];
         for (int e = A.pt_eoff[gp]; e < e1; ++e) {
             const int a = A.edge_fc[e];
-            if (a < 0) continue;
-            Real Ae[18];
-            Rec<Real>::load18(A.edge_a + (long long)Rec<Real>::kEdge * e, Ae);
-#pragma unroll
-            for (int r = 0; r < 6; ++r) {
-                const Real d = (Real)dcl[6 * a + r];
-                u0 -= Ae[r * 3 + 0] * d;
-                u1 -= Ae[r * 3 + 1] * d;
-                u2 -= Ae[r * 3 + 2] * d;
-            }
+            if (a >= 0) sub_at_d(A, e, dcl + 6 * a, fx, fy, u0, u1, u2);
         }
         // dx = L^T u
         const Real d0 = lt[0] * u0 + lt[1] * u1 + lt[3] * u2;
         const Real d1 = lt[2] * u1 + lt[4] * u2;
         const Real d2 = lt[5] * u2;
-        Xt[4LL * gp + 0] = Xc[4LL * gp + 0] + (double)d0;
-        Xt[4LL * gp + 1] = Xc[4LL * gp + 1] + (double)d1;
-        Xt[4LL * gp + 2] = Xc[4LL * gp + 2] + (double)d2;
+        store_trial_point(Xc, Xt, XRt, gp, d0, d1, d2);
         Real vg[12];
         Rec<Real>::load12(A.pt_vg + 12LL * gp, vg);
         sc += (double)d0 * (lambda * (double)d0 + (double)vg[6]) + (double)d1 * (lambda * (double)d1 + (double)vg[7]) +
@@ -340,9 +453,11 @@ __device__ double update_points(const WinArgs<Real>& A, const CC& c, const WinDe
 // Returns (this thread's dx^T(lambda dx + g) part, its Kahan-compensated d chi part).
 template <class Real>
 __device__ double2 update_points_dcost(const WinArgs<Real>& A, const CC& c, const WinDesc& D, double lambda,
-                                       const double* dcl, int cur, const Real* camr, const Real* camdel) {
+                                       const Real* dcl, int cur, const Real* camr, const Real* camdel) {
     const double* Xc = A.x[cur];
     double* Xt = A.x[cur ^ 1];
+    const Real* XRc = A.xr[cur];
+    Real* XRt = A.xr[cur ^ 1];
     const Real* ecur = A.edge_e[cur];
     Real* etr = A.edge_e[cur ^ 1];
     const Real fx = (Real)A.intr.fx, fy = (Real)A.intr.fy;
@@ -361,29 +476,19 @@ __device__ double2 update_points_dcost(const WinArgs<Real>& A, const CC& c, cons
             Real u0 = lt[6], u1 = lt[7], u2 = lt[8];
             for (int e = e0i; e < e1i; ++e) {
                 const int a = A.edge_fc[e];
-                if (a < 0) continue;
-                Real Ae[18];
-                Rec<Real>::load18(A.edge_a + (long long)Rec<Real>::kEdge * e, Ae);
-#pragma unroll
-                for (int r = 0; r < 6; ++r) {
-                    const Real d = (Real)dcl[6 * a + r];
-                    u0 -= Ae[r * 3 + 0] * d;
-                    u1 -= Ae[r * 3 + 1] * d;
-                    u2 -= Ae[r * 3 + 2] * d;
-                }
+                if (a >= 0) sub_at_d(A, e, dcl + 6 * a, fx, fy, u0, u1, u2);
             }
             d0 = lt[0] * u0 + lt[1] * u1 + lt[3] * u2;
             d1 = lt[2] * u1 + lt[4] * u2;
             d2 = lt[5] * u2;
-            Xt[4LL * gp + 0] = Xc[4LL * gp + 0] + (double)d0;
-            Xt[4LL * gp + 1] = Xc[4LL * gp + 1] + (double)d1;
-            Xt[4LL * gp + 2] = Xc[4LL * gp + 2] + (double)d2;
+            store_trial_point(Xc, Xt, XRt, gp, d0, d1, d2);
             Real vg[12];
             Rec<Real>::load12(A.pt_vg + 12LL * gp, vg);
             sc += (double)d0 * (lambda * (double)d0 + (double)vg[6]) + (double)d1 * (lambda * (double)d1 + (double)vg[7]) +
                   (double)d2 * (lambda * (double)d2 + (double)vg[8]);
         }
-        const Real X[3] = {(Real)Xc[4LL * gp], (Real)Xc[4LL * gp + 1], (Real)Xc[4LL * gp + 2]};
+        Real X[3];
+        point_real(Xc, XRc, gp, X);
         for (int e = e0i; e < e1i; ++e) {
             const int cam = A.edge_cam[e];
             const Real* cr = camr + 12 * cam;

@@ -105,7 +105,11 @@ nav_ba_status solve_window_noalloc(int device, cudaStream_t stream, const nav_ba
     const size_t o_w = carve(o.precision == NAV_BA_MIXED ? 16 : rs * rec * ne), o_a = carve(rs * rec * ne);
     const size_t eb = o.precision == NAV_BA_MIXED ? rs * 2 * ne : 16;
     const size_t o_e0 = carve(eb), o_e1 = carve(eb);
-    const size_t o_list = carve(sizeof(int32_t) * ne), o_pairs = carve(sizeof(uint32_t) * npair);
+    const size_t o_list = carve(sizeof(int32_t) * ne);
+    const size_t o_pairs = carve(sizeof(uint32_t) * npair);
+    const size_t o_uvr = carve(o.precision == NAV_BA_MIXED ? rs * 2 * ne : 16);
+    const size_t o_xr0 = carve(o.precision == NAV_BA_MIXED ? rs * 4 * np : 16);
+    const size_t o_xr1 = carve(o.precision == NAV_BA_MIXED ? rs * 4 * np : 16);
     const size_t o_cout = carve(sizeof(CamState) * nc), o_pout = carve(sizeof(double) * 4 * np);
     const size_t o_trace = carve(sizeof(double) * trace_stride), o_stats = carve(sizeof(WinStats));
     if (off > (size_t)NAV_BA_NOALLOC_ARENA_BYTES)
@@ -134,6 +138,9 @@ nav_ba_status solve_window_noalloc(int device, cudaStream_t stream, const nav_ba
     b.d_edge_e[0] = arena + o_e0;
     b.d_edge_e[1] = arena + o_e1;
     b.d_cam_list = reinterpret_cast<int32_t*>(arena + o_list);
+    b.d_edge_uvr = arena + o_uvr;
+    b.d_xr[0] = arena + o_xr0;
+    b.d_xr[1] = arena + o_xr1;
     b.d_pairs = reinterpret_cast<uint32_t*>(arena + o_pairs);
     b.d_cam_out = reinterpret_cast<CamState*>(arena + o_cout);
     b.d_pt_out = reinterpret_cast<double*>(arena + o_pout);

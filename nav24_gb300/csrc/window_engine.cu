@@ -59,11 +59,13 @@ struct SmemHead {
     int32_t pcnt[kMaxBlocks];              // rank 0: pairs per S block
     int32_t whist[16][kWinMaxFreeCams];    // per warp: pair counts / cursors of one block row
     int32_t cur, ok, win, slot;
+    double lm[4];    // the LM decision of a trial: rho, lambda, nu, chi (made by thread 0)
+    int32_t lm_acc;  // the trial was accepted
 };
 
 // Offsets of the dynamic part of shared memory (after SmemHead), shared by host and device.
 struct Dyn {
-    size_t cams, camr, camd, camdel, dcl, S, bs, rinv, total;
+    size_t cams, camr, camd, camdel, dcl, dclr, S, bs, rinv, total;
 };
 
 NAVBA_HD size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -76,6 +78,7 @@ NAVBA_HD Dyn dyn_layout(int max_m, int max_ncam, int real_size) {
     d.camd = o; o = align16(o + sizeof(double) * 2 * max_ncam * 12);
     d.camdel = o; o = align16(o + (size_t)real_size * max_ncam * 12);
     d.dcl = o;  o = align16(o + sizeof(double) * max_m);
+    d.dclr = o; o = align16(o + (size_t)real_size * max_m);
     d.S = o;    o = align16(o + sizeof(double) * ((size_t)max_m * (max_m + 1) / 2));
     d.bs = o;   o = align16(o + sizeof(double) * max_m);
     d.rinv = o; o = align16(o + sizeof(double) * max_m);
@@ -263,7 +266,7 @@ __device__ void build_lists(const WinArgs<Real>& A, CC& c, const WinDesc& D) {
 // Camera-major linearization: U_c, g_c (warp per free camera) into rank 0; returns max |diag U|.
 template <class Real>
 __device__ double linearize_cameras(const WinArgs<Real>& A, const CC& c, const WinDesc& D, const Real* camr,
-                                    const double* X) {
+                                    const double* X, const Real* XR) {
     const Real delta = (Real)A.lm.huber_delta;
     const SmemHead& s = *c.s;
     double mx = 0.0;
@@ -278,8 +281,9 @@ __device__ double linearize_cameras(const WinArgs<Real>& A, const CC& c, const W
         for (int i = c.lane; i < cnt; i += 32) {
             const int e = list[i];
             const int gp = D.pt0 + A.edge_pt[e];
-            const Real Xr[3] = {(Real)X[4LL * gp], (Real)X[4LL * gp + 1], (Real)X[4LL * gp + 2]};
-            const Real z[2] = {(Real)A.edge_uv[2LL * e], (Real)A.edge_uv[2LL * e + 1]};
+            Real Xr[3], z[2];
+            point_real(X, XR, gp, Xr);
+            obs_real(A, e, z);
             EdgeLin<Real> L;
             edge_linearize<Real>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta, L);
             const Real w = L.w;
@@ -304,9 +308,99 @@ __device__ double linearize_cameras(const WinArgs<Real>& A, const CC& c, const W
     return mx;
 }
 
+// Sums one S block's lane partials over the warp and writes -sum (plus U_a + lambda I on the
+// diagonal) into rank 0's packed S, and b'_a = g'_a - sum A t on the diagonal.
+template <class Real>
+__device__ __forceinline__ void write_block(const CC& c, int a, int b, Real* acc, Real* accb, double lambda) {
+#pragma unroll
+    for (int k = 0; k < 36; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_xor_sync(kFull, acc[k], o);
+    if (a == b) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) accb[k] += __shfl_xor_sync(kFull, accb[k], o);
+    }
+#pragma unroll
+    for (int k = 0; k < 36; ++k) {
+        if ((k & 31) != c.lane) continue;
+        const int r = k / 6, q = k % 6;
+        if (a == b && q > r) continue;
+        double v = -(double)acc[k];
+        if (a == b) {
+            v += c.s0->U[a][tri(r, q)];
+            if (r == q) v += lambda;
+        }
+        c.S0[tri(6 * a + r, 6 * b + q)] = v;
+    }
+    if (a == b && c.lane < 6) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k)
+            if (k == c.lane) c.bs0[6 * a + k] = c.s0->U[a][21 + k] - (double)accb[k];
+    }
+}
+
+// S blocks from Jacobian-factored records (mixed form, pinhole): per pair (i, j) of block (a, b),
+// A_i A_j^T = J_ci^T M J_cj with M = B_i B_j^T (2x2), the J_c rebuilt from each record's (u, v, iz).
+__device__ void schur_blocks_jf(const WinArgs<float>& A, const CC& c, const WinDesc& D, double lambda) {
+    const int nblk = D.nfc * (D.nfc + 1) / 2;
+    const float fx = (float)A.intr.fx, fy = (float)A.intr.fy;
+    for (int blk = c.gw; blk < nblk; blk += c.CW) {
+        int a, b;
+        decode_block(blk, a, b);
+        const int64_t base = D.pair0 + c.s0->poff[blk];
+        const int n = c.s0->pcnt[blk];
+        float acc[36], accb[6];
+#pragma unroll
+        for (int k = 0; k < 36; ++k) acc[k] = 0.f;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) accb[k] = 0.f;
+        uint32_t pr_next = c.lane < n ? A.pairs[base + c.lane] : 0u;
+        for (int k = c.lane; k < n; k += 32) {
+            const uint32_t pr = pr_next;
+            pr_next = k + 32 < n ? A.pairs[base + k + 32] : 0u;  // prefetch the next pair index
+            const int ei = D.e0 + (int)(pr >> 16), ej = D.e0 + (int)(pr & 0xffffu);
+            float ri[12], rj[12];
+            JRec::load(A.edge_a + (long long)JRec::kEdge * ei, ri);
+            JRec::load(A.edge_a + (long long)JRec::kEdge * ej, rj);
+            const float m00 = ri[3] * rj[3] + ri[4] * rj[4] + ri[5] * rj[5];
+            const float m01 = ri[3] * rj[6] + ri[4] * rj[7] + ri[5] * rj[8];
+            const float m10 = ri[6] * rj[3] + ri[7] * rj[4] + ri[8] * rj[5];
+            const float m11 = ri[6] * rj[6] + ri[7] * rj[7] + ri[8] * rj[8];
+            float jj[12], t0[6], t1[6];
+            pinhole_jc(fx, fy, rj[0], rj[1], rj[2], jj);
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+                t0[q] = m00 * jj[q] + m01 * jj[6 + q];
+                t1[q] = m10 * jj[q] + m11 * jj[6 + q];
+            }
+            float ji[12];
+            pinhole_jc(fx, fy, ri[0], ri[1], ri[2], ji);
+#pragma unroll
+            for (int r = 0; r < 6; ++r)
+#pragma unroll
+                for (int q = 0; q < 6; ++q) acc[r * 6 + q] += ji[r] * t0[q] + ji[6 + r] * t1[q];
+            if (a == b && ei == ej) {
+                const float b0 = ri[3] * ri[9] + ri[4] * ri[10] + ri[5] * ri[11];
+                const float b1 = ri[6] * ri[9] + ri[7] * ri[10] + ri[8] * ri[11];
+#pragma unroll
+                for (int r = 0; r < 6; ++r) accb[r] += ji[r] * b0 + ji[6 + r] * b1;
+            }
+        }
+        write_block<float>(c, a, b, acc, accb, lambda);
+    }
+}
+
 // S blocks (warp per block over its pair list) into rank 0's packed S, and b'.
 template <class Real>
 __device__ void schur_blocks(const WinArgs<Real>& A, const CC& c, const WinDesc& D, double lambda) {
+    if constexpr (sizeof(Real) == 4) {
+        if (A.jfact) {
+            schur_blocks_jf(A, c, D, lambda);
+            return;
+        }
+    }
     const int nblk = D.nfc * (D.nfc + 1) / 2;
     for (int blk = c.gw; blk < nblk; blk += c.CW) {
         int a, b;
@@ -339,57 +433,37 @@ __device__ void schur_blocks(const WinArgs<Real>& A, const CC& c, const WinDesc&
                 for (int r = 0; r < 6; ++r) accb[r] += ai[r * 3 + 0] * t0 + ai[r * 3 + 1] * t1 + ai[r * 3 + 2] * t2;
             }
         }
-#pragma unroll
-        for (int k = 0; k < 36; ++k)
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_xor_sync(kFull, acc[k], o);
-        if (a == b) {
-#pragma unroll
-            for (int k = 0; k < 6; ++k)
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) accb[k] += __shfl_xor_sync(kFull, accb[k], o);
-        }
-#pragma unroll
-        for (int k = 0; k < 36; ++k) {
-            if ((k & 31) != c.lane) continue;
-            const int r = k / 6, q = k % 6;
-            if (a == b && q > r) continue;
-            double v = -(double)acc[k];
-            if (a == b) {
-                v += c.s0->U[a][tri(r, q)];
-                if (r == q) v += lambda;
-            }
-            c.S0[tri(6 * a + r, 6 * b + q)] = v;
-        }
-        if (a == b && c.lane < 6) {
-#pragma unroll
-            for (int k = 0; k < 6; ++k)
-                if (k == c.lane) c.bs0[6 * a + k] = c.s0->U[a][21 + k] - (double)accb[k];
-        }
+        write_block<Real>(c, a, b, acc, accb, lambda);
     }
 }
 
 // In-place Cholesky (LL^T) of packed lower S (m x m) in this CTA's shared memory, FP64; rinv
-// receives 1/L_jj.  One reciprocal square root per column (FP64 divides and square roots are
-// long instruction sequences on GB300's FP64 pipe, so the column is scaled by a product).
+// receives 1/L_jj.  Right-looking: per column j, the column is scaled by 1/L_jj (thread per row),
+// then the trailing rows are updated (warp per row).  The next pivot's row is the first row of
+// warp 0, whose lane 0 takes the pivot right after updating it, so a column costs two barriers.
+// One reciprocal square root per column (FP64 divides and square roots are long instruction
+// sequences on GB300's FP64 pipe, so the column is scaled by a product); every FP64 product is
+// made by one lane only (the pipe's throughput is counted in lanes).
 __device__ bool smem_cholesky(double* S, double* rinv, int m, SmemHead& s) {
-    if (threadIdx.x == 0) s.ok = 1;
-    __syncthreads();
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int j = 0; j < m; ++j) {
-        if (threadIdx.x == 0) {
-            const double d = S[tri(j, j)];
-            if (!(d > 0.0) || !isfinite(d)) {
-                s.ok = 0;
-                S[tri(j, j)] = 1.0;
-                rinv[j] = 1.0;
-            } else {
-                const double r = rsqrt(d);
-                S[tri(j, j)] = d * r;
-                rinv[j] = r;
-            }
+    auto pivot = [&](int j) {  // L_jj and rinv[j]; a pivot that is not positive and finite fails
+        const double d = S[tri(j, j)];
+        if (!(d > 0.0) || !isfinite(d)) {
+            s.ok = 0;
+            S[tri(j, j)] = 1.0;
+            rinv[j] = 1.0;
+        } else {
+            const double r = rsqrt(d);
+            S[tri(j, j)] = d * r;
+            rinv[j] = r;
         }
-        __syncthreads();
+    };
+    if (threadIdx.x == 0) {
+        s.ok = 1;
+        if (m > 0) pivot(0);
+    }
+    __syncthreads();
+    for (int j = 0; j < m; ++j) {
         const double ri = rinv[j];
         for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) S[tri(i, j)] *= ri;
         __syncthreads();
@@ -397,6 +471,7 @@ __device__ bool smem_cholesky(double* S, double* rinv, int m, SmemHead& s) {
             const double lij = S[tri(i, j)];
             double* Si = S + tri(i, 0);
             for (int k = j + 1 + lane; k <= i; k += 32) Si[k] -= lij * S[tri(k, j)];
+            if (i == j + 1 && lane == 0) pivot(j + 1);  // lane 0 updated S[j+1][j+1] itself
         }
         __syncthreads();
     }
@@ -462,6 +537,7 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
     double* camd_tr = camd + 12 * A.max_ncam;
     Real* camdel = reinterpret_cast<Real*>(smem + dl.camdel);  // trial step per camera: E - I, E_t
     double* dcl = reinterpret_cast<double*>(smem + dl.dcl);
+    Real* dclr = reinterpret_cast<Real*>(smem + dl.dclr);  // dcl rounded to Real
     double* S = reinterpret_cast<double*>(smem + dl.S);
     double* bs = reinterpret_cast<double*>(smem + dl.bs);
     double* rinv = reinterpret_cast<double*>(smem + dl.rinv);
@@ -486,8 +562,14 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
         for (int k = 0; k < 4; ++k) {
             A.x[0][4 * gp + k] = A.pt_init[4 * gp + k];
             A.x[1][4 * gp + k] = A.pt_init[4 * gp + k];
+            if (A.xr[0]) {
+                A.xr[0][4 * gp + k] = (Real)A.pt_init[4 * gp + k];
+                A.xr[1][4 * gp + k] = (Real)A.pt_init[4 * gp + k];
+            }
         }
     }
+    if (A.edge_uvr)
+        for (int e = c.gt; e < 2 * D.ne; e += c.CT) A.edge_uvr[2LL * D.e0 + e] = (Real)A.edge_uv[2LL * D.e0 + e];
     if (threadIdx.x == 0) s.cur = 0;
     __syncthreads();
     build_lists(A, c, D);  // ends with a cluster barrier: points are initialized everywhere
@@ -508,9 +590,9 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
         for (int it = 0; it < A.lm.iterations; ++it) {
             const int cur = s.cur;
             Real* cr_cur = cur == 0 ? camr : camr_tr;
-            const double mxp = linearize_points<Real>(A, c, D, cr_cur, A.x[cur]);
+            const double mxp = linearize_points<Real>(A, c, D, cr_cur, A.x[cur], A.xr[cur]);
             pc.mark(2);
-            const double mxc = linearize_cameras<Real>(A, c, D, cr_cur, A.x[cur]);
+            const double mxc = linearize_cameras<Real>(A, c, D, cr_cur, A.x[cur], A.xr[cur]);
             const double maxdiag = cluster_reduce3<true>(c, fmax(mxp, mxc), 0.0, 0.0).x;
             pc.mark(3);
             if (it == 0) {
@@ -523,7 +605,7 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
                 const double lam_use = (A.debug && it == 0 && q == 0) ? A.debug_lambda : lambda;
                 if (c.rank == 0)
                     for (int k = threadIdx.x; k < m * (m + 1) / 2; k += blockDim.x) S[k] = 0.0;
-                const int npd = schur_points<Real>(A, c, D, lam_use, cr_cur, A.x[cur]);
+                const int npd = schur_points<Real>(A, c, D, lam_use, cr_cur, A.x[cur], A.xr[cur]);
                 const double3 r0 = cluster_reduce3<false>(c, (double)npd, 0.0, 0.0);  // also orders S zeroing
                 pc.mark(4);
                 schur_blocks<Real>(A, c, D, lam_use);
@@ -553,7 +635,10 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
                 csync();
                 pc.mark(6);
                 // every CTA takes the camera step from rank 0 and updates all cameras itself
-                for (int k = threadIdx.x; k < m; k += blockDim.x) dcl[k] = c.bs0[k];
+                for (int k = threadIdx.x; k < m; k += blockDim.x) {
+                    dcl[k] = c.bs0[k];
+                    dclr[k] = (Real)dcl[k];
+                }
                 __syncthreads();
                 const bool ok = c.s0->ok != 0;
                 CamState* ccur = cur == 0 ? cams0 : cams1;
@@ -583,37 +668,52 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
                 __syncthreads();
                 double chi_new, scale;
                 if (dcost) {
-                    const double2 ud = update_points_dcost<Real>(A, c, D, lambda, dcl, cur, cr_cur, camdel);
+                    const double2 ud = update_points_dcost<Real>(A, c, D, lambda, dclr, cur, cr_cur, camdel);
                     pc.mark(7);
                     const double3 red = cluster_reduce3<false>(c, ud.y, sc + ud.x, 0.0);
                     chi_new = chi + red.x;
                     scale = red.y;
                 } else {
-                    sc += update_points<Real>(A, c, D, lambda, dcl, cur);
+                    sc += update_points<Real>(A, c, D, lambda, dclr, cur);
                     pc.mark(7);
                     const double3 red = cluster_reduce3<false>(
                         c, cost_partial<double, Real>(A, c, D, cdt, A.x[cur ^ 1]), sc, 0.0);
                     chi_new = red.x;
                     scale = red.y;
                 }
-                if (!ok) chi_new = DBL_MAX;
-                rho = chi - chi_new;
-                scale += 1e-3;
-                rho /= scale;
-                if (rho > 0 && isfinite(chi_new)) {
-                    double alpha = 1.0 - pow(2 * rho - 1, 3.0);
-                    alpha = fmin(alpha, 2.0 / 3.0);
-                    lambda *= fmax(1.0 / 3.0, alpha);
-                    nu = 2.0;
-                    chi = chi_new;
-                    ++acc;
-                    if (threadIdx.x == 0) s.cur = cur ^ 1;
-                } else {
-                    lambda *= nu;
-                    nu *= 2;
-                    ++rej;
+                // the decision is scalar FP64 work (a pow among it): one thread makes it, the others
+                // read it, so the FP64 pipe is not charged once per thread
+                if (threadIdx.x == 0) {
+                    if (!ok) chi_new = DBL_MAX;
+                    double r = chi - chi_new;
+                    scale += 1e-3;
+                    r /= scale;
+                    const bool accept = r > 0 && isfinite(chi_new);
+                    double lam = lambda, n2 = nu, ch = chi;
+                    if (accept) {
+                        double alpha = 1.0 - pow(2 * r - 1, 3.0);
+                        alpha = fmin(alpha, 2.0 / 3.0);
+                        lam *= fmax(1.0 / 3.0, alpha);
+                        n2 = 2.0;
+                        ch = chi_new;
+                        s.cur = cur ^ 1;
+                    } else {
+                        lam *= n2;
+                        n2 *= 2;
+                    }
+                    s.lm[0] = r;
+                    s.lm[1] = lam;
+                    s.lm[2] = n2;
+                    s.lm[3] = ch;
+                    s.lm_acc = accept;
                 }
                 __syncthreads();
+                rho = s.lm[0];
+                lambda = s.lm[1];
+                nu = s.lm[2];
+                chi = s.lm[3];
+                if (s.lm_acc) ++acc; else ++rej;
+                __syncthreads();  // the decision is read before the next trial overwrites it
                 pc.mark(8);
                 ++q;
             } while (rho < 0 && q < A.lm.max_trials);
@@ -707,12 +807,16 @@ cudaError_t launch_typed(PreparedBatch& pb, cudaStream_t stream, WindowLaunch sh
     A.edge_fc = b.d_edge_fc;
     A.edge_pt = b.d_edge_pt;
     A.edge_uv = b.d_edge_uv;
+    A.edge_uvr = sizeof(Real) == 4 ? (Real*)b.d_edge_uvr : nullptr;
     A.x[0] = b.d_x[0];
     A.x[1] = b.d_x[1];
+    A.xr[0] = sizeof(Real) == 4 ? (Real*)b.d_xr[0] : nullptr;
+    A.xr[1] = sizeof(Real) == 4 ? (Real*)b.d_xr[1] : nullptr;
     A.pt_vg = (Real*)b.d_pt_vg;
     A.pt_lt = (Real*)b.d_pt_lt;
     A.edge_w = sizeof(Real) == 8 ? (Real*)b.d_edge_w : nullptr;
     A.edge_a = (Real*)b.d_edge_a;
+    A.jfact = sizeof(Real) == 4 && pb.intr.model == 0;
     A.edge_e[0] = sizeof(Real) == 4 ? (Real*)b.d_edge_e[0] : nullptr;
     A.edge_e[1] = sizeof(Real) == 4 ? (Real*)b.d_edge_e[1] : nullptr;
     A.cam_list = b.d_cam_list;
@@ -884,8 +988,7 @@ void HostStaging::release() {
 void window_batch_free(WindowBatch& b) {
     void* ptrs[] = {b.d_win, b.d_order, b.d_queue, b.d_cam_init, b.d_cam_free, b.d_pt_init, b.d_pt_free,
                     b.d_pt_eoff, b.d_edge_cam, b.d_edge_fc, b.d_edge_pt, b.d_edge_uv, b.d_x[0], b.d_x[1], b.d_pt_vg,
-                    b.d_pt_lt, b.d_edge_w, b.d_edge_a, b.d_edge_e[0], b.d_edge_e[1], b.d_cam_list, b.d_pairs,
-                    b.d_cam_out, b.d_pt_out,
+                    b.d_pt_lt, b.d_edge_w, b.d_edge_a, b.d_edge_e[0], b.d_edge_e[1], b.d_cam_list, b.d_pairs, b.d_edge_uvr, b.d_xr[0], b.d_xr[1], b.d_cam_out, b.d_pt_out,
                     b.d_trace, b.d_stats, b.d_debug, b.d_phase};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -989,6 +1092,9 @@ cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int prec
     ensure(&b.d_edge_e[1], precision == NAV_BA_MIXED ? rs * 2 * ne : 16);
     ensure(&b.d_cam_list, sizeof(int32_t) * ne);
     ensure(&b.d_pairs, sizeof(uint32_t) * npair);
+    ensure(&b.d_edge_uvr, precision == NAV_BA_MIXED ? rs * 2 * ne : 16);  // mixed form only
+    ensure(&b.d_xr[0], precision == NAV_BA_MIXED ? rs * 4 * np : 16);
+    ensure(&b.d_xr[1], precision == NAV_BA_MIXED ? rs * 4 * np : 16);
     ensure(&b.d_cam_out, sizeof(CamState) * nc);
     ensure(&b.d_pt_out, sizeof(double) * 4 * np);
     ensure(&b.d_trace, sizeof(double) * trace_stride * nw);
