@@ -404,6 +404,11 @@ def main():
         dt, ei, its, res_o = cpu_reference(sample, of, nth)
         cpu = {"value": ei / dt, "unit": UNIT, "cores": nth, "kind": "port",
                "sample": f"{len(sample)} windows x 10 LM iterations (FP64 oracle), one window per thread"}
+        # and on one core, as g2o runs by default (a smaller sample of the same windows)
+        one = sample[: max(1, len(sample) // 16)]
+        dt1, ei1, _, _ = cpu_reference(one, of, 1)
+        cpu["single_thread"] = {"value": ei1 / dt1, "unit": UNIT, "cores": 1,
+                                "sample": f"{len(one)} windows x 10 LM iterations (FP64 oracle)"}
         # "same final cost": both GPU forms against the FP64 oracle, per window
         oracle_diff = {
             name: max(abs(a.stats["final_cost"] - b.stats["final_cost"]) / b.stats["final_cost"]

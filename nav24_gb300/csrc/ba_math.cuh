@@ -29,6 +29,14 @@ NAVBA_HD Intr make_intr(const double* k8, int model) {
     return in;
 }
 
+// New radial coefficients (k1, k2), in both precisions.
+NAVBA_HD void set_radial(Intr& in, double k1, double k2) {
+    in.k1 = k1;
+    in.k2 = k2;
+    in.f[4] = (float)k1;
+    in.f[5] = (float)k2;
+}
+
 // The intrinsics in precision Real: the FP64 values, or their float copies (no conversion per use).
 template <class Real>
 struct IntrV {

@@ -9,6 +9,7 @@
 
 #include "../../include/nav_ba.h"
 #include "ba_math.cuh"
+#include "host_pool.hpp"
 #include "structure.hpp"
 
 namespace navba {
@@ -97,10 +98,12 @@ struct WindowLaunch {
     int32_t threads = 256;    // threads per CTA
 };
 
-// Pinned host buffers reused across calls (inputs staged for upload, outputs for download).
+// Host resources of a context reused across calls: pinned buffers (inputs staged for upload,
+// outputs for download) and the worker threads of the host-side passes.
 struct HostStaging {
     void* buf[16] = {};
     size_t cap[16] = {};
+    HostPool pool;
     void* get(int id, size_t bytes);  // grows buffer `id` to at least `bytes`; null on failure
     void release();
 };
@@ -128,7 +131,7 @@ cudaError_t window_batch_launch(PreparedBatch& pb, cudaStream_t stream, int prec
                                 WindowLaunch shape, double debug_lambda);
 
 // Print the per-phase cycle breakdown of the last launch to stderr (NAVBA_PHASE_TIMING=1).
-constexpr int kWinPhases = 10;
+constexpr int kWinPhases = 13;
 struct WindowLaunch;
 void window_phase_report(const PreparedBatch& pb, const WindowLaunch& shape, int precision);
 

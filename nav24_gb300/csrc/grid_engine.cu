@@ -1653,8 +1653,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             k_update_points<Real><<<pblocks, TB, 0, st>>>(A, D, lambda, d_bs, cur, d_part);
             scale += sum_part(pblocks, false);
             scale += dk[0] * (lambda * dk[0] + gk[0]) + dk[1] * (lambda * dk[1] + gk[1]);
-            A.intr.k1 = kcur[0] + dk[0];
-            A.intr.k2 = kcur[1] + dk[1];
+            set_radial(A.intr, kcur[0] + dk[0], kcur[1] + dk[1]);
             double chi_new = cost_of(cur ^ 1, true);
             if (e != cudaSuccess) return e;
             if (!ok) chi_new = DBL_MAX;
@@ -1679,8 +1678,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                 lambda *= nu;
                 nu *= 2;
                 ++out.rejected;
-                A.intr.k1 = kcur[0];
-                A.intr.k2 = kcur[1];
+                set_radial(A.intr, kcur[0], kcur[1]);
             }
             ++q;
         } while (rho < 0 && q < lm.max_trials);

@@ -170,7 +170,7 @@ nav_ba_status build_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, c
     pb.host_status.assign(n, NAV_BA_OK);
     std::vector<nav_ba_status> vst(n, NAV_BA_OK);
     std::vector<std::string> vwhy(n);
-    const int nth = std::max(1, std::min<int>(n / 8, (int)std::thread::hardware_concurrency()));
+    const int nth = HostPool::tasks_for(n, 8);
     auto work = [&](int t) {
         for (int i = t; i < n; i += nth) {
             nav_ba_status s = validate_problem(&probs[i], &vwhy[i]);
@@ -194,13 +194,7 @@ nav_ba_status build_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, c
             if (probs[i].n_cams == 0 || h.ne == 0) pb.host_status[i] = NAV_BA_EMPTY;
         }
     };
-    if (nth == 1) {
-        work(0);
-    } else {
-        std::vector<std::thread> ths;
-        for (int t = 0; t < nth; ++t) ths.emplace_back(work, t);
-        for (auto& th : ths) th.join();
-    }
+    ctx->stg.pool.run(nth, work);
     for (int i = 0; i < n; ++i)
         if (vst[i] != NAV_BA_OK) return set_err(ctx, vst[i], "problem " + std::to_string(i) + ": " + vwhy[i]);
     for (int i = 0; i < n; ++i)
@@ -275,17 +269,10 @@ nav_ba_status download_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n
         if (r->cost_trace)
             for (int k = 0; k <= s.iterations_done; ++k) r->cost_trace[k] = trace[(size_t)i * b.trace_stride + k];
     };
-    const int nth = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), n / 8));
-    if (nth <= 1) {
-        for (int i = 0; i < n; ++i) one(i);
-    } else {
-        std::vector<std::thread> th;
-        for (int t = 0; t < nth; ++t)
-            th.emplace_back([&, t] {
-                for (int i = (int)((long long)n * t / nth); i < (int)((long long)n * (t + 1) / nth); ++i) one(i);
-            });
-        for (auto& x : th) x.join();
-    }
+    const int nth = HostPool::tasks_for(n, 8);
+    ctx->stg.pool.run(nth, [&](int t) {
+        for (int i = (int)((long long)n * t / nth); i < (int)((long long)n * (t + 1) / nth); ++i) one(i);
+    });
     for (int i = 0; i < n; ++i)
         if (st_out[i] != NAV_BA_OK) return (nav_ba_status)st_out[i];
     return NAV_BA_OK;

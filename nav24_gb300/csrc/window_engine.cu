@@ -65,7 +65,7 @@ struct SmemHead {
 
 // Offsets of the dynamic part of shared memory (after SmemHead), shared by host and device.
 struct Dyn {
-    size_t cams, camr, camd, camdel, dcl, dclr, S, bs, rinv, total;
+    size_t cams, camr, camd, camdel, dcl, dclr, S, bs, rinv, s32, v32, total;
 };
 
 NAVBA_HD size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -82,6 +82,10 @@ NAVBA_HD Dyn dyn_layout(int max_m, int max_ncam, int real_size) {
     d.S = o;    o = align16(o + sizeof(double) * ((size_t)max_m * (max_m + 1) / 2));
     d.bs = o;   o = align16(o + sizeof(double) * max_m);
     d.rinv = o; o = align16(o + sizeof(double) * max_m);
+    // mixed form: the FP32 factor of S and three FP32 vectors (1/L_jj, solution, correction)
+    const bool f32 = real_size == 4;
+    d.s32 = o;  o = align16(o + (f32 ? sizeof(float) * ((size_t)max_m * (max_m + 1) / 2) : 0));
+    d.v32 = o;  o = align16(o + (f32 ? sizeof(float) * 3 * max_m : 0));
     d.total = o;
     return d;
 }
@@ -278,12 +282,19 @@ __device__ double linearize_cameras(const WinArgs<Real>& A, const CC& c, const W
         Real u[27];
 #pragma unroll
         for (int k = 0; k < 27; ++k) u[k] = Real(0);
+        // the list position's edge is loaded two rounds ahead and its point one round ahead, so a
+        // round waits for one memory latency instead of three dependent ones
+        int e_n = c.lane < cnt ? list[c.lane] : 0;
+        int gp_n = c.lane < cnt ? D.pt0 + A.edge_pt[e_n] : 0;
+        int e_nn = c.lane + 32 < cnt ? list[c.lane + 32] : 0;
         for (int i = c.lane; i < cnt; i += 32) {
-            const int e = list[i];
-            const int gp = D.pt0 + A.edge_pt[e];
+            const int e = e_n, gp = gp_n;
             Real Xr[3], z[2];
             point_real(X, XR, gp, Xr);
             obs_real(A, e, z);
+            e_n = e_nn;
+            if (i + 32 < cnt) gp_n = D.pt0 + A.edge_pt[e_n];
+            if (i + 64 < cnt) e_nn = list[i + 64];
             EdgeLin<Real> L;
             edge_linearize<Real>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta, L);
             const Real w = L.w;
@@ -444,16 +455,17 @@ __device__ void schur_blocks(const WinArgs<Real>& A, const CC& c, const WinDesc&
 // One reciprocal square root per column (FP64 divides and square roots are long instruction
 // sequences on GB300's FP64 pipe, so the column is scaled by a product); every FP64 product is
 // made by one lane only (the pipe's throughput is counted in lanes).
-__device__ bool smem_cholesky(double* S, double* rinv, int m, SmemHead& s) {
+template <class T>
+__device__ bool smem_cholesky(T* S, T* rinv, int m, SmemHead& s) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     auto pivot = [&](int j) {  // L_jj and rinv[j]; a pivot that is not positive and finite fails
-        const double d = S[tri(j, j)];
-        if (!(d > 0.0) || !isfinite(d)) {
+        const T d = S[tri(j, j)];
+        if (!(d > T(0)) || !isfinite(d)) {
             s.ok = 0;
-            S[tri(j, j)] = 1.0;
-            rinv[j] = 1.0;
+            S[tri(j, j)] = T(1);
+            rinv[j] = T(1);
         } else {
-            const double r = rsqrt(d);
+            const T r = rsqrt(d);
             S[tri(j, j)] = d * r;
             rinv[j] = r;
         }
@@ -464,12 +476,12 @@ __device__ bool smem_cholesky(double* S, double* rinv, int m, SmemHead& s) {
     }
     __syncthreads();
     for (int j = 0; j < m; ++j) {
-        const double ri = rinv[j];
+        const T ri = rinv[j];
         for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) S[tri(i, j)] *= ri;
         __syncthreads();
         for (int i = j + 1 + wid; i < m; i += nw) {
-            const double lij = S[tri(i, j)];
-            double* Si = S + tri(i, 0);
+            const T lij = S[tri(i, j)];
+            T* Si = S + tri(i, 0);
             for (int k = j + 1 + lane; k <= i; k += 32) Si[k] -= lij * S[tri(k, j)];
             if (i == j + 1 && lane == 0) pivot(j + 1);  // lane 0 updated S[j+1][j+1] itself
         }
@@ -507,6 +519,94 @@ __device__ void smem_chol_solve(const double* L, const double* rinv, int m, doub
     }
 }
 
+// Solve L L^T x = b in place in FP32 by warp 0 alone (no block barriers): lane l holds rows
+// l + 32 q, q < kSolveRows (m <= 32 kSolveRows); the owner of row j finalizes x_j and broadcasts it.
+constexpr int kSolveRows = 5;
+static_assert(6 * kWinMaxFreeCams <= 32 * kSolveRows, "reduced system larger than the warp solve");
+__device__ void warp_chol_solve32(const float* L, const float* rinv, int m, float* x) {
+    if (threadIdx.x >= 32) return;
+    const int lane = threadIdx.x;
+    float xr[kSolveRows];
+#pragma unroll
+    for (int q = 0; q < kSolveRows; ++q) xr[q] = lane + 32 * q < m ? x[lane + 32 * q] : 0.f;
+#pragma unroll
+    for (int q = 0; q < kSolveRows; ++q) {
+        for (int jj = 0; jj < 32; ++jj) {
+            const int j = 32 * q + jj;
+            if (j >= m) break;
+            if (lane == jj) xr[q] *= rinv[j];
+            const float xj = __shfl_sync(kFull, xr[q], jj);
+#pragma unroll
+            for (int qq = q; qq < kSolveRows; ++qq) {
+                const int i = lane + 32 * qq;
+                if (i > j && i < m) xr[qq] -= L[tri(i, j)] * xj;
+            }
+        }
+    }
+#pragma unroll
+    for (int q = kSolveRows - 1; q >= 0; --q) {
+        for (int jj = 31; jj >= 0; --jj) {
+            const int j = 32 * q + jj;
+            if (j >= m) continue;
+            if (lane == jj) xr[q] *= rinv[j];
+            const float xj = __shfl_sync(kFull, xr[q], jj);
+            const float* Lj = L + tri(j, 0);
+#pragma unroll
+            for (int qq = 0; qq <= q; ++qq) {
+                const int i = lane + 32 * qq;
+                if (i < j) xr[qq] -= Lj[i] * xj;
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < kSolveRows; ++q)
+        if (lane + 32 * q < m) x[lane + 32 * q] = xr[q];
+}
+
+// Mixed form: solve S x = b (x into b) with the Cholesky factor of S rounded to FP32 and one
+// refinement step against the FP64 S: x0 from the FP32 factor, r = b - S x0 in FP64, x = x0 +
+// (the FP32 factor's solution of r).  S's entries are FP32 sums already, so the FP32 factor adds
+// an error of the same order, which the refinement step removes.  When the FP32 factorization
+// meets a pivot that is not positive, S is factored in FP64 (S is kept intact for this).
+// Returns false if S is not positive definite in FP64 either.  mark(k): phase-timer marks.
+template <class Mark>
+__device__ bool solve_s_mixed(double* S, double* rinv, float* S32, float* v32, int m, SmemHead& s, double* b,
+                              Mark&& mark) {
+    float* r32 = v32;           // 1/L_jj
+    float* x32 = v32 + m;       // x0
+    float* y32 = v32 + 2 * m;   // correction
+    for (int k = threadIdx.x; k < m * (m + 1) / 2; k += blockDim.x) S32[k] = (float)S[k];
+    for (int k = threadIdx.x; k < m; k += blockDim.x) x32[k] = (float)b[k];
+    __syncthreads();
+    const bool ok32 = smem_cholesky<float>(S32, r32, m, s);
+    __syncthreads();  // every thread has read the outcome before s.ok is used again
+    mark(10);
+    if (!ok32) {
+        if (!smem_cholesky<double>(S, rinv, m, s)) return false;
+        smem_chol_solve(S, rinv, m, b);
+        return true;
+    }
+    warp_chol_solve32(S32, r32, m, x32);
+    __syncthreads();
+    mark(11);
+    // r = b - S x0, thread per row (row i of the packed lower S, then column i below it)
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        double acc = b[i];
+        const double* Si = S + tri(i, 0);
+        for (int k = 0; k <= i; ++k) acc -= Si[k] * (double)x32[k];
+        for (int k = i + 1; k < m; ++k) acc -= S[tri(k, i)] * (double)x32[k];
+        y32[i] = (float)acc;
+    }
+    __syncthreads();
+    mark(12);
+    warp_chol_solve32(S32, r32, m, y32);
+    __syncthreads();
+    mark(11);
+    for (int k = threadIdx.x; k < m; k += blockDim.x) b[k] = (double)x32[k] + (double)y32[k];
+    __syncthreads();
+    return true;
+}
+
 // Phase timer: thread 0 of rank 0 adds the SM cycles since the previous mark to phase `ph`.
 struct PhaseClock {
     unsigned long long* acc;
@@ -541,6 +641,8 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
     double* S = reinterpret_cast<double*>(smem + dl.S);
     double* bs = reinterpret_cast<double*>(smem + dl.bs);
     double* rinv = reinterpret_cast<double*>(smem + dl.rinv);
+    float* S32 = reinterpret_cast<float*>(smem + dl.s32);
+    float* v32 = reinterpret_cast<float*>(smem + dl.v32);
     WinStats* st = A.stats + w;
     double* trace = A.trace + (long long)w * A.trace_stride;
     const bool mixed = sizeof(Real) == 4;
@@ -623,10 +725,14 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
                     return;
                 }
                 if (c.rank == 0) {
-                    bool okc = smem_cholesky(S, rinv, m, s) && r0.x == 0.0;
-                    if (okc) {
-                        smem_chol_solve(S, rinv, m, bs);
+                    bool okc;
+                    if (mixed) {
+                        okc = solve_s_mixed(S, rinv, S32, v32, m, s, bs, [&](int k) { pc.mark(k); }) && r0.x == 0.0;
                     } else {
+                        okc = smem_cholesky<double>(S, rinv, m, s) && r0.x == 0.0;
+                        if (okc) smem_chol_solve(S, rinv, m, bs);
+                    }
+                    if (!okc) {
                         for (int k = threadIdx.x; k < m; k += blockDim.x) bs[k] = 0.0;
                     }
                     __syncthreads();
@@ -997,21 +1103,14 @@ void window_batch_free(WindowBatch& b) {
 
 namespace {
 
-// Run fn(i) for i in [0, n) on up to hardware_concurrency threads (contiguous chunks).
+// Run fn(i) for i in [0, n) on the context's host workers (contiguous chunks).
 template <class Fn>
-void parallel_for(int n, Fn fn) {
-    const int nth = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), n / 4));
-    if (nth <= 1) {
-        for (int i = 0; i < n; ++i) fn(i);
-        return;
-    }
-    std::vector<std::thread> th;
-    for (int t = 0; t < nth; ++t)
-        th.emplace_back([&, t] {
-            const int lo = (int)((long long)n * t / nth), hi = (int)((long long)n * (t + 1) / nth);
-            for (int i = lo; i < hi; ++i) fn(i);
-        });
-    for (auto& x : th) x.join();
+void parallel_for(HostPool& pool, int n, Fn fn) {
+    const int nt = HostPool::tasks_for(n, 4);
+    pool.run(nt, [&](int t) {
+        const int lo = (int)((long long)n * t / nt), hi = (int)((long long)n * (t + 1) / nt);
+        for (int i = lo; i < hi; ++i) fn(i);
+    });
 }
 
 }  // namespace
@@ -1136,7 +1235,7 @@ cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int prec
     }
     std::copy(pb.desc.begin(), pb.desc.end(), desc);
     std::copy(order.begin(), order.end(), ord);
-    parallel_for((int)nw, [&](int i) {
+    parallel_for(stg.pool, (int)nw, [&](int i) {
         const HostWindow& h = pb.host[i];
         const WinDesc& d = pb.desc[i];
         std::copy(h.cam.begin(), h.cam.end(), cam + d.cam0);
@@ -1179,7 +1278,7 @@ void window_phase_report(const PreparedBatch& pb, const WindowLaunch& shape, int
     if (cudaMemcpy(h, pb.dev.d_phase, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return;
     static const char* names[kWinPhases] = {"init+lists", "initial cost", "linearize points", "linearize cameras",
                                             "schur points", "schur blocks", "cholesky", "update", "trial cost",
-                                            "outputs"};
+                                            "outputs", "  chol: f32 factor", "  chol: f32 solves", "  chol: refine"};
     unsigned long long tot = 0;
     for (int k = 0; k < kWinPhases; ++k) tot += h[k];
     fprintf(stderr, "[navba phases] precision=%d cluster=%d threads=%d total=%llu cycles (rank-0 CTAs, summed)\n",
