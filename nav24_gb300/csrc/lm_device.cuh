@@ -463,6 +463,7 @@ __device__ double2 update_points_dcost(const WinArgs<Real>& A, const CC& c, cons
     const Real fx = (Real)A.intr.fx, fy = (Real)A.intr.fy;
     const bool robust = A.lm.robust != 0;
     const Real hd = (Real)A.lm.huber_delta, hd2 = hd * hd;
+    const Real lam = (Real)lambda;
     double sc = 0.0;
     Real ks = Real(0), kc = Real(0);
     for (int p = c.gt; p < D.npt; p += c.CT) {
@@ -484,8 +485,9 @@ __device__ double2 update_points_dcost(const WinArgs<Real>& A, const CC& c, cons
             store_trial_point(Xc, Xt, XRt, gp, d0, d1, d2);
             Real vg[12];
             Rec<Real>::load12(A.pt_vg + 12LL * gp, vg);
-            sc += (double)d0 * (lambda * (double)d0 + (double)vg[6]) + (double)d1 * (lambda * (double)d1 + (double)vg[7]) +
-                  (double)d2 * (lambda * (double)d2 + (double)vg[8]);
+            // the point's model-decrease term in Real (its relative error is Real's; the terms are
+            // summed in FP64)
+            sc += (double)(d0 * (lam * d0 + vg[6]) + d1 * (lam * d1 + vg[7]) + d2 * (lam * d2 + vg[8]));
         }
         Real X[3];
         point_real(Xc, XRc, gp, X);

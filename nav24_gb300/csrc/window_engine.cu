@@ -198,13 +198,20 @@ __device__ void build_lists(const WinArgs<Real>& A, CC& c, const WinDesc& D) {
         const int ca = s.fcam[a];
         const int* list = A.cam_list + D.e0 + s.loff[ca];
         const int cnt = s.lcnt[ca];
+        // the list entry's edge is loaded a round ahead; the point's edges' free cameras four at a time
+        int ei_n = c.lane < cnt ? list[c.lane] : 0;
         for (int i = c.lane; i < cnt; i += 32) {
-            const int gp = D.pt0 + A.edge_pt[list[i]];
+            const int gp = D.pt0 + A.edge_pt[ei_n];
+            if (i + 32 < cnt) ei_n = list[i + 32];
             if (A.pt_free[gp] < 0) continue;
-            const int e1 = A.pt_eoff[gp + 1];
-            for (int ej = A.pt_eoff[gp]; ej < e1; ++ej) {
-                const int bb = A.edge_fc[ej];
-                if (bb >= 0 && bb <= a) atomicAdd(&hist[bb], 1);  // integer counts: order-independent
+            const int e0 = A.pt_eoff[gp], e1 = A.pt_eoff[gp + 1];
+            for (int ej = e0; ej < e1; ej += 4) {
+                int bb[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) bb[u] = ej + u < e1 ? A.edge_fc[ej + u] : -1;
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (bb[u] >= 0 && bb[u] <= a) atomicAdd(&hist[bb[u]], 1);  // integer counts: order-independent
             }
         }
         __syncwarp();
@@ -267,6 +274,16 @@ __device__ void build_lists(const WinArgs<Real>& A, CC& c, const WinDesc& D) {
     csync();
 }
 
+// v[k] for a runtime k < N (0 otherwise) from a register array, by selects (no local-memory copy).
+template <int N, class Real>
+__device__ __forceinline__ Real lane_value(const Real* v, int k) {
+    Real o = Real(0);
+#pragma unroll
+    for (int x = 0; x < N; ++x)
+        if (x == k) o = v[x];
+    return o;
+}
+
 // Camera-major linearization: U_c, g_c (warp per free camera) into rank 0; returns max |diag U|.
 template <class Real>
 __device__ double linearize_cameras(const WinArgs<Real>& A, const CC& c, const WinDesc& D, const Real* camr,
@@ -310,17 +327,22 @@ __device__ double linearize_cameras(const WinArgs<Real>& A, const CC& c, const W
         for (int k = 0; k < 27; ++k)
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) u[k] += __shfl_xor_sync(kFull, u[k], o);
+        // lane k widens value k: one FP64 conversion per warp, not one per value
+        const Real uk = lane_value<27>(u, c.lane);
+        if (c.lane < 27) c.s0->U[a][c.lane] = (double)uk;
+        Real dm = Real(0);
 #pragma unroll
-        for (int k = 0; k < 27; ++k)
-            if ((k & 31) == c.lane) c.s0->U[a][k] = (double)u[k];
-#pragma unroll
-        for (int r = 0; r < 6; ++r) mx = fmax(mx, fabs((double)u[tri(r, r)]));
+        for (int r = 0; r < 6; ++r) dm = fmax(dm, fabs(u[tri(r, r)]));
+        mx = fmax(mx, (double)dm);
     }
     return mx;
 }
 
 // Sums one S block's lane partials over the warp and writes -sum (plus U_a + lambda I on the
-// diagonal) into rank 0's packed S, and b'_a = g'_a - sum A t on the diagonal.
+// diagonal) into rank 0's packed S, and b'_a = g'_a - sum A t on the diagonal.  After the butterfly
+// every lane holds every sum; lane l writes entries l and l + 32, so each FP64 operation is one warp
+// instruction with all lanes active (GB300's FP64 pipe costs 16 cycles per warp instruction, however
+// few lanes are active).
 template <class Real>
 __device__ __forceinline__ void write_block(const CC& c, int a, int b, Real* acc, Real* accb, double lambda) {
 #pragma unroll
@@ -334,21 +356,22 @@ __device__ __forceinline__ void write_block(const CC& c, int a, int b, Real* acc
             for (int o = 16; o > 0; o >>= 1) accb[k] += __shfl_xor_sync(kFull, accb[k], o);
     }
 #pragma unroll
-    for (int k = 0; k < 36; ++k) {
-        if ((k & 31) != c.lane) continue;
+    for (int rnd = 0; rnd < 2; ++rnd) {
+        const int k = c.lane + 32 * rnd;
+        const Real vk = lane_value<36>(acc, k);
         const int r = k / 6, q = k % 6;
-        if (a == b && q > r) continue;
-        double v = -(double)acc[k];
-        if (a == b) {
-            v += c.s0->U[a][tri(r, q)];
-            if (r == q) v += lambda;
+        if (k < 36 && !(a == b && q > r)) {
+            double v = -(double)vk;
+            if (a == b) {
+                v += c.s0->U[a][tri(r, q)];
+                if (r == q) v += lambda;
+            }
+            c.S0[tri(6 * a + r, 6 * b + q)] = v;
         }
-        c.S0[tri(6 * a + r, 6 * b + q)] = v;
     }
-    if (a == b && c.lane < 6) {
-#pragma unroll
-        for (int k = 0; k < 6; ++k)
-            if (k == c.lane) c.bs0[6 * a + k] = c.s0->U[a][21 + k] - (double)accb[k];
+    if (a == b) {
+        const Real bk = lane_value<6>(accb, c.lane);
+        if (c.lane < 6) c.bs0[6 * a + c.lane] = c.s0->U[a][21 + c.lane] - (double)bk;
     }
 }
 
@@ -519,6 +542,86 @@ __device__ void smem_chol_solve(const double* L, const double* rinv, int m, doub
     }
 }
 
+// FP32 Cholesky (LL^T) of packed lower S (m x m) in shared memory, blocked in panels of kNB columns:
+// warp 0 factors the panel's diagonal block (row r in lane r, shuffles) and solves the rows below
+// it against that block; then every warp applies the panel's rank-kNB update to the trailing
+// matrix.  Two block barriers per panel instead of two per column.  rinv receives 1/L_jj; a pivot
+// that is not positive and finite fails the factorization (it is replaced by 1 so the pass ends).
+constexpr int kNB = 8;
+__device__ bool smem_cholesky_blocked(float* S, float* rinv, int m, SmemHead& s) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (threadIdx.x == 0) s.ok = 1;
+    __syncthreads();
+    for (int p0 = 0; p0 < m; p0 += kNB) {
+        const int pb = min(kNB, m - p0);
+        if (wid == 0) {
+            float d[kNB];  // lane r < pb: row p0 + r of the diagonal block, columns 0..r
+#pragma unroll
+            for (int c2 = 0; c2 < kNB; ++c2) d[c2] = (lane < pb && c2 <= lane) ? S[tri(p0 + lane, p0 + c2)] : 0.f;
+            bool bad = false;
+#pragma unroll
+            for (int cc = 0; cc < kNB; ++cc) {
+                if (cc >= pb) break;
+                const float dc = __shfl_sync(kFull, d[cc], cc);
+                const bool colbad = !(dc > 0.f) || !isfinite(dc);
+                const float r = colbad ? 1.f : rsqrtf(dc);
+                bad = bad || colbad;
+                if (lane == cc) d[cc] = colbad ? 1.f : dc * r;
+                else if (lane > cc) d[cc] *= r;
+                if (lane == 0) rinv[p0 + cc] = r;
+#pragma unroll
+                for (int j = cc + 1; j < kNB; ++j) {
+                    const float ljc = __shfl_sync(kFull, d[cc], j);
+                    if (lane >= j) d[j] -= d[cc] * ljc;
+                }
+            }
+            if (bad && lane == 0) s.ok = 0;
+#pragma unroll
+            for (int c2 = 0; c2 < kNB; ++c2)
+                if (lane < pb && c2 <= lane) S[tri(p0 + lane, p0 + c2)] = d[c2];
+            __syncwarp();
+            // rows below the block: x_c = (x_c - sum_{c' < c} x_c' L_cc') / L_cc
+            for (int i = p0 + pb + lane; i < m; i += 32) {
+                float* Si = S + tri(i, p0);
+                float x[kNB];
+#pragma unroll
+                for (int c2 = 0; c2 < kNB; ++c2) x[c2] = c2 < pb ? Si[c2] : 0.f;
+#pragma unroll
+                for (int cc = 0; cc < kNB; ++cc) {
+                    if (cc >= pb) break;
+                    const float* Dc = S + tri(p0 + cc, p0);
+                    float v = x[cc];
+#pragma unroll
+                    for (int c2 = 0; c2 < cc; ++c2) v -= x[c2] * Dc[c2];
+                    x[cc] = v * rinv[p0 + cc];
+                }
+#pragma unroll
+                for (int c2 = 0; c2 < kNB; ++c2)
+                    if (c2 < pb) Si[c2] = x[c2];
+            }
+        }
+        __syncthreads();
+        const int t0 = p0 + pb;
+        for (int i = t0 + wid; i < m; i += nw) {
+            const float* Li = S + tri(i, p0);
+            float li[kNB];
+#pragma unroll
+            for (int c2 = 0; c2 < kNB; ++c2) li[c2] = c2 < pb ? Li[c2] : 0.f;
+            float* Si = S + tri(i, 0);
+            for (int j = t0 + lane; j <= i; j += 32) {
+                const float* Lj = S + tri(j, p0);
+                float acc = Si[j];
+#pragma unroll
+                for (int c2 = 0; c2 < kNB; ++c2)
+                    if (c2 < pb) acc -= li[c2] * Lj[c2];
+                Si[j] = acc;
+            }
+        }
+        __syncthreads();
+    }
+    return s.ok != 0;
+}
+
 // Solve L L^T x = b in place in FP32 by warp 0 alone (no block barriers): lane l holds rows
 // l + 32 q, q < kSolveRows (m <= 32 kSolveRows); the owner of row j finalizes x_j and broadcasts it.
 constexpr int kSolveRows = 5;
@@ -578,7 +681,7 @@ __device__ bool solve_s_mixed(double* S, double* rinv, float* S32, float* v32, i
     for (int k = threadIdx.x; k < m * (m + 1) / 2; k += blockDim.x) S32[k] = (float)S[k];
     for (int k = threadIdx.x; k < m; k += blockDim.x) x32[k] = (float)b[k];
     __syncthreads();
-    const bool ok32 = smem_cholesky<float>(S32, r32, m, s);
+    const bool ok32 = smem_cholesky_blocked(S32, r32, m, s);
     __syncthreads();  // every thread has read the outcome before s.ok is used again
     mark(10);
     if (!ok32) {
@@ -589,12 +692,16 @@ __device__ bool solve_s_mixed(double* S, double* rinv, float* S32, float* v32, i
     warp_chol_solve32(S32, r32, m, x32);
     __syncthreads();
     mark(11);
-    // r = b - S x0, thread per row (row i of the packed lower S, then column i below it)
+    // r = b - S x0, thread per row (row i of the packed lower S, then column i below it); x0 is
+    // widened to FP64 once, into rinv (unused on this path)
+    double* x0 = rinv;
+    for (int k = threadIdx.x; k < m; k += blockDim.x) x0[k] = (double)x32[k];
+    __syncthreads();
     for (int i = threadIdx.x; i < m; i += blockDim.x) {
         double acc = b[i];
         const double* Si = S + tri(i, 0);
-        for (int k = 0; k <= i; ++k) acc -= Si[k] * (double)x32[k];
-        for (int k = i + 1; k < m; ++k) acc -= S[tri(k, i)] * (double)x32[k];
+        for (int k = 0; k <= i; ++k) acc -= Si[k] * x0[k];
+        for (int k = i + 1; k < m; ++k) acc -= S[tri(k, i)] * x0[k];
         y32[i] = (float)acc;
     }
     __syncthreads();
@@ -602,7 +709,7 @@ __device__ bool solve_s_mixed(double* S, double* rinv, float* S32, float* v32, i
     warp_chol_solve32(S32, r32, m, y32);
     __syncthreads();
     mark(11);
-    for (int k = threadIdx.x; k < m; k += blockDim.x) b[k] = (double)x32[k] + (double)y32[k];
+    for (int k = threadIdx.x; k < m; k += blockDim.x) b[k] = x0[k] + (double)y32[k];
     __syncthreads();
     return true;
 }
