@@ -120,9 +120,8 @@ __global__ void k_lin_cams(WinArgs<Real> A, const int4* items, int n_items, cons
         for (int k = 0; k < 27; ++k)
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) u[k] += __shfl_xor_sync(kFullG, u[k], o);
-#pragma unroll
-        for (int k = 0; k < 27; ++k)
-            if ((k & 31) == c.lane) upart[28LL * it + k] = (double)u[k];
+        const Real uk = lane_value<27>(u, c.lane);  // one FP64 conversion per warp, not per value
+        if (c.lane < 27) upart[28LL * it + c.lane] = (double)uk;
     }
 }
 
@@ -190,22 +189,25 @@ __global__ void k_schur_blocks(WinArgs<Real> A, const int2* blocks, const int32_
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) accb[k] += __shfl_xor_sync(kFullG, accb[k], o);
         }
+        // every lane holds every sum: lane l writes entries l and l + 32, so each FP64 operation is
+        // one warp instruction with all lanes active (the FP64 pipe is charged per warp instruction)
 #pragma unroll
-        for (int k = 0; k < 36; ++k) {
-            if ((k & 31) != c.lane) continue;
+        for (int rnd = 0; rnd < 2; ++rnd) {
+            const int k = c.lane + 32 * rnd;
+            const Real vk = lane_value<36>(acc, k);
             const int r = k / 6, q = k % 6;
-            if (a == b && q > r) continue;
-            double v = -(double)acc[k];
-            if (a == b) {
-                v += U[28LL * a + tri(r, q)];
-                if (r == q) v += lambda;
+            if (k < 36 && !(a == b && q > r)) {
+                double v = -(double)vk;
+                if (a == b) {
+                    v += U[28LL * a + tri(r, q)];
+                    if (r == q) v += lambda;
+                }
+                S[(size_t)(6 * a + r) * m + 6 * b + q] = v;
             }
-            S[(size_t)(6 * a + r) * m + 6 * b + q] = v;
         }
-        if (a == b && c.lane < 6) {
-#pragma unroll
-            for (int k = 0; k < 6; ++k)
-                if (k == c.lane) bs[6 * a + k] = U[28LL * a + 21 + k] - (double)accb[k];
+        if (a == b) {
+            const Real bk = lane_value<6>(accb, c.lane);
+            if (c.lane < 6) bs[6 * a + c.lane] = U[28LL * a + 21 + c.lane] - (double)bk;
         }
     }
 }
@@ -224,21 +226,22 @@ __global__ void k_schur_blocks(WinArgs<Real> A, const int2* blocks, const int32_
 // is sized to the largest column's work (a grid synchronization costs more with more blocks).
 // Every block runs the same loops, so all reach every synchronization; a non-positive pivot is
 // replaced by 1 and reported through ok.
-__device__ void factor_diag_tile(double (*tk)[kTile + 1], double* rv, const double* S, int m, int k0, int kb, int& bad) {
+template <class T>
+__device__ void factor_diag_tile(T (*tk)[kTile + 1], T* rv, const T* S, int m, int k0, int kb, int& bad) {
     const int tid = threadIdx.x, nth = blockDim.x;
     for (int idx = tid; idx < kTile * kTile; idx += nth) {
         const int i = idx / kTile, j = idx % kTile;
-        tk[i][j] = (i < kb && j <= i) ? S[(size_t)(k0 + i) * m + k0 + j] : 0.0;
+        tk[i][j] = (i < kb && j <= i) ? S[(size_t)(k0 + i) * m + k0 + j] : T(0);
     }
     __syncthreads();
     for (int j = 0; j < kb; ++j) {
         if (tid == 0) {
-            const double d = tk[j][j];
-            double r;
-            if (!(d > 0.0) || !isfinite(d)) {
+            const T d = tk[j][j];
+            T r;
+            if (!(d > T(0)) || !isfinite(d)) {
                 bad = 1;
-                r = 1.0;
-                tk[j][j] = 1.0;
+                r = T(1);
+                tk[j][j] = T(1);
             } else {
                 r = rsqrt(d);
                 tk[j][j] = d * r;
@@ -257,14 +260,14 @@ __device__ void factor_diag_tile(double (*tk)[kTile + 1], double* rv, const doub
     }
 }
 
-__global__ void __launch_bounds__(256) k_cholesky_coop(double* S, int m, const int32_t* pan_off, const int32_t* pan_row,
-                                                       const int32_t* tr_off, const int2* tr_ij, double* rinv,
-                                                       int32_t* ok) {
+template <class T>
+__global__ void __launch_bounds__(256) k_cholesky_coop(T* S, int m, const int32_t* pan_off, const int32_t* pan_row,
+                                                       const int32_t* tr_off, const int2* tr_ij, T* rinv, int32_t* ok) {
     cg::grid_group grid = cg::this_grid();
-    __shared__ double tk[kTile][kTile + 1];
-    __shared__ double ta[kTile][kTile + 1];
-    __shared__ double tb[kTile][kTile + 1];
-    __shared__ double rv[kTile];
+    __shared__ T tk[kTile][kTile + 1];
+    __shared__ T ta[kTile][kTile + 1];
+    __shared__ T tb[kTile][kTile + 1];
+    __shared__ T rv[kTile];
     __shared__ int sbad;
     const int tid = threadIdx.x, nth = blockDim.x, nb = gridDim.x, bid = blockIdx.x;
     const int nt = (m + kTile - 1) / kTile;
@@ -281,13 +284,13 @@ __global__ void __launch_bounds__(256) k_cholesky_coop(double* S, int m, const i
                 __syncthreads();
                 for (int idx = tid; idx < kTile * kTile; idx += nth) {
                     const int i = idx / kTile, j = idx % kTile;
-                    ta[i][j] = (i < ib && j < kb) ? S[(size_t)(i0 + i) * m + k0 + j] : 0.0;
+                    ta[i][j] = (i < ib && j < kb) ? S[(size_t)(i0 + i) * m + k0 + j] : T(0);
                 }
                 __syncthreads();
                 if (tid < ib) {
                     // x_c = (a_c - sum_{j<c} x_j L_cj) / L_cc; the sum in four independent partial sums
                     for (int cc = 0; cc < kb; ++cc) {
-                        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+                        T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
                         int j = 0;
                         for (; j + 3 < cc; j += 4) {
                             s0 += ta[tid][j] * tk[cc][j];
@@ -325,13 +328,13 @@ __global__ void __launch_bounds__(256) k_cholesky_coop(double* S, int m, const i
             __syncthreads();
             for (int idx = tid; idx < kTile * kTile; idx += nth) {
                 const int i = idx / kTile, j = idx % kTile;
-                tb[i][j] = (i < jb && j < kb) ? S[(size_t)(j0 + i) * m + k0 + j] : 0.0;
-                if (i < 8) ta[i][j] = (r0 + i < ib && j < kb) ? S[(size_t)(i0 + r0 + i) * m + k0 + j] : 0.0;
+                tb[i][j] = (i < jb && j < kb) ? S[(size_t)(j0 + i) * m + k0 + j] : T(0);
+                if (i < 8) ta[i][j] = (r0 + i < ib && j < kb) ? S[(size_t)(i0 + r0 + i) * m + k0 + j] : T(0);
             }
             __syncthreads();
             const int r = tid / kTile, c = tid % kTile;  // 256 threads: 8 rows x 32 columns
             if (r < 8 && r0 + r < ib && c < jb && !(I == J && c > r0 + r)) {
-                double sum = 0.0;
+                T sum = T(0);
 #pragma unroll 8
                 for (int t = 0; t < kTile; ++t) sum += ta[r][t] * tb[c][t];
                 S[(size_t)(i0 + r0 + r) * m + j0 + c] -= sum;
@@ -346,18 +349,19 @@ __global__ void __launch_bounds__(256) k_cholesky_coop(double* S, int m, const i
 // warp 0 solves the diagonal tile; the rows below (those whose tile row reaches column K) are
 // spread over the warps with the lanes over the tile's columns, so every load of L is a
 // contiguous 256-byte row segment; sums are shuffle trees and a fixed-order sum over warps.
-__global__ void k_chol_solve(const double* L, int m, const int32_t* tfirst, const double* rinv, double* x) {
-    __shared__ double red[32][kTile];
-    __shared__ double dt[kTile][kTile + 1];  // the diagonal tile, staged for the serial chain
-    __shared__ double dr[kTile];
+template <class T>
+__global__ void k_chol_solve(const T* L, int m, const int32_t* tfirst, const T* rinv, T* x) {
+    __shared__ T red[32][kTile];
+    __shared__ T dt[kTile][kTile + 1];  // the diagonal tile, staged for the serial chain
+    __shared__ T dr[kTile];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
     const int nt = (m + kTile - 1) / kTile;
     auto stage = [&](int k0, int kb) {
         for (int idx = tid; idx < kTile * kTile; idx += blockDim.x) {
             const int i = idx / kTile, j = idx % kTile;
-            dt[i][j] = (i < kb && j < kb) ? L[(size_t)(k0 + i) * m + k0 + j] : 0.0;
+            dt[i][j] = (i < kb && j < kb) ? L[(size_t)(k0 + i) * m + k0 + j] : T(0);
         }
-        for (int j = tid; j < kTile; j += blockDim.x) dr[j] = j < kb ? rinv[k0 + j] : 1.0;
+        for (int j = tid; j < kTile; j += blockDim.x) dr[j] = j < kb ? rinv[k0 + j] : T(1);
         __syncthreads();
     };
     // forward: L y = b
@@ -365,19 +369,19 @@ __global__ void k_chol_solve(const double* L, int m, const int32_t* tfirst, cons
         const int k0 = K * kTile, kb = min(kTile, m - k0);
         stage(k0, kb);
         if (tid < 32) {  // warp 0 solves the diagonal tile
-            double v = lane < kb ? x[k0 + lane] : 0.0;
+            T v = lane < kb ? x[k0 + lane] : T(0);
             for (int j = 0; j < kb; ++j) {
-                const double xj = __shfl_sync(kFullG, v * (lane == j ? dr[j] : 1.0), j);
+                const T xj = __shfl_sync(kFullG, v * (lane == j ? dr[j] : T(1)), j);
                 if (lane == j) v = xj;
                 if (lane > j && lane < kb) v -= dt[lane][j] * xj;
             }
             if (lane < kb) x[k0 + lane] = v;
         }
         __syncthreads();
-        const double xk = lane < kb ? x[k0 + lane] : 0.0;
+        const T xk = lane < kb ? x[k0 + lane] : T(0);
         for (int r = k0 + kb + wid; r < m; r += nw) {
             if (tfirst[r / kTile] > K) continue;  // uniform per warp
-            double s = lane < kb ? L[(size_t)r * m + k0 + lane] * xk : 0.0;
+            T s = lane < kb ? L[(size_t)r * m + k0 + lane] * xk : T(0);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(kFullG, s, o);
             if (lane == 0) x[r] -= s;
@@ -388,7 +392,7 @@ __global__ void k_chol_solve(const double* L, int m, const int32_t* tfirst, cons
     for (int K = nt - 1; K >= 0; --K) {
         const int k0 = K * kTile, kb = min(kTile, m - k0);
         // x_K -= sum over the rows below of L_rK x_r (rows whose tile row reaches column K)
-        double acc = 0.0;
+        T acc = T(0);
         for (int r = k0 + kb + wid; r < m; r += nw) {
             if (tfirst[r / kTile] > K) continue;
             if (lane < kb) acc += L[(size_t)r * m + k0 + lane] * x[r];
@@ -396,16 +400,16 @@ __global__ void k_chol_solve(const double* L, int m, const int32_t* tfirst, cons
         red[wid][lane] = acc;
         __syncthreads();
         if (tid < kb) {
-            double s = 0.0;
+            T s = T(0);
             for (int w = 0; w < nw; ++w) s += red[w][tid];
             x[k0 + tid] -= s;
         }
         __syncthreads();
         stage(k0, kb);
         if (tid < 32) {
-            double v = lane < kb ? x[k0 + lane] : 0.0;
+            T v = lane < kb ? x[k0 + lane] : T(0);
             for (int j = kb - 1; j >= 0; --j) {
-                const double xj = __shfl_sync(kFullG, v * (lane == j ? dr[j] : 1.0), j);
+                const T xj = __shfl_sync(kFullG, v * (lane == j ? dr[j] : T(1)), j);
                 if (lane == j) v = xj;
                 if (lane < j) v -= dt[j][lane] * xj;
             }
@@ -413,6 +417,44 @@ __global__ void k_chol_solve(const double* L, int m, const int32_t* tfirst, cons
         }
         __syncthreads();
     }
+}
+
+// Mixed form: S (FP64, lower part) rounded to FP32 into S32, and both mirrored into their upper
+// parts (the refinement residual is then a plain row-major product; the factorization and the
+// solves read the lower parts only).
+__global__ void k_s_round(double* S, float* S32, int m) {
+    const size_t n = (size_t)m * m;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(k / m), j = (int)(k % m);
+        if (j > i) continue;
+        const double v = S[k];
+        S32[k] = (float)v;
+        if (j < i) {
+            S[(size_t)j * m + i] = v;
+            S32[(size_t)j * m + i] = (float)v;
+        }
+    }
+}
+
+// r = b - S x in FP64 (warp per row of the mirrored S), rounded to FP32; x in FP32.
+__global__ void k_s_residual(const double* S, const float* x, const double* b, int m, float* r) {
+    const CC c = grid_view();
+    for (int i = c.gw; i < m; i += c.CW) {
+        const double* Si = S + (size_t)i * m;
+        double acc = 0.0;
+        for (int j = c.lane; j < m; j += 32) acc += Si[j] * (double)x[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(kFullG, acc, o);
+        if (c.lane == 0) r[i] = (float)(b[i] - acc);
+    }
+}
+
+// b (FP64) -> x (FP32); and b = x + y after the refinement.
+__global__ void k_vec_round(const double* b, float* x, int m) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) x[i] = (float)b[i];
+}
+__global__ void k_vec_sum(double* b, const float* x, const float* y, int m) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) b[i] = (double)x[i] + (double)y[i];
 }
 
 // Cameras: trial = exp(dx_a) * current for free cameras; Real / FP64 copies; scale part.
@@ -543,9 +585,8 @@ __global__ void k_lin_intr_cams(WinArgs<Real> A, const int4* items, int n_items,
         for (int k = 0; k < 12; ++k)
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) h[k] += __shfl_xor_sync(kFullG, h[k], o);
-#pragma unroll
-        for (int k = 0; k < 12; ++k)
-            if ((k & 31) == c.lane) hpart[12LL * it + k] = (double)h[k];
+        const Real hk = lane_value<12>(h, c.lane);
+        if (c.lane < 12) hpart[12LL * it + c.lane] = (double)hk;
     }
 }
 
@@ -618,9 +659,8 @@ __global__ void k_pcg_diag_items(WinArgs<Real> A, const int4* items, int n_items
         for (int k = 0; k < 27; ++k)
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) u[k] += __shfl_xor_sync(kFullG, u[k], o);
-#pragma unroll
-        for (int k = 0; k < 27; ++k)
-            if ((k & 31) == c.lane) part[28LL * it + k] = (double)u[k];
+        const Real uk = lane_value<27>(u, c.lane);
+        if (c.lane < 27) part[28LL * it + c.lane] = (double)uk;
     }
 }
 
@@ -1239,6 +1279,12 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     const int nk = (lm.optimize_k && intr.model == 1) ? 2 : 0;
     const int mt = m + nk;
     double* d_S = dv.alloc<double>(pcg ? 1 : (size_t)std::max(1, m) * std::max(1, m));
+    // mixed form, Cholesky path (not the differentiable solve, which is FP64): the FP32 factor of S
+    const bool mixed_chol = sizeof(Real) == 4 && !pcg && !vjp;
+    float* d_S32 = mixed_chol ? dv.alloc<float>((size_t)std::max(1, m) * std::max(1, m)) : nullptr;
+    float* d_rinv32 = mixed_chol ? dv.alloc<float>(std::max(1, m)) : nullptr;
+    float* d_x32 = mixed_chol ? dv.alloc<float>(std::max(1, m)) : nullptr;
+    float* d_y32 = mixed_chol ? dv.alloc<float>(std::max(1, m)) : nullptr;
     double* d_bs = dv.alloc<double>(std::max(1, mt));
     double* d_rinv = dv.alloc<double>(std::max(1, m));
     int32_t* d_ok = dv.alloc<int32_t>(1);
@@ -1440,7 +1486,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         int dev = 0, nsm = 0, bps = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_cholesky_coop, 256, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_cholesky_coop<double>, 256, 0);
         chol_grid = std::max(1, std::min(nsm * std::max(1, std::min(bps, 2)), g.max_col_work));
     }
     auto factor_S = [&]() -> bool {
@@ -1455,11 +1501,48 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         double* ri = d_rinv;
         int32_t* okp = d_ok;
         void* kargs[] = {&Sp, &mm, &po, &pr, &to, &tij, &ri, &okp};
-        chk(cudaLaunchCooperativeKernel((const void*)k_cholesky_coop, dim3(chol_grid), dim3(256), kargs, 0, st));
+        chk(cudaLaunchCooperativeKernel((const void*)k_cholesky_coop<double>, dim3(chol_grid), dim3(256), kargs, 0, st));
         int32_t okh = 1;
         chk(cudaMemcpyAsync(&okh, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
         chk(cudaStreamSynchronize(st));
         return e == cudaSuccess && okh != 0;
+    };
+    // Mixed form: S x = b (x into d_bs) with the Cholesky factor of S rounded to FP32 and one FP64
+    // refinement step (r = b - S x0 over the FP64 S, then the FP32 factor's solution of r added).
+    // S's entries are FP32 sums already, so the FP32 factor's error is of the order of S's own; the
+    // refinement step removes it.  A pivot that is not positive in FP32 falls back to the FP64
+    // factorization.  Returns false if S is not positive definite in FP64 either.
+    auto solve_S_mixed = [&]() -> bool {
+        const int32_t one = 1;
+        chk(cudaMemcpyAsync(d_ok, &one, sizeof(int32_t), cudaMemcpyHostToDevice, st));
+        k_s_round<<<nsm_blocks, TB, 0, st>>>(d_S, d_S32, m);
+        float* Sp = d_S32;
+        int mm = m;
+        const int32_t* po = d_pan_off;
+        const int32_t* pr = d_pan_row;
+        const int32_t* to = d_tr_off;
+        const int2* tij = d_tr_ij;
+        float* ri = d_rinv32;
+        int32_t* okp = d_ok;
+        void* kargs[] = {&Sp, &mm, &po, &pr, &to, &tij, &ri, &okp};
+        chk(cudaLaunchCooperativeKernel((const void*)k_cholesky_coop<float>, dim3(chol_grid), dim3(256), kargs, 0, st));
+        int32_t okh = 1;
+        chk(cudaMemcpyAsync(&okh, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        chk(cudaStreamSynchronize(st));
+        if (e != cudaSuccess) return false;
+        if (!okh) {
+            if (!factor_S()) return false;
+            k_chol_solve<<<1, 1024, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_bs);
+            return true;
+        }
+        const int vb = (m + TB - 1) / TB;
+        k_vec_round<<<vb, TB, 0, st>>>(d_bs, d_x32, m);
+        k_chol_solve<<<1, 1024, 0, st>>>(d_S32, m, d_tfirst, d_rinv32, d_x32);
+        k_s_residual<<<nsm_blocks, TB, 0, st>>>(d_S, d_x32, d_bs, m, d_y32);
+        k_chol_solve<<<1, 1024, 0, st>>>(d_S32, m, d_tfirst, d_rinv32, d_y32);
+        k_vec_sum<<<vb, TB, 0, st>>>(d_bs, d_x32, d_y32, m);
+        chk(cudaGetLastError());
+        return true;
     };
     // state c -> tape slot s
     auto save_state = [&](int c, int s) {
@@ -1638,13 +1721,14 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                     chk(cudaStreamSynchronize(st));
                     return e;
                 }
-                ok = factor_S() && ok;
-                if (e != cudaSuccess) return e;
-                if (ok) {
-                    k_chol_solve<<<1, 1024, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_bs);
+                if (mixed_chol) {
+                    ok = solve_S_mixed() && ok;
                 } else {
-                    chk(cudaMemsetAsync(d_bs, 0, sizeof(double) * m, st));
+                    ok = factor_S() && ok;
+                    if (ok) k_chol_solve<<<1, 1024, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_bs);
                 }
+                if (e != cudaSuccess) return e;
+                if (!ok) chk(cudaMemsetAsync(d_bs, 0, sizeof(double) * m, st));
                 chk(cudaGetLastError());
             }
             k_update_cams<Real><<<cblocks, TB, 0, st>>>(cams[cur], cams[cur ^ 1], camr[cur ^ 1], d_cam_free, nc, d_bs, d_U,

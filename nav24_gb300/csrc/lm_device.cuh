@@ -236,6 +236,16 @@ __device__ __forceinline__ void sub_at_d(const WinArgs<Real>& A, long long e, co
     }
 }
 
+// v[k] for a runtime k < N (0 otherwise) from a register array, by selects (no local-memory copy).
+template <int N, class Real>
+__device__ __forceinline__ Real lane_value(const Real* v, int k) {
+    Real o = Real(0);
+#pragma unroll
+    for (int x = 0; x < N; ++x)
+        if (x == k) o = v[x];
+    return o;
+}
+
 // Cluster-split robust chi2 of the window for cameras `camc` (12 values per camera, precision
 // Cost) and points X; returns this thread's partial sum.  e_out != null: each edge's residual is
 // also written there (2 values per edge, rounded to Real).
@@ -318,6 +328,62 @@ __device__ double linearize_points(const WinArgs<Real>& A, const CC& c, const Wi
     return mx;
 }
 
+// Point gp's damped block: R R^T = V + lambda I, L = R^-1 (packed lower: l00 l10 l11 l20 l21 l22),
+// t = L g; ltv = (L, t, 0 0 0) is also stored in pt_lt.  Returns false if V + lambda I is not
+// positive definite.
+template <class Real>
+__device__ __forceinline__ bool point_factor(const WinArgs<Real>& A, long long gp, Real lam, Real* ltv) {
+    Real vg[12];
+    Rec<Real>::load12(A.pt_vg + 12LL * gp, vg);
+    const Real v00 = vg[0] + lam, v01 = vg[1], v02 = vg[2], v11 = vg[3] + lam, v12 = vg[4], v22 = vg[5] + lam;
+    const Real r00 = sqrt(v00);
+    const Real r10 = v01 / r00, r20 = v02 / r00;
+    const Real d11 = v11 - r10 * r10;
+    const Real r11 = sqrt(d11);
+    const Real r21 = (v12 - r20 * r10) / r11;
+    const Real d22 = v22 - r20 * r20 - r21 * r21;
+    const Real r22 = sqrt(d22);
+    const Real l00 = Real(1) / r00, l11 = Real(1) / r11, l22 = Real(1) / r22;
+    const Real l10 = -r10 * l00 * l11;
+    const Real l21 = -r21 * l11 * l22;
+    const Real l20 = -(r20 * l00 + r21 * l10) * l22;
+    ltv[0] = l00; ltv[1] = l10; ltv[2] = l11; ltv[3] = l20; ltv[4] = l21; ltv[5] = l22;
+    ltv[6] = l00 * vg[6];
+    ltv[7] = l10 * vg[6] + l11 * vg[7];
+    ltv[8] = l20 * vg[6] + l21 * vg[7] + l22 * vg[8];
+    ltv[9] = ltv[10] = ltv[11] = Real(0);
+    Rec<Real>::store12(A.pt_lt + 12LL * gp, ltv);
+    return v00 > Real(0) && d11 > Real(0) && d22 > Real(0);
+}
+
+// Jacobian-factored record of edge e (free camera, free point) from the point's ltv (point_factor)
+// and Real copy Xr, at the linearization state (camr, Xr).
+template <class Real>
+__device__ __forceinline__ void edge_jrec(const WinArgs<Real>& A, long long e, const Real* camr, const Real* Xr,
+                                          const Real* ltv, Real delta) {
+    const Real* cr = camr + 12 * A.edge_cam[e];
+    Real z[2];
+    obs_real(A, e, z);
+    EdgeLin<Real> L;
+    edge_linearize<Real>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta, L);
+    const Real iz = Real(1) / L.xc[2];
+    Real rec[12];
+    rec[0] = L.xc[0] * iz;
+    rec[1] = L.xc[1] * iz;
+    rec[2] = iz;
+#pragma unroll
+    for (int s2 = 0; s2 < 2; ++s2) {
+        const Real j0 = L.w * L.jp[s2 * 3 + 0], j1 = L.w * L.jp[s2 * 3 + 1], j2 = L.w * L.jp[s2 * 3 + 2];
+        rec[3 + s2 * 3 + 0] = j0 * ltv[0];
+        rec[3 + s2 * 3 + 1] = j0 * ltv[1] + j1 * ltv[2];
+        rec[3 + s2 * 3 + 2] = j0 * ltv[3] + j1 * ltv[4] + j2 * ltv[5];
+    }
+    rec[9] = ltv[6];
+    rec[10] = ltv[7];
+    rec[11] = ltv[8];
+    Rec<Real>::store12(A.edge_a + (long long)JRec::kEdge * e, rec);
+}
+
 // Per free point: R R^T = V + lambda I, L = R^-1, t = L g, A_e = W_e L^T.  W_e = w J_c^T J_p is read
 // from edge_w (FP64 form, where recomputing costs FP64-pipe time) or recomputed from the edge's
 // Jacobians at the current state (mixed form: camr, X are the state the point blocks were
@@ -332,24 +398,9 @@ __device__ int schur_points(const WinArgs<Real>& A, const CC& c, const WinDesc& 
     for (int p = c.gt; p < D.npt; p += c.CT) {
         const int gp = D.pt0 + p;
         if (A.pt_free[gp] < 0) continue;
-        Real vg[12];
-        Rec<Real>::load12(A.pt_vg + 12LL * gp, vg);
-        const Real v00 = vg[0] + lam, v01 = vg[1], v02 = vg[2], v11 = vg[3] + lam, v12 = vg[4], v22 = vg[5] + lam;
-        const Real r00 = sqrt(v00);
-        const Real r10 = v01 / r00, r20 = v02 / r00;
-        const Real d11 = v11 - r10 * r10;
-        const Real r11 = sqrt(d11);
-        const Real r21 = (v12 - r20 * r10) / r11;
-        const Real d22 = v22 - r20 * r20 - r21 * r21;
-        const Real r22 = sqrt(d22);
-        if (!(v00 > Real(0)) || !(d11 > Real(0)) || !(d22 > Real(0))) ++bad;
-        const Real l00 = Real(1) / r00, l11 = Real(1) / r11, l22 = Real(1) / r22;
-        const Real l10 = -r10 * l00 * l11;
-        const Real l21 = -r21 * l11 * l22;
-        const Real l20 = -(r20 * l00 + r21 * l10) * l22;
-        const Real ltv[12] = {l00, l10, l11, l20, l21, l22, l00 * vg[6], l10 * vg[6] + l11 * vg[7],
-                              l20 * vg[6] + l21 * vg[7] + l22 * vg[8], Real(0), Real(0), Real(0)};
-        Rec<Real>::store12(A.pt_lt + 12LL * gp, ltv);
+        Real ltv[12];
+        bad += point_factor(A, gp, lam, ltv) ? 0 : 1;
+        const Real l00 = ltv[0], l10 = ltv[1], l11 = ltv[2], l20 = ltv[3], l21 = ltv[4], l22 = ltv[5];
         Real Xr[3];
         point_real(X, XR, gp, Xr);
         const int e1 = A.pt_eoff[gp + 1];
@@ -357,27 +408,7 @@ __device__ int schur_points(const WinArgs<Real>& A, const CC& c, const WinDesc& 
             if (A.edge_fc[e] < 0) continue;
             if constexpr (sizeof(Real) == 4) {
                 if (A.jfact) {  // Jacobian-factored record
-                    const Real* cr = camr + 12 * A.edge_cam[e];
-                    Real z[2];
-                    obs_real(A, e, z);
-                    EdgeLin<Real> L;
-                    edge_linearize<Real>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta, L);
-                    const Real iz = Real(1) / L.xc[2];
-                    Real rec[12];
-                    rec[0] = L.xc[0] * iz;
-                    rec[1] = L.xc[1] * iz;
-                    rec[2] = iz;
-#pragma unroll
-                    for (int s2 = 0; s2 < 2; ++s2) {
-                        const Real j0 = L.w * L.jp[s2 * 3 + 0], j1 = L.w * L.jp[s2 * 3 + 1], j2 = L.w * L.jp[s2 * 3 + 2];
-                        rec[3 + s2 * 3 + 0] = j0 * l00;
-                        rec[3 + s2 * 3 + 1] = j0 * l10 + j1 * l11;
-                        rec[3 + s2 * 3 + 2] = j0 * l20 + j1 * l21 + j2 * l22;
-                    }
-                    rec[9] = ltv[6];
-                    rec[10] = ltv[7];
-                    rec[11] = ltv[8];
-                    Rec<Real>::store12(A.edge_a + (long long)JRec::kEdge * e, rec);
+                    edge_jrec(A, e, camr, Xr, ltv, delta);
                     continue;
                 }
             }

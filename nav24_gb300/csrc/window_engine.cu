@@ -274,16 +274,6 @@ __device__ void build_lists(const WinArgs<Real>& A, CC& c, const WinDesc& D) {
     csync();
 }
 
-// v[k] for a runtime k < N (0 otherwise) from a register array, by selects (no local-memory copy).
-template <int N, class Real>
-__device__ __forceinline__ Real lane_value(const Real* v, int k) {
-    Real o = Real(0);
-#pragma unroll
-    for (int x = 0; x < N; ++x)
-        if (x == k) o = v[x];
-    return o;
-}
-
 // Camera-major linearization: U_c, g_c (warp per free camera) into rank 0; returns max |diag U|.
 template <class Real>
 __device__ double linearize_cameras(const WinArgs<Real>& A, const CC& c, const WinDesc& D, const Real* camr,
