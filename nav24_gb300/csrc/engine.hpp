@@ -131,7 +131,7 @@ cudaError_t window_batch_launch(PreparedBatch& pb, cudaStream_t stream, int prec
                                 WindowLaunch shape, double debug_lambda);
 
 // Print the per-phase cycle breakdown of the last launch to stderr (NAVBA_PHASE_TIMING=1).
-constexpr int kWinPhases = 13;
+constexpr int kWinPhases = 16;
 struct WindowLaunch;
 void window_phase_report(const PreparedBatch& pb, const WindowLaunch& shape, int precision);
 

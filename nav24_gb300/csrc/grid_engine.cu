@@ -867,7 +867,15 @@ __global__ void __launch_bounds__(256) k_pcg_solve(PcgArgs<Real> P) {
         {
             constexpr int G = 8, GPW = 32 / G;
             const int gl = lane % G, gi = lane / G;
-            double acc[2] = {0, 0};
+            // B^T t2 partials in Real with Kahan compensation, widened once at the end: only the
+            // group leaders hold them, and FP64 operations are charged per warp instruction
+            Real ks[2] = {Real(0), Real(0)}, kc[2] = {Real(0), Real(0)};
+            auto kahan = [&](int i, Real v) {
+                const Real y = v - kc[i];
+                const Real t = ks[i] + y;
+                kc[i] = (t - ks[i]) - y;
+                ks[i] = t;
+            };
             const Real k1 = P.nk ? (Real)v.p[kb] : Real(0), k2 = P.nk ? (Real)v.p[kb + 1] : Real(0);
             for (int p0 = gw * GPW; p0 < P.np; p0 += nwarp * GPW) {
                 const int p = p0 + gi;
@@ -901,14 +909,15 @@ __global__ void __launch_bounds__(256) k_pcg_solve(PcgArgs<Real> P) {
                         t0 += bp[0] * k1 + bp[3] * k2;
                         t1 += bp[1] * k1 + bp[4] * k2;
                         t2 += bp[2] * k1 + bp[5] * k2;
-                        acc[0] += (double)(bp[0] * t0 + bp[1] * t1 + bp[2] * t2);
-                        acc[1] += (double)(bp[3] * t0 + bp[4] * t1 + bp[5] * t2);
+                        kahan(0, bp[0] * t0 + bp[1] * t1 + bp[2] * t2);
+                        kahan(1, bp[3] * t0 + bp[4] * t1 + bp[5] * t2);
                     }
                     P.pt_t2[4LL * p] = t0;
                     P.pt_t2[4LL * p + 1] = t1;
                     P.pt_t2[4LL * p + 2] = t2;
                 }
             }
+            double acc[2] = {(double)ks[0] - (double)kc[0], (double)ks[1] - (double)kc[1]};
             block_partials<2>(acc, pk_part);
         }
         grid.sync();
@@ -930,10 +939,8 @@ __global__ void __launch_bounds__(256) k_pcg_solve(PcgArgs<Real> P) {
             for (int k = 0; k < 6; ++k)
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) y[k] += __shfl_xor_sync(kFullG, y[k], o);
-            if (lane < 6)
-#pragma unroll
-                for (int k = 0; k < 6; ++k)
-                    if (k == lane) P.camp[8LL * it + k] = (double)y[k];
+            const Real yk = lane_value<6>(y, lane);  // one FP64 conversion per warp, not per value
+            if (lane < 6) P.camp[8LL * it + lane] = (double)yk;
         }
         {
             double hk[2] = {0, 0};

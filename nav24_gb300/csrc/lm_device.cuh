@@ -203,25 +203,33 @@ struct JRec {
     static __device__ __forceinline__ void load(const float* p, float* v) { Rec<float>::load12(p, v); }
 };
 
+// u -= A_e^T d = B^T (J_c d) from a Jacobian-factored record and the edge camera's step d.
+template <class Real, class DC>
+__device__ __forceinline__ void sub_at_d_rec(const Real* rec, const DC* d, Real fx, Real fy, Real& u0, Real& u1,
+                                             Real& u2) {
+    Real jc[12];
+    pinhole_jc(fx, fy, rec[0], rec[1], rec[2], jc);
+    Real j0 = Real(0), j1 = Real(0);
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+        const Real dr = (Real)d[r];
+        j0 += jc[r] * dr;
+        j1 += jc[6 + r] * dr;
+    }
+    u0 -= rec[3] * j0 + rec[6] * j1;
+    u1 -= rec[4] * j0 + rec[7] * j1;
+    u2 -= rec[5] * j0 + rec[8] * j1;
+}
+
 // u -= A_e^T d for edge e and its camera's step d (6 values).
 template <class Real, class DC>
 __device__ __forceinline__ void sub_at_d(const WinArgs<Real>& A, long long e, const DC* d, Real fx, Real fy, Real& u0,
                                          Real& u1, Real& u2) {
     if constexpr (sizeof(Real) == 4) {
         if (A.jfact) {
-            Real rec[12], jc[12];
+            Real rec[12];
             JRec::load(A.edge_a + (long long)JRec::kEdge * e, rec);
-            pinhole_jc(fx, fy, rec[0], rec[1], rec[2], jc);
-            Real j0 = Real(0), j1 = Real(0);
-#pragma unroll
-            for (int r = 0; r < 6; ++r) {
-                const Real dr = (Real)d[r];
-                j0 += jc[r] * dr;
-                j1 += jc[6 + r] * dr;
-            }
-            u0 -= rec[3] * j0 + rec[6] * j1;
-            u1 -= rec[4] * j0 + rec[7] * j1;
-            u2 -= rec[5] * j0 + rec[8] * j1;
+            sub_at_d_rec(rec, d, fx, fy, u0, u1, u2);
             return;
         }
     }
@@ -292,12 +300,19 @@ __device__ double linearize_points(const WinArgs<Real>& A, const CC& c, const Wi
         Real Xr[3];
         point_real(X, XR, gp, Xr);
         Real V[6] = {0, 0, 0, 0, 0, 0}, g[3] = {0, 0, 0};
-        const int e1 = A.pt_eoff[gp + 1];
-        for (int e = A.pt_eoff[gp]; e < e1; ++e) {
-            const int cam = A.edge_cam[e];
+        const int e0 = A.pt_eoff[gp], e1 = A.pt_eoff[gp + 1];
+        // the next edge's camera and observation are loaded before the current edge's products
+        int cam_n = A.edge_cam[e0];
+        Real z_n[2];
+        obs_real(A, e0, z_n);
+        for (int e = e0; e < e1; ++e) {
+            const int cam = cam_n;
+            const Real z[2] = {z_n[0], z_n[1]};
+            if (e + 1 < e1) {
+                cam_n = A.edge_cam[e + 1];
+                obs_real(A, e + 1, z_n);
+            }
             const Real* cr = camr + 12 * cam;
-            Real z[2];
-            obs_real(A, e, z);
             EdgeLin<Real> L;
             edge_linearize<Real>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta, L);
             const Real w = L.w;
@@ -356,14 +371,11 @@ __device__ __forceinline__ bool point_factor(const WinArgs<Real>& A, long long g
     return v00 > Real(0) && d11 > Real(0) && d22 > Real(0);
 }
 
-// Jacobian-factored record of edge e (free camera, free point) from the point's ltv (point_factor)
-// and Real copy Xr, at the linearization state (camr, Xr).
+// Jacobian-factored record of edge e (free camera, free point) from the point's ltv (point_factor),
+// its camera cr and observation z, at the linearization state (cr, Xr).
 template <class Real>
-__device__ __forceinline__ void edge_jrec(const WinArgs<Real>& A, long long e, const Real* camr, const Real* Xr,
-                                          const Real* ltv, Real delta) {
-    const Real* cr = camr + 12 * A.edge_cam[e];
-    Real z[2];
-    obs_real(A, e, z);
+__device__ __forceinline__ void edge_jrec(const WinArgs<Real>& A, long long e, const Real* cr, const Real* z,
+                                          const Real* Xr, const Real* ltv, Real delta) {
     EdgeLin<Real> L;
     edge_linearize<Real>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta, L);
     const Real iz = Real(1) / L.xc[2];
@@ -404,14 +416,29 @@ __device__ int schur_points(const WinArgs<Real>& A, const CC& c, const WinDesc& 
         Real Xr[3];
         point_real(X, XR, gp, Xr);
         const int e1 = A.pt_eoff[gp + 1];
+        if constexpr (sizeof(Real) == 4) {
+            if (A.jfact) {
+                // Jacobian-factored records; the next edge's camera, observation and free index are
+                // loaded before the current edge's record is formed
+                const int e0 = A.pt_eoff[gp];
+                int fc_n = A.edge_fc[e0], cam_n = A.edge_cam[e0];
+                Real z_n[2];
+                obs_real(A, e0, z_n);
+                for (int e = e0; e < e1; ++e) {
+                    const int fc = fc_n, cam = cam_n;
+                    const Real z[2] = {z_n[0], z_n[1]};
+                    if (e + 1 < e1) {
+                        fc_n = A.edge_fc[e + 1];
+                        cam_n = A.edge_cam[e + 1];
+                        obs_real(A, e + 1, z_n);
+                    }
+                    if (fc >= 0) edge_jrec(A, e, camr + 12 * cam, z, Xr, ltv, delta);
+                }
+                continue;
+            }
+        }
         for (int e = A.pt_eoff[gp]; e < e1; ++e) {
             if (A.edge_fc[e] < 0) continue;
-            if constexpr (sizeof(Real) == 4) {
-                if (A.jfact) {  // Jacobian-factored record
-                    edge_jrec(A, e, camr, Xr, ltv, delta);
-                    continue;
-                }
-            }
             Real W[18];
             if (A.edge_w) {
                 Rec<Real>::load18(A.edge_w + (long long)Rec<Real>::kEdge * e, W);
@@ -506,10 +533,32 @@ __device__ double2 update_points_dcost(const WinArgs<Real>& A, const CC& c, cons
             Real lt[12];
             Rec<Real>::load12(A.pt_lt + 12LL * gp, lt);
             Real u0 = lt[6], u1 = lt[7], u2 = lt[8];
-            for (int e = e0i; e < e1i; ++e) {
-                const int a = A.edge_fc[e];
-                if (a >= 0) sub_at_d(A, e, dcl + 6 * a, fx, fy, u0, u1, u2);
+            bool done = false;
+            if constexpr (sizeof(Real) == 4) {
+              if (A.jfact) {
+                // Jacobian-factored records: the next edge's record and free camera are loaded before
+                // the current edge's products (a fixed camera's record is loaded and not used)
+                Real rec[12], nrec[12];
+                int a_n = A.edge_fc[e0i];
+                JRec::load(A.edge_a + (long long)JRec::kEdge * e0i, nrec);
+                for (int e = e0i; e < e1i; ++e) {
+                    const int a = a_n;
+#pragma unroll
+                    for (int k = 0; k < 12; ++k) rec[k] = nrec[k];
+                    if (e + 1 < e1i) {
+                        a_n = A.edge_fc[e + 1];
+                        JRec::load(A.edge_a + (long long)JRec::kEdge * (e + 1), nrec);
+                    }
+                    if (a >= 0) sub_at_d_rec(rec, dcl + 6 * a, fx, fy, u0, u1, u2);
+                }
+                done = true;
+              }
             }
+            if (!done)
+                for (int e = e0i; e < e1i; ++e) {
+                    const int a = A.edge_fc[e];
+                    if (a >= 0) sub_at_d(A, e, dcl + 6 * a, fx, fy, u0, u1, u2);
+                }
             d0 = lt[0] * u0 + lt[1] * u1 + lt[3] * u2;
             d1 = lt[2] * u1 + lt[4] * u2;
             d2 = lt[5] * u2;

@@ -150,8 +150,8 @@ __device__ double3 cluster_reduce3(CC& c, double a, double b, double d) {
 }
 
 // Camera-major edge lists of the free cameras and the pair lists of the S blocks.
-template <class Real>
-__device__ void build_lists(const WinArgs<Real>& A, CC& c, const WinDesc& D) {
+template <class Real, class Mark>
+__device__ void build_lists(const WinArgs<Real>& A, CC& c, const WinDesc& D, Mark&& mark) {
     SmemHead& s = *c.s;
     cg::cluster_group cl = cg::this_cluster();
     for (int cam = c.gw; cam < D.ncam; cam += c.CW) {
@@ -188,6 +188,7 @@ __device__ void build_lists(const WinArgs<Real>& A, CC& c, const WinDesc& D) {
         }
     }
     csync();  // every camera list is in global memory
+    mark(14);
     // Schur pairs by block row: the warp of free camera a walks a's edges i and, for each, the other
     // edges j of i's free point whose free camera b <= a; pair (i, j) belongs to block (a, b).
     const int nblk = D.nfc * (D.nfc + 1) / 2;
@@ -219,6 +220,7 @@ __device__ void build_lists(const WinArgs<Real>& A, CC& c, const WinDesc& D) {
         __syncwarp();
     }
     csync();
+    mark(15);
     if (c.rank == 0 && threadIdx.x == 0) {
         int acc = 0;
         for (int k = 0; k < nblk; ++k) {
@@ -619,15 +621,18 @@ static_assert(6 * kWinMaxFreeCams <= 32 * kSolveRows, "reduced system larger tha
 __device__ void warp_chol_solve32(const float* L, const float* rinv, int m, float* x) {
     if (threadIdx.x >= 32) return;
     const int lane = threadIdx.x;
-    float xr[kSolveRows];
+    float xr[kSolveRows], rr[kSolveRows];  // the lane's rows of x and their 1/L_jj (off the serial chain)
 #pragma unroll
-    for (int q = 0; q < kSolveRows; ++q) xr[q] = lane + 32 * q < m ? x[lane + 32 * q] : 0.f;
+    for (int q = 0; q < kSolveRows; ++q) {
+        xr[q] = lane + 32 * q < m ? x[lane + 32 * q] : 0.f;
+        rr[q] = lane + 32 * q < m ? rinv[lane + 32 * q] : 1.f;
+    }
 #pragma unroll
     for (int q = 0; q < kSolveRows; ++q) {
         for (int jj = 0; jj < 32; ++jj) {
             const int j = 32 * q + jj;
             if (j >= m) break;
-            if (lane == jj) xr[q] *= rinv[j];
+            if (lane == jj) xr[q] *= rr[q];
             const float xj = __shfl_sync(kFull, xr[q], jj);
 #pragma unroll
             for (int qq = q; qq < kSolveRows; ++qq) {
@@ -641,7 +646,7 @@ __device__ void warp_chol_solve32(const float* L, const float* rinv, int m, floa
         for (int jj = 31; jj >= 0; --jj) {
             const int j = 32 * q + jj;
             if (j >= m) continue;
-            if (lane == jj) xr[q] *= rinv[j];
+            if (lane == jj) xr[q] *= rr[q];
             const float xj = __shfl_sync(kFull, xr[q], jj);
             const float* Lj = L + tri(j, 0);
 #pragma unroll
@@ -771,7 +776,8 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
         for (int e = c.gt; e < 2 * D.ne; e += c.CT) A.edge_uvr[2LL * D.e0 + e] = (Real)A.edge_uv[2LL * D.e0 + e];
     if (threadIdx.x == 0) s.cur = 0;
     __syncthreads();
-    build_lists(A, c, D);  // ends with a cluster barrier: points are initialized everywhere
+    pc.mark(13);
+    build_lists(A, c, D, [&](int k) { pc.mark(k); });  // ends with a cluster barrier: points are initialized everywhere
     pc.mark(0);
 
     // the initial cost is FP64 in both forms; the FP64 form evaluates every trial cost in FP64, the
@@ -1373,9 +1379,10 @@ void window_phase_report(const PreparedBatch& pb, const WindowLaunch& shape, int
     if (!pb.dev.d_phase) return;
     unsigned long long h[kWinPhases] = {};
     if (cudaMemcpy(h, pb.dev.d_phase, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return;
-    static const char* names[kWinPhases] = {"init+lists", "initial cost", "linearize points", "linearize cameras",
+    static const char* names[kWinPhases] = {"lists: pair fill", "initial cost", "linearize points", "linearize cameras",
                                             "schur points", "schur blocks", "cholesky", "update", "trial cost",
-                                            "outputs", "  chol: f32 factor", "  chol: f32 solves", "  chol: refine"};
+                                            "outputs", "  chol: f32 factor", "  chol: f32 solves", "  chol: refine",
+                                            "  init: states", "  lists: cameras", "  lists: pair counts"};
     unsigned long long tot = 0;
     for (int k = 0; k < kWinPhases; ++k) tot += h[k];
     fprintf(stderr, "[navba phases] precision=%d cluster=%d threads=%d total=%llu cycles (rank-0 CTAs, summed)\n",
