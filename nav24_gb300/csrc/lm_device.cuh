@@ -244,6 +244,28 @@ __device__ __forceinline__ void sub_at_d(const WinArgs<Real>& A, long long e, co
     }
 }
 
+// The 12 values (R row-major, t) of camera record cr into registers with 16-byte loads (camera
+// records start 16-byte aligned): three loads in FP32 instead of twelve.
+template <class Real>
+__device__ __forceinline__ void cam_load(const Real* cr, Real* o) {
+    if constexpr (sizeof(Real) == 4) {
+        const float4* q = reinterpret_cast<const float4*>(cr);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float4 t = q[k];
+            o[4 * k] = t.x; o[4 * k + 1] = t.y; o[4 * k + 2] = t.z; o[4 * k + 3] = t.w;
+        }
+    } else {
+        const double2* q = reinterpret_cast<const double2*>(cr);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const double2 t = q[k];
+            o[2 * k] = t.x;
+            o[2 * k + 1] = t.y;
+        }
+    }
+}
+
 // v[k] for a runtime k < N (0 otherwise) from a register array, by selects (no local-memory copy).
 template <int N, class Real>
 __device__ __forceinline__ Real lane_value(const Real* v, int k) {
@@ -267,7 +289,8 @@ __device__ double cost_partial(const WinArgs<Real>& A, const CC& c, const WinDes
         const Cost Xr[3] = {(Cost)X[4LL * gp], (Cost)X[4LL * gp + 1], (Cost)X[4LL * gp + 2]};
         const int e1 = A.pt_eoff[gp + 1];
         for (int e = A.pt_eoff[gp]; e < e1; ++e) {
-            const Cost* cr = camc + 12 * A.edge_cam[e];
+            Cost cr[12];
+            cam_load(camc + 12 * A.edge_cam[e], cr);
             const Cost z[2] = {(Cost)A.edge_uv[2LL * e], (Cost)A.edge_uv[2LL * e + 1]};
             if (e_out) {
                 Cost Xc[3], uv[2];
@@ -312,7 +335,8 @@ __device__ double linearize_points(const WinArgs<Real>& A, const CC& c, const Wi
                 cam_n = A.edge_cam[e + 1];
                 obs_real(A, e + 1, z_n);
             }
-            const Real* cr = camr + 12 * cam;
+            Real cr[12];
+            cam_load(camr + 12 * cam, cr);
             EdgeLin<Real> L;
             edge_linearize<Real>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta, L);
             const Real w = L.w;
@@ -432,7 +456,11 @@ __device__ int schur_points(const WinArgs<Real>& A, const CC& c, const WinDesc& 
                         cam_n = A.edge_cam[e + 1];
                         obs_real(A, e + 1, z_n);
                     }
-                    if (fc >= 0) edge_jrec(A, e, camr + 12 * cam, z, Xr, ltv, delta);
+                    if (fc >= 0) {
+                        Real cr[12];
+                        cam_load(camr + 12 * cam, cr);
+                        edge_jrec(A, e, cr, z, Xr, ltv, delta);
+                    }
                 }
                 continue;
             }
@@ -443,7 +471,8 @@ __device__ int schur_points(const WinArgs<Real>& A, const CC& c, const WinDesc& 
             if (A.edge_w) {
                 Rec<Real>::load18(A.edge_w + (long long)Rec<Real>::kEdge * e, W);
             } else {
-                const Real* cr = camr + 12 * A.edge_cam[e];
+                Real cr[12];
+                cam_load(camr + 12 * A.edge_cam[e], cr);
                 Real z[2];
                 obs_real(A, e, z);
                 EdgeLin<Real> L;
@@ -573,8 +602,9 @@ __device__ double2 update_points_dcost(const WinArgs<Real>& A, const CC& c, cons
         point_real(Xc, XRc, gp, X);
         for (int e = e0i; e < e1i; ++e) {
             const int cam = A.edge_cam[e];
-            const Real* cr = camr + 12 * cam;
-            const Real* cd = camdel + 12 * cam;
+            Real cr[12], cd[12];
+            cam_load(camr + 12 * cam, cr);
+            cam_load(camdel + 12 * cam, cd);
             Real xc[3];
             transform(cr, cr + 9, X, xc);
             const Real rd[3] = {cr[0] * d0 + cr[1] * d1 + cr[2] * d2, cr[3] * d0 + cr[4] * d1 + cr[5] * d2,

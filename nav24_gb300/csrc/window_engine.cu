@@ -79,7 +79,9 @@ NAVBA_HD Dyn dyn_layout(int max_m, int max_ncam, int real_size) {
     d.camdel = o; o = align16(o + (size_t)real_size * max_ncam * 12);
     d.dcl = o;  o = align16(o + sizeof(double) * max_m);
     d.dclr = o; o = align16(o + (size_t)real_size * max_m);
-    d.S = o;    o = align16(o + sizeof(double) * ((size_t)max_m * (max_m + 1) / 2));
+    // S, at least the camera-list counting sort's [16][kWinMaxCams] table, which borrows it
+    d.S = o;    o = align16(o + std::max(sizeof(double) * ((size_t)max_m * (max_m + 1) / 2),
+                                         sizeof(int32_t) * 16 * (size_t)kWinMaxCams));
     d.bs = o;   o = align16(o + sizeof(double) * max_m);
     d.rinv = o; o = align16(o + sizeof(double) * max_m);
     // mixed form: the FP32 factor of S and three FP32 vectors (1/L_jj, solution, correction)
@@ -151,43 +153,60 @@ __device__ double3 cluster_reduce3(CC& c, double a, double b, double d) {
 
 // Camera-major edge lists of the free cameras and the pair lists of the S blocks.
 template <class Real, class Mark>
-__device__ void build_lists(const WinArgs<Real>& A, CC& c, const WinDesc& D, Mark&& mark) {
+__device__ void build_lists(const WinArgs<Real>& A, CC& c, const WinDesc& D, int32_t (*wcam)[kWinMaxCams], Mark&& mark) {
     SmemHead& s = *c.s;
-    cg::cluster_group cl = cg::this_cluster();
-    for (int cam = c.gw; cam < D.ncam; cam += c.CW) {
-        int cnt = 0;
-        if (A.cam_free[D.cam0 + cam] >= 0) {
-            for (int base = 0; base < D.ne; base += 32) {
-                const int e = base + c.lane;
-                cnt += __popc(__ballot_sync(kFull, e < D.ne && A.edge_cam[D.e0 + e] == cam));
+    // Camera-major lists of the free cameras' edges, stable (point-major order within a camera): a
+    // counting sort by rank 0's warps, each over one contiguous range of the window's edges.  Pass 1
+    // counts per (warp, camera) (match + popc), the offsets are camera-major then warp-major, pass 2
+    // places each 32-edge chunk's edges of one camera in lane order.
+    if (c.rank == 0) {
+        const int nw = c.nw;
+        for (int k = threadIdx.x; k < nw * kWinMaxCams; k += blockDim.x) wcam[k / kWinMaxCams][k % kWinMaxCams] = 0;
+        __syncthreads();
+        const int per = (D.ne + nw - 1) / nw;
+        const int lo = c.wid * per, hi = min(D.ne, lo + per);
+        const unsigned below = (1u << c.lane) - 1u;
+        auto cam_of = [&](int e) { return e < hi && A.edge_fc[D.e0 + e] >= 0 ? A.edge_cam[D.e0 + e] : -1; };
+        for (int base = lo; base < hi; base += 32) {
+            const int cam = cam_of(base + c.lane);
+            const unsigned grp = __match_any_sync(kFull, cam);
+            if (cam >= 0 && (grp & below) == 0) wcam[c.wid][cam] += __popc(grp);
+            __syncwarp();
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int acc = 0;
+            for (int cam = 0; cam < D.ncam; ++cam) {
+                s.loff[cam] = acc;
+                for (int w = 0; w < nw; ++w) {
+                    const int t = wcam[w][cam];
+                    wcam[w][cam] = acc;
+                    acc += t;
+                }
+                s.lcnt[cam] = acc - s.loff[cam];
+                const int a = A.cam_free[D.cam0 + cam];
+                if (a >= 0) s.fcam[a] = cam;
             }
+            s.loff[D.ncam] = acc;
         }
-        if (c.lane < c.csize) cl.map_shared_rank(c.s, c.lane)->lcnt[cam] = cnt;
+        __syncthreads();
+        for (int base = lo; base < hi; base += 32) {
+            const int e = base + c.lane;
+            const int cam = cam_of(e);
+            const unsigned grp = __match_any_sync(kFull, cam);
+            if (cam >= 0) A.cam_list[D.e0 + wcam[c.wid][cam] + __popc(grp & below)] = D.e0 + e;
+            __syncwarp();
+            if (cam >= 0 && (grp & below) == 0) wcam[c.wid][cam] += __popc(grp);
+            __syncwarp();
+        }
     }
-    csync();
-    if (threadIdx.x == 0) {
-        int acc = 0;
-        for (int cam = 0; cam < D.ncam; ++cam) {
-            s.loff[cam] = acc;
-            acc += s.lcnt[cam];
-            const int a = A.cam_free[D.cam0 + cam];
-            if (a >= 0) s.fcam[a] = cam;
-        }
-        s.loff[D.ncam] = acc;
+    csync();  // the lists are in global memory and their offsets in rank 0's head
+    if (c.rank != 0) {  // the other CTAs of the cluster take rank 0's offsets
+        for (int k = threadIdx.x; k <= D.ncam; k += blockDim.x) s.loff[k] = c.s0->loff[k];
+        for (int k = threadIdx.x; k < D.ncam; k += blockDim.x) s.lcnt[k] = c.s0->lcnt[k];
+        for (int k = threadIdx.x; k < D.nfc; k += blockDim.x) s.fcam[k] = c.s0->fcam[k];
     }
     __syncthreads();
-    for (int cam = c.gw; cam < D.ncam; cam += c.CW) {
-        if (A.cam_free[D.cam0 + cam] < 0) continue;
-        int pos = s.loff[cam];
-        for (int base = 0; base < D.ne; base += 32) {
-            const int e = base + c.lane;
-            const bool hit = e < D.ne && A.edge_cam[D.e0 + e] == cam;
-            const unsigned msk = __ballot_sync(kFull, hit);
-            if (hit) A.cam_list[D.e0 + pos + __popc(msk & ((1u << c.lane) - 1u))] = D.e0 + e;
-            pos += __popc(msk);
-        }
-    }
-    csync();  // every camera list is in global memory
     mark(14);
     // Schur pairs by block row: the warp of free camera a walks a's edges i and, for each, the other
     // edges j of i's free point whose free camera b <= a; pair (i, j) belongs to block (a, b).
@@ -287,7 +306,8 @@ __device__ double linearize_cameras(const WinArgs<Real>& A, const CC& c, const W
         const int cam = s.fcam[a];
         const int* list = A.cam_list + D.e0 + s.loff[cam];
         const int cnt = s.lcnt[cam];
-        const Real* cr = camr + 12 * cam;
+        Real cr[12];
+        cam_load(camr + 12 * cam, cr);
         Real u[27];
 #pragma unroll
         for (int k = 0; k < 27; ++k) u[k] = Real(0);
@@ -777,7 +797,9 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
     if (threadIdx.x == 0) s.cur = 0;
     __syncthreads();
     pc.mark(13);
-    build_lists(A, c, D, [&](int k) { pc.mark(k); });  // ends with a cluster barrier: points are initialized everywhere
+    // the camera-list counting sort's per-warp table borrows the S region (unused until the first
+    // trial; dyn_layout sizes it for the table)
+    build_lists(A, c, D, reinterpret_cast<int32_t(*)[kWinMaxCams]>(S), [&](int k) { pc.mark(k); });  // ends with a cluster barrier: points are initialized everywhere
     pc.mark(0);
 
     // the initial cost is FP64 in both forms; the FP64 form evaluates every trial cost in FP64, the
