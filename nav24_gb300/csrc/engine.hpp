@@ -25,6 +25,7 @@ struct WinDesc {
     int32_t nfc, nfp;     // free cameras / points
     int64_t pair0;        // first slot of the window's Schur pair list (global)
     int64_t npair;        // pair-list length
+    int64_t s0;           // mixed form: first value of the window's FP64 reduced system (global scratch)
 };
 
 struct WinStats {
@@ -79,6 +80,7 @@ struct WindowBatch {
     int32_t* d_cam_list = nullptr; // [ne] camera-major edge list (free cameras only)
     uint32_t* d_pairs = nullptr;   // [npair] Schur pairs (edge i << 16 | edge j), window-local
     void* d_edge_uvr = nullptr;    // mixed: [ne][2] f32 observations
+    double* d_s = nullptr;         // mixed: the windows' packed FP64 reduced systems (sum of m(m+1)/2)
     void* d_xr[2] = {nullptr, nullptr};  // mixed: [npt][4] f32 copies of d_x
     // device outputs
     CamState* d_cam_out = nullptr;

@@ -38,6 +38,7 @@ struct WinArgs {
                               // records (JRec) instead of A
     Real* edge_e[2];          // mixed form: residual (u, v) of each edge at the current / trial state
     int32_t* cam_list;
+    double* s_glob;           // window engine, mixed form: the windows' FP64 reduced systems (WinDesc::s0)
     uint32_t* pairs;
     CamState* cam_out;
     double* pt_out;
@@ -62,7 +63,8 @@ struct CC {
     int lane, wid, nw;
     SmemHead* s;   // this CTA's head
     SmemHead* s0;  // rank 0's head (distributed shared memory)
-    double* S0;    // rank 0's reduced system
+    double* S0;    // the reduced system (rank 0's shared memory, or the mixed form's global scratch)
+    float* S0f;    // mixed form: rank 0's FP32 copy of it (factored in place), else null
     double* bs0;   // rank 0's right-hand side / step
 };
 
@@ -600,8 +602,17 @@ __device__ double2 update_points_dcost(const WinArgs<Real>& A, const CC& c, cons
         }
         Real X[3];
         point_real(Xc, XRc, gp, X);
+        // the next edge's camera and current residual are loaded before this edge's products
+        int cam_n = e0i < e1i ? A.edge_cam[e0i] : 0;
+        Real r0_n = e0i < e1i ? ecur[2LL * e0i] : Real(0), r1_n = e0i < e1i ? ecur[2LL * e0i + 1] : Real(0);
         for (int e = e0i; e < e1i; ++e) {
-            const int cam = A.edge_cam[e];
+            const int cam = cam_n;
+            const Real r0 = r0_n, r1 = r1_n;
+            if (e + 1 < e1i) {
+                cam_n = A.edge_cam[e + 1];
+                r0_n = ecur[2LL * e + 2];
+                r1_n = ecur[2LL * e + 3];
+            }
             Real cr[12], cd[12];
             cam_load(camr + 12 * cam, cr);
             cam_load(camdel + 12 * cam, cd);
@@ -617,7 +628,6 @@ __device__ double2 update_points_dcost(const WinArgs<Real>& A, const CC& c, cons
             const Real inv = Real(1) / (z * zt);
             const Real dpu = fx * (dx[0] * z - xc[0] * dx[2]) * inv;
             const Real dpv = fy * (dx[1] * z - xc[1] * dx[2]) * inv;
-            const Real r0 = ecur[2LL * e], r1 = ecur[2LL * e + 1];
             const Real n0 = r0 - dpu, n1 = r1 - dpv;
             etr[2LL * e] = n0;
             etr[2LL * e + 1] = n1;

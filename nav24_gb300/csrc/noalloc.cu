@@ -108,6 +108,7 @@ nav_ba_status solve_window_noalloc(int device, cudaStream_t stream, const nav_ba
     const size_t o_list = carve(sizeof(int32_t) * ne);
     const size_t o_pairs = carve(sizeof(uint32_t) * npair);
     const size_t o_uvr = carve(o.precision == NAV_BA_MIXED ? rs * 2 * ne : 16);
+    const size_t o_s = carve(o.precision == NAV_BA_MIXED ? sizeof(double) * (size_t)(6 * h.nfc) * (6 * h.nfc + 1) / 2 : 16);
     const size_t o_xr0 = carve(o.precision == NAV_BA_MIXED ? rs * 4 * np : 16);
     const size_t o_xr1 = carve(o.precision == NAV_BA_MIXED ? rs * 4 * np : 16);
     const size_t o_cout = carve(sizeof(CamState) * nc), o_pout = carve(sizeof(double) * 4 * np);
@@ -139,6 +140,7 @@ nav_ba_status solve_window_noalloc(int device, cudaStream_t stream, const nav_ba
     b.d_edge_e[1] = arena + o_e1;
     b.d_cam_list = reinterpret_cast<int32_t*>(arena + o_list);
     b.d_edge_uvr = arena + o_uvr;
+    b.d_s = reinterpret_cast<double*>(arena + o_s);
     b.d_xr[0] = arena + o_xr0;
     b.d_xr[1] = arena + o_xr1;
     b.d_pairs = reinterpret_cast<uint32_t*>(arena + o_pairs);
@@ -159,7 +161,7 @@ nav_ba_status solve_window_noalloc(int device, cudaStream_t stream, const nav_ba
     // host-side staging (pageable host memory; the runtime copies it)
     WinDesc d{};
     d.cam0 = 0; d.ncam = h.ncam; d.pt0 = 0; d.npt = h.npt; d.e0 = 0; d.ne = h.ne;
-    d.nfc = h.nfc; d.nfp = h.nfp; d.pair0 = 0; d.npair = h.n_pairs;
+    d.nfc = h.nfc; d.nfp = h.nfp; d.pair0 = 0; d.npair = h.n_pairs; d.s0 = 0;
     pb.desc.assign(1, d);
     const int32_t order0 = 0;
     std::vector<int32_t> edge_fc(ne);

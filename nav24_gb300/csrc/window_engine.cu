@@ -79,9 +79,10 @@ NAVBA_HD Dyn dyn_layout(int max_m, int max_ncam, int real_size) {
     d.camdel = o; o = align16(o + (size_t)real_size * max_ncam * 12);
     d.dcl = o;  o = align16(o + sizeof(double) * max_m);
     d.dclr = o; o = align16(o + (size_t)real_size * max_m);
-    // S, at least the camera-list counting sort's [16][kWinMaxCams] table, which borrows it
-    d.S = o;    o = align16(o + std::max(sizeof(double) * ((size_t)max_m * (max_m + 1) / 2),
-                                         sizeof(int32_t) * 16 * (size_t)kWinMaxCams));
+    // S (FP64 form; the mixed form keeps its FP64 S in global memory, WinArgs::s_glob), at least
+    // the camera-list counting sort's [16][kWinMaxCams] table, which borrows it
+    const size_t s_bytes = real_size == 4 ? 0 : sizeof(double) * ((size_t)max_m * (max_m + 1) / 2);
+    d.S = o;    o = align16(o + std::max(s_bytes, sizeof(int32_t) * 16 * (size_t)kWinMaxCams));
     d.bs = o;   o = align16(o + sizeof(double) * max_m);
     d.rinv = o; o = align16(o + sizeof(double) * max_m);
     // mixed form: the FP32 factor of S and three FP32 vectors (1/L_jj, solution, correction)
@@ -379,6 +380,7 @@ __device__ __forceinline__ void write_block(const CC& c, int a, int b, Real* acc
                 if (r == q) v += lambda;
             }
             c.S0[tri(6 * a + r, 6 * b + q)] = v;
+            if (c.S0f) c.S0f[tri(6 * a + r, 6 * b + q)] = (float)v;
         }
     }
     if (a == b) {
@@ -693,7 +695,7 @@ __device__ bool solve_s_mixed(double* S, double* rinv, float* S32, float* v32, i
     float* r32 = v32;           // 1/L_jj
     float* x32 = v32 + m;       // x0
     float* y32 = v32 + 2 * m;   // correction
-    for (int k = threadIdx.x; k < m * (m + 1) / 2; k += blockDim.x) S32[k] = (float)S[k];
+    // S32 holds S rounded to FP32 already (written beside S by the block write-back)
     for (int k = threadIdx.x; k < m; k += blockDim.x) x32[k] = (float)b[k];
     __syncthreads();
     const bool ok32 = smem_cholesky_blocked(S32, r32, m, s);
@@ -760,7 +762,12 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
     Real* camdel = reinterpret_cast<Real*>(smem + dl.camdel);  // trial step per camera: E - I, E_t
     double* dcl = reinterpret_cast<double*>(smem + dl.dcl);
     Real* dclr = reinterpret_cast<Real*>(smem + dl.dclr);  // dcl rounded to Real
-    double* S = reinterpret_cast<double*>(smem + dl.S);
+    double* S_smem = reinterpret_cast<double*>(smem + dl.S);
+    // the reduced system: rank 0's shared memory (FP64 form) or the window's global scratch (mixed
+    // form: it is read only by the refinement residual and the FP64 fallback; the FP32 factor is
+    // in shared memory), written by every rank of the cluster
+    double* S = sizeof(Real) == 4 ? A.s_glob + D.s0 : S_smem;
+    if (sizeof(Real) == 4) c.S0 = S;
     double* bs = reinterpret_cast<double*>(smem + dl.bs);
     double* rinv = reinterpret_cast<double*>(smem + dl.rinv);
     float* S32 = reinterpret_cast<float*>(smem + dl.s32);
@@ -799,7 +806,7 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
     pc.mark(13);
     // the camera-list counting sort's per-warp table borrows the S region (unused until the first
     // trial; dyn_layout sizes it for the table)
-    build_lists(A, c, D, reinterpret_cast<int32_t(*)[kWinMaxCams]>(S), [&](int k) { pc.mark(k); });  // ends with a cluster barrier: points are initialized everywhere
+    build_lists(A, c, D, reinterpret_cast<int32_t(*)[kWinMaxCams]>(S_smem), [&](int k) { pc.mark(k); });  // ends with a cluster barrier: points are initialized everywhere
     pc.mark(0);
 
     // the initial cost is FP64 in both forms; the FP64 form evaluates every trial cost in FP64, the
@@ -831,7 +838,10 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
             do {
                 const double lam_use = (A.debug && it == 0 && q == 0) ? A.debug_lambda : lambda;
                 if (c.rank == 0)
-                    for (int k = threadIdx.x; k < m * (m + 1) / 2; k += blockDim.x) S[k] = 0.0;
+                    for (int k = threadIdx.x; k < m * (m + 1) / 2; k += blockDim.x) {
+                        S[k] = 0.0;
+                        if (mixed) S32[k] = 0.f;
+                    }
                 const int npd = schur_points<Real>(A, c, D, lam_use, cr_cur, A.x[cur], A.xr[cur]);
                 const double3 r0 = cluster_reduce3<false>(c, (double)npd, 0.0, 0.0);  // also orders S zeroing
                 pc.mark(4);
@@ -1004,6 +1014,7 @@ __global__ void __launch_bounds__(sizeof(Real) == 8 ? 256 : 512) window_lm_kerne
     const Dyn dl = dyn_layout(A.max_m, A.max_ncam, (int)sizeof(Real));
     c.S0 = cl.map_shared_rank(reinterpret_cast<double*>(smem_raw + dl.S), 0);
     c.bs0 = cl.map_shared_rank(reinterpret_cast<double*>(smem_raw + dl.bs), 0);
+    c.S0f = sizeof(Real) == 4 ? cl.map_shared_rank(reinterpret_cast<float*>(smem_raw + dl.s32), 0) : nullptr;
     if (threadIdx.x == 0) c.s->slot = 0;
     __syncthreads();
     for (;;) {
@@ -1051,6 +1062,7 @@ cudaError_t launch_typed(PreparedBatch& pb, cudaStream_t stream, WindowLaunch sh
     A.edge_e[0] = sizeof(Real) == 4 ? (Real*)b.d_edge_e[0] : nullptr;
     A.edge_e[1] = sizeof(Real) == 4 ? (Real*)b.d_edge_e[1] : nullptr;
     A.cam_list = b.d_cam_list;
+    A.s_glob = sizeof(Real) == 4 ? b.d_s : nullptr;
     A.pairs = b.d_pairs;
     A.cam_out = b.d_cam_out;
     A.pt_out = b.d_pt_out;
@@ -1219,7 +1231,7 @@ void HostStaging::release() {
 void window_batch_free(WindowBatch& b) {
     void* ptrs[] = {b.d_win, b.d_order, b.d_queue, b.d_cam_init, b.d_cam_free, b.d_pt_init, b.d_pt_free,
                     b.d_pt_eoff, b.d_edge_cam, b.d_edge_fc, b.d_edge_pt, b.d_edge_uv, b.d_x[0], b.d_x[1], b.d_pt_vg,
-                    b.d_pt_lt, b.d_edge_w, b.d_edge_a, b.d_edge_e[0], b.d_edge_e[1], b.d_cam_list, b.d_pairs, b.d_edge_uvr, b.d_xr[0], b.d_xr[1], b.d_cam_out, b.d_pt_out,
+                    b.d_pt_lt, b.d_edge_w, b.d_edge_a, b.d_edge_e[0], b.d_edge_e[1], b.d_cam_list, b.d_pairs, b.d_edge_uvr, b.d_s, b.d_xr[0], b.d_xr[1], b.d_cam_out, b.d_pt_out,
                     b.d_trace, b.d_stats, b.d_debug, b.d_phase};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -1247,7 +1259,7 @@ cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int prec
     for (size_t i = 0; i < pb.host.size(); ++i)
         if (pb.host_status[i] == NAV_BA_OK) idx.push_back((int32_t)i);
     pb.desc.assign(pb.host.size(), WinDesc{});
-    int64_t nc = 0, np = 0, ne = 0, npair = 0;
+    int64_t nc = 0, np = 0, ne = 0, npair = 0, ns = 0;
     int max_m = 0, max_nc = 0;
     for (size_t i = 0; i < pb.host.size(); ++i) {
         const HostWindow& h = pb.host[i];
@@ -1257,7 +1269,9 @@ cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int prec
         d.e0 = (int32_t)ne; d.ne = h.ne;
         d.nfc = h.nfc; d.nfp = h.nfp;
         d.pair0 = npair; d.npair = h.n_pairs;
+        d.s0 = ns;
         nc += h.ncam; np += h.npt; ne += h.ne; npair += h.n_pairs;
+        ns += (int64_t)(6 * h.nfc) * (6 * h.nfc + 1) / 2;
         if (pb.host_status[i] == NAV_BA_OK) {
             max_m = std::max(max_m, 6 * h.nfc);
             max_nc = std::max(max_nc, h.ncam);
@@ -1317,6 +1331,7 @@ cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int prec
     ensure(&b.d_cam_list, sizeof(int32_t) * ne);
     ensure(&b.d_pairs, sizeof(uint32_t) * npair);
     ensure(&b.d_edge_uvr, precision == NAV_BA_MIXED ? rs * 2 * ne : 16);  // mixed form only
+    ensure(&b.d_s, precision == NAV_BA_MIXED ? sizeof(double) * ns : 16);
     ensure(&b.d_xr[0], precision == NAV_BA_MIXED ? rs * 4 * np : 16);
     ensure(&b.d_xr[1], precision == NAV_BA_MIXED ? rs * 4 * np : 16);
     ensure(&b.d_cam_out, sizeof(CamState) * nc);
