@@ -174,7 +174,7 @@ nav_ba_status build_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, c
         return set_err(ctx, NAV_BA_ERR_ARGUMENT, "pcg_max_iterations < 1");
     // validation and graph build of every problem spread over host threads; the first failing
     // problem (lowest index) is reported, as a sequential pass would
-    pb.host.assign(n, HostWindow());
+    pb.host.resize(n);  // the windows' host arrays are reused across calls (build_window rewrites them)
     pb.host_status.assign(n, NAV_BA_OK);
     std::vector<nav_ba_status> vst(n, NAV_BA_OK);
     std::vector<std::string> vwhy(n);
