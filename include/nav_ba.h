@@ -129,8 +129,10 @@ typedef struct nav_ba_result {
     double initial_cost;
     double final_cost;
     double final_lambda;
-    double time_setup_ms;         /* host-side structure build and upload                   */
-    double time_solve_ms;         /* device LM loop                                          */
+    double time_setup_ms;         /* host-side structure build and upload (batches of >= 64
+                                     windows: until the last part is launched, the device
+                                     already solving the earlier parts)                     */
+    double time_solve_ms;         /* device LM loop (pipelined batches: the wait after setup) */
     double time_download_ms;
     int32_t iterations_done;
     int32_t trials_accepted;

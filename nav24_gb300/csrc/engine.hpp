@@ -123,7 +123,7 @@ struct PreparedBatch {
 // Allocate (reusing pb.dev's buffers when large enough) and upload through pinned staging
 // (synchronous on return).  Returns a CUDA error or 0.
 cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int precision,
-                                int trace_stride, HostStaging& stg, std::string* why);
+                                int trace_stride, HostStaging& stg, HostPool& pool, std::string* why);
 void window_batch_free(WindowBatch& b);
 
 // Launch the persistent window kernel over all windows of the batch.

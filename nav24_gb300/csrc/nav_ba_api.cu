@@ -28,8 +28,18 @@ struct nav_ba_ctx {
     WindowLaunch shape[2];        // per precision (autotuned on nav_ba_prepare_batched)
     bool tuned[2] = {false, false};
     WindowBatch solve_dev;        // device buffers of nav_ba_solve / _batched, reused across calls
+    std::vector<HostWindow> solve_host;  // their host-side windows, reused across calls
     int grid_cluster = 8;         // CTAs of the grid engine's Cholesky cluster
     HostStaging stg;              // pinned staging reused across calls
+    // pipelined batched solves: the batch's parts, each with its windows, device buffers, pinned
+    // staging and stream (the host builds part k + 1 while the device solves part k)
+    struct Part {
+        std::vector<HostWindow> host;
+        WindowBatch dev;
+        HostStaging stg;
+        cudaStream_t stream = nullptr;
+    };
+    Part parts[4];
 };
 
 namespace {
@@ -164,9 +174,49 @@ cudaError_t autotune(nav_ba_ctx* ctx, PreparedBatch& pb, int precision) {
     return cudaSuccess;
 }
 
+// Checks of problem i of a batch: validate_problem and the batch rules (one calibration, one camera
+// model, distortion optimization only with PCG).
+nav_ba_status check_problem(const nav_ba_problem* probs, int i, const nav_ba_options* o, std::string* why) {
+    nav_ba_status s = validate_problem(&probs[i], why);
+    if (s == NAV_BA_OK && o->optimize_distortion && probs[i].camera_model == NAV_BA_CAM_PINHOLE_RADIAL &&
+        o->solver != NAV_BA_SOLVER_PCG) {
+        s = NAV_BA_ERR_UNSUPPORTED;
+        *why = "distortion optimization needs the PCG solver";
+    }
+    if (s == NAV_BA_OK && i > 0 && std::memcmp(probs[i].intrinsics, probs[0].intrinsics, sizeof(double) * 8) != 0) {
+        s = NAV_BA_ERR_UNSUPPORTED;
+        *why = "a batch shares one calibration";
+    }
+    if (s == NAV_BA_OK && i > 0 && probs[i].camera_model != probs[0].camera_model) {
+        s = NAV_BA_ERR_UNSUPPORTED;
+        *why = "a batch shares one camera model";
+    }
+    return s;
+}
+
+// The options and every problem of a batch checked over the host workers; the first failing
+// problem (lowest index) is reported, as a sequential pass would.
+nav_ba_status check_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, const nav_ba_options* o) {
+    std::string why;
+    nav_ba_status st = validate_options(o, &why);
+    if (st != NAV_BA_OK) return set_err(ctx, st, why);
+    if (o->solver == NAV_BA_SOLVER_PCG && o->pcg_max_iterations < 1)
+        return set_err(ctx, NAV_BA_ERR_ARGUMENT, "pcg_max_iterations < 1");
+    std::vector<nav_ba_status> vst(n, NAV_BA_OK);
+    std::vector<std::string> vwhy(n);
+    const int nth = HostPool::tasks_for(n, 8);
+    ctx->stg.pool.run(nth, [&](int t) {
+        for (int i = t; i < n; i += nth) vst[i] = check_problem(probs, i, o, &vwhy[i]);
+    });
+    for (int i = 0; i < n; ++i)
+        if (vst[i] != NAV_BA_OK) return set_err(ctx, vst[i], "problem " + std::to_string(i) + ": " + vwhy[i]);
+    return NAV_BA_OK;
+}
+
 // Validate and build all windows on the host.  Returns an error (nothing written) or OK.
+// checked: the caller has run check_batch over these problems already.
 nav_ba_status build_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, const nav_ba_options* o,
-                          PreparedBatch& pb) {
+                          PreparedBatch& pb, bool checked = false) {
     std::string why;
     nav_ba_status st = validate_options(o, &why);
     if (st != NAV_BA_OK) return set_err(ctx, st, why);
@@ -181,20 +231,7 @@ nav_ba_status build_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, c
     const int nth = HostPool::tasks_for(n, 8);
     auto work = [&](int t) {
         for (int i = t; i < n; i += nth) {
-            nav_ba_status s = validate_problem(&probs[i], &vwhy[i]);
-            if (s == NAV_BA_OK && o->optimize_distortion && probs[i].camera_model == NAV_BA_CAM_PINHOLE_RADIAL &&
-                o->solver != NAV_BA_SOLVER_PCG) {
-                s = NAV_BA_ERR_UNSUPPORTED;
-                vwhy[i] = "distortion optimization needs the PCG solver";
-            }
-            if (s == NAV_BA_OK && i > 0 && std::memcmp(probs[i].intrinsics, probs[0].intrinsics, sizeof(double) * 8) != 0) {
-                s = NAV_BA_ERR_UNSUPPORTED;
-                vwhy[i] = "a batch shares one calibration";
-            }
-            if (s == NAV_BA_OK && i > 0 && probs[i].camera_model != probs[0].camera_model) {
-                s = NAV_BA_ERR_UNSUPPORTED;
-                vwhy[i] = "a batch shares one camera model";
-            }
+            const nav_ba_status s = checked ? NAV_BA_OK : check_problem(probs, i, o, &vwhy[i]);
             vst[i] = s;
             if (s != NAV_BA_OK) continue;
             build_window(probs[i], *o, pb.host[i]);
@@ -204,7 +241,8 @@ nav_ba_status build_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, c
     };
     ctx->stg.pool.run(nth, work);
     for (int i = 0; i < n; ++i)
-        if (vst[i] != NAV_BA_OK) return set_err(ctx, vst[i], "problem " + std::to_string(i) + ": " + vwhy[i]);
+        if (vst[i] != NAV_BA_OK)
+            return set_err(ctx, vst[i], "problem " + std::to_string(i) + ": " + vwhy[i]);
     for (int i = 0; i < n; ++i)
         if (pb.host_status[i] == NAV_BA_OK && (o->solver == NAV_BA_SOLVER_PCG || !fits_window_engine(pb.host[i])))
             pb.host_status[i] = kGridWindow;  // the window engine is Cholesky-only
@@ -215,25 +253,27 @@ nav_ba_status build_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, c
 
 // Download results of every window into results[] (outputs of EMPTY windows: passthrough).
 nav_ba_status download_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, PreparedBatch& pb,
-                             nav_ba_result* results) {
+                             nav_ba_result* results, HostStaging* stg_in = nullptr, cudaStream_t stream = nullptr) {
     WindowBatch& b = pb.dev;
-    CamState* cams = (CamState*)ctx->stg.get(10, sizeof(CamState) * b.ncam);
-    double* pts = (double*)ctx->stg.get(11, sizeof(double) * 4 * b.npt);
-    double* trace = (double*)ctx->stg.get(12, sizeof(double) * (size_t)b.trace_stride * n);
-    WinStats* stats = (WinStats*)ctx->stg.get(13, sizeof(WinStats) * n);
+    HostStaging& stg = stg_in ? *stg_in : ctx->stg;
+    if (!stg_in) stream = ctx->stream;
+    CamState* cams = (CamState*)stg.get(10, sizeof(CamState) * b.ncam);
+    double* pts = (double*)stg.get(11, sizeof(double) * 4 * b.npt);
+    double* trace = (double*)stg.get(12, sizeof(double) * (size_t)b.trace_stride * n);
+    WinStats* stats = (WinStats*)stg.get(13, sizeof(WinStats) * n);
     if (!cams || !pts || !trace || !stats) return set_err(ctx, NAV_BA_ERR_OUT_OF_MEMORY, "pinned host allocation failed");
     cudaError_t e = cudaSuccess;
     int64_t d2h = 0;
     auto dn = [&](void* dst, const void* src, size_t bytes) {
         if (e != cudaSuccess || bytes == 0) return;
-        e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+        e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream);
         d2h += (int64_t)bytes;
     };
     dn(cams, b.d_cam_out, sizeof(CamState) * b.ncam);
     dn(pts, b.d_pt_out, sizeof(double) * 4 * b.npt);
     dn(trace, b.d_trace, sizeof(double) * (size_t)b.trace_stride * n);
     dn(stats, b.d_stats, sizeof(WinStats) * n);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) return cuda_status(ctx, e, "download");
     std::vector<int32_t> st_out(n, NAV_BA_OK);
     auto one = [&](int i) {
@@ -337,23 +377,134 @@ nav_ba_status solve_grid_window(nav_ba_ctx* ctx, const nav_ba_problem& p, const 
     return NAV_BA_OK;
 }
 
+// Batched solve in parts pipelined across the host and the device: part k is built on the host,
+// staged and uploaded, and its window kernel launched on the part's stream; the host goes on with
+// part k + 1 while the device solves part k (the parts' kernels also run side by side).  A window
+// is solved start to finish by one CTA (several milliseconds for the largest), so the parts take
+// the windows largest first: the last part, launched last, holds the smallest windows and ends
+// soon after its launch.  Windows are independent, so the results equal those of one launch over
+// the batch.  The whole batch is checked before any part is built, so errors are reported as by
+// the single-launch path (the first failing problem, nothing written).
+constexpr int kSolveParts = 4;  // 8 measured slower: 64-window parts leave host workers idle
+constexpr int kPipelineMinWindows = 64;
+
+nav_ba_status solve_pipelined(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, const nav_ba_options* o,
+                              nav_ba_result* results) {
+    const auto t0 = std::chrono::steady_clock::now();
+    nav_ba_status st = check_batch(ctx, probs, n, o);
+    if (st != NAV_BA_OK) return st;
+    // windows by decreasing size (observations, then cameras); part k takes the k-th quarter
+    std::vector<int32_t> perm(n);
+    for (int i = 0; i < n; ++i) perm[i] = i;
+    std::stable_sort(perm.begin(), perm.end(), [&](int32_t x, int32_t y) {
+        if (probs[x].n_obs != probs[y].n_obs) return probs[x].n_obs > probs[y].n_obs;
+        return probs[x].n_cams > probs[y].n_cams;
+    });
+    std::vector<nav_ba_problem> pp(n);
+    for (int j = 0; j < n; ++j) pp[j] = probs[perm[j]];
+    PreparedBatch pbs[kSolveParts];
+    for (int k = 0; k < kSolveParts; ++k) {
+        auto& part = ctx->parts[k];
+        if (!part.stream && cudaStreamCreateWithFlags(&part.stream, cudaStreamNonBlocking) != cudaSuccess) {
+            part.stream = nullptr;
+            return set_err(ctx, NAV_BA_ERR_CUDA, "cudaStreamCreate failed");
+        }
+        std::swap(pbs[k].host, part.host);
+        std::swap(pbs[k].dev, part.dev);
+    }
+    int launched = 0;
+    struct SwapBack {
+        PreparedBatch* pbs;
+        nav_ba_ctx* ctx;
+        int* launched;
+        ~SwapBack() {
+            for (int k = 0; k < *launched; ++k) cudaStreamSynchronize(ctx->parts[k].stream);  // nothing left in flight
+            for (int k = 0; k < kSolveParts; ++k) {
+                std::swap(pbs[k].host, ctx->parts[k].host);
+                std::swap(pbs[k].dev, ctx->parts[k].dev);
+            }
+        }
+    } swap_back{pbs, ctx, &launched};
+    auto part_lo = [&](int k) { return (int)((long long)n * k / kSolveParts); };
+    double t_build = 0.0;
+    for (int k = 0; k < kSolveParts; ++k) {
+        const int lo = part_lo(k), hi = part_lo(k + 1);
+        auto& part = ctx->parts[k];
+        const auto tb = std::chrono::steady_clock::now();
+        st = build_batch(ctx, pp.data() + lo, hi - lo, o, pbs[k], true);
+        t_build += ms_since(tb);
+        if (st != NAV_BA_OK) return st;
+        std::string why;
+        cudaError_t e = window_batch_upload(pbs[k], part.stream, o->precision, o->iterations + 1, part.stg, ctx->stg.pool, &why);
+        if (e != cudaSuccess) return cuda_status(ctx, e, "upload");
+        e = window_batch_launch(pbs[k], part.stream, o->precision, ctx->shape[o->precision], -1.0);
+        if (e != cudaSuccess) return cuda_status(ctx, e, "window kernel");
+        launched = k + 1;
+    }
+    const double t_setup = ms_since(t0);
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < kSolveParts; ++k) {
+        const cudaError_t ek = cudaStreamSynchronize(ctx->parts[k].stream);
+        if (e == cudaSuccess) e = ek;
+    }
+    if (e != cudaSuccess) return cuda_status(ctx, e, "window kernel");
+    const double t_solve = ms_since(t0) - t_setup;
+    const auto t1 = std::chrono::steady_clock::now();
+    // results in the parts' (size) order, then back to the caller's order
+    std::vector<nav_ba_result> tp(n);
+    for (int j = 0; j < n; ++j) {
+        tp[j] = results[perm[j]];
+        clear_stats(&tp[j]);
+    }
+    for (int k = 0; k < kSolveParts; ++k) {
+        const int lo = part_lo(k), hi = part_lo(k + 1);
+        st = download_batch(ctx, pp.data() + lo, hi - lo, pbs[k], tp.data() + lo, &ctx->parts[k].stg, ctx->parts[k].stream);
+        if (st != NAV_BA_OK && st != NAV_BA_EMPTY) return set_err(ctx, st, "a problem has a non-finite initial cost");
+        for (int j = lo; j < hi; ++j) {
+            if (pbs[k].host_status[j - lo] != kGridWindow) continue;
+            st = solve_grid_window(ctx, pp[j], pbs[k].host[j - lo], *o, tp[j]);
+            if (st != NAV_BA_OK) return st;
+        }
+    }
+    const double t_down = ms_since(t1);
+    const char* verbose = getenv("NAVBA_VERBOSE");
+    if (verbose && verbose[0] == '1')
+        fprintf(stderr, "[navba host] %d problems in %d parts: build %.2f ms, setup (checks, build, stage, upload, "
+                "launch; device already running) %.2f ms, wait %.2f ms, download %.2f ms\n", n, kSolveParts, t_build,
+                t_setup, t_solve, t_down);
+    for (int j = 0; j < n; ++j) {
+        tp[j].time_setup_ms = t_setup;
+        tp[j].time_solve_ms += t_solve;  // grid-engine problems already hold their own solve time
+        tp[j].time_download_ms = t_down;
+    }
+    for (int j = 0; j < n; ++j) results[perm[j]] = tp[j];
+    return NAV_BA_OK;
+}
+
 nav_ba_status solve_impl(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, const nav_ba_options* o,
                          nav_ba_result* results) {
     if (!ctx) return NAV_BA_ERR_ARGUMENT;
     if (!probs || !results || n < 0) return set_err(ctx, NAV_BA_ERR_ARGUMENT, "NULL argument");
+    if (n >= kPipelineMinWindows && o && o->solver == NAV_BA_SOLVER_CHOLESKY)
+        return solve_pipelined(ctx, probs, n, o, results);
     const auto t0 = std::chrono::steady_clock::now();
     PreparedBatch pb;
+    // the context's host windows and device buffers are reused (their arrays keep their capacity)
+    std::swap(pb.host, ctx->solve_host);
+    std::swap(pb.dev, ctx->solve_dev);
+    struct SwapBack {
+        PreparedBatch& pb;
+        nav_ba_ctx* ctx;
+        ~SwapBack() {
+            std::swap(pb.host, ctx->solve_host);
+            std::swap(pb.dev, ctx->solve_dev);
+        }
+    } swap_back{pb, ctx};
     nav_ba_status st = build_batch(ctx, probs, n, o, pb);
     if (st != NAV_BA_OK) return st;
     const double t_build = ms_since(t0);
     std::string why;
-    std::swap(pb.dev, ctx->solve_dev);  // reuse the context's device buffers
-    struct SwapBack {
-        PreparedBatch& pb;
-        nav_ba_ctx* ctx;
-        ~SwapBack() { std::swap(pb.dev, ctx->solve_dev); }
-    } swap_back{pb, ctx};
-    cudaError_t e = window_batch_upload(pb, ctx->stream, o->precision, o->iterations + 1, ctx->stg, &why);
+    cudaError_t e = window_batch_upload(pb, ctx->stream, o->precision, o->iterations + 1, ctx->stg, ctx->stg.pool, &why);
     if (e != cudaSuccess) return cuda_status(ctx, e, "upload");
     const double t_setup = ms_since(t0);
     cudaEventRecord(ctx->ev0, ctx->stream);
@@ -431,6 +582,11 @@ void nav_ba_destroy(nav_ba_ctx* ctx) {
     cudaSetDevice(ctx->device);
     window_batch_free(ctx->prepared.dev);
     window_batch_free(ctx->solve_dev);
+    for (auto& part : ctx->parts) {
+        window_batch_free(part.dev);
+        part.stg.release();
+        if (part.stream) cudaStreamDestroy(part.stream);
+    }
     ctx->pose.release();
     ctx->stg.release();
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -479,7 +635,7 @@ nav_ba_status nav_ba_prepare_batched(nav_ba_ctx* ctx, const nav_ba_problem* p, i
                            "nav_ba_prepare: problem " + std::to_string(i) + " exceeds the window engine (" +
                                std::to_string(kWinMaxFreeCams) + " free cameras); use nav_ba_solve");
     std::string why;
-    cudaError_t e = window_batch_upload(pb, ctx->stream, o->precision, o->iterations + 1, ctx->stg, &why);
+    cudaError_t e = window_batch_upload(pb, ctx->stream, o->precision, o->iterations + 1, ctx->stg, ctx->stg.pool, &why);
     if (e != cudaSuccess) return cuda_status(ctx, e, "upload");
     e = autotune(ctx, pb, o->precision);
     if (e != cudaSuccess) return cuda_status(ctx, e, "autotune");
@@ -611,7 +767,7 @@ nav_ba_status nav_ba_reduced_system(nav_ba_ctx* ctx, const nav_ba_problem* p, co
     }
     std::string why;
     std::swap(pb.dev, ctx->solve_dev);
-    cudaError_t e = window_batch_upload(pb, ctx->stream, o1.precision, 2, ctx->stg, &why);
+    cudaError_t e = window_batch_upload(pb, ctx->stream, o1.precision, 2, ctx->stg, ctx->stg.pool, &why);
     if (e == cudaSuccess) e = window_batch_launch(pb, ctx->stream, o1.precision, ctx->shape[o1.precision], lambda);
     const int m = 6 * h.nfc;
     std::vector<double> out((size_t)m * m + m);

@@ -1253,7 +1253,7 @@ void parallel_for(HostPool& pool, int n, Fn fn) {
 }  // namespace
 
 cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int precision, int trace_stride,
-                                HostStaging& stg, std::string* why) {
+                                HostStaging& stg, HostPool& pool, std::string* why) {
     WindowBatch& b = pb.dev;
     std::vector<int32_t> idx;
     for (size_t i = 0; i < pb.host.size(); ++i)
@@ -1375,7 +1375,7 @@ cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int prec
     }
     std::copy(pb.desc.begin(), pb.desc.end(), desc);
     std::copy(order.begin(), order.end(), ord);
-    parallel_for(stg.pool, (int)nw, [&](int i) {
+    parallel_for(pool, (int)nw, [&](int i) {
         const HostWindow& h = pb.host[i];
         const WinDesc& d = pb.desc[i];
         std::copy(h.cam.begin(), h.cam.end(), cam + d.cam0);

@@ -132,6 +132,38 @@ def test_batched_windows_match_oracle_per_window(ctx):
         assert np.allclose(g.points, r.points, rtol=0, atol=1e-5)
 
 
+@pytest.mark.parametrize("precision", [abi.FP64, abi.MIXED])
+def test_pipelined_batch_equals_single_solves(ctx, precision):
+    """A batch of >= 64 windows runs in parts pipelined across host and device; every window's
+    result equals (bitwise) that of solving the window alone."""
+    s = Synth(2, n_windows=96, seed=8)
+    wins = s.windows()
+    o = workload_options(2, precision=precision)
+    gs = ctx.solve_batched(wins, o)
+    for i in [0, 23, 24, 47, 50, 71, 72, 95]:  # both sides of every part boundary
+        g1 = ctx.solve(wins[i], o)
+        assert gs[i].status == g1.status == abi.OK
+        assert gs[i].stats["final_cost"] == g1.stats["final_cost"]
+        assert np.array_equal(gs[i].points, g1.points)
+        assert np.array_equal(gs[i].cam_pose, g1.cam_pose)
+
+
+def test_pipelined_batch_reports_first_bad_window(ctx):
+    """An invalid window in a later part fails the call with its own index; nothing is written."""
+    from nav24_gb300._lib import BAError
+    s = Synth(2, n_windows=80, seed=9)
+    wins = s.windows()
+    wins[70] = wins[70].copy()
+    wins[70].points[3, 1] = np.nan
+    with pytest.raises(BAError) as ei:
+        ctx.solve_batched(wins, workload_options(2))
+    assert ei.value.status == abi.ERR_NONFINITE_INPUT
+    assert "problem 70" in str(ei.value)
+    # the context stays usable
+    g = ctx.solve_batched(wins[:70], workload_options(2))
+    assert all(r.status == abi.OK for r in g)
+
+
 def test_batched_mixed_reaches_fp64_cost(ctx):
     s = Synth(2, n_windows=16, seed=6)
     wins = s.windows()
