@@ -472,10 +472,23 @@ nav_ba_status solve_pipelined(nav_ba_ctx* ctx, const nav_ba_problem* probs, int 
         fprintf(stderr, "[navba host] %d problems in %d parts: build %.2f ms, setup (checks, build, stage, upload, "
                 "launch; device already running) %.2f ms, wait %.2f ms, download %.2f ms\n", n, kSolveParts, t_build,
                 t_setup, t_solve, t_down);
+    // byte counts of the whole call (each part's download reported its own)
+    int64_t h2d = 0, d2h = 0;
+    for (int k = 0; k < kSolveParts; ++k) {
+        const int lo = part_lo(k), hi = part_lo(k + 1);
+        h2d += pbs[k].dev.h2d_bytes;
+        for (int j = lo; j < hi; ++j)
+            if (pbs[k].host_status[j - lo] == NAV_BA_OK) {
+                d2h += tp[j].d2h_bytes;
+                break;
+            }
+    }
     for (int j = 0; j < n; ++j) {
         tp[j].time_setup_ms = t_setup;
         tp[j].time_solve_ms += t_solve;  // grid-engine problems already hold their own solve time
         tp[j].time_download_ms = t_down;
+        tp[j].h2d_bytes = h2d;
+        tp[j].d2h_bytes = d2h;
     }
     for (int j = 0; j < n; ++j) results[perm[j]] = tp[j];
     return NAV_BA_OK;

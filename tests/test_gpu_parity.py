@@ -140,7 +140,8 @@ def test_pipelined_batch_equals_single_solves(ctx, precision):
     wins = s.windows()
     o = workload_options(2, precision=precision)
     gs = ctx.solve_batched(wins, o)
-    for i in [0, 23, 24, 47, 50, 71, 72, 95]:  # both sides of every part boundary
+    assert len({g.stats["h2d_bytes"] for g in gs}) == 1  # the whole call's bytes in every result
+    for i in [0, 23, 24, 47, 50, 71, 72, 95]:
         g1 = ctx.solve(wins[i], o)
         assert gs[i].status == g1.status == abi.OK
         assert gs[i].stats["final_cost"] == g1.stats["final_cost"]
