@@ -6,10 +6,24 @@
 
 namespace navba {
 
+// x * 0 is 0 for every finite x and NaN for NaN and +-Inf, so sums of x * 0 in independent
+// accumulators are 0 exactly when every value is finite (branch-free: the loop vectorizes).
 static bool all_finite(const double* a, long long n) {
-    for (long long i = 0; i < n; ++i)
-        if (!std::isfinite(a[i])) return false;
-    return true;
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    long long i = 0;
+    for (; i + 8 <= n; i += 8)
+        for (int k = 0; k < 8; ++k) acc[k] += a[i + k] * 0.0;
+    for (; i < n; ++i) acc[0] += a[i] * 0.0;
+    double t = 0.0;
+    for (int k = 0; k < 8; ++k) t += acc[k];
+    return t == 0.0;
+}
+
+// Every index in [0, bound) (branch-free).
+static bool all_below(const int32_t* v, long long n, int32_t bound) {
+    uint32_t bad = 0;
+    for (long long i = 0; i < n; ++i) bad |= (uint32_t)v[i] >= (uint32_t)bound;
+    return bad == 0;
 }
 
 nav_ba_status validate_problem(const nav_ba_problem* p, std::string* why) {
@@ -25,10 +39,8 @@ nav_ba_status validate_problem(const nav_ba_problem* p, std::string* why) {
     if (p->camera_model != NAV_BA_CAM_PINHOLE && p->camera_model != NAV_BA_CAM_PINHOLE_RADIAL &&
         p->camera_model != NAV_BA_CAM_KANNALA_BRANDT8)
         return fail(NAV_BA_ERR_ARGUMENT, "unknown camera model");
-    for (int o = 0; o < p->n_obs; ++o)
-        if (p->obs_cam[o] < 0 || p->obs_cam[o] >= p->n_cams || p->obs_point[o] < 0 ||
-            p->obs_point[o] >= p->n_points)
-            return fail(NAV_BA_ERR_ARGUMENT, "observation index out of range");
+    if (!all_below(p->obs_cam, p->n_obs, p->n_cams) || !all_below(p->obs_point, p->n_obs, p->n_points))
+        return fail(NAV_BA_ERR_ARGUMENT, "observation index out of range");
     if (!all_finite(p->cam_pose, 12LL * p->n_cams) || !all_finite(p->points, 3LL * p->n_points) ||
         !all_finite(p->obs_uv, 2LL * p->n_obs) || !all_finite(p->intrinsics, 8))
         return fail(NAV_BA_ERR_NONFINITE_INPUT, "non-finite input value");
@@ -97,11 +109,46 @@ void build_window(const nav_ba_problem& p, const nav_ba_options& o, HostWindow& 
     w.pt.assign(4LL * w.npt, 0.0);
     for (int i = 0; i < w.npt; ++i)
         for (int k = 0; k < 3; ++k) w.pt[4LL * i + k] = p.points[3LL * i + k];
-    // Schur pairs (same free point, free cameras, b <= a) and the distinct lower blocks they touch,
-    // in one pass over each point's free-camera edges
+    // Schur pairs (same free point, free cameras, b <= a) and the distinct lower blocks they touch.
+    // Up to 64 free cameras: per point the mask of its free cameras gives k(k+1)/2 pairs (when no
+    // camera observes the point twice) and each row's lower blocks by an OR; beyond, or with a
+    // repeated camera, the pairs are counted one by one.
     w.n_pairs = 0;
     w.n_schur_blocks = w.nfc;  // the diagonal blocks
-    if (w.nfc > 0) {
+    if (w.nfc > 0 && w.nfc <= 64) {
+        std::vector<uint64_t> row(w.nfc, 0);  // row a: cameras b < a sharing a point with a
+        for (int i = 0; i < w.npt; ++i) {
+            if (w.pt_free[i] < 0) continue;
+            uint64_t m = 0;
+            int k = 0;
+            bool repeat = false;
+            for (int e = w.pt_eoff[i]; e < w.pt_eoff[i + 1]; ++e) {
+                const int a = w.cam_free[w.edge_cam[e]];
+                if (a < 0) continue;
+                const uint64_t bit = 1ull << a;
+                repeat = repeat || (m & bit);
+                m |= bit;
+                ++k;
+            }
+            if (!repeat) {
+                w.n_pairs += (int64_t)k * (k + 1) / 2;
+            } else {
+                for (int e = w.pt_eoff[i]; e < w.pt_eoff[i + 1]; ++e) {
+                    const int a = w.cam_free[w.edge_cam[e]];
+                    if (a < 0) continue;
+                    for (int f = w.pt_eoff[i]; f < w.pt_eoff[i + 1]; ++f) {
+                        const int b = w.cam_free[w.edge_cam[f]];
+                        if (b >= 0 && b <= a) ++w.n_pairs;
+                    }
+                }
+            }
+            for (uint64_t r = m; r; r &= r - 1) {
+                const int a = __builtin_ctzll(r);
+                row[a] |= m & ((1ull << a) - 1);
+            }
+        }
+        for (int a = 0; a < w.nfc; ++a) w.n_schur_blocks += __builtin_popcountll(row[a]);
+    } else if (w.nfc > 0) {
         std::vector<uint8_t> seen((size_t)w.nfc * w.nfc, 0);
         std::vector<int32_t> fc;
         for (int i = 0; i < w.npt; ++i) {
