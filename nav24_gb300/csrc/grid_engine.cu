@@ -179,25 +179,22 @@ __global__ void k_schur_blocks(WinArgs<Real> A, const int2* blocks, const int32_
                 for (int r = 0; r < 6; ++r) accb[r] += ai[r * 3 + 0] * t0 + ai[r * 3 + 1] * t1 + ai[r * 3 + 2] * t2;
             }
         }
-#pragma unroll
-        for (int k = 0; k < 36; ++k)
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_xor_sync(kFullG, acc[k], o);
+        Real sums[2];
+        reduce_scatter36(acc, c.lane, sums[0], sums[1]);  // lane: the two entries it writes
+        const int slot = rs36_slot(c.lane);
         if (a == b) {
 #pragma unroll
             for (int k = 0; k < 6; ++k)
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) accb[k] += __shfl_xor_sync(kFullG, accb[k], o);
         }
-        // every lane holds every sum: lane l writes entries l and l + 32, so each FP64 operation is
-        // one warp instruction with all lanes active (the FP64 pipe is charged per warp instruction)
+        // one FP64 warp instruction per operation with all lanes active (charged per warp instruction)
 #pragma unroll
         for (int rnd = 0; rnd < 2; ++rnd) {
-            const int k = c.lane + 32 * rnd;
-            const Real vk = lane_value<36>(acc, k);
+            const int k = slot + rnd;
             const int r = k / 6, q = k % 6;
             if (k < 36 && !(a == b && q > r)) {
-                double v = -(double)vk;
+                double v = -(double)sums[rnd];
                 if (a == b) {
                     v += U[28LL * a + tri(r, q)];
                     if (r == q) v += lambda;

@@ -268,6 +268,40 @@ __device__ __forceinline__ void cam_load(const Real* cr, Real* o) {
     }
 }
 
+// Warp reduce-scatter of 36 per-lane values (a 6x6 block's partial sums): each exchange sends the
+// half of the lane's current values that its partner keeps, so 32 + 16 + 8 + 4 + 2 = 62 shuffles
+// instead of 36 x 5 for a full butterfly.  Lane l ends with the sums of entries rs36_slot(l) and
+// rs36_slot(l) + 1 (entries 36..63 are zero padding).  v is clobbered.
+__device__ __forceinline__ int rs36_slot(int lane) {
+    return 32 * ((lane >> 4) & 1) + 16 * ((lane >> 3) & 1) + 8 * ((lane >> 2) & 1) + 4 * ((lane >> 1) & 1) + 2 * (lane & 1);
+}
+
+template <class T>
+__device__ __forceinline__ void reduce_scatter36(T* v, int lane, T& s0, T& s1) {
+    constexpr unsigned kAll = 0xffffffffu;
+    {
+        const bool hi = (lane & 16) != 0;
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+            const T a = v[i], b = i + 32 < 36 ? v[i + 32 < 36 ? i + 32 : 0] : T(0);
+            const T send = hi ? a : b, keep = hi ? b : a;
+            v[i] = keep + __shfl_xor_sync(kAll, send, 16);
+        }
+    }
+#pragma unroll
+    for (int st = 0; st < 4; ++st) {
+        const int o = 8 >> st, n = 16 >> st;
+        const bool hi = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < n; ++i) {
+            const T send = hi ? v[i] : v[i + n], keep = hi ? v[i + n] : v[i];
+            v[i] = keep + __shfl_xor_sync(kAll, send, o);
+        }
+    }
+    s0 = v[0];
+    s1 = v[1];
+}
+
 // v[k] for a runtime k < N (0 otherwise) from a register array, by selects (no local-memory copy).
 template <int N, class Real>
 __device__ __forceinline__ Real lane_value(const Real* v, int k) {

@@ -352,16 +352,14 @@ __device__ double linearize_cameras(const WinArgs<Real>& A, const CC& c, const W
 }
 
 // Sums one S block's lane partials over the warp and writes -sum (plus U_a + lambda I on the
-// diagonal) into rank 0's packed S, and b'_a = g'_a - sum A t on the diagonal.  After the butterfly
-// every lane holds every sum; lane l writes entries l and l + 32, so each FP64 operation is one warp
-// instruction with all lanes active (GB300's FP64 pipe costs 16 cycles per warp instruction, however
-// few lanes are active).
+// diagonal) into the packed S, and b'_a = g'_a - sum A t on the diagonal.  The reduce-scatter leaves
+// each lane the two entries it writes, so each FP64 operation is one warp instruction with all lanes
+// active (GB300's FP64 pipe costs 16 cycles per warp instruction, however few lanes are active).
 template <class Real>
 __device__ __forceinline__ void write_block(const CC& c, int a, int b, Real* acc, Real* accb, double lambda) {
-#pragma unroll
-    for (int k = 0; k < 36; ++k)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_xor_sync(kFull, acc[k], o);
+    Real sums[2];
+    reduce_scatter36(acc, c.lane, sums[0], sums[1]);
+    const int k0 = rs36_slot(c.lane);
     if (a == b) {
 #pragma unroll
         for (int k = 0; k < 6; ++k)
@@ -370,11 +368,10 @@ __device__ __forceinline__ void write_block(const CC& c, int a, int b, Real* acc
     }
 #pragma unroll
     for (int rnd = 0; rnd < 2; ++rnd) {
-        const int k = c.lane + 32 * rnd;
-        const Real vk = lane_value<36>(acc, k);
+        const int k = k0 + rnd;
         const int r = k / 6, q = k % 6;
         if (k < 36 && !(a == b && q > r)) {
-            double v = -(double)vk;
+            double v = -(double)sums[rnd];
             if (a == b) {
                 v += c.s0->U[a][tri(r, q)];
                 if (r == q) v += lambda;

@@ -160,9 +160,16 @@ def test_pipelined_batch_reports_first_bad_window(ctx):
         ctx.solve_batched(wins, workload_options(2))
     assert ei.value.status == abi.ERR_NONFINITE_INPUT
     assert "problem 70" in str(ei.value)
-    # the context stays usable
-    g = ctx.solve_batched(wins[:70], workload_options(2))
-    assert all(r.status == abi.OK for r in g)
+    # the context stays usable; an empty window inside a pipelined batch is passed through
+    good = wins[:70]
+    e = good[40]
+    good[40] = abi.Problem(cam_pose=e.cam_pose, points=e.points, obs_uv=np.zeros((0, 2)), obs_cam=[], obs_point=[],
+                           intrinsics=e.intrinsics)
+    g = ctx.solve_batched(good, workload_options(2))
+    assert g[40].status == abi.EMPTY and np.array_equal(g[40].points, e.points)
+    assert all(r.status == abi.OK for i, r in enumerate(g) if i != 40)
+    g1 = ctx.solve(good[39], workload_options(2))
+    assert g[39].stats["final_cost"] == g1.stats["final_cost"]
 
 
 def test_batched_mixed_reaches_fp64_cost(ctx):
