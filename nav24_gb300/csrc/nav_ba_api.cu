@@ -40,6 +40,10 @@ struct nav_ba_ctx {
         cudaStream_t stream = nullptr;
     };
     Part parts[4];
+    // nav_ba_run's launch sequence over the prepared batch (queue reset, persistent kernel),
+    // captured once in a CUDA graph at prepare time and replayed by every run with the same options
+    cudaGraphExec_t run_graph = nullptr;
+    LmOptions graph_lm{};
 };
 
 namespace {
@@ -172,6 +176,29 @@ cudaError_t autotune(nav_ba_ctx* ctx, PreparedBatch& pb, int precision) {
         fprintf(stderr, "[navba autotune] precision=%d cluster=%d threads=%d %.3f ms\n", precision, best_shape.cluster,
                 best_shape.threads, best);
     return cudaSuccess;
+}
+
+// Captures the prepared batch's launch sequence in ctx->run_graph (null if capture fails: the runs
+// then launch directly).
+void capture_run_graph(nav_ba_ctx* ctx, int precision) {
+    if (ctx->run_graph) cudaGraphExecDestroy(ctx->run_graph);
+    ctx->run_graph = nullptr;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    const cudaError_t le = window_batch_launch(ctx->prepared, ctx->stream, precision, ctx->shape[precision], -1.0);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    if (le == cudaSuccess && e == cudaSuccess && g) e = cudaGraphInstantiate(&ctx->run_graph, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (le != cudaSuccess || e != cudaSuccess) {
+        if (ctx->run_graph) cudaGraphExecDestroy(ctx->run_graph);
+        ctx->run_graph = nullptr;
+        cudaGetLastError();
+        return;
+    }
+    ctx->graph_lm = ctx->prepared.lm;
 }
 
 // Checks of problem i of a batch: validate_problem and the batch rules (one calibration, one camera
@@ -595,6 +622,7 @@ void nav_ba_destroy(nav_ba_ctx* ctx) {
     cudaSetDevice(ctx->device);
     window_batch_free(ctx->prepared.dev);
     window_batch_free(ctx->solve_dev);
+    if (ctx->run_graph) cudaGraphExecDestroy(ctx->run_graph);
     for (auto& part : ctx->parts) {
         window_batch_free(part.dev);
         part.stg.release();
@@ -636,6 +664,10 @@ nav_ba_status nav_ba_prepare_batched(nav_ba_ctx* ctx, const nav_ba_problem* p, i
     if (!p || !o || n < 0) return set_err(ctx, NAV_BA_ERR_ARGUMENT, "NULL argument");
     cudaSetDevice(ctx->device);
     ctx->has_prepared = false;
+    if (ctx->run_graph) {  // its buffers may be reallocated: captured again below
+        cudaGraphExecDestroy(ctx->run_graph);
+        ctx->run_graph = nullptr;
+    }
     PreparedBatch& pb = ctx->prepared;
     pb.host.clear();
     pb.host_status.clear();
@@ -652,6 +684,7 @@ nav_ba_status nav_ba_prepare_batched(nav_ba_ctx* ctx, const nav_ba_problem* p, i
     if (e != cudaSuccess) return cuda_status(ctx, e, "upload");
     e = autotune(ctx, pb, o->precision);
     if (e != cudaSuccess) return cuda_status(ctx, e, "autotune");
+    capture_run_graph(ctx, o->precision);
     ctx->prepared_problems.assign(p, p + n);
     ctx->prepared_opts = *o;
     ctx->has_prepared = true;
@@ -684,7 +717,11 @@ nav_ba_status nav_ba_run(nav_ba_ctx* ctx, const nav_ba_options* o, nav_ba_result
     cudaSetDevice(ctx->device);
     if (o) ctx->prepared.lm = lm_options(*o);
     cudaEventRecord(ctx->ev0, ctx->stream);
-    cudaError_t e = window_batch_launch(ctx->prepared, ctx->stream, po.precision, ctx->shape[po.precision], -1.0);
+    cudaError_t e;
+    if (ctx->run_graph && std::memcmp(&ctx->graph_lm, &ctx->prepared.lm, sizeof(LmOptions)) == 0)
+        e = cudaGraphLaunch(ctx->run_graph, ctx->stream);  // the launch captured at prepare time
+    else
+        e = window_batch_launch(ctx->prepared, ctx->stream, po.precision, ctx->shape[po.precision], -1.0);
     cudaEventRecord(ctx->ev1, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_status(ctx, e, "window kernel");

@@ -233,6 +233,27 @@ def test_prepare_run_fetch_equals_solve(ctx):
     assert np.array_equal(f.cam_pose, g.cam_pose)
 
 
+def test_run_replays_captured_launch_and_follows_new_options(ctx):
+    """nav_ba_run replays the launch captured at prepare time; a run with other LM options (same
+    precision and iterations) launches with those.  (Runs share the shape tuned at prepare time, so
+    they compare bitwise among themselves; against solves, which may run another shape, the mixed
+    form's partial sums differ in the last bits.)"""
+    import copy
+    s = Synth(2, n_windows=8, seed=12)
+    p = s.window(3)
+    o = workload_options(2, precision=abi.MIXED)
+    o2 = copy.copy(o)
+    o2.tau = o.tau * 100.0
+    o2.robust = 1 - o.robust
+    g, g2 = ctx.solve(p, o), ctx.solve(p, o2)
+    ctx.prepare(p, o)
+    r1, r2, r3 = ctx.run(o), ctx.run(o2), ctx.run(o)
+    assert r3["final_cost"] == r1["final_cost"]
+    assert r2["final_cost"] != r1["final_cost"]
+    assert abs(r1["final_cost"] - g.stats["final_cost"]) / g.stats["final_cost"] < 1e-9
+    assert abs(r2["final_cost"] - g2.stats["final_cost"]) / g2.stats["final_cost"] < 1e-9
+
+
 def test_fp64_solve_is_bitwise_repeatable(ctx):
     p = Synth(2, n_windows=1, seed=9).window(0)
     o = workload_options(2)
