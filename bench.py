@@ -56,6 +56,8 @@ def parse():
                          "secondary workload (for profiler captures)")
     ap.add_argument("--no-secondary", action="store_true", help="skip the secondary workloads")
     ap.add_argument("--pcg-cams", type=int, default=1000, help="cameras of the figure-eight PCG workload")
+    ap.add_argument("--profile-precision", choices=["both", "fp64", "mixed"], default="both",
+                    help="precisions the grid and PCG profile cases run")
     ap.add_argument("--pcg-points", type=int, default=500000, help="points of the figure-eight PCG workload")
     return ap.parse_args()
 
@@ -252,12 +254,14 @@ def time_device(ctx, wins, opt, steps, warmup, dist):
     return ms, stats, results
 
 
-def solve_pair(ctx, p, family):
+def solve_pair(ctx, p, family, precisions=("fp64", "mixed")):
     """One warm-up and one timed solve of problem p in each precision; device time per solve."""
     from nav24_gb300 import abi
     from nav24_gb300.synth import workload_options
     out = {}
     for name, prec in (("fp64", abi.FP64), ("mixed", abi.MIXED)):
+        if name not in precisions:
+            continue
         o = workload_options(family, prec)
         ctx.solve(p, o)
         r = ctx.solve(p, o)
@@ -265,12 +269,13 @@ def solve_pair(ctx, p, family):
         out[name] = {"obs_per_s": r.stats["edge_iterations"] / t, "lm_iter_per_s": r.stats["iterations_done"] / t,
                      "ms": t * 1e3, "final_cost": r.stats["final_cost"], "initial_cost": r.stats["initial_cost"],
                      "iterations": r.stats["iterations_done"], "pcg_iterations": r.stats["pcg_iterations_total"]}
-    out["mixed_over_fp64"] = out["mixed"]["obs_per_s"] / out["fp64"]["obs_per_s"]
-    out["final_cost_rel_diff"] = abs(out["mixed"]["final_cost"] - out["fp64"]["final_cost"]) / out["fp64"]["final_cost"]
+    if len(out) == 2:
+        out["mixed_over_fp64"] = out["mixed"]["obs_per_s"] / out["fp64"]["obs_per_s"]
+        out["final_cost_rel_diff"] = abs(out["mixed"]["final_cost"] - out["fp64"]["final_cost"]) / out["fp64"]["final_cost"]
     return out
 
 
-def secondary_workloads(ctx, only=None, pcg_cams=1000, pcg_points=500000):
+def secondary_workloads(ctx, only=None, pcg_cams=1000, pcg_points=500000, precisions=("fp64", "mixed")):
     """One solve of each other named workload (device time, including the per-solve upload)."""
     from nav24_gb300 import abi
     from nav24_gb300.synth import Synth, workload_options
@@ -279,7 +284,7 @@ def secondary_workloads(ctx, only=None, pcg_cams=1000, pcg_points=500000):
         p = Synth(1).window(0)
         out["grid_200cams"] = {"workload": "200 cameras on a 20x10 grid facing down, 50,000 points, Huber 2 px, "
                                            "20 LM iterations (family 1, seed 1001), grid engine, Cholesky",
-                               "observations": p.n_obs, **solve_pair(ctx, p, 1)}
+                               "observations": p.n_obs, **solve_pair(ctx, p, 1, precisions)}
     if only in (None, "vjp"):
         p = Synth(3).window(0)
         o = workload_options(3)
@@ -316,7 +321,7 @@ def secondary_workloads(ctx, only=None, pcg_cams=1000, pcg_points=500000):
             "workload": f"{pcg_cams} cameras on a {2 * pcg_cams} m figure-eight, {pcg_points} points, shared radial "
                         "k1/k2 optimized, 5% outliers, Huber 1.5 px, 30 LM iterations, PCG (block-Jacobi, tol 1e-6, "
                         "<= 100 iterations) (family 4, seed 1004), grid engine", "observations": p.n_obs,
-            **solve_pair(ctx, p, 4)}
+            **solve_pair(ctx, p, 4, precisions)}
     return out
 
 
@@ -339,7 +344,8 @@ def main():
     of = workload_options(2, abi.FP64)
 
     if args.profile_case in ("grid", "pcg", "vjp", "pose"):
-        print(json.dumps(secondary_workloads(ctx, args.profile_case, args.pcg_cams, args.pcg_points)), flush=True)
+        precs = ("fp64", "mixed") if args.profile_precision == "both" else (args.profile_precision,)
+        print(json.dumps(secondary_workloads(ctx, args.profile_case, args.pcg_cams, args.pcg_points, precs)), flush=True)
         ctx.close()
         dist.close()
         return

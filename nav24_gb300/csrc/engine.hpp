@@ -181,7 +181,7 @@ struct GridVjp {
 // reduced system at damping debug_lambda and return [S (m*m, row-major, lower part) | b'].
 // vjp != nullptr (FP64 only): record or replay the damping schedule and run the backward.
 cudaError_t grid_solve(const HostWindow& h, const LmOptions& lm, const Intr& intr, int precision,
-                       cudaStream_t stream, int cluster, GridResult& out, double debug_lambda,
+                       cudaStream_t stream, HostPool* pool, GridResult& out, double debug_lambda,
                        std::vector<double>* debug_S, GridVjp* vjp = nullptr);
 
 // Motion-only BA (pose_engine.cu): per problem descriptor, statistics, and the reused device buffers.

@@ -26,6 +26,9 @@
 #include <cstdlib>
 #include <cmath>
 #include <cstring>
+#include <functional>
+#include <memory>
+#include <thread>
 #include <type_traits>
 
 #include <cooperative_groups.h>
@@ -148,10 +151,13 @@ __global__ void k_schur_points(WinArgs<Real> A, WinDesc D, double lambda, const 
     block_partial<false>((double)schur_points<Real>(A, c, D, lambda, camr, X), part);
 }
 
-// Warp per nonzero block (a >= b) of S over its pair list; dense row-major S (m x m, lower part).
+// Warp per nonzero block (a >= b) of S over its pair list; dense row-major S (m x m, lower part),
+// or, with Sb, block rows of both triangles in Real (row-major 6x6 per slot; bslot[blk]: the slot
+// of the block and of its transpose, -1 on the diagonal, whose block is written whole).
 template <class Real>
 __global__ void k_schur_blocks(WinArgs<Real> A, const int2* blocks, const int32_t* boff, int nblk, const int2* pairs,
-                               const double* U, double lambda, double* S, int m, double* bs) {
+                               const double* U, double lambda, double* S, int m, double* bs, Real* Sb,
+                               const int2* bslot) {
     const CC c = grid_view();
     for (int blk = c.gw; blk < nblk; blk += c.CW) {
         const int a = blocks[blk].x, b = blocks[blk].y;
@@ -189,17 +195,23 @@ __global__ void k_schur_blocks(WinArgs<Real> A, const int2* blocks, const int32_
                 for (int o = 16; o > 0; o >>= 1) accb[k] += __shfl_xor_sync(kFullG, accb[k], o);
         }
         // one FP64 warp instruction per operation with all lanes active (charged per warp instruction)
+        const int2 bs2 = Sb ? bslot[blk] : make_int2(0, -1);
 #pragma unroll
         for (int rnd = 0; rnd < 2; ++rnd) {
             const int k = slot + rnd;
             const int r = k / 6, q = k % 6;
-            if (k < 36 && !(a == b && q > r)) {
+            if (k < 36 && (Sb || !(a == b && q > r))) {
                 double v = -(double)sums[rnd];
                 if (a == b) {
-                    v += U[28LL * a + tri(r, q)];
+                    v += U[28LL * a + (r >= q ? tri(r, q) : tri(q, r))];
                     if (r == q) v += lambda;
                 }
-                S[(size_t)(6 * a + r) * m + 6 * b + q] = v;
+                if (Sb) {
+                    Sb[36LL * bs2.x + k] = (Real)v;
+                    if (bs2.y >= 0) Sb[36LL * bs2.y + q * 6 + r] = (Real)v;
+                } else {
+                    S[(size_t)(6 * a + r) * m + 6 * b + q] = v;
+                }
             }
         }
         if (a == b) {
@@ -661,16 +673,9 @@ __global__ void k_pcg_diag_items(WinArgs<Real> A, const int4* items, int n_items
     }
 }
 
-// Per free camera: P_a = U_a + lambda I - sum A A^T, FP64 Cholesky (packed lower L, with 1/L_jj in
-// the diagonal slots of pinv); b'_a = g_a - sum A t.  pc[28 a]: 21 L entries + 6 inverse diagonal.
-__global__ void k_pcg_precond(const double* U, const double* aat, int nfc, double lambda, double* pc, double* b,
-                              int32_t* ok) {
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= nfc) return;
-    double P[21];
-    for (int k = 0; k < 21; ++k) P[k] = U[28LL * a + k] - aat[28LL * a + k];
-    for (int r = 0; r < 6; ++r) P[tri(r, r)] += lambda;
-    double rinv[6];
+// FP64 Cholesky of a packed 6x6 block in place (lower L) and 1/L_jj; false (with the pivot
+// replaced by 1) if the block is not positive definite.
+__device__ bool chol6_packed(double (&P)[21], double (&rinv)[6]) {
     bool good = true;
     for (int j = 0; j < 6; ++j) {
         double d = P[tri(j, j)];
@@ -688,10 +693,73 @@ __global__ void k_pcg_precond(const double* U, const double* aat, int nfc, doubl
             P[tri(i, j)] = v * r;
         }
     }
+    return good;
+}
+
+// Per free camera: P_a = U_a + lambda I - sum A A^T, FP64 Cholesky (packed lower L, with 1/L_jj in
+// the diagonal slots of pinv); b'_a = g_a - sum A t.  pc[28 a]: 21 L entries + 6 inverse diagonal.
+__global__ void k_pcg_precond(const double* U, const double* aat, int nfc, double lambda, double* pc, double* b,
+                              int32_t* ok) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nfc) return;
+    double P[21];
+    for (int k = 0; k < 21; ++k) P[k] = U[28LL * a + k] - aat[28LL * a + k];
+    for (int r = 0; r < 6; ++r) P[tri(r, r)] += lambda;
+    double rinv[6];
+    const bool good = chol6_packed(P, rinv);
     for (int k = 0; k < 21; ++k) pc[28LL * a + k] = P[k];
     for (int k = 0; k < 6; ++k) pc[28LL * a + 21 + k] = rinv[k];
     for (int k = 0; k < 6; ++k) b[6 * a + k] = U[28LL * a + 21 + k] - aat[28LL * a + 21 + k];
     if (!good) ok[0] = 0;
+}
+
+// The same block-Jacobi factor from the diagonal slots of the explicit S (lambda included).
+template <class Real>
+__global__ void k_pcg_precond_blocks(const Real* Sb, const int32_t* dslot, int nfc, double* pc, int32_t* ok) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nfc) return;
+    const Real* d = Sb + 36LL * dslot[a];
+    double P[21];
+    for (int r = 0; r < 6; ++r)
+        for (int q = 0; q <= r; ++q) P[tri(r, q)] = (double)d[6 * r + q];
+    double rinv[6];
+    const bool good = chol6_packed(P, rinv);
+    for (int k = 0; k < 21; ++k) pc[28LL * a + k] = P[k];
+    for (int k = 0; k < 6; ++k) pc[28LL * a + 21 + k] = rinv[k];
+    if (!good) ok[0] = 0;
+}
+
+// Camera-k coupling of the reduced system, per work item over the camera lists: sum A_e B_p
+// (6 x 2, entry r * 2 + j) -> part[12 * item]; S_ak = H_ck,a - the camera's sum.
+template <class Real>
+__global__ void k_pcg_xak_items(WinArgs<Real> A, const int4* items, int n_items, const int32_t* cam_list,
+                                const Real* pt_b, double* part) {
+    const CC c = grid_view();
+    for (int it = c.gw; it < n_items; it += c.CW) {
+        const int4 wi = items[it];
+        Real u[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) u[k] = Real(0);
+        for (int i = c.lane; i < wi.z; i += 32) {
+            const int e = cam_list[wi.y + i];
+            const int gp = A.edge_pt[e];
+            if (A.pt_free[gp] < 0) continue;
+            Real a[18], bp[12];
+            Rec<Real>::load18(A.edge_a + (long long)Rec<Real>::kEdge * e, a);
+            Rec<Real>::load12(pt_b + 12LL * gp, bp);
+#pragma unroll
+            for (int r = 0; r < 6; ++r)
+#pragma unroll
+                for (int j = 0; j < 2; ++j)
+                    u[2 * r + j] += a[3 * r] * bp[3 * j] + a[3 * r + 1] * bp[3 * j + 1] + a[3 * r + 2] * bp[3 * j + 2];
+        }
+#pragma unroll
+        for (int k = 0; k < 12; ++k)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) u[k] += __shfl_xor_sync(kFullG, u[k], o);
+        const Real uk = lane_value<12>(u, c.lane);
+        if (c.lane < 12) part[12LL * it + c.lane] = (double)uk;
+    }
 }
 
 // Structure-of-arrays copies of A_e for the PCG products (18 arrays of Real each): point-major in
@@ -759,6 +827,7 @@ struct PcgArgs {
     int max_it;
     double tol2;
     int32_t* iters;         // out: iterations run
+    unsigned long long* phase;  // optional: SM cycles of the five phases (block 0 after each sync), or null
 };
 
 // Sum of n per-block partials (stride `stride`) in a fixed order; every thread gets the result.
@@ -775,6 +844,50 @@ __device__ double grid_partials_sum(const double* part, int n, int stride) {
     for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r += red[i];
     __syncthreads();
     return r;
+}
+
+// Reductions of the explicit PCG whose FP64 adds run in warp 0 alone (the FP64 pipe is shared by
+// the SM and charged per warp instruction; the other warps only stage or read values).  Orders are
+// fixed: every block gets the same bits.
+// Block sum of N doubles per thread (blockDim.x <= 256); warp 0 writes out[N * blockIdx.x + k].
+template <int N>
+__device__ void block_sum_w0(const double (&v)[N], double* out) {
+    __shared__ double stage[N][256];
+#pragma unroll
+    for (int k = 0; k < N; ++k) stage[k][threadIdx.x] = v[k];
+    __syncthreads();
+    if (threadIdx.x < 32) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            double s = 0.0;
+            for (int i = threadIdx.x; i < (int)blockDim.x; i += 32) s += stage[k][i];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(kFullG, s, o);
+            if (threadIdx.x == 0) out[N * blockIdx.x + k] = s;
+        }
+    }
+    __syncthreads();
+}
+
+// The N sums of per-block partials laid out [block][N], returned to every thread.
+template <int N>
+__device__ void grid_sum_w0(const double* part, int n, double (&out)[N]) {
+    __shared__ double res[N];
+    if (threadIdx.x < 32) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            double s = 0.0;
+#pragma unroll 4
+            for (int i = threadIdx.x; i < n; i += 32) s += part[(long long)i * N + k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(kFullG, s, o);
+            if (threadIdx.x == 0) res[k] = s;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < N; ++k) out[k] = res[k];
+    __syncthreads();
 }
 
 // z = P_a^-1 r for camera a (6x6 Cholesky factors with inverse diagonal).
@@ -819,6 +932,13 @@ __global__ void __launch_bounds__(256) k_pcg_solve(PcgArgs<Real> P) {
     double* pq_part = P.part + 4LL * nb;    // phase 3: p.q
     double* rz_part = P.part + 5LL * nb;    // phase 4: r.z, r.r (2 per block)
     const double* pkc = P.kk + 3;
+    long long tmark = clock64();
+    auto mark = [&](int k) {  // phase timer: block 0's view, taken after the grid synchronization
+        if (!P.phase || blockIdx.x != 0 || threadIdx.x != 0) return;
+        const long long now = clock64();
+        P.phase[k] += (unsigned long long)(now - tmark);
+        tmark = now;
+    };
     // init: x = 0, r = b, z = M^-1 r, p = z
     double rz = 0.0, rr = 0.0;
     for (int a = tid; a < P.nfc; a += nth) {
@@ -918,6 +1038,7 @@ __global__ void __launch_bounds__(256) k_pcg_solve(PcgArgs<Real> P) {
             block_partials<2>(acc, pk_part);
         }
         grid.sync();
+        mark(0);
         // phase 2: per camera item sum A_s t2 (warp per item); Hck_a^T p_a partials
         for (int it = gw; it < P.n_items; it += nwarp) {
             const int4 wi = P.items[it];
@@ -950,6 +1071,7 @@ __global__ void __launch_bounds__(256) k_pcg_solve(PcgArgs<Real> P) {
             block_partials<2>(hk, hk_part);
         }
         grid.sync();
+        mark(1);
         // phase 3: q = S p per camera (and the k block), p.q partials
         {
             double pq = 0.0;
@@ -982,6 +1104,7 @@ __global__ void __launch_bounds__(256) k_pcg_solve(PcgArgs<Real> P) {
             block_partial<false>(pq, pq_part);
         }
         grid.sync();
+        mark(2);
         // phase 4: x += alpha p, r -= alpha q, z = M^-1 r, r.z and r.r partials
         {
             const double pq = grid_partials_sum(pq_part, nb, 1);
@@ -1014,6 +1137,7 @@ __global__ void __launch_bounds__(256) k_pcg_solve(PcgArgs<Real> P) {
             block_partials<2>(two, rz_part);
         }
         grid.sync();
+        mark(3);
         // phase 5: p = z + beta p
         {
             const double rzn = grid_partials_sum(rz_part, nb, 2);
@@ -1027,11 +1151,302 @@ __global__ void __launch_bounds__(256) k_pcg_solve(PcgArgs<Real> P) {
             rz = rzn;
         }
         grid.sync();
+        mark(4);
     }
     if (tid == 0) P.iters[0] = pit;
 }
 
 // t_p -= B_p^T dk before the point back-substitution (the distortion part of the step).
+// ---- PCG over the explicit reduced system --------------------------------------------------
+//
+// S in block rows of both triangles (36 Real per slot, row-major, lambda in the diagonal slots),
+// S_ak = H_ck - sum A B per camera and S_kk (2 x 2) when the shared distortion is free.  One CG
+// iteration is two grid-wide phases:
+//   1. warp per camera row a: p_b = z_b + beta p_b (old) for every column camera b, computed by
+//      each reader from z and the previous direction (the row's owner stores its own p_a in the
+//      other buffer), q_a = sum_b S_ab p_b + S_ak p_k; partials of p.q and S_ka p
+//   2. thread per camera: q_k, alpha = r.z / p.q, x += alpha p, r -= alpha q, z = M^-1 r;
+//      partials of r.z and r.r
+// so the direction update needs no grid synchronization of its own.  The block rows are a few
+// MB (one camera's row: its co-observing cameras), read from L2 by every iteration; the
+// per-observation records are read once per damping trial, when S is formed.  Sums run in the
+// same fixed order in every block and every run.
+
+template <class Real>
+struct PcgXArgs {
+    const Real* Sb;         // block rows, 36 per slot
+    const int32_t* rs_off;  // first slot of each camera row (nfc + 1)
+    const int32_t* rs_col;  // column camera of each slot
+    const double* Hck;      // H_ck per camera (12, entry r * 2 + j), when nk
+    const double* Xak;      // sum A B per camera (12), when nk
+    const double* pc;       // block-Jacobi factors (28 per camera)
+    const double* kk;       // [3..5]: factor of the k block's preconditioner
+    double skk[3];          // S_kk (00, 01, 11), lambda included
+    const double* b;        // right-hand side (6 nfc + nk)
+    double *x, *r, *z, *q;  // CG vectors
+    double* p[2];           // directions, alternating
+    Real* zr;               // z of the cameras in Real, 8 per camera (read by the products)
+    Real* pr[2];            // the directions of the cameras in Real, 8 per camera
+    double* part;           // per-block partials (5 per block)
+    int nfc, nk, max_it;
+    double tol2;
+    int32_t* iters;
+    unsigned long long* phase;  // optional: SM cycles per phase (block 0), or null
+};
+
+__device__ __forceinline__ void load36(const float* s, float (&v)[36]) {
+    const float4* s4 = reinterpret_cast<const float4*>(s);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        const float4 t = s4[k];
+        v[4 * k] = t.x;
+        v[4 * k + 1] = t.y;
+        v[4 * k + 2] = t.z;
+        v[4 * k + 3] = t.w;
+    }
+}
+
+__device__ __forceinline__ void load36(const double* s, double (&v)[36]) {
+    const double2* s2 = reinterpret_cast<const double2*>(s);
+#pragma unroll
+    for (int k = 0; k < 18; ++k) {
+        const double2 t = s2[k];
+        v[2 * k] = t.x;
+        v[2 * k + 1] = t.y;
+    }
+}
+
+// The first 6 of a camera's 8 Real entries (32- or 64-byte aligned).
+__device__ __forceinline__ void load6(const float* s, float (&v)[6]) {
+    const float4 a = *reinterpret_cast<const float4*>(s);
+    const float2 b = *reinterpret_cast<const float2*>(s + 4);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y;
+}
+
+__device__ __forceinline__ void load6(const double* s, double (&v)[6]) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double2 t = reinterpret_cast<const double2*>(s)[k];
+        v[2 * k] = t.x;
+        v[2 * k + 1] = t.y;
+    }
+}
+
+template <class Real>
+__global__ void __launch_bounds__(256) k_pcg_explicit(PcgXArgs<Real> P) {
+    cg::grid_group grid = cg::this_grid();
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    const int nb = gridDim.x;
+    const int lane = threadIdx.x & 31;
+    const int gw = tid >> 5, nwarp = nth >> 5;
+    const int kb = 6 * P.nfc;
+    double* mv_part = P.part;             // phase 1: p.q over the cameras, S_ka p (3 per block)
+    double* rz_part = P.part + 3LL * nb;  // phase 2: r.z, r.r (2 per block)
+    const double* pkc = P.kk + 3;
+    long long tmark = clock64();
+    auto mark = [&](int k) {  // phase timer: block 0's view
+        if (!P.phase || blockIdx.x != 0 || threadIdx.x != 0) return;
+        const long long now = clock64();
+        P.phase[k] += (unsigned long long)(now - tmark);
+        tmark = now;
+    };
+    // per-camera work (thread per camera) in chunks of 32 cameras spread over the blocks first:
+    // the FP64 pipe is per SM, and a few thousand cameras are a few warps' work.  Each camera's
+    // vectors are read into registers before anything is stored (the vectors may alias as far as
+    // the compiler knows, which would otherwise order every load after the previous store).
+    const int nchunk = (P.nfc + 31) >> 5, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+    // init: x = 0, r = b, z = M^-1 r, previous direction 0 (the first direction is z)
+    double rz = 0.0, rr = 0.0;
+    for (int c = blockIdx.x + nb * wib; c < nchunk; c += nb * nwb) {
+        const int a = 32 * c + lane;
+        if (a >= P.nfc) continue;
+        double rv[6], zv[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) rv[i] = P.b[6 * a + i];
+        precond_cam(P.pc, a, rv, zv);
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            P.x[6 * a + i] = 0.0;
+            P.p[0][6 * a + i] = 0.0;
+            P.r[6 * a + i] = rv[i];
+            P.z[6 * a + i] = zv[i];
+            P.zr[8 * a + i] = (Real)zv[i];
+            P.pr[0][8 * a + i] = Real(0);
+            rz += rv[i] * zv[i];
+            rr += rv[i] * rv[i];
+        }
+    }
+    if (P.nk && tid == 0) {
+        for (int i = 0; i < 2; ++i) {
+            P.x[kb + i] = 0.0;
+            P.p[0][kb + i] = 0.0;
+            P.r[kb + i] = P.b[kb + i];
+        }
+        precond_k(pkc, P.r + kb, P.z + kb);
+        for (int i = 0; i < 2; ++i) {
+            rz += P.r[kb + i] * P.z[kb + i];
+            rr += P.r[kb + i] * P.r[kb + i];
+        }
+    }
+    {
+        double two[2] = {rz, rr};
+        block_sum_w0<2>(two, rz_part);
+    }
+    grid.sync();
+    {
+        double two[2];
+        grid_sum_w0<2>(rz_part, nb, two);
+        rz = two[0];
+        rr = two[1];
+    }
+    const double bb = rr;
+    double beta = 0.0;
+    int pit = 0, cur = 0;
+    for (; pit < P.max_it; ++pit) {
+        if (pit % 4 == 0 && !(rr > P.tol2 * bb)) break;
+        const double* po = P.p[cur];
+        double* pn = P.p[cur ^ 1];
+        const Real* pro = P.pr[cur];
+        Real* prn = P.pr[cur ^ 1];
+        const Real betar = (Real)beta;
+        const double pk0 = P.nk ? P.z[kb] + beta * po[kb] : 0.0;
+        const double pk1 = P.nk ? P.z[kb + 1] + beta * po[kb + 1] : 0.0;
+        // phase 1: p = z + beta p, q = S p (warp per camera row)
+        {
+            double pq = 0.0, kq0 = 0.0, kq1 = 0.0;
+            for (int a = gw; a < P.nfc; a += nwarp) {
+                Real acc[6] = {Real(0), Real(0), Real(0), Real(0), Real(0), Real(0)};
+                const int s1 = P.rs_off[a + 1];
+                // two slots per lane per round (both slots' loads in flight together); the second
+                // is a copy of the first with a zero direction where the row has no more slots
+                for (int sl = P.rs_off[a] + lane; sl < s1; sl += 64) {
+                    const bool two = sl + 32 < s1;
+                    const int sl2 = two ? sl + 32 : sl;
+                    const int bc = P.rs_col[sl], bc2 = P.rs_col[sl2];
+                    Real sv[36], sv2[36];
+                    load36(P.Sb + 36LL * sl, sv);
+                    load36(P.Sb + 36LL * sl2, sv2);
+                    Real pb[6], zb[6], pb2[6], zb2[6];
+                    load6(P.zr + 8LL * bc, zb);
+                    load6(pro + 8LL * bc, pb);
+                    load6(P.zr + 8LL * bc2, zb2);
+                    load6(pro + 8LL * bc2, pb2);
+#pragma unroll
+                    for (int j = 0; j < 6; ++j) {
+                        pb[j] = zb[j] + betar * pb[j];
+                        pb2[j] = two ? zb2[j] + betar * pb2[j] : Real(0);
+                    }
+#pragma unroll
+                    for (int i = 0; i < 6; ++i)
+#pragma unroll
+                        for (int j = 0; j < 6; ++j) acc[i] += sv[6 * i + j] * pb[j];
+#pragma unroll
+                    for (int i = 0; i < 6; ++i)
+#pragma unroll
+                        for (int j = 0; j < 6; ++j) acc[i] += sv2[6 * i + j] * pb2[j];
+                }
+#pragma unroll
+                for (int i = 0; i < 6; ++i)
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) acc[i] += __shfl_xor_sync(kFullG, acc[i], o);
+                const Real qv = lane_value<6>(acc, lane);  // lanes 0..5: entry `lane` of the row
+                if (lane < 6) {
+                    const int i = 6 * a + lane;
+                    const double zi = P.z[i], poi = po[i];
+                    const Real zri = P.zr[8 * a + lane], pori = pro[8 * a + lane];
+                    double c0 = 0.0, c1 = 0.0;
+                    if (P.nk) {
+                        c0 = P.Hck[12LL * a + 2 * lane] - P.Xak[12LL * a + 2 * lane];
+                        c1 = P.Hck[12LL * a + 2 * lane + 1] - P.Xak[12LL * a + 2 * lane + 1];
+                    }
+                    const double pv = zi + beta * poi;
+                    const double qa = (double)qv + c0 * pk0 + c1 * pk1;
+                    kq0 += c0 * pv;
+                    kq1 += c1 * pv;
+                    pn[i] = pv;
+                    prn[8 * a + lane] = zri + betar * pori;
+                    P.q[i] = qa;
+                    pq += pv * qa;
+                }
+            }
+            if (P.nk && tid == 0) {
+                pn[kb] = pk0;
+                pn[kb + 1] = pk1;
+            }
+            mark(1);
+            double three[3] = {pq, kq0, kq1};
+            block_sum_w0<3>(three, mv_part);
+        }
+        grid.sync();
+        mark(2);
+        // phase 2: q_k, alpha; x += alpha p, r -= alpha q, z = M^-1 r; r.z and r.r partials
+        {
+            double sums[3];
+            grid_sum_w0<3>(mv_part, nb, sums);
+            double pq = sums[0];
+            double qk0 = 0.0, qk1 = 0.0;
+            if (P.nk) {
+                qk0 = P.skk[0] * pk0 + P.skk[1] * pk1 + sums[1];
+                qk1 = P.skk[1] * pk0 + P.skk[2] * pk1 + sums[2];
+                pq += pk0 * qk0 + pk1 * qk1;
+            }
+            const double alpha = pq != 0.0 ? rz / pq : 0.0;
+            double rzn = 0.0, rrn = 0.0;
+            for (int c = blockIdx.x + nb * wib; c < nchunk; c += nb * nwb) {
+                const int a = 32 * c + lane;
+                if (a >= P.nfc) continue;
+                double xv[6], rv[6], pv[6], qv[6], zv[6];
+#pragma unroll
+                for (int i = 0; i < 6; ++i) {
+                    xv[i] = P.x[6 * a + i];
+                    rv[i] = P.r[6 * a + i];
+                    pv[i] = pn[6 * a + i];
+                    qv[i] = P.q[6 * a + i];
+                }
+#pragma unroll
+                for (int i = 0; i < 6; ++i) {
+                    xv[i] += alpha * pv[i];
+                    rv[i] -= alpha * qv[i];
+                }
+                precond_cam(P.pc, a, rv, zv);
+#pragma unroll
+                for (int i = 0; i < 6; ++i) {
+                    P.x[6 * a + i] = xv[i];
+                    P.r[6 * a + i] = rv[i];
+                    P.z[6 * a + i] = zv[i];
+                    P.zr[8 * a + i] = (Real)zv[i];
+                    rzn += rv[i] * zv[i];
+                    rrn += rv[i] * rv[i];
+                }
+            }
+            if (P.nk && tid == 0) {
+                P.x[kb] += alpha * pk0;
+                P.x[kb + 1] += alpha * pk1;
+                P.r[kb] -= alpha * qk0;
+                P.r[kb + 1] -= alpha * qk1;
+                precond_k(pkc, P.r + kb, P.z + kb);
+                for (int i = 0; i < 2; ++i) {
+                    rzn += P.r[kb + i] * P.z[kb + i];
+                    rrn += P.r[kb + i] * P.r[kb + i];
+                }
+            }
+            mark(3);
+            double two[2] = {rzn, rrn};
+            block_sum_w0<2>(two, rz_part);
+        }
+        grid.sync();
+        mark(4);
+        double two[2];
+        grid_sum_w0<2>(rz_part, nb, two);
+        rr = two[1];
+        beta = rz != 0.0 ? two[0] / rz : 0.0;
+        rz = two[0];
+        cur ^= 1;
+        mark(0);
+    }
+    if (tid == 0) P.iters[0] = pit;
+}
+
 template <class Real>
 __global__ void k_fold_intr(WinArgs<Real> A, WinDesc D, const Real* pt_b, double dk1, double dk2) {
     const CC c = grid_view();
@@ -1048,20 +1463,70 @@ __global__ void k_fold_intr(WinArgs<Real> A, WinDesc D, const Real* pt_b, double
 
 // ---- host side ---------------------------------------------------------------------------
 
+// Pair list storage: default-initialized (no zero fill of arrays of tens of millions of entries).
+template <class T>
+struct RawVec {
+    std::unique_ptr<T[]> d;
+    size_t n = 0;
+    void resize(size_t k) {
+        d.reset(new T[std::max<size_t>(k, 1)]);
+        n = k;
+    }
+    T* data() { return d.get(); }
+    const T* data() const { return d.get(); }
+    size_t size() const { return n; }
+    T& operator[](size_t i) { return d[i]; }
+};
+
+// Form of the reduced system a grid solve needs.
+enum GridForm {
+    kFormNone = 0,      // implicit PCG: S only as products with the per-edge records
+    kFormCholesky = 1,  // lower blocks with pair lists, dense S, Cholesky work lists
+    kFormBlocks = 2,    // lower blocks with pair lists, block rows of both triangles (explicit PCG)
+};
+
 struct GridHost {
     std::vector<int32_t> cam_list, item_off, fcam, boff, tfirst;
     std::vector<int4> items;
-    std::vector<int2> blocks, pairs;
+    std::vector<int2> blocks;
+    RawVec<int2> pairs;
     // Cholesky work per tile column K: panel tile rows and trailing tiles (I, J), K < J <= I
     std::vector<int32_t> pan_off, pan_row, tr_off;
     std::vector<int2> tr_ij;
     int max_col_work = 1;  // largest per-column count of panel tiles or trailing quarter items
+    // block rows of both triangles: row a's slots [rs_off[a], rs_off[a+1]) with their column
+    // cameras rs_col in increasing order, its diagonal slot rs_dslot[a]; per lower block its slot
+    // in its own row and the slot of the transposed block (-1 on the diagonal)
+    std::vector<int32_t> rs_off, rs_col, rs_dslot;
+    std::vector<int2> bslot;
 };
 
-// schur: also the reduced system's block structure, pair lists and Cholesky work lists (the dense
-// Cholesky path; the PCG path forms S only implicitly and needs none of them).
-void build_grid_host(const HostWindow& h, GridHost& g, bool schur) {
+// Sum over points of k (k + 1) / 2 (k: free-camera observations of a free point): the pair count
+// of the lower blocks, from the point offsets alone.
+long long schur_pair_count(const HostWindow& h) {
+    long long n = 0;
+    for (int i = 0; i < h.npt; ++i) {
+        if (h.pt_free[i] < 0) continue;
+        long long k = 0;
+        for (int e = h.pt_eoff[i]; e < h.pt_eoff[i + 1]; ++e) k += h.cam_free[h.edge_cam[e]] >= 0;
+        n += k * (k + 1) / 2;
+    }
+    return n;
+}
+
+// The reduced system's structure for the given form.  Rows of the lower block structure are
+// independent (row a's blocks and pairs come from camera a's edges alone), so they are built by
+// row ranges on the host workers; every row is filled in the same order as a single pass would.
+void build_grid_host(const HostWindow& h, GridHost& g, int form, HostPool* pool) {
     const int nfc = h.nfc;
+    const char* verbose = getenv("NAVBA_VERBOSE");
+    auto t0 = std::chrono::steady_clock::now();
+    auto lap = [&](const char* what) {
+        if (!verbose || verbose[0] != '1') return;
+        const auto t1 = std::chrono::steady_clock::now();
+        fprintf(stderr, "[navba grid] host %-14s %.2f ms\n", what, std::chrono::duration<double, std::milli>(t1 - t0).count());
+        t0 = t1;
+    };
     g.fcam.assign(std::max(1, nfc), 0);
     for (int c = 0; c < h.ncam; ++c)
         if (h.cam_free[c] >= 0) g.fcam[h.cam_free[c]] = c;
@@ -1086,93 +1551,148 @@ void build_grid_host(const HostWindow& h, GridHost& g, bool schur) {
         g.item_off[a + 1] = (int32_t)g.items.size();
     }
     if (g.items.empty()) g.items.push_back(make_int4(0, 0, 0, 0));
-    if (!schur) {
-        g.blocks.assign(1, make_int2(0, 0));
-        g.boff.assign(2, 0);
-        g.pairs.assign(1, make_int2(0, 0));
-        g.tfirst.assign(1, 0);
-        g.pan_off.assign(2, 0);
-        g.tr_off.assign(2, 0);
-        g.pan_row.assign(1, 0);
-        g.tr_ij.assign(1, make_int2(0, 0));
-        g.max_col_work = 1;
-        return;
-    }
-    // nonzero lower blocks and their pair lists (per block: pairs in camera-major, point order)
-    // (up to 4096 free cameras through a dense nfc x nfc index, beyond that by sorted rows)
-    const bool dense = (size_t)nfc * nfc <= ((size_t)1 << 24);
-    std::vector<int32_t> bidx;  // dense: block index of (a, b), b <= a, or -1
-    std::vector<std::vector<int32_t>> rowcols(nfc);
-    auto for_each_block = [&](auto fn) {  // fn(a, b) for every co-observing pair, b <= a
-        for (int i = 0; i < h.npt; ++i) {
-            if (h.pt_free[i] < 0) continue;
-            for (int e = h.pt_eoff[i]; e < h.pt_eoff[i + 1]; ++e) {
-                const int a = h.cam_free[h.edge_cam[e]];
-                if (a < 0) continue;
+    g.blocks.assign(1, make_int2(0, 0));
+    g.boff.assign(2, 0);
+    g.pairs.resize(1);
+    g.pairs[0] = make_int2(0, 0);
+    g.tfirst.assign(1, 0);
+    g.pan_off.assign(2, 0);
+    g.tr_off.assign(2, 0);
+    g.pan_row.assign(1, 0);
+    g.tr_ij.assign(1, make_int2(0, 0));
+    g.max_col_work = 1;
+    g.rs_off.assign(nfc + 1, 0);
+    g.rs_col.assign(1, 0);
+    g.rs_dslot.assign(std::max(1, nfc), 0);
+    g.bslot.assign(1, make_int2(0, -1));
+    lap("camera lists");
+    if (form == kFormNone) return;
+    // row ranges on the workers (more ranges than workers: rows differ in cost)
+    const int hw = std::max(1, (int)std::thread::hardware_concurrency());
+    const int ntask = std::max(1, std::min(nfc, pool ? 4 * hw : 1));
+    auto rows_of = [&](int t, int& a0, int& a1) {
+        a0 = (int)((long long)nfc * t / ntask);
+        a1 = (int)((long long)nfc * (t + 1) / ntask);
+    };
+    auto run = [&](const std::function<void(int)>& fn) {
+        if (pool && ntask > 1)
+            pool->run(ntask, fn);
+        else
+            for (int t = 0; t < ntask; ++t) fn(t);
+    };
+    // pass 1, per row a: the columns b <= a of its nonzero blocks (sorted; a itself always) and
+    // each block's pair count
+    std::vector<std::vector<int32_t>> rowcols(nfc), rowcnt(nfc);
+    run([&](int t) {
+        int a0, a1;
+        rows_of(t, a0, a1);
+        std::vector<int32_t> loc(nfc, -1), cols, cn, perm;
+        for (int a = a0; a < a1; ++a) {
+            cols.assign(1, a);
+            cn.assign(1, 0);
+            loc[a] = 0;
+            for (int s = loff[a]; s < loff[a + 1]; ++s) {
+                const int i = h.edge_pt[g.cam_list[s]];
+                if (h.pt_free[i] < 0) continue;
                 for (int f = h.pt_eoff[i]; f < h.pt_eoff[i + 1]; ++f) {
                     const int b = h.cam_free[h.edge_cam[f]];
-                    if (b >= 0 && b <= a) fn(a, b);
+                    if (b < 0 || b > a) continue;
+                    int k = loc[b];
+                    if (k < 0) {
+                        k = loc[b] = (int)cols.size();
+                        cols.push_back(b);
+                        cn.push_back(0);
+                    }
+                    cn[k]++;
                 }
             }
+            perm.resize(cols.size());
+            for (size_t k = 0; k < perm.size(); ++k) perm[k] = (int32_t)k;
+            std::sort(perm.begin(), perm.end(), [&](int32_t x, int32_t y) { return cols[x] < cols[y]; });
+            rowcols[a].resize(cols.size());
+            rowcnt[a].resize(cols.size());
+            for (size_t k = 0; k < perm.size(); ++k) {
+                rowcols[a][k] = cols[perm[k]];
+                rowcnt[a][k] = cn[perm[k]];
+            }
+            for (int b : cols) loc[b] = -1;
         }
-    };
-    if (dense) {
-        bidx.assign((size_t)nfc * nfc, -1);
-        for_each_block([&](int a, int b) { bidx[(size_t)a * nfc + b] = 0; });
-        for (int a = 0; a < nfc; ++a) {
-            bidx[(size_t)a * nfc + a] = 0;
-            for (int b = 0; b <= a; ++b)
-                if (bidx[(size_t)a * nfc + b] == 0) rowcols[a].push_back(b);
-        }
-    } else {
-        for_each_block([&](int a, int b) { rowcols[a].push_back(b); });
-        for (int a = 0; a < nfc; ++a) {
-            rowcols[a].push_back(a);
-            std::sort(rowcols[a].begin(), rowcols[a].end());
-            rowcols[a].erase(std::unique(rowcols[a].begin(), rowcols[a].end()), rowcols[a].end());
-        }
-    }
-    // block index of (a, b)
+    });
     std::vector<int32_t> row_start(nfc + 1, 0);
     for (int a = 0; a < nfc; ++a) row_start[a + 1] = row_start[a] + (int32_t)rowcols[a].size();
     const int nblk = row_start[nfc];
     g.blocks.resize(std::max(1, nblk));
+    g.boff.assign(nblk + 1, 0);
     for (int a = 0; a < nfc; ++a)
         for (size_t k = 0; k < rowcols[a].size(); ++k) {
-            g.blocks[row_start[a] + k] = make_int2(a, rowcols[a][k]);
-            if (dense) bidx[(size_t)a * nfc + rowcols[a][k]] = row_start[a] + (int32_t)k;
-        }
-    auto block_of = [&](int a, int b) {
-        if (dense) return bidx[(size_t)a * nfc + b];
-        const auto& rc = rowcols[a];
-        return row_start[a] + (int32_t)(std::lower_bound(rc.begin(), rc.end(), b) - rc.begin());
-    };
-    std::vector<int32_t> pcnt(nblk + 1, 0);
-    for (int a = 0; a < nfc; ++a)
-        for (int s = loff[a]; s < loff[a + 1]; ++s) {
-            const int e = g.cam_list[s];
-            const int i = h.edge_pt[e];
-            if (h.pt_free[i] < 0) continue;
-            for (int f = h.pt_eoff[i]; f < h.pt_eoff[i + 1]; ++f) {
-                const int b = h.cam_free[h.edge_cam[f]];
-                if (b >= 0 && b <= a) pcnt[block_of(a, b) + 1]++;
-            }
-        }
-    g.boff.assign(nblk + 1, 0);
-    for (int k = 0; k < nblk; ++k) g.boff[k + 1] = g.boff[k] + pcnt[k + 1];
-    g.pairs.assign(std::max(1, g.boff[nblk]), make_int2(0, 0));
-    std::vector<int32_t> pf(g.boff.begin(), g.boff.end() - 1);
-    for (int a = 0; a < nfc; ++a)
-        for (int s = loff[a]; s < loff[a + 1]; ++s) {
-            const int e = g.cam_list[s];
-            const int i = h.edge_pt[e];
-            if (h.pt_free[i] < 0) continue;
-            for (int f = h.pt_eoff[i]; f < h.pt_eoff[i + 1]; ++f) {
-                const int b = h.cam_free[h.edge_cam[f]];
-                if (b >= 0 && b <= a) g.pairs[pf[block_of(a, b)]++] = make_int2(e, f);
-            }
+            const int blk = row_start[a] + (int)k;
+            g.blocks[blk] = make_int2(a, rowcols[a][k]);
+            g.boff[blk + 1] = g.boff[blk] + rowcnt[a][k];
         }
     if (g.boff.size() == 1) g.boff.push_back(0);
+    lap("blocks");
+    // pass 2, per row: the pairs of each block in camera-list (point) order
+    g.pairs.resize(std::max<size_t>(1, (size_t)g.boff[nblk]));
+    g.pairs[0] = make_int2(0, 0);
+    run([&](int t) {
+        int a0, a1;
+        rows_of(t, a0, a1);
+        std::vector<int32_t> loc(nfc, -1), cur;
+        for (int a = a0; a < a1; ++a) {
+            const auto& rc = rowcols[a];
+            cur.resize(rc.size());
+            for (size_t k = 0; k < rc.size(); ++k) {
+                loc[rc[k]] = (int32_t)k;
+                cur[k] = g.boff[row_start[a] + k];
+            }
+            for (int s = loff[a]; s < loff[a + 1]; ++s) {
+                const int e = g.cam_list[s];
+                const int i = h.edge_pt[e];
+                if (h.pt_free[i] < 0) continue;
+                for (int f = h.pt_eoff[i]; f < h.pt_eoff[i + 1]; ++f) {
+                    const int b = h.cam_free[h.edge_cam[f]];
+                    if (b >= 0 && b <= a) g.pairs[cur[loc[b]]++] = make_int2(e, f);
+                }
+            }
+            for (int b : rc) loc[b] = -1;
+        }
+    });
+    lap("pairs");
+    if (form == kFormBlocks) {
+        // row a: its lower columns (ending with a), then the columns c > a whose row holds a
+        std::vector<int32_t> upc(nfc, 0);
+        for (int a = 0; a < nfc; ++a)
+            for (int b : rowcols[a])
+                if (b < a) upc[b]++;
+        for (int a = 0; a < nfc; ++a) g.rs_off[a + 1] = g.rs_off[a] + (int32_t)rowcols[a].size() + upc[a];
+        g.rs_col.assign(std::max(1, g.rs_off[nfc]), 0);
+        g.bslot.resize(std::max(1, nblk));
+        std::vector<int32_t> ucur(nfc);
+        for (int a = 0; a < nfc; ++a) {
+            const int nl = (int)rowcols[a].size();
+            ucur[a] = g.rs_off[a] + nl;
+            g.rs_dslot[a] = g.rs_off[a] + nl - 1;
+            for (int k = 0; k < nl; ++k) g.rs_col[g.rs_off[a] + k] = rowcols[a][k];
+        }
+        for (int a = 0; a < nfc; ++a)  // increasing a: the upper columns of each row come sorted
+            for (size_t k = 0; k < rowcols[a].size(); ++k) {
+                const int b = rowcols[a][k];
+                int up = -1;
+                if (b < a) {
+                    up = ucur[b]++;
+                    g.rs_col[up] = a;
+                }
+                g.bslot[row_start[a] + k] = make_int2(g.rs_off[a] + (int)k, up);
+            }
+        lap("block rows");
+        if (verbose && verbose[0] == '1') {
+            int longest = 0;
+            for (int a = 0; a < nfc; ++a) longest = std::max(longest, g.rs_off[a + 1] - g.rs_off[a]);
+            fprintf(stderr, "[navba grid] explicit S: %d cameras, %d lower blocks, %d slots (longest row %d), %zu pairs\n",
+                    nfc, nblk, g.rs_off[nfc], longest, g.pairs.size());
+        }
+        return;
+    }
     // envelope at tile level: first nonzero tile column of each tile row
     const int m = 6 * nfc;
     const int nt = (m + kTile - 1) / kTile;
@@ -1229,17 +1749,36 @@ cudaError_t up(T* d, const std::vector<T>& h, cudaStream_t s) {
     return cudaMemcpyAsync(d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, s);
 }
 
+template <class T>
+cudaError_t up(T* d, const RawVec<T>& h, cudaStream_t s) {
+    if (!h.size()) return cudaSuccess;
+    return cudaMemcpyAsync(d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, s);
+}
+
 template <class Real>
 cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Intr& intr, cudaStream_t st,
-                             int cluster, GridResult& out, double debug_lambda, std::vector<double>* debug_S,
+                             HostPool* pool, GridResult& out, double debug_lambda, std::vector<double>* debug_S,
                              GridVjp* vjp) {
     const auto tg0 = std::chrono::steady_clock::now();
     auto ms_from = [](std::chrono::steady_clock::time_point a) {
         return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
     };
     const bool pcg = lm.solver == NAV_BA_SOLVER_PCG && !debug_S;
+    // PCG over the explicit block-sparse S unless its pair lists would be long against the
+    // observations (points seen by very many cameras): then the products go through the
+    // per-observation records (implicit S).  NAVBA_PCG_FORM=explicit|implicit fixes the form.
+    bool pcg_x = false;
+    if (pcg && !vjp) {
+        const char* f = getenv("NAVBA_PCG_FORM");
+        if (f && !strcmp(f, "implicit"))
+            pcg_x = false;
+        else if (f && !strcmp(f, "explicit"))
+            pcg_x = true;
+        else
+            pcg_x = schur_pair_count(h) <= 24LL * std::max(1, h.ne);
+    }
     GridHost g;
-    build_grid_host(h, g, !pcg || vjp != nullptr);
+    build_grid_host(h, g, (!pcg || vjp != nullptr) ? kFormCholesky : (pcg_x ? kFormBlocks : kFormNone), pool);
     const double t_host = ms_from(tg0);
     const int nc = h.ncam, np = h.npt, ne = h.ne, nfc = h.nfc;
     const int m = 6 * nfc;
@@ -1304,11 +1843,21 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     Real* d_pb = nk ? dv.alloc<Real>(12LL * np) : nullptr;
     double* d_hpart = nk ? dv.alloc<double>(12LL * n_items) : nullptr;
     double* d_Hck = dv.alloc<double>(12LL * std::max(1, nfc));
-    Real* d_t2 = pcg ? dv.alloc<Real>(4LL * np) : nullptr;
-    double* d_aat = pcg ? dv.alloc<double>(28LL * std::max(1, nfc)) : nullptr;
+    const bool pcg_i = pcg && !pcg_x;  // implicit S
+    Real* d_t2 = pcg_i ? dv.alloc<Real>(4LL * np) : nullptr;
+    double* d_aat = pcg_i ? dv.alloc<double>(28LL * std::max(1, nfc)) : nullptr;
     double* d_pc = pcg ? dv.alloc<double>(28LL * std::max(1, nfc)) : nullptr;
-    double* d_camp = pcg ? dv.alloc<double>(8LL * n_items) : nullptr;
-    double* d_vec = pcg ? dv.alloc<double>(5LL * std::max(1, mt) + 8) : nullptr;
+    double* d_camp = pcg_i ? dv.alloc<double>(8LL * n_items) : nullptr;
+    double* d_vec = pcg ? dv.alloc<double>(6LL * std::max(1, mt) + 8) : nullptr;
+    // explicit S: block rows, slots of the lower blocks, camera-k coupling
+    const int nslot = pcg_x ? g.rs_off[nfc] : 0;
+    Real* d_Sb = pcg_x ? dv.alloc<Real>(36LL * std::max(1, nslot)) : nullptr;
+    int32_t* d_rs_off = pcg_x ? dv.alloc<int32_t>(g.rs_off.size()) : nullptr;
+    int32_t* d_rs_col = pcg_x ? dv.alloc<int32_t>(g.rs_col.size()) : nullptr;
+    int32_t* d_rs_dslot = pcg_x ? dv.alloc<int32_t>(g.rs_dslot.size()) : nullptr;
+    int2* d_bslot = pcg_x ? dv.alloc<int2>(g.bslot.size()) : nullptr;
+    double* d_xak = (pcg_x && nk) ? dv.alloc<double>(12LL * std::max(1, nfc)) : nullptr;
+    Real* d_zpr = pcg_x ? dv.alloc<Real>(24LL * std::max(1, nfc)) : nullptr;  // z, p, p in Real (8 per camera)
     double* d_kvals = dv.alloc<double>(8);  // [0..2] H_kk + lambda-free, [3..5] pk (2x2 Cholesky)
     // tape of the accepted steps (state before each step) and the backward's vectors
     const int tape_cap = vjp ? (vjp->replay ? (int)vjp->lambdas.size() : lm.iterations) : 0;
@@ -1331,22 +1880,31 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     double* d_ptbar = (bwd && vjp->point_bar) ? dv.alloc<double>(3LL * np) : nullptr;
     // PCG: structure-of-arrays copies of A (point-major, camera-major) and the camera list's points
     const int ncl = (int)g.cam_list.size();
-    Real* d_apm = pcg ? dv.alloc<Real>(18LL * ne) : nullptr;
-    Real* d_acm = pcg ? dv.alloc<Real>(18LL * ncl) : nullptr;
-    int32_t* d_cmpt = pcg ? dv.alloc<int32_t>(ncl) : nullptr;
-    float* d_pf = (pcg && sizeof(Real) == 4) ? dv.alloc<float>(6LL * nfc1) : nullptr;
+    Real* d_apm = pcg_i ? dv.alloc<Real>(18LL * ne) : nullptr;
+    Real* d_acm = pcg_i ? dv.alloc<Real>(18LL * ncl) : nullptr;
+    int32_t* d_cmpt = pcg_i ? dv.alloc<int32_t>(ncl) : nullptr;
+    float* d_pf = (pcg_i && sizeof(Real) == 4) ? dv.alloc<float>(6LL * nfc1) : nullptr;
     // cooperative PCG grid: every block resident (the occupancy bound of the kernel)
     int pcg_grid = 1;
     if (pcg) {
         int dev = 0, nsm = 0, bps = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_pcg_solve<Real>, 256, 0);
-        pcg_grid = std::max(1, nsm * std::max(1, std::min(bps, 4)));
+        if (pcg_x) {
+            // enough warps for one camera row each, within what is resident
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_pcg_explicit<Real>, 256, 0);
+            pcg_grid = std::max(1, std::min(nsm * std::max(1, std::min(bps, 4)), (nfc + 7) / 8));
+        } else {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_pcg_solve<Real>, 256, 0);
+            pcg_grid = std::max(1, nsm * std::max(1, std::min(bps, 4)));
+        }
     }
     double* d_ppart = pcg ? dv.alloc<double>(7LL * pcg_grid) : nullptr;
     int32_t* d_pit = pcg ? dv.alloc<int32_t>(1) : nullptr;
+    const char* ptv = getenv("NAVBA_PHASE_TIMING");
+    unsigned long long* d_pcg_phase = pcg && ptv && ptv[0] == '1' ? dv.alloc<unsigned long long>(5) : nullptr;
     if (dv.err != cudaSuccess) return dv.err;
+    if (d_pcg_phase) cudaMemsetAsync(d_pcg_phase, 0, 5 * sizeof(unsigned long long), st);
     std::vector<int32_t> edge_fc(ne);
     for (int e = 0; e < ne; ++e) edge_fc[e] = h.cam_free[h.edge_cam[e]];
     cudaError_t e = cudaSuccess;
@@ -1375,8 +1933,14 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     chk(up(d_pan_row, g.pan_row, st));
     chk(up(d_tr_off, g.tr_off, st));
     chk(up(d_tr_ij, g.tr_ij, st));
+    if (pcg_x) {
+        chk(up(d_rs_off, g.rs_off, st));
+        chk(up(d_rs_col, g.rs_col, st));
+        chk(up(d_rs_dslot, g.rs_dslot, st));
+        chk(up(d_bslot, g.bslot, st));
+    }
     std::vector<int32_t> cm_pt;
-    if (pcg) {
+    if (pcg_i) {
         cm_pt.resize(ncl);
         for (int sl = 0; sl < ncl; ++sl) {
             const int pt = h.edge_pt[g.cam_list[sl]];
@@ -1441,15 +2005,29 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         std::chrono::steady_clock::time_point t0;
         double host, setup;
         double (*ms)(std::chrono::steady_clock::time_point);
+        unsigned long long* phase;
+        cudaStream_t st;
+        int explicit_s;
         ~LoopTimer() {
             const char* v = getenv("NAVBA_VERBOSE");
             if (v && v[0] == '1')
                 fprintf(stderr, "[navba grid] host structure %.2f ms, allocation + upload %.2f ms, LM loop %.2f ms\n", host,
                         setup - host, ms(t0));
+            unsigned long long cyc[5] = {0, 0, 0, 0, 0};
+            if (phase && cudaMemcpyAsync(cyc, phase, sizeof(cyc), cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+                cudaStreamSynchronize(st) == cudaSuccess) {
+                static const char* names[2][5] = {{"point t2", "camera items", "S p", "x/r update", "p update"},
+                                                  {"beta sums", "S p (own)", "S p (sync)", "x/r (own)", "x/r (sync)"}};
+                double tot = 0;
+                for (int k = 0; k < 5; ++k) tot += (double)cyc[k];
+                for (int k = 0; k < 5; ++k)
+                    fprintf(stderr, "[navba grid] pcg phase %-13s %14llu cycles %5.1f%%\n", names[explicit_s][k], cyc[k],
+                            tot > 0 ? 100.0 * cyc[k] / tot : 0.0);
+            }
         }
     } loop_timer{std::chrono::steady_clock::now(), t_host, t_setup, +[](std::chrono::steady_clock::time_point a) {
                      return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
-                 }};
+                 }, d_pcg_phase, st, pcg_x ? 1 : 0};
     int cur = 0;
     // costs (initial, every trial) are evaluated in FP64 in both forms: they drive the gain ratio
     double chi = cost_of(0, true);
@@ -1480,10 +2058,9 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         chk(cudaMemsetAsync(d_S, 0, sizeof(double) * (size_t)m * m, st));
         const int nb = (int)g.blocks.size();
         k_schur_blocks<Real><<<std::max(1, std::min(nsm_blocks, (nb * 32 + TB - 1) / TB)), TB, 0, st>>>(
-            A, d_blocks, d_boff, (int)(g.boff.size() - 1), d_pairs, d_U, lam, d_S, m, d_bs);
+            A, d_blocks, d_boff, (int)(g.boff.size() - 1), d_pairs, d_U, lam, d_S, m, d_bs, (Real*)nullptr, nullptr);
         chk(cudaGetLastError());
     };
-    (void)cluster;
     // Cholesky of S in place (cooperative, whole GPU); false if S is not positive definite
     int chol_grid = 1;
     {
@@ -1632,17 +2209,26 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             bool ok = npd == 0.0;
             double dk[2] = {0.0, 0.0};
             if (pcg && mt > 0) {
-                k_pcg_pack<Real><<<nsm_blocks, TB, 0, st>>>(A, ne, d_list, ncl, d_apm, d_acm);
+                if (pcg_i) k_pcg_pack<Real><<<nsm_blocks, TB, 0, st>>>(A, ne, d_list, ncl, d_apm, d_acm);
                 // right-hand side and block-Jacobi preconditioner of the reduced system [cameras; k]
                 const int32_t one = 1;
                 chk(cudaMemcpyAsync(d_ok, &one, sizeof(int32_t), cudaMemcpyHostToDevice, st));
-                if (nfc > 0) {
+                if (nfc > 0 && pcg_x) {
+                    // S_ab (block rows, both triangles) and b' from the pair lists, then the factors
+                    const int nb = (int)g.blocks.size();
+                    k_schur_blocks<Real><<<std::max(1, std::min(nsm_blocks, (nb * 32 + TB - 1) / TB)), TB, 0, st>>>(
+                        A, d_blocks, d_boff, (int)(g.boff.size() - 1), d_pairs, d_U, lam_use, nullptr, 0, d_bs, d_Sb,
+                        d_bslot);
+                    k_pcg_precond_blocks<Real><<<(nfc + TB - 1) / TB, TB, 0, st>>>(d_Sb, d_rs_dslot, nfc, d_pc, d_ok);
+                    chk(cudaGetLastError());
+                } else if (nfc > 0) {
                     k_pcg_diag_items<Real><<<iblocks, TB, 0, st>>>(A, d_items, n_items, d_list, d_upart);
                     k_reduce_items<<<(nfc * 27 + TB - 1) / TB, TB, 0, st>>>(d_upart, 28, 27, d_item_off, nfc, d_aat, 28);
                     k_pcg_precond<<<(nfc + TB - 1) / TB, TB, 0, st>>>(d_U, d_aat, nfc, lam_use, d_pc, d_bs, d_ok);
                     chk(cudaGetLastError());
                 }
                 double pkh[3] = {1.0, 0.0, 1.0};
+                double skk[3] = {0.0, 0.0, 0.0};
                 if (nk) {
                     k_schur_intr_points<Real><<<pblocks, TB, 0, st>>>(A, D, d_kp, d_pb, d_part);
                     double v5[5];
@@ -1655,6 +2241,12 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                     const double l11 = d11 > 0 ? std::sqrt(d11) : 1.0;
                     if (!(p00 > 0) || !(d11 > 0)) ok = false;
                     pkh[0] = l00; pkh[1] = l10; pkh[2] = l11;
+                    skk[0] = p00; skk[1] = p01; skk[2] = p11;
+                    if (pcg_x && nfc > 0) {
+                        k_pcg_xak_items<Real><<<iblocks, TB, 0, st>>>(A, d_items, n_items, d_list, d_pb, d_hpart);
+                        k_reduce_items<<<(nfc * 12 + TB - 1) / TB, TB, 0, st>>>(d_hpart, 12, 12, d_item_off, nfc, d_xak, 12);
+                        chk(cudaGetLastError());
+                    }
                     const double bk[2] = {gk[0] - v5[3], gk[1] - v5[4]};
                     const double kv[6] = {Kk[0], Kk[1], Kk[2], pkh[0], pkh[1], pkh[2]};
                     chk(cudaMemcpyAsync(d_kvals, kv, sizeof(kv), cudaMemcpyHostToDevice, st));
@@ -1699,8 +2291,41 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                 PA.max_it = lm.pcg_max_iterations;
                 PA.tol2 = lm.pcg_tolerance * lm.pcg_tolerance;
                 PA.iters = d_pit;
-                void* kargs[] = {&PA};
-                chk(cudaLaunchCooperativeKernel((const void*)k_pcg_solve<Real>, dim3(pcg_grid), dim3(256), kargs, 0, st));
+                PA.phase = d_pcg_phase;
+                if (pcg_x) {
+                    PcgXArgs<Real> XA;
+                    XA.Sb = d_Sb;
+                    XA.rs_off = d_rs_off;
+                    XA.rs_col = d_rs_col;
+                    XA.Hck = d_Hck;
+                    XA.Xak = d_xak;
+                    XA.pc = d_pc;
+                    XA.kk = d_kvals;
+                    for (int i = 0; i < 3; ++i) XA.skk[i] = skk[i];
+                    XA.b = d_bs;
+                    XA.x = v.x;
+                    XA.r = v.r;
+                    XA.z = v.z;
+                    XA.q = v.q;
+                    XA.p[0] = v.p;
+                    XA.p[1] = d_vec + 5LL * mt;
+                    XA.zr = d_zpr;
+                    XA.pr[0] = d_zpr + 8LL * std::max(1, nfc);
+                    XA.pr[1] = d_zpr + 16LL * std::max(1, nfc);
+                    XA.part = d_ppart;
+                    XA.nfc = nfc;
+                    XA.nk = nk;
+                    XA.max_it = lm.pcg_max_iterations;
+                    XA.tol2 = PA.tol2;
+                    XA.iters = d_pit;
+                    XA.phase = d_pcg_phase;
+                    void* kargs[] = {&XA};
+                    chk(cudaLaunchCooperativeKernel((const void*)k_pcg_explicit<Real>, dim3(pcg_grid), dim3(256), kargs, 0,
+                                                    st));
+                } else {
+                    void* kargs[] = {&PA};
+                    chk(cudaLaunchCooperativeKernel((const void*)k_pcg_solve<Real>, dim3(pcg_grid), dim3(256), kargs, 0, st));
+                }
                 int32_t pit = 0;
                 chk(cudaMemcpyAsync(&pit, d_pit, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
                 chk(cudaMemcpyAsync(d_bs, v.x, sizeof(double) * mt, cudaMemcpyDeviceToDevice, st));
@@ -1893,10 +2518,10 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
 }  // namespace
 
 cudaError_t grid_solve(const HostWindow& h, const LmOptions& lm, const Intr& intr, int precision, cudaStream_t stream,
-                       int cluster, GridResult& out, double debug_lambda, std::vector<double>* debug_S, GridVjp* vjp) {
+                       HostPool* pool, GridResult& out, double debug_lambda, std::vector<double>* debug_S, GridVjp* vjp) {
     if (precision == NAV_BA_MIXED)
-        return grid_solve_typed<float>(h, lm, intr, stream, cluster, out, debug_lambda, debug_S, vjp && !vjp->backward ? vjp : nullptr);
-    return grid_solve_typed<double>(h, lm, intr, stream, cluster, out, debug_lambda, debug_S, vjp);
+        return grid_solve_typed<float>(h, lm, intr, stream, pool, out, debug_lambda, debug_S, vjp && !vjp->backward ? vjp : nullptr);
+    return grid_solve_typed<double>(h, lm, intr, stream, pool, out, debug_lambda, debug_S, vjp);
 }
 
 }  // namespace navba

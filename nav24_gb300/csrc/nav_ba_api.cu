@@ -29,7 +29,6 @@ struct nav_ba_ctx {
     bool tuned[2] = {false, false};
     WindowBatch solve_dev;        // device buffers of nav_ba_solve / _batched, reused across calls
     std::vector<HostWindow> solve_host;  // their host-side windows, reused across calls
-    int grid_cluster = 8;         // CTAs of the grid engine's Cholesky cluster
     HostStaging stg;              // pinned staging reused across calls
     // pipelined batched solves: the batch's parts, each with its windows, device buffers, pinned
     // staging and stream (the host builds part k + 1 while the device solves part k)
@@ -391,7 +390,7 @@ nav_ba_status solve_grid_window(nav_ba_ctx* ctx, const nav_ba_problem& p, const 
                                 nav_ba_result& r) {
     GridResult g;
     cudaEventRecord(ctx->ev0, ctx->stream);
-    cudaError_t e = grid_solve(h, lm_options(o), intrinsics_of(p), o.precision, ctx->stream, ctx->grid_cluster, g, -1.0,
+    cudaError_t e = grid_solve(h, lm_options(o), intrinsics_of(p), o.precision, ctx->stream, &ctx->stg.pool, g, -1.0,
                                nullptr);
     cudaEventRecord(ctx->ev1, ctx->stream);
     if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev1);
@@ -806,7 +805,7 @@ nav_ba_status nav_ba_reduced_system(nav_ba_ctx* ctx, const nav_ba_problem* p, co
     if (pb.host_status[0] == kGridWindow) {
         GridResult g;
         std::vector<double> dbg;
-        cudaError_t e = grid_solve(h, lm_options(o1), intrinsics_of(*p), o1.precision, ctx->stream, ctx->grid_cluster, g,
+        cudaError_t e = grid_solve(h, lm_options(o1), intrinsics_of(*p), o1.precision, ctx->stream, &ctx->stg.pool, g,
                                    lambda, &dbg);
         if (e != cudaSuccess) return cuda_status(ctx, e, "reduced system");
         const int m = 6 * h.nfc;
@@ -964,7 +963,7 @@ nav_ba_status nav_ba_vjp(nav_ba_ctx* ctx, const nav_ba_problem* p, const nav_ba_
     const double t_setup = ms_since(t0);
     GridResult g;
     cudaEventRecord(ctx->ev0, ctx->stream);
-    cudaError_t e = grid_solve(h, lm_options(*o), intrinsics_of(*p), NAV_BA_FP64, ctx->stream, ctx->grid_cluster, g, -1.0,
+    cudaError_t e = grid_solve(h, lm_options(*o), intrinsics_of(*p), NAV_BA_FP64, ctx->stream, &ctx->stg.pool, g, -1.0,
                                nullptr, &v);
     cudaEventRecord(ctx->ev1, ctx->stream);
     if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev1);
