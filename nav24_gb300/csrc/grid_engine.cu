@@ -153,13 +153,21 @@ __global__ void k_schur_points(WinArgs<Real> A, WinDesc D, double lambda, const 
 
 // Warp per nonzero block (a >= b) of S over its pair list; dense row-major S (m x m, lower part),
 // or, with Sb, block rows of both triangles in Real (row-major 6x6 per slot; bslot[blk]: the slot
-// of the block and of its transpose, -1 on the diagonal, whose block is written whole).
+// of the block and of its transpose, -1 on the diagonal, whose block is written whole).  Warps take
+// the blocks in order from a counter (next, zero at launch): block costs differ by an order of
+// magnitude (a diagonal block holds all of its camera's observations), and in-order work keeps the
+// records being read to a window of consecutive camera rows, which stays in L2.  Each block is
+// summed by one warp in a fixed order whichever warp takes it.
 template <class Real>
 __global__ void k_schur_blocks(WinArgs<Real> A, const int2* blocks, const int32_t* boff, int nblk, const int2* pairs,
                                const double* U, double lambda, double* S, int m, double* bs, Real* Sb,
-                               const int2* bslot) {
+                               const int2* bslot, int32_t* next) {
     const CC c = grid_view();
-    for (int blk = c.gw; blk < nblk; blk += c.CW) {
+    for (;;) {
+        int blk = 0;
+        if (c.lane == 0) blk = atomicAdd(next, 1);
+        blk = __shfl_sync(kFullG, blk, 0);
+        if (blk >= nblk) break;
         const int a = blocks[blk].x, b = blocks[blk].y;
         const int k0 = boff[blk], k1 = boff[blk + 1];
         Real acc[36];
@@ -1242,7 +1250,6 @@ __global__ void __launch_bounds__(256) k_pcg_explicit(PcgXArgs<Real> P) {
     const int kb = 6 * P.nfc;
     double* mv_part = P.part;             // phase 1: p.q over the cameras, S_ka p (3 per block)
     double* rz_part = P.part + 3LL * nb;  // phase 2: r.z, r.r (2 per block)
-    const double* pkc = P.kk + 3;
     long long tmark = clock64();
     auto mark = [&](int k) {  // phase timer: block 0's view
         if (!P.phase || blockIdx.x != 0 || threadIdx.x != 0) return;
@@ -1255,52 +1262,86 @@ __global__ void __launch_bounds__(256) k_pcg_explicit(PcgXArgs<Real> P) {
     // vectors are read into registers before anything is stored (the vectors may alias as far as
     // the compiler knows, which would otherwise order every load after the previous store).
     const int nchunk = (P.nfc + 31) >> 5, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+    // the k block's scalar work: thread 0 of the first block without a camera chunk
+    const bool kthread = P.nk && threadIdx.x == 0 && blockIdx.x == min(nchunk, nb - 1);
+    // k preconditioner: lower Cholesky l00 l10 l11 with the reciprocals of the diagonal
+    const double l10 = P.kk[4], il00 = P.nk ? 1.0 / P.kk[3] : 0.0, il11 = P.nk ? 1.0 / P.kk[5] : 0.0;
+    auto precond_k2 = [&](double r0, double r1, double& z0, double& z1) {
+        const double y0 = r0 * il00;
+        const double y1 = (r1 - l10 * y0) * il11;
+        z1 = y1 * il11;
+        z0 = (y0 - l10 * z1) * il00;
+    };
+    // Scalars of the iteration, reduced by warp 0 of every block (fixed order: the same bits in
+    // every block) and broadcast through shared memory.
+    __shared__ double sc[5];
     // init: x = 0, r = b, z = M^-1 r, previous direction 0 (the first direction is z)
-    double rz = 0.0, rr = 0.0;
-    for (int c = blockIdx.x + nb * wib; c < nchunk; c += nb * nwb) {
-        const int a = 32 * c + lane;
-        if (a >= P.nfc) continue;
-        double rv[6], zv[6];
-#pragma unroll
-        for (int i = 0; i < 6; ++i) rv[i] = P.b[6 * a + i];
-        precond_cam(P.pc, a, rv, zv);
-#pragma unroll
-        for (int i = 0; i < 6; ++i) {
-            P.x[6 * a + i] = 0.0;
-            P.p[0][6 * a + i] = 0.0;
-            P.r[6 * a + i] = rv[i];
-            P.z[6 * a + i] = zv[i];
-            P.zr[8 * a + i] = (Real)zv[i];
-            P.pr[0][8 * a + i] = Real(0);
-            rz += rv[i] * zv[i];
-            rr += rv[i] * rv[i];
-        }
-    }
-    if (P.nk && tid == 0) {
-        for (int i = 0; i < 2; ++i) {
-            P.x[kb + i] = 0.0;
-            P.p[0][kb + i] = 0.0;
-            P.r[kb + i] = P.b[kb + i];
-        }
-        precond_k(pkc, P.r + kb, P.z + kb);
-        for (int i = 0; i < 2; ++i) {
-            rz += P.r[kb + i] * P.z[kb + i];
-            rr += P.r[kb + i] * P.r[kb + i];
-        }
-    }
     {
+        double rz = 0.0, rr = 0.0;
+        for (int c = blockIdx.x + nb * wib; c < nchunk; c += nb * nwb) {
+            const int a = 32 * c + lane;
+            if (a >= P.nfc) continue;
+            double rv[6], zv[6];
+#pragma unroll
+            for (int i = 0; i < 6; ++i) rv[i] = P.b[6 * a + i];
+            precond_cam(P.pc, a, rv, zv);
+#pragma unroll
+            for (int i = 0; i < 6; ++i) {
+                P.x[6 * a + i] = 0.0;
+                P.p[0][6 * a + i] = 0.0;
+                P.r[6 * a + i] = rv[i];
+                P.z[6 * a + i] = zv[i];
+                P.zr[8 * a + i] = (Real)zv[i];
+                P.pr[0][8 * a + i] = Real(0);
+                rz += rv[i] * zv[i];
+                rr += rv[i] * rv[i];
+            }
+        }
+        if (kthread) {
+            const double r0 = P.b[kb], r1 = P.b[kb + 1];
+            double z0, z1;
+            precond_k2(r0, r1, z0, z1);
+            P.x[kb] = P.x[kb + 1] = 0.0;
+            P.p[0][kb] = P.p[0][kb + 1] = 0.0;
+            P.r[kb] = r0;
+            P.r[kb + 1] = r1;
+            P.z[kb] = z0;
+            P.z[kb + 1] = z1;
+            rz += r0 * z0 + r1 * z1;
+            rr += r0 * r0 + r1 * r1;
+        }
         double two[2] = {rz, rr};
         block_sum_w0<2>(two, rz_part);
     }
     grid.sync();
-    {
-        double two[2];
-        grid_sum_w0<2>(rz_part, nb, two);
-        rz = two[0];
-        rr = two[1];
+    if (threadIdx.x < 32) {
+        double zk0 = 0.0, zk1 = 0.0;
+        if (P.nk && lane == 0) {
+            zk0 = P.z[kb];
+            zk1 = P.z[kb + 1];
+        }
+        double s2[2] = {0.0, 0.0};
+        for (int i = lane; i < nb; i += 32) {
+            s2[0] += rz_part[2 * i];
+            s2[1] += rz_part[2 * i + 1];
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            s2[0] += __shfl_down_sync(kFullG, s2[0], o);
+            s2[1] += __shfl_down_sync(kFullG, s2[1], o);
+        }
+        if (lane == 0) {
+            sc[0] = 0.0;    // beta
+            sc[1] = s2[0];  // r.z
+            sc[2] = s2[1];  // r.r
+            sc[3] = zk0;    // p_k
+            sc[4] = zk1;
+        }
     }
+    __syncthreads();
+    double beta = sc[0], rz = sc[1], rr = sc[2], pk0 = sc[3], pk1 = sc[4];
+    __syncthreads();
     const double bb = rr;
-    double beta = 0.0;
     int pit = 0, cur = 0;
     for (; pit < P.max_it; ++pit) {
         if (pit % 4 == 0 && !(rr > P.tol2 * bb)) break;
@@ -1309,12 +1350,21 @@ __global__ void __launch_bounds__(256) k_pcg_explicit(PcgXArgs<Real> P) {
         const Real* pro = P.pr[cur];
         Real* prn = P.pr[cur ^ 1];
         const Real betar = (Real)beta;
-        const double pk0 = P.nk ? P.z[kb] + beta * po[kb] : 0.0;
-        const double pk1 = P.nk ? P.z[kb + 1] + beta * po[kb + 1] : 0.0;
         // phase 1: p = z + beta p, q = S p (warp per camera row)
         {
             double pq = 0.0, kq0 = 0.0, kq1 = 0.0;
             for (int a = gw; a < P.nfc; a += nwarp) {
+                // the row owner's own entries (lanes 0..5), loaded ahead of the products
+                const int io = 6 * a + (lane < 6 ? lane : 0);
+                const double zi = P.z[io], poi = po[io];
+                const Real zri = P.zr[8 * a + (lane < 6 ? lane : 0)], pori = pro[8 * a + (lane < 6 ? lane : 0)];
+                double h0 = 0.0, h1 = 0.0, x0 = 0.0, x1 = 0.0;
+                if (P.nk && lane < 6) {
+                    h0 = P.Hck[12LL * a + 2 * lane];
+                    h1 = P.Hck[12LL * a + 2 * lane + 1];
+                    x0 = P.Xak[12LL * a + 2 * lane];
+                    x1 = P.Xak[12LL * a + 2 * lane + 1];
+                }
                 Real acc[6] = {Real(0), Real(0), Real(0), Real(0), Real(0), Real(0)};
                 const int s1 = P.rs_off[a + 1];
                 // two slots per lane per round (both slots' loads in flight together); the second
@@ -1351,25 +1401,18 @@ __global__ void __launch_bounds__(256) k_pcg_explicit(PcgXArgs<Real> P) {
                     for (int o = 16; o > 0; o >>= 1) acc[i] += __shfl_xor_sync(kFullG, acc[i], o);
                 const Real qv = lane_value<6>(acc, lane);  // lanes 0..5: entry `lane` of the row
                 if (lane < 6) {
-                    const int i = 6 * a + lane;
-                    const double zi = P.z[i], poi = po[i];
-                    const Real zri = P.zr[8 * a + lane], pori = pro[8 * a + lane];
-                    double c0 = 0.0, c1 = 0.0;
-                    if (P.nk) {
-                        c0 = P.Hck[12LL * a + 2 * lane] - P.Xak[12LL * a + 2 * lane];
-                        c1 = P.Hck[12LL * a + 2 * lane + 1] - P.Xak[12LL * a + 2 * lane + 1];
-                    }
+                    const double c0 = h0 - x0, c1 = h1 - x1;
                     const double pv = zi + beta * poi;
                     const double qa = (double)qv + c0 * pk0 + c1 * pk1;
                     kq0 += c0 * pv;
                     kq1 += c1 * pv;
-                    pn[i] = pv;
+                    pn[6 * a + lane] = pv;
                     prn[8 * a + lane] = zri + betar * pori;
-                    P.q[i] = qa;
+                    P.q[6 * a + lane] = qa;
                     pq += pv * qa;
                 }
             }
-            if (P.nk && tid == 0) {
+            if (kthread) {
                 pn[kb] = pk0;
                 pn[kb + 1] = pk1;
             }
@@ -1381,16 +1424,34 @@ __global__ void __launch_bounds__(256) k_pcg_explicit(PcgXArgs<Real> P) {
         mark(2);
         // phase 2: q_k, alpha; x += alpha p, r -= alpha q, z = M^-1 r; r.z and r.r partials
         {
-            double sums[3];
-            grid_sum_w0<3>(mv_part, nb, sums);
-            double pq = sums[0];
-            double qk0 = 0.0, qk1 = 0.0;
-            if (P.nk) {
-                qk0 = P.skk[0] * pk0 + P.skk[1] * pk1 + sums[1];
-                qk1 = P.skk[1] * pk0 + P.skk[2] * pk1 + sums[2];
-                pq += pk0 * qk0 + pk1 * qk1;
+            if (threadIdx.x < 32) {
+                double s3[3] = {0.0, 0.0, 0.0};
+                for (int i = lane; i < nb; i += 32) {
+                    s3[0] += mv_part[3 * i];
+                    s3[1] += mv_part[3 * i + 1];
+                    s3[2] += mv_part[3 * i + 2];
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    s3[0] += __shfl_down_sync(kFullG, s3[0], o);
+                    s3[1] += __shfl_down_sync(kFullG, s3[1], o);
+                    s3[2] += __shfl_down_sync(kFullG, s3[2], o);
+                }
+                if (lane == 0) {
+                    double pq = s3[0], qk0 = 0.0, qk1 = 0.0;
+                    if (P.nk) {
+                        qk0 = P.skk[0] * pk0 + P.skk[1] * pk1 + s3[1];
+                        qk1 = P.skk[1] * pk0 + P.skk[2] * pk1 + s3[2];
+                        pq += pk0 * qk0 + pk1 * qk1;
+                    }
+                    sc[0] = pq != 0.0 ? rz / pq : 0.0;  // alpha
+                    sc[1] = qk0;
+                    sc[2] = qk1;
+                }
             }
-            const double alpha = pq != 0.0 ? rz / pq : 0.0;
+            __syncthreads();
+            const double alpha = sc[0], qk0 = sc[1], qk1 = sc[2];
+            __syncthreads();
             double rzn = 0.0, rrn = 0.0;
             for (int c = blockIdx.x + nb * wib; c < nchunk; c += nb * nwb) {
                 const int a = 32 * c + lane;
@@ -1419,16 +1480,19 @@ __global__ void __launch_bounds__(256) k_pcg_explicit(PcgXArgs<Real> P) {
                     rrn += rv[i] * rv[i];
                 }
             }
-            if (P.nk && tid == 0) {
-                P.x[kb] += alpha * pk0;
-                P.x[kb + 1] += alpha * pk1;
-                P.r[kb] -= alpha * qk0;
-                P.r[kb + 1] -= alpha * qk1;
-                precond_k(pkc, P.r + kb, P.z + kb);
-                for (int i = 0; i < 2; ++i) {
-                    rzn += P.r[kb + i] * P.z[kb + i];
-                    rrn += P.r[kb + i] * P.r[kb + i];
-                }
+            if (kthread) {
+                const double xk0 = P.x[kb], xk1 = P.x[kb + 1], rk0 = P.r[kb], rk1 = P.r[kb + 1];
+                const double r0 = rk0 - alpha * qk0, r1 = rk1 - alpha * qk1;
+                double z0, z1;
+                precond_k2(r0, r1, z0, z1);
+                P.x[kb] = xk0 + alpha * pk0;
+                P.x[kb + 1] = xk1 + alpha * pk1;
+                P.r[kb] = r0;
+                P.r[kb + 1] = r1;
+                P.z[kb] = z0;
+                P.z[kb + 1] = z1;
+                rzn += r0 * z0 + r1 * z1;
+                rrn += r0 * r0 + r1 * r1;
             }
             mark(3);
             double two[2] = {rzn, rrn};
@@ -1436,11 +1500,41 @@ __global__ void __launch_bounds__(256) k_pcg_explicit(PcgXArgs<Real> P) {
         }
         grid.sync();
         mark(4);
-        double two[2];
-        grid_sum_w0<2>(rz_part, nb, two);
-        rr = two[1];
-        beta = rz != 0.0 ? two[0] / rz : 0.0;
-        rz = two[0];
+        // beta, r.z, r.r and the next direction's k entries
+        if (threadIdx.x < 32) {
+            double zk0 = 0.0, zk1 = 0.0, pk0n = 0.0, pk1n = 0.0;
+            if (P.nk && lane == 0) {
+                zk0 = P.z[kb];
+                zk1 = P.z[kb + 1];
+                pk0n = pn[kb];
+                pk1n = pn[kb + 1];
+            }
+            double s2[2] = {0.0, 0.0};
+            for (int i = lane; i < nb; i += 32) {
+                s2[0] += rz_part[2 * i];
+                s2[1] += rz_part[2 * i + 1];
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                s2[0] += __shfl_down_sync(kFullG, s2[0], o);
+                s2[1] += __shfl_down_sync(kFullG, s2[1], o);
+            }
+            if (lane == 0) {
+                const double bn = rz != 0.0 ? s2[0] / rz : 0.0;
+                sc[0] = bn;
+                sc[1] = s2[0];
+                sc[2] = s2[1];
+                sc[3] = zk0 + bn * pk0n;
+                sc[4] = zk1 + bn * pk1n;
+            }
+        }
+        __syncthreads();
+        beta = sc[0];
+        rz = sc[1];
+        rr = sc[2];
+        pk0 = sc[3];
+        pk1 = sc[4];
+        __syncthreads();
         cur ^= 1;
         mark(0);
     }
@@ -1580,83 +1674,178 @@ void build_grid_host(const HostWindow& h, GridHost& g, int form, HostPool* pool)
         else
             for (int t = 0; t < ntask; ++t) fn(t);
     };
-    // pass 1, per row a: the columns b <= a of its nonzero blocks (sorted; a itself always) and
-    // each block's pair count
-    std::vector<std::vector<int32_t>> rowcols(nfc), rowcnt(nfc);
-    run([&](int t) {
-        int a0, a1;
-        rows_of(t, a0, a1);
-        std::vector<int32_t> loc(nfc, -1), cols, cn, perm;
-        for (int a = a0; a < a1; ++a) {
-            cols.assign(1, a);
-            cn.assign(1, 0);
-            loc[a] = 0;
-            for (int s = loff[a]; s < loff[a + 1]; ++s) {
-                const int i = h.edge_pt[g.cam_list[s]];
-                if (h.pt_free[i] < 0) continue;
-                for (int f = h.pt_eoff[i]; f < h.pt_eoff[i + 1]; ++f) {
-                    const int b = h.cam_free[h.edge_cam[f]];
-                    if (b < 0 || b > a) continue;
-                    int k = loc[b];
-                    if (k < 0) {
-                        k = loc[b] = (int)cols.size();
-                        cols.push_back(b);
-                        cn.push_back(0);
-                    }
-                    cn[k]++;
-                }
-            }
-            perm.resize(cols.size());
-            for (size_t k = 0; k < perm.size(); ++k) perm[k] = (int32_t)k;
-            std::sort(perm.begin(), perm.end(), [&](int32_t x, int32_t y) { return cols[x] < cols[y]; });
-            rowcols[a].resize(cols.size());
-            rowcnt[a].resize(cols.size());
-            for (size_t k = 0; k < perm.size(); ++k) {
-                rowcols[a][k] = cols[perm[k]];
-                rowcnt[a][k] = cn[perm[k]];
-            }
-            for (int b : cols) loc[b] = -1;
-        }
-    });
+    std::vector<std::vector<int32_t>> rowcols(nfc);
     std::vector<int32_t> row_start(nfc + 1, 0);
-    for (int a = 0; a < nfc; ++a) row_start[a + 1] = row_start[a] + (int32_t)rowcols[a].size();
-    const int nblk = row_start[nfc];
-    g.blocks.resize(std::max(1, nblk));
-    g.boff.assign(nblk + 1, 0);
-    for (int a = 0; a < nfc; ++a)
-        for (size_t k = 0; k < rowcols[a].size(); ++k) {
-            const int blk = row_start[a] + (int)k;
-            g.blocks[blk] = make_int2(a, rowcols[a][k]);
-            g.boff[blk + 1] = g.boff[blk] + rowcnt[a][k];
-        }
-    if (g.boff.size() == 1) g.boff.push_back(0);
-    lap("blocks");
-    // pass 2, per row: the pairs of each block in camera-list (point) order
-    g.pairs.resize(std::max<size_t>(1, (size_t)g.boff[nblk]));
-    g.pairs[0] = make_int2(0, 0);
-    run([&](int t) {
-        int a0, a1;
-        rows_of(t, a0, a1);
-        std::vector<int32_t> loc(nfc, -1), cur;
-        for (int a = a0; a < a1; ++a) {
-            const auto& rc = rowcols[a];
-            cur.resize(rc.size());
-            for (size_t k = 0; k < rc.size(); ++k) {
-                loc[rc[k]] = (int32_t)k;
-                cur[k] = g.boff[row_start[a] + k];
-            }
-            for (int s = loff[a]; s < loff[a + 1]; ++s) {
-                const int e = g.cam_list[s];
-                const int i = h.edge_pt[e];
-                if (h.pt_free[i] < 0) continue;
-                for (int f = h.pt_eoff[i]; f < h.pt_eoff[i + 1]; ++f) {
+    int nblk = 0;
+    // NAVBA_GRID_HOST=rows takes the per-row passes at any size (they give the same lists)
+    const char* hp = getenv("NAVBA_GRID_HOST");
+    const bool by_rows = hp && !strcmp(hp, "rows");
+    if (!by_rows && (size_t)nfc * nfc <= ((size_t)1 << 24)) {
+        // Point-major passes over contiguous point ranges (sequential reads of each point's
+        // observations), with a dense nfc x nfc map of the co-observing pairs.  Within a block
+        // the pairs come in point order, then edge order: the same list the per-row passes build.
+        const int npt = h.npt;
+        const int T = std::max(1, std::min(pool ? hw : 1, npt / 4096));
+        auto pts_of = [&](int t, int& i0, int& i1) {
+            i0 = (int)((long long)npt * t / T);
+            i1 = (int)((long long)npt * (t + 1) / T);
+        };
+        auto run_pts = [&](const std::function<void(int)>& fn) {
+            if (pool && T > 1)
+                pool->run(T, fn);
+            else
+                for (int t = 0; t < T; ++t) fn(t);
+        };
+        // every (e, f) pair of a free point with free cameras a = cam(e) >= b = cam(f)
+        auto for_pairs = [&](int i, auto fn) {
+            const int e0 = h.pt_eoff[i], e1 = h.pt_eoff[i + 1];
+            for (int e = e0; e < e1; ++e) {
+                const int a = h.cam_free[h.edge_cam[e]];
+                if (a < 0) continue;
+                for (int f = e0; f < e1; ++f) {
                     const int b = h.cam_free[h.edge_cam[f]];
-                    if (b >= 0 && b <= a) g.pairs[cur[loc[b]]++] = make_int2(e, f);
+                    if (b >= 0 && b <= a) fn(a, b, e, f);
                 }
             }
-            for (int b : rc) loc[b] = -1;
+        };
+        // pass 1: the map of nonzero lower blocks (relaxed atomic flags: the same value from any task)
+        std::vector<uint8_t> seen((size_t)nfc * nfc, 0);
+        run_pts([&](int t) {
+            int i0, i1;
+            pts_of(t, i0, i1);
+            for (int i = i0; i < i1; ++i) {
+                if (h.pt_free[i] < 0) continue;
+                for_pairs(i, [&](int a, int b, int, int) {
+                    uint8_t* m = &seen[(size_t)a * nfc + b];
+                    if (!__atomic_load_n(m, __ATOMIC_RELAXED)) __atomic_store_n(m, (uint8_t)1, __ATOMIC_RELAXED);
+                });
+            }
+        });
+        std::vector<int32_t> bidx((size_t)nfc * nfc, -1);
+        for (int a = 0; a < nfc; ++a) {
+            seen[(size_t)a * nfc + a] = 1;
+            for (int b = 0; b <= a; ++b)
+                if (seen[(size_t)a * nfc + b]) rowcols[a].push_back(b);
+            row_start[a + 1] = row_start[a] + (int32_t)rowcols[a].size();
+            for (size_t k = 0; k < rowcols[a].size(); ++k) bidx[(size_t)a * nfc + rowcols[a][k]] = row_start[a] + (int32_t)k;
         }
-    });
+        nblk = row_start[nfc];
+        g.blocks.resize(std::max(1, nblk));
+        for (int a = 0; a < nfc; ++a)
+            for (size_t k = 0; k < rowcols[a].size(); ++k) g.blocks[row_start[a] + k] = make_int2(a, rowcols[a][k]);
+        // pass 2: pair counts per point range and block; the ranges' cursors in point order
+        std::vector<int32_t> cnt((size_t)T * std::max(1, nblk), 0);
+        run_pts([&](int t) {
+            int i0, i1;
+            pts_of(t, i0, i1);
+            int32_t* c = cnt.data() + (size_t)t * nblk;
+            for (int i = i0; i < i1; ++i) {
+                if (h.pt_free[i] < 0) continue;
+                for_pairs(i, [&](int a, int b, int, int) { c[bidx[(size_t)a * nfc + b]]++; });
+            }
+        });
+        g.boff.assign(nblk + 1, 0);
+        for (int k = 0; k < nblk; ++k) {
+            int32_t sum = g.boff[k];
+            for (int t = 0; t < T; ++t) {
+                const int32_t n = cnt[(size_t)t * nblk + k];
+                cnt[(size_t)t * nblk + k] = sum;  // now the range's cursor
+                sum += n;
+            }
+            g.boff[k + 1] = sum;
+        }
+        if (g.boff.size() == 1) g.boff.push_back(0);
+        lap("blocks");
+        // pass 3: fill
+        g.pairs.resize(std::max<size_t>(1, (size_t)g.boff[nblk]));
+        g.pairs[0] = make_int2(0, 0);
+        run_pts([&](int t) {
+            int i0, i1;
+            pts_of(t, i0, i1);
+            int32_t* c = cnt.data() + (size_t)t * nblk;
+            for (int i = i0; i < i1; ++i) {
+                if (h.pt_free[i] < 0) continue;
+                for_pairs(i, [&](int a, int b, int e, int f) { g.pairs[c[bidx[(size_t)a * nfc + b]]++] = make_int2(e, f); });
+            }
+        });
+    } else {
+        // pass 1, per row a: the columns b <= a of its nonzero blocks (sorted; a itself always) and
+        // each block's pair count
+        std::vector<std::vector<int32_t>> rowcnt(nfc);
+        run([&](int t) {
+            int a0, a1;
+            rows_of(t, a0, a1);
+            std::vector<int32_t> loc(nfc, -1), cols, cn, perm;
+            for (int a = a0; a < a1; ++a) {
+                cols.assign(1, a);
+                cn.assign(1, 0);
+                loc[a] = 0;
+                for (int s = loff[a]; s < loff[a + 1]; ++s) {
+                    const int i = h.edge_pt[g.cam_list[s]];
+                    if (h.pt_free[i] < 0) continue;
+                    for (int f = h.pt_eoff[i]; f < h.pt_eoff[i + 1]; ++f) {
+                        const int b = h.cam_free[h.edge_cam[f]];
+                        if (b < 0 || b > a) continue;
+                        int k = loc[b];
+                        if (k < 0) {
+                            k = loc[b] = (int)cols.size();
+                            cols.push_back(b);
+                            cn.push_back(0);
+                        }
+                        cn[k]++;
+                    }
+                }
+                perm.resize(cols.size());
+                for (size_t k = 0; k < perm.size(); ++k) perm[k] = (int32_t)k;
+                std::sort(perm.begin(), perm.end(), [&](int32_t x, int32_t y) { return cols[x] < cols[y]; });
+                rowcols[a].resize(cols.size());
+                rowcnt[a].resize(cols.size());
+                for (size_t k = 0; k < perm.size(); ++k) {
+                    rowcols[a][k] = cols[perm[k]];
+                    rowcnt[a][k] = cn[perm[k]];
+                }
+                for (int b : cols) loc[b] = -1;
+            }
+        });
+        for (int a = 0; a < nfc; ++a) row_start[a + 1] = row_start[a] + (int32_t)rowcols[a].size();
+        nblk = row_start[nfc];
+        g.blocks.resize(std::max(1, nblk));
+        g.boff.assign(nblk + 1, 0);
+        for (int a = 0; a < nfc; ++a)
+            for (size_t k = 0; k < rowcols[a].size(); ++k) {
+                const int blk = row_start[a] + (int)k;
+                g.blocks[blk] = make_int2(a, rowcols[a][k]);
+                g.boff[blk + 1] = g.boff[blk] + rowcnt[a][k];
+            }
+        if (g.boff.size() == 1) g.boff.push_back(0);
+        lap("blocks");
+        // pass 2, per row: the pairs of each block in camera-list (point) order
+        g.pairs.resize(std::max<size_t>(1, (size_t)g.boff[nblk]));
+        g.pairs[0] = make_int2(0, 0);
+        run([&](int t) {
+            int a0, a1;
+            rows_of(t, a0, a1);
+            std::vector<int32_t> loc(nfc, -1), cur;
+            for (int a = a0; a < a1; ++a) {
+                const auto& rc = rowcols[a];
+                cur.resize(rc.size());
+                for (size_t k = 0; k < rc.size(); ++k) {
+                    loc[rc[k]] = (int32_t)k;
+                    cur[k] = g.boff[row_start[a] + k];
+                }
+                for (int s = loff[a]; s < loff[a + 1]; ++s) {
+                    const int e = g.cam_list[s];
+                    const int i = h.edge_pt[e];
+                    if (h.pt_free[i] < 0) continue;
+                    for (int f = h.pt_eoff[i]; f < h.pt_eoff[i + 1]; ++f) {
+                        const int b = h.cam_free[h.edge_cam[f]];
+                        if (b >= 0 && b <= a) g.pairs[cur[loc[b]]++] = make_int2(e, f);
+                    }
+                }
+                for (int b : rc) loc[b] = -1;
+            }
+        });
+    }
     lap("pairs");
     if (form == kFormBlocks) {
         // row a: its lower columns (ending with a), then the columns c > a whose row holds a
@@ -1831,6 +2020,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     double* d_bs = dv.alloc<double>(std::max(1, mt));
     double* d_rinv = dv.alloc<double>(std::max(1, m));
     int32_t* d_ok = dv.alloc<int32_t>(1);
+    int32_t* d_next = dv.alloc<int32_t>(1);  // work counter of the block-ordered Schur kernel
     const int TB = 256;
     const int nsm_blocks = 152 * 4;
     const int pblocks = std::max(1, std::min(nsm_blocks, (np + TB - 1) / TB));
@@ -2057,8 +2247,9 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     auto assemble_S = [&](double lam) {
         chk(cudaMemsetAsync(d_S, 0, sizeof(double) * (size_t)m * m, st));
         const int nb = (int)g.blocks.size();
+        chk(cudaMemsetAsync(d_next, 0, sizeof(int32_t), st));
         k_schur_blocks<Real><<<std::max(1, std::min(nsm_blocks, (nb * 32 + TB - 1) / TB)), TB, 0, st>>>(
-            A, d_blocks, d_boff, (int)(g.boff.size() - 1), d_pairs, d_U, lam, d_S, m, d_bs, (Real*)nullptr, nullptr);
+            A, d_blocks, d_boff, (int)(g.boff.size() - 1), d_pairs, d_U, lam, d_S, m, d_bs, (Real*)nullptr, nullptr, d_next);
         chk(cudaGetLastError());
     };
     // Cholesky of S in place (cooperative, whole GPU); false if S is not positive definite
@@ -2216,9 +2407,10 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                 if (nfc > 0 && pcg_x) {
                     // S_ab (block rows, both triangles) and b' from the pair lists, then the factors
                     const int nb = (int)g.blocks.size();
+                    chk(cudaMemsetAsync(d_next, 0, sizeof(int32_t), st));
                     k_schur_blocks<Real><<<std::max(1, std::min(nsm_blocks, (nb * 32 + TB - 1) / TB)), TB, 0, st>>>(
                         A, d_blocks, d_boff, (int)(g.boff.size() - 1), d_pairs, d_U, lam_use, nullptr, 0, d_bs, d_Sb,
-                        d_bslot);
+                        d_bslot, d_next);
                     k_pcg_precond_blocks<Real><<<(nfc + TB - 1) / TB, TB, 0, st>>>(d_Sb, d_rs_dslot, nfc, d_pc, d_ok);
                     chk(cudaGetLastError());
                 } else if (nfc > 0) {

@@ -73,3 +73,23 @@ def test_grid_workload_full_size(ctx):
     assert rel(g.stats["final_cost"], r.stats["final_cost"]) < 1e-6
     g = ctx.solve(p, workload_options(1, abi.MIXED))
     assert rel(g.stats["final_cost"], r.stats["final_cost"]) < 1e-6
+
+
+@pytest.mark.parametrize("solver", [abi.SOLVER_CHOLESKY, abi.SOLVER_PCG])
+def test_grid_host_structure_passes_agree(ctx, monkeypatch, solver):
+    """The reduced system's pair lists are built point-major with a dense block map up to 4096 free
+    cameras and per camera row beyond; both give the same lists, so the solves agree bit for bit
+    (NAVBA_GRID_HOST=rows forces the per-row passes)."""
+    p = Synth(4, n_cams=60, n_points=6000, seed=8).window(0)
+    o = workload_options(4)
+    o.iterations = 6
+    o.solver = solver
+    o.optimize_distortion = 1 if solver == abi.SOLVER_PCG else 0
+    res = []
+    for mode in ("", "rows"):
+        monkeypatch.setenv("NAVBA_GRID_HOST", mode)
+        res.append(ctx.solve(p, o))
+    a, b = res
+    assert a.status == abi.OK and b.status == abi.OK
+    assert np.array_equal(a.cam_pose, b.cam_pose) and np.array_equal(a.points, b.points)
+    assert np.array_equal(a.cost_trace, b.cost_trace, equal_nan=True)
