@@ -45,6 +45,7 @@ namespace {
 constexpr unsigned kFullG = 0xffffffffu;
 constexpr int kTile = 32;
 constexpr int kCamChunk = 256;
+constexpr int kPairChunk = 256;  // pairs per work item of the Schur-block kernel
 
 __device__ __forceinline__ CC grid_view() {
     CC c{};
@@ -151,32 +152,37 @@ __global__ void k_schur_points(WinArgs<Real> A, WinDesc D, double lambda, const 
     block_partial<false>((double)schur_points<Real>(A, c, D, lambda, camr, X), part);
 }
 
-// Warp per nonzero block (a >= b) of S over its pair list; dense row-major S (m x m, lower part),
-// or, with Sb, block rows of both triangles in Real (row-major 6x6 per slot; bslot[blk]: the slot
-// of the block and of its transpose, -1 on the diagonal, whose block is written whole).  Warps take
-// the blocks in order from a counter (next, zero at launch): block costs differ by an order of
-// magnitude (a diagonal block holds all of its camera's observations), and in-order work keeps the
-// records being read to a window of consecutive camera rows, which stays in L2.  Each block is
-// summed by one warp in a fixed order whichever warp takes it.
+// Warp per work item: up to kPairChunk pairs of one nonzero block (a >= b) of S.  Output: dense
+// row-major S (m x m, lower part), or, with Sb, block rows of both triangles in Real (row-major 6x6
+// per slot; bslot[blk]: the slot of the block and of its transpose, -1 on the diagonal, whose block is
+// written whole).  Warps take the items in order from a counter (next, zero at launch), so the
+// records being read stay within a window of consecutive camera rows, which stays in L2; items are
+// short so that no warp lags far behind the window (a diagonal block holds all of its camera's
+// observations).  A block of several items is finished by whichever of its items ends last (count
+// in done[blk], zero at launch): it sums the items' partials (48 Real per item in part) in item
+// order.  Every sum has a fixed order whichever warps take the items.
 template <class Real>
-__global__ void k_schur_blocks(WinArgs<Real> A, const int2* blocks, const int32_t* boff, int nblk, const int2* pairs,
-                               const double* U, double lambda, double* S, int m, double* bs, Real* Sb,
-                               const int2* bslot, int32_t* next) {
+__global__ void k_schur_blocks(WinArgs<Real> A, const int2* blocks, const int32_t* boff, const int4* items,
+                               int n_items, const int2* pairs, const double* U, double lambda, double* S, int m,
+                               double* bs, Real* Sb, const int2* bslot, int32_t* next, int32_t* done, Real* part,
+                               int chunk) {
     const CC c = grid_view();
+    const int slot = rs36_slot(c.lane);  // this lane's two entries of the block (slot, slot + 1)
     for (;;) {
-        int blk = 0;
-        if (c.lane == 0) blk = atomicAdd(next, 1);
-        blk = __shfl_sync(kFullG, blk, 0);
-        if (blk >= nblk) break;
+        int j = 0;
+        if (c.lane == 0) j = atomicAdd(next, 1);
+        j = __shfl_sync(kFullG, j, 0);
+        if (j >= n_items) break;
+        const int4 it = items[j];  // block, first and end pair, first item of the block
+        const int blk = it.x;
         const int a = blocks[blk].x, b = blocks[blk].y;
-        const int k0 = boff[blk], k1 = boff[blk + 1];
         Real acc[36];
         Real accb[6];
 #pragma unroll
         for (int k = 0; k < 36; ++k) acc[k] = Real(0);
 #pragma unroll
         for (int k = 0; k < 6; ++k) accb[k] = Real(0);
-        for (int k = k0 + c.lane; k < k1; k += 32) {
+        for (int k = it.y + c.lane; k < it.z; k += 32) {
             const int2 pr = pairs[k];
             Real ai[18], aj[18];
             Rec<Real>::load18(A.edge_a + (long long)Rec<Real>::kEdge * pr.x, ai);
@@ -195,12 +201,42 @@ __global__ void k_schur_blocks(WinArgs<Real> A, const int2* blocks, const int32_
         }
         Real sums[2];
         reduce_scatter36(acc, c.lane, sums[0], sums[1]);  // lane: the two entries it writes
-        const int slot = rs36_slot(c.lane);
+        Real bk = Real(0);
         if (a == b) {
 #pragma unroll
             for (int k = 0; k < 6; ++k)
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) accb[k] += __shfl_xor_sync(kFullG, accb[k], o);
+            bk = lane_value<6>(accb, c.lane);
+        }
+        const int np_blk = boff[blk + 1] - boff[blk];
+        const int nit = np_blk > chunk ? (int)(((long long)np_blk + chunk - 1) / chunk) : 1;
+        double sumd[2] = {(double)sums[0], (double)sums[1]}, bkd = (double)bk;
+        if (nit > 1) {
+            Real* pp = part + 48LL * j;
+#pragma unroll
+            for (int rnd = 0; rnd < 2; ++rnd)
+                if (slot + rnd < 36) pp[slot + rnd] = sums[rnd];
+            if (c.lane < 6) pp[36 + c.lane] = bk;
+            __threadfence();
+            int last = 0;
+            if (c.lane == 0) last = atomicAdd(done + blk, 1) == nit - 1;
+            if (!__shfl_sync(kFullG, last, 0)) continue;
+            __threadfence();
+            // the partials are summed in FP64: a diagonal block's sum nearly cancels U_a, and the
+            // mixed form factors S in FP32
+            const Real* p0 = part + 48LL * it.w;
+#pragma unroll
+            for (int rnd = 0; rnd < 2; ++rnd) {
+                double v = 0.0;
+                if (slot + rnd < 36)
+                    for (int i = 0; i < nit; ++i) v += (double)__ldcg(p0 + 48LL * i + slot + rnd);
+                sumd[rnd] = v;
+            }
+            double vb = 0.0;
+            if (c.lane < 6)
+                for (int i = 0; i < nit; ++i) vb += (double)__ldcg(p0 + 48LL * i + 36 + c.lane);
+            bkd = vb;
         }
         // one FP64 warp instruction per operation with all lanes active (charged per warp instruction)
         const int2 bs2 = Sb ? bslot[blk] : make_int2(0, -1);
@@ -209,7 +245,7 @@ __global__ void k_schur_blocks(WinArgs<Real> A, const int2* blocks, const int32_
             const int k = slot + rnd;
             const int r = k / 6, q = k % 6;
             if (k < 36 && (Sb || !(a == b && q > r))) {
-                double v = -(double)sums[rnd];
+                double v = -sumd[rnd];
                 if (a == b) {
                     v += U[28LL * a + (r >= q ? tri(r, q) : tri(q, r))];
                     if (r == q) v += lambda;
@@ -222,10 +258,7 @@ __global__ void k_schur_blocks(WinArgs<Real> A, const int2* blocks, const int32_
                 }
             }
         }
-        if (a == b) {
-            const Real bk = lane_value<6>(accb, c.lane);
-            if (c.lane < 6) bs[6 * a + c.lane] = U[28LL * a + 21 + c.lane] - (double)bk;
-        }
+        if (a == b && c.lane < 6) bs[6 * a + c.lane] = U[28LL * a + 21 + c.lane] - bkd;
     }
 }
 
@@ -1593,6 +1626,8 @@ struct GridHost {
     // in its own row and the slot of the transposed block (-1 on the diagonal)
     std::vector<int32_t> rs_off, rs_col, rs_dslot;
     std::vector<int2> bslot;
+    // work items of the Schur-block kernel: block, first and end pair, first item of the block
+    std::vector<int4> sitems;
 };
 
 // Sum over points of k (k + 1) / 2 (k: free-camera observations of a free point): the pair count
@@ -1659,6 +1694,7 @@ void build_grid_host(const HostWindow& h, GridHost& g, int form, HostPool* pool)
     g.rs_col.assign(1, 0);
     g.rs_dslot.assign(std::max(1, nfc), 0);
     g.bslot.assign(1, make_int2(0, -1));
+    g.sitems.assign(1, make_int4(0, 0, 0, 0));
     lap("camera lists");
     if (form == kFormNone) return;
     // row ranges on the workers (more ranges than workers: rows differ in cost)
@@ -1846,6 +1882,21 @@ void build_grid_host(const HostWindow& h, GridHost& g, int form, HostPool* pool)
             }
         });
     }
+    // work items: the explicit-PCG form splits the pair lists (large problems: the L2 window); the
+    // Cholesky form keeps one item per block
+    const int chunk = form == kFormBlocks ? kPairChunk : INT32_MAX;
+    g.sitems.clear();
+    for (int k = 0; k < nblk; ++k) {
+        const int first = (int)g.sitems.size();
+        const int p0 = g.boff[k], p1 = g.boff[k + 1];
+        int q = p0;
+        do {
+            const int q1 = p1 - q > chunk ? q + chunk : p1;
+            g.sitems.push_back(make_int4(k, q, q1, first));
+            q = q1;
+        } while (q < p1);
+    }
+    if (g.sitems.empty()) g.sitems.push_back(make_int4(0, 0, 0, 0));
     lap("pairs");
     if (form == kFormBlocks) {
         // row a: its lower columns (ending with a), then the columns c > a whose row holds a
@@ -2020,7 +2071,11 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     double* d_bs = dv.alloc<double>(std::max(1, mt));
     double* d_rinv = dv.alloc<double>(std::max(1, m));
     int32_t* d_ok = dv.alloc<int32_t>(1);
-    int32_t* d_next = dv.alloc<int32_t>(1);  // work counter of the block-ordered Schur kernel
+    int32_t* d_next = dv.alloc<int32_t>(1);  // work counter of the item-ordered Schur kernel
+    const int n_sitems = (int)g.sitems.size();
+    int4* d_sitems = dv.alloc<int4>(g.sitems.size());
+    int32_t* d_sdone = dv.alloc<int32_t>(g.blocks.size());
+    Real* d_spart = dv.alloc<Real>(48LL * n_sitems);
     const int TB = 256;
     const int nsm_blocks = 152 * 4;
     const int pblocks = std::max(1, std::min(nsm_blocks, (np + TB - 1) / TB));
@@ -2118,6 +2173,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     chk(up(d_blocks, g.blocks, st));
     chk(up(d_boff, g.boff, st));
     chk(up(d_pairs, g.pairs, st));
+    chk(up(d_sitems, g.sitems, st));
     chk(up(d_tfirst, g.tfirst, st));
     chk(up(d_pan_off, g.pan_off, st));
     chk(up(d_pan_row, g.pan_row, st));
@@ -2246,10 +2302,11 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     // dense reduced system S = U + lam I - sum A A^T (lower part) and b'
     auto assemble_S = [&](double lam) {
         chk(cudaMemsetAsync(d_S, 0, sizeof(double) * (size_t)m * m, st));
-        const int nb = (int)g.blocks.size();
         chk(cudaMemsetAsync(d_next, 0, sizeof(int32_t), st));
-        k_schur_blocks<Real><<<std::max(1, std::min(nsm_blocks, (nb * 32 + TB - 1) / TB)), TB, 0, st>>>(
-            A, d_blocks, d_boff, (int)(g.boff.size() - 1), d_pairs, d_U, lam, d_S, m, d_bs, (Real*)nullptr, nullptr, d_next);
+        chk(cudaMemsetAsync(d_sdone, 0, sizeof(int32_t) * g.blocks.size(), st));
+        k_schur_blocks<Real><<<std::max(1, std::min(nsm_blocks, (n_sitems * 32 + TB - 1) / TB)), TB, 0, st>>>(
+            A, d_blocks, d_boff, d_sitems, n_sitems, d_pairs, d_U, lam, d_S, m, d_bs, (Real*)nullptr, nullptr, d_next,
+            d_sdone, d_spart, INT32_MAX);
         chk(cudaGetLastError());
     };
     // Cholesky of S in place (cooperative, whole GPU); false if S is not positive definite
@@ -2284,7 +2341,16 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     // S's entries are FP32 sums already, so the FP32 factor's error is of the order of S's own; the
     // refinement step removes it.  A pivot that is not positive in FP32 falls back to the FP64
     // factorization.  Returns false if S is not positive definite in FP64 either.
-    auto solve_S_mixed = [&]() -> bool {
+    // FP32 factorization with one FP64 refinement; a non-positive FP32 pivot falls back to the FP64
+    // factorization, and so do later trials at up to 4x the damping of the last failure (S is then
+    // too close to singular for FP32, and the failed attempt is not repeated)
+    double f32_fail_lambda = -1.0;
+    auto solve_S_mixed = [&](double lam) -> bool {
+        if (f32_fail_lambda > 0.0 && lam <= 4.0 * f32_fail_lambda) {
+            if (!factor_S()) return false;
+            k_chol_solve<<<1, 1024, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_bs);
+            return true;
+        }
         const int32_t one = 1;
         chk(cudaMemcpyAsync(d_ok, &one, sizeof(int32_t), cudaMemcpyHostToDevice, st));
         k_s_round<<<nsm_blocks, TB, 0, st>>>(d_S, d_S32, m);
@@ -2303,6 +2369,9 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         chk(cudaStreamSynchronize(st));
         if (e != cudaSuccess) return false;
         if (!okh) {
+            const char* vb = getenv("NAVBA_VERBOSE");
+            if (vb && vb[0] == '1') fprintf(stderr, "[navba grid] FP32 factor: non-positive pivot, FP64 factor instead\n");
+            f32_fail_lambda = std::max(f32_fail_lambda, lam);
             if (!factor_S()) return false;
             k_chol_solve<<<1, 1024, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_bs);
             return true;
@@ -2406,11 +2475,11 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                 chk(cudaMemcpyAsync(d_ok, &one, sizeof(int32_t), cudaMemcpyHostToDevice, st));
                 if (nfc > 0 && pcg_x) {
                     // S_ab (block rows, both triangles) and b' from the pair lists, then the factors
-                    const int nb = (int)g.blocks.size();
                     chk(cudaMemsetAsync(d_next, 0, sizeof(int32_t), st));
-                    k_schur_blocks<Real><<<std::max(1, std::min(nsm_blocks, (nb * 32 + TB - 1) / TB)), TB, 0, st>>>(
-                        A, d_blocks, d_boff, (int)(g.boff.size() - 1), d_pairs, d_U, lam_use, nullptr, 0, d_bs, d_Sb,
-                        d_bslot, d_next);
+                    chk(cudaMemsetAsync(d_sdone, 0, sizeof(int32_t) * g.blocks.size(), st));
+                    k_schur_blocks<Real><<<std::max(1, std::min(nsm_blocks, (n_sitems * 32 + TB - 1) / TB)), TB, 0, st>>>(
+                        A, d_blocks, d_boff, d_sitems, n_sitems, d_pairs, d_U, lam_use, nullptr, 0, d_bs, d_Sb,
+                        d_bslot, d_next, d_sdone, d_spart, kPairChunk);
                     k_pcg_precond_blocks<Real><<<(nfc + TB - 1) / TB, TB, 0, st>>>(d_Sb, d_rs_dslot, nfc, d_pc, d_ok);
                     chk(cudaGetLastError());
                 } else if (nfc > 0) {
@@ -2543,7 +2612,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                     return e;
                 }
                 if (mixed_chol) {
-                    ok = solve_S_mixed() && ok;
+                    ok = solve_S_mixed(lam_use) && ok;
                 } else {
                     ok = factor_S() && ok;
                     if (ok) k_chol_solve<<<1, 1024, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_bs);
