@@ -120,10 +120,12 @@ struct PreparedBatch {
     Intr intr{};
 };
 
-// Allocate (reusing pb.dev's buffers when large enough) and upload through pinned staging
-// (synchronous on return).  Returns a CUDA error or 0.
+// Allocate (reusing pb.dev's buffers when large enough) and upload through pinned staging.
+// Synchronous on return unless sync is false: then the copies are in flight on `stream`, and stg
+// must not be restaged before the stream has passed them.  Returns a CUDA error or 0.
 cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int precision,
-                                int trace_stride, HostStaging& stg, HostPool& pool, std::string* why);
+                                int trace_stride, HostStaging& stg, HostPool& pool, std::string* why,
+                                bool sync = true);
 void window_batch_free(WindowBatch& b);
 
 // Launch the persistent window kernel over all windows of the batch.

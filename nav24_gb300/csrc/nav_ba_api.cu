@@ -15,6 +15,9 @@
 
 using namespace navba;
 
+// Parts of a pipelined batched solve (8 measured slower: 64-window parts leave host workers idle).
+constexpr int kSolveParts = 4;
+
 struct nav_ba_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -38,7 +41,7 @@ struct nav_ba_ctx {
         HostStaging stg;
         cudaStream_t stream = nullptr;
     };
-    Part parts[4];
+    Part parts[kSolveParts];
     // nav_ba_run's launch sequence over the prepared batch (queue reset, persistent kernel),
     // captured once in a CUDA graph at prepare time and replayed by every run with the same options
     cudaGraphExec_t run_graph = nullptr;
@@ -254,7 +257,7 @@ nav_ba_status build_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, c
     pb.host_status.assign(n, NAV_BA_OK);
     std::vector<nav_ba_status> vst(n, NAV_BA_OK);
     std::vector<std::string> vwhy(n);
-    const int nth = HostPool::tasks_for(n, 8);
+    const int nth = HostPool::tasks_for(n, 2);
     auto work = [&](int t) {
         for (int i = t; i < n; i += nth) {
             const nav_ba_status s = checked ? NAV_BA_OK : check_problem(probs, i, o, &vwhy[i]);
@@ -406,12 +409,11 @@ nav_ba_status solve_grid_window(nav_ba_ctx* ctx, const nav_ba_problem& p, const 
 // Batched solve in parts pipelined across the host and the device: part k is built on the host,
 // staged and uploaded, and its window kernel launched on the part's stream; the host goes on with
 // part k + 1 while the device solves part k (the parts' kernels also run side by side).  A window
-// is solved start to finish by one CTA (several milliseconds for the largest), so the parts take
-// the windows largest first: the last part, launched last, holds the smallest windows and ends
-// soon after its launch.  Windows are independent, so the results equal those of one launch over
+// is solved start to finish by one cluster (several milliseconds for the largest), so the parts take
+// the windows largest first: the first part's windows set the critical path and go to the device
+// as early as possible; the last part, launched last, holds the smallest windows.  Windows are independent, so the results equal those of one launch over
 // the batch.  The whole batch is checked before any part is built, so errors are reported as by
 // the single-launch path (the first failing problem, nothing written).
-constexpr int kSolveParts = 4;  // 8 measured slower: 64-window parts leave host workers idle
 constexpr int kPipelineMinWindows = 64;
 
 nav_ba_status solve_pipelined(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, const nav_ba_options* o,
@@ -451,8 +453,19 @@ nav_ba_status solve_pipelined(nav_ba_ctx* ctx, const nav_ba_problem* probs, int 
             }
         }
     } swap_back{pbs, ctx, &launched};
-    auto part_lo = [&](int k) { return (int)((long long)n * k / kSolveParts); };
+    // part boundaries at (k / parts)^2 of the batch: the first part (the largest windows, whose solves
+    // are the longest) is small, so the device starts on it early; later parts grow while the device
+    // is busy (4 parts: 1/16, 3/16, 5/16, 7/16)
+    auto part_lo = [&](int k) { return (int)((long long)n * k * k / (kSolveParts * kSolveParts)); };
     double t_build = 0.0;
+    // NAVBA_VERBOSE: the device timeline of the parts (upload start, kernel start and end per part)
+    const char* verbose = getenv("NAVBA_VERBOSE");
+    const bool timeline = verbose && verbose[0] == '1';
+    cudaEvent_t tev[1 + 3 * kSolveParts] = {};
+    if (timeline) {
+        for (auto& ev : tev) cudaEventCreate(&ev);
+        cudaEventRecord(tev[0], ctx->parts[0].stream);
+    }
     for (int k = 0; k < kSolveParts; ++k) {
         const int lo = part_lo(k), hi = part_lo(k + 1);
         auto& part = ctx->parts[k];
@@ -461,10 +474,16 @@ nav_ba_status solve_pipelined(nav_ba_ctx* ctx, const nav_ba_problem* probs, int 
         t_build += ms_since(tb);
         if (st != NAV_BA_OK) return st;
         std::string why;
-        cudaError_t e = window_batch_upload(pbs[k], part.stream, o->precision, o->iterations + 1, part.stg, ctx->stg.pool, &why);
+        if (timeline) cudaEventRecord(tev[1 + 3 * k], part.stream);
+        // no wait for the copies: each part stages into its own pinned buffers, and every part's
+        // stream is synchronized before the results are read (or on an error return)
+        cudaError_t e = window_batch_upload(pbs[k], part.stream, o->precision, o->iterations + 1, part.stg, ctx->stg.pool,
+                                            &why, false);
         if (e != cudaSuccess) return cuda_status(ctx, e, "upload");
+        if (timeline) cudaEventRecord(tev[2 + 3 * k], part.stream);
         e = window_batch_launch(pbs[k], part.stream, o->precision, ctx->shape[o->precision], -1.0);
         if (e != cudaSuccess) return cuda_status(ctx, e, "window kernel");
+        if (timeline) cudaEventRecord(tev[3 + 3 * k], part.stream);
         launched = k + 1;
     }
     const double t_setup = ms_since(t0);
@@ -493,11 +512,20 @@ nav_ba_status solve_pipelined(nav_ba_ctx* ctx, const nav_ba_problem* probs, int 
         }
     }
     const double t_down = ms_since(t1);
-    const char* verbose = getenv("NAVBA_VERBOSE");
-    if (verbose && verbose[0] == '1')
+    if (timeline) {
         fprintf(stderr, "[navba host] %d problems in %d parts: build %.2f ms, setup (checks, build, stage, upload, "
                 "launch; device already running) %.2f ms, wait %.2f ms, download %.2f ms\n", n, kSolveParts, t_build,
                 t_setup, t_solve, t_down);
+        for (int k = 0; k < launched; ++k) {
+            float u = 0.f, ks = 0.f, ke = 0.f;
+            cudaEventElapsedTime(&u, tev[0], tev[1 + 3 * k]);
+            cudaEventElapsedTime(&ks, tev[0], tev[2 + 3 * k]);
+            cudaEventElapsedTime(&ke, tev[0], tev[3 + 3 * k]);
+            fprintf(stderr, "[navba host]   part %d (%d windows): upload from %.2f ms, kernel %.2f -> %.2f ms\n", k,
+                    part_lo(k + 1) - part_lo(k), u, ks, ke);
+        }
+        for (auto& ev : tev) cudaEventDestroy(ev);
+    }
     // byte counts of the whole call (each part's download reported its own)
     int64_t h2d = 0, d2h = 0;
     for (int k = 0; k < kSolveParts; ++k) {

@@ -1250,7 +1250,7 @@ void parallel_for(HostPool& pool, int n, Fn fn) {
 }  // namespace
 
 cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int precision, int trace_stride,
-                                HostStaging& stg, HostPool& pool, std::string* why) {
+                                HostStaging& stg, HostPool& pool, std::string* why, bool sync) {
     WindowBatch& b = pb.dev;
     std::vector<int32_t> idx;
     for (size_t i = 0; i < pb.host.size(); ++i)
@@ -1403,7 +1403,7 @@ cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int prec
     up(b.d_edge_fc, edge_fc, sizeof(int32_t) * ne);
     up(b.d_edge_pt, edge_pt, sizeof(int32_t) * ne);
     up(b.d_edge_uv, uv, sizeof(double) * 2 * ne);
-    if (err == cudaSuccess) err = cudaStreamSynchronize(stream);
+    if (err == cudaSuccess && sync) err = cudaStreamSynchronize(stream);
     b.n_queue = (int32_t)order.size();
     if (err != cudaSuccess && why) *why = cudaGetErrorString(err);
     return err;
