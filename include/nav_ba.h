@@ -132,8 +132,10 @@ typedef struct nav_ba_result {
     double time_setup_ms;         /* host-side structure build and upload (batches of >= 64
                                      windows: until the last part is launched, the device
                                      already solving the earlier parts)                     */
-    double time_solve_ms;         /* device LM loop (pipelined batches: the wait after setup) */
-    double time_download_ms;
+    double time_solve_ms;         /* device LM loop (pipelined batches: the waits for the
+                                     parts' streams after setup)                            */
+    double time_download_ms;      /* results to the caller (pipelined batches: each part
+                                     read back while the later parts still run)             */
     int32_t iterations_done;
     int32_t trials_accepted;
     int32_t trials_rejected;

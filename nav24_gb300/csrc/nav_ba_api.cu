@@ -487,13 +487,6 @@ nav_ba_status solve_pipelined(nav_ba_ctx* ctx, const nav_ba_problem* probs, int 
         launched = k + 1;
     }
     const double t_setup = ms_since(t0);
-    cudaError_t e = cudaSuccess;
-    for (int k = 0; k < kSolveParts; ++k) {
-        const cudaError_t ek = cudaStreamSynchronize(ctx->parts[k].stream);
-        if (e == cudaSuccess) e = ek;
-    }
-    if (e != cudaSuccess) return cuda_status(ctx, e, "window kernel");
-    const double t_solve = ms_since(t0) - t_setup;
     const auto t1 = std::chrono::steady_clock::now();
     // results in the parts' (size) order, then back to the caller's order
     std::vector<nav_ba_result> tp(n);
@@ -501,8 +494,15 @@ nav_ba_status solve_pipelined(nav_ba_ctx* ctx, const nav_ba_problem* probs, int 
         tp[j] = results[perm[j]];
         clear_stats(&tp[j]);
     }
+    // each part is read back as soon as its own stream is done (the parts end in order: the first
+    // holds the largest windows but started first), overlapping the later parts' kernels
+    double t_solve = 0.0;
     for (int k = 0; k < kSolveParts; ++k) {
         const int lo = part_lo(k), hi = part_lo(k + 1);
+        const auto tw = std::chrono::steady_clock::now();
+        cudaError_t e = cudaStreamSynchronize(ctx->parts[k].stream);
+        t_solve += ms_since(tw);
+        if (e != cudaSuccess) return cuda_status(ctx, e, "window kernel");
         st = download_batch(ctx, pp.data() + lo, hi - lo, pbs[k], tp.data() + lo, &ctx->parts[k].stg, ctx->parts[k].stream);
         if (st != NAV_BA_OK && st != NAV_BA_EMPTY) return set_err(ctx, st, "a problem has a non-finite initial cost");
         for (int j = lo; j < hi; ++j) {
@@ -511,7 +511,7 @@ nav_ba_status solve_pipelined(nav_ba_ctx* ctx, const nav_ba_problem* probs, int 
             if (st != NAV_BA_OK) return st;
         }
     }
-    const double t_down = ms_since(t1);
+    const double t_down = ms_since(t1) - t_solve;
     if (timeline) {
         fprintf(stderr, "[navba host] %d problems in %d parts: build %.2f ms, setup (checks, build, stage, upload, "
                 "launch; device already running) %.2f ms, wait %.2f ms, download %.2f ms\n", n, kSolveParts, t_build,

@@ -1247,6 +1247,24 @@ void parallel_for(HostPool& pool, int n, Fn fn) {
     });
 }
 
+// Per-edge arrays derived on the device from what is uploaded (8 of the 36 bytes an observation
+// would otherwise take on the bus): the window-local point of each edge (edges are point-major,
+// pt_eoff holds the global offsets) and its free-camera index.  Block per window, thread per point.
+__global__ void k_edge_derive(const WinDesc* win, int nw, const int32_t* pt_eoff, const int32_t* edge_cam,
+                              const int32_t* cam_free, int32_t* edge_pt, int32_t* edge_fc) {
+    for (int w = blockIdx.x; w < nw; w += gridDim.x) {
+        const WinDesc d = win[w];
+        for (int k = threadIdx.x; k < d.npt; k += blockDim.x) {
+            const int e0 = pt_eoff[d.pt0 + k];
+            const int e1 = k + 1 < d.npt ? pt_eoff[d.pt0 + k + 1] : d.e0 + d.ne;
+            for (int e = e0; e < e1; ++e) {
+                edge_pt[e] = k;
+                edge_fc[e] = cam_free[d.cam0 + edge_cam[e]];
+            }
+        }
+    }
+}
+
 }  // namespace
 
 cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int precision, int trace_stride,
@@ -1361,12 +1379,10 @@ cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int prec
     int32_t* pt_free = (int32_t*)stg.get(3, sizeof(int32_t) * np);
     int32_t* pt_eoff = (int32_t*)stg.get(4, sizeof(int32_t) * (np + 1));
     int32_t* edge_cam = (int32_t*)stg.get(5, sizeof(int32_t) * ne);
-    int32_t* edge_fc = (int32_t*)stg.get(14, sizeof(int32_t) * ne);
-    int32_t* edge_pt = (int32_t*)stg.get(6, sizeof(int32_t) * ne);
     double* uv = (double*)stg.get(7, sizeof(double) * 2 * ne);
     WinDesc* desc = (WinDesc*)stg.get(8, sizeof(WinDesc) * nw);
     int32_t* ord = (int32_t*)stg.get(9, sizeof(int32_t) * order.size());
-    if (!cam || !cam_free || !pt || !pt_free || !pt_eoff || !edge_cam || !edge_fc || !edge_pt || !uv || !desc || !ord) {
+    if (!cam || !cam_free || !pt || !pt_free || !pt_eoff || !edge_cam || !uv || !desc || !ord) {
         if (why) *why = "pinned host allocation failed";
         return cudaErrorMemoryAllocation;
     }
@@ -1381,8 +1397,6 @@ cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int prec
         std::copy(h.pt.begin(), h.pt.end(), pt + 4LL * d.pt0);
         for (int k = 0; k < h.npt; ++k) pt_eoff[d.pt0 + k] = d.e0 + h.pt_eoff[k];
         std::copy(h.edge_cam.begin(), h.edge_cam.end(), edge_cam + d.e0);
-        for (int k = 0; k < h.ne; ++k) edge_fc[d.e0 + k] = h.cam_free[h.edge_cam[k]];
-        std::copy(h.edge_pt.begin(), h.edge_pt.end(), edge_pt + d.e0);
         std::copy(h.edge_uv.begin(), h.edge_uv.end(), uv + 2LL * d.e0);
     });
     pt_eoff[np] = (int32_t)ne;
@@ -1400,9 +1414,12 @@ cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int prec
     up(b.d_pt_free, pt_free, sizeof(int32_t) * np);
     up(b.d_pt_eoff, pt_eoff, sizeof(int32_t) * (np + 1));
     up(b.d_edge_cam, edge_cam, sizeof(int32_t) * ne);
-    up(b.d_edge_fc, edge_fc, sizeof(int32_t) * ne);
-    up(b.d_edge_pt, edge_pt, sizeof(int32_t) * ne);
     up(b.d_edge_uv, uv, sizeof(double) * 2 * ne);
+    if (err == cudaSuccess && nw > 0) {
+        k_edge_derive<<<(int)std::min<size_t>(nw, 4096), 128, 0, stream>>>(b.d_win, (int)nw, b.d_pt_eoff, b.d_edge_cam,
+                                                                          b.d_cam_free, b.d_edge_pt, b.d_edge_fc);
+        err = cudaGetLastError();
+    }
     if (err == cudaSuccess && sync) err = cudaStreamSynchronize(stream);
     b.n_queue = (int32_t)order.size();
     if (err != cudaSuccess && why) *why = cudaGetErrorString(err);
