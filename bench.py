@@ -51,7 +51,8 @@ def parse():
     ap.add_argument("--workload", choices=["windows"], default="windows")
     ap.add_argument("--windows", type=int, default=512)
     ap.add_argument("--cpu-sample", type=int, default=512, help="windows in the CPU baseline sample")
-    ap.add_argument("--profile-case", choices=["mixed", "fp64", "grid", "pcg", "vjp", "pose"], default=None,
+    ap.add_argument("--profile-case", choices=["mixed", "fp64", "grid", "pcg", "vjp", "pose", "twoview", "undistort"],
+                    default=None,
                     help="run only the device-resident solves of one precision (mixed, fp64), or one solve of a "
                          "secondary workload (for profiler captures)")
     ap.add_argument("--no-secondary", action="store_true", help="skip the secondary workloads")
@@ -275,6 +276,46 @@ def solve_pair(ctx, p, family, precisions=("fp64", "mixed")):
     return out
 
 
+def twoview_workload(ctx):
+    """nav_ba_twoview_check on synthetic matches: one frame pair at a typical match count, and a
+    large batch of matches for throughput."""
+    K = np.array([500.0, 500.0, 320.0, 240.0])
+    res = {}
+    for n in (2000, 1 << 18):
+        rng = np.random.default_rng(1006)
+        rv = np.array([0.02, -0.06, 0.01])
+        th = np.linalg.norm(rv)
+        kx = np.array([[0, -rv[2], rv[1]], [rv[2], 0, -rv[0]], [-rv[1], rv[0], 0]]) / th
+        R = np.eye(3) + np.sin(th) * kx + (1 - np.cos(th)) * kx @ kx
+        t = np.array([-0.3, 0.02, 0.01])
+        X = np.stack([rng.uniform(-2, 2, n), rng.uniform(-1.5, 1.5, n), rng.uniform(2, 8, n)], axis=1)
+        proj = lambda P: np.stack([K[0] * P[:, 0] / P[:, 2] + K[2], K[1] * P[:, 1] / P[:, 2] + K[3]], axis=1)
+        kp1 = proj(X) + 0.5 * rng.standard_normal((n, 2))
+        kp2 = proj(X @ R.T + t) + 0.5 * rng.standard_normal((n, 2))
+        bad = rng.random(n) < 0.1
+        kp2[bad] = np.stack([rng.uniform(0, 640, bad.sum()), rng.uniform(0, 480, bad.sum())], axis=1)
+        u = t / np.linalg.norm(t)
+        ux = np.array([[0, -u[2], u[1]], [u[2], 0, -u[0]], [-u[1], u[0], 0]])
+        tw = np.eye(3) + 2 * ux @ ux  # rotation by pi about t
+        Rs = np.stack([R, R, tw @ R, tw @ R])
+        ts_ = np.stack([t, -t, t, -t])
+        th2 = 4.0  # 4 sigma^2 with sigma = 1 px, as the reconstruction's CheckRT calls it
+        ctx.twoview_check(K, kp1, kp2, Rs, ts_, th2, 0.99998)
+        ts = []
+        for _ in range(5):
+            t0 = time.perf_counter()
+            r = ctx.twoview_check(K, kp1, kp2, Rs, ts_, th2, 0.99998)
+            ts.append(time.perf_counter() - t0)
+        dt = float(np.median(ts))
+        res[f"{n}_matches"] = {"hypotheses": 4, "matches": n, "ms": dt * 1e3, "checks_per_s": 4 * n / dt,
+                               "n_good": [int(v) for v in r["n_good"]]}
+    res["workload"] = ("4 relative-pose hypotheses x matches of one frame pair (0.3 m baseline, points 2-8 m, "
+                       "0.5 px noise, 10% outliers); per match: linear triangulation (4x4 SVD), cheirality, "
+                       "reprojection gates, parallax")
+    res["timing"] = "median wall clock of 5 C-ABI calls with host buffers (copies in, kernel, copies out)"
+    return res
+
+
 def secondary_workloads(ctx, only=None, pcg_cams=1000, pcg_points=500000, precisions=("fp64", "mixed")):
     """One solve of each other named workload (device time, including the per-solve upload)."""
     from nav24_gb300 import abi
@@ -315,6 +356,30 @@ def secondary_workloads(ctx, only=None, pcg_cams=1000, pcg_points=500000, precis
             "observations": nobs, "ms": dt * 1e3, "frames_per_s": len(probs) / dt,
             "obs_per_s": sum(p.obs_uv.shape[0] * st["iterations_done"] for p, (_, st) in zip(probs, res)) / dt,
             "lm_iterations": its, "timing": "wall clock of the C-ABI call (host layout, upload, kernel, download)"}
+    if only in (None, "undistort"):
+        # keypoints over a VGA image with a typical radial-tangential calibration, 5 fixed-point
+        # iterations (cv::undistortPoints' default count as nav24 calls it)
+        K = np.array([458.654, 457.296, 367.215, 248.375])
+        D = np.array([-0.28340811, 0.07395907, 0.00019359, 1.76187114e-05])
+        rng = np.random.default_rng(1005)
+        n = 1 << 21
+        uv = np.stack([rng.uniform(0, 752, n), rng.uniform(0, 480, n)], axis=1)
+        ctx.undistort_points(K, D, uv[:4096])
+        ts = []
+        for _ in range(5):
+            t0 = time.perf_counter()
+            ctx.undistort_points(K, D, uv)
+            ts.append(time.perf_counter() - t0)
+        dt = float(np.median(ts))
+        out["undistort_keypoints"] = {
+            "workload": f"{n} keypoints uniform over a 752x480 image, radial-tangential (k1, k2, p1, p2), 5 "
+                        "iterations, FP64", "keypoints": n, "ms": dt * 1e3, "keypoints_per_s": n / dt,
+            "h2d_bytes": 16 * n, "d2h_bytes": 16 * n,
+            "timing": "median wall clock of 5 C-ABI calls with host buffers (copies in, kernel, copies out)"}
+    if only in (None, "twoview"):
+        # map-initialization triangulation: 4 relative-pose hypotheses x matches of one frame pair,
+        # points 2-8 m ahead of a 0.3 m baseline, 0.5 px noise, 10% outlier matches
+        out["twoview_triangulation"] = twoview_workload(ctx)
     if only in (None, "pcg"):
         p = Synth(4, n_cams=pcg_cams, n_points=pcg_points).window(0)
         out["figure_eight_pcg"] = {
@@ -343,7 +408,7 @@ def main():
     om = workload_options(2, abi.MIXED)
     of = workload_options(2, abi.FP64)
 
-    if args.profile_case in ("grid", "pcg", "vjp", "pose"):
+    if args.profile_case in ("grid", "pcg", "vjp", "pose", "twoview", "undistort"):
         precs = ("fp64", "mixed") if args.profile_precision == "both" else (args.profile_precision,)
         print(json.dumps(secondary_workloads(ctx, args.profile_case, args.pcg_cams, args.pcg_points, precs)), flush=True)
         ctx.close()

@@ -4,11 +4,13 @@
 // TwoViewReconstruction::Triangulate (core/operators/mapInit/OP_2ViewReconstruction.cpp:1179-1193)
 // takes the right singular vector of the 4x4 DLT matrix A for its smallest singular value; here it
 // comes from a one-sided Jacobi SVD of the same A, in FP64 (the reference: cv::SVD on CV_32F).
+// The per-match host work (nGood, the k-th smallest parallax cosine) is linear in the matches.
 // The checks follow TwoViewReconstruction::CheckRT (:1244-1353) in order.  The reductions CheckRT
 // makes over matches (nGood, the parallax statistic) are formed on the host from the flags.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -31,6 +33,32 @@ struct TvArgs {
     double* cosp;    // [nh][n]
 };
 
+// FP64 reciprocal and reciprocal square root for the rotation parameters, by Newton-Raphson from
+// the FP32 estimate: x <- x (2 - z x) and r <- r (3 - y r^2) / 2 converge quadratically, so the
+// estimate's ~2^-22 relative error falls below an FP64 ulp in two steps.  Outside the FP32 range the
+// IEEE operations are used.  (GB300 issues FP64 at 2 lanes per clock per SM; the IEEE divide and
+// square root are long sequences, and the rotations are this kernel's FP64 work.)
+__device__ __forceinline__ double recip_nr(double z) {
+    const double az = fabs(z);
+    if (az > 1e-30 && az < 1e30) {
+        double x = (double)(1.0f / (float)z);
+        x = fma(x, fma(-z, x, 1.0), x);
+        x = fma(x, fma(-z, x, 1.0), x);
+        return x;
+    }
+    return 1.0 / z;
+}
+
+__device__ __forceinline__ double rsqrt_nr(double y) {
+    if (y > 1e-30 && y < 1e30) {
+        double r = (double)rsqrtf((float)y);
+        r = r * fma(-0.5 * y * r, r, 1.5);
+        r = r * fma(-0.5 * y * r, r, 1.5);
+        return r;
+    }
+    return 1.0 / sqrt(y);
+}
+
 // Right singular vector of a 4x4 matrix for its smallest singular value: one-sided Jacobi
 // (Hestenes 1958): column pairs of A are rotated until mutually orthogonal, the rotations
 // accumulate in V, and the column of V belonging to the shortest column of A is the vector.
@@ -47,11 +75,20 @@ __device__ void svd4_min_right(double A[4][4], double v[4]) {
                     be += A[k][q] * A[k][q];
                     ga += A[k][p] * A[k][q];
                 }
-                if (!(fabs(ga) > 1e-15 * sqrt(al * be))) continue;
+                if (!(ga * ga > 1e-30 * (al * be))) continue;  // |ga| > 1e-15 sqrt(al be)
                 rotated = true;
-                const double ze = (be - al) / (2.0 * ga);
-                const double tt = (ze >= 0 ? 1.0 : -1.0) / (fabs(ze) + sqrt(1.0 + ze * ze));
-                const double c = 1.0 / sqrt(1.0 + tt * tt), s = c * tt;
+                // tan of the rotation angle: sign(ze) / (|ze| + sqrt(1 + ze^2)), or 1 / (2 ze) once
+                // sqrt(1 + ze^2) = |ze| in FP64
+                const double ze = (be - al) * recip_nr(2.0 * ga);
+                const double aze = fabs(ze);
+                double tt;
+                if (aze < 1e15) {
+                    const double y = 1.0 + ze * ze;
+                    tt = (ze >= 0 ? 1.0 : -1.0) * recip_nr(aze + y * rsqrt_nr(y));
+                } else {
+                    tt = 0.5 * recip_nr(ze);
+                }
+                const double c = rsqrt_nr(1.0 + tt * tt), s = c * tt;
                 for (int k = 0; k < 4; ++k) {
                     const double a = A[k][p], b = A[k][q];
                     A[k][p] = c * a - s * b;
@@ -151,8 +188,12 @@ nav_ba_status twoview_check(cudaStream_t st, const nav_ba_twoview& in, nav_ba_tw
         return NAV_BA_ERR_NONFINITE_INPUT;
     }
     const int64_t m = (int64_t)n * nh;
-    std::vector<double> pts(3 * std::max<int64_t>(m, 1)), cosp(std::max<int64_t>(m, 1));
-    std::vector<uint8_t> flags(std::max<int64_t>(m, 1));
+    // host copies of the per-pair outputs (default-initialized: every entry is read back); the
+    // points go straight to the caller's buffer when it gives one
+    std::unique_ptr<double[]> pts_own(out.points ? nullptr : new double[3 * std::max<int64_t>(m, 1)]);
+    double* pts = out.points ? out.points : pts_own.get();
+    std::unique_ptr<double[]> cosp(new double[std::max<int64_t>(m, 1)]);
+    std::unique_ptr<uint8_t[]> flags(new uint8_t[std::max<int64_t>(m, 1)]);
     if (m > 0) {
         void* buf = nullptr;
         const size_t b_kp = sizeof(double) * 2 * n, b_in = in.inlier ? (size_t)n : 0, b_R = sizeof(double) * 9 * nh,
@@ -193,9 +234,9 @@ nav_ba_status twoview_check(cudaStream_t st, const nav_ba_twoview& in, nav_ba_tw
             k_twoview<<<(unsigned)((m + 127) / 128), 128, 0, st>>>(A);
             e = cudaGetLastError();
         }
-        if (e == cudaSuccess) e = cudaMemcpyAsync(pts.data(), A.pts, b_pts, cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(cosp.data(), A.cosp, b_cos, cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(flags.data(), A.flags, b_fl, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(pts, A.pts, b_pts, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(cosp.get(), A.cosp, b_cos, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(flags.get(), A.flags, b_fl, cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (buf) cudaFree(buf);
         if (e != cudaSuccess) {
@@ -203,20 +244,21 @@ nav_ba_status twoview_check(cudaStream_t st, const nav_ba_twoview& in, nav_ba_tw
             return NAV_BA_ERR_CUDA;
         }
     }
+    std::vector<double> cs;
     for (int h = 0; h < nh; ++h) {
-        std::vector<double> cs;
+        cs.clear();
         for (int i = 0; i < n; ++i)
             if (flags[(size_t)h * n + i] & 1) cs.push_back(cosp[(size_t)h * n + i]);
         out.n_good[h] = (int32_t)cs.size();
         if (cs.empty()) {
             out.parallax_deg[h] = 0.0;
         } else {
-            std::sort(cs.begin(), cs.end());
+            // the k-th smallest cosine, the element CheckRT reads after sorting them all
             const size_t k = std::min<size_t>((size_t)std::max(0, in.min_triangulated), cs.size() - 1);
+            std::nth_element(cs.begin(), cs.begin() + k, cs.end());
             out.parallax_deg[h] = std::acos(cs[k]) * 180.0 / M_PI;
         }
     }
-    if (out.points && m > 0) std::memcpy(out.points, pts.data(), sizeof(double) * 3 * m);
     for (int64_t k = 0; k < m; ++k) {
         if (out.triangulated) out.triangulated[k] = flags[k] & 1;
         if (out.good) out.good[k] = (flags[k] >> 1) & 1;
