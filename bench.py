@@ -51,7 +51,8 @@ def parse():
     ap.add_argument("--workload", choices=["windows"], default="windows")
     ap.add_argument("--windows", type=int, default=512)
     ap.add_argument("--cpu-sample", type=int, default=512, help="windows in the CPU baseline sample")
-    ap.add_argument("--profile-case", choices=["mixed", "fp64", "grid", "pcg", "vjp", "pose", "twoview", "undistort"],
+    ap.add_argument("--profile-case", choices=["mixed", "fp64", "grid", "pcg", "vjp", "pose", "twoview", "undistort",
+                                               "kb8"],
                     default=None,
                     help="run only the device-resident solves of one precision (mixed, fp64), or one solve of a "
                          "secondary workload (for profiler captures)")
@@ -316,6 +317,62 @@ def twoview_workload(ctx):
     return res
 
 
+KB8_INTR = np.array([380.0, 380.0, 320.0, 240.0, -0.012, 0.0025, -0.0006, 0.00008])
+
+
+def kb8_windows(n_windows, seed=1002, noise=1.0):
+    """The batched-window family's windows with their observations made through the Kannala-Brandt
+    fisheye model (theta = atan2(rho, z), r = theta + k1 theta^3 + ... + k4 theta^9) from the true
+    geometry, 1 px noise; the pinhole originals alongside."""
+    from nav24_gb300 import abi
+    from nav24_gb300.synth import Synth
+    s = Synth(2, seed=seed, n_windows=n_windows)
+    rng = np.random.default_rng(seed + 5)
+    kb, ph = [], []
+    k = KB8_INTR
+    for w in range(n_windows):
+        truth, init = s.window(w, truth=True), s.window(w)
+        P = truth.cam_pose.reshape(-1, 3, 4)
+        Xc = np.einsum("nij,nj->ni", P[truth.obs_cam, :, :3], truth.points[truth.obs_point]) + P[truth.obs_cam, :, 3]
+        th = np.arctan2(np.hypot(Xc[:, 0], Xc[:, 1]), Xc[:, 2])
+        psi = np.arctan2(Xc[:, 1], Xc[:, 0])
+        r = th + k[4] * th ** 3 + k[5] * th ** 5 + k[6] * th ** 7 + k[7] * th ** 9
+        uv = np.stack([k[0] * r * np.cos(psi) + k[2], k[1] * r * np.sin(psi) + k[3]], axis=1)
+        q = init.copy()
+        q.obs_uv = np.ascontiguousarray(uv + noise * rng.standard_normal(uv.shape))
+        q.intrinsics = k.copy()
+        q.camera_model = abi.CAM_KANNALA_BRANDT8
+        kb.append(q)
+        ph.append(init)
+    return kb, ph
+
+
+def kb8_workload(ctx, n_windows=128):
+    from nav24_gb300 import abi
+    from nav24_gb300.synth import workload_options
+    kb, ph = kb8_windows(n_windows)
+    res = {"workload": f"{n_windows} windows of the batched family observed through the Kannala-Brandt 8 "
+                       "model (1 px noise), 10 LM iterations, one batched call; the same windows with "
+                       "their pinhole observations alongside",
+           "timing": "median wall clock of 3 nav_ba_solve_batched calls with host buffers; device_ms = "
+                     "the calls' time_solve_ms"}
+    for model, probs in (("kb8", kb), ("pinhole", ph)):
+        for name, prec in (("fp64", abi.FP64), ("mixed", abi.MIXED)):
+            o = workload_options(2, prec)
+            ctx.solve_batched(probs, o)
+            ts, rr = [], None
+            for _ in range(3):
+                t0 = time.perf_counter()
+                rr = ctx.solve_batched(probs, o)
+                ts.append(time.perf_counter() - t0)
+            dt = float(np.median(ts))
+            ei = sum(r.stats["edge_iterations"] for r in rr)
+            res[f"{model}_{name}"] = {"ms": dt * 1e3, "obs_per_s": ei / dt, "device_ms": rr[0].stats["time_solve_ms"],
+                                      "final_cost_sum": float(sum(r.stats["final_cost"] for r in rr)),
+                                      "status_ok": int(sum(r.status == abi.OK for r in rr))}
+    return res
+
+
 def secondary_workloads(ctx, only=None, pcg_cams=1000, pcg_points=500000, precisions=("fp64", "mixed")):
     """One solve of each other named workload (device time, including the per-solve upload)."""
     from nav24_gb300 import abi
@@ -376,6 +433,8 @@ def secondary_workloads(ctx, only=None, pcg_cams=1000, pcg_points=500000, precis
                         "iterations, FP64", "keypoints": n, "ms": dt * 1e3, "keypoints_per_s": n / dt,
             "h2d_bytes": 16 * n, "d2h_bytes": 16 * n,
             "timing": "median wall clock of 5 C-ABI calls with host buffers (copies in, kernel, copies out)"}
+    if only in (None, "kb8"):
+        out["kb8_windows"] = kb8_workload(ctx)
     if only in (None, "twoview"):
         # map-initialization triangulation: 4 relative-pose hypotheses x matches of one frame pair,
         # points 2-8 m ahead of a 0.3 m baseline, 0.5 px noise, 10% outlier matches
@@ -408,7 +467,7 @@ def main():
     om = workload_options(2, abi.MIXED)
     of = workload_options(2, abi.FP64)
 
-    if args.profile_case in ("grid", "pcg", "vjp", "pose", "twoview", "undistort"):
+    if args.profile_case in ("grid", "pcg", "vjp", "pose", "twoview", "undistort", "kb8"):
         precs = ("fp64", "mixed") if args.profile_precision == "both" else (args.profile_precision,)
         print(json.dumps(secondary_workloads(ctx, args.profile_case, args.pcg_cams, args.pcg_points, precs)), flush=True)
         ctx.close()
