@@ -269,6 +269,11 @@ class Context:
         that repeated calls time the C ABI alone."""
         return BatchedCall(self, probs, opt)
 
+    def pose_call(self, probs: list[abi.PoseProblem], opt: abi.nav_ba_options) -> "PoseCall":
+        """A nav_ba_solve_pose_batched call with its C structs and host output buffers built once,
+        so that repeated calls time the C ABI alone."""
+        return PoseCall(self, probs, opt)
+
     def prepare(self, prob: abi.Problem, opt: abi.nav_ba_options):
         self._prepared = prob  # keep the arrays alive
         p = prob.as_c()
@@ -348,3 +353,23 @@ class BatchedCall:
             b.c = r
             out.append(b.result(r.status))
         return out
+
+
+class PoseCall:
+    def __init__(self, ctx: Context, probs: list[abi.PoseProblem], opt: abi.nav_ba_options):
+        self.ctx, self.probs, self.opt = ctx, probs, opt
+        n = len(probs)
+        self.n = n
+        self.cp = (abi.nav_ba_pose_problem * max(n, 1))(*[p.as_c() for p in probs])
+        self.outs = [np.zeros(12) for _ in probs]
+        self.cr = (abi.nav_ba_pose_result * max(n, 1))()
+        for i in range(n):
+            self.cr[i].pose_out = _d(self.outs[i])
+
+    def __call__(self) -> int:
+        return self.ctx._check(self.ctx.L.nav_ba_solve_pose_batched(self.ctx.h, self.cp, self.n, C.byref(self.opt),
+                                                                    self.cr))
+
+    def results(self):
+        return [(self.outs[i], {f: getattr(self.cr[i], f) for f, _ in abi.nav_ba_pose_result._fields_
+                                if f != "pose_out"}) for i in range(self.n)]

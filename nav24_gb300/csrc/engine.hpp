@@ -207,8 +207,10 @@ struct PoseBatch {
     size_t cap[6] = {};
     void release();
 };
+// stg: pinned staging and host workers (the call is synchronous on return)
 nav_ba_status solve_pose_batch(cudaStream_t stream, PoseBatch& B, const nav_ba_pose_problem* probs, int n,
-                               const nav_ba_options& o, nav_ba_pose_result* res, float* ms, std::string* why);
+                               const nav_ba_options& o, nav_ba_pose_result* res, float* ms, std::string* why,
+                               HostStaging& stg);
 
 // Two-view triangulation and hypothesis checks (twoview.cu).
 nav_ba_status twoview_check(cudaStream_t stream, const nav_ba_twoview& in, nav_ba_twoview_result& out, std::string* why);

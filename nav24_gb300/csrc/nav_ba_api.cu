@@ -909,12 +909,16 @@ nav_ba_status nav_ba_solve_pose_batched(nav_ba_ctx* ctx, const nav_ba_pose_probl
     if (st != NAV_BA_OK) return set_err(ctx, st, why);
     if (o->solver != NAV_BA_SOLVER_CHOLESKY || o->optimize_distortion)
         return set_err(ctx, NAV_BA_ERR_UNSUPPORTED, "motion-only BA solves its 6x6 system by Cholesky, without distortion");
+    const auto t0 = std::chrono::steady_clock::now();
     std::vector<nav_ba_pose_result> tmp(results, results + n);  // outputs untouched on error
     float ms = 0.f;
-    st = solve_pose_batch(ctx->stream, ctx->pose, probs, n, *o, tmp.data(), &ms, &why);
+    st = solve_pose_batch(ctx->stream, ctx->pose, probs, n, *o, tmp.data(), &ms, &why, ctx->stg);
     if (st != NAV_BA_OK) return set_err(ctx, st, why);
     for (int i = 0; i < n; ++i) results[i] = tmp[i];
-    (void)ms;
+    const char* verbose = getenv("NAVBA_VERBOSE");
+    if (verbose && verbose[0] == '1')
+        fprintf(stderr, "[navba pose] %d problems: kernel %.3f ms, call %.3f ms\n", n, ms,
+                std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
     return NAV_BA_OK;
 }
 

@@ -223,25 +223,41 @@ void PoseBatch::release() {
 }
 
 nav_ba_status solve_pose_batch(cudaStream_t st, PoseBatch& B, const nav_ba_pose_problem* probs, int n,
-                               const nav_ba_options& o, nav_ba_pose_result* res, float* ms, std::string* why) {
-    // validation (nothing is written on error)
-    for (int i = 0; i < n; ++i) {
+                               const nav_ba_options& o, nav_ba_pose_result* res, float* ms, std::string* why,
+                               HostStaging& stg) {
+    // validation of every problem on the host workers (nothing is written on error; the lowest
+    // failing index is reported, as a sequential pass would)
+    auto check = [&](int i, std::string* w) -> nav_ba_status {
         const nav_ba_pose_problem& p = probs[i];
-        const std::string at = "pose problem " + std::to_string(i) + ": ";
+        auto at = [i]() { return "pose problem " + std::to_string(i) + ": "; };
         if (p.n_obs < 0 || !p.pose || (p.n_obs > 0 && (!p.points || !p.obs_uv))) {
-            *why = at + "NULL array or negative size";
+            *w = at() + "NULL array or negative size";
             return NAV_BA_ERR_ARGUMENT;
         }
         if (p.camera_model != NAV_BA_CAM_PINHOLE && p.camera_model != NAV_BA_CAM_PINHOLE_RADIAL &&
             p.camera_model != NAV_BA_CAM_KANNALA_BRANDT8) {
-            *why = at + "unknown camera model";
+            *w = at() + "unknown camera model";
             return NAV_BA_ERR_ARGUMENT;
         }
         if (!finite_all(p.pose, 12) || !finite_all(p.intrinsics, 8) || !finite_all(p.points, 3LL * p.n_obs) ||
             !finite_all(p.obs_uv, 2LL * p.n_obs)) {
-            *why = at + "non-finite input";
+            *w = at() + "non-finite input";
             return NAV_BA_ERR_NONFINITE_INPUT;
         }
+        return NAV_BA_OK;
+    };
+    {
+        std::vector<nav_ba_status> vst(n, NAV_BA_OK);
+        std::vector<std::string> vwhy(n);
+        const int nth = HostPool::tasks_for(n, 16);
+        stg.pool.run(nth, [&](int t) {
+            for (int i = t; i < n; i += nth) vst[i] = check(i, &vwhy[i]);
+        });
+        for (int i = 0; i < n; ++i)
+            if (vst[i] != NAV_BA_OK) {
+                *why = vwhy[i];
+                return vst[i];
+            }
     }
     // host layout: descriptors, camera states, points [no][4], measurements [no][2]
     std::vector<PoseDesc> desc;
@@ -263,15 +279,32 @@ nav_ba_status solve_pose_batch(cudaStream_t st, PoseBatch& B, const nav_ba_pose_
         no += probs[i].n_obs;
     }
     const int m = (int)desc.size();
-    std::vector<double> pts(4 * std::max<int64_t>(no, 1), 0.0), uv(2 * std::max<int64_t>(no, 1), 0.0);
-    for (int i = 0; i < n; ++i) {
-        if (slot[i] < 0) continue;
-        const int64_t o0 = desc[slot[i]].o0;
-        for (int64_t k = 0; k < probs[i].n_obs; ++k) {
-            for (int j = 0; j < 3; ++j) pts[4 * (o0 + k) + j] = probs[i].points[3 * k + j];
-            uv[2 * (o0 + k)] = probs[i].obs_uv[2 * k];
-            uv[2 * (o0 + k) + 1] = probs[i].obs_uv[2 * k + 1];
-        }
+    // points [no][4] and measurements [no][2] staged in pinned memory, in parallel over problems
+    const size_t b_pts = sizeof(double) * 4 * std::max<int64_t>(no, 1), b_uv = sizeof(double) * 2 * std::max<int64_t>(no, 1);
+    double* pts = static_cast<double*>(stg.get(0, b_pts));
+    double* uv = static_cast<double*>(stg.get(1, b_uv));
+    if (!pts || !uv) {
+        *why = "pinned host allocation failed";
+        return NAV_BA_ERR_CUDA;
+    }
+    {
+        const int nth = HostPool::tasks_for(n, 16);
+        stg.pool.run(nth, [&](int t) {
+            for (int i = t; i < n; i += nth) {
+                if (slot[i] < 0) continue;
+                const int64_t o0 = desc[slot[i]].o0;
+                const double* P = probs[i].points;
+                const double* Z = probs[i].obs_uv;
+                for (int64_t k = 0; k < probs[i].n_obs; ++k) {
+                    double* q = pts + 4 * (o0 + k);
+                    q[0] = P[3 * k];
+                    q[1] = P[3 * k + 1];
+                    q[2] = P[3 * k + 2];
+                    q[3] = 0.0;
+                }
+                std::memcpy(uv + 2 * o0, Z, sizeof(double) * 2 * probs[i].n_obs);
+            }
+        });
     }
     std::vector<CamState> cout(std::max(1, m));
     std::vector<PoseStat> stats(std::max(1, m));
@@ -289,16 +322,16 @@ nav_ba_status solve_pose_batch(cudaStream_t st, PoseBatch& B, const nav_ba_pose_
         ensure(&B.d_desc, B.cap[0], sizeof(PoseDesc) * m);
         ensure(&B.d_cam_in, B.cap[1], sizeof(CamState) * m);
         ensure(&B.d_cam_out, B.cap[2], sizeof(CamState) * m);
-        ensure(&B.d_pts, B.cap[3], sizeof(double) * pts.size());
-        ensure(&B.d_uv, B.cap[4], sizeof(double) * uv.size());
+        ensure(&B.d_pts, B.cap[3], b_pts);
+        ensure(&B.d_uv, B.cap[4], b_uv);
         ensure(&B.d_stats, B.cap[5], sizeof(PoseStat) * m);
         auto upl = [&](void* d, const void* h, size_t bytes) {
             if (e == cudaSuccess) e = cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, st);
         };
         upl(B.d_desc, desc.data(), sizeof(PoseDesc) * m);
         upl(B.d_cam_in, cams.data(), sizeof(CamState) * m);
-        upl(B.d_pts, pts.data(), sizeof(double) * pts.size());
-        upl(B.d_uv, uv.data(), sizeof(double) * uv.size());
+        upl(B.d_pts, pts, b_pts);
+        upl(B.d_uv, uv, b_uv);
         PoseArgs A;
         A.desc = B.d_desc;
         A.n = m;
