@@ -1,15 +1,17 @@
 // pose_engine.cu - motion-only BA (one free pose against fixed world points), many problems per
-// launch, one warp per problem.
+// launch, one block per problem.
 //
 // The edge is nav24's EdgeSE3ProjectXYZOnlyPose (core/dataTypes/optimization/OptimizableTypes.hpp:34-60,
 // OptimizableTypes.cpp:50-64): e = z - pi(T Xw) with J = -Jpi [-[Xc]x | I], the same residual and pose
 // Jacobian as the full edge with the point block dropped.  The LM control is the one of the other
 // engines (g2o OptimizationAlgorithmLevenberg::solve semantics) on the 6x6 normal equations:
-//   lanes stride over the problem's observations (structure of arrays: point [n][4], uv [n][2]);
-//   H (21 packed) and b (6) accumulate per lane in Real and are summed by a warp butterfly in FP64,
-//   so every lane holds the same system; every lane factors H + lambda I (FP64 Cholesky, in
-//   registers) and applies the same SE(3) update, so the control flow stays warp-uniform;
-//   costs are FP64 per-lane partial sums reduced the same way (fixed order: bitwise repeatable).
+//   the block's threads stride over the problem's observations (structure of arrays: point [n][4],
+//   uv [n][2]); H (21 packed) and b (6) accumulate per thread in Real and are summed in FP64 (warp
+//   butterfly, then over the warps in order); thread 0 factors H + lambda I (FP64 Cholesky, in
+//   registers), applies the SE(3) update and makes the LM decisions, which the block reads from
+//   shared memory; costs are FP64 per-thread partial sums reduced the same way (fixed order:
+//   bitwise repeatable).  A single frame is one block, not one warp: its dependent FP64 chains
+//   (one warp: IPC 0.08, fixed-latency waits) overlap over eight warps.
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -51,18 +53,20 @@ __device__ __forceinline__ void cam12(const CamState& c, Real* o) {
     o[11] = (Real)c.t[2];
 }
 
-// FP64 robust chi2 of one problem at camera state c (every lane returns the total).
-__device__ double pose_cost(const PoseArgs& A, const PoseDesc& d, const Intr& in, const CamState& c, int lane) {
+// This thread's part of the FP64 robust chi2 of one problem at camera state c (observations
+// first, first + stride, ...).
+__device__ double pose_cost(const PoseArgs& A, const PoseDesc& d, const Intr& in, const CamState& c, int first,
+                            int stride) {
     double cr[12];
     cam12<double>(c, cr);
     double acc = 0.0;
-    for (int i = lane; i < d.n; i += 32) {
+    for (int i = first; i < d.n; i += stride) {
         const long long k = d.o0 + i;
         const double X[3] = {A.pts[4 * k], A.pts[4 * k + 1], A.pts[4 * k + 2]};
         const double z[2] = {A.uv[2 * k], A.uv[2 * k + 1]};
         acc += edge_cost<double>(in, cr, cr + 9, X, z, A.lm.robust != 0, A.lm.huber_delta);
     }
-    return warp_sum(acc);
+    return acc;
 }
 
 // (H + lambda I) x = b by FP64 Cholesky of the packed lower 6x6 H; false if not positive definite.
@@ -114,28 +118,68 @@ __device__ bool chol_solve6(const double* H, double lambda, const double* b, dou
     return ok;
 }
 
+// One block of kPoseThreads threads per problem.  The observation passes (linearization, costs)
+// stride over the block's threads; their sums go warp butterfly -> lane-parallel over the warps ->
+// shared memory, in a fixed order.  Thread 0 holds the LM state and does the scalar work (6x6
+// factorization, SE(3) update, gain ratio, damping), so the FP64 pipe, shared by the SM, runs it
+// once; the trial state and the decisions reach the other threads through shared memory.  The
+// same kernel serves every batch size, so a problem's result does not depend on its batch.
+constexpr int kPoseThreads = 256;
+constexpr int kPoseWarps = kPoseThreads / 32;
+
 template <class Real>
-__global__ void __launch_bounds__(256) pose_lm_kernel(PoseArgs A) {
-    const int lane = threadIdx.x & 31;
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (w >= A.n) return;  // uniform per warp
+__global__ void __launch_bounds__(kPoseThreads) pose_lm_kernel(PoseArgs A) {
+    const int w = blockIdx.x;  // problem (uniform per block)
+    if (w >= A.n) return;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    __shared__ double s_part[kPoseWarps][28];
+    __shared__ double s_tot[28];
+    __shared__ double s_hb[28];  // H (21 packed) and b (6) of the current linearization
+    __shared__ CamState s_cam;  // the state the observation passes evaluate
+    __shared__ int s_flag[2];
     const PoseDesc d = A.desc[w];
     const Intr in = make_intr(d.intr, d.model);
     const bool robust = A.lm.robust != 0;
     const Real delta = (Real)A.lm.huber_delta;
-    CamState cur = A.cam_in[w], trial;
-    double chi = pose_cost(A, d, in, cur, lane);
+    // sum over the block of N per-thread values, returned in s_tot (read after the call)
+    auto block_sum = [&](auto& v) {
+        constexpr int nv = (int)(sizeof(v) / sizeof(v[0]));
+#pragma unroll
+        for (int k = 0; k < nv; ++k) {
+            const double t = warp_sum((double)v[k]);
+            if (lane == 0) s_part[wid][k] = t;
+        }
+        __syncthreads();
+        if (tid < nv) {
+            double t = 0.0;
+#pragma unroll
+            for (int i = 0; i < kPoseWarps; ++i) t += s_part[i][tid];
+            s_tot[tid] = t;
+        }
+        __syncthreads();
+    };
+    auto cost_at_shared = [&]() {
+        double c[1] = {pose_cost(A, d, in, s_cam, tid, kPoseThreads)};
+        block_sum(c);
+        return s_tot[0];
+    };
+    if (tid == 0) s_cam = A.cam_in[w];
+    __syncthreads();
+    // LM state (meaningful in thread 0; chi in every thread)
+    CamState cur = s_cam, trial;
+    double chi = cost_at_shared();
     const double chi0 = chi;
     int iters = 0, acc = 0, rej = 0, term = NAV_BA_TERM_ITERATIONS;
     double lambda = 0.0, nu = 2.0;
     const bool bad = !isfinite(chi);
     for (int it = 0; !bad && it < A.lm.iterations; ++it) {
+        // linearize at cur (= s_cam)
         Real cr[12];
-        cam12<Real>(cur, cr);
+        cam12<Real>(s_cam, cr);
         Real u[27];
 #pragma unroll
         for (int k = 0; k < 27; ++k) u[k] = Real(0);
-        for (int i = lane; i < d.n; i += 32) {
+        for (int i = tid; i < d.n; i += kPoseThreads) {
             const long long k = d.o0 + i;
             const Real X[3] = {(Real)A.pts[4 * k], (Real)A.pts[4 * k + 1], (Real)A.pts[4 * k + 2]};
             const Real z[2] = {(Real)A.uv[2 * k], (Real)A.uv[2 * k + 1]};
@@ -150,60 +194,90 @@ __global__ void __launch_bounds__(256) pose_lm_kernel(PoseArgs A) {
 #pragma unroll
             for (int r = 0; r < 6; ++r) u[21 + r] += L.jc[r] * we0 + L.jc[6 + r] * we1;
         }
-        double H[21], b[6];
-#pragma unroll
-        for (int k = 0; k < 21; ++k) H[k] = warp_sum((double)u[k]);
-#pragma unroll
-        for (int k = 0; k < 6; ++k) b[k] = warp_sum((double)u[21 + k]);
-        if (it == 0) {
+        block_sum(u);
+        if (tid < 27) s_hb[tid] = s_tot[tid];  // kept through the trials' cost sums
+        if (tid == 0 && it == 0) {
             double mx = 0.0;
 #pragma unroll
-            for (int r = 0; r < 6; ++r) mx = fmax(mx, fabs(H[ptri(r, r)]));
+            for (int r = 0; r < 6; ++r) mx = fmax(mx, fabs(s_tot[ptri(r, r)]));
             lambda = A.lm.initial_lambda > 0 ? A.lm.initial_lambda : A.lm.tau * mx;
             nu = 2.0;
         }
-        double rho = 0.0;
+        double rho = 0.0, scale = 0.0;
         int q = 0;
-        do {
-            double dx[6];
-            const bool ok = chol_solve6(H, lambda, b, dx);
-            se3_left_update(dx, cur, trial);
-            double chi_new = ok ? pose_cost(A, d, in, trial, lane) : DBL_MAX;
-            double scale = 1e-3;
+        for (;;) {
+            // thread 0: the damped step and the trial state
+            if (tid == 0) {
+                double dx[6];
+                const double* b = s_hb + 21;
+                const bool ok = chol_solve6(s_hb, lambda, b, dx);
+                se3_left_update(dx, cur, trial);
+                scale = 1e-3;
 #pragma unroll
-            for (int r = 0; r < 6; ++r) scale += dx[r] * (lambda * dx[r] + b[r]);
-            rho = (chi - chi_new) / scale;
-            if (rho > 0 && isfinite(chi_new)) {
-                double alpha = 1.0 - pow(2 * rho - 1, 3.0);
-                alpha = fmin(alpha, 2.0 / 3.0);
-                lambda *= fmax(1.0 / 3.0, alpha);
-                nu = 2.0;
-                chi = chi_new;
-                cur = trial;
-                ++acc;
-            } else {
-                lambda *= nu;
-                nu *= 2;
-                ++rej;
+                for (int r = 0; r < 6; ++r) scale += dx[r] * (lambda * dx[r] + b[r]);
+                s_cam = trial;
+                s_flag[0] = ok ? 1 : 0;
             }
-            ++q;
-        } while (rho < 0 && q < A.lm.max_trials);
-        iters = it + 1;
-        if (q == A.lm.max_trials) { term = NAV_BA_TERM_TRIALS_EXHAUSTED; break; }
-        if (rho == 0) { term = NAV_BA_TERM_ZERO_GAIN; break; }
-        if (!isfinite(lambda)) { term = NAV_BA_TERM_LAMBDA_NONFINITE; break; }
+            __syncthreads();
+            const bool ok = s_flag[0] != 0;
+            const double chi_new = ok ? cost_at_shared() : DBL_MAX;
+            // thread 0: gain ratio and damping; whether to try again
+            if (tid == 0) {
+                rho = (chi - chi_new) / scale;
+                if (rho > 0 && isfinite(chi_new)) {
+                    double alpha = 1.0 - pow(2 * rho - 1, 3.0);
+                    alpha = fmin(alpha, 2.0 / 3.0);
+                    lambda *= fmax(1.0 / 3.0, alpha);
+                    nu = 2.0;
+                    chi = chi_new;
+                    cur = trial;
+                    ++acc;
+                } else {
+                    lambda *= nu;
+                    nu *= 2;
+                    ++rej;
+                }
+                ++q;
+                s_flag[1] = (rho < 0 && q < A.lm.max_trials) ? 1 : 0;
+            }
+            __syncthreads();
+            const bool again = s_flag[1] != 0;
+            __syncthreads();  // s_flag is rewritten by the next trial
+            if (!again) break;
+        }
+        // thread 0: termination; the next linearization point
+        if (tid == 0) {
+            iters = it + 1;
+            int stop = 0;
+            if (q == A.lm.max_trials) {
+                term = NAV_BA_TERM_TRIALS_EXHAUSTED;
+                stop = 1;
+            } else if (rho == 0) {
+                term = NAV_BA_TERM_ZERO_GAIN;
+                stop = 1;
+            } else if (!isfinite(lambda)) {
+                term = NAV_BA_TERM_LAMBDA_NONFINITE;
+                stop = 1;
+            }
+            s_cam = cur;
+            s_flag[0] = stop;
+        }
+        __syncthreads();
+        const bool stop = s_flag[0] != 0;
+        __syncthreads();
+        if (stop) break;
     }
-    if (lane == 0) {
+    if (tid == 0) {
         A.cam_out[w] = cur;
-        PoseStat& s = A.stats[w];
-        s.initial_cost = chi0;
-        s.final_cost = chi;
-        s.final_lambda = lambda;
-        s.iters = iters;
-        s.acc = acc;
-        s.rej = rej;
-        s.term = term;
-        s.status = bad ? NAV_BA_ERR_NONFINITE_COST : NAV_BA_OK;
+        PoseStat& st = A.stats[w];
+        st.initial_cost = chi0;
+        st.final_cost = chi;
+        st.final_lambda = lambda;
+        st.iters = iters;
+        st.acc = acc;
+        st.rej = rej;
+        st.term = term;
+        st.status = bad ? NAV_BA_ERR_NONFINITE_COST : NAV_BA_OK;
     }
 }
 
@@ -352,12 +426,11 @@ nav_ba_status solve_pose_batch(cudaStream_t st, PoseBatch& B, const nav_ba_pose_
         if (e == cudaSuccess) e = cudaEventCreate(&ev0);
         if (e == cudaSuccess) e = cudaEventCreate(&ev1);
         if (e == cudaSuccess) e = cudaEventRecord(ev0, st);
-        const int blocks = (m * 32 + 255) / 256;
         if (e == cudaSuccess) {
             if (o.precision == NAV_BA_MIXED)
-                pose_lm_kernel<float><<<blocks, 256, 0, st>>>(A);
+                pose_lm_kernel<float><<<m, kPoseThreads, 0, st>>>(A);
             else
-                pose_lm_kernel<double><<<blocks, 256, 0, st>>>(A);
+                pose_lm_kernel<double><<<m, kPoseThreads, 0, st>>>(A);
             e = cudaGetLastError();
         }
         if (e == cudaSuccess) e = cudaEventRecord(ev1, st);
