@@ -85,3 +85,25 @@ def test_pcg_forms_agree_and_repeat_bitwise(ctx, monkeypatch, precision):
     if precision == abi.FP64:
         ie, ii = res["explicit"].stats["pcg_iterations_total"], res["implicit"].stats["pcg_iterations_total"]
         assert abs(ie - ii) <= max(4, ii // 50)
+
+
+@pytest.mark.parametrize("fixed", ["every_7th", "all"])
+def test_pcg_with_fixed_cameras_matches_oracle(ctx, pcg_form, fixed):
+    """Fixed cameras leave holes in the reduced system's block rows; with every camera fixed and the
+    shared distortion free, the reduced system is the 2x2 k block alone (no camera rows)."""
+    p = Synth(4, n_cams=60, n_points=6000, seed=8).window(0)
+    f = np.zeros(p.n_cams, np.uint8)
+    if fixed == "all":
+        f[:] = 1
+    else:
+        f[::7] = 1
+    p.cam_fixed = f
+    o = workload_options(4)
+    o.iterations = 6
+    r = oracle.solve(p, o, n_threads=8)
+    g = ctx.solve(p, o)
+    assert g.status == abi.OK and g.stats["n_free_cams"] == int((f == 0).sum())
+    assert rel(g.stats["final_cost"], r.stats["final_cost"]) < 1e-6
+    assert abs(g.intrinsics[4] - r.intrinsics[4]) < 1e-5 and abs(g.intrinsics[5] - r.intrinsics[5]) < 1e-5
+    gp, pp = g.cam_pose.reshape(-1, 12), p.cam_pose.reshape(-1, 12)
+    assert np.allclose(gp[f == 1], pp[f == 1], rtol=0, atol=1e-12)  # fixed cameras do not move
