@@ -213,11 +213,37 @@ nav_ba_status solve_pose_batch(cudaStream_t stream, PoseBatch& B, const nav_ba_p
                                HostStaging& stg);
 
 // Two-view triangulation and hypothesis checks (twoview.cu).
-nav_ba_status twoview_check(cudaStream_t stream, const nav_ba_twoview& in, nav_ba_twoview_result& out, std::string* why);
+// Grow-only device scratch of a context for its synchronous small calls (two-view check,
+// undistortion): no allocation, and no free (which synchronizes the device), per call.
+struct DevScratch {
+    void* p = nullptr;
+    size_t cap = 0;
+    void* get(size_t bytes, cudaError_t* e) {
+        if (p && cap >= bytes) return p;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        *e = cudaMalloc(&p, std::max<size_t>(bytes, 256));
+        if (*e != cudaSuccess) {
+            p = nullptr;
+            return nullptr;
+        }
+        cap = std::max<size_t>(bytes, 256);
+        return p;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+nav_ba_status twoview_check(cudaStream_t stream, const nav_ba_twoview& in, nav_ba_twoview_result& out, std::string* why,
+                            DevScratch& scratch);
 
 // Keypoint undistortion (undistort.cu).
 nav_ba_status undistort_points(cudaStream_t stream, const double* K, const double* dist, int iters, int n,
-                               const double* uv_in, double* uv_out, std::string* why);
+                               const double* uv_in, double* uv_out, std::string* why, DevScratch& scratch);
 
 // One-window solve in the library's static device array (no device allocation), noalloc.cu.
 nav_ba_status solve_window_noalloc(int device, cudaStream_t stream, const nav_ba_problem& p,

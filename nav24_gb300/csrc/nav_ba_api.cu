@@ -27,6 +27,7 @@ struct nav_ba_ctx {
     std::vector<nav_ba_problem> prepared_problems;  // shapes of the prepared problem (no data)
     nav_ba_options prepared_opts{};
     PoseBatch pose;  // device buffers of nav_ba_solve_pose_batched (reused)
+    DevScratch scratch;  // device buffer of the two-view check and the undistortion (reused)
     bool has_prepared = false;
     WindowLaunch shape[2];        // per precision (autotuned on nav_ba_prepare_batched)
     bool tuned[2] = {false, false};
@@ -461,9 +462,16 @@ nav_ba_status solve_pipelined(nav_ba_ctx* ctx, const nav_ba_problem* probs, int 
     // NAVBA_VERBOSE: the device timeline of the parts (upload start, kernel start and end per part)
     const char* verbose = getenv("NAVBA_VERBOSE");
     const bool timeline = verbose && verbose[0] == '1';
-    cudaEvent_t tev[1 + 3 * kSolveParts] = {};
+    struct Events {  // destroyed on every return
+        cudaEvent_t ev[1 + 3 * kSolveParts] = {};
+        ~Events() {
+            for (auto& e : ev)
+                if (e) cudaEventDestroy(e);
+        }
+    } tl;
+    cudaEvent_t* tev = tl.ev;
     if (timeline) {
-        for (auto& ev : tev) cudaEventCreate(&ev);
+        for (auto& ev : tl.ev) cudaEventCreate(&ev);
         cudaEventRecord(tev[0], ctx->parts[0].stream);
     }
     for (int k = 0; k < kSolveParts; ++k) {
@@ -524,7 +532,6 @@ nav_ba_status solve_pipelined(nav_ba_ctx* ctx, const nav_ba_problem* probs, int 
             fprintf(stderr, "[navba host]   part %d (%d windows): upload from %.2f ms, kernel %.2f -> %.2f ms\n", k,
                     part_lo(k + 1) - part_lo(k), u, ks, ke);
         }
-        for (auto& ev : tev) cudaEventDestroy(ev);
     }
     // byte counts of the whole call (each part's download reported its own)
     int64_t h2d = 0, d2h = 0;
@@ -656,6 +663,7 @@ void nav_ba_destroy(nav_ba_ctx* ctx) {
         if (part.stream) cudaStreamDestroy(part.stream);
     }
     ctx->pose.release();
+    ctx->scratch.release();
     ctx->stg.release();
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -927,7 +935,7 @@ nav_ba_status nav_ba_twoview_check(nav_ba_ctx* ctx, const nav_ba_twoview* in, na
     if (!in || !out) return set_err(ctx, NAV_BA_ERR_ARGUMENT, "NULL argument");
     cudaSetDevice(ctx->device);
     std::string why;
-    const nav_ba_status st = twoview_check(ctx->stream, *in, *out, &why);
+    const nav_ba_status st = twoview_check(ctx->stream, *in, *out, &why, ctx->scratch);
     if (st != NAV_BA_OK) return set_err(ctx, st, why);
     return NAV_BA_OK;
 }
@@ -937,7 +945,7 @@ nav_ba_status nav_ba_undistort_points(nav_ba_ctx* ctx, const double* K, const do
     if (!ctx) return NAV_BA_ERR_ARGUMENT;
     cudaSetDevice(ctx->device);
     std::string why;
-    const nav_ba_status st = undistort_points(ctx->stream, K, dist, iterations, n, uv_in, uv_out, &why);
+    const nav_ba_status st = undistort_points(ctx->stream, K, dist, iterations, n, uv_in, uv_out, &why, ctx->scratch);
     if (st != NAV_BA_OK) return set_err(ctx, st, why);
     return NAV_BA_OK;
 }

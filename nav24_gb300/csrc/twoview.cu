@@ -174,7 +174,8 @@ bool all_finite(const double* p, int64_t n) {
 
 }  // namespace
 
-nav_ba_status twoview_check(cudaStream_t st, const nav_ba_twoview& in, nav_ba_twoview_result& out, std::string* why) {
+nav_ba_status twoview_check(cudaStream_t st, const nav_ba_twoview& in, nav_ba_twoview_result& out, std::string* why,
+                            DevScratch& scratch) {
     const int n = in.n_matches, nh = in.n_hyp;
     if (n < 0 || nh < 0 || (n > 0 && (!in.kp1 || !in.kp2)) || (nh > 0 && (!in.R || !in.t)) ||
         (nh > 0 && (!out.n_good || !out.parallax_deg))) {
@@ -195,7 +196,6 @@ nav_ba_status twoview_check(cudaStream_t st, const nav_ba_twoview& in, nav_ba_tw
     std::unique_ptr<double[]> cosp(new double[std::max<int64_t>(m, 1)]);
     std::unique_ptr<uint8_t[]> flags(new uint8_t[std::max<int64_t>(m, 1)]);
     if (m > 0) {
-        void* buf = nullptr;
         const size_t b_kp = sizeof(double) * 2 * n, b_in = in.inlier ? (size_t)n : 0, b_R = sizeof(double) * 9 * nh,
                      b_t = sizeof(double) * 3 * nh, b_pts = sizeof(double) * 3 * m, b_cos = sizeof(double) * m,
                      b_fl = (size_t)m;
@@ -203,8 +203,8 @@ nav_ba_status twoview_check(cudaStream_t st, const nav_ba_twoview& in, nav_ba_tw
         const size_t o_kp1 = 0, o_kp2 = o_kp1 + up16(b_kp), o_in = o_kp2 + up16(b_kp), o_R = o_in + up16(b_in),
                      o_t = o_R + up16(b_R), o_pts = o_t + up16(b_t), o_cos = o_pts + up16(b_pts), o_fl = o_cos + up16(b_cos),
                      total = o_fl + up16(b_fl);
-        cudaError_t e = cudaMalloc(&buf, total);
-        auto* base = static_cast<unsigned char*>(buf);
+        cudaError_t e = cudaSuccess;
+        auto* base = static_cast<unsigned char*>(scratch.get(total, &e));
         auto upl = [&](size_t off, const void* h, size_t bytes) {
             if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(base + off, h, bytes, cudaMemcpyHostToDevice, st);
         };
@@ -238,7 +238,6 @@ nav_ba_status twoview_check(cudaStream_t st, const nav_ba_twoview& in, nav_ba_tw
         if (e == cudaSuccess) e = cudaMemcpyAsync(cosp.get(), A.cosp, b_cos, cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(flags.get(), A.flags, b_fl, cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-        if (buf) cudaFree(buf);
         if (e != cudaSuccess) {
             *why = std::string("two-view kernel: ") + cudaGetErrorString(e);
             return NAV_BA_ERR_CUDA;

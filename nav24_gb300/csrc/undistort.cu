@@ -36,7 +36,7 @@ __global__ void k_undistort(int n, double fx, double fy, double cx, double cy, d
 }  // namespace
 
 nav_ba_status undistort_points(cudaStream_t st, const double* K, const double* dist, int iters, int n, const double* uv_in,
-                               double* uv_out, std::string* why) {
+                               double* uv_out, std::string* why, DevScratch& scratch) {
     if (n < 0 || !K || !dist || (n > 0 && (!uv_in || !uv_out)) || iters < 0) {
         *why = "NULL array or negative size";
         return NAV_BA_ERR_ARGUMENT;
@@ -51,9 +51,9 @@ nav_ba_status undistort_points(cudaStream_t st, const double* K, const double* d
         return NAV_BA_ERR_ARGUMENT;
     }
     if (n == 0) return NAV_BA_OK;
-    void* buf = nullptr;
     const size_t bytes = sizeof(double2) * (size_t)n;
-    cudaError_t e = cudaMalloc(&buf, 2 * bytes);
+    cudaError_t e = cudaSuccess;
+    void* buf = scratch.get(2 * bytes, &e);
     double2* din = static_cast<double2*>(buf);
     double2* dout = din + n;
     if (e == cudaSuccess) e = cudaMemcpyAsync(din, uv_in, bytes, cudaMemcpyHostToDevice, st);
@@ -64,7 +64,6 @@ nav_ba_status undistort_points(cudaStream_t st, const double* K, const double* d
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(uv_out, dout, bytes, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (buf) cudaFree(buf);
     if (e != cudaSuccess) {
         *why = std::string("undistort kernel: ") + cudaGetErrorString(e);
         return NAV_BA_ERR_CUDA;
