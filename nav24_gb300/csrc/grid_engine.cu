@@ -2007,15 +2007,18 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     // PCG over the explicit block-sparse S unless its pair lists would be long against the
     // observations (points seen by very many cameras): then the products go through the
     // per-observation records (implicit S).  NAVBA_PCG_FORM=explicit|implicit fixes the form.
+    // (pair lists are indexed by int32 offsets: beyond 2^30 pairs the implicit form is taken)
     bool pcg_x = false;
     if (pcg && !vjp) {
+        const long long npairs = schur_pair_count(h);
         const char* f = getenv("NAVBA_PCG_FORM");
         if (f && !strcmp(f, "implicit"))
             pcg_x = false;
         else if (f && !strcmp(f, "explicit"))
             pcg_x = true;
         else
-            pcg_x = schur_pair_count(h) <= 24LL * std::max(1, h.ne);
+            pcg_x = npairs <= 24LL * std::max(1, h.ne);
+        pcg_x = pcg_x && npairs < (1LL << 30);
     }
     GridHost g;
     build_grid_host(h, g, (!pcg || vjp != nullptr) ? kFormCholesky : (pcg_x ? kFormBlocks : kFormNone), pool);
