@@ -413,15 +413,26 @@ nav_ba_status solve_grid_window(nav_ba_ctx* ctx, const nav_ba_problem& p, const 
 // is solved start to finish by one cluster (several milliseconds for the largest), so the parts take
 // the windows largest first: the first part's windows set the critical path and go to the device
 // as early as possible; the last part, launched last, holds the smallest windows.  Windows are independent, so the results equal those of one launch over
-// the batch.  The whole batch is checked before any part is built, so errors are reported as by
-// the single-launch path (the first failing problem, nothing written).
+// the batch.  Each part's build checks its problems; on a failure the whole batch is checked in
+// the caller's order, so errors are reported as by the single-launch path (the first failing
+// problem, nothing written).
 constexpr int kPipelineMinWindows = 64;
 
 nav_ba_status solve_pipelined(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n, const nav_ba_options* o,
                               nav_ba_result* results) {
     const auto t0 = std::chrono::steady_clock::now();
-    nav_ba_status st = check_batch(ctx, probs, n, o);
-    if (st != NAV_BA_OK) return st;
+    // the options here; each problem is checked by its part's build, so the device starts on the
+    // first part before the rest of the batch is checked.  A failure is reported by one check over
+    // the caller's order (the lowest failing index, as a single pass would), after the parts already
+    // launched have finished; nothing is written to the results.
+    nav_ba_status st = NAV_BA_OK;
+    {
+        std::string why;
+        st = validate_options(o, &why);
+        if (st != NAV_BA_OK) return set_err(ctx, st, why);
+        if (o->solver == NAV_BA_SOLVER_PCG && o->pcg_max_iterations < 1)
+            return set_err(ctx, NAV_BA_ERR_ARGUMENT, "pcg_max_iterations < 1");
+    }
     // windows by decreasing size (observations, then cameras); part k takes the k-th quarter
     std::vector<int32_t> perm(n);
     for (int i = 0; i < n; ++i) perm[i] = i;
@@ -478,9 +489,12 @@ nav_ba_status solve_pipelined(nav_ba_ctx* ctx, const nav_ba_problem* probs, int 
         const int lo = part_lo(k), hi = part_lo(k + 1);
         auto& part = ctx->parts[k];
         const auto tb = std::chrono::steady_clock::now();
-        st = build_batch(ctx, pp.data() + lo, hi - lo, o, pbs[k], true);
+        st = build_batch(ctx, pp.data() + lo, hi - lo, o, pbs[k]);
         t_build += ms_since(tb);
-        if (st != NAV_BA_OK) return st;
+        if (st != NAV_BA_OK) {
+            const nav_ba_status sc = check_batch(ctx, probs, n, o);
+            return sc != NAV_BA_OK ? sc : st;
+        }
         std::string why;
         if (timeline) cudaEventRecord(tev[1 + 3 * k], part.stream);
         // no wait for the copies: each part stages into its own pinned buffers, and every part's
