@@ -1,20 +1,25 @@
 // grid_engine.cu - one large BA problem on the whole GPU (problems beyond the window engine's
-// 24 free cameras: the 200-camera grid, the 50-camera sphere cap, global BA after map merges).
+// 24 free cameras: the 200-camera grid, the 50-camera sphere cap, global BA after map merges, and
+// every PCG solve).
 //
 // Every phase of an LM iteration is a grid-wide kernel over all points / edges / cameras; the
 // Levenberg-Marquardt control (g2o OptimizationAlgorithmLevenberg::solve semantics, as in the
-// window engine) runs on the host, which reads the two reduced scalars of each damping trial
+// window engine) runs on the host, which reads the reduced scalars of each damping trial
 // (cost and dx^T(lambda dx + b)) and decides.  Phases:
 //   lin_points    thread per point: e, J, Huber weight, V_p, g_p (shared with the window engine)
 //   lin_cameras   warp per chunk of <= 256 edges of one camera (camera-major list), U/g_c partial
 //                 sums reduced per camera in a fixed order (no atomics)
 //   schur_points  thread per point: chol(V + lambda I), L, t, A_e = W_e L^T with W_e recomputed (shared)
-//   schur_blocks  warp per nonzero 6x6 block of S over its pair list: S_ab = [a==b](U_a + lambda I)
-//                 - sum A_i A_j^T into a dense FP64 S; b'
-//   cholesky      one thread-block cluster, right-looking 32x32 tiles inside the envelope of S
-//                 (tiles left of a tile row's first nonzero tile stay zero), FP64, one reciprocal
-//                 square root per column
+//   schur_blocks  warp per work item (<= 256 observation pairs of one nonzero 6x6 block of S, taken in
+//                 order from a counter): S_ab = [a==b](U_a + lambda I) - sum A_i A_j^T, into a dense
+//                 FP64 S (Cholesky) or block rows of both triangles (explicit PCG); b'
+//   cholesky      cooperative persistent kernel, right-looking 32x32 tiles inside the envelope of S
+//                 (tiles left of a tile row's first nonzero tile stay zero); FP32 factor + one FP64
+//                 refinement in the mixed form
 //   solve         one CTA, tile-blocked forward/back substitution inside the envelope
+//   pcg           cooperative persistent kernel per damped system, block-Jacobi preconditioner:
+//                 explicit S (two grid phases per CG iteration) or, for long pair lists, products
+//                 through the per-edge records (five phases)
 //   update        thread per point (dx_p = L^T (t - sum A^T dx_c), shared) and per camera (SE(3))
 //   cost          thread per point, per-block partial sums reduced on the host in a fixed order
 // With a GridVjp, the accepted steps' states and damping are taped (or a given damping schedule
