@@ -246,7 +246,7 @@ nav_ba_status nav_ba_solve_noalloc(nav_ba_ctx* ctx, const nav_ba_problem* proble
  * OptimizableTypes.cpp:50-64: e = z - pi(T Xw), J = -Jpi [-[Xc]x | I]), the problem of the tracking call
  * core/frontEnd/FE_SlamMonoV.cpp:153-165 when the current frame is optimized against a fixed map.
  * The LM is the one of nav_ba_solve (iterations, robust kernel, damping, trials, precision), on the
- * 6x6 normal equations.  nav_ba_solve_pose_batched solves n problems in one launch (one warp each).
+ * 6x6 normal equations.  nav_ba_solve_pose_batched solves n problems in one launch (one block each).
  * Statuses per problem as in nav_ba_solve_batched; a problem with no observation is EMPTY. */
 typedef struct nav_ba_pose_problem {
     int32_t n_obs;
