@@ -68,38 +68,53 @@ void build_window(const nav_ba_problem& p, const nav_ba_options& o, HostWindow& 
     w.npt = p.n_points;
     auto cam_fixed = [&](int c) { return p.cam_fixed && p.cam_fixed[c]; };
     auto pt_fixed = [&](int i) { return p.point_fixed && p.point_fixed[i]; };
-    // active edges, counted per point (counting sort keeps input order within a point)
+    // active edges, counted per point (counting sort keeps input order within a point), and the
+    // cameras with an active edge: the free cameras are known before the edges are placed
+    auto active = [&](int c, int i) { return free_intr || !(cam_fixed(c) && pt_fixed(i)); };
     std::vector<int32_t> cnt(w.npt + 1, 0);
-    std::vector<uint8_t> act(p.n_obs, 0);
+    std::vector<uint8_t> cam_has(w.ncam, 0);
     for (int k = 0; k < p.n_obs; ++k) {
         const int c = p.obs_cam[k], i = p.obs_point[k];
-        act[k] = free_intr || !(cam_fixed(c) && pt_fixed(i));
-        if (act[k]) cnt[i + 1]++;
+        if (active(c, i)) {
+            cnt[i + 1]++;
+            cam_has[c] = 1;
+        }
     }
     w.pt_eoff.assign(w.npt + 1, 0);
     for (int i = 0; i < w.npt; ++i) w.pt_eoff[i + 1] = w.pt_eoff[i] + cnt[i + 1];
     w.ne = w.pt_eoff[w.npt];
-    w.edge_cam.resize(w.ne);
-    w.edge_obs.resize(w.ne);
-    w.edge_uv.resize(2LL * w.ne);
-    w.edge_pt.resize(w.ne);
-    std::vector<int32_t> fill(w.pt_eoff.begin(), w.pt_eoff.end() - 1);
-    std::vector<uint8_t> cam_has(w.ncam, 0);
-    for (int k = 0; k < p.n_obs; ++k) {
-        if (!act[k]) continue;
-        const int i = p.obs_point[k];
-        const int e = fill[i]++;
-        w.edge_cam[e] = p.obs_cam[k];
-        w.edge_obs[e] = k;
-        w.edge_pt[e] = i;
-        w.edge_uv[2LL * e] = p.obs_uv[2LL * k];
-        w.edge_uv[2LL * e + 1] = p.obs_uv[2LL * k + 1];
-        cam_has[p.obs_cam[k]] = 1;
-    }
     w.cam_free.assign(w.ncam, -1);
     w.nfc = 0;
     for (int c = 0; c < w.ncam; ++c)
         if (!cam_fixed(c) && cam_has[c]) w.cam_free[c] = w.nfc++;
+    // edges point-major; up to 64 free cameras each point's mask of free cameras and whether one
+    // of them observes it twice come along (for the Schur counts below)
+    w.edge_cam.resize(w.ne);
+    w.edge_obs.resize(w.ne);
+    w.edge_uv.resize(2LL * w.ne);
+    w.edge_pt.resize(w.ne);
+    const bool masks = w.nfc > 0 && w.nfc <= 64;
+    std::vector<uint64_t> pmask(masks ? w.npt : 0, 0);
+    std::vector<uint8_t> prep(masks ? w.npt : 0, 0);
+    std::vector<int32_t> fill(w.pt_eoff.begin(), w.pt_eoff.end() - 1);
+    for (int k = 0; k < p.n_obs; ++k) {
+        const int c = p.obs_cam[k], i = p.obs_point[k];
+        if (!active(c, i)) continue;
+        const int e = fill[i]++;
+        w.edge_cam[e] = c;
+        w.edge_obs[e] = k;
+        w.edge_pt[e] = i;
+        w.edge_uv[2LL * e] = p.obs_uv[2LL * k];
+        w.edge_uv[2LL * e + 1] = p.obs_uv[2LL * k + 1];
+        if (masks) {
+            const int a = w.cam_free[c];
+            if (a >= 0) {
+                const uint64_t bit = 1ull << a;
+                prep[i] |= (uint8_t)((pmask[i] & bit) != 0);
+                pmask[i] |= bit;
+            }
+        }
+    }
     w.pt_free.assign(w.npt, -1);
     w.nfp = 0;
     for (int i = 0; i < w.npt; ++i)
@@ -115,23 +130,14 @@ void build_window(const nav_ba_problem& p, const nav_ba_options& o, HostWindow& 
     // repeated camera, the pairs are counted one by one.
     w.n_pairs = 0;
     w.n_schur_blocks = w.nfc;  // the diagonal blocks
-    if (w.nfc > 0 && w.nfc <= 64) {
+    if (masks) {
         std::vector<uint64_t> row(w.nfc, 0);  // row a: cameras b < a sharing a point with a
         for (int i = 0; i < w.npt; ++i) {
             if (w.pt_free[i] < 0) continue;
-            uint64_t m = 0;
-            int k = 0;
-            bool repeat = false;
-            for (int e = w.pt_eoff[i]; e < w.pt_eoff[i + 1]; ++e) {
-                const int a = w.cam_free[w.edge_cam[e]];
-                if (a < 0) continue;
-                const uint64_t bit = 1ull << a;
-                repeat = repeat || (m & bit);
-                m |= bit;
-                ++k;
-            }
-            if (!repeat) {
-                w.n_pairs += (int64_t)k * (k + 1) / 2;
+            const uint64_t m = pmask[i];
+            if (!prep[i]) {
+                const int64_t k = __builtin_popcountll(m);
+                w.n_pairs += k * (k + 1) / 2;
             } else {
                 for (int e = w.pt_eoff[i]; e < w.pt_eoff[i + 1]; ++e) {
                     const int a = w.cam_free[w.edge_cam[e]];
