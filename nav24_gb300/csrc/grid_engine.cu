@@ -224,6 +224,8 @@ __global__ void k_schur_blocks(WinArgs<Real> A, const int2* blocks, const int32_
                 if (slot + rnd < 36) pp[slot + rnd] = sums[rnd];
             if (c.lane < 6) pp[36 + c.lane] = bk;
             __threadfence();
+            // every lane's partials and fence come before lane 0 publishes the item as done
+            __syncwarp();
             int last = 0;
             if (c.lane == 0) last = atomicAdd(done + blk, 1) == nit - 1;
             if (!__shfl_sync(kFullG, last, 0)) continue;

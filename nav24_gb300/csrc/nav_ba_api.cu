@@ -456,15 +456,17 @@ nav_ba_status solve_pipelined(nav_ba_ctx* ctx, const nav_ba_problem* probs, int 
     struct SwapBack {
         PreparedBatch* pbs;
         nav_ba_ctx* ctx;
-        int* launched;
         ~SwapBack() {
-            for (int k = 0; k < *launched; ++k) cudaStreamSynchronize(ctx->parts[k].stream);  // nothing left in flight
+            // nothing left in flight: every part's stream, also one whose upload was enqueued and
+            // whose launch then failed (its copies still read that part's pinned staging)
+            for (int k = 0; k < kSolveParts; ++k)
+                if (ctx->parts[k].stream) cudaStreamSynchronize(ctx->parts[k].stream);
             for (int k = 0; k < kSolveParts; ++k) {
                 std::swap(pbs[k].host, ctx->parts[k].host);
                 std::swap(pbs[k].dev, ctx->parts[k].dev);
             }
         }
-    } swap_back{pbs, ctx, &launched};
+    } swap_back{pbs, ctx};
     // part boundaries at (k / parts)^2 of the batch: the first part (the largest windows, whose solves
     // are the longest) is small, so the device starts on it early; later parts grow while the device
     // is busy (4 parts: 1/16, 3/16, 5/16, 7/16)

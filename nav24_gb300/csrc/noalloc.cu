@@ -14,6 +14,7 @@
 // kernel rewrites everything it reads before reading it, and this file clears the work-queue
 // counter and the statistics on every call.  Two calls whose work overlaps on the GPU (for example
 // from two contexts on the same device) race on the array.
+#include <chrono>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -57,6 +58,11 @@ nav_ba_status solve_window_noalloc(int device, cudaStream_t stream, const nav_ba
     auto fail = [&](nav_ba_status st, const std::string& msg) {
         if (why) *why = msg;
         return st;
+    };
+    // host-clock timings (events would have to be created, which this call avoids)
+    const auto t0 = std::chrono::steady_clock::now();
+    auto ms_since = [](std::chrono::steady_clock::time_point t) {
+        return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t).count();
     };
     if (o.solver != NAV_BA_SOLVER_CHOLESKY)
         return fail(NAV_BA_ERR_UNSUPPORTED, "the no-allocation solve uses the Cholesky solver");
@@ -173,9 +179,11 @@ nav_ba_status solve_window_noalloc(int device, cudaStream_t stream, const nav_ba
     pb.lm.initial_lambda = o.initial_lambda;
     pb.lm.tau = o.tau;
     pb.intr = make_intr(p.intrinsics, p.camera_model);
+    int64_t h2d = 0, d2h = 0;
     auto up = [&](void* dst, const void* src, size_t bytes) {
         if (e != cudaSuccess || bytes == 0) return;
         e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream);
+        h2d += (int64_t)bytes;
     };
     up(b.d_win, &d, sizeof(WinDesc));
     up(b.d_order, &order0, sizeof(int32_t));
@@ -191,13 +199,20 @@ nav_ba_status solve_window_noalloc(int device, cudaStream_t stream, const nav_ba
     // the arena keeps the previous call's contents: clear the statistics (the queue counter is
     // reset by the launch itself)
     if (e == cudaSuccess) e = cudaMemsetAsync(b.d_stats, 0, sizeof(WinStats), stream);
+    // setup: host structure and the enqueued uploads; solve: until the kernel has finished
+    const double t_setup = ms_since(t0);
+    const auto t1 = std::chrono::steady_clock::now();
     if (e == cudaSuccess) e = window_batch_launch(pb, stream, o.precision, WindowLaunch{1, 256}, -1.0);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    const double t_solve = ms_since(t1);
+    const auto t2 = std::chrono::steady_clock::now();
     std::vector<CamState> cams(nc);
     std::vector<double> pts(4 * np), trace(trace_stride);
     WinStats st{};
     auto dn = [&](void* dst, const void* src, size_t bytes) {
         if (e != cudaSuccess || bytes == 0) return;
         e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream);
+        d2h += (int64_t)bytes;
     };
     dn(cams.data(), b.d_cam_out, sizeof(CamState) * nc);
     dn(pts.data(), b.d_pt_out, sizeof(double) * 4 * np);
@@ -205,7 +220,9 @@ nav_ba_status solve_window_noalloc(int device, cudaStream_t stream, const nav_ba
     dn(&st, b.d_stats, sizeof(WinStats));
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) return fail(NAV_BA_ERR_CUDA, std::string("no-allocation solve: ") + cudaGetErrorString(e));
-    if (st.status != NAV_BA_OK) return fail((nav_ba_status)st.status, "non-finite initial cost");
+    if (st.status != NAV_BA_OK)
+        return fail((nav_ba_status)st.status,
+                    std::string("no-allocation solve: ") + nav_ba_status_string((nav_ba_status)st.status));
     r.initial_cost = st.initial_cost;
     r.final_cost = st.final_cost;
     r.final_lambda = st.final_lambda;
@@ -218,6 +235,10 @@ nav_ba_status solve_window_noalloc(int device, cudaStream_t stream, const nav_ba
     r.n_free_points = h.nfp;
     r.n_schur_blocks = h.n_schur_blocks;
     r.edge_iterations = (int64_t)h.ne * st.iterations_done;
+    r.h2d_bytes = h2d;
+    r.d2h_bytes = d2h;
+    r.time_setup_ms = t_setup;
+    r.time_solve_ms = t_solve;
     r.status = NAV_BA_OK;
     if (r.cam_pose_out)
         for (int c = 0; c < p.n_cams; ++c) pose12_from_cam(cams[c], r.cam_pose_out + 12LL * c);
@@ -227,6 +248,7 @@ nav_ba_status solve_window_noalloc(int device, cudaStream_t stream, const nav_ba
     if (r.intrinsics_out) std::memcpy(r.intrinsics_out, p.intrinsics, sizeof(double) * 8);
     if (r.cost_trace)
         for (int k = 0; k <= st.iterations_done; ++k) r.cost_trace[k] = trace[k];
+    r.time_download_ms = ms_since(t2);
     return NAV_BA_OK;
 }
 

@@ -213,6 +213,12 @@ struct EdgeLin {
 struct Model {
     int model;
     double fx, fy, cx, cy, k1, k2, k3 = 0.0, k4 = 0.0;
+    // Kannala-Brandt 8 with the reference's own roundings (oracle_linearize_mode, mode 1): project
+    // takes theta and psi through atan2f/sqrtf on float-rounded inputs and evaluates
+    // r = theta + k1 theta^3 + ... with theta^5 = theta^3 theta^2, ... (KannalaBrandt8.cpp:92-107);
+    // projectJac forms 3 k1, 5 k2, ... in float (int times float parameter) before widening
+    // (:205-209).  The intrinsics are the float parameters nav24 keeps (Calibration.cpp:42-60).
+    bool kb8_reference_rounding = false;
 };
 
 // Residual and Jacobians of one edge.  Returns false when the edge cannot be evaluated
@@ -244,9 +250,21 @@ void linearize_edge(const Model& m, const SE3& T, const double* X, const double*
             const double t2 = th * th, t3 = t2 * th, t4 = t2 * t2, t5 = t4 * th, t6 = t4 * t2, t7 = t6 * th,
                          t8 = t4 * t4, t9 = t8 * th;
             const double f = th + m.k1 * t3 + m.k2 * t5 + m.k3 * t7 + m.k4 * t9;
-            const double fd = 1.0 + 3.0 * m.k1 * t2 + 5.0 * m.k2 * t4 + 7.0 * m.k3 * t6 + 9.0 * m.k4 * t8;
-            u = m.fx * f * x / rho + m.cx;
-            v = m.fy * f * y / rho + m.cy;
+            double fd = 1.0 + 3.0 * m.k1 * t2 + 5.0 * m.k2 * t4 + 7.0 * m.k3 * t6 + 9.0 * m.k4 * t8;
+            if (m.kb8_reference_rounding) {
+                const float k1f = (float)m.k1, k2f = (float)m.k2, k3f = (float)m.k3, k4f = (float)m.k4;
+                fd = 1.0 + (double)(3 * k1f) * t2 + (double)(5 * k2f) * t4 + (double)(7 * k3f) * t6 +
+                     (double)(9 * k4f) * t8;
+                const double thf = (double)atan2f(sqrtf((float)rho2), (float)zc);
+                const double psi = (double)atan2f((float)y, (float)x);
+                const double q2 = thf * thf, q3 = thf * q2, q5 = q3 * q2, q7 = q5 * q2, q9 = q7 * q2;
+                const double r = thf + m.k1 * q3 + m.k2 * q5 + m.k3 * q7 + m.k4 * q9;
+                u = m.fx * r * std::cos(psi) + m.cx;
+                v = m.fy * r * std::sin(psi) + m.cy;
+            } else {
+                u = m.fx * f * x / rho + m.cx;
+                v = m.fy * f * y / rho + m.cy;
+            }
             const double rho3 = rho2 * rho, x2 = x * x, y2 = y * y;
             J[0] = m.fx * (fd * zc * x2 / (rho2 * (rho2 + z2)) + f * y2 / rho3);
             J[1] = m.fx * (fd * zc * y * x / (rho2 * (rho2 + z2)) - f * y * x / rho3);
@@ -1041,10 +1059,16 @@ extern "C" int32_t oracle_solve(const nav_ba_problem* p, const nav_ba_options* o
 
 extern "C" int32_t oracle_linearize(const nav_ba_problem* p, const nav_ba_options* o, double* e,
                                     double* jc, double* jp, double* w) {
-    if (!o) return NAV_BA_ERR_ARGUMENT;
+    return oracle_linearize_mode(p, o, 0, e, jc, jp, w);
+}
+
+extern "C" int32_t oracle_linearize_mode(const nav_ba_problem* p, const nav_ba_options* o, int32_t mode,
+                                         double* e, double* jc, double* jp, double* w) {
+    if (!o || mode < 0 || mode > 1) return NAV_BA_ERR_ARGUMENT;
     int32_t st = validate(p);
     if (st != NAV_BA_OK) return st;
     Model m;
+    m.kb8_reference_rounding = mode == 1;
     m.model = p->camera_model;
     m.fx = p->intrinsics[0]; m.fy = p->intrinsics[1]; m.cx = p->intrinsics[2]; m.cy = p->intrinsics[3];
     m.k1 = p->intrinsics[4]; m.k2 = p->intrinsics[5];

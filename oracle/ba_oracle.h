@@ -30,6 +30,12 @@ int32_t oracle_solve_schedule(const nav_ba_problem* p, const nav_ba_options* o, 
 int32_t oracle_linearize(const nav_ba_problem* p, const nav_ba_options* o, double* e,
                          double* jc, double* jp, double* w);
 
+/* oracle_linearize with a rounding mode: 0 = FP64 throughout (as oracle_linearize); 1 = the
+ * reference's own roundings in KannalaBrandt8::project / projectJac (theta and psi through
+ * atan2f/sqrtf, 3 k1 ... 9 k4 in float), to compare with nav24's code built in oracle/_ref. */
+int32_t oracle_linearize_mode(const nav_ba_problem* p, const nav_ba_options* o, int32_t mode,
+                              double* e, double* jc, double* jp, double* w);
+
 /* Distortion-parameter Jacobian [n_obs][2][2] (d e / d (k1, k2)); radial model only. */
 int32_t oracle_distortion_jacobian(const nav_ba_problem* p, double* jk);
 

@@ -1,8 +1,9 @@
 """Build recipe of the CPU oracle (test infrastructure): oracle/_build/libnavba_oracle.so.
 
 The oracle is plain C++17 with no dependencies; it is compiled with g++ directly.  The
-reference's own BA path cannot be compiled here (it needs g2o, Eigen, OpenCV, Boost and glog,
-none of which exist in this environment), so there is no oracle/_ref build.
+reference's whole BA path cannot be compiled here (it needs g2o, Eigen, OpenCV, Boost and glog,
+none of which exist in this environment); its edge and camera-model code is, against stand-in
+headers, by oracle/ref_build.py into oracle/_ref.
 """
 from __future__ import annotations
 

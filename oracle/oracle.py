@@ -24,6 +24,8 @@ def lib():
         L.oracle_solve_schedule.restype = C.c_int32
         L.oracle_linearize.argtypes = [P, O, dp, dp, dp, dp]
         L.oracle_linearize.restype = C.c_int32
+        L.oracle_linearize_mode.argtypes = [P, O, C.c_int32, dp, dp, dp, dp]
+        L.oracle_linearize_mode.restype = C.c_int32
         L.oracle_distortion_jacobian.argtypes = [P, dp]
         L.oracle_distortion_jacobian.restype = C.c_int32
         L.oracle_reduced_system.argtypes = [P, O, C.c_double, C.c_int32, C.POINTER(C.c_int32), dp, dp,
@@ -58,11 +60,14 @@ def solve_schedule(prob: abi.Problem, opt: abi.nav_ba_options, lambdas=None, n_t
     return buf.result(st), sched.lambdas
 
 
-def linearize(prob: abi.Problem, opt: abi.nav_ba_options):
+def linearize(prob: abi.Problem, opt: abi.nav_ba_options, reference_rounding: bool = False):
+    """Residuals, Jacobians and robust weights of every observation.  reference_rounding: the
+    Kannala-Brandt 8 model with the reference's own float roundings (oracle_linearize_mode 1)."""
     n = prob.n_obs
     e, jc, jp, w = (np.zeros((n, 2)), np.zeros((n, 2, 6)), np.zeros((n, 2, 3)), np.zeros(n))
     p = prob.as_c()
-    st = lib().oracle_linearize(C.byref(p), C.byref(opt), _d(e), _d(jc), _d(jp), _d(w))
+    st = lib().oracle_linearize_mode(C.byref(p), C.byref(opt), 1 if reference_rounding else 0, _d(e), _d(jc),
+                                     _d(jp), _d(w))
     if st != abi.OK:
         raise RuntimeError(f"oracle_linearize status {st}")
     return e, jc, jp, w

@@ -1,0 +1,3 @@
+// Forwards to the OpenCV stand-in (reference-pin build only).
+#pragma once
+#include <ref_cv.hpp>

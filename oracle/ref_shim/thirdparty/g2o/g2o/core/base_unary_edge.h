@@ -1,0 +1,3 @@
+// Forwards to the g2o stand-in (reference-pin build only).
+#pragma once
+#include <ref_g2o.hpp>
