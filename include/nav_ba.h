@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define NAV_BA_ABI_VERSION 1
+#define NAV_BA_ABI_VERSION 2
 
 typedef enum nav_ba_status {
     NAV_BA_OK = 0,
@@ -149,6 +149,12 @@ typedef struct nav_ba_result {
     int64_t edge_iterations;      /* active edges x LM iterations done (nav_ba_run: summed) */
     int64_t h2d_bytes;            /* bytes this call copied host -> device                  */
     int64_t d2h_bytes;            /* bytes this call copied device -> host                  */
+    /* active edges whose point lies at or behind its camera (Z <= 0 in the camera frame) at the
+     * final state: the edges for which EdgeSE3ProjectXYZ::isDepthPositive
+     * (core/dataTypes/optimization/OptimizableTypes.hpp:109-113) is false.  nav24's GraphOptim never
+     * calls that test; ORB-SLAM-style callers use it after a solve to drop such edges. */
+    int32_t n_depth_nonpositive;
+    int32_t reserved1;
 } nav_ba_result;
 
 typedef struct nav_ba_ctx nav_ba_ctx;
@@ -267,7 +273,7 @@ typedef struct nav_ba_pose_result {
     int32_t trials_rejected;
     int32_t termination;          /* nav_ba_termination                                         */
     int32_t status;               /* nav_ba_status of this problem                              */
-    int32_t reserved;
+    int32_t n_depth_nonpositive;  /* observations behind the final pose (Z <= 0), as nav_ba_result */
 } nav_ba_pose_result;
 
 nav_ba_status nav_ba_solve_pose_batched(nav_ba_ctx* ctx, const nav_ba_pose_problem* problems,

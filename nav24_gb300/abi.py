@@ -104,6 +104,8 @@ class nav_ba_result(C.Structure):
         ("edge_iterations", C.c_int64),
         ("h2d_bytes", C.c_int64),
         ("d2h_bytes", C.c_int64),
+        ("n_depth_nonpositive", C.c_int32),
+        ("reserved1", C.c_int32),
     ]
 
 
@@ -116,7 +118,7 @@ class nav_ba_pose_result(C.Structure):
     _fields_ = [("pose_out", C.POINTER(C.c_double)), ("initial_cost", C.c_double), ("final_cost", C.c_double),
                 ("final_lambda", C.c_double), ("iterations_done", C.c_int32), ("trials_accepted", C.c_int32),
                 ("trials_rejected", C.c_int32), ("termination", C.c_int32), ("status", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("n_depth_nonpositive", C.c_int32)]
 
 
 @dataclass

@@ -118,6 +118,12 @@ struct CamState {
     double pad1;
 };
 
+// The complement of EdgeSE3ProjectXYZ::isDepthPositive (core/dataTypes/optimization/
+// OptimizableTypes.hpp:109-113): the point X lies at or behind the camera, Z_c <= 0 (FP64).
+NAVBA_HD bool depth_nonpositive(const CamState& c, const double* X) {
+    return c.R[6] * X[0] + c.R[7] * X[1] + c.R[8] * X[2] + c.t[2] <= 0.0;
+}
+
 NAVBA_HD void cam_from_pose12(const double* P, CamState& c) {
     const double R[9] = {P[0], P[1], P[2], P[4], P[5], P[6], P[8], P[9], P[10]};
     q_from_rot(R, c.q);
@@ -241,7 +247,7 @@ NAVBA_HD void transform(const Real* R, const Real* t, const Real* X, Real* Xc) {
 
 // 1/z.  In FP64 on the device by Newton-Raphson for the reciprocal (x <- x + x (1 - z x), quadratic
 // convergence) from the FP32 reciprocal: its ~2^-23 relative error falls below an ulp in two steps
-// (checked: at most 1 ulp from the IEEE quotient over 2.3M depths from 1e-20 to 1e20).  The IEEE
+// (at most 1 ulp from the IEEE quotient: tests/test_gpu_nr_math.py over 1e-20..1e20).  The IEEE
 // FP64 divide is a long instruction sequence on GB300's FP64 pipe; this is two conversions and four
 // fused multiply-adds.  Outside the FP32 range, and in FP32 or on the host, the plain quotient.
 template <class Real>
@@ -259,6 +265,24 @@ NAVBA_HD Real recip(Real z) {
 #endif
     return Real(1) / z;
 }
+
+#ifdef __CUDACC__
+// FP64 reciprocal and reciprocal square root by Newton-Raphson from the FP32 estimate (device):
+// x <- x (2 - z x) and r <- r (3 - y r^2) / 2 converge quadratically, so the estimate's ~2^-22
+// relative error falls to the FP64 rounding level in two steps.  Outside the FP32 range the IEEE
+// operations are used.  Bounded against the IEEE results in ulps by tests/test_gpu_nr_math.py.
+__device__ __forceinline__ double recip_nr(double z) { return recip<double>(z); }
+
+__device__ __forceinline__ double rsqrt_nr(double y) {
+    if (y > 1e-30 && y < 1e30) {
+        double r = (double)rsqrtf((float)y);
+        r = r * fma(-0.5 * y * r, r, 1.5);
+        r = r * fma(-0.5 * y * r, r, 1.5);
+        return r;
+    }
+    return 1.0 / sqrt(y);
+}
+#endif
 
 // Projection pi(Xc) and, if J != nullptr, d pi / d Xc (2x3); if Jk != nullptr (radial model),
 // d pi / d (k1, k2) (2x2).

@@ -31,7 +31,9 @@ struct WinDesc {
 struct WinStats {
     double initial_cost, final_cost, final_lambda;
     int32_t iterations_done, accepted, rejected, termination;
-    int32_t status, pad0, pad1, pad2;
+    int32_t status;
+    int32_t depth_nonpos;  // active edges with the point at or behind its camera, final state
+    int32_t pad1, pad2;
 };
 
 // Per-launch options of the LM loop.
@@ -158,6 +160,7 @@ struct GridResult {
     std::vector<double> points;  // [npt][4]
     double k1 = 0, k2 = 0;       // final distortion (optimize_k)
     int32_t pcg_iterations = 0;
+    int32_t depth_nonpos = 0;    // active edges with the point at or behind its camera, final state
 };
 
 // Differentiation through the accepted LM steps (grid engine, FP64, Cholesky, pinhole).
@@ -195,7 +198,8 @@ struct PoseDesc {
 };
 struct PoseStat {
     double initial_cost, final_cost, final_lambda;
-    int32_t iters, acc, rej, term, status, pad;
+    int32_t iters, acc, rej, term, status;
+    int32_t depth_nonpos;  // observations at or behind the final pose
 };
 struct PoseBatch {
     PoseDesc* d_desc = nullptr;

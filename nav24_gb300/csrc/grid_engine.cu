@@ -90,6 +90,20 @@ __global__ void k_cost(WinArgs<Real> A, WinDesc D, const Cost* camc, const doubl
     block_partial<false>(cost_partial<Cost, Real>(A, c, D, camc, X), part);
 }
 
+// Active edges whose point is at or behind its camera (Z_c <= 0, FP64), per-block partial counts.
+template <class Real>
+__global__ void k_depth_count(WinArgs<Real> A, WinDesc D, const CamState* cams, const double* X, double* part) {
+    const CC c = grid_view();
+    double n = 0.0;
+    for (int p = c.gt; p < D.npt; p += c.CT) {
+        const int gp = D.pt0 + p;
+        const double Xp[3] = {X[4LL * gp], X[4LL * gp + 1], X[4LL * gp + 2]};
+        const int e1 = A.pt_eoff[gp + 1];
+        for (int e = A.pt_eoff[gp]; e < e1; ++e) n += depth_nonpositive(cams[A.edge_cam[e]], Xp) ? 1.0 : 0.0;
+    }
+    block_partial<false>(n, part);
+}
+
 template <class Real>
 __global__ void k_lin_points(WinArgs<Real> A, WinDesc D, const Real* camr, const double* X, double* part) {
     const CC c = grid_view();
@@ -2678,6 +2692,9 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     out.k1 = kcur[0];
     out.k2 = kcur[1];
     out.pcg_iterations = pcg_total;
+    k_depth_count<Real><<<pblocks, TB, 0, st>>>(A, D, cams[cur], A.x[cur], d_part);
+    chk(cudaGetLastError());
+    out.depth_nonpos = (int32_t)sum_part(pblocks, false);
     out.trace.resize(out.iterations_done + 1);
     out.cams.resize(nc);
     out.points.resize(4LL * np);

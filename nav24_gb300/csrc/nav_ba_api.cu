@@ -112,6 +112,7 @@ void clear_stats(nav_ba_result* r) {
     r->pcg_iterations_total = 0;
     r->status = NAV_BA_OK;
     r->edge_iterations = r->h2d_bytes = r->d2h_bytes = 0;
+    r->n_depth_nonpositive = 0;
 }
 
 // host_status of a window that goes to the grid engine (too large for the window engine)
@@ -334,6 +335,7 @@ nav_ba_status download_batch(nav_ba_ctx* ctx, const nav_ba_problem* probs, int n
         r->trials_rejected = s.rejected;
         r->termination = s.termination;
         r->edge_iterations = (int64_t)h.ne * s.iterations_done;
+        r->n_depth_nonpositive = s.depth_nonpos;
         if (s.status != NAV_BA_OK) {
             st_out[i] = s.status;
             return;
@@ -372,6 +374,7 @@ void fill_grid_result(const nav_ba_problem& p, const HostWindow& h, const nav_ba
     r.n_free_points = h.nfp;
     r.n_schur_blocks = h.n_schur_blocks;
     r.edge_iterations = (int64_t)h.ne * g.iterations_done;
+    r.n_depth_nonpositive = g.depth_nonpos;
     if (r.cam_pose_out)
         for (int c = 0; c < p.n_cams; ++c) pose12_from_cam(g.cams[c], r.cam_pose_out + 12LL * c);
     if (r.points_out)
@@ -803,6 +806,7 @@ nav_ba_status nav_ba_run(nav_ba_ctx* ctx, const nav_ba_options* o, nav_ba_result
             stats->n_active_edges += ctx->prepared.host[i].ne;
             stats->n_free_cams += ctx->prepared.host[i].nfc;
             stats->n_free_points += ctx->prepared.host[i].nfp;
+            stats->n_depth_nonpositive += s.depth_nonpos;
             edge_iters += (int64_t)ctx->prepared.host[i].ne * s.iterations_done;
         }
         stats->edge_iterations = edge_iters;

@@ -235,6 +235,7 @@ nav_ba_status solve_window_noalloc(int device, cudaStream_t stream, const nav_ba
     r.n_free_points = h.nfp;
     r.n_schur_blocks = h.n_schur_blocks;
     r.edge_iterations = (int64_t)h.ne * st.iterations_done;
+    r.n_depth_nonpositive = st.depth_nonpos;
     r.h2d_bytes = h2d;
     r.d2h_bytes = d2h;
     r.time_setup_ms = t_setup;

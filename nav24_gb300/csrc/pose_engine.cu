@@ -267,8 +267,16 @@ __global__ void __launch_bounds__(kPoseThreads) pose_lm_kernel(PoseArgs A) {
         __syncthreads();
         if (stop) break;
     }
+    // observations at or behind the final pose
+    __syncthreads();
+    if (tid == 0) s_cam = cur;
+    __syncthreads();
+    double nneg[1] = {0.0};
+    for (int i = tid; i < d.n; i += kPoseThreads) nneg[0] += depth_nonpositive(s_cam, A.pts + 4 * (d.o0 + i)) ? 1.0 : 0.0;
+    block_sum(nneg);
     if (tid == 0) {
         A.cam_out[w] = cur;
+        A.stats[w].depth_nonpos = (int32_t)s_tot[0];
         PoseStat& st = A.stats[w];
         st.initial_cost = chi0;
         st.final_cost = chi;
@@ -461,9 +469,11 @@ nav_ba_status solve_pose_batch(cudaStream_t st, PoseBatch& B, const nav_ba_pose_
             r.iterations_done = r.trials_accepted = r.trials_rejected = 0;
             r.termination = NAV_BA_TERM_NOTHING_TO_DO;
             r.status = NAV_BA_EMPTY;
+            r.n_depth_nonpositive = 0;
             continue;
         }
         const PoseStat& s = stats[slot[i]];
+        r.n_depth_nonpositive = s.depth_nonpos;
         r.initial_cost = s.initial_cost;
         r.final_cost = s.final_cost;
         r.final_lambda = s.final_lambda;

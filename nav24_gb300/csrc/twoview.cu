@@ -33,31 +33,10 @@ struct TvArgs {
     double* cosp;    // [nh][n]
 };
 
-// FP64 reciprocal and reciprocal square root for the rotation parameters, by Newton-Raphson from
-// the FP32 estimate: x <- x (2 - z x) and r <- r (3 - y r^2) / 2 converge quadratically, so the
-// estimate's ~2^-22 relative error falls below an FP64 ulp in two steps.  Outside the FP32 range the
-// IEEE operations are used.  (GB300 issues FP64 at 2 lanes per clock per SM; the IEEE divide and
-// square root are long sequences, and the rotations are this kernel's FP64 work.)
-__device__ __forceinline__ double recip_nr(double z) {
-    const double az = fabs(z);
-    if (az > 1e-30 && az < 1e30) {
-        double x = (double)(1.0f / (float)z);
-        x = fma(x, fma(-z, x, 1.0), x);
-        x = fma(x, fma(-z, x, 1.0), x);
-        return x;
-    }
-    return 1.0 / z;
-}
-
-__device__ __forceinline__ double rsqrt_nr(double y) {
-    if (y > 1e-30 && y < 1e30) {
-        double r = (double)rsqrtf((float)y);
-        r = r * fma(-0.5 * y * r, r, 1.5);
-        r = r * fma(-0.5 * y * r, r, 1.5);
-        return r;
-    }
-    return 1.0 / sqrt(y);
-}
+// The rotation parameters' FP64 reciprocals and reciprocal square roots are Newton-Raphson
+// refinements of FP32 estimates (recip_nr, rsqrt_nr in ba_math.cuh): GB300 issues FP64 at 2 lanes
+// per clock per SM, the IEEE divide and square root are long sequences, and the rotations are this
+// kernel's FP64 work.
 
 // Right singular vector of a 4x4 matrix for its smallest singular value: one-sided Jacobi
 // (Hestenes 1958): column pairs of A are rotated until mutually orthogonal, the rotations

@@ -799,6 +799,7 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
     if (A.edge_uvr)
         for (int e = c.gt; e < 2 * D.ne; e += c.CT) A.edge_uvr[2LL * D.e0 + e] = (Real)A.edge_uv[2LL * D.e0 + e];
     if (threadIdx.x == 0) s.cur = 0;
+    if (c.rank == 0 && threadIdx.x == 0) st->depth_nonpos = 0;  // summed by every warp at the end
     __syncthreads();
     pc.mark(13);
     // the camera-list counting sort's per-warp table borrows the S region (unused until the first
@@ -973,11 +974,21 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
     }
     if (c.rank == 0)
         for (int k = threadIdx.x; k < D.ncam; k += blockDim.x) A.cam_out[D.cam0 + k] = cfin[k];
+    // the final points out, and the active edges whose point is at or behind its camera
+    int nneg = 0;
     for (int p = c.gt; p < D.npt; p += c.CT) {
         const long long gp = D.pt0 + p;
+        double X[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) A.pt_out[4 * gp + k] = A.x[cur][4 * gp + k];
+        for (int k = 0; k < 4; ++k) {
+            X[k] = A.x[cur][4 * gp + k];
+            A.pt_out[4 * gp + k] = X[k];
+        }
+        const int e1 = A.pt_eoff[gp + 1];
+        for (int e = A.pt_eoff[gp]; e < e1; ++e) nneg += depth_nonpositive(cfin[A.edge_cam[e]], X) ? 1 : 0;
     }
+    nneg = __reduce_add_sync(kFull, nneg);
+    if (c.lane == 0 && nneg) atomicAdd(&st->depth_nonpos, nneg);
     if (c.rank == 0 && threadIdx.x == 0) {
         st->initial_cost = chi0_fp64;
         st->final_cost = chi_final;

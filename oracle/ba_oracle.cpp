@@ -983,7 +983,22 @@ public:
         return NAV_BA_OK;
     }
 
+    // Active edges for which EdgeSE3ProjectXYZ::isDepthPositive (OptimizableTypes.hpp:109-113) is
+    // false at the current state: T.map(X)(2) <= 0.
+    int depth_nonpositive() const {
+        int n = 0;
+        for (int i = 0; i < np; ++i)
+            for (int e = pe_off[i]; e < pe_off[i + 1]; ++e) {
+                double Xc[3];
+                const SE3& Tc = T[P.obs_cam[pe[e]]];
+                rotate(Tc.q, &X[3LL * i], Xc);
+                n += Xc[2] + Tc.t[2] <= 0.0 ? 1 : 0;
+            }
+        return n;
+    }
+
     void write_outputs(nav_ba_result* res) const {
+        res->n_depth_nonpositive = depth_nonpositive();
         if (res->cam_pose_out)
             for (int c = 0; c < nc; ++c) pose12_from_se3(T[c], res->cam_pose_out + 12LL * c);
         if (res->points_out) std::memcpy(res->points_out, X.data(), sizeof(double) * 3 * np);

@@ -23,13 +23,17 @@ def triangulate(K, kp1, kp2, R, t):
     return x[:3] / x[3]
 
 
-def check_rt(K, kp1, kp2, R, t, th2, min_parallax_cos, min_triangulated, inlier=None):
+def check_rt(K, kp1, kp2, R, t, th2, min_parallax_cos, min_triangulated, inlier=None, quantities=None):
+    """quantities: a dict that receives, per match, the values CheckRT compares with its thresholds
+    (z1, z2: depths in the two cameras, r1, r2: the point's distances from them; err1, err2: squared
+    reprojection errors; cos: cos-parallax); NaN where a match has no finite point."""
     fx, fy, cx, cy = K
     n = kp1.shape[0]
     pts = np.full((n, 3), np.nan)
     tri = np.zeros(n, bool)
     good = np.zeros(n, bool)
     cosp = np.full(n, np.nan)
+    qv = {k: np.full(n, np.nan) for k in ("z1", "z2", "r1", "r2", "err1", "err2", "cos")}
     O2 = -R.T @ t
     for i in range(n):
         if inlier is not None and not inlier[i]:
@@ -42,17 +46,23 @@ def check_rt(K, kp1, kp2, R, t, th2, min_parallax_cos, min_triangulated, inlier=
         n2 = p - O2
         c = p @ n2 / (np.linalg.norm(p) * np.linalg.norm(n2))
         cosp[i] = c
+        q = R @ p + t
+        e1 = (fx * p[0] / p[2] + cx - kp1[i, 0]) ** 2 + (fy * p[1] / p[2] + cy - kp1[i, 1]) ** 2
+        e2 = (fx * q[0] / q[2] + cx - kp2[i, 0]) ** 2 + (fy * q[1] / q[2] + cy - kp2[i, 1]) ** 2
+        qv["z1"][i], qv["z2"][i], qv["err1"][i], qv["err2"][i], qv["cos"][i] = p[2], q[2], e1, e2, c
+        qv["r1"][i], qv["r2"][i] = np.linalg.norm(p), np.linalg.norm(q)
         if p[2] <= 0 and c < min_parallax_cos:
             continue
-        q = R @ p + t
         if q[2] <= 0 and c < min_parallax_cos:
             continue
-        if (fx * p[0] / p[2] + cx - kp1[i, 0]) ** 2 + (fy * p[1] / p[2] + cy - kp1[i, 1]) ** 2 > th2:
+        if e1 > th2:
             continue
-        if (fx * q[0] / q[2] + cx - kp2[i, 0]) ** 2 + (fy * q[1] / q[2] + cy - kp2[i, 1]) ** 2 > th2:
+        if e2 > th2:
             continue
         tri[i] = True
         good[i] = c < min_parallax_cos
+    if quantities is not None:
+        quantities.update(qv)
     cs = np.sort(cosp[tri])
     par = float(np.degrees(np.arccos(cs[min(min_triangulated, len(cs) - 1)]))) if len(cs) else 0.0
     return pts, tri, good, int(tri.sum()), par

@@ -78,7 +78,7 @@ def test_option_defaults_match_binding(product_lib):
         if name == "reserved":
             continue
         assert getattr(o, name) == getattr(d, name), name
-    assert L.nav_ba_abi_version() == 1
+    assert L.nav_ba_abi_version() == 2
     assert L.nav_ba_status_string(abi.ERR_UNSUPPORTED).decode() == "unsupported size or option"
 
 

@@ -172,6 +172,29 @@ def test_pipelined_batch_reports_first_bad_window(ctx):
     assert g[39].stats["final_cost"] == g1.stats["final_cost"]
 
 
+@pytest.mark.parametrize("precision", [abi.FP64, abi.MIXED])
+def test_batched_512_windows_match_oracle(ctx, precision):
+    """The whole batched workload (512 windows of family 2, seed 1002, 10 LM iterations: the
+    benchmark's batch) in one call, every window's final cost against the FP64 oracle's within
+    1e-6 relative, in both precisions (the oracle runs one window per host thread)."""
+    from concurrent.futures import ThreadPoolExecutor
+    import os
+    wins = Synth(2).windows()
+    assert len(wins) == 512
+    o = workload_options(2)
+    with ThreadPoolExecutor(max(1, os.cpu_count() or 1)) as ex:
+        ref = list(ex.map(lambda w: oracle.solve(w, o), wins))
+    og = workload_options(2, precision=precision)
+    gs = ctx.solve_batched(wins, og)
+    worst = max(abs(g.stats["final_cost"] - r.stats["final_cost"]) / r.stats["final_cost"] for g, r in zip(gs, ref))
+    assert all(g.status == abi.OK for g in gs)
+    assert worst < 1e-6, worst
+    if precision == abi.FP64:
+        assert worst < 1e-12, worst
+        assert all(g.stats["iterations_done"] == r.stats["iterations_done"] and
+                   g.stats["trials_accepted"] == r.stats["trials_accepted"] for g, r in zip(gs, ref))
+
+
 def test_batched_mixed_reaches_fp64_cost(ctx):
     s = Synth(2, n_windows=16, seed=6)
     wins = s.windows()

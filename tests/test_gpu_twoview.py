@@ -14,14 +14,28 @@ TH2 = 4.0 * 1.0  # 4 sigma^2 with sigma = 1 px
 MINPC = 0.99998  # cos of the minimum parallax (about 0.36 deg)
 
 
+def near_threshold(q, i, th2, minpc):
+    """Whether match i sits within rounding of one of CheckRT's thresholds: a squared reprojection
+    error within 1e-6 of th2 (relative), the cos-parallax within 1e-9 of its minimum, or a depth
+    within 1e-9 of zero relative to the point's distance (the GPU's DLT point agrees with the
+    restatement's to 1e-8 relative, so only such matches can be decided differently)."""
+    return bool(abs(q["err1"][i] - th2) <= 1e-6 * th2 or abs(q["err2"][i] - th2) <= 1e-6 * th2 or
+                abs(q["cos"][i] - minpc) <= 1e-9 or abs(q["z1"][i]) <= 1e-9 * q["r1"][i] or
+                abs(q["z2"][i]) <= 1e-9 * q["r2"][i])
+
+
 def test_twoview_matches_oracle(ctx):
     kp1, kp2, inl, Rs, ts, X = scene()
     g = ctx.twoview_check(K, kp1, kp2, Rs, ts, TH2, MINPC, 50, inlier=inl)
     for h in range(len(Rs)):
-        pts, tri, good, ngood, par = ref.check_rt(K, kp1, kp2, Rs[h], ts[h], TH2, MINPC, 50, inl)
+        q = {}
+        pts, tri, good, ngood, par = ref.check_rt(K, kp1, kp2, Rs[h], ts[h], TH2, MINPC, 50, inl, quantities=q)
         assert abs(int(g["n_good"][h]) - ngood) <= 2
         assert np.sum(g["triangulated"][h] != tri) <= 2
         assert np.sum(g["good"][h] != good) <= 2
+        # every decision that differs sits within rounding of a threshold
+        for i in np.nonzero((g["triangulated"][h] != tri) | (g["good"][h] != good))[0]:
+            assert near_threshold(q, i, TH2, MINPC), (h, i, {k: v[i] for k, v in q.items()})
         both = tri & g["triangulated"][h]
         if both.any():
             err = np.abs(g["points"][h][both] - pts[both]) / np.abs(pts[both]).max(axis=1, keepdims=True)

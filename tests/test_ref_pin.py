@@ -101,3 +101,51 @@ def test_gpu_linearize_matches_reference(ctx, fix, name):
         assert rel(e[idx], fix[f"{name}/e"]) < 1e-10
         assert rel(jc[idx], fix[f"{name}/jc"]) < 1e-10
         assert rel(jp[idx], fix[f"{name}/jp"]) < 1e-10
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("solver", [abi.SOLVER_CHOLESKY, abi.SOLVER_PCG])
+def test_gpu_depth_count_matches_reference(ctx, fix, solver):
+    """nav_ba_result.n_depth_nonpositive counts the active edges whose isDepthPositive is false:
+    at the initial state (0 iterations) it equals the reference's own depth tests of the 'behind'
+    case, in the window engine (Cholesky) and the whole-GPU engine (PCG)."""
+    p, idx = _problem("behind", fix)
+    assert idx.size == p.n_obs  # every edge is in the fixture
+    o = abi.default_options(iterations=0, solver=solver)
+    g = ctx.solve(p, o)
+    assert g.status == abi.OK
+    assert g.stats["n_depth_nonpositive"] == int((fix["behind/depth_positive"] == 0).sum())
+    r = oracle.solve(p, o)
+    assert r.stats["n_depth_nonpositive"] == g.stats["n_depth_nonpositive"]
+
+
+@pytest.mark.gpu
+def test_gpu_depth_count_after_solve_matches_oracle(ctx):
+    """After a solve the count is taken at the final state; on the ring workload every point ends in
+    front of its cameras, in both precisions, as in the oracle."""
+    from nav24_gb300.synth import Synth, workload_options
+    p = Synth(0).window(0)
+    r = oracle.solve(p, workload_options(0))
+    for precision in (abi.FP64, abi.MIXED):
+        o = workload_options(0)
+        o.precision = precision
+        g = ctx.solve(p, o)
+        assert g.stats["n_depth_nonpositive"] == r.stats["n_depth_nonpositive"] == 0
+
+
+@pytest.mark.gpu
+def test_gpu_pose_depth_count(ctx, fix):
+    """Motion-only problems report the observations behind the final pose (0 iterations: the
+    reference's depth tests of the 'behind' case, camera by camera)."""
+    p, _ = _problem("behind", fix)
+    dpos = fix["behind/depth_positive"]
+    probs, want = [], []
+    for c in range(p.n_cams):
+        sel = np.nonzero(p.obs_cam == c)[0]
+        if sel.size == 0:
+            continue
+        probs.append(abi.PoseProblem(pose=p.cam_pose[c], points=p.points[p.obs_point[sel]], obs_uv=p.obs_uv[sel],
+                                     intrinsics=p.intrinsics, camera_model=p.camera_model))
+        want.append(int((dpos[sel] == 0).sum()))
+    res = ctx.solve_pose_batched(probs, abi.default_options(iterations=0))
+    assert [st["n_depth_nonpositive"] for _, st in res] == want
