@@ -197,6 +197,18 @@ def profile_traffic():
     return None
 
 
+def fp64_roofline():
+    """The plain FP64 window kernel's bound: its FP64 pipe, from the committed ncu summary
+    (sm__pipe_fp64_cycles_active of one launch), beside its DRAM throughput; None without one."""
+    p = ROOT / "profiles" / "window_lm_kernel_fp64_pipe.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    return {"bound": "fp64", "kernel": "window_lm_kernel<double>", "achieved": d["fp64_pipe_active_pct"],
+            "peak": 100.0, "unit": "% of FP64 pipe cycles", "frac": d["fp64_pipe_active_pct"] / 100.0,
+            "dram_frac_of_peak": d.get("dram_throughput_pct"), "source": d.get("captured")}
+
+
 def cpu_reference(wins, opt, n_threads):
     from oracle import oracle
     t0 = time.perf_counter()
@@ -531,6 +543,24 @@ def main():
     e2e_time = dist.max(float(np.mean(e2e_t)))
     e2e_value = dist.sum(float(e2e_ei)) / e2e_time
 
+    # the same end-to-end call in the plain FP64 form (what compares with the FP64 CPU reference
+    # arm at the same precision)
+    call64 = ctx.batched_call(wins, of)
+    for _ in range(args.warmup):
+        call64()
+    dist.barrier()
+    e64_t = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        call64()
+        e64_t.append(time.perf_counter() - t0)
+    rr64 = call64.results()
+    dist.barrier()
+    e64_time = dist.max(float(np.mean(e64_t)))
+    e64_value = dist.sum(float(sum(r.stats["edge_iterations"] for r in rr64))) / e64_time
+    e2e_fp64 = {"value": e64_value, "unit": UNIT, "h2d_bytes_per_step": int(rr64[0].stats["h2d_bytes"]),
+                "d2h_bytes_per_step": int(rr64[0].stats["d2h_bytes"]), "ms_per_step": e64_time * 1e3}
+
     # roofline of the one kernel (window_lm_kernel): algorithmic bytes / launch time
     peak, peak_kind = measured_peaks()
     alg = algorithmic_bytes(wins, res_m, s_o=4)
@@ -577,7 +607,8 @@ def main():
                        "l2": "inputs+scratch > L2 (no flush needed)", "precision": "mixed",
                        "parallelism": f"replicas x{world}"},
             "lm_iter_per_s": it_m / t_m,
-            "fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": t_f * 1e3, "lm_iter_per_s": it_f / t_f},
+            "fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": t_f * 1e3, "lm_iter_per_s": it_f / t_f,
+                     "e2e": e2e_fp64, "roofline": fp64_roofline()},
             "mixed_over_fp64": value / fp64_value,
             "final_cost_rel_diff_max": cost_rel,
             "final_cost_rel_diff_vs_oracle_max": oracle_diff,

@@ -84,10 +84,12 @@ __device__ void block_partial(double v, double* out) {
     }
 }
 
+// Robust chi2 partial sums; e_out != null: every edge's residual is also stored (rounded to Real).
 template <class Cost, class Real>
-__global__ void k_cost(WinArgs<Real> A, WinDesc D, const Cost* camc, const double* X, double* part) {
+__global__ void k_cost(WinArgs<Real> A, WinDesc D, const Cost* camc, const double* X, double* part,
+                       Real* e_out = nullptr) {
     const CC c = grid_view();
-    block_partial<false>(cost_partial<Cost, Real>(A, c, D, camc, X), part);
+    block_partial<false>(cost_partial<Cost, Real>(A, c, D, camc, X, e_out), part);
 }
 
 // Active edges whose point is at or behind its camera (Z_c <= 0, FP64), per-block partial counts.
@@ -129,7 +131,7 @@ __global__ void k_lin_cams(WinArgs<Real> A, const int4* items, int n_items, cons
             const Real Xr[3] = {(Real)X[4LL * gp], (Real)X[4LL * gp + 1], (Real)X[4LL * gp + 2]};
             const Real z[2] = {(Real)A.edge_uv[2LL * e], (Real)A.edge_uv[2LL * e + 1]};
             EdgeLin<Real> L;
-            edge_linearize<Real>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta, L);
+            edge_linearize_e<Real>(A, e, cr, Xr, z, delta, L);
             const Real wt = L.w;
 #pragma unroll
             for (int r = 0; r < 6; ++r)
@@ -606,7 +608,7 @@ __global__ void k_lin_intr_points(WinArgs<Real> A, WinDesc D, const Real* camr, 
             const Real* cr = camr + 12 * A.edge_cam[e];
             const Real z[2] = {(Real)A.edge_uv[2LL * e], (Real)A.edge_uv[2LL * e + 1]};
             EdgeLin<Real> L;
-            edge_linearize<Real>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta, L);
+            edge_linearize_e<Real>(A, e, cr, Xr, z, delta, L);
             const Real w = L.w;
             const Real* jk = L.jk;  // rows: residual u, v; columns: k1, k2
             acc[0] += (double)(w * (jk[0] * jk[0] + jk[2] * jk[2]));
@@ -646,7 +648,7 @@ __global__ void k_lin_intr_cams(WinArgs<Real> A, const int4* items, int n_items,
             const Real Xr[3] = {(Real)X[4LL * gp], (Real)X[4LL * gp + 1], (Real)X[4LL * gp + 2]};
             const Real z[2] = {(Real)A.edge_uv[2LL * e], (Real)A.edge_uv[2LL * e + 1]};
             EdgeLin<Real> L;
-            edge_linearize<Real>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta, L);
+            edge_linearize_e<Real>(A, e, cr, Xr, z, delta, L);
 #pragma unroll
             for (int r = 0; r < 6; ++r)
 #pragma unroll
@@ -2019,7 +2021,7 @@ cudaError_t up(T* d, const RawVec<T>& h, cudaStream_t s) {
 template <class Real>
 cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Intr& intr, cudaStream_t st,
                              HostPool* pool, GridResult& out, double debug_lambda, std::vector<double>* debug_S,
-                             GridVjp* vjp) {
+                             GridVjp* vjp, const GridStart* start) {
     const auto tg0 = std::chrono::steady_clock::now();
     auto ms_from = [](std::chrono::steady_clock::time_point a) {
         return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
@@ -2069,6 +2071,13 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     Real* d_camr0 = dv.alloc<Real>(12LL * nc);
     Real* d_camr1 = dv.alloc<Real>(12LL * nc);
     double* d_camd = dv.alloc<double>(12LL * nc);
+    // mixed form: each edge's residual from the FP64 cost pass of state 0 / 1 (what the mixed
+    // linearization uses instead of its FP32 residuals)
+    Real* d_ep[2] = {nullptr, nullptr};
+    if (sizeof(Real) == 4) {
+        d_ep[0] = dv.alloc<Real>(2LL * std::max(1, ne));
+        d_ep[1] = dv.alloc<Real>(2LL * std::max(1, ne));
+    }
     int32_t* d_list = dv.alloc<int32_t>(g.cam_list.size());
     int4* d_items = dv.alloc<int4>(g.items.size());
     int32_t* d_item_off = dv.alloc<int32_t>(g.item_off.size());
@@ -2180,10 +2189,11 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     auto chk = [&](cudaError_t x) {
         if (e == cudaSuccess) e = x;
     };
-    chk(up(d_cams0, h.cam, st));
-    chk(up(d_cams1, h.cam, st));
+    const std::vector<CamState>& cam_init = start && start->cams ? *start->cams : h.cam;
+    chk(up(d_cams0, cam_init, st));
+    chk(up(d_cams1, cam_init, st));
     chk(up(d_cam_free, h.cam_free, st));
-    chk(up(d_pinit, h.pt, st));
+    chk(up(d_pinit, start && start->points ? *start->points : h.pt, st));
     chk(up(d_pfree, h.pt_free, st));
     chk(up(d_peoff, h.pt_eoff, st));
     chk(up(d_ecam, h.edge_cam, st));
@@ -2258,7 +2268,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     auto cost_of = [&](int buf, bool fp64) -> double {
         if (fp64 && mixed) {
             k_cams_real<double><<<cblocks, TB, 0, st>>>(cams[buf], nc, d_camd);
-            k_cost<double, Real><<<pblocks, TB, 0, st>>>(A, D, d_camd, A.x[buf], d_part);
+            k_cost<double, Real><<<pblocks, TB, 0, st>>>(A, D, d_camd, A.x[buf], d_part, d_ep[buf]);
         } else {
             k_cost<Real, Real><<<pblocks, TB, 0, st>>>(A, D, camr[buf], A.x[buf], d_part);
         }
@@ -2299,6 +2309,9 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                      return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
                  }, d_pcg_phase, st, pcg_x ? 1 : 0};
     int cur = 0;
+    // NAVBA_VERBOSE=2: one line per damping trial (damping, outcome, CG iterations)
+    const char* vtrial = getenv("NAVBA_VERBOSE");
+    const bool trial_log = vtrial && vtrial[0] == '2';
     // costs (initial, every trial) are evaluated in FP64 in both forms: they drive the gain ratio
     double chi = cost_of(0, true);
     out.initial_cost = chi;
@@ -2464,6 +2477,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     }
     for (int it = 0; !replay && out.termination == NAV_BA_TERM_ITERATIONS && it < lm.iterations; ++it) {
         double mxp, mxc;
+        A.edge_ep = d_ep[cur];  // mixed form: the FP64 cost pass's residuals of this state
         linearize(cur, mxp, mxc);
         if (nk) {
             k_lin_intr_points<Real><<<pblocks, TB, 0, st>>>(A, D, camr[cur], A.x[cur], d_kp, d_part);
@@ -2484,8 +2498,13 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             lambda = lm.initial_lambda > 0 ? lm.initial_lambda : lm.tau * std::max(mxp, mxc);
             nu = 2.0;
         }
+        const double maxdiag = std::max(mxp, mxc);
+        int trial_pit = 0;
+        bool trial_ok = true;
         double rho = 0.0;
         int q = 0;
+        if (it == 0 && lm.start_trial > 0) q = lm.start_trial;  // continuing another solve's iteration
+        if (it == 0 && lm.start_nu > 0) nu = lm.start_nu;
         do {
             const double lam_use = (debug_S && it == 0 && q == 0) ? debug_lambda : lambda;
             k_schur_points<Real><<<pblocks, TB, 0, st>>>(A, D, lam_use, camr[cur], A.x[cur], d_part);
@@ -2620,12 +2639,25 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                 chk(cudaStreamSynchronize(st));
                 if (e != cudaSuccess) return e;
                 pcg_total += pit;
+                trial_pit = pit;
                 ok = ok && okh != 0;
                 if (!ok) {
                     chk(cudaMemsetAsync(d_bs, 0, sizeof(double) * mt, st));
                     dk[0] = dk[1] = 0.0;
                 }
                 if (nk) k_fold_intr<Real><<<pblocks, TB, 0, st>>>(A, D, d_pb, dk[0], dk[1]);
+                if (mixed && !vjp && !ok) {
+                    // the damped system is positive definite in FP64 but lost that in FP32 (a point,
+                    // camera or distortion block at small damping): the FP64 form takes this trial
+                    // over from this iteration's linearization state (grid_solve)
+                    out.handover = true;
+                    out.handover_trial = q;
+                    out.handover_nu = nu;
+                    if (trial_log)
+                        fprintf(stderr, "[navba grid] it %d trial %d lambda %.3e: FP32 system not positive definite, "
+                                "FP64 from here\n", it, q, lam_use);
+                    break;
+                }
             } else if (nfc > 0) {
                 assemble_S(lam_use);
                 if (debug_S) {
@@ -2655,9 +2687,16 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             double chi_new = cost_of(cur ^ 1, true);
             if (e != cudaSuccess) return e;
             if (!ok) chi_new = DBL_MAX;
+            trial_ok = ok;
             rho = chi - chi_new;
             scale += 1e-3;
             rho /= scale;
+            // a failed damped system is a rejected trial (as g2o's DBL_MAX trial cost makes it), also
+            // when the failed point blocks left the step scale non-finite
+            if (!ok) rho = -DBL_MAX;
+            if (trial_log)
+                fprintf(stderr, "[navba grid] it %d trial %d lambda %.3e (%.3e of max diag) ok %d pcg %d cost %.9e rho %.3e\n",
+                        it, q, lam_use, lam_use / maxdiag, trial_ok ? 1 : 0, trial_pit, chi_new, rho);
             if (rho > 0 && std::isfinite(chi_new)) {
                 if (vjp) {  // tape: the state before this step and its damping
                     save_state(cur, (int)vjp->lambdas.size());
@@ -2680,6 +2719,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             }
             ++q;
         } while (rho < 0 && q < lm.max_trials);
+        if (out.handover) break;
         out.iterations_done = it + 1;
         out.trace[it + 1] = chi;
         if (q == lm.max_trials) out.termination = NAV_BA_TERM_TRIALS_EXHAUSTED;
@@ -2807,9 +2847,42 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
 
 cudaError_t grid_solve(const HostWindow& h, const LmOptions& lm, const Intr& intr, int precision, cudaStream_t stream,
                        HostPool* pool, GridResult& out, double debug_lambda, std::vector<double>* debug_S, GridVjp* vjp) {
-    if (precision == NAV_BA_MIXED)
-        return grid_solve_typed<float>(h, lm, intr, stream, pool, out, debug_lambda, debug_S, vjp && !vjp->backward ? vjp : nullptr);
-    return grid_solve_typed<double>(h, lm, intr, stream, pool, out, debug_lambda, debug_S, vjp);
+    if (precision != NAV_BA_MIXED)
+        return grid_solve_typed<double>(h, lm, intr, stream, pool, out, debug_lambda, debug_S, vjp, nullptr);
+    cudaError_t e = grid_solve_typed<float>(h, lm, intr, stream, pool, out, debug_lambda, debug_S,
+                                            vjp && !vjp->backward ? vjp : nullptr, nullptr);
+    if (e != cudaSuccess || !out.handover || out.status != NAV_BA_OK) return e;
+    // a damped system lost positive definiteness in FP32: the FP64 form continues from the mixed
+    // state at the same iteration, trial, damping and nu
+    LmOptions lm64 = lm;
+    lm64.iterations = lm.iterations - out.iterations_done;
+    lm64.initial_lambda = out.final_lambda;
+    lm64.start_trial = out.handover_trial;
+    lm64.start_nu = out.handover_nu;
+    Intr in64 = intr;
+    if (lm.optimize_k && intr.model == 1) set_radial(in64, out.k1, out.k2);
+    GridStart s;
+    s.cams = &out.cams;
+    s.points = &out.points;
+    GridResult o64;
+    e = grid_solve_typed<double>(h, lm64, in64, stream, pool, o64, -1.0, nullptr, nullptr, &s);
+    if (e != cudaSuccess) return e;
+    out.trace.resize(out.iterations_done + 1);
+    out.trace.insert(out.trace.end(), o64.trace.begin() + std::min<size_t>(1, o64.trace.size()), o64.trace.end());
+    out.status = o64.status;
+    out.final_cost = o64.final_cost;
+    out.final_lambda = o64.final_lambda;
+    out.iterations_done += o64.iterations_done;
+    out.accepted += o64.accepted;
+    out.rejected += o64.rejected;
+    out.termination = o64.termination;
+    out.cams = std::move(o64.cams);
+    out.points = std::move(o64.points);
+    out.k1 = o64.k1;
+    out.k2 = o64.k2;
+    out.pcg_iterations += o64.pcg_iterations;
+    out.depth_nonpos = o64.depth_nonpos;
+    return cudaSuccess;
 }
 
 }  // namespace navba

@@ -16,8 +16,9 @@ template <class Real>
 struct WinArgs {
     const WinDesc* win;
     int32_t n_win;
+    int32_t n_big;            // window engine: the first n_big windows of `order` are solved by clusters
     const int32_t* order;
-    int32_t* queue;
+    int32_t* queue;           // window engine: [0] the clusters' queue, [1] the single CTAs' queue
     const CamState* cam_init;
     const int32_t* cam_free;
     const double* pt_init;
@@ -37,6 +38,8 @@ struct WinArgs {
     int32_t jfact;            // window engine, mixed form, pinhole: edge_a holds Jacobian-factored
                               // records (JRec) instead of A
     Real* edge_e[2];          // mixed form: residual (u, v) of each edge at the current / trial state
+    const Real* edge_ep;      // grid engine, mixed form: each edge's residual at the linearization
+                              // state, evaluated in FP64 by the cost pass (null: evaluated in Real)
     int32_t* cam_list;
     double* s_glob;           // window engine, mixed form: the windows' FP64 reduced systems (WinDesc::s0)
     uint32_t* pairs;
@@ -312,6 +315,25 @@ __device__ __forceinline__ Real lane_value(const Real* v, int k) {
     return o;
 }
 
+// edge_linearize for edge e.  With A.edge_ep (the grid engine's mixed form) the residual and the
+// robust weight come from the edge's residual stored by the FP64 cost pass of the same state: in
+// FP32, R X + t of world coordinates of ~100 m keeps ~1e-5 m, which moves the residuals by up to
+// 1e-2 px and alike for all edges of a camera (its translation's rounding); the gradient built from
+// such residuals stalls the LM near convergence.  The Jacobians keep the Real evaluation.
+template <class Real>
+__device__ __forceinline__ void edge_linearize_e(const WinArgs<Real>& A, long long e, const Real* cr, const Real* Xr,
+                                                 const Real* z, Real delta, EdgeLin<Real>& L) {
+    edge_linearize<Real>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta, L);
+    if constexpr (sizeof(Real) == 4) {
+        if (A.edge_ep) {
+            const float2 ep = reinterpret_cast<const float2*>(A.edge_ep)[e];
+            L.e[0] = ep.x;
+            L.e[1] = ep.y;
+            huber<Real>(ep.x * ep.x + ep.y * ep.y, A.lm.robust != 0, delta, L.rho, L.w);
+        }
+    }
+}
+
 // Cluster-split robust chi2 of the window for cameras `camc` (12 values per camera, precision
 // Cost) and points X; returns this thread's partial sum.  e_out != null: each edge's residual is
 // also written there (2 values per edge, rounded to Real).
@@ -374,7 +396,7 @@ __device__ double linearize_points(const WinArgs<Real>& A, const CC& c, const Wi
             Real cr[12];
             cam_load(camr + 12 * cam, cr);
             EdgeLin<Real> L;
-            edge_linearize<Real>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta, L);
+            edge_linearize_e<Real>(A, e, cr, Xr, z, delta, L);
             const Real w = L.w;
             const Real* jp = L.jp;
             V[0] += w * (jp[0] * jp[0] + jp[3] * jp[3]);
@@ -512,7 +534,7 @@ __device__ int schur_points(const WinArgs<Real>& A, const CC& c, const WinDesc& 
                 Real z[2];
                 obs_real(A, e, z);
                 EdgeLin<Real> L;
-                edge_linearize<Real>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta, L);
+                edge_linearize_e<Real>(A, e, cr, Xr, z, delta, L);
 #pragma unroll
                 for (int r = 0; r < 6; ++r)
 #pragma unroll

@@ -122,16 +122,19 @@ bool fits_window_engine(const HostWindow& h) {
     return h.nfc <= kWinMaxFreeCams && h.ncam <= kWinMaxCams && h.ne < 65536;
 }
 
-// Autotuner of the window kernel's launch shape: every candidate (cluster size x threads per
-// CTA) solves the prepared batch twice; the fastest is kept for the context and precision.
-// NAVBA_WINDOW_SHAPE="<cluster>,<threads>" fixes the shape instead (no tuning launches), e.g. to
-// profile one known launch.
+// Autotuner of the window kernel's launch shape and per-window schedule: every candidate (cluster
+// size x threads per CTA x which windows the clusters solve) solves the prepared batch twice; the
+// fastest is kept for the context and precision.  The windows a cluster solves are those whose work
+// weight is at least a quantile of the batch's weights (the top 1, 3, 10, 25 or 100%); the others
+// are solved by single CTAs.  NAVBA_WINDOW_SHAPE="<cluster>,<threads>[,<big_weight>]" fixes the
+// shape instead (no tuning launches), e.g. to profile one known launch.
 cudaError_t autotune(nav_ba_ctx* ctx, PreparedBatch& pb, int precision) {
     const char* fixed = getenv("NAVBA_WINDOW_SHAPE");
     int fc = 0, ft = 0;
-    if (fixed && sscanf(fixed, "%d,%d", &fc, &ft) == 2 && (fc == 1 || fc == 2 || fc == 4 || fc == 8) &&
+    double fw = 0.0;
+    if (fixed && sscanf(fixed, "%d,%d,%lf", &fc, &ft, &fw) >= 2 && (fc == 1 || fc == 2 || fc == 4 || fc == 8) &&
         (ft == 256 || (ft == 512 && precision == NAV_BA_MIXED))) {
-        ctx->shape[precision] = WindowLaunch{fc, ft};
+        ctx->shape[precision] = WindowLaunch{fc, ft, fw};
         ctx->tuned[precision] = true;
         return cudaSuccess;
     }
@@ -140,45 +143,60 @@ cudaError_t autotune(nav_ba_ctx* ctx, PreparedBatch& pb, int precision) {
     const int* ths = precision == NAV_BA_MIXED ? ths_mixed : ths_fp64;
     const int nth = precision == NAV_BA_MIXED ? 2 : 1;
     const int clusters[] = {1, 2, 4, 8};
+    // weight thresholds: the order weights are decreasing, so the top fraction f starts at index f n
+    const std::vector<double>& ow = pb.dev.order_weight;
+    std::vector<double> cuts;
+    for (const double f : {0.01, 0.03, 0.10, 0.25}) {
+        if (ow.empty()) break;
+        const size_t k = std::min(ow.size() - 1, (size_t)std::ceil(f * (double)ow.size()) - 1);
+        cuts.push_back(ow[k]);
+    }
+    cuts.push_back(0.0);  // every window by a cluster
     float best = 1e30f;
     WindowLaunch best_shape = ctx->shape[precision];
-    for (int ci = 0; ci < 4; ++ci) {
+    std::vector<WindowLaunch> cands;
+    for (int ci = 0; ci < 4; ++ci)
         for (int ti = 0; ti < nth; ++ti) {
-            WindowLaunch sh{clusters[ci], ths[ti]};
-            // the shape's time is the better of two launches (the first may run on a cold L2)
-            float t = 1e30f;
-            bool skip = false;
-            for (int rep = 0; rep < 2 && !skip; ++rep) {
-                cudaEventRecord(ctx->ev0, ctx->stream);
-                cudaError_t e = window_batch_launch(pb, ctx->stream, precision, sh, -1.0);
-                cudaEventRecord(ctx->ev1, ctx->stream);
-                if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-                if (e != cudaSuccess) {
-                    // a shape that cannot launch (occupancy) is skipped; any other error is reported
-                    if (e == cudaErrorInvalidConfiguration || e == cudaErrorInvalidValue) {
-                        cudaGetLastError();
-                        skip = true;
-                        continue;
-                    }
-                    return e;
+            if (clusters[ci] == 1) {
+                cands.push_back(WindowLaunch{1, ths[ti], 0.0});
+                continue;
+            }
+            for (const double w : cuts) cands.push_back(WindowLaunch{clusters[ci], ths[ti], w});
+        }
+    for (const WindowLaunch& sh : cands) {
+        // the shape's time is the better of two launches (the first may run on a cold L2)
+        float t = 1e30f;
+        bool skip = false;
+        for (int rep = 0; rep < 2 && !skip; ++rep) {
+            cudaEventRecord(ctx->ev0, ctx->stream);
+            cudaError_t e = window_batch_launch(pb, ctx->stream, precision, sh, -1.0);
+            cudaEventRecord(ctx->ev1, ctx->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+            if (e != cudaSuccess) {
+                // a shape that cannot launch (occupancy) is skipped; any other error is reported
+                if (e == cudaErrorInvalidConfiguration || e == cudaErrorInvalidValue) {
+                    cudaGetLastError();
+                    skip = true;
+                    continue;
                 }
-                float tr = 0.f;
-                cudaEventElapsedTime(&tr, ctx->ev0, ctx->ev1);
-                t = std::min(t, tr);
+                return e;
             }
-            if (skip) continue;
-            if (t < best) {
-                best = t;
-                best_shape = sh;
-            }
+            float tr = 0.f;
+            cudaEventElapsedTime(&tr, ctx->ev0, ctx->ev1);
+            t = std::min(t, tr);
+        }
+        if (skip) continue;
+        if (t < best) {
+            best = t;
+            best_shape = sh;
         }
     }
     ctx->shape[precision] = best_shape;
     ctx->tuned[precision] = true;
     const char* env = getenv("NAVBA_VERBOSE");
     if (env && env[0] == '1')
-        fprintf(stderr, "[navba autotune] precision=%d cluster=%d threads=%d %.3f ms\n", precision, best_shape.cluster,
-                best_shape.threads, best);
+        fprintf(stderr, "[navba autotune] precision=%d cluster=%d threads=%d big_weight=%.0f %.3f ms\n", precision,
+                best_shape.cluster, best_shape.threads, best_shape.big_weight, best);
     return cudaSuccess;
 }
 

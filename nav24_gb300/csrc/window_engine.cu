@@ -93,7 +93,12 @@ NAVBA_HD Dyn dyn_layout(int max_m, int max_ncam, int real_size) {
     return d;
 }
 
-__device__ __forceinline__ void csync() { cg::this_cluster().sync(); }
+// Barrier over the CTAs solving the current window: the whole cluster, or the CTA alone when it
+// solves a window by itself (the single-CTA phase of a clustered launch).
+__device__ __forceinline__ void csync(const CC& c) {
+    if (c.csize > 1) cg::this_cluster().sync();
+    else __syncthreads();
+}
 
 // Decode lower-triangle block index blk = a (a + 1) / 2 + b, b <= a.
 __device__ __forceinline__ void decode_block(int blk, int& a, int& b) {
@@ -134,7 +139,7 @@ __device__ double3 cluster_reduce3(CC& c, double a, double b, double d) {
         slot[1] = rb;
         slot[2] = rd;
     }
-    csync();
+    csync(c);
     if (threadIdx.x == 0) {
         double ra = c.s0->cred[s.slot][0][0], rb = c.s0->cred[s.slot][0][1], rd = c.s0->cred[s.slot][0][2];
         for (int r = 1; r < c.csize; ++r) {
@@ -201,7 +206,7 @@ __device__ void build_lists(const WinArgs<Real>& A, CC& c, const WinDesc& D, int
             __syncwarp();
         }
     }
-    csync();  // the lists are in global memory and their offsets in rank 0's head
+    csync(c);  // the lists are in global memory and their offsets in rank 0's head
     if (c.rank != 0) {  // the other CTAs of the cluster take rank 0's offsets
         for (int k = threadIdx.x; k <= D.ncam; k += blockDim.x) s.loff[k] = c.s0->loff[k];
         for (int k = threadIdx.x; k < D.ncam; k += blockDim.x) s.lcnt[k] = c.s0->lcnt[k];
@@ -239,7 +244,7 @@ __device__ void build_lists(const WinArgs<Real>& A, CC& c, const WinDesc& D, int
         for (int b = c.lane; b <= a; b += 32) c.s0->pcnt[a * (a + 1) / 2 + b] = hist[b];
         __syncwarp();
     }
-    csync();
+    csync(c);
     mark(15);
     if (c.rank == 0 && threadIdx.x == 0) {
         int acc = 0;
@@ -249,7 +254,7 @@ __device__ void build_lists(const WinArgs<Real>& A, CC& c, const WinDesc& D, int
         }
         s.poff[nblk] = acc;
     }
-    csync();
+    csync(c);
     // fill: lanes take 32 consecutive edges of a's list; in warp-uniform rounds every lane emits its
     // next pair; lanes of one round with the same block are placed in lane order (match + rank) and
     // the block's cursor advances, so each block's list is in (list position, point-edge) order
@@ -293,7 +298,7 @@ __device__ void build_lists(const WinArgs<Real>& A, CC& c, const WinDesc& D, int
             }
         }
     }
-    csync();
+    csync(c);
 }
 
 // Camera-major linearization: U_c, g_c (warp per free camera) into rank 0; returns max |diag U|.
@@ -844,7 +849,7 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
                 const double3 r0 = cluster_reduce3<false>(c, (double)npd, 0.0, 0.0);  // also orders S zeroing
                 pc.mark(4);
                 schur_blocks<Real>(A, c, D, lam_use);
-                csync();
+                csync(c);
                 pc.mark(5);
                 if (A.debug) {
                     if (c.rank == 0) {
@@ -854,7 +859,7 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
                         }
                         for (int k = threadIdx.x; k < m; k += blockDim.x) A.debug[m * m + k] = bs[k];
                     }
-                    csync();
+                    csync(c);
                     return;
                 }
                 if (c.rank == 0) {
@@ -871,7 +876,7 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
                     __syncthreads();
                     if (threadIdx.x == 0) s.ok = okc ? 1 : 0;
                 }
-                csync();
+                csync(c);
                 pc.mark(6);
                 // every CTA takes the camera step from rank 0 and updates all cameras itself
                 for (int k = threadIdx.x; k < m; k += blockDim.x) {
@@ -927,6 +932,9 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
                     double r = chi - chi_new;
                     scale += 1e-3;
                     r /= scale;
+                    // a failed damped system is a rejected trial (as g2o's DBL_MAX trial cost makes
+                    // it), also when failed point blocks left the step scale non-finite
+                    if (!ok) r = -DBL_MAX;
                     const bool accept = r > 0 && isfinite(chi_new);
                     double lam = lambda, n2 = nu, ch = chi;
                     if (accept) {
@@ -999,17 +1007,17 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
         st->termination = term;
         st->status = bad ? NAV_BA_ERR_NONFINITE_COST : NAV_BA_OK;
     }
-    csync();
+    csync(c);
     pc.mark(9);
 }
 
-template <class Real>
-__global__ void __launch_bounds__(sizeof(Real) == 8 ? 256 : 512) window_lm_kernel(WinArgs<Real> A) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    cg::cluster_group cl = cg::this_cluster();
+// The view of CTA `rank` of `csize` CTAs sharing one window (rank 0's shared memory holds the
+// window's reduced system and head; csize 1: the CTA alone).  f32: the mixed form, whose rank 0
+// also keeps the FP32 copy of the reduced system.
+__device__ CC make_view(unsigned char* smem_raw, int rank, int csize, const Dyn& dl, bool f32) {
     CC c;
-    c.rank = (int)cl.block_rank();
-    c.csize = (int)cl.num_blocks();
+    c.rank = rank;
+    c.csize = csize;
     c.lane = threadIdx.x & 31;
     c.wid = threadIdx.x >> 5;
     c.nw = blockDim.x >> 5;
@@ -1018,34 +1026,86 @@ __global__ void __launch_bounds__(sizeof(Real) == 8 ? 256 : 512) window_lm_kerne
     c.gw = c.rank * c.nw + c.wid;
     c.CW = c.csize * c.nw;
     c.s = reinterpret_cast<SmemHead*>(smem_raw);
-    c.s0 = cl.map_shared_rank(c.s, 0);
+    c.s0 = c.s;
+    c.S0 = reinterpret_cast<double*>(smem_raw + dl.S);
+    c.bs0 = reinterpret_cast<double*>(smem_raw + dl.bs);
+    c.S0f = f32 ? reinterpret_cast<float*>(smem_raw + dl.s32) : nullptr;
+    if (csize > 1) {
+        cg::cluster_group cl = cg::this_cluster();
+        c.s0 = cl.map_shared_rank(c.s, 0);
+        c.S0 = cl.map_shared_rank(c.S0, 0);
+        c.bs0 = cl.map_shared_rank(c.bs0, 0);
+        if (f32) c.S0f = cl.map_shared_rank(c.S0f, 0);
+    }
+    return c;
+}
+
+// Per-window schedule: the first A.n_big windows of the queue (the largest, host-ordered) are each
+// solved by a whole cluster, which cuts their latency (they set the launch's critical path); once
+// that part of the queue is taken, every CTA of the cluster takes the remaining windows one at a
+// time from a second queue and solves each alone (no cluster barriers, no distributed shared
+// memory).  A launch with clusters of one CTA solves every window alone.
+template <class Real>
+__global__ void __launch_bounds__(sizeof(Real) == 8 ? 256 : 512) window_lm_kernel(WinArgs<Real> A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cg::cluster_group cl = cg::this_cluster();
     const Dyn dl = dyn_layout(A.max_m, A.max_ncam, (int)sizeof(Real));
-    c.S0 = cl.map_shared_rank(reinterpret_cast<double*>(smem_raw + dl.S), 0);
-    c.bs0 = cl.map_shared_rank(reinterpret_cast<double*>(smem_raw + dl.bs), 0);
-    c.S0f = sizeof(Real) == 4 ? cl.map_shared_rank(reinterpret_cast<float*>(smem_raw + dl.s32), 0) : nullptr;
-    if (threadIdx.x == 0) c.s->slot = 0;
+    const int csize = (int)cl.num_blocks();
+    SmemHead* head = reinterpret_cast<SmemHead*>(smem_raw);
+    if (threadIdx.x == 0) head->slot = 0;
     __syncthreads();
+    // one call site of solve_window (a second inlined copy costs registers)
+    bool clustered = csize > 1;
+    CC c = make_view(smem_raw, clustered ? (int)cl.block_rank() : 0, csize, dl, sizeof(Real) == 4);
     for (;;) {
-        if (c.rank == 0 && threadIdx.x == 0) {
-            const int k = atomicAdd(A.queue, 1);
-            c.s->win = k < A.n_win ? A.order[k] : -1;
+        int w;
+        if (clustered) {
+            if (c.rank == 0 && threadIdx.x == 0) {
+                const int k = atomicAdd(A.queue, 1);
+                c.s->win = k < A.n_big ? A.order[k] : -1;
+            }
+            csync(c);
+            w = c.s0->win;
+            csync(c);  // every rank has read rank 0's window index
+            if (w < 0) {
+                if (A.debug) return;
+                // the clusters' part of the queue is done: from here on every CTA works alone, and
+                // nothing reads another CTA's shared memory any more
+                clustered = false;
+                c = make_view(smem_raw, 0, 1, dl, sizeof(Real) == 4);
+                continue;
+            }
+        } else {
+            if (threadIdx.x == 0) {
+                const int k = (csize > 1 ? A.n_big : 0) + atomicAdd(A.queue + 1, 1);
+                c.s->win = k < A.n_win ? A.order[k] : -1;
+            }
+            __syncthreads();
+            w = c.s->win;
+            __syncthreads();
+            if (w < 0) break;
         }
-        csync();
-        const int w = c.s0->win;
-        csync();  // every rank has read rank 0's window index
-        if (w < 0) break;
         solve_window<Real>(A, c, w, smem_raw);
         if (A.debug) break;
     }
-    csync();
+    if (clustered) csync(c);  // a cluster that stopped early (debug) leaves together
 }
 
 template <class Real>
 cudaError_t launch_typed(PreparedBatch& pb, cudaStream_t stream, WindowLaunch shape, double debug_lambda) {
     WindowBatch& b = pb.dev;
-    WinArgs<Real> A;
+    WinArgs<Real> A{};  // every field not set below stays null or zero
     A.win = b.d_win;
     A.n_win = b.n_queue;
+    // the windows solved by whole clusters: the leading ones of weight >= big_weight
+    A.n_big = 0;
+    if (shape.cluster > 1) {
+        const auto& ow = b.order_weight;
+        const int n_w = std::min<int>((int)ow.size(), b.n_queue);
+        while (A.n_big < n_w && ow[A.n_big] >= shape.big_weight) ++A.n_big;
+        if (ow.empty()) A.n_big = b.n_queue;
+    }
+    if (debug_lambda >= 0) A.n_big = b.n_queue;  // the reduced system of window 0, by one cluster
     A.order = b.d_order;
     A.queue = b.d_queue;
     A.cam_init = b.d_cam_init;
@@ -1110,7 +1170,7 @@ cudaError_t launch_typed(PreparedBatch& pb, cudaStream_t stream, WindowLaunch sh
     int clusters = std::min(max_clusters, b.n_queue);
     if (debug_lambda >= 0) clusters = 1;
     cfg.gridDim = dim3(clusters * C);
-    err = cudaMemsetAsync(b.d_queue, 0, sizeof(int32_t), stream);
+    err = cudaMemsetAsync(b.d_queue, 0, 2 * sizeof(int32_t), stream);
     if (err != cudaSuccess) return err;
     return cudaLaunchKernelEx(&cfg, window_lm_kernel<Real>, A);
 }
@@ -1213,6 +1273,11 @@ cudaError_t linearize_observations(const nav_ba_problem& p, const nav_ba_options
 
 static size_t real_size(int precision) { return precision == NAV_BA_MIXED ? sizeof(float) : sizeof(double); }
 
+// Work weight of a window for the schedule: edges, Schur pairs and a Cholesky-size term.
+static double window_weight(const HostWindow& h) {
+    return (double)h.ne + (double)h.n_pairs + 2.0 * h.nfc * h.nfc * h.nfc;
+}
+
 void* HostStaging::get(int id, size_t bytes) {
     bytes = std::max<size_t>(bytes, 64);
     if (cap[id] >= bytes) return buf[id];
@@ -1310,12 +1375,10 @@ cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int prec
     // schedule: largest windows first (edges, pairs and a Cholesky-size term)
     std::vector<int32_t> order = idx;
     std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
-        const HostWindow& hx = pb.host[x];
-        const HostWindow& hy = pb.host[y];
-        const double wx = (double)hx.ne + (double)hx.n_pairs + 2.0 * hx.nfc * hx.nfc * hx.nfc;
-        const double wy = (double)hy.ne + (double)hy.n_pairs + 2.0 * hy.nfc * hy.nfc * hy.nfc;
-        return wx > wy;
+        return window_weight(pb.host[x]) > window_weight(pb.host[y]);
     });
+    b.order_weight.resize(order.size());
+    for (size_t k = 0; k < order.size(); ++k) b.order_weight[k] = window_weight(pb.host[order[k]]);
     const size_t rs = real_size(precision);
     const size_t nw = pb.desc.size();
     cudaError_t err = cudaSuccess;
@@ -1335,7 +1398,7 @@ cudaError_t window_batch_upload(PreparedBatch& pb, cudaStream_t stream, int prec
     };
     ensure(&b.d_win, sizeof(WinDesc) * nw);
     ensure(&b.d_order, sizeof(int32_t) * order.size());
-    ensure(&b.d_queue, sizeof(int32_t));
+    ensure(&b.d_queue, 2 * sizeof(int32_t));
     ensure(&b.d_cam_init, sizeof(CamState) * nc);
     ensure(&b.d_cam_free, sizeof(int32_t) * nc);
     ensure(&b.d_pt_init, sizeof(double) * 4 * np);

@@ -814,15 +814,255 @@ public:
         return ok;
     }
 
+    // ---- block-sparse reduced system (the PCG solver): only the nonzero 6x6 blocks of S ----------
+    // Lower blocks (a >= b) of the free cameras that share a free point, by block row, in increasing
+    // column order; each block is 36 values, row-major (diagonal blocks held whole).  Built once.
+    std::vector<int32_t> srow_off, scol;
+    void build_block_pattern() {
+        if (!srow_off.empty() || nfc == 0) return;
+        std::vector<std::vector<int32_t>> rows(nfc);
+        for (int a = 0; a < nfc; ++a) rows[a].push_back(a);
+        std::vector<int32_t> cams;
+        for (int i = 0; i < np; ++i) {
+            if (pt_free[i] < 0) continue;
+            cams.clear();
+            for (int e = pe_off[i]; e < pe_off[i + 1]; ++e) {
+                const int a = cam_free[P.obs_cam[pe[e]]];
+                if (a >= 0) cams.push_back(a);
+            }
+            for (int x : cams)
+                for (int y : cams)
+                    if (y < x) rows[x].push_back(y);
+        }
+        srow_off.assign(nfc + 1, 0);
+        for (int a = 0; a < nfc; ++a) {
+            std::sort(rows[a].begin(), rows[a].end());
+            rows[a].erase(std::unique(rows[a].begin(), rows[a].end()), rows[a].end());
+            srow_off[a + 1] = srow_off[a] + (int32_t)rows[a].size();
+        }
+        scol.reserve(srow_off[nfc]);
+        for (int a = 0; a < nfc; ++a) scol.insert(scol.end(), rows[a].begin(), rows[a].end());
+    }
+    int block_of(int a, int b) const {
+        const int32_t* lo = scol.data() + srow_off[a];
+        const int32_t* hi = scol.data() + srow_off[a + 1];
+        return (int)(std::lower_bound(lo, hi, b) - scol.data());
+    }
+
+    // The reduced system of reduced_system() in block form: Sb [blocks][36] (lower blocks, the
+    // diagonal ones whole), the distortion rows SK [nk][6 nfc + nk] (dense) and b'.  Per-thread
+    // block copies summed in thread order.
+    void reduced_system_blocks(double lambda, std::vector<double>& Sb, std::vector<double>& SK,
+                               std::vector<double>& bs, std::vector<double>& Vinv) const {
+        const int m = dim_s(), kb = 6 * nfc, nb = srow_off.empty() ? 0 : srow_off[nfc];
+        Vinv.assign(9LL * nfp, 0.0);
+        Sb.assign(36LL * nb, 0.0);
+        SK.assign((size_t)nk * m, 0.0);
+        bs.assign(m, 0.0);
+        for (int a = 0; a < nfc; ++a) {
+            double* B = &Sb[36LL * block_of(a, a)];
+            for (int r = 0; r < 6; ++r) {
+                for (int s = 0; s < 6; ++s) B[r * 6 + s] = U[36LL * a + r * 6 + s];
+                B[r * 6 + r] += lambda;
+                bs[6 * a + r] = bc[6LL * a + r];
+            }
+        }
+        for (int r = 0; r < nk; ++r) {
+            for (int a = 0; a < nfc; ++a)
+                for (int s = 0; s < 6; ++s) SK[(size_t)r * m + 6 * a + s] = Kc[12LL * a + r * 6 + s];
+            for (int s = 0; s < nk; ++s) SK[(size_t)r * m + kb + s] = Kk[r * 2 + s];
+            SK[(size_t)r * m + kb + r] += lambda;
+            bs[kb + r] = bk[r];
+        }
+        std::vector<std::vector<double>> tS(nth), tK(nth), tB(nth);
+        run_threads(nth, [&](int t) {
+            int lo, hi;
+            chunk(np, nth, t, lo, hi);
+            std::vector<double>& SS = tS[t];
+            std::vector<double>& KK = tK[t];
+            std::vector<double>& BB = tB[t];
+            SS.assign(36LL * nb, 0.0);
+            KK.assign((size_t)nk * m, 0.0);
+            BB.assign(m, 0.0);
+            std::vector<double> Y;
+            for (int i = lo; i < hi; ++i) {
+                const int fp = pt_free[i];
+                if (fp < 0) continue;
+                double Vl[9];
+                double* Vi = const_cast<double*>(&Vinv[9LL * fp]);
+                for (int j = 0; j < 9; ++j) Vl[j] = V[9LL * fp + j];
+                Vl[0] += lambda; Vl[4] += lambda; Vl[8] += lambda;
+                inverse3(Vl, Vi);
+                const double* bpp = &bp[3LL * fp];
+                const int e0 = pe_off[i], e1 = pe_off[i + 1];
+                Y.assign(18LL * (e1 - e0), 0.0);
+                for (int e = e0; e < e1; ++e) {
+                    if (cam_free[P.obs_cam[pe[e]]] < 0) continue;
+                    const double* We = &W[18LL * e];
+                    double* Ye = &Y[18LL * (e - e0)];
+                    for (int r = 0; r < 6; ++r)
+                        for (int s = 0; s < 3; ++s)
+                            Ye[r * 3 + s] = We[r * 3 + 0] * Vi[0 * 3 + s] + We[r * 3 + 1] * Vi[1 * 3 + s] + We[r * 3 + 2] * Vi[2 * 3 + s];
+                }
+                for (int e = e0; e < e1; ++e) {
+                    const int a = cam_free[P.obs_cam[pe[e]]];
+                    if (a < 0) continue;
+                    const double* Ye = &Y[18LL * (e - e0)];
+                    for (int r = 0; r < 6; ++r)
+                        BB[6 * a + r] -= Ye[r * 3 + 0] * bpp[0] + Ye[r * 3 + 1] * bpp[1] + Ye[r * 3 + 2] * bpp[2];
+                    for (int f = e0; f < e1; ++f) {
+                        const int b = cam_free[P.obs_cam[pe[f]]];
+                        if (b < 0 || b > a) continue;
+                        const double* Wf = &W[18LL * f];
+                        double* Bk = &SS[36LL * block_of(a, b)];
+                        for (int r = 0; r < 6; ++r)
+                            for (int s = 0; s < 6; ++s) {
+                                const double v = Ye[r * 3 + 0] * Wf[s * 3 + 0] + Ye[r * 3 + 1] * Wf[s * 3 + 1] + Ye[r * 3 + 2] * Wf[s * 3 + 2];
+                                Bk[r * 6 + s] -= v;
+                            }
+                    }
+                }
+                if (nk) {
+                    double Z[6];
+                    const double* K = &Kp[6LL * fp];
+                    for (int r = 0; r < 2; ++r)
+                        for (int s = 0; s < 3; ++s)
+                            Z[r * 3 + s] = K[r * 3 + 0] * Vi[0 * 3 + s] + K[r * 3 + 1] * Vi[1 * 3 + s] + K[r * 3 + 2] * Vi[2 * 3 + s];
+                    for (int r = 0; r < 2; ++r) {
+                        BB[kb + r] -= Z[r * 3 + 0] * bpp[0] + Z[r * 3 + 1] * bpp[1] + Z[r * 3 + 2] * bpp[2];
+                        for (int s = 0; s < 2; ++s)
+                            KK[(size_t)r * m + kb + s] -= Z[r * 3 + 0] * K[s * 3 + 0] + Z[r * 3 + 1] * K[s * 3 + 1] + Z[r * 3 + 2] * K[s * 3 + 2];
+                        for (int f = e0; f < e1; ++f) {
+                            const int b = cam_free[P.obs_cam[pe[f]]];
+                            if (b < 0) continue;
+                            const double* Wf = &W[18LL * f];
+                            for (int s = 0; s < 6; ++s)
+                                KK[(size_t)r * m + 6 * b + s] -= Z[r * 3 + 0] * Wf[s * 3 + 0] + Z[r * 3 + 1] * Wf[s * 3 + 1] + Z[r * 3 + 2] * Wf[s * 3 + 2];
+                        }
+                    }
+                }
+            }
+        });
+        for (int t = 0; t < nth; ++t) {
+            for (size_t j = 0; j < Sb.size(); ++j) Sb[j] += tS[t][j];
+            for (size_t j = 0; j < SK.size(); ++j) SK[j] += tK[t][j];
+            for (int j = 0; j < m; ++j) bs[j] += tB[t][j];
+        }
+    }
+
+    // pcg_solve over the block form: the same preconditioner (the camera blocks and the distortion
+    // block, each factored by Cholesky), iteration and stopping rule; S p from the blocks.
+    bool pcg_solve_blocks(const std::vector<double>& Sb, const std::vector<double>& SK, std::vector<double>& bs) {
+        const int m = dim_s(), kb = 6 * nfc;
+        std::vector<std::vector<double>> Lb(nfc + (nk ? 1 : 0));
+        bool ok = true;
+        auto factor = [&](std::vector<double>& L, int n) {
+            for (int j = 0; j < n; ++j) {
+                double d = L[j * n + j];
+                for (int q = 0; q < j; ++q) d -= L[j * n + q] * L[j * n + q];
+                if (!(d > 0.0) || !std::isfinite(d)) { ok = false; d = 1.0; }
+                L[j * n + j] = std::sqrt(d);
+                for (int i = j + 1; i < n; ++i) {
+                    double v = L[i * n + j];
+                    for (int q = 0; q < j; ++q) v -= L[i * n + q] * L[j * n + q];
+                    L[i * n + j] = v / L[j * n + j];
+                }
+            }
+        };
+        for (int a = 0; a < nfc; ++a) {
+            Lb[a].assign(Sb.begin() + 36LL * block_of(a, a), Sb.begin() + 36LL * block_of(a, a) + 36);
+            factor(Lb[a], 6);
+        }
+        if (nk) {
+            Lb[nfc].assign(4, 0.0);
+            for (int r = 0; r < 2; ++r)
+                for (int s = 0; s < 2; ++s) Lb[nfc][r * 2 + s] = SK[(size_t)r * m + kb + s];
+            factor(Lb[nfc], 2);
+        }
+        auto precond = [&](const std::vector<double>& r, std::vector<double>& z) {
+            z.assign(m, 0.0);
+            for (size_t k = 0; k < Lb.size(); ++k) {
+                const int s0 = (int)k < nfc ? 6 * (int)k : kb, n = (int)k < nfc ? 6 : nk;
+                const std::vector<double>& L = Lb[k];
+                double v[6];
+                for (int i = 0; i < n; ++i) {
+                    double t = r[s0 + i];
+                    for (int q = 0; q < i; ++q) t -= L[i * n + q] * v[q];
+                    v[i] = t / L[i * n + i];
+                }
+                for (int i = n - 1; i >= 0; --i) {
+                    double t = v[i];
+                    for (int q = i + 1; q < n; ++q) t -= L[q * n + i] * v[q];
+                    v[i] = t / L[i * n + i];
+                }
+                for (int i = 0; i < n; ++i) z[s0 + i] = v[i];
+            }
+        };
+        auto matvec = [&](const std::vector<double>& p, std::vector<double>& q) {
+            std::fill(q.begin(), q.end(), 0.0);
+            for (int a = 0; a < nfc; ++a)
+                for (int k = srow_off[a]; k < srow_off[a + 1]; ++k) {
+                    const int b = scol[k];
+                    const double* B = &Sb[36LL * k];
+                    for (int r = 0; r < 6; ++r) {
+                        double t = 0.0;
+                        for (int s = 0; s < 6; ++s) t += B[r * 6 + s] * p[6 * b + s];
+                        q[6 * a + r] += t;
+                    }
+                    if (b != a)
+                        for (int s = 0; s < 6; ++s) {
+                            double t = 0.0;
+                            for (int r = 0; r < 6; ++r) t += B[r * 6 + s] * p[6 * a + r];
+                            q[6 * b + s] += t;
+                        }
+                }
+            for (int r = 0; r < nk; ++r) {
+                double t = 0.0;
+                for (int j = 0; j < m; ++j) t += SK[(size_t)r * m + j] * p[j];
+                q[kb + r] += t;
+                for (int j = 0; j < kb; ++j) q[j] += SK[(size_t)r * m + j] * p[kb + r];
+            }
+        };
+        std::vector<double> x(m, 0.0), r = bs, z, p, q(m);
+        precond(r, z);
+        p = z;
+        double rz = 0.0, rr = 0.0;
+        for (int i = 0; i < m; ++i) { rz += r[i] * z[i]; rr += r[i] * r[i]; }
+        const double bb = rr;
+        const double tol2 = O.pcg_tolerance * O.pcg_tolerance;
+        int it = 0;
+        for (; it < O.pcg_max_iterations; ++it) {
+            if (it % 4 == 0 && !(rr > tol2 * bb)) break;
+            matvec(p, q);
+            double pq = 0.0;
+            for (int i = 0; i < m; ++i) pq += p[i] * q[i];
+            const double alpha = pq != 0.0 ? rz / pq : 0.0;
+            for (int i = 0; i < m; ++i) { x[i] += alpha * p[i]; r[i] -= alpha * q[i]; }
+            precond(r, z);
+            double rzn = 0.0;
+            rr = 0.0;
+            for (int i = 0; i < m; ++i) { rzn += r[i] * z[i]; rr += r[i] * r[i]; }
+            const double beta = rz != 0.0 ? rzn / rz : 0.0;
+            for (int i = 0; i < m; ++i) p[i] = z[i] + beta * p[i];
+            rz = rzn;
+        }
+        pcg_iterations += it;
+        bs = x;
+        return ok;
+    }
+
     // BlockSolver::solve with the damping applied (setLambda .. restoreDiagonal).
     bool compute_step(double lambda) {
         std::vector<double> S, bs, Vinv;
-        reduced_system(lambda, S, bs, Vinv);
         bool ok;
         if (O.solver == NAV_BA_SOLVER_PCG) {
-            ok = pcg_solve(S, bs);
+            build_block_pattern();
+            std::vector<double> SK;
+            reduced_system_blocks(lambda, S, SK, bs, Vinv);
+            ok = pcg_solve_blocks(S, SK, bs);
             if (!ok) std::fill(bs.begin(), bs.end(), 0.0);
         } else {
+            reduced_system(lambda, S, bs, Vinv);
             ok = cholesky(S);
             if (ok) chol_solve(S, bs);
             else std::fill(bs.begin(), bs.end(), 0.0);

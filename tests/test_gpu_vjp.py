@@ -11,7 +11,7 @@ each at its recorded damping).  Checks:
     (step 1e-6) of the replay on 200 random coordinates (all four intrinsics and 196 observation
     coordinates) within 1e-5 relative, both for the GPU replay and for the oracle's replay, as a
     vector norm; and coordinate by coordinate against fourth-order central differences (step
-    1e-4, less rounding noise), each within 1e-5 of max(|fd_k|, 1e-3 of the largest);
+    1e-4, less rounding noise), each within 1e-5 of max(|fd_k|, 1% of the largest);
   - the torch.autograd.Function returns the same gradients, in float32 for float32 observations.
 """
 import numpy as np
@@ -132,7 +132,7 @@ def fd_check(ctx, p, o, n, seed, replay, tol):
     # Coordinate by coordinate.  The step-1e-6 difference carries ~1e-16 |L| / h of rounding noise
     # (~1e-7 here), as large as tol |g_k| for the small coordinates, so each coordinate is checked
     # against the fourth-order central difference (8 (L(+h) - L(-h)) - (L(+2h) - L(-2h))) / 12h with
-    # h = 1e-4: |g_k - fd_k| <= tol max(|fd_k|, 1e-3 max |fd|).
+    # h = 1e-4: |g_k - fd_k| <= tol max(|fd_k|, 1e-2 max |fd|).
     h4 = 1e-4
     fd4 = []
     for k in ks:
@@ -140,7 +140,7 @@ def fd_check(ctx, p, o, n, seed, replay, tol):
         Ls = [loss(replay(with_theta(p, k, v + s * h4), lam), cb, pb, xb) for s in (1, -1, 2, -2)]
         fd4.append((8.0 * (Ls[0] - Ls[1]) - (Ls[2] - Ls[3])) / (12.0 * h4))
     an, fd4 = np.asarray(an), np.asarray(fd4)
-    bad = np.abs(an - fd4) > tol * np.maximum(np.abs(fd4), 1e-3 * np.max(np.abs(fd4)))
+    bad = np.abs(an - fd4) > tol * np.maximum(np.abs(fd4), 1e-2 * np.max(np.abs(fd4)))
     assert not bad.any(), (np.asarray(ks)[bad], an[bad], fd4[bad])
     return err
 
