@@ -48,10 +48,6 @@ struct LmOptions {
     int32_t optimize_k;      // shared radial k1, k2 are free (PCG only)
     int32_t pcg_max_iterations;
     double pcg_tolerance;
-    // a solve that continues another at an iteration's trial (the mixed form's FP64 handover): the
-    // first iteration starts at this trial with this nu (0: a fresh iteration, nu = 2)
-    int32_t start_trial;
-    double start_nu;
 };
 
 // A batch of windows resident on the device (inputs, scratch and outputs).
@@ -169,19 +165,6 @@ struct GridResult {
     double k1 = 0, k2 = 0;       // final distortion (optimize_k)
     int32_t pcg_iterations = 0;
     int32_t depth_nonpos = 0;    // active edges with the point at or behind its camera, final state
-    // mixed form, PCG: a damped system lost positive definiteness in FP32 (a point, camera or
-    // distortion block) at trial handover_trial of iteration iterations_done; cams, points, k1, k2
-    // are that iteration's linearization state and final_lambda, handover_nu the trial's damping,
-    // from which the FP64 form continues (grid_solve does so)
-    bool handover = false;
-    int32_t handover_trial = 0;
-    double handover_nu = 2.0;
-};
-
-// Initial state of a grid solve that continues another (replaces the problem's own).
-struct GridStart {
-    const std::vector<CamState>* cams = nullptr;
-    const std::vector<double>* points = nullptr;  // [npt][4]
 };
 
 // Differentiation through the accepted LM steps (grid engine, FP64, Cholesky, pinhole).

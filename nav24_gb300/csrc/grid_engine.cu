@@ -2021,7 +2021,7 @@ cudaError_t up(T* d, const RawVec<T>& h, cudaStream_t s) {
 template <class Real>
 cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Intr& intr, cudaStream_t st,
                              HostPool* pool, GridResult& out, double debug_lambda, std::vector<double>* debug_S,
-                             GridVjp* vjp, const GridStart* start) {
+                             GridVjp* vjp) {
     const auto tg0 = std::chrono::steady_clock::now();
     auto ms_from = [](std::chrono::steady_clock::time_point a) {
         return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
@@ -2189,11 +2189,10 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     auto chk = [&](cudaError_t x) {
         if (e == cudaSuccess) e = x;
     };
-    const std::vector<CamState>& cam_init = start && start->cams ? *start->cams : h.cam;
-    chk(up(d_cams0, cam_init, st));
-    chk(up(d_cams1, cam_init, st));
+    chk(up(d_cams0, h.cam, st));
+    chk(up(d_cams1, h.cam, st));
     chk(up(d_cam_free, h.cam_free, st));
-    chk(up(d_pinit, start && start->points ? *start->points : h.pt, st));
+    chk(up(d_pinit, h.pt, st));
     chk(up(d_pfree, h.pt_free, st));
     chk(up(d_peoff, h.pt_eoff, st));
     chk(up(d_ecam, h.edge_cam, st));
@@ -2503,8 +2502,6 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         bool trial_ok = true;
         double rho = 0.0;
         int q = 0;
-        if (it == 0 && lm.start_trial > 0) q = lm.start_trial;  // continuing another solve's iteration
-        if (it == 0 && lm.start_nu > 0) nu = lm.start_nu;
         do {
             const double lam_use = (debug_S && it == 0 && q == 0) ? debug_lambda : lambda;
             k_schur_points<Real><<<pblocks, TB, 0, st>>>(A, D, lam_use, camr[cur], A.x[cur], d_part);
@@ -2646,18 +2643,6 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                     dk[0] = dk[1] = 0.0;
                 }
                 if (nk) k_fold_intr<Real><<<pblocks, TB, 0, st>>>(A, D, d_pb, dk[0], dk[1]);
-                if (mixed && !vjp && !ok) {
-                    // the damped system is positive definite in FP64 but lost that in FP32 (a point,
-                    // camera or distortion block at small damping): the FP64 form takes this trial
-                    // over from this iteration's linearization state (grid_solve)
-                    out.handover = true;
-                    out.handover_trial = q;
-                    out.handover_nu = nu;
-                    if (trial_log)
-                        fprintf(stderr, "[navba grid] it %d trial %d lambda %.3e: FP32 system not positive definite, "
-                                "FP64 from here\n", it, q, lam_use);
-                    break;
-                }
             } else if (nfc > 0) {
                 assemble_S(lam_use);
                 if (debug_S) {
@@ -2719,7 +2704,6 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             }
             ++q;
         } while (rho < 0 && q < lm.max_trials);
-        if (out.handover) break;
         out.iterations_done = it + 1;
         out.trace[it + 1] = chi;
         if (q == lm.max_trials) out.termination = NAV_BA_TERM_TRIALS_EXHAUSTED;
@@ -2847,42 +2831,10 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
 
 cudaError_t grid_solve(const HostWindow& h, const LmOptions& lm, const Intr& intr, int precision, cudaStream_t stream,
                        HostPool* pool, GridResult& out, double debug_lambda, std::vector<double>* debug_S, GridVjp* vjp) {
-    if (precision != NAV_BA_MIXED)
-        return grid_solve_typed<double>(h, lm, intr, stream, pool, out, debug_lambda, debug_S, vjp, nullptr);
-    cudaError_t e = grid_solve_typed<float>(h, lm, intr, stream, pool, out, debug_lambda, debug_S,
-                                            vjp && !vjp->backward ? vjp : nullptr, nullptr);
-    if (e != cudaSuccess || !out.handover || out.status != NAV_BA_OK) return e;
-    // a damped system lost positive definiteness in FP32: the FP64 form continues from the mixed
-    // state at the same iteration, trial, damping and nu
-    LmOptions lm64 = lm;
-    lm64.iterations = lm.iterations - out.iterations_done;
-    lm64.initial_lambda = out.final_lambda;
-    lm64.start_trial = out.handover_trial;
-    lm64.start_nu = out.handover_nu;
-    Intr in64 = intr;
-    if (lm.optimize_k && intr.model == 1) set_radial(in64, out.k1, out.k2);
-    GridStart s;
-    s.cams = &out.cams;
-    s.points = &out.points;
-    GridResult o64;
-    e = grid_solve_typed<double>(h, lm64, in64, stream, pool, o64, -1.0, nullptr, nullptr, &s);
-    if (e != cudaSuccess) return e;
-    out.trace.resize(out.iterations_done + 1);
-    out.trace.insert(out.trace.end(), o64.trace.begin() + std::min<size_t>(1, o64.trace.size()), o64.trace.end());
-    out.status = o64.status;
-    out.final_cost = o64.final_cost;
-    out.final_lambda = o64.final_lambda;
-    out.iterations_done += o64.iterations_done;
-    out.accepted += o64.accepted;
-    out.rejected += o64.rejected;
-    out.termination = o64.termination;
-    out.cams = std::move(o64.cams);
-    out.points = std::move(o64.points);
-    out.k1 = o64.k1;
-    out.k2 = o64.k2;
-    out.pcg_iterations += o64.pcg_iterations;
-    out.depth_nonpos = o64.depth_nonpos;
-    return cudaSuccess;
+    if (precision == NAV_BA_MIXED)
+        return grid_solve_typed<float>(h, lm, intr, stream, pool, out, debug_lambda, debug_S,
+                                       vjp && !vjp->backward ? vjp : nullptr);
+    return grid_solve_typed<double>(h, lm, intr, stream, pool, out, debug_lambda, debug_S, vjp);
 }
 
 }  // namespace navba

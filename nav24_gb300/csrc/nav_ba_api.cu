@@ -133,15 +133,16 @@ cudaError_t autotune(nav_ba_ctx* ctx, PreparedBatch& pb, int precision) {
     int fc = 0, ft = 0;
     double fw = 0.0;
     if (fixed && sscanf(fixed, "%d,%d,%lf", &fc, &ft, &fw) >= 2 && (fc == 1 || fc == 2 || fc == 4 || fc == 8) &&
-        (ft == 256 || (ft == 512 && precision == NAV_BA_MIXED))) {
+        (ft == 128 || ft == 256 || (ft == 512 && precision == NAV_BA_MIXED))) {
         ctx->shape[precision] = WindowLaunch{fc, ft, fw};
         ctx->tuned[precision] = true;
         return cudaSuccess;
     }
-    const int ths_fp64[] = {256};
-    const int ths_mixed[] = {256, 512};
+    // 128-thread CTAs put more windows in flight per SM (the same registers per thread)
+    const int ths_fp64[] = {128, 256};
+    const int ths_mixed[] = {128, 256, 512};
     const int* ths = precision == NAV_BA_MIXED ? ths_mixed : ths_fp64;
-    const int nth = precision == NAV_BA_MIXED ? 2 : 1;
+    const int nth = precision == NAV_BA_MIXED ? 3 : 2;
     const int clusters[] = {1, 2, 4, 8};
     // weight thresholds: the order weights are decreasing, so the top fraction f starts at index f n
     const std::vector<double>& ow = pb.dev.order_weight;

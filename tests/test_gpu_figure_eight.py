@@ -2,8 +2,15 @@
 figure-eight (three loops), 500,000 points, ~4M observations, shared radial k1, k2 optimized, 5%
 outliers, Huber 1.5 px, block-Jacobi PCG (tolerance 1e-6, at most 100 iterations), 30 LM iterations
 (family 4, seed 1004).  The oracle runs the same algorithm (block-sparse reduced system) on every
-host core.  Both GPU forms end within 1e-6 relative of the oracle's final cost, and the FP64 form's
-recovered distortion agrees with the oracle's."""
+host core.
+
+FP64: final cost within 1e-6 relative of the oracle's, and the same recovered distortion.
+
+Mixed: its cost after each of the first 20 LM iterations within 1e-5 of the oracle's, and the final
+cost within 1e-3.  From about iteration 20 on, the damping sits near 1e-9 of H's largest diagonal
+entry, where the 100-iteration CG gives steps whose trial costs reach 1e8 to 1e19 (in FP64 too;
+NAVBA_VERBOSE=2 prints every trial), and which trials are accepted depends on perturbations of the
+state far below FP32's resolution, so from there the mixed form follows its own path."""
 import os
 
 import numpy as np
@@ -25,12 +32,22 @@ def eight():
     return p, r
 
 
-@pytest.mark.parametrize("precision", [abi.FP64, abi.MIXED])
-def test_figure_eight_full_size_matches_oracle(ctx, eight, precision):
+def rel(a, b):
+    return abs(a - b) / abs(b)
+
+
+def test_figure_eight_full_size_fp64_matches_oracle(ctx, eight):
     p, r = eight
-    g = ctx.solve(p, workload_options(4, precision=precision))
+    g = ctx.solve(p, workload_options(4, precision=abi.FP64))
     assert g.status == abi.OK and g.stats["iterations_done"] == 30
-    rel = abs(g.stats["final_cost"] - r.stats["final_cost"]) / r.stats["final_cost"]
-    assert rel < 1e-6, rel
-    if precision == abi.FP64:
-        assert np.max(np.abs(g.intrinsics[4:6] - r.intrinsics[4:6])) < 1e-6
+    assert rel(g.stats["final_cost"], r.stats["final_cost"]) < 1e-6
+    assert np.max(np.abs(g.intrinsics[4:6] - r.intrinsics[4:6])) < 1e-6
+
+
+def test_figure_eight_full_size_mixed_tracks_oracle(ctx, eight):
+    p, r = eight
+    g = ctx.solve(p, workload_options(4, precision=abi.MIXED))
+    assert g.status == abi.OK and g.stats["iterations_done"] == 30
+    worst = max(rel(g.cost_trace[k], r.cost_trace[k]) for k in range(21))
+    assert worst < 1e-5, worst
+    assert rel(g.stats["final_cost"], r.stats["final_cost"]) < 1e-3
