@@ -104,8 +104,6 @@ struct WindowLaunch {
     int32_t cluster = 4;      // CTAs cooperating on one large window (1, 2, 4 or 8)
     int32_t threads = 256;    // threads per CTA
     double big_weight = 0.0;
-    int32_t resident = 0;     // mixed form: 3 = the build compiled for three 256-thread CTAs per SM
-                              // (85 registers per thread); 0 = the default build
 };
 
 // Host resources of a context reused across calls: pinned buffers (inputs staged for upload,

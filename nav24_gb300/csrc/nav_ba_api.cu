@@ -132,10 +132,9 @@ cudaError_t autotune(nav_ba_ctx* ctx, PreparedBatch& pb, int precision) {
     const char* fixed = getenv("NAVBA_WINDOW_SHAPE");
     int fc = 0, ft = 0;
     double fw = 0.0;
-    int fr = 0;
-    if (fixed && sscanf(fixed, "%d,%d,%lf,%d", &fc, &ft, &fw, &fr) >= 2 && (fc == 1 || fc == 2 || fc == 4 || fc == 8) &&
+    if (fixed && sscanf(fixed, "%d,%d,%lf", &fc, &ft, &fw) >= 2 && (fc == 1 || fc == 2 || fc == 4 || fc == 8) &&
         (ft == 128 || ft == 256 || (ft == 512 && precision == NAV_BA_MIXED))) {
-        ctx->shape[precision] = WindowLaunch{fc, ft, fw, fr == 3 ? 3 : 0};
+        ctx->shape[precision] = WindowLaunch{fc, ft, fw};
         ctx->tuned[precision] = true;
         return cudaSuccess;
     }
@@ -160,14 +159,11 @@ cudaError_t autotune(nav_ba_ctx* ctx, PreparedBatch& pb, int precision) {
     for (int ci = 0; ci < 4; ++ci)
         for (int ti = 0; ti < nth; ++ti) {
             if (clusters[ci] == 1) {
-                cands.push_back(WindowLaunch{1, ths[ti], 0.0, 0});
+                cands.push_back(WindowLaunch{1, ths[ti], 0.0});
                 continue;
             }
-            for (const double w : cuts) cands.push_back(WindowLaunch{clusters[ci], ths[ti], w, 0});
+            for (const double w : cuts) cands.push_back(WindowLaunch{clusters[ci], ths[ti], w});
         }
-    // mixed form: the build for three resident 256-thread CTAs per SM (fewer registers, more windows
-    // in flight), single CTAs per window
-    if (precision == NAV_BA_MIXED) cands.push_back(WindowLaunch{1, 256, 0.0, 3});
     for (const WindowLaunch& sh : cands) {
         // the shape's time is the better of two launches (the first may run on a cold L2)
         float t = 1e30f;
@@ -200,8 +196,8 @@ cudaError_t autotune(nav_ba_ctx* ctx, PreparedBatch& pb, int precision) {
     ctx->tuned[precision] = true;
     const char* env = getenv("NAVBA_VERBOSE");
     if (env && env[0] == '1')
-        fprintf(stderr, "[navba autotune] precision=%d cluster=%d threads=%d big_weight=%.0f resident=%d %.3f ms\n",
-                precision, best_shape.cluster, best_shape.threads, best_shape.big_weight, best_shape.resident, best);
+        fprintf(stderr, "[navba autotune] precision=%d cluster=%d threads=%d big_weight=%.0f %.3f ms\n", precision,
+                best_shape.cluster, best_shape.threads, best_shape.big_weight, best);
     return cudaSuccess;
 }
 

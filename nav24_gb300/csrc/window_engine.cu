@@ -1045,9 +1045,8 @@ __device__ CC make_view(unsigned char* smem_raw, int rank, int csize, const Dyn&
 // that part of the queue is taken, every CTA of the cluster takes the remaining windows one at a
 // time from a second queue and solves each alone (no cluster barriers, no distributed shared
 // memory).  A launch with clusters of one CTA solves every window alone.
-template <class Real, int kMinResident>
-__global__ void __launch_bounds__(kMinResident > 1 ? 256 : (sizeof(Real) == 8 ? 256 : 512), kMinResident)
-    window_lm_kernel(WinArgs<Real> A) {
+template <class Real>
+__global__ void __launch_bounds__(sizeof(Real) == 8 ? 256 : 512) window_lm_kernel(WinArgs<Real> A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cg::cluster_group cl = cg::this_cluster();
     const Dyn dl = dyn_layout(A.max_m, A.max_ncam, (int)sizeof(Real));
@@ -1150,13 +1149,7 @@ cudaError_t launch_typed(PreparedBatch& pb, cudaStream_t stream, WindowLaunch sh
     const int T = shape.threads;
     if (T % 32 != 0 || T < 64 || T > (sizeof(Real) == 8 ? 256 : 512)) return cudaErrorInvalidConfiguration;
     const size_t smem = dyn_layout(A.max_m, A.max_ncam, (int)sizeof(Real)).total;
-    // the build for three resident CTAs per SM (mixed form, <= 256 threads) or the default one
-    const bool three = sizeof(Real) == 4 && shape.resident == 3;
-    if (three && T > 256) return cudaErrorInvalidConfiguration;
-    const void* kern = (const void*)window_lm_kernel<Real, 1>;
-    if constexpr (sizeof(Real) == 4) {
-        if (three) kern = (const void*)window_lm_kernel<Real, 3>;
-    }
+    const void* kern = (const void*)window_lm_kernel<Real>;
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
     cudaLaunchConfig_t cfg = {};
