@@ -17,6 +17,7 @@ using namespace navba;
 
 // Parts of a pipelined batched solve (8 measured slower: 64-window parts leave host workers idle).
 constexpr int kSolveParts = 4;
+constexpr int kPart0Cluster = 4;  // CTAs per window in the first part of a pipelined batch
 
 struct nav_ba_ctx {
     int device = 0;
@@ -493,6 +494,18 @@ nav_ba_status solve_pipelined(nav_ba_ctx* ctx, const nav_ba_problem* probs, int 
     // are the longest) is small, so the device starts on it early; later parts grow while the device
     // is busy (4 parts: 1/16, 3/16, 5/16, 7/16)
     auto part_lo = [&](int k) { return (int)((long long)n * k * k / (kSolveParts * kSolveParts)); };
+    // the first part holds the largest windows and has the device nearly to itself until the later
+    // parts are uploaded: each of its windows is solved by a cluster of CTAs, which shortens those
+    // windows (the batch's critical path) and fills the otherwise idle SMs of the ramp.
+    // NAVBA_PART0_SHAPE="<cluster>,<threads>" sets it (diagnostics).
+    WindowLaunch part0_shape{kPart0Cluster, 256, 0.0};
+    {
+        const char* ps = getenv("NAVBA_PART0_SHAPE");
+        int pc = 0, pt = 0;
+        if (ps && sscanf(ps, "%d,%d", &pc, &pt) == 2 && (pc == 1 || pc == 2 || pc == 4 || pc == 8) &&
+            (pt == 128 || pt == 256))
+            part0_shape = WindowLaunch{pc, pt, 0.0};
+    }
     double t_build = 0.0;
     // NAVBA_VERBOSE: the device timeline of the parts (upload start, kernel start and end per part)
     const char* verbose = getenv("NAVBA_VERBOSE");
@@ -527,7 +540,8 @@ nav_ba_status solve_pipelined(nav_ba_ctx* ctx, const nav_ba_problem* probs, int 
                                             &why, false);
         if (e != cudaSuccess) return cuda_status(ctx, e, "upload");
         if (timeline) cudaEventRecord(tev[2 + 3 * k], part.stream);
-        e = window_batch_launch(pbs[k], part.stream, o->precision, ctx->shape[o->precision], -1.0);
+        e = window_batch_launch(pbs[k], part.stream, o->precision, k == 0 ? part0_shape : ctx->shape[o->precision],
+                                -1.0);
         if (e != cudaSuccess) return cuda_status(ctx, e, "window kernel");
         if (timeline) cudaEventRecord(tev[3 + 3 * k], part.stream);
         launched = k + 1;
