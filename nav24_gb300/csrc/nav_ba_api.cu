@@ -17,7 +17,10 @@ using namespace navba;
 
 // Parts of a pipelined batched solve (8 measured slower: 64-window parts leave host workers idle).
 constexpr int kSolveParts = 4;
-constexpr int kPart0Cluster = 4;  // CTAs per window in the first part of a pipelined batch
+// The shape of the first part of a pipelined batch (the largest windows), by precision
+// (NAV_BA_FP64, NAV_BA_MIXED): clusters over a window of that part, measured best on the
+// 256-window workload (FP64 4 x 128 threads, mixed 2 x 256; 1 to 8 CTAs lie within 1 to 10 %).
+constexpr WindowLaunch kPart0Shape[2] = {{4, 128, 0.0}, {2, 256, 0.0}};
 
 struct nav_ba_ctx {
     int device = 0;
@@ -498,7 +501,7 @@ nav_ba_status solve_pipelined(nav_ba_ctx* ctx, const nav_ba_problem* probs, int 
     // parts are uploaded: each of its windows is solved by a cluster of CTAs, which shortens those
     // windows (the batch's critical path) and fills the otherwise idle SMs of the ramp.
     // NAVBA_PART0_SHAPE="<cluster>,<threads>" sets it (diagnostics).
-    WindowLaunch part0_shape{kPart0Cluster, 256, 0.0};
+    WindowLaunch part0_shape = kPart0Shape[o->precision == NAV_BA_FP64 ? 0 : 1];
     {
         const char* ps = getenv("NAVBA_PART0_SHAPE");
         int pc = 0, pt = 0;

@@ -59,6 +59,7 @@ struct SmemHead {
     int32_t pcnt[kMaxBlocks];              // rank 0: pairs per S block
     int32_t whist[16][kWinMaxFreeCams];    // per warp: pair counts / cursors of one block row
     int32_t cur, ok, win, slot;
+    int32_t next_blk;  // a CTA solving a window alone: the Schur-block work counter
     double lm[4];    // the LM decision of a trial: rho, lambda, nu, chi (made by thread 0)
     int32_t lm_acc;  // the trial was accepted
 };
@@ -107,6 +108,43 @@ __device__ __forceinline__ void decode_block(int blk, int& a, int& b) {
     while (a * (a + 1) / 2 > blk) --a;
     b = blk - a * (a + 1) / 2;
 }
+
+// The S blocks a warp takes: in a cluster, a fixed share (warp gw takes blocks gw, gw + CW, ...);
+// in a CTA solving its window alone, the next one from a shared-memory counter, diagonal blocks
+// first (each carries every observation of its camera, the longest pair lists), so that no warp
+// is left with several of them while the others wait at the barrier.  next() returns false when
+// the blocks are exhausted; a, b, blk are the block's camera pair and packed index.
+struct BlockSchedule {
+    int k, nblk, nfc;
+    bool dynamic;
+    __device__ BlockSchedule(const CC& c, int nfc_) : nblk(nfc_ * (nfc_ + 1) / 2), nfc(nfc_), dynamic(c.csize == 1) {
+        k = dynamic ? -1 : c.gw - c.CW;
+    }
+    __device__ bool next(const CC& c, int& a, int& b, int& blk) {
+        if (dynamic) {
+            int j = 0;
+            if (c.lane == 0) j = atomicAdd(&c.s->next_blk, 1);
+            k = __shfl_sync(0xffffffffu, j, 0);
+            if (k >= nblk) return false;
+            if (k < nfc) {
+                a = b = k;
+            } else {  // off-diagonal o = a (a - 1) / 2 + b, b < a
+                const int o = k - nfc;
+                a = (int)((1.0f + sqrtf(8.0f * (float)o + 1.0f)) * 0.5f);
+                while (a * (a - 1) / 2 > o) --a;
+                while ((a + 1) * a / 2 <= o) ++a;
+                b = o - a * (a - 1) / 2;
+            }
+            blk = a * (a + 1) / 2 + b;
+            return true;
+        }
+        k += c.CW;
+        if (k >= nblk) return false;
+        blk = k;
+        decode_block(blk, a, b);
+        return true;
+    }
+};
 
 // Sums (or a max for the first value when MAX0) of three per-thread values over the whole
 // cluster; every thread of every CTA gets the same result (fixed reduction order).
@@ -394,11 +432,10 @@ __device__ __forceinline__ void write_block(const CC& c, int a, int b, Real* acc
 // S blocks from Jacobian-factored records (mixed form, pinhole): per pair (i, j) of block (a, b),
 // A_i A_j^T = J_ci^T M J_cj with M = B_i B_j^T (2x2), the J_c rebuilt from each record's (u, v, iz).
 __device__ void schur_blocks_jf(const WinArgs<float>& A, const CC& c, const WinDesc& D, double lambda) {
-    const int nblk = D.nfc * (D.nfc + 1) / 2;
     const float fx = (float)A.intr.fx, fy = (float)A.intr.fy;
-    for (int blk = c.gw; blk < nblk; blk += c.CW) {
-        int a, b;
-        decode_block(blk, a, b);
+    BlockSchedule sched(c, D.nfc);
+    int a, b, blk;
+    while (sched.next(c, a, b, blk)) {
         const int64_t base = D.pair0 + c.s0->poff[blk];
         const int n = c.s0->pcnt[blk];
         float acc[36], accb[6];
@@ -451,10 +488,9 @@ __device__ void schur_blocks(const WinArgs<Real>& A, const CC& c, const WinDesc&
             return;
         }
     }
-    const int nblk = D.nfc * (D.nfc + 1) / 2;
-    for (int blk = c.gw; blk < nblk; blk += c.CW) {
-        int a, b;
-        decode_block(blk, a, b);
+    BlockSchedule sched(c, D.nfc);
+    int a, b, blk;
+    while (sched.next(c, a, b, blk)) {
         const int64_t base = D.pair0 + c.s0->poff[blk];
         const int n = c.s0->pcnt[blk];
         Real acc[36];
@@ -845,6 +881,7 @@ __device__ void solve_window(const WinArgs<Real>& A, CC& c, int w, unsigned char
                         S[k] = 0.0;
                         if (mixed) S32[k] = 0.f;
                     }
+                if (threadIdx.x == 0) s.next_blk = 0;  // ordered before the blocks by the reduction's barriers
                 const int npd = schur_points<Real>(A, c, D, lam_use, cr_cur, A.x[cur], A.xr[cur]);
                 const double3 r0 = cluster_reduce3<false>(c, (double)npd, 0.0, 0.0);  // also orders S zeroing
                 pc.mark(4);
