@@ -49,6 +49,9 @@ namespace {
 
 constexpr unsigned kFullG = 0xffffffffu;
 constexpr int kTile = 32;
+// the dynamic shared memory of a triangular solve (x and its ring of tile steps), beside ~2-4 KB
+// of static shared memory
+constexpr size_t kSolveSmem = 200 * 1024;
 constexpr int kCamChunk = 256;
 constexpr int kPairChunk = 256;  // pairs per work item of the Schur-block kernel
 
@@ -285,211 +288,504 @@ __global__ void k_schur_blocks(WinArgs<Real> A, const int2* blocks, const int32_
     }
 }
 
-// ---- FP64 tiled Cholesky inside the envelope -------------------------------------------
+// ---- Tiled Cholesky inside the envelope -------------------------------------------------
 
-// tfirst[I]: first tile column of tile row I that may be nonzero (the envelope, at tile level).
-// FP64 Cholesky of the envelope over the whole GPU (cooperative launch, every block resident).
-// Per tile column K: each block owning a panel tile (tile row I > K whose envelope reaches K)
-// factors the diagonal tile L_KK in its own shared memory (block 0 also stores it and 1/L_jj), then
-// solves its panel tiles L_IK = A_IK L_KK^-T; after a grid synchronization block 0 stores L_KK and the
-// trailing tiles
-// (I, J), K < J <= I inside the envelope, are updated A_IJ -= L_IK L_JK^T in quarter-tile work items
-// (8 rows x 32 columns, one output per thread) spread over the blocks; a grid synchronization ends
-// the column.  The per-column panel rows and trailing tiles come from host-built lists, and the grid
-// is sized to the largest column's work (a grid synchronization costs more with more blocks).
-// Every block runs the same loops, so all reach every synchronization; a non-positive pivot is
-// replaced by 1 and reported through ok.
+// tfirst[I]: first tile column of tile row I that may be nonzero (the envelope, at tile level);
+// rows(K) = the tile rows I > K with tfirst[I] <= K (the panel of tile column K).
+//
+// Right-looking Cholesky of the envelope over the whole GPU (cooperative launch, every block
+// resident).  Per tile column K, every block owning a panel tile of column K factors the diagonal
+// tile in its shared memory (warp 0, the tile's rows in lane registers) and solves its panel tiles
+// L_IK = A_IK L_KK^-T (warp 0, a row per lane); block 0 also stores L_KK and 1/L_jj once no block
+// reads A_KK any more.  The trailing tiles (I, J), I >= J, both in rows(K), are updated
+// A_IJ -= L_IK L_JK^T in quarter-tile work items spread over the blocks, first to the blocks
+// without panel work.
+// - FP64: a grid synchronization after the panels and one after the trailing update.
+// - FP32 (latency-bound): one grid synchronization per column.  Phase K applies column K - 1's
+//   update to the trailing tiles right of column K while column K is finished: the panel blocks
+//   apply it to A_KK and their own panel tiles in shared memory before factoring and solving.
+// Either way the updates reach every element column by column.  A non-positive pivot is replaced by 1 and reported through
+// ok.  Each panel tile is also stored contiguously, transposed into LT and as is into LN (32 x 32
+// per entry of the panel list, in list order), and each diagonal tile's inverse into DI (L^-T and
+// L^-1, 32 x 32 each, by tile), which the solves read.  Requires 256 threads per block.  tr_ij lists each
+// column's trailing tiles by column J
+// (J ascending), so the tiles of column K + 1 are the first tr_skip[K] of column K's list.
 template <class T>
-__device__ void factor_diag_tile(T (*tk)[kTile + 1], T* rv, const T* S, int m, int k0, int kb, int& bad) {
-    const int tid = threadIdx.x, nth = blockDim.x;
-    for (int idx = tid; idx < kTile * kTile; idx += nth) {
-        const int i = idx / kTile, j = idx % kTile;
-        tk[i][j] = (i < kb && j <= i) ? S[(size_t)(k0 + i) * m + k0 + j] : T(0);
-    }
-    __syncthreads();
-    for (int j = 0; j < kb; ++j) {
-        if (tid == 0) {
-            const T d = tk[j][j];
-            T r;
-            if (!(d > T(0)) || !isfinite(d)) {
-                bad = 1;
-                r = T(1);
-                tk[j][j] = T(1);
-            } else {
-                r = rsqrt(d);
-                tk[j][j] = d * r;
-            }
-            rv[j] = r;
-        }
-        __syncthreads();
-        for (int i = j + 1 + tid; i < kb; i += nth) tk[i][j] *= rv[j];
-        __syncthreads();
-        const int w = kb - j - 1;
-        for (int idx = tid; idx < w * w; idx += nth) {
-            const int i = j + 1 + idx / w, l = j + 1 + idx % w;
-            if (l <= i) tk[i][l] -= tk[i][j] * tk[l][j];
-        }
-        __syncthreads();
+using TileT = T[kTile][kTile + 1];
+
+// rows r0.. (rb of them) and columns c0.. (cb) of row-major S (leading dimension m) into t; zero
+// elsewhere (lower_only: only j <= i)
+template <class T>
+__device__ __forceinline__ void tile_load(TileT<T>& t, const T* S, int m, int r0, int rb, int c0, int cb,
+                                          bool lower_only = false) {
+    for (int idx = threadIdx.x; idx < kTile * kTile; idx += blockDim.x) {
+        const int i = idx >> 5, j = idx & 31;
+        t[i][j] = (i < rb && j < cb && (!lower_only || j <= i)) ? S[(size_t)(r0 + i) * m + c0 + j] : T(0);
     }
 }
 
+// s[q] = sum_t a[r + 8q][t] b[c][t] (t = 0..31 in order) for this thread's column c = tid & 31 and
+// rows r + 8q, r = tid >> 5 (256 threads: one 32 x 32 tile product)
 template <class T>
-__global__ void __launch_bounds__(256) k_cholesky_coop(T* S, int m, const int32_t* pan_off, const int32_t* pan_row,
-                                                       const int32_t* tr_off, const int2* tr_ij, T* rinv, int32_t* ok) {
+__device__ __forceinline__ void tile_abt(const TileT<T>& a, const TileT<T>& b, T s[4]) {
+    const int c = threadIdx.x & 31, r = threadIdx.x >> 5;
+    s[0] = s[1] = s[2] = s[3] = T(0);
+#pragma unroll 8
+    for (int t = 0; t < kTile; ++t) {
+        const T bv = b[c][t];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) s[q] += a[r + 8 * q][t] * bv;
+    }
+}
+
+// LL^T of the kb x kb lower tile tk in place; rv[j] receives 1/L_jj.  Per column: the pivot, the
+// column scaled by 1/L_jj, the rank-1 update of the columns to its right.  Called by every thread
+// of the block; a barrier must follow.
+// - FP32: warp 0 alone, lane i holding row i in registers.  Each column's unscaled values go
+//   through shared memory (col, double-buffered): every lane reads the pivot u_cc, forms
+//   r = 1/sqrt(u_cc) itself and its L_ic = u_ic r, and updates u_ij -= (L_ic r) u_jc; one warp
+//   barrier per column (a shuffle per element was 5x slower).
+// - FP64: the whole block (warp per row of the update), so that the FP64 products are spread over
+//   the SM's four partitions.
+template <class T>
+__device__ void factor_diag_tile(TileT<T>& tk, T* rv, T (*col)[kTile], int kb, int& bad) {
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if constexpr (sizeof(T) == 4) {
+        if (wid != 0) return;
+        T d[kTile];
+#pragma unroll
+        for (int j = 0; j < kTile; ++j) d[j] = (lane < kb && j <= lane) ? tk[lane][j] : T(0);
+        col[0][lane] = d[0];
+        __syncwarp();
+#pragma unroll
+        for (int cc = 0; cc < kTile; ++cc) {
+            if (cc < kb) {
+                const T* cu = col[cc & 1];  // column cc, unscaled
+                const T piv = cu[cc];
+                const bool colbad = !(piv > T(0)) || !isfinite(piv);
+                const T r = colbad ? T(1) : rsqrtf(piv);
+                if (colbad) bad = 1;
+                const T li = lane == cc ? (colbad ? T(1) : piv * r) : d[cc] * r;
+                d[cc] = li;
+                const T wi = li * r;
+                if (lane == 0) rv[cc] = r;
+#pragma unroll
+                for (int j = cc + 1; j < kTile; ++j)
+                    if (lane >= j) d[j] -= wi * cu[j];
+                if (cc + 1 < kTile) col[(cc + 1) & 1][lane] = d[cc + 1];
+                __syncwarp();
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < kTile; ++j)
+            if (lane < kb && j <= lane) tk[lane][j] = d[j];
+    } else {
+        const int nw = blockDim.x >> 5;
+        for (int j = 0; j < kb; ++j) {
+            if (tid == 0) {
+                const T dj = tk[j][j];
+                T r;
+                if (!(dj > T(0)) || !isfinite(dj)) {
+                    bad = 1;
+                    r = T(1);
+                    tk[j][j] = T(1);
+                } else {
+                    r = rsqrt(dj);
+                    tk[j][j] = dj * r;
+                }
+                rv[j] = r;
+            }
+            __syncthreads();
+            for (int i = j + 1 + tid; i < kb; i += blockDim.x) tk[i][j] *= rv[j];
+            __syncthreads();
+            for (int i = j + 1 + wid; i < kb; i += nw)
+                for (int l = j + 1 + lane; l <= i; l += 32) tk[i][l] -= tk[i][j] * tk[l][j];
+            __syncthreads();
+        }
+    }
+}
+
+// The inverse of the lower tile L = tk (1/L_jj in rv) by warp 0: lane j forms column j,
+// y_i = -(1/L_ii) sum_{j<=k<i} L_ik y_k (y_j = 1/L_jj), and stores it into di (two 32 x 32
+// row-major blocks: L^-T, then L^-1), so the triangular solves apply each diagonal tile as a
+// product, reading row c of the block for every c with lanes over its columns in both directions.
+template <class T>
+__device__ void invert_diag_tile(const TileT<T>& tk, const T* rv, T* di) {
+    const int lane = threadIdx.x & 31;
+    T y[kTile];
+#pragma unroll
+    for (int i = 0; i < kTile; ++i) {
+        T s = T(0);
+#pragma unroll
+        for (int k = 0; k < i; ++k) s += tk[i][k] * y[k];
+        y[i] = i < lane ? T(0) : (i == lane ? rv[i] : -rv[i] * s);
+    }
+#pragma unroll
+    for (int i = 0; i < kTile; ++i) {
+        di[lane * kTile + i] = y[i];                  // (L^-T)_lane,i = (L^-1)_i,lane
+        di[kTile * kTile + i * kTile + lane] = y[i];  // (L^-1)_i,lane
+    }
+}
+
+// x L_KK^T = a for the ib rows of ta by warp 0 (lane i: row i in registers):
+// x_c = (a_c - sum_{j<c} x_j L_cj) / L_cc, the sum in four partial sums (j mod 4).
+template <class T>
+__device__ void panel_solve(TileT<T>& ta, const TileT<T>& tk, const T* rv, int ib, int kb) {
+    const int lane = threadIdx.x & 31;
+    T a[kTile];
+#pragma unroll
+    for (int j = 0; j < kTile; ++j) a[j] = ta[lane][j];
+#pragma unroll
+    for (int cc = 0; cc < kTile; ++cc) {
+        if (cc < kb) {
+            T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
+            int j = 0;
+#pragma unroll
+            for (; j + 3 < cc; j += 4) {
+                s0 += a[j] * tk[cc][j];
+                s1 += a[j + 1] * tk[cc][j + 1];
+                s2 += a[j + 2] * tk[cc][j + 2];
+                s3 += a[j + 3] * tk[cc][j + 3];
+            }
+#pragma unroll
+            for (; j < cc; ++j) s0 += a[j] * tk[cc][j];
+            a[cc] = (a[cc] - ((s0 + s1) + (s2 + s3))) * rv[cc];
+        }
+    }
+    if (lane < ib)
+#pragma unroll
+        for (int j = 0; j < kTile; ++j) ta[lane][j] = a[j];
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_cholesky_coop(T* S, int m, const int32_t* tfirst, const int32_t* pan_off,
+                                                       const int32_t* pan_row, const int32_t* tr_off, const int32_t* tr_skip,
+                                                       const int2* tr_ij, T* rinv, T* LT, T* LN, T* DI, int32_t* ok,
+                                                       unsigned long long* phase) {
+    constexpr bool one_sync = sizeof(T) == 4;
     cg::grid_group grid = cg::this_grid();
-    __shared__ T tk[kTile][kTile + 1];
-    __shared__ T ta[kTile][kTile + 1];
-    __shared__ T tb[kTile][kTile + 1];
-    __shared__ T rv[kTile];
+    __shared__ TileT<T> tk, ta, tb, tc;
+    __shared__ T rv[kTile], col[2][kTile];
     __shared__ int sbad;
-    const int tid = threadIdx.x, nth = blockDim.x, nb = gridDim.x, bid = blockIdx.x;
+    const int tid = threadIdx.x, nb = gridDim.x, bid = blockIdx.x, wid = tid >> 5;
     const int nt = (m + kTile - 1) / kTile;
+    const bool timed = phase && bid == 0 && tid == 0;
+    long long tmark = timed ? clock64() : 0;
+    auto mark = [&](int k) {
+        if (timed) {
+            const long long now = clock64();
+            phase[k] += (unsigned long long)(now - tmark);
+            tmark = now;
+        }
+    };
     if (tid == 0) sbad = 0;
-    __syncthreads();
-    for (int K = 0; K < nt; ++K) {
-        const int k0 = K * kTile, kb = min(kTile, m - k0);
+    int bad = 0;  // pivot failures this thread saw
+    auto store_diag = [&](int k0, int kb) {  // L_KK (from tk) and 1/L_jj into S and rinv
+        for (int idx = tid; idx < kb * kb; idx += blockDim.x) {
+            const int i = idx / kb, j = idx % kb;
+            if (j <= i) S[(size_t)(k0 + i) * m + k0 + j] = tk[i][j];
+        }
+        for (int j = tid; j < kb; j += blockDim.x) rinv[k0 + j] = rv[j];
+    };
+    // tk -= a a^T (a: a 32 x 32 tile in shared memory); a barrier follows
+    auto sub_aat = [&](TileT<T>& dst, const TileT<T>& a, const TileT<T>& b) {
+        T s[4];
+        tile_abt(a, b, s);
+        const int c = tid & 31, r = tid >> 5;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) dst[r + 8 * q][c] -= s[q];
+    };
+    // this block's panel tiles of column K (L_KK in tk, 1/L_jj in rv); with upd_prev, first
+    // A_IK -= L_I,K-1 L_K,K-1^T (L_K,K-1 in tb) for the rows inside column K - 1's envelope
+    auto panel_tiles = [&](int K, bool upd_prev) {
+        const int k0 = K * kTile, kb = min(kTile, m - k0), kp = k0 - kTile;
         const int p0 = pan_off[K], npan = pan_off[K + 1] - p0;
-        if (bid == 0 || bid < npan) {
-            factor_diag_tile(tk, rv, S, m, k0, kb, sbad);
-            for (int pi = bid; pi < npan; pi += nb) {  // this block's panel tiles
-                const int I = pan_row[p0 + pi];
-                const int i0 = I * kTile, ib = min(kTile, m - i0);
+        for (int pi = bid; pi < npan; pi += nb) {
+            const int I = pan_row[p0 + pi];
+            const int i0 = I * kTile, ib = min(kTile, m - i0);
+            const bool upd = upd_prev && tfirst[I] <= K - 1;
+            tile_load(ta, S, m, i0, ib, k0, kb);
+            if (upd) tile_load(tc, S, m, i0, ib, kp, kTile);
+            __syncthreads();
+            if (upd) {
+                sub_aat(ta, tc, tb);
                 __syncthreads();
-                for (int idx = tid; idx < kTile * kTile; idx += nth) {
-                    const int i = idx / kTile, j = idx % kTile;
-                    ta[i][j] = (i < ib && j < kb) ? S[(size_t)(i0 + i) * m + k0 + j] : T(0);
-                }
-                __syncthreads();
-                if (tid < ib) {
-                    // x_c = (a_c - sum_{j<c} x_j L_cj) / L_cc; the sum in four independent partial sums
-                    for (int cc = 0; cc < kb; ++cc) {
-                        T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
-                        int j = 0;
-                        for (; j + 3 < cc; j += 4) {
-                            s0 += ta[tid][j] * tk[cc][j];
-                            s1 += ta[tid][j + 1] * tk[cc][j + 1];
-                            s2 += ta[tid][j + 2] * tk[cc][j + 2];
-                            s3 += ta[tid][j + 3] * tk[cc][j + 3];
-                        }
-                        for (; j < cc; ++j) s0 += ta[tid][j] * tk[cc][j];
-                        ta[tid][cc] = (ta[tid][cc] - ((s0 + s1) + (s2 + s3))) * rv[cc];
-                    }
-                }
-                __syncthreads();
-                for (int idx = tid; idx < ib * kb; idx += nth) {
-                    const int i = idx / kb, j = idx % kb;
-                    S[(size_t)(i0 + i) * m + k0 + j] = ta[i][j];
-                }
             }
-        }
-        grid.sync();
-        // block 0 stores L_KK now that every block has read A_KK (the trailing tiles do not touch it)
-        if (bid == 0) {
-            for (int idx = tid; idx < kb * kb; idx += nth) {
+            if (wid == 0) panel_solve(ta, tk, rv, ib, kb);
+            __syncthreads();
+            for (int idx = tid; idx < ib * kb; idx += blockDim.x) {
                 const int i = idx / kb, j = idx % kb;
-                if (j <= i) S[(size_t)(k0 + i) * m + k0 + j] = tk[i][j];
+                S[(size_t)(i0 + i) * m + k0 + j] = ta[i][j];
             }
-            for (int j = tid; j < kb; j += nth) rinv[k0 + j] = rv[j];
+            // the tile contiguous for the solves: transposed for the forward one, as is for the backward
+            T* lt = LT + (size_t)(p0 + pi) * (kTile * kTile);
+            T* ln = LN + (size_t)(p0 + pi) * (kTile * kTile);
+            for (int idx = tid; idx < kTile * kTile; idx += blockDim.x) {
+                lt[idx] = ta[idx & 31][idx >> 5];
+                ln[idx] = ta[idx >> 5][idx & 31];
+            }
+            __syncthreads();
         }
-        // trailing update: work item w = 4 * tile + quarter over the column's tile list
-        const int t0 = tr_off[K], nitems = 4 * (tr_off[K + 1] - t0);
-        for (int w = bid; w < nitems; w += nb) {
+    };
+    // trailing update A_IJ -= L_I,c L_J,c^T over the listed tiles [t0, t1) of column c, in
+    // quarter-tile work items (8 rows x 32 columns, one output per thread), first to the blocks
+    // after the npan panel owners
+    auto trailing = [&](int c, int t0, int t1, int npan) {
+        const int c0 = c * kTile, nitems = 4 * (t1 - t0);
+        int w = bid - min(npan, nb);
+        if (w < 0) w += nb;
+        for (; w < nitems; w += nb) {
             const int2 ij = tr_ij[t0 + w / 4];
             const int I = ij.x, J = ij.y, r0 = 8 * (w % 4);
             const int i0 = I * kTile, ib = min(kTile, m - i0), j0 = J * kTile, jb = min(kTile, m - j0);
             if (r0 >= ib) continue;  // uniform per block
             __syncthreads();
-            for (int idx = tid; idx < kTile * kTile; idx += nth) {
-                const int i = idx / kTile, j = idx % kTile;
-                tb[i][j] = (i < jb && j < kb) ? S[(size_t)(j0 + i) * m + k0 + j] : T(0);
-                if (i < 8) ta[i][j] = (r0 + i < ib && j < kb) ? S[(size_t)(i0 + r0 + i) * m + k0 + j] : T(0);
+            for (int idx = tid; idx < kTile * kTile; idx += blockDim.x) {
+                const int i = idx >> 5, j = idx & 31;
+                tb[i][j] = i < jb ? S[(size_t)(j0 + i) * m + c0 + j] : T(0);
+                if (i < 8) ta[i][j] = r0 + i < ib ? S[(size_t)(i0 + r0 + i) * m + c0 + j] : T(0);
             }
             __syncthreads();
-            const int r = tid / kTile, c = tid % kTile;  // 256 threads: 8 rows x 32 columns
-            if (r < 8 && r0 + r < ib && c < jb && !(I == J && c > r0 + r)) {
-                T sum = T(0);
-#pragma unroll 8
-                for (int t = 0; t < kTile; ++t) sum += ta[r][t] * tb[c][t];
-                S[(size_t)(i0 + r0 + r) * m + j0 + c] -= sum;
+            const int r = tid >> 5, cc = tid & 31;  // 256 threads: 8 rows x 32 columns
+            if (r0 + r < ib && cc < jb && !(I == J && cc > r0 + r)) {
+                T s4[4] = {T(0), T(0), T(0), T(0)};  // four partial sums (t mod 4)
+#pragma unroll
+                for (int t = 0; t < kTile; ++t) s4[t & 3] += ta[r][t] * tb[cc][t];
+                S[(size_t)(i0 + r0 + r) * m + j0 + cc] -= (s4[0] + s4[1]) + (s4[2] + s4[3]);
             }
         }
-        grid.sync();
+    };
+    if constexpr (one_sync) {
+        for (int K = 0; K < nt; ++K) {
+            const int k0 = K * kTile, kb = min(kTile, m - k0), kp = k0 - kTile;
+            const int npan = pan_off[K + 1] - pan_off[K];
+            const bool upd_prev = K > 0 && tfirst[K] <= K - 1;  // L_K,K-1 is inside the envelope
+            if (bid == 0 || bid < npan) {
+                // A_KK minus column K - 1's update, factored (every panel block, redundantly)
+                __syncthreads();
+                tile_load(tk, S, m, k0, kb, k0, kb, true);
+                if (upd_prev) tile_load(tb, S, m, k0, kb, kp, kTile);
+                __syncthreads();
+                if (upd_prev) {
+                    sub_aat(tk, tb, tb);
+                    __syncthreads();
+                }
+                factor_diag_tile(tk, rv, col, kb, bad);
+                __syncthreads();
+                mark(0);
+                panel_tiles(K, upd_prev);
+                mark(1);
+            }
+            // column K - 1's update of the trailing tiles right of column K
+            if (K > 0) trailing(K - 1, tr_off[K - 1] + tr_skip[K - 1], tr_off[K], npan);
+            mark(2);
+            grid.sync();
+            mark(3);
+            if (bid == 0) store_diag(k0, kb);  // no block reads A_KK any more
+        }
+    } else {
+        for (int K = 0; K < nt; ++K) {
+            const int k0 = K * kTile, kb = min(kTile, m - k0);
+            const int npan = pan_off[K + 1] - pan_off[K];
+            if (bid == 0 || bid < npan) {
+                __syncthreads();
+                tile_load(tk, S, m, k0, kb, k0, kb, true);
+                __syncthreads();
+                factor_diag_tile(tk, rv, col, kb, bad);
+                __syncthreads();
+                mark(0);
+                panel_tiles(K, false);
+                mark(1);
+            }
+            grid.sync();
+            mark(3);
+            if (bid == 0) store_diag(k0, kb);  // every block has read A_KK
+            trailing(K, tr_off[K], tr_off[K + 1], npan);
+            mark(2);
+            grid.sync();
+            mark(3);
+        }
     }
+    // the inverses of the diagonal tiles, a tile per block
+    grid.sync();
+    for (int K = bid; K < nt; K += nb) {
+        const int k0 = K * kTile, kb = min(kTile, m - k0);
+        __syncthreads();
+        tile_load(tk, S, m, k0, kb, k0, kb, true);
+        if (tid < kTile) rv[tid] = tid < kb ? rinv[k0 + tid] : T(1);
+        __syncthreads();
+        if (wid == 0) invert_diag_tile(tk, rv, DI + (size_t)K * 2 * kTile * kTile);
+    }
+    mark(4);
+    if (bad) atomicOr(&sbad, 1);
+    __syncthreads();
     if (tid == 0 && sbad) ok[0] = 0;
 }
 
-// Solve L L^T x = b in place (one CTA), tile-blocked, inside the envelope.  Per tile column K:
-// warp 0 solves the diagonal tile; the rows below (those whose tile row reaches column K) are
-// spread over the warps with the lanes over the tile's columns, so every load of L is a
-// contiguous 256-byte row segment; sums are shuffle trees and a fixed-order sum over warps.
+// Asynchronous global -> shared copies (cp.async, completed through commit groups).
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+
+// Triangular solves: the shared-memory ring of tile steps (kSolveRing slots).  A slot holds one
+// step's diagonal-tile inverse (forward L^-T, backward L^-1; 32 x 32) and up to P panel tiles of
+// the step's column (forward: transposed, from LT; backward: as is, from LN), all contiguous.
+constexpr int kSolveRing = 3;
 template <class T>
-__global__ void k_chol_solve(const T* L, int m, const int32_t* tfirst, const T* rinv, T* x) {
-    __shared__ T red[32][kTile];
-    __shared__ T dt[kTile][kTile + 1];  // the diagonal tile, staged for the serial chain
-    __shared__ T dr[kTile];
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+__host__ __device__ constexpr size_t solve_slot_elems(int P) {
+    return (size_t)(1 + P) * kTile * kTile;
+}
+
+// Solve L L^T x = b in place (one CTA of 512 threads), tile by tile inside the envelope: the
+// forward sweep then the backward sweep, 2 nt tile steps.  The data of step i + 2 (its diagonal
+// tile's inverse and panel tiles, contiguous copies the factorization left) is copied into the
+// shared-memory ring with 16-byte cp.async while step i runs: on GB300 an L2 round trip (~1.5k
+// cycles) is longer than a tile step, and loading a step's data one step ahead left that latency
+// on the serial chain (78 us of a 146 us solve on the 200-camera grid with its panel work removed).
+// - Warp 0 applies the diagonal tile's inverse as a 32 x 32 product, lane per output.
+// - Warps 1..15 take the column's panel tiles (rows(K)), a tile per warp.  Forward,
+//   x_r -= L_r,K x_K: lane per row over the transposed tile (no cross-lane reduction: a warp
+//   shuffle issues at one per SM clock on GB300).  Backward, x_K -= sum_r L_r,K^T x_r: lane per
+//   column over the tile's rows; then over warps in order.  Tiles beyond the P a slot holds are
+//   read from global memory.  Warp 0 copies nothing: it carries the serial chain.
+// Every shared-memory read is a row of a block with lanes over its columns (conflict-free), every
+// sum runs in four partial sums (index mod 4).  Bitwise repeatable.  kXs: x is kept in dynamic
+// shared memory (padded with zeros to whole tiles) ahead of the ring.
+template <class T, bool kXs>
+__global__ void __launch_bounds__(512) k_chol_solve(const T* __restrict__ LT, const T* __restrict__ LN,
+                                                    const T* __restrict__ DI, int m, const int32_t* __restrict__ pan_off,
+                                                    const int32_t* __restrict__ pan_row, T* __restrict__ xg, int P) {
+    constexpr int kW = 16;  // warps
+    constexpr int kPer16 = 16 / sizeof(T);
+    constexpr int kChunks = kTile * kTile / kPer16;  // 16-byte chunks per 32 x 32 block
+    __shared__ T xk[kTile];
+    __shared__ T red[kW][kTile + 1];
+    extern __shared__ __align__(16) unsigned char dyn_raw[];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int nt = (m + kTile - 1) / kTile;
-    auto stage = [&](int k0, int kb) {
-        for (int idx = tid; idx < kTile * kTile; idx += blockDim.x) {
-            const int i = idx / kTile, j = idx % kTile;
-            dt[i][j] = (i < kb && j < kb) ? L[(size_t)(k0 + i) * m + k0 + j] : T(0);
+    if (nt == 0) return;
+    T* const xs = reinterpret_cast<T*>(dyn_raw);
+    T* const ring = xs + (kXs ? (size_t)nt * kTile : 0);
+    const size_t slot_elems = solve_slot_elems<T>(P);
+    T* x = kXs ? xs : xg;
+    if constexpr (kXs) {
+        for (int i = tid; i < nt * kTile; i += blockDim.x) x[i] = i < m ? xg[i] : T(0);
+    }
+    auto xrow = [&](int r) -> T { return kXs ? x[r] : x[min(r, m - 1)]; };
+    const int nsteps = 2 * nt;
+    auto step_col = [&](int i) { return i < nt ? i : nsteps - 1 - i; };
+    // copies step i's blocks into its ring slot (warps 1..15), one commit group per thread
+    auto issue = [&](int i) {
+        if (i < nsteps && wid > 0) {
+            const bool fwd = i < nt;
+            const int K = step_col(i);
+            T* sl = ring + (size_t)(i % kSolveRing) * slot_elems;
+            const int p0 = pan_off[K], n = min(pan_off[K + 1] - p0, P);
+            const T* di = DI + ((size_t)2 * K + (fwd ? 0 : 1)) * kTile * kTile;
+            const T* src = fwd ? LT : LN;
+            for (int e = tid - kTile; e < (1 + n) * kChunks; e += blockDim.x - kTile) {
+                const int b = e / kChunks, q = e % kChunks;
+                const T* g = b == 0 ? di + q * kPer16 : src + (size_t)(p0 + b - 1) * kTile * kTile + q * kPer16;
+                cp_async16(sl + (size_t)b * kTile * kTile + q * kPer16, g);
+            }
         }
-        for (int j = tid; j < kTile; j += blockDim.x) dr[j] = j < kb ? rinv[k0 + j] : T(1);
-        __syncthreads();
+        cp_async_commit();
     };
-    // forward: L y = b
-    for (int K = 0; K < nt; ++K) {
-        const int k0 = K * kTile, kb = min(kTile, m - k0);
-        stage(k0, kb);
-        if (tid < 32) {  // warp 0 solves the diagonal tile
-            T v = lane < kb ? x[k0 + lane] : T(0);
-            for (int j = 0; j < kb; ++j) {
-                const T xj = __shfl_sync(kFullG, v * (lane == j ? dr[j] : T(1)), j);
-                if (lane == j) v = xj;
-                if (lane > j && lane < kb) v -= dt[lane][j] * xj;
-            }
-            if (lane < kb) x[k0 + lane] = v;
-        }
-        __syncthreads();
-        const T xk = lane < kb ? x[k0 + lane] : T(0);
-        for (int r = k0 + kb + wid; r < m; r += nw) {
-            if (tfirst[r / kTile] > K) continue;  // uniform per warp
-            T s = lane < kb ? L[(size_t)r * m + k0 + lane] * xk : T(0);
+    for (int i = 0; i < kSolveRing - 1; ++i) issue(i);
+    for (int i = 0; i < nsteps; ++i) {
+        cp_async_wait<kSolveRing - 2>();  // step i's group is complete
+        __syncthreads();                   // ... for every thread; slot (i - 1) is free
+        issue(i + kSolveRing - 1);
+        const bool fwd = i < nt;
+        const int K = step_col(i), k0 = K * kTile, kb = min(kTile, m - k0);
+        const T* sl = ring + (size_t)(i % kSolveRing) * slot_elems;
+        const T* tl = sl + kTile * kTile;
+        const int p0 = pan_off[K], npan = pan_off[K + 1] - p0;
+        if (!fwd && wid > 0) {  // backward: sum_r L_r,K^T x_r over the panel rows
+            T a4[4] = {T(0), T(0), T(0), T(0)};  // four partial sums (row mod 4)
+            for (int t = wid - 1; t < npan; t += kW - 1) {
+                const int r0 = pan_row[p0 + t] * kTile;
+                const T* ln = t < P ? tl + (size_t)t * kTile * kTile : LN + (size_t)(p0 + t) * kTile * kTile;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(kFullG, s, o);
-            if (lane == 0) x[r] -= s;
-        }
-        __syncthreads();
-    }
-    // backward: L^T x = y
-    for (int K = nt - 1; K >= 0; --K) {
-        const int k0 = K * kTile, kb = min(kTile, m - k0);
-        // x_K -= sum over the rows below of L_rK x_r (rows whose tile row reaches column K)
-        T acc = T(0);
-        for (int r = k0 + kb + wid; r < m; r += nw) {
-            if (tfirst[r / kTile] > K) continue;
-            if (lane < kb) acc += L[(size_t)r * m + k0 + lane] * x[r];
-        }
-        red[wid][lane] = acc;
-        __syncthreads();
-        if (tid < kb) {
-            T s = T(0);
-            for (int w = 0; w < nw; ++w) s += red[w][tid];
-            x[k0 + tid] -= s;
-        }
-        __syncthreads();
-        stage(k0, kb);
-        if (tid < 32) {
-            T v = lane < kb ? x[k0 + lane] : T(0);
-            for (int j = kb - 1; j >= 0; --j) {
-                const T xj = __shfl_sync(kFullG, v * (lane == j ? dr[j] : T(1)), j);
-                if (lane == j) v = xj;
-                if (lane < j) v -= dt[j][lane] * xj;
+                for (int c = 0; c < kTile; ++c) a4[c & 3] += ln[c * kTile + lane] * xrow(r0 + c);
             }
-            if (lane < kb) x[k0 + lane] = v;
+            red[wid][lane] = (a4[0] + a4[1]) + (a4[2] + a4[3]);
         }
-        __syncthreads();
+        if (!fwd) __syncthreads();
+        if (wid == 0) {
+            // x_K = L_KK^-1 b_K (forward; block L^-T) or L_KK^-T (y_K - sum) (backward; block L^-1):
+            // v_lane = sum_j block[j][lane] u_j
+            T u = lane < kb ? x[k0 + lane] : T(0);
+            if (!fwd) {
+                T s4[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+                for (int w = 1; w < kW; ++w) s4[w & 3] += red[w][lane];
+                u -= (s4[0] + s4[1]) + (s4[2] + s4[3]);
+                if (lane >= kb) u = T(0);
+            }
+            xk[lane] = u;
+            __syncwarp();
+            T v4[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+            for (int j = 0; j < kTile; ++j) v4[j & 3] += sl[j * kTile + lane] * xk[j];
+            const T v = (v4[0] + v4[1]) + (v4[2] + v4[3]);
+            __syncwarp();
+            if (lane < kb) x[k0 + lane] = v;
+            xk[lane] = lane < kb ? v : T(0);
+        }
+        if (fwd) {
+            __syncthreads();
+            if (wid > 0) {  // forward: x_r -= L_r,K x_K over the panel rows
+                for (int t = wid - 1; t < npan; t += kW - 1) {
+                    const int r = pan_row[p0 + t] * kTile + lane;
+                    const T* lt = t < P ? tl + (size_t)t * kTile * kTile : LT + (size_t)(p0 + t) * kTile * kTile;
+                    T s4[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+                    for (int c = 0; c < kTile; ++c) s4[c & 3] += lt[c * kTile + lane] * xk[c];
+                    if (r < m) x[r] -= (s4[0] + s4[1]) + (s4[2] + s4[3]);
+                }
+            }
+        }
     }
+    cp_async_wait<0>();
+    __syncthreads();
+    if constexpr (kXs) {
+        for (int i = tid; i < m; i += blockDim.x) xg[i] = x[i];
+    }
+}
+
+// Launches the triangular solves of a factored S: x in shared memory when it fits beside a ring
+// of at least one panel tile per slot (NAVBA_SOLVE_GLOBAL_X=1 keeps it in global memory, the form
+// for larger systems, to test it); each ring slot holds up to max_npan panel tiles, as many as
+// the shared-memory budget allows.
+template <class T>
+cudaError_t chol_solve(const T* LT, const T* LN, const T* DI, int m, const int32_t* pan_off, const int32_t* pan_row,
+                       T* x, int max_npan, cudaStream_t st) {
+    const char* gx = getenv("NAVBA_SOLVE_GLOBAL_X");
+    const bool global_x = gx && gx[0] == '1';
+    const size_t xs_bytes = sizeof(T) * (size_t)std::max(1, (m + kTile - 1) / kTile * kTile);
+    auto ring_bytes = [](int P) { return kSolveRing * solve_slot_elems<T>(P) * sizeof(T); };
+    const bool use_xs = !global_x && xs_bytes + ring_bytes(1) <= kSolveSmem;
+    const size_t budget = kSolveSmem - (use_xs ? xs_bytes : 0);
+    int P = std::max(0, max_npan);
+    while (P > 0 && ring_bytes(P) > budget) --P;
+    const size_t smem = (use_xs ? xs_bytes : 0) + ring_bytes(P);
+    cudaError_t e;
+    if (use_xs) {
+        e = cudaFuncSetAttribute(k_chol_solve<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k_chol_solve<T, true><<<1, 512, smem, st>>>(LT, LN, DI, m, pan_off, pan_row, x, P);
+    } else {
+        e = cudaFuncSetAttribute(k_chol_solve<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k_chol_solve<T, false><<<1, 512, smem, st>>>(LT, LN, DI, m, pan_off, pan_row, x, P);
+    }
+    return cudaGetLastError();
 }
 
 // Mixed form: S (FP64, lower part) rounded to FP32 into S32, and both mirrored into their upper
@@ -1641,9 +1937,10 @@ struct GridHost {
     std::vector<int2> blocks;
     RawVec<int2> pairs;
     // Cholesky work per tile column K: panel tile rows and trailing tiles (I, J), K < J <= I
-    std::vector<int32_t> pan_off, pan_row, tr_off;
+    std::vector<int32_t> pan_off, pan_row, tr_off, tr_skip;
     std::vector<int2> tr_ij;
     int max_col_work = 1;  // largest per-column count of panel tiles or trailing quarter items
+    int max_npan = 0;      // largest per-column count of panel tiles
     // block rows of both triangles: row a's slots [rs_off[a], rs_off[a+1]) with their column
     // cameras rs_col in increasing order, its diagonal slot rs_dslot[a]; per lower block its slot
     // in its own row and the slot of the transposed block (-1 on the diagonal)
@@ -1710,9 +2007,11 @@ void build_grid_host(const HostWindow& h, GridHost& g, int form, HostPool* pool)
     g.tfirst.assign(1, 0);
     g.pan_off.assign(2, 0);
     g.tr_off.assign(2, 0);
+    g.tr_skip.assign(1, 0);
     g.pan_row.assign(1, 0);
     g.tr_ij.assign(1, make_int2(0, 0));
     g.max_col_work = 1;
+    g.max_npan = 0;
     g.rs_off.assign(nfc + 1, 0);
     g.rs_col.assign(1, 0);
     g.rs_dslot.assign(std::max(1, nfc), 0);
@@ -1972,17 +2271,24 @@ void build_grid_host(const HostWindow& h, GridHost& g, int form, HostPool* pool)
     g.tr_off.assign(nt + 1, 0);
     g.pan_row.clear();
     g.tr_ij.clear();
+    // per tile column K: its panel rows rows(K) and the trailing tiles it updates (pairs of rows(K))
     g.max_col_work = 1;
+    g.max_npan = 0;
+    g.tr_skip.assign(std::max(1, nt), 0);
     for (int K = 0; K < nt; ++K) {
         std::vector<int32_t> rows;
         for (int I = K + 1; I < nt; ++I)
             if (g.tfirst[I] <= K) rows.push_back(I);
         for (int I : rows) g.pan_row.push_back(I);
-        for (size_t x = 0; x < rows.size(); ++x)
-            for (size_t y = 0; y <= x; ++y) g.tr_ij.push_back(make_int2(rows[x], rows[y]));
+        for (size_t y = 0; y < rows.size(); ++y)  // by column J = rows[y]
+            for (size_t x = y; x < rows.size(); ++x) g.tr_ij.push_back(make_int2(rows[x], rows[y]));
+        // left out when the FP32 factorization applies this column's update one phase later: the
+        // tiles of column K + 1, which their panel blocks update themselves
+        g.tr_skip[K] = (!rows.empty() && rows[0] == K + 1) ? (int32_t)rows.size() : 0;
         g.pan_off[K + 1] = (int32_t)g.pan_row.size();
         g.tr_off[K + 1] = (int32_t)g.tr_ij.size();
-        g.max_col_work = std::max(g.max_col_work, std::max((int)rows.size(), 4 * (g.tr_off[K + 1] - g.tr_off[K])));
+        g.max_col_work = std::max(g.max_col_work, (int)rows.size() + 4 * (g.tr_off[K + 1] - g.tr_off[K]));
+        g.max_npan = std::max(g.max_npan, (int)rows.size());
     }
     if (g.pan_row.empty()) g.pan_row.push_back(0);
     if (g.tr_ij.empty()) g.tr_ij.push_back(make_int2(0, 0));
@@ -2093,6 +2399,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     int32_t* d_pan_off = dv.alloc<int32_t>(g.pan_off.size());
     int32_t* d_pan_row = dv.alloc<int32_t>(g.pan_row.size());
     int32_t* d_tr_off = dv.alloc<int32_t>(g.tr_off.size());
+    int32_t* d_tr_skip = dv.alloc<int32_t>(g.tr_skip.size());
     int2* d_tr_ij = dv.alloc<int2>(g.tr_ij.size());
     const int nk = (lm.optimize_k && intr.model == 1) ? 2 : 0;
     const int mt = m + nk;
@@ -2101,6 +2408,15 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     const bool mixed_chol = sizeof(Real) == 4 && !pcg && !vjp;
     float* d_S32 = mixed_chol ? dv.alloc<float>((size_t)std::max(1, m) * std::max(1, m)) : nullptr;
     float* d_rinv32 = mixed_chol ? dv.alloc<float>(std::max(1, m)) : nullptr;
+    // the panel tiles transposed, for the forward solves (Cholesky path only)
+    const size_t lt_elems = (!pcg || vjp != nullptr) ? g.pan_row.size() * (size_t)(kTile * kTile) : 1;
+    const size_t di_elems = (!pcg || vjp != nullptr) ? (size_t)std::max(1, (m + kTile - 1) / kTile) * 2 * kTile * kTile : 1;
+    float* d_LT32 = mixed_chol ? dv.alloc<float>(lt_elems) : nullptr;
+    float* d_LN32 = mixed_chol ? dv.alloc<float>(lt_elems) : nullptr;
+    float* d_DI32 = mixed_chol ? dv.alloc<float>(di_elems) : nullptr;
+    double* d_LT = dv.alloc<double>(lt_elems);
+    double* d_LN = dv.alloc<double>(lt_elems);
+    double* d_DI = dv.alloc<double>(di_elems);
     float* d_x32 = mixed_chol ? dv.alloc<float>(std::max(1, m)) : nullptr;
     float* d_y32 = mixed_chol ? dv.alloc<float>(std::max(1, m)) : nullptr;
     double* d_bs = dv.alloc<double>(std::max(1, mt));
@@ -2182,9 +2498,10 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     double* d_ppart = pcg ? dv.alloc<double>(7LL * pcg_grid) : nullptr;
     int32_t* d_pit = pcg ? dv.alloc<int32_t>(1) : nullptr;
     const char* ptv = getenv("NAVBA_PHASE_TIMING");
-    unsigned long long* d_pcg_phase = pcg && ptv && ptv[0] == '1' ? dv.alloc<unsigned long long>(5) : nullptr;
+    // NAVBA_PHASE_TIMING=1: block 0's cycles per phase of the PCG kernel or of the factorization
+    unsigned long long* d_phase = ptv && ptv[0] == '1' ? dv.alloc<unsigned long long>(5) : nullptr;
     if (dv.err != cudaSuccess) return dv.err;
-    if (d_pcg_phase) cudaMemsetAsync(d_pcg_phase, 0, 5 * sizeof(unsigned long long), st);
+    if (d_phase) cudaMemsetAsync(d_phase, 0, 5 * sizeof(unsigned long long), st);
     std::vector<int32_t> edge_fc(ne);
     for (int e = 0; e < ne; ++e) edge_fc[e] = h.cam_free[h.edge_cam[e]];
     cudaError_t e = cudaSuccess;
@@ -2213,6 +2530,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     chk(up(d_pan_off, g.pan_off, st));
     chk(up(d_pan_row, g.pan_row, st));
     chk(up(d_tr_off, g.tr_off, st));
+    chk(up(d_tr_skip, g.tr_skip, st));
     chk(up(d_tr_ij, g.tr_ij, st));
     if (pcg_x) {
         chk(up(d_rs_off, g.rs_off, st));
@@ -2297,18 +2615,20 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             unsigned long long cyc[5] = {0, 0, 0, 0, 0};
             if (phase && cudaMemcpyAsync(cyc, phase, sizeof(cyc), cudaMemcpyDeviceToHost, st) == cudaSuccess &&
                 cudaStreamSynchronize(st) == cudaSuccess) {
-                static const char* names[2][5] = {{"point t2", "camera items", "S p", "x/r update", "p update"},
-                                                  {"beta sums", "S p (own)", "S p (sync)", "x/r (own)", "x/r (sync)"}};
+                static const char* names[3][5] = {{"point t2", "camera items", "S p", "x/r update", "p update"},
+                                                  {"beta sums", "S p (own)", "S p (sync)", "x/r (own)", "x/r (sync)"},
+                                                  {"diagonal", "panels", "trailing", "grid sync", "inverses"}};
                 double tot = 0;
                 for (int k = 0; k < 5; ++k) tot += (double)cyc[k];
                 for (int k = 0; k < 5; ++k)
-                    fprintf(stderr, "[navba grid] pcg phase %-13s %14llu cycles %5.1f%%\n", names[explicit_s][k], cyc[k],
+                    fprintf(stderr, "[navba grid] %s phase %-13s %14llu cycles %5.1f%%\n",
+                            explicit_s == 2 ? "factorization" : "pcg", names[explicit_s][k], cyc[k],
                             tot > 0 ? 100.0 * cyc[k] / tot : 0.0);
             }
         }
     } loop_timer{std::chrono::steady_clock::now(), t_host, t_setup, +[](std::chrono::steady_clock::time_point a) {
                      return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
-                 }, d_pcg_phase, st, pcg_x ? 1 : 0};
+                 }, d_phase, st, pcg ? (pcg_x ? 1 : 0) : 2};
     int cur = 0;
     // NAVBA_VERBOSE=2: one line per damping trial (damping, outcome, CG iterations)
     const char* vtrial = getenv("NAVBA_VERBOSE");
@@ -2353,7 +2673,10 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         int dev = 0, nsm = 0, bps = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        int bps32 = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_cholesky_coop<double>, 256, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps32, k_cholesky_coop<float>, 256, 0);
+        bps = std::min(bps, bps32);
         chol_grid = std::max(1, std::min(nsm * std::max(1, std::min(bps, 2)), g.max_col_work));
     }
     auto factor_S = [&]() -> bool {
@@ -2361,13 +2684,19 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         chk(cudaMemcpyAsync(d_ok, &one, sizeof(int32_t), cudaMemcpyHostToDevice, st));
         double* Sp = d_S;
         int mm = m;
+        const int32_t* tf = d_tfirst;
         const int32_t* po = d_pan_off;
         const int32_t* pr = d_pan_row;
         const int32_t* to = d_tr_off;
+        const int32_t* tsk = d_tr_skip;
         const int2* tij = d_tr_ij;
         double* ri = d_rinv;
+        double* ltp = d_LT;
+        double* lnp = d_LN;
+        double* dip = d_DI;
         int32_t* okp = d_ok;
-        void* kargs[] = {&Sp, &mm, &po, &pr, &to, &tij, &ri, &okp};
+        unsigned long long* cph = d_phase;
+        void* kargs[] = {&Sp, &mm, &tf, &po, &pr, &to, &tsk, &tij, &ri, &ltp, &lnp, &dip, &okp, &cph};
         chk(cudaLaunchCooperativeKernel((const void*)k_cholesky_coop<double>, dim3(chol_grid), dim3(256), kargs, 0, st));
         int32_t okh = 1;
         chk(cudaMemcpyAsync(&okh, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
@@ -2377,16 +2706,21 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     // Mixed form: S x = b (x into d_bs) with the Cholesky factor of S rounded to FP32 and one FP64
     // refinement step (r = b - S x0 over the FP64 S, then the FP32 factor's solution of r added).
     // S's entries are FP32 sums already, so the FP32 factor's error is of the order of S's own; the
-    // refinement step removes it.  A pivot that is not positive in FP32 falls back to the FP64
-    // factorization.  Returns false if S is not positive definite in FP64 either.
-    // FP32 factorization with one FP64 refinement; a non-positive FP32 pivot falls back to the FP64
-    // factorization, and so do later trials at up to 4x the damping of the last failure (S is then
-    // too close to singular for FP32, and the failed attempt is not repeated)
+    // refinement step removes it.  A pivot that is not positive in FP32:
+    // - at a damping below kF32Resolution of the largest Hessian diagonal entry ends the trial as a
+    //   system that is not positive definite does (the damping grows): S's own FP32 rounding is then
+    //   larger than the damping that makes it definite, and the FP64 factorization of the same S
+    //   fails as well (measured on the 200-camera grid: every such attempt failed);
+    // - above it, falls back to the FP64 factorization, and so do later trials at up to 4x the
+    //   damping of the last failure (the failed attempt is not repeated).
+    // Returns false if S is not positive definite.
+    constexpr double kF32Resolution = 1e-6;
     double f32_fail_lambda = -1.0;
-    auto solve_S_mixed = [&](double lam) -> bool {
-        if (f32_fail_lambda > 0.0 && lam <= 4.0 * f32_fail_lambda) {
+    auto solve_S_mixed = [&](double lam, double maxdiag) -> bool {
+        const bool f64_useful = lam >= kF32Resolution * maxdiag;
+        if (f64_useful && f32_fail_lambda > 0.0 && lam <= 4.0 * f32_fail_lambda) {
             if (!factor_S()) return false;
-            k_chol_solve<<<1, 1024, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_bs);
+            chk(chol_solve(d_LT, d_LN, d_DI, m, d_pan_off, d_pan_row, d_bs, g.max_npan, st));
             return true;
         }
         const int32_t one = 1;
@@ -2394,13 +2728,19 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         k_s_round<<<nsm_blocks, TB, 0, st>>>(d_S, d_S32, m);
         float* Sp = d_S32;
         int mm = m;
+        const int32_t* tf = d_tfirst;
         const int32_t* po = d_pan_off;
         const int32_t* pr = d_pan_row;
         const int32_t* to = d_tr_off;
+        const int32_t* tsk = d_tr_skip;
         const int2* tij = d_tr_ij;
         float* ri = d_rinv32;
+        float* ltp = d_LT32;
+        float* lnp = d_LN32;
+        float* dip = d_DI32;
         int32_t* okp = d_ok;
-        void* kargs[] = {&Sp, &mm, &po, &pr, &to, &tij, &ri, &okp};
+        unsigned long long* cph = d_phase;
+        void* kargs[] = {&Sp, &mm, &tf, &po, &pr, &to, &tsk, &tij, &ri, &ltp, &lnp, &dip, &okp, &cph};
         chk(cudaLaunchCooperativeKernel((const void*)k_cholesky_coop<float>, dim3(chol_grid), dim3(256), kargs, 0, st));
         int32_t okh = 1;
         chk(cudaMemcpyAsync(&okh, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
@@ -2408,17 +2748,20 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         if (e != cudaSuccess) return false;
         if (!okh) {
             const char* vb = getenv("NAVBA_VERBOSE");
-            if (vb && vb[0] == '1') fprintf(stderr, "[navba grid] FP32 factor: non-positive pivot, FP64 factor instead\n");
+            if (vb && vb[0] == '1')
+                fprintf(stderr, "[navba grid] FP32 factor: non-positive pivot, %s\n",
+                        f64_useful ? "FP64 factor instead" : "trial rejected");
+            if (!f64_useful) return false;
             f32_fail_lambda = std::max(f32_fail_lambda, lam);
             if (!factor_S()) return false;
-            k_chol_solve<<<1, 1024, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_bs);
+            chk(chol_solve(d_LT, d_LN, d_DI, m, d_pan_off, d_pan_row, d_bs, g.max_npan, st));
             return true;
         }
         const int vb = (m + TB - 1) / TB;
         k_vec_round<<<vb, TB, 0, st>>>(d_bs, d_x32, m);
-        k_chol_solve<<<1, 1024, 0, st>>>(d_S32, m, d_tfirst, d_rinv32, d_x32);
+        chk(chol_solve(d_LT32, d_LN32, d_DI32, m, d_pan_off, d_pan_row, d_x32, g.max_npan, st));
         k_s_residual<<<nsm_blocks, TB, 0, st>>>(d_S, d_x32, d_bs, m, d_y32);
-        k_chol_solve<<<1, 1024, 0, st>>>(d_S32, m, d_tfirst, d_rinv32, d_y32);
+        chk(chol_solve(d_LT32, d_LN32, d_DI32, m, d_pan_off, d_pan_row, d_y32, g.max_npan, st));
         k_vec_sum<<<vb, TB, 0, st>>>(d_bs, d_x32, d_y32, m);
         chk(cudaGetLastError());
         return true;
@@ -2455,7 +2798,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             if (nfc > 0) {
                 assemble_S(lam);
                 ok = factor_S() && ok;
-                if (ok) k_chol_solve<<<1, 1024, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_bs);
+                if (ok) chk(chol_solve(d_LT, d_LN, d_DI, m, d_pan_off, d_pan_row, d_bs, g.max_npan, st));
                 chk(cudaGetLastError());
             }
             if (e != cudaSuccess) return e;
@@ -2594,7 +2937,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                 PA.max_it = lm.pcg_max_iterations;
                 PA.tol2 = lm.pcg_tolerance * lm.pcg_tolerance;
                 PA.iters = d_pit;
-                PA.phase = d_pcg_phase;
+                PA.phase = d_phase;
                 if (pcg_x) {
                     PcgXArgs<Real> XA;
                     XA.Sb = d_Sb;
@@ -2621,7 +2964,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                     XA.max_it = lm.pcg_max_iterations;
                     XA.tol2 = PA.tol2;
                     XA.iters = d_pit;
-                    XA.phase = d_pcg_phase;
+                    XA.phase = d_phase;
                     void* kargs[] = {&XA};
                     chk(cudaLaunchCooperativeKernel((const void*)k_pcg_explicit<Real>, dim3(pcg_grid), dim3(256), kargs, 0,
                                                     st));
@@ -2655,10 +2998,10 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                     return e;
                 }
                 if (mixed_chol) {
-                    ok = solve_S_mixed(lam_use) && ok;
+                    ok = solve_S_mixed(lam_use, maxdiag) && ok;
                 } else {
                     ok = factor_S() && ok;
-                    if (ok) k_chol_solve<<<1, 1024, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_bs);
+                    if (ok) chk(chol_solve(d_LT, d_LN, d_DI, m, d_pan_off, d_pan_row, d_bs, g.max_npan, st));
                 }
                 if (e != cudaSuccess) return e;
                 if (!ok) chk(cudaMemsetAsync(d_bs, 0, sizeof(double) * m, st));
@@ -2783,7 +3126,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                     return cudaSuccess;
                 }
                 // the step: dx_c (in d_bs), dx_p
-                if (nfc > 0) k_chol_solve<<<1, 1024, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_bs);
+                if (nfc > 0) chk(chol_solve(d_LT, d_LN, d_DI, m, d_pan_off, d_pan_row, d_bs, g.max_npan, st));
                 k_vjp_point_solve<<<pblocks, TB, 0, st>>>(A, np, d_lt, 12, 6, d_bs, d_dp);
                 // adjoint through [+]: rc = J_l^T xbar'_c, xa = Ad^T xbar'_c; r_p = xbar'_p
                 if (nfc > 0) k_vjp_cams_step<<<(nfc + 127) / 128, 128, 0, st>>>(d_bs, xb, d_rc, xa, nfc);
@@ -2793,7 +3136,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                     cam_sum(d_tr, true);
                     chk(cudaMemcpyAsync(d_uc, d_rc, sizeof(double) * m, cudaMemcpyDeviceToDevice, st));
                     k_vjp_axpy<<<rblocks, TB, 0, st>>>(d_uc, d_ctmp, -1.0, m);
-                    k_chol_solve<<<1, 1024, 0, st>>>(d_S, m, d_tfirst, d_rinv, d_uc);
+                    chk(chol_solve(d_LT, d_LN, d_DI, m, d_pan_off, d_pan_row, d_uc, g.max_npan, st));
                 }
                 k_vjp_point_solve<<<pblocks, TB, 0, st>>>(A, np, d_tr, 4, 0, d_uc, d_up);
                 // grad psi at the state: points into d_pbar, cameras into xa, observations, intrinsics

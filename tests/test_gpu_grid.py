@@ -93,3 +93,21 @@ def test_grid_host_structure_passes_agree(ctx, monkeypatch, solver):
     assert a.status == abi.OK and b.status == abi.OK
     assert np.array_equal(a.cam_pose, b.cam_pose) and np.array_equal(a.points, b.points)
     assert np.array_equal(a.cost_trace, b.cost_trace, equal_nan=True)
+
+
+@pytest.mark.parametrize("precision", [abi.FP64, abi.MIXED])
+def test_grid_solve_forms_agree(ctx, monkeypatch, precision):
+    """The triangular solves keep x in shared memory when it fits and in global memory beyond
+    (NAVBA_SOLVE_GLOBAL_X=1 forces the latter); both run the same operations in the same order, so
+    the solves agree bit for bit."""
+    p = grid_problem()
+    o = abi.default_options(iterations=6, robust=1, huber_delta=2.0)
+    o.precision = precision
+    res = []
+    for mode in ("", "1"):
+        monkeypatch.setenv("NAVBA_SOLVE_GLOBAL_X", mode)
+        res.append(ctx.solve(p, o))
+    a, b = res
+    assert a.status == abi.OK and b.status == abi.OK
+    assert np.array_equal(a.cam_pose, b.cam_pose) and np.array_equal(a.points, b.points)
+    assert np.array_equal(a.cost_trace, b.cost_trace, equal_nan=True)
