@@ -495,37 +495,84 @@ __global__ void __launch_bounds__(256) k_cholesky_coop(T* S, int m, const int32_
 #pragma unroll
         for (int q = 0; q < 4; ++q) dst[r + 8 * q][c] -= s[q];
     };
-    // this block's panel tiles of column K (L_KK in tk, 1/L_jj in rv); with upd_prev, first
-    // A_IK -= L_I,K-1 L_K,K-1^T (L_K,K-1 in tb) for the rows inside column K - 1's envelope
-    auto panel_tiles = [&](int K, bool upd_prev) {
+    // dst -= a b^T by warps 1..7 (while warp 0 factors the diagonal tile), four partial sums
+    auto sub_abt_w = [&](TileT<T>& dst, const TileT<T>& a, const TileT<T>& b) {
+        for (int o = tid - kTile; o < kTile * kTile; o += blockDim.x - kTile) {
+            const int r = o >> 5, c = o & 31;
+            T s4[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+            for (int t = 0; t < kTile; ++t) s4[t & 3] += a[r][t] * b[c][t];
+            dst[r][c] -= (s4[0] + s4[1]) + (s4[2] + s4[3]);
+        }
+    };
+    // panel tile pi of column K: its loads into ta (and L_I,K-1 into tc when it gets column K - 1's
+    // update, upd_prev: L_K,K-1 in tb); returns whether it does
+    auto panel_load = [&](int K, int pi, bool upd_prev) {
         const int k0 = K * kTile, kb = min(kTile, m - k0), kp = k0 - kTile;
-        const int p0 = pan_off[K], npan = pan_off[K + 1] - p0;
-        for (int pi = bid; pi < npan; pi += nb) {
-            const int I = pan_row[p0 + pi];
-            const int i0 = I * kTile, ib = min(kTile, m - i0);
-            const bool upd = upd_prev && tfirst[I] <= K - 1;
-            tile_load(ta, S, m, i0, ib, k0, kb);
-            if (upd) tile_load(tc, S, m, i0, ib, kp, kTile);
+        const int I = pan_row[pan_off[K] + pi], i0 = I * kTile, ib = min(kTile, m - i0);
+        const bool upd = upd_prev && tfirst[I] <= K - 1;
+        tile_load(ta, S, m, i0, ib, k0, kb);
+        if (upd) tile_load(tc, S, m, i0, ib, kp, kTile);
+        return upd;
+    };
+    // panel tile pi of column K, updated, in ta: L_IK = A_IK L_KK^-T (L_KK in tk, 1/L_jj in rv),
+    // stored into S and, contiguous, into LT (transposed) and LN for the solves
+    auto panel_finish = [&](int K, int pi) {
+        const int k0 = K * kTile, kb = min(kTile, m - k0), p0 = pan_off[K];
+        const int i0 = pan_row[p0 + pi] * kTile, ib = min(kTile, m - i0);
+        if (wid == 0) panel_solve(ta, tk, rv, ib, kb);
+        __syncthreads();
+        for (int idx = tid; idx < ib * kb; idx += blockDim.x) {
+            const int i = idx / kb, j = idx % kb;
+            S[(size_t)(i0 + i) * m + k0 + j] = ta[i][j];
+        }
+        T* lt = LT + (size_t)(p0 + pi) * (kTile * kTile);
+        T* ln = LN + (size_t)(p0 + pi) * (kTile * kTile);
+        for (int idx = tid; idx < kTile * kTile; idx += blockDim.x) {
+            lt[idx] = ta[idx & 31][idx >> 5];
+            ln[idx] = ta[idx >> 5][idx & 31];
+        }
+        __syncthreads();
+    };
+    // the diagonal tile of column K (minus column K - 1's update with upd_prev), factored, and this
+    // block's panel tiles: the first tile's loads go with the diagonal tile's, and its update runs
+    // on warps 1..7 while warp 0 factors (FP32)
+    auto column = [&](int K, bool upd_prev) {
+        const int k0 = K * kTile, kb = min(kTile, m - k0), kp = k0 - kTile;
+        const int npan = pan_off[K + 1] - pan_off[K];
+        __syncthreads();
+        tile_load(tk, S, m, k0, kb, k0, kb, true);
+        if (upd_prev) tile_load(tb, S, m, k0, kb, kp, kTile);
+        const bool first = bid < npan;
+        const bool upd0 = first && panel_load(K, bid, upd_prev);
+        __syncthreads();
+        if (upd_prev) {
+            sub_aat(tk, tb, tb);
+            __syncthreads();
+        }
+        factor_diag_tile(tk, rv, col, kb, bad);
+        if constexpr (sizeof(T) == 4) {
+            if (upd0 && wid > 0) sub_abt_w(ta, tc, tb);
+        }
+        __syncthreads();
+        if constexpr (sizeof(T) != 4) {
+            if (upd0) {
+                sub_aat(ta, tc, tb);
+                __syncthreads();
+            }
+        }
+        mark(0);
+        if (first) panel_finish(K, bid);
+        for (int pi = bid + nb; pi < npan; pi += nb) {
+            const bool upd = panel_load(K, pi, upd_prev);
             __syncthreads();
             if (upd) {
                 sub_aat(ta, tc, tb);
                 __syncthreads();
             }
-            if (wid == 0) panel_solve(ta, tk, rv, ib, kb);
-            __syncthreads();
-            for (int idx = tid; idx < ib * kb; idx += blockDim.x) {
-                const int i = idx / kb, j = idx % kb;
-                S[(size_t)(i0 + i) * m + k0 + j] = ta[i][j];
-            }
-            // the tile contiguous for the solves: transposed for the forward one, as is for the backward
-            T* lt = LT + (size_t)(p0 + pi) * (kTile * kTile);
-            T* ln = LN + (size_t)(p0 + pi) * (kTile * kTile);
-            for (int idx = tid; idx < kTile * kTile; idx += blockDim.x) {
-                lt[idx] = ta[idx & 31][idx >> 5];
-                ln[idx] = ta[idx >> 5][idx & 31];
-            }
-            __syncthreads();
+            panel_finish(K, pi);
         }
+        mark(1);
     };
     // trailing update A_IJ -= L_I,c L_J,c^T over the listed tiles [t0, t1) of column c, in
     // quarter-tile work items (8 rows x 32 columns, one output per thread), first to the blocks
@@ -557,25 +604,11 @@ __global__ void __launch_bounds__(256) k_cholesky_coop(T* S, int m, const int32_
     };
     if constexpr (one_sync) {
         for (int K = 0; K < nt; ++K) {
-            const int k0 = K * kTile, kb = min(kTile, m - k0), kp = k0 - kTile;
+            const int k0 = K * kTile, kb = min(kTile, m - k0);
             const int npan = pan_off[K + 1] - pan_off[K];
             const bool upd_prev = K > 0 && tfirst[K] <= K - 1;  // L_K,K-1 is inside the envelope
-            if (bid == 0 || bid < npan) {
-                // A_KK minus column K - 1's update, factored (every panel block, redundantly)
-                __syncthreads();
-                tile_load(tk, S, m, k0, kb, k0, kb, true);
-                if (upd_prev) tile_load(tb, S, m, k0, kb, kp, kTile);
-                __syncthreads();
-                if (upd_prev) {
-                    sub_aat(tk, tb, tb);
-                    __syncthreads();
-                }
-                factor_diag_tile(tk, rv, col, kb, bad);
-                __syncthreads();
-                mark(0);
-                panel_tiles(K, upd_prev);
-                mark(1);
-            }
+            // A_KK minus column K - 1's update, factored by every panel block (redundantly)
+            if (bid == 0 || bid < npan) column(K, upd_prev);
             // column K - 1's update of the trailing tiles right of column K
             if (K > 0) trailing(K - 1, tr_off[K - 1] + tr_skip[K - 1], tr_off[K], npan);
             mark(2);
@@ -587,16 +620,7 @@ __global__ void __launch_bounds__(256) k_cholesky_coop(T* S, int m, const int32_
         for (int K = 0; K < nt; ++K) {
             const int k0 = K * kTile, kb = min(kTile, m - k0);
             const int npan = pan_off[K + 1] - pan_off[K];
-            if (bid == 0 || bid < npan) {
-                __syncthreads();
-                tile_load(tk, S, m, k0, kb, k0, kb, true);
-                __syncthreads();
-                factor_diag_tile(tk, rv, col, kb, bad);
-                __syncthreads();
-                mark(0);
-                panel_tiles(K, false);
-                mark(1);
-            }
+            if (bid == 0 || bid < npan) column(K, false);
             grid.sync();
             mark(3);
             if (bid == 0) store_diag(k0, kb);  // every block has read A_KK
