@@ -341,14 +341,17 @@ __device__ __forceinline__ void tile_abt(const TileT<T>& a, const TileT<T>& b, T
 // LL^T of the kb x kb lower tile tk in place; rv[j] receives 1/L_jj.  Per column: the pivot, the
 // column scaled by 1/L_jj, the rank-1 update of the columns to its right.  Called by every thread
 // of the block; a barrier must follow.
-// - FP32: warp 0 alone, lane i holding row i in registers.  Each column's unscaled values go
-//   through shared memory (col, double-buffered): every lane reads the pivot u_cc, forms
-//   r = 1/sqrt(u_cc) itself and its L_ic = u_ic r, and updates u_ij -= (L_ic r) u_jc; one warp
-//   barrier per column (a shuffle per element was 5x slower).
+// - FP32: warp 0 alone, lane i holding row i in registers, in panels of 8 columns.  Each column's
+//   unscaled values go through shared memory (col, double-buffered): every lane reads the pivot
+//   u_cc, forms r = 1/sqrt(u_cc) itself and its L_ic = u_ic r, and updates the panel's columns,
+//   u_ij -= (L_ic r) u_jc; one warp barrier per column (a shuffle per element was 5x slower).  The
+//   panel's L columns (pcol) then update the columns to its right in one rank-8 pass, so the
+//   column-by-column chain touches 8 columns instead of up to 31.
 // - FP64: the whole block (warp per row of the update), so that the FP64 products are spread over
 //   the SM's four partitions.
+constexpr int kDiagPanel = 8;  // FP32 diagonal-tile factorization: columns per panel
 template <class T>
-__device__ void factor_diag_tile(TileT<T>& tk, T* rv, T (*col)[kTile], int kb, int& bad) {
+__device__ void factor_diag_tile(TileT<T>& tk, T* rv, T (*col)[kTile], T (*pcol)[kTile], int kb, int& bad) {
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     if constexpr (sizeof(T) == 4) {
         if (wid != 0) return;
@@ -358,21 +361,38 @@ __device__ void factor_diag_tile(TileT<T>& tk, T* rv, T (*col)[kTile], int kb, i
         col[0][lane] = d[0];
         __syncwarp();
 #pragma unroll
-        for (int cc = 0; cc < kTile; ++cc) {
-            if (cc < kb) {
-                const T* cu = col[cc & 1];  // column cc, unscaled
-                const T piv = cu[cc];
-                const bool colbad = !(piv > T(0)) || !isfinite(piv);
-                const T r = colbad ? T(1) : rsqrtf(piv);
-                if (colbad) bad = 1;
-                const T li = lane == cc ? (colbad ? T(1) : piv * r) : d[cc] * r;
-                d[cc] = li;
-                const T wi = li * r;
-                if (lane == 0) rv[cc] = r;
+        for (int c0 = 0; c0 < kTile; c0 += kDiagPanel) {
+            // the panel's columns one by one, updating only the panel's own columns
 #pragma unroll
-                for (int j = cc + 1; j < kTile; ++j)
-                    if (lane >= j) d[j] -= wi * cu[j];
-                if (cc + 1 < kTile) col[(cc + 1) & 1][lane] = d[cc + 1];
+            for (int cc = c0; cc < c0 + kDiagPanel; ++cc) {
+                if (cc < kb) {
+                    const T* cu = col[cc & 1];  // column cc, unscaled
+                    const T piv = cu[cc];
+                    const bool colbad = !(piv > T(0)) || !isfinite(piv);
+                    const T r = colbad ? T(1) : rsqrtf(piv);
+                    if (colbad) bad = 1;
+                    const T li = lane == cc ? (colbad ? T(1) : piv * r) : d[cc] * r;
+                    d[cc] = li;
+                    pcol[cc - c0][lane] = li;
+                    const T wi = li * r;
+                    if (lane == 0) rv[cc] = r;
+#pragma unroll
+                    for (int j = cc + 1; j < c0 + kDiagPanel; ++j)
+                        if (lane >= j) d[j] -= wi * cu[j];
+                    if (cc + 1 < c0 + kDiagPanel) col[(cc + 1) & 1][lane] = d[cc + 1];
+                    __syncwarp();
+                }
+            }
+            // the panel's rank-kDiagPanel update of the columns to its right: u_ij -= sum_c L_ic L_jc
+            if (c0 + kDiagPanel < kb) {
+#pragma unroll
+                for (int j = c0 + kDiagPanel; j < kTile; ++j) {
+                    T s = T(0);
+#pragma unroll
+                    for (int c = 0; c < kDiagPanel; ++c) s += d[c0 + c] * pcol[c][j];
+                    if (lane >= j) d[j] -= s;
+                }
+                col[(c0 + kDiagPanel) & 1][lane] = d[c0 + kDiagPanel];
                 __syncwarp();
             }
         }
@@ -465,7 +485,7 @@ __global__ void __launch_bounds__(256) k_cholesky_coop(T* S, int m, const int32_
     constexpr bool one_sync = sizeof(T) == 4;
     cg::grid_group grid = cg::this_grid();
     __shared__ TileT<T> tk, ta, tb, tc;
-    __shared__ T rv[kTile], col[2][kTile];
+    __shared__ T rv[kTile], col[2][kTile], pcol[kDiagPanel][kTile];
     __shared__ int sbad;
     const int tid = threadIdx.x, nb = gridDim.x, bid = blockIdx.x, wid = tid >> 5;
     const int nt = (m + kTile - 1) / kTile;
@@ -550,7 +570,7 @@ __global__ void __launch_bounds__(256) k_cholesky_coop(T* S, int m, const int32_
             sub_aat(tk, tb, tb);
             __syncthreads();
         }
-        factor_diag_tile(tk, rv, col, kb, bad);
+        factor_diag_tile(tk, rv, col, pcol, kb, bad);
         if constexpr (sizeof(T) == 4) {
             if (upd0 && wid > 0) sub_abt_w(ta, tc, tb);
         }
