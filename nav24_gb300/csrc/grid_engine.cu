@@ -2477,6 +2477,9 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     const int cblocks = std::max(1, (nc + TB - 1) / TB);
     const int npart = std::max(5 * pblocks, std::max(cblocks, (nfc * 27 + TB - 1) / TB + 1));
     double* d_part = dv.alloc<double>(npart);
+    // a damping trial's partial sums, read back together at its end: point blocks that failed,
+    // the model decrease's camera and point terms, the trial cost
+    double* d_tpart = dv.alloc<double>(3LL * pblocks + cblocks);
     // PCG and distortion buffers
     const int n_items = (int)g.items.size();
     Real* d_kp = nk ? dv.alloc<Real>(12LL * np) : nullptr;
@@ -2619,7 +2622,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     double kcur[2] = {intr.k1, intr.k2};  // current shared distortion (free when nk == 2)
     double Kk[3] = {0, 0, 0}, gk[2] = {0, 0};
     int pcg_total = 0;
-    std::vector<double> hpart(npart);
+    std::vector<double> hpart(npart), hpart_trial(3LL * pblocks + cblocks);
     auto sum_part = [&](int n, bool mx) -> double {
         if (e != cudaSuccess) return 0.0;
         e = cudaMemcpyAsync(hpart.data(), d_part, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
@@ -2723,7 +2726,8 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         bps = std::min(bps, bps32);
         chol_grid = std::max(1, std::min(nsm * std::max(1, std::min(bps, 2)), g.max_col_work));
     }
-    auto factor_S = [&]() -> bool {
+    // defer: the pivot flag (d_ok) is left for the trial's read-back instead of read here
+    auto factor_S = [&](bool defer = false) -> bool {
         const int32_t one = 1;
         chk(cudaMemcpyAsync(d_ok, &one, sizeof(int32_t), cudaMemcpyHostToDevice, st));
         double* Sp = d_S;
@@ -2742,6 +2746,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         unsigned long long* cph = d_phase;
         void* kargs[] = {&Sp, &mm, &tf, &po, &pr, &to, &tsk, &tij, &ri, &ltp, &lnp, &dip, &okp, &cph};
         chk(cudaLaunchCooperativeKernel((const void*)k_cholesky_coop<double>, dim3(chol_grid), dim3(256), kargs, 0, st));
+        if (defer) return e == cudaSuccess;
         int32_t okh = 1;
         chk(cudaMemcpyAsync(&okh, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
         chk(cudaStreamSynchronize(st));
@@ -2760,8 +2765,11 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     // Returns false if S is not positive definite.
     constexpr double kF32Resolution = 1e-6;
     double f32_fail_lambda = -1.0;
-    auto solve_S_mixed = [&](double lam, double maxdiag) -> bool {
+    // deferred: set when the FP32 pivot flag is left for the trial's read-back (no FP64 fallback
+    // at this damping, so nothing waits on it)
+    auto solve_S_mixed = [&](double lam, double maxdiag, bool& deferred) -> bool {
         const bool f64_useful = lam >= kF32Resolution * maxdiag;
+        deferred = false;
         if (f64_useful && f32_fail_lambda > 0.0 && lam <= 4.0 * f32_fail_lambda) {
             if (!factor_S()) return false;
             chk(chol_solve(d_LT, d_LN, d_DI, m, d_pan_off, d_pan_row, d_bs, g.max_npan, st));
@@ -2787,8 +2795,12 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         void* kargs[] = {&Sp, &mm, &tf, &po, &pr, &to, &tsk, &tij, &ri, &ltp, &lnp, &dip, &okp, &cph};
         chk(cudaLaunchCooperativeKernel((const void*)k_cholesky_coop<float>, dim3(chol_grid), dim3(256), kargs, 0, st));
         int32_t okh = 1;
-        chk(cudaMemcpyAsync(&okh, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-        chk(cudaStreamSynchronize(st));
+        if (f64_useful) {
+            chk(cudaMemcpyAsync(&okh, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+            chk(cudaStreamSynchronize(st));
+        } else {
+            deferred = true;
+        }
         if (e != cudaSuccess) return false;
         if (!okh) {
             const char* vb = getenv("NAVBA_VERBOSE");
@@ -2893,9 +2905,10 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         int q = 0;
         do {
             const double lam_use = (debug_S && it == 0 && q == 0) ? debug_lambda : lambda;
-            k_schur_points<Real><<<pblocks, TB, 0, st>>>(A, D, lam_use, camr[cur], A.x[cur], d_part);
-            const double npd = sum_part(pblocks, false);
-            bool ok = npd == 0.0;
+            // point blocks whose V + lambda I is not positive definite: counted into the trial's
+            // read-back (the trial is then rejected; the work between is discarded)
+            k_schur_points<Real><<<pblocks, TB, 0, st>>>(A, D, lam_use, camr[cur], A.x[cur], d_tpart);
+            bool ok = true, okh_deferred = false;
             double dk[2] = {0.0, 0.0};
             if (pcg && mt > 0) {
                 if (pcg_i) k_pcg_pack<Real><<<nsm_blocks, TB, 0, st>>>(A, ne, d_list, ncl, d_apm, d_acm);
@@ -3042,9 +3055,11 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                     return e;
                 }
                 if (mixed_chol) {
-                    ok = solve_S_mixed(lam_use, maxdiag) && ok;
+                    ok = solve_S_mixed(lam_use, maxdiag, okh_deferred) && ok;
                 } else {
-                    ok = factor_S() && ok;
+                    // a failed factorization rejects the trial: its flag is read with the trial's sums
+                    ok = factor_S(true) && ok;
+                    okh_deferred = true;
                     if (ok) chk(chol_solve(d_LT, d_LN, d_DI, m, d_pan_off, d_pan_row, d_bs, g.max_npan, st));
                 }
                 if (e != cudaSuccess) return e;
@@ -3052,14 +3067,35 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                 chk(cudaGetLastError());
             }
             k_update_cams<Real><<<cblocks, TB, 0, st>>>(cams[cur], cams[cur ^ 1], camr[cur ^ 1], d_cam_free, nc, d_bs, d_U,
-                                                         lambda, d_part);
-            double scale = sum_part(cblocks, false);
-            k_update_points<Real><<<pblocks, TB, 0, st>>>(A, D, lambda, d_bs, cur, d_part);
-            scale += sum_part(pblocks, false);
-            scale += dk[0] * (lambda * dk[0] + gk[0]) + dk[1] * (lambda * dk[1] + gk[1]);
+                                                         lambda, d_tpart + pblocks);
+            k_update_points<Real><<<pblocks, TB, 0, st>>>(A, D, lambda, d_bs, cur, d_tpart + pblocks + cblocks);
             set_radial(A.intr, kcur[0] + dk[0], kcur[1] + dk[1]);
-            double chi_new = cost_of(cur ^ 1, true);
+            {  // the trial cost (FP64 in both forms)
+                const int buf = cur ^ 1;
+                double* cpart = d_tpart + 2LL * pblocks + cblocks;
+                if (mixed) {
+                    k_cams_real<double><<<cblocks, TB, 0, st>>>(cams[buf], nc, d_camd);
+                    k_cost<double, Real><<<pblocks, TB, 0, st>>>(A, D, d_camd, A.x[buf], cpart, d_ep[buf]);
+                } else {
+                    k_cost<Real, Real><<<pblocks, TB, 0, st>>>(A, D, camr[buf], A.x[buf], cpart);
+                }
+                chk(cudaGetLastError());
+            }
+            // the trial's one read-back
+            std::vector<double>& tp = hpart_trial;
+            int32_t okd = 1;
+            chk(cudaMemcpyAsync(tp.data(), d_tpart, sizeof(double) * tp.size(), cudaMemcpyDeviceToHost, st));
+            if (okh_deferred) chk(cudaMemcpyAsync(&okd, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+            chk(cudaStreamSynchronize(st));
             if (e != cudaSuccess) return e;
+            double npd = 0.0, scale_c = 0.0, scale_p = 0.0, chi_new = 0.0;
+            for (int k = 0; k < pblocks; ++k) npd += tp[k];
+            for (int k = 0; k < cblocks; ++k) scale_c += tp[pblocks + k];
+            for (int k = 0; k < pblocks; ++k) scale_p += tp[pblocks + cblocks + k];
+            for (int k = 0; k < pblocks; ++k) chi_new += tp[2 * pblocks + cblocks + k];
+            double scale = scale_c + scale_p;
+            scale += dk[0] * (lambda * dk[0] + gk[0]) + dk[1] * (lambda * dk[1] + gk[1]);
+            if (npd != 0.0 || okd == 0) ok = false;
             if (!ok) chi_new = DBL_MAX;
             trial_ok = ok;
             rho = chi - chi_new;
