@@ -1118,8 +1118,27 @@ __global__ void k_pcg_precond(const double* U, const double* aat, int nfc, doubl
 }
 
 // The same block-Jacobi factor from the diagonal slots of the explicit S (lambda included).
+// z = P_a^-1 r for camera a (6x6 Cholesky factors with inverse diagonal).
+__device__ __forceinline__ void precond_cam(const double* pc, int a, const double* r, double* z) {
+    const double* L = pc + 28LL * a;
+    const double* ri = L + 21;
+    double v[6];
+    for (int i = 0; i < 6; ++i) {
+        double s = r[i];
+        for (int k = 0; k < i; ++k) s -= L[tri(i, k)] * v[k];
+        v[i] = s * ri[i];
+    }
+    for (int i = 5; i >= 0; --i) {
+        double s = v[i];
+        for (int k = i + 1; k < 6; ++k) s -= L[tri(k, i)] * v[k];
+        v[i] = s * ri[i];
+    }
+    for (int i = 0; i < 6; ++i) z[i] = v[i];
+}
+
 template <class Real>
-__global__ void k_pcg_precond_blocks(const Real* Sb, const int32_t* dslot, int nfc, double* pc, int32_t* ok) {
+__global__ void k_pcg_precond_blocks(const Real* Sb, const int32_t* dslot, int nfc, double* pc, double* pcinv,
+                                     int32_t* ok) {
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= nfc) return;
     const Real* d = Sb + 36LL * dslot[a];
@@ -1130,6 +1149,13 @@ __global__ void k_pcg_precond_blocks(const Real* Sb, const int32_t* dslot, int n
     const bool good = chol6_packed(P, rinv);
     for (int k = 0; k < 21; ++k) pc[28LL * a + k] = P[k];
     for (int k = 0; k < 6; ++k) pc[28LL * a + 21 + k] = rinv[k];
+    // the block's inverse (row-major 6 x 6), column by column through the factors
+    for (int j = 0; j < 6; ++j) {
+        double e[6] = {0, 0, 0, 0, 0, 0}, z[6];
+        e[j] = 1.0;
+        precond_cam(pc, a, e, z);
+        for (int i = 0; i < 6; ++i) pcinv[36LL * a + 6 * i + j] = z[i];
+    }
     if (!good) ok[0] = 0;
 }
 
@@ -1292,24 +1318,6 @@ __device__ void grid_sum_w0(const double* part, int n, double (&out)[N]) {
 #pragma unroll
     for (int k = 0; k < N; ++k) out[k] = res[k];
     __syncthreads();
-}
-
-// z = P_a^-1 r for camera a (6x6 Cholesky factors with inverse diagonal).
-__device__ __forceinline__ void precond_cam(const double* pc, int a, const double* r, double* z) {
-    const double* L = pc + 28LL * a;
-    const double* ri = L + 21;
-    double v[6];
-    for (int i = 0; i < 6; ++i) {
-        double s = r[i];
-        for (int k = 0; k < i; ++k) s -= L[tri(i, k)] * v[k];
-        v[i] = s * ri[i];
-    }
-    for (int i = 5; i >= 0; --i) {
-        double s = v[i];
-        for (int k = i + 1; k < 6; ++k) s -= L[tri(k, i)] * v[k];
-        v[i] = s * ri[i];
-    }
-    for (int i = 0; i < 6; ++i) z[i] = v[i];
 }
 
 // z = P_k^-1 r for the 2x2 intrinsics block (lower Cholesky l00 l10 l11 in pk).
@@ -1583,7 +1591,7 @@ struct PcgXArgs {
     const int32_t* rs_col;  // column camera of each slot
     const double* Hck;      // H_ck per camera (12, entry r * 2 + j), when nk
     const double* Xak;      // sum A B per camera (12), when nk
-    const double* pc;       // block-Jacobi factors (28 per camera)
+    const double* pcinv;    // block-Jacobi blocks' inverses (36 per camera, row-major)
     const double* kk;       // [3..5]: factor of the k block's preconditioner
     double skk[3];          // S_kk (00, 01, 11), lambda included
     const double* b;        // right-hand side (6 nfc + nk)
@@ -1637,7 +1645,7 @@ __device__ __forceinline__ void load6(const double* s, double (&v)[6]) {
 }
 
 template <class Real>
-__global__ void __launch_bounds__(256) k_pcg_explicit(PcgXArgs<Real> P) {
+__global__ void __launch_bounds__(256, 2) k_pcg_explicit(PcgXArgs<Real> P) {
     cg::grid_group grid = cg::this_grid();
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     const int nb = gridDim.x;
@@ -1653,11 +1661,26 @@ __global__ void __launch_bounds__(256) k_pcg_explicit(PcgXArgs<Real> P) {
         P.phase[k] += (unsigned long long)(now - tmark);
         tmark = now;
     };
-    // per-camera work (thread per camera) in chunks of 32 cameras spread over the blocks first:
-    // the FP64 pipe is per SM, and a few thousand cameras are a few warps' work.  Each camera's
-    // vectors are read into registers before anything is stored (the vectors may alias as far as
-    // the compiler knows, which would otherwise order every load after the previous store).
-    const int nchunk = (P.nfc + 31) >> 5, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+    // per-camera work in chunks of 5 cameras per warp, lane per component (lanes 6g..6g+5: camera
+    // 5c + g; lanes 30, 31 idle), spread over the blocks first.  An FP64 instruction costs its SM
+    // partition 64 cycles per warp whatever its active lanes, so a camera's six components go across
+    // lanes (an FP64 instruction per warp for all of them) rather than down one lane's registers (six
+    // or more); the block-Jacobi inverse is applied as a row per lane against the group's residual.
+    // Each lane's values are read into registers before anything is stored (the vectors may alias
+    // as far as the compiler knows).
+    const int nchunk = (P.nfc + 4) / 5, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+    const int grp = lane / 6, comp = lane - 6 * grp, glead = 6 * min(grp, 4);
+    // z_comp = (M_a^-1 r)_comp from the group's six residual components (all lanes shuffle)
+    auto apply_inv = [&](int a, bool act, double rv) {
+        const double* mi = P.pcinv + 36LL * (act ? a : 0) + 6 * (act ? comp : 0);
+        double z = 0.0;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const double rk = __shfl_sync(kFullG, rv, glead + k);
+            z += mi[k] * rk;
+        }
+        return z;
+    };
     // the k block's scalar work: thread 0 of the first block without a camera chunk
     const bool kthread = P.nk && threadIdx.x == 0 && blockIdx.x == min(nchunk, nb - 1);
     // k preconditioner: lower Cholesky l00 l10 l11 with the reciprocals of the diagonal
@@ -1675,22 +1698,20 @@ __global__ void __launch_bounds__(256) k_pcg_explicit(PcgXArgs<Real> P) {
     {
         double rz = 0.0, rr = 0.0;
         for (int c = blockIdx.x + nb * wib; c < nchunk; c += nb * nwb) {
-            const int a = 32 * c + lane;
-            if (a >= P.nfc) continue;
-            double rv[6], zv[6];
-#pragma unroll
-            for (int i = 0; i < 6; ++i) rv[i] = P.b[6 * a + i];
-            precond_cam(P.pc, a, rv, zv);
-#pragma unroll
-            for (int i = 0; i < 6; ++i) {
-                P.x[6 * a + i] = 0.0;
-                P.p[0][6 * a + i] = 0.0;
-                P.r[6 * a + i] = rv[i];
-                P.z[6 * a + i] = zv[i];
-                P.zr[8 * a + i] = (Real)zv[i];
-                P.pr[0][8 * a + i] = Real(0);
-                rz += rv[i] * zv[i];
-                rr += rv[i] * rv[i];
+            const int a = 5 * c + grp;
+            const bool act = grp < 5 && a < P.nfc;
+            const int i = 6 * a + comp;
+            const double rv = act ? P.b[i] : 0.0;
+            const double zv = apply_inv(a, act, rv);
+            if (act) {
+                P.x[i] = 0.0;
+                P.p[0][i] = 0.0;
+                P.r[i] = rv;
+                P.z[i] = zv;
+                P.zr[8 * a + comp] = (Real)zv;
+                P.pr[0][8 * a + comp] = Real(0);
+                rz += rv * zv;
+                rr += rv * rv;
             }
         }
         if (kthread) {
@@ -1850,30 +1871,26 @@ __global__ void __launch_bounds__(256) k_pcg_explicit(PcgXArgs<Real> P) {
             __syncthreads();
             double rzn = 0.0, rrn = 0.0;
             for (int c = blockIdx.x + nb * wib; c < nchunk; c += nb * nwb) {
-                const int a = 32 * c + lane;
-                if (a >= P.nfc) continue;
-                double xv[6], rv[6], pv[6], qv[6], zv[6];
-#pragma unroll
-                for (int i = 0; i < 6; ++i) {
-                    xv[i] = P.x[6 * a + i];
-                    rv[i] = P.r[6 * a + i];
-                    pv[i] = pn[6 * a + i];
-                    qv[i] = P.q[6 * a + i];
+                const int a = 5 * c + grp;
+                const bool act = grp < 5 && a < P.nfc;
+                const int i = 6 * a + comp;
+                double xv = 0.0, rv = 0.0, pv = 0.0, qv = 0.0;
+                if (act) {
+                    xv = P.x[i];
+                    rv = P.r[i];
+                    pv = pn[i];
+                    qv = P.q[i];
                 }
-#pragma unroll
-                for (int i = 0; i < 6; ++i) {
-                    xv[i] += alpha * pv[i];
-                    rv[i] -= alpha * qv[i];
-                }
-                precond_cam(P.pc, a, rv, zv);
-#pragma unroll
-                for (int i = 0; i < 6; ++i) {
-                    P.x[6 * a + i] = xv[i];
-                    P.r[6 * a + i] = rv[i];
-                    P.z[6 * a + i] = zv[i];
-                    P.zr[8 * a + i] = (Real)zv[i];
-                    rzn += rv[i] * zv[i];
-                    rrn += rv[i] * rv[i];
+                xv += alpha * pv;
+                rv -= alpha * qv;
+                const double zv = apply_inv(a, act, rv);
+                if (act) {
+                    P.x[i] = xv;
+                    P.r[i] = rv;
+                    P.z[i] = zv;
+                    P.zr[8 * a + comp] = (Real)zv;
+                    rzn += rv * zv;
+                    rrn += rv * rv;
                 }
             }
             if (kthread) {
@@ -2490,6 +2507,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     Real* d_t2 = pcg_i ? dv.alloc<Real>(4LL * np) : nullptr;
     double* d_aat = pcg_i ? dv.alloc<double>(28LL * std::max(1, nfc)) : nullptr;
     double* d_pc = pcg ? dv.alloc<double>(28LL * std::max(1, nfc)) : nullptr;
+    double* d_pcinv = pcg ? dv.alloc<double>(36LL * std::max(1, nfc)) : nullptr;
     double* d_camp = pcg_i ? dv.alloc<double>(8LL * n_items) : nullptr;
     double* d_vec = pcg ? dv.alloc<double>(6LL * std::max(1, mt) + 8) : nullptr;
     // explicit S: block rows, slots of the lower blocks, camera-k coupling
@@ -2922,7 +2940,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                     k_schur_blocks<Real><<<std::max(1, std::min(nsm_blocks, (n_sitems * 32 + TB - 1) / TB)), TB, 0, st>>>(
                         A, d_blocks, d_boff, d_sitems, n_sitems, d_pairs, d_U, lam_use, nullptr, 0, d_bs, d_Sb,
                         d_bslot, d_next, d_sdone, d_spart, kPairChunk);
-                    k_pcg_precond_blocks<Real><<<(nfc + TB - 1) / TB, TB, 0, st>>>(d_Sb, d_rs_dslot, nfc, d_pc, d_ok);
+                    k_pcg_precond_blocks<Real><<<(nfc + TB - 1) / TB, TB, 0, st>>>(d_Sb, d_rs_dslot, nfc, d_pc, d_pcinv, d_ok);
                     chk(cudaGetLastError());
                 } else if (nfc > 0) {
                     k_pcg_diag_items<Real><<<iblocks, TB, 0, st>>>(A, d_items, n_items, d_list, d_upart);
@@ -3002,7 +3020,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                     XA.rs_col = d_rs_col;
                     XA.Hck = d_Hck;
                     XA.Xak = d_xak;
-                    XA.pc = d_pc;
+                    XA.pcinv = d_pcinv;
                     XA.kk = d_kvals;
                     for (int i = 0; i < 3; ++i) XA.skk[i] = skk[i];
                     XA.b = d_bs;
