@@ -489,12 +489,15 @@ __global__ void __launch_bounds__(256) k_cholesky_coop(T* S, int m, const int32_
     __shared__ int sbad;
     const int tid = threadIdx.x, nb = gridDim.x, bid = blockIdx.x, wid = tid >> 5;
     const int nt = (m + kTile - 1) / kTile;
+    // phase timer (block 0's view), accumulated in registers and written once at the end, so the
+    // marks add no memory round trip to the chain they measure
     const bool timed = phase && bid == 0 && tid == 0;
     long long tmark = timed ? clock64() : 0;
+    unsigned long long tacc[5] = {0, 0, 0, 0, 0};
     auto mark = [&](int k) {
         if (timed) {
             const long long now = clock64();
-            phase[k] += (unsigned long long)(now - tmark);
+            tacc[k] += (unsigned long long)(now - tmark);
             tmark = now;
         }
     };
@@ -661,6 +664,8 @@ __global__ void __launch_bounds__(256) k_cholesky_coop(T* S, int m, const int32_
         if (wid == 0) invert_diag_tile(tk, rv, DI + (size_t)K * 2 * kTile * kTile);
     }
     mark(4);
+    if (timed)
+        for (int k = 0; k < 5; ++k) phase[k] += tacc[k];
     if (bad) atomicOr(&sbad, 1);
     __syncthreads();
     if (tid == 0 && sbad) ok[0] = 0;
