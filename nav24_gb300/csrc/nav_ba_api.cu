@@ -17,6 +17,7 @@ using namespace navba;
 
 // Parts of a pipelined batched solve (8 measured slower: 64-window parts leave host workers idle).
 constexpr int kSolveParts = 4;
+static_assert(kSolveParts == 4, "NAVBA_PART_BOUNDS parses three inner boundaries");
 // The shape of the first part of a pipelined batch (the largest windows), by precision
 // (NAV_BA_FP64, NAV_BA_MIXED): clusters over a window of that part, measured best on the
 // 256-window workload (FP64 4 x 128 threads, mixed 2 x 256; 1 to 8 CTAs lie within 1 to 10 %).
@@ -496,7 +497,20 @@ nav_ba_status solve_pipelined(nav_ba_ctx* ctx, const nav_ba_problem* probs, int 
     // part boundaries at (k / parts)^2 of the batch: the first part (the largest windows, whose solves
     // are the longest) is small, so the device starts on it early; later parts grow while the device
     // is busy (4 parts: 1/16, 3/16, 5/16, 7/16)
-    auto part_lo = [&](int k) { return (int)((long long)n * k * k / (kSolveParts * kSolveParts)); };
+    // NAVBA_PART_BOUNDS="<f1>,<f2>,<f3>" (fractions of the batch, increasing) sets the boundaries
+    // instead (diagnostics)
+    double fb[kSolveParts + 1];
+    for (int k = 0; k <= kSolveParts; ++k) fb[k] = (double)(k * k) / (kSolveParts * kSolveParts);
+    {
+        const char* pb = getenv("NAVBA_PART_BOUNDS");
+        double f1 = 0, f2 = 0, f3 = 0;
+        if (pb && sscanf(pb, "%lf,%lf,%lf", &f1, &f2, &f3) == 3 && 0 < f1 && f1 < f2 && f2 < f3 && f3 < 1) {
+            fb[1] = f1;
+            fb[2] = f2;
+            fb[3] = f3;
+        }
+    }
+    auto part_lo = [&](int k) { return k >= kSolveParts ? n : (int)(n * fb[k]); };
     // the first part holds the largest windows and has the device nearly to itself until the later
     // parts are uploaded: each of its windows is solved by a cluster of CTAs, which shortens those
     // windows (the batch's critical path) and fills the otherwise idle SMs of the ramp.
