@@ -15,8 +15,10 @@
 //                 FP64 S (Cholesky) or block rows of both triangles (explicit PCG); b'
 //   cholesky      cooperative persistent kernel, right-looking 32x32 tiles inside the envelope of S
 //                 (tiles left of a tile row's first nonzero tile stay zero); FP32 factor + one FP64
-//                 refinement in the mixed form
-//   solve         one CTA, tile-blocked forward/back substitution inside the envelope
+//                 refinement in the mixed form; leaves the diagonal tiles' inverses and contiguous
+//                 copies of the panel tiles for the solves
+//   solve         one CTA, tile by tile inside the envelope, each tile step's data copied ahead into
+//                 a shared-memory ring (cp.async)
 //   pcg           cooperative persistent kernel per damped system, block-Jacobi preconditioner:
 //                 explicit S (two grid phases per CG iteration) or, for long pair lists, products
 //                 through the per-edge records (five phases)
