@@ -90,11 +90,38 @@ __device__ void block_partial(double v, double* out) {
 }
 
 // Robust chi2 partial sums; e_out != null: every edge's residual is also stored (rounded to Real).
+// Thread per edge (grid-stride over the point-major edges, the point from edge_pt): with a thread
+// per point a warp ran as many rounds as its most-observed point, and in the FP64 cost every round
+// costs an FP64 instruction per warp whatever its active lanes.  The grid is fixed per problem, so
+// the per-thread sums (and the fixed-order block partials) repeat bitwise.
 template <class Cost, class Real>
 __global__ void k_cost(WinArgs<Real> A, WinDesc D, const Cost* camc, const double* X, double* part,
                        Real* e_out = nullptr) {
     const CC c = grid_view();
-    block_partial<false>(cost_partial<Cost, Real>(A, c, D, camc, X, e_out), part);
+    double acc = 0.0;
+    const Cost delta = (Cost)A.lm.huber_delta;
+    for (int k = c.gt; k < D.ne; k += c.CT) {
+        const int e = D.e0 + k, gp = D.pt0 + A.edge_pt[e];
+        const Cost Xr[3] = {(Cost)X[4LL * gp], (Cost)X[4LL * gp + 1], (Cost)X[4LL * gp + 2]};
+        Cost cr[12];
+        cam_load(camc + 12 * A.edge_cam[e], cr);
+        const Cost z[2] = {(Cost)A.edge_uv[2LL * e], (Cost)A.edge_uv[2LL * e + 1]};
+        if (e_out) {
+            Cost Xc[3], uv[2];
+            transform(cr, cr + 9, Xr, Xc);
+            project<Cost>(A.intr, Xc, uv, nullptr);
+            const Cost e0 = z[0] - uv[0], e1v = z[1] - uv[1];
+            double rho;
+            Cost w;
+            huber<Cost>(e0 * e0 + e1v * e1v, A.lm.robust != 0, delta, rho, w);
+            acc += rho;
+            e_out[2LL * e] = (Real)e0;
+            e_out[2LL * e + 1] = (Real)e1v;
+        } else {
+            acc += edge_cost<Cost>(A.intr, cr, cr + 9, Xr, z, A.lm.robust != 0, delta);
+        }
+    }
+    block_partial<false>(acc, part);
 }
 
 // Active edges whose point is at or behind its camera (Z_c <= 0, FP64), per-block partial counts.
