@@ -370,15 +370,17 @@ __device__ __forceinline__ void tile_abt(const TileT<T>& a, const TileT<T>& b, T
 // LL^T of the kb x kb lower tile tk in place; rv[j] receives 1/L_jj.  Per column: the pivot, the
 // column scaled by 1/L_jj, the rank-1 update of the columns to its right.  Called by every thread
 // of the block; a barrier must follow.
-// - FP32: warp 0 alone, lane i holding row i in registers.  Each column's unscaled values go
-//   through shared memory (col, double-buffered): every lane reads the pivot u_cc, forms
-//   r = 1/sqrt(u_cc) itself and its L_ic = u_ic r, and updates u_ij -= (L_ic r) u_jc; one warp
-//   barrier per column (a shuffle per element was 5x slower).  Measured alone on one SM: 7.2k
-//   cycles per tile; in 8-column panels with a rank-8 update per panel, 11.6k.
+// - FP32: warp 0 alone, lane i holding row i in registers, in panels of 8 columns.  Each column's
+//   unscaled values go through shared memory (col, double-buffered): every lane reads the pivot
+//   u_cc, forms r = 1/sqrt(u_cc) itself and its L_ic = u_ic r, and updates the panel's columns,
+//   u_ij -= (L_ic r) u_jc; one warp barrier per column (a shuffle per element was 5x slower).  The
+//   panel's L columns (pcol) then update the columns to its right in one rank-8 pass, so the
+//   column-by-column chain touches 8 columns instead of up to 31.
 // - FP64: the whole block (warp per row of the update), so that the FP64 products are spread over
 //   the SM's four partitions.
+constexpr int kDiagPanel = 8;  // FP32 diagonal-tile factorization: columns per panel
 template <class T>
-__device__ void factor_diag_tile(TileT<T>& tk, T* rv, T (*col)[kTile], int kb, int& bad) {
+__device__ void factor_diag_tile(TileT<T>& tk, T* rv, T (*col)[kTile], T (*pcol)[kTile], int kb, int& bad) {
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     if constexpr (sizeof(T) == 4) {
         if (wid != 0) return;
@@ -388,21 +390,38 @@ __device__ void factor_diag_tile(TileT<T>& tk, T* rv, T (*col)[kTile], int kb, i
         col[0][lane] = d[0];
         __syncwarp();
 #pragma unroll
-        for (int cc = 0; cc < kTile; ++cc) {
-            if (cc < kb) {
-                const T* cu = col[cc & 1];  // column cc, unscaled
-                const T piv = cu[cc];
-                const bool colbad = !(piv > T(0)) || !isfinite(piv);
-                const T r = colbad ? T(1) : rsqrtf(piv);
-                if (colbad) bad = 1;
-                const T li = lane == cc ? (colbad ? T(1) : piv * r) : d[cc] * r;
-                d[cc] = li;
-                const T wi = li * r;
-                if (lane == 0) rv[cc] = r;
+        for (int c0 = 0; c0 < kTile; c0 += kDiagPanel) {
+            // the panel's columns one by one, updating only the panel's own columns
 #pragma unroll
-                for (int j = cc + 1; j < kTile; ++j)
-                    if (lane >= j) d[j] -= wi * cu[j];
-                if (cc + 1 < kTile) col[(cc + 1) & 1][lane] = d[cc + 1];
+            for (int cc = c0; cc < c0 + kDiagPanel; ++cc) {
+                if (cc < kb) {
+                    const T* cu = col[cc & 1];  // column cc, unscaled
+                    const T piv = cu[cc];
+                    const bool colbad = !(piv > T(0)) || !isfinite(piv);
+                    const T r = colbad ? T(1) : rsqrtf(piv);
+                    if (colbad) bad = 1;
+                    const T li = lane == cc ? (colbad ? T(1) : piv * r) : d[cc] * r;
+                    d[cc] = li;
+                    pcol[cc - c0][lane] = li;
+                    const T wi = li * r;
+                    if (lane == 0) rv[cc] = r;
+#pragma unroll
+                    for (int j = cc + 1; j < c0 + kDiagPanel; ++j)
+                        if (lane >= j) d[j] -= wi * cu[j];
+                    if (cc + 1 < c0 + kDiagPanel) col[(cc + 1) & 1][lane] = d[cc + 1];
+                    __syncwarp();
+                }
+            }
+            // the panel's rank-kDiagPanel update of the columns to its right: u_ij -= sum_c L_ic L_jc
+            if (c0 + kDiagPanel < kb) {
+#pragma unroll
+                for (int j = c0 + kDiagPanel; j < kTile; ++j) {
+                    T s = T(0);
+#pragma unroll
+                    for (int c = 0; c < kDiagPanel; ++c) s += d[c0 + c] * pcol[c][j];
+                    if (lane >= j) d[j] -= s;
+                }
+                col[(c0 + kDiagPanel) & 1][lane] = d[c0 + kDiagPanel];
                 __syncwarp();
             }
         }
@@ -495,7 +514,7 @@ __global__ void __launch_bounds__(256) k_cholesky_coop(T* S, int m, const int32_
     constexpr bool one_sync = sizeof(T) == 4;
     cg::grid_group grid = cg::this_grid();
     __shared__ TileT<T> tk, ta, tb, tc;
-    __shared__ T rv[kTile], col[2][kTile];
+    __shared__ T rv[kTile], col[2][kTile], pcol[kDiagPanel][kTile];
     __shared__ int sbad;
     const int tid = threadIdx.x, nb = gridDim.x, bid = blockIdx.x, wid = tid >> 5;
     const int nt = (m + kTile - 1) / kTile;
@@ -528,6 +547,16 @@ __global__ void __launch_bounds__(256) k_cholesky_coop(T* S, int m, const int32_
 #pragma unroll
         for (int q = 0; q < 4; ++q) dst[r + 8 * q][c] -= s[q];
     };
+    // dst -= a b^T by warps 1..7 (while warp 0 factors the diagonal tile), four partial sums
+    auto sub_abt_w = [&](TileT<T>& dst, const TileT<T>& a, const TileT<T>& b) {
+        for (int o = tid - kTile; o < kTile * kTile; o += blockDim.x - kTile) {
+            const int r = o >> 5, c = o & 31;
+            T s4[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+            for (int t = 0; t < kTile; ++t) s4[t & 3] += a[r][t] * b[c][t];
+            dst[r][c] -= (s4[0] + s4[1]) + (s4[2] + s4[3]);
+        }
+    };
     // panel tile pi of column K: its loads into ta (and L_I,K-1 into tc when it gets column K - 1's
     // update, upd_prev: L_K,K-1 in tb); returns whether it does
     auto panel_load = [&](int K, int pi, bool upd_prev) {
@@ -558,7 +587,8 @@ __global__ void __launch_bounds__(256) k_cholesky_coop(T* S, int m, const int32_
         __syncthreads();
     };
     // the diagonal tile of column K (minus column K - 1's update with upd_prev), factored, and this
-    // block's panel tiles: the first tile's loads and update go with the diagonal tile's
+    // block's panel tiles: the first tile's loads go with the diagonal tile's, and its update runs
+    // on warps 1..7 while warp 0 factors (FP32)
     auto column = [&](int K, bool upd_prev) {
         const int k0 = K * kTile, kb = min(kTile, m - k0), kp = k0 - kTile;
         const int npan = pan_off[K + 1] - pan_off[K];
@@ -568,15 +598,21 @@ __global__ void __launch_bounds__(256) k_cholesky_coop(T* S, int m, const int32_
         const bool first = bid < npan;
         const bool upd0 = first && panel_load(K, bid, upd_prev);
         __syncthreads();
-        // column K - 1's update of A_KK and of the first panel tile, together (the factorization then
-        // runs without other warps' shared-memory traffic beside it)
         if (upd_prev) {
             sub_aat(tk, tb, tb);
-            if (upd0) sub_aat(ta, tc, tb);
             __syncthreads();
         }
-        factor_diag_tile(tk, rv, col, kb, bad);
+        factor_diag_tile(tk, rv, col, pcol, kb, bad);
+        if constexpr (sizeof(T) == 4) {
+            if (upd0 && wid > 0) sub_abt_w(ta, tc, tb);
+        }
         __syncthreads();
+        if constexpr (sizeof(T) != 4) {
+            if (upd0) {
+                sub_aat(ta, tc, tb);
+                __syncthreads();
+            }
+        }
         mark(0);
         if (first) panel_finish(K, bid);
         for (int pi = bid + nb; pi < npan; pi += nb) {
