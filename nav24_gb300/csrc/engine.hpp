@@ -186,12 +186,15 @@ struct GridVjp {
     std::string why;                    // reason of a non-OK status
 };
 
+struct GridWorkspace;
+
 // Solve one large problem on the whole GPU.  debug_S != nullptr: stop after assembling the
 // reduced system at damping debug_lambda and return [S (m*m, row-major, lower part) | b'].
 // vjp != nullptr (FP64 only): record or replay the damping schedule and run the backward.
+// ws: buffers kept across calls (nullptr: the call allocates and frees its own, pageable read-backs).
 cudaError_t grid_solve(const HostWindow& h, const LmOptions& lm, const Intr& intr, int precision,
-                       cudaStream_t stream, HostPool* pool, GridResult& out, double debug_lambda,
-                       std::vector<double>* debug_S, GridVjp* vjp = nullptr);
+                       cudaStream_t stream, HostPool* pool, GridWorkspace* ws, GridResult& out,
+                       double debug_lambda, std::vector<double>* debug_S, GridVjp* vjp = nullptr);
 
 // Motion-only BA (pose_engine.cu): per problem descriptor, statistics, and the reused device buffers.
 struct PoseDesc {
@@ -243,6 +246,26 @@ struct DevScratch {
         if (p) cudaFree(p);
         p = nullptr;
         cap = 0;
+    }
+};
+
+// Buffers of grid-engine solves kept by a context across calls (one context per host thread).
+// - slab: device memory the next call carves its buffers from, grown at the end of a call to what
+//   that call needed (the largest so far); a call that finds the slab too small allocates the
+//   rest buffer by buffer.
+// - pinned: page-locked host memory for the per-trial read-backs, grown on demand.
+// A call holds the workspace while it runs (busy); a call that finds it held works without it.
+// NAVBA_GRID_WORKSPACE=0 turns the slab off (every call allocates and frees its own buffers).
+struct GridWorkspace {
+    DevScratch slab;
+    bool busy = false;
+    void* pinned = nullptr;
+    size_t pinned_cap = 0;
+    void release() {
+        slab.release();
+        if (pinned) cudaFreeHost(pinned);
+        pinned = nullptr;
+        pinned_cap = 0;
     }
 };
 

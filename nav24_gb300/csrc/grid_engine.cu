@@ -2389,21 +2389,70 @@ void build_grid_host(const HostWindow& h, GridHost& g, int form, HostPool* pool)
     if (g.tr_ij.empty()) g.tr_ij.push_back(make_int2(0, 0));
 }
 
-// Device buffers of one grid solve (allocated per call; problems here are large, so the
-// allocation cost is small against the solve).
+// Device buffers of one grid solve, carved in order from the workspace's slab (256-byte aligned)
+// while it has room, else allocated one by one.  At the end of the call the slab grows to what
+// the call needed, so a repeated solve of the same size allocates nothing (the per-buffer
+// allocations and frees were ~1 ms of a 20 ms solve of 200 cameras; a free also waits for the
+// device).  The buffers' contents are not initialized either way.
 struct GridDev {
+    GridWorkspace* ws = nullptr;  // non-null while this call holds the workspace
+    bool use_slab = false;
+    char* base = nullptr;
+    size_t cap = 0, off = 0, need = 0;
     std::vector<void*> ptrs;
     cudaError_t err = cudaSuccess;
+    explicit GridDev(GridWorkspace* w) {
+        if (!w || w->busy) return;
+        ws = w;
+        ws->busy = true;
+        const char* v = getenv("NAVBA_GRID_WORKSPACE");
+        use_slab = !(v && v[0] == '0');
+        if (use_slab) {
+            base = static_cast<char*>(ws->slab.p);
+            cap = ws->slab.cap;
+        }
+    }
     template <class T>
     T* alloc(size_t n) {
         if (err != cudaSuccess) return nullptr;
+        const size_t bytes = (std::max<size_t>(n, 1) * sizeof(T) + 255) & ~size_t(255);
+        need += bytes;
+        if (base && off + bytes <= cap) {
+            void* p = base + off;
+            off += bytes;
+            return static_cast<T*>(p);
+        }
         void* p = nullptr;
-        err = cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T));
+        err = cudaMalloc(&p, bytes);
         if (err == cudaSuccess) ptrs.push_back(p);
         return static_cast<T*>(p);
     }
+    // page-locked host memory of at least `bytes` from the workspace (grown on demand), or nullptr
+    void* pinned(size_t bytes) {
+        if (!ws) return nullptr;
+        if (ws->pinned_cap < bytes) {
+            if (ws->pinned) cudaFreeHost(ws->pinned);
+            ws->pinned = nullptr;
+            ws->pinned_cap = 0;
+            if (cudaMallocHost(&ws->pinned, bytes) != cudaSuccess) {
+                ws->pinned = nullptr;
+                cudaGetLastError();
+                return nullptr;
+            }
+            ws->pinned_cap = bytes;
+        }
+        return ws->pinned;
+    }
     ~GridDev() {
         for (void* p : ptrs) cudaFree(p);
+        if (!ws) return;
+        if (use_slab && need > ws->slab.cap) {
+            // a failed allocation leaves no slab: the next call allocates buffer by buffer
+            cudaError_t e = cudaSuccess;
+            ws->slab.release();
+            if (!ws->slab.get(need, &e)) cudaGetLastError();
+        }
+        ws->busy = false;
     }
 };
 
@@ -2421,8 +2470,8 @@ cudaError_t up(T* d, const RawVec<T>& h, cudaStream_t s) {
 
 template <class Real>
 cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Intr& intr, cudaStream_t st,
-                             HostPool* pool, GridResult& out, double debug_lambda, std::vector<double>* debug_S,
-                             GridVjp* vjp) {
+                             HostPool* pool, GridWorkspace* ws, GridResult& out, double debug_lambda,
+                             std::vector<double>* debug_S, GridVjp* vjp) {
     const auto tg0 = std::chrono::steady_clock::now();
     auto ms_from = [](std::chrono::steady_clock::time_point a) {
         return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
@@ -2449,7 +2498,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     const double t_host = ms_from(tg0);
     const int nc = h.ncam, np = h.npt, ne = h.ne, nfc = h.nfc;
     const int m = 6 * nfc;
-    GridDev dv;
+    GridDev dv(ws);
     const size_t rec = Rec<Real>::kEdge;
     // inputs
     CamState* d_cams0 = dv.alloc<CamState>(nc);
@@ -2526,7 +2575,8 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     const int nsm_blocks = 152 * 4;
     const int pblocks = std::max(1, std::min(nsm_blocks, (np + TB - 1) / TB));
     const int cblocks = std::max(1, (nc + TB - 1) / TB);
-    const int npart = std::max(5 * pblocks, std::max(cblocks, (nfc * 27 + TB - 1) / TB + 1));
+    const int rblocks = (nfc * 27 + TB - 1) / TB;  // partials of the camera blocks' maxima
+    const int npart = std::max(5 * pblocks, std::max(cblocks, pblocks + rblocks + 1));
     double* d_part = dv.alloc<double>(npart);
     // a damping trial's partial sums, read back together at its end: point blocks that failed,
     // the model decrease's camera and point terms, the trial cost
@@ -2674,10 +2724,25 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     double kcur[2] = {intr.k1, intr.k2};  // current shared distortion (free when nk == 2)
     double Kk[3] = {0, 0, 0}, gk[2] = {0, 0};
     int pcg_total = 0;
-    std::vector<double> hpart(npart), hpart_trial(3LL * pblocks + cblocks);
+    // read-back buffers, page-locked when the workspace gives them (copies then run as the
+    // stream's work; from pageable memory each copy waits for the device on its own): partial
+    // sums, the linearization's maxima, a trial's partials, the shared-distortion step, flags
+    const size_t ntp = 3LL * pblocks + cblocks;
+    const size_t nhost = 2 * (size_t)npart + ntp + 4;
+    std::vector<double> hfallback;
+    double* hpart = static_cast<double*>(dv.pinned(sizeof(double) * nhost));
+    if (!hpart) {
+        hfallback.assign(nhost, 0.0);
+        hpart = hfallback.data();
+    }
+    double* hlin = hpart + npart;
+    double* hpart_trial = hlin + npart;
+    double* hdk = hpart_trial + ntp;
+    int32_t* hflag = reinterpret_cast<int32_t*>(hdk + 2);  // [0] a pivot flag, [1] CG iterations, [2] 1
+    hflag[2] = 1;  // the value a pivot flag is reset to
     auto sum_part = [&](int n, bool mx) -> double {
         if (e != cudaSuccess) return 0.0;
-        e = cudaMemcpyAsync(hpart.data(), d_part, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
+        e = cudaMemcpyAsync(hpart, d_part, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         double s = 0.0;
         for (int k = 0; k < n; ++k) s = mx ? std::max(s, hpart[k]) : s + hpart[k];
@@ -2737,24 +2802,42 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     out.initial_cost = chi;
     auto sum_parts = [&](int nblocks, int nval, double* outv) {
         if (e != cudaSuccess) return;
-        e = cudaMemcpyAsync(hpart.data(), d_part, sizeof(double) * nblocks * nval, cudaMemcpyDeviceToHost, st);
+        e = cudaMemcpyAsync(hpart, d_part, sizeof(double) * nblocks * nval, cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         for (int k = 0; k < nval; ++k) outv[k] = 0.0;
         for (int bI = 0; bI < nblocks; ++bI)
             for (int k = 0; k < nval; ++k) outv[k] += hpart[(size_t)nval * bI + k];
     };
     const int iblocks = std::max(1, std::min(nsm_blocks, (n_items * 32 + TB - 1) / TB));
-    // linearization at state c: V_p, g_p (point-major), U_a, g_a (camera-major); the max
-    // |diag| of the point and camera blocks (g2o's initial damping)
-    auto linearize = [&](int c, double& mxp, double& mxc) {
+    // linearization at state c: V_p, g_p (point-major), U_a, g_a (camera-major).  The max |diag|
+    // of the point and camera blocks (g2o's initial damping; the mixed form's FP32 resolution) is
+    // copied back behind an event and waited for only where it is used (lin_maxima), so the
+    // device goes on with the trial's kernels meanwhile.
+    cudaEvent_t ev_lin = nullptr;
+    chk(cudaEventCreateWithFlags(&ev_lin, cudaEventDisableTiming));
+    struct EventGuard {
+        cudaEvent_t ev;
+        ~EventGuard() {
+            if (ev) cudaEventDestroy(ev);
+        }
+    } ev_lin_guard{ev_lin};
+    auto linearize = [&](int c) {
         k_lin_points<Real><<<pblocks, TB, 0, st>>>(A, D, camr[c], A.x[c], d_part);
-        mxp = sum_part(pblocks, true);
         if (nfc > 0) {
             k_lin_cams<Real><<<iblocks, TB, 0, st>>>(A, d_items, n_items, d_list, d_fcam, camr[c], A.x[c], d_upart);
-            k_reduce_cams<<<(nfc * 27 + TB - 1) / TB, TB, 0, st>>>(d_upart, d_item_off, nfc, d_U, d_part);
-            chk(cudaGetLastError());
+            k_reduce_cams<<<rblocks, TB, 0, st>>>(d_upart, d_item_off, nfc, d_U, d_part + pblocks);
         }
-        mxc = nfc > 0 ? sum_part((nfc * 27 + TB - 1) / TB, true) : 0.0;
+        chk(cudaGetLastError());
+        chk(cudaMemcpyAsync(hlin, d_part, sizeof(double) * (pblocks + (nfc > 0 ? rblocks : 0)), cudaMemcpyDeviceToHost,
+                            st));
+        chk(cudaEventRecord(ev_lin, st));
+    };
+    auto lin_maxima = [&](double& mxp, double& mxc) {
+        if (e == cudaSuccess) e = cudaEventSynchronize(ev_lin);
+        mxp = mxc = 0.0;
+        if (e != cudaSuccess) return;
+        for (int k = 0; k < pblocks; ++k) mxp = std::max(mxp, hlin[k]);
+        for (int k = 0; nfc > 0 && k < rblocks; ++k) mxc = std::max(mxc, hlin[pblocks + k]);
     };
     // dense reduced system S = U + lam I - sum A A^T (lower part) and b'
     auto assemble_S = [&](double lam) {
@@ -2780,8 +2863,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     }
     // defer: the pivot flag (d_ok) is left for the trial's read-back instead of read here
     auto factor_S = [&](bool defer = false) -> bool {
-        const int32_t one = 1;
-        chk(cudaMemcpyAsync(d_ok, &one, sizeof(int32_t), cudaMemcpyHostToDevice, st));
+        chk(cudaMemcpyAsync(d_ok, hflag + 2, sizeof(int32_t), cudaMemcpyHostToDevice, st));
         double* Sp = d_S;
         int mm = m;
         const int32_t* tf = d_tfirst;
@@ -2799,19 +2881,20 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         void* kargs[] = {&Sp, &mm, &tf, &po, &pr, &to, &tsk, &tij, &ri, &ltp, &lnp, &dip, &okp, &cph};
         chk(cudaLaunchCooperativeKernel((const void*)k_cholesky_coop<double>, dim3(chol_grid), dim3(256), kargs, 0, st));
         if (defer) return e == cudaSuccess;
-        int32_t okh = 1;
-        chk(cudaMemcpyAsync(&okh, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        chk(cudaMemcpyAsync(hflag, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
         chk(cudaStreamSynchronize(st));
-        return e == cudaSuccess && okh != 0;
+        return e == cudaSuccess && hflag[0] != 0;
     };
     // Mixed form: S x = b (x into d_bs) with the Cholesky factor of S rounded to FP32 and one FP64
     // refinement step (r = b - S x0 over the FP64 S, then the FP32 factor's solution of r added).
     // S's entries are FP32 sums already, so the FP32 factor's error is of the order of S's own; the
     // refinement step removes it.  A pivot that is not positive in FP32:
     // - at a damping below kF32Resolution of the largest Hessian diagonal entry ends the trial as a
-    //   system that is not positive definite does (the damping grows): S's own FP32 rounding is then
+    //   system that is not positive definite does (the damping grows; the flag is read with the
+    //   trial's sums): the rounding of S, whose point blocks' (V + lambda I)^-1 are then large, is
     //   larger than the damping that makes it definite, and the FP64 factorization of the same S
-    //   fails as well (measured on the 200-camera grid: every such attempt failed);
+    //   fails as well (measured on the 200-camera grid: every such attempt failed; raising only the
+    //   FP32 factorization's diagonal, up to 64x the damping, did not make it definite either);
     // - above it, falls back to the FP64 factorization, and so do later trials at up to 4x the
     //   damping of the last failure (the failed attempt is not repeated).
     // Returns false if S is not positive definite.
@@ -2827,8 +2910,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             chk(chol_solve(d_LT, d_LN, d_DI, m, d_pan_off, d_pan_row, d_bs, g.max_npan, st));
             return true;
         }
-        const int32_t one = 1;
-        chk(cudaMemcpyAsync(d_ok, &one, sizeof(int32_t), cudaMemcpyHostToDevice, st));
+        chk(cudaMemcpyAsync(d_ok, hflag + 2, sizeof(int32_t), cudaMemcpyHostToDevice, st));
         k_s_round<<<nsm_blocks, TB, 0, st>>>(d_S, d_S32, m);
         float* Sp = d_S32;
         int mm = m;
@@ -2848,8 +2930,9 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         chk(cudaLaunchCooperativeKernel((const void*)k_cholesky_coop<float>, dim3(chol_grid), dim3(256), kargs, 0, st));
         int32_t okh = 1;
         if (f64_useful) {
-            chk(cudaMemcpyAsync(&okh, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+            chk(cudaMemcpyAsync(hflag, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
             chk(cudaStreamSynchronize(st));
+            okh = hflag[0];
         } else {
             deferred = true;
         }
@@ -2899,8 +2982,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         for (int s = 0; s < n_out; ++s) {
             const double lam = vjp->lambdas[s];
             save_state(cur, s);
-            double mxp, mxc;
-            linearize(cur, mxp, mxc);
+            linearize(cur);
             k_schur_points<Real><<<pblocks, TB, 0, st>>>(A, D, lam, camr[cur], A.x[cur], d_part);
             bool ok = sum_part(pblocks, false) == 0.0;
             if (nfc > 0) {
@@ -2928,16 +3010,14 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         out.iterations_done = out.accepted = n_out;
     }
     for (int it = 0; !replay && out.termination == NAV_BA_TERM_ITERATIONS && it < lm.iterations; ++it) {
-        double mxp, mxc;
         A.edge_ep = d_ep[cur];  // mixed form: the FP64 cost pass's residuals of this state
-        linearize(cur, mxp, mxc);
+        linearize(cur);
         if (nk) {
             k_lin_intr_points<Real><<<pblocks, TB, 0, st>>>(A, D, camr[cur], A.x[cur], d_kp, d_part);
             double v5[5];
             sum_parts(pblocks, 5, v5);
             Kk[0] = v5[0]; Kk[1] = v5[1]; Kk[2] = v5[2];
             gk[0] = v5[3]; gk[1] = v5[4];
-            mxc = std::max(mxc, std::max(std::fabs(Kk[0]), std::fabs(Kk[2])));
             if (nfc > 0) {
                 k_lin_intr_cams<Real><<<iblocks, TB, 0, st>>>(A, d_items, n_items, d_list, d_fcam, camr[cur], A.x[cur],
                                                               d_hpart);
@@ -2946,11 +3026,21 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             }
         }
         if (e != cudaSuccess) return e;
+        // the largest Hessian diagonal entry of this linearization, read back where first needed
+        double maxdiag = -1.0;
+        auto get_maxdiag = [&]() -> double {
+            if (maxdiag < 0.0) {
+                double mxp, mxc;
+                lin_maxima(mxp, mxc);
+                if (nk) mxc = std::max(mxc, std::max(std::fabs(Kk[0]), std::fabs(Kk[2])));
+                maxdiag = std::max(mxp, mxc);
+            }
+            return maxdiag;
+        };
         if (it == 0) {
-            lambda = lm.initial_lambda > 0 ? lm.initial_lambda : lm.tau * std::max(mxp, mxc);
+            lambda = lm.initial_lambda > 0 ? lm.initial_lambda : lm.tau * get_maxdiag();
             nu = 2.0;
         }
-        const double maxdiag = std::max(mxp, mxc);
         int trial_pit = 0;
         bool trial_ok = true;
         double rho = 0.0;
@@ -2965,8 +3055,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             if (pcg && mt > 0) {
                 if (pcg_i) k_pcg_pack<Real><<<nsm_blocks, TB, 0, st>>>(A, ne, d_list, ncl, d_apm, d_acm);
                 // right-hand side and block-Jacobi preconditioner of the reduced system [cameras; k]
-                const int32_t one = 1;
-                chk(cudaMemcpyAsync(d_ok, &one, sizeof(int32_t), cudaMemcpyHostToDevice, st));
+                chk(cudaMemcpyAsync(d_ok, hflag + 2, sizeof(int32_t), cudaMemcpyHostToDevice, st));
                 if (nfc > 0 && pcg_x) {
                     // S_ab (block rows, both triangles) and b' from the pair lists, then the factors
                     chk(cudaMemsetAsync(d_next, 0, sizeof(int32_t), st));
@@ -3081,14 +3170,17 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                     void* kargs[] = {&PA};
                     chk(cudaLaunchCooperativeKernel((const void*)k_pcg_solve<Real>, dim3(pcg_grid), dim3(256), kargs, 0, st));
                 }
-                int32_t pit = 0;
-                chk(cudaMemcpyAsync(&pit, d_pit, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+                chk(cudaMemcpyAsync(hflag + 1, d_pit, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
                 chk(cudaMemcpyAsync(d_bs, v.x, sizeof(double) * mt, cudaMemcpyDeviceToDevice, st));
-                int32_t okh = 1;
-                chk(cudaMemcpyAsync(&okh, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-                if (nk) chk(cudaMemcpyAsync(dk, v.x + m, sizeof(dk), cudaMemcpyDeviceToHost, st));
+                chk(cudaMemcpyAsync(hflag, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+                if (nk) chk(cudaMemcpyAsync(hdk, v.x + m, sizeof(dk), cudaMemcpyDeviceToHost, st));
                 chk(cudaStreamSynchronize(st));
                 if (e != cudaSuccess) return e;
+                const int32_t pit = hflag[1], okh = hflag[0];
+                if (nk) {
+                    dk[0] = hdk[0];
+                    dk[1] = hdk[1];
+                }
                 pcg_total += pit;
                 trial_pit = pit;
                 ok = ok && okh != 0;
@@ -3107,7 +3199,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                     return e;
                 }
                 if (mixed_chol) {
-                    ok = solve_S_mixed(lam_use, maxdiag, okh_deferred) && ok;
+                    ok = solve_S_mixed(lam_use, get_maxdiag(), okh_deferred) && ok;
                 } else {
                     // a failed factorization rejects the trial: its flag is read with the trial's sums
                     ok = factor_S(true) && ok;
@@ -3134,12 +3226,12 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                 chk(cudaGetLastError());
             }
             // the trial's one read-back
-            std::vector<double>& tp = hpart_trial;
-            int32_t okd = 1;
-            chk(cudaMemcpyAsync(tp.data(), d_tpart, sizeof(double) * tp.size(), cudaMemcpyDeviceToHost, st));
-            if (okh_deferred) chk(cudaMemcpyAsync(&okd, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+            const double* tp = hpart_trial;
+            chk(cudaMemcpyAsync(hpart_trial, d_tpart, sizeof(double) * ntp, cudaMemcpyDeviceToHost, st));
+            if (okh_deferred) chk(cudaMemcpyAsync(hflag, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
             chk(cudaStreamSynchronize(st));
             if (e != cudaSuccess) return e;
+            const int32_t okd = okh_deferred ? hflag[0] : 1;
             double npd = 0.0, scale_c = 0.0, scale_p = 0.0, chi_new = 0.0;
             for (int k = 0; k < pblocks; ++k) npd += tp[k];
             for (int k = 0; k < cblocks; ++k) scale_c += tp[pblocks + k];
@@ -3158,7 +3250,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             if (!ok) rho = -DBL_MAX;
             if (trial_log)
                 fprintf(stderr, "[navba grid] it %d trial %d lambda %.3e (%.3e of max diag) ok %d pcg %d cost %.9e rho %.3e\n",
-                        it, q, lam_use, lam_use / maxdiag, trial_ok ? 1 : 0, trial_pit, chi_new, rho);
+                        it, q, lam_use, lam_use / get_maxdiag(), trial_ok ? 1 : 0, trial_pit, chi_new, rho);
             if (rho > 0 && std::isfinite(chi_new)) {
                 if (vjp) {  // tape: the state before this step and its damping
                     save_state(cur, (int)vjp->lambdas.size());
@@ -3243,8 +3335,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                 chk(cudaMemcpyAsync(A.x[0], d_tape_x + (size_t)s * 4 * np, sizeof(double) * 4 * np,
                                     cudaMemcpyDeviceToDevice, st));
                 k_cams_real<double><<<cblocks, TB, 0, st>>>(cams[0], nc, camr[0]);
-                double mxp, mxc;
-                linearize(0, mxp, mxc);
+                linearize(0);
                 k_schur_points<double><<<pblocks, TB, 0, st>>>(A, D, lam, camr[0], A.x[0], d_part);
                 bool ok = sum_part(pblocks, false) == 0.0;
                 if (nfc > 0) {
@@ -3307,11 +3398,12 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
 }  // namespace
 
 cudaError_t grid_solve(const HostWindow& h, const LmOptions& lm, const Intr& intr, int precision, cudaStream_t stream,
-                       HostPool* pool, GridResult& out, double debug_lambda, std::vector<double>* debug_S, GridVjp* vjp) {
+                       HostPool* pool, GridWorkspace* ws, GridResult& out, double debug_lambda,
+                       std::vector<double>* debug_S, GridVjp* vjp) {
     if (precision == NAV_BA_MIXED)
-        return grid_solve_typed<float>(h, lm, intr, stream, pool, out, debug_lambda, debug_S,
+        return grid_solve_typed<float>(h, lm, intr, stream, pool, ws, out, debug_lambda, debug_S,
                                        vjp && !vjp->backward ? vjp : nullptr);
-    return grid_solve_typed<double>(h, lm, intr, stream, pool, out, debug_lambda, debug_S, vjp);
+    return grid_solve_typed<double>(h, lm, intr, stream, pool, ws, out, debug_lambda, debug_S, vjp);
 }
 
 }  // namespace navba

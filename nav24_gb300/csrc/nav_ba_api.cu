@@ -39,6 +39,7 @@ struct nav_ba_ctx {
     WindowBatch solve_dev;        // device buffers of nav_ba_solve / _batched, reused across calls
     std::vector<HostWindow> solve_host;  // their host-side windows, reused across calls
     HostStaging stg;              // pinned staging reused across calls
+    GridWorkspace gws;            // device and pinned buffers of grid-engine solves, reused across calls
     // pipelined batched solves: the batch's parts, each with its windows, device buffers, pinned
     // staging and stream (the host builds part k + 1 while the device solves part k)
     struct Part {
@@ -421,8 +422,8 @@ nav_ba_status solve_grid_window(nav_ba_ctx* ctx, const nav_ba_problem& p, const 
                                 nav_ba_result& r) {
     GridResult g;
     cudaEventRecord(ctx->ev0, ctx->stream);
-    cudaError_t e = grid_solve(h, lm_options(o), intrinsics_of(p), o.precision, ctx->stream, &ctx->stg.pool, g, -1.0,
-                               nullptr);
+    cudaError_t e = grid_solve(h, lm_options(o), intrinsics_of(p), o.precision, ctx->stream, &ctx->stg.pool, &ctx->gws,
+                               g, -1.0, nullptr);
     cudaEventRecord(ctx->ev1, ctx->stream);
     if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev1);
     if (e != cudaSuccess) return cuda_status(ctx, e, "grid engine");
@@ -733,6 +734,7 @@ void nav_ba_destroy(nav_ba_ctx* ctx) {
     }
     ctx->pose.release();
     ctx->scratch.release();
+    ctx->gws.release();
     ctx->stg.release();
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -911,8 +913,8 @@ nav_ba_status nav_ba_reduced_system(nav_ba_ctx* ctx, const nav_ba_problem* p, co
     if (pb.host_status[0] == kGridWindow) {
         GridResult g;
         std::vector<double> dbg;
-        cudaError_t e = grid_solve(h, lm_options(o1), intrinsics_of(*p), o1.precision, ctx->stream, &ctx->stg.pool, g,
-                                   lambda, &dbg);
+        cudaError_t e = grid_solve(h, lm_options(o1), intrinsics_of(*p), o1.precision, ctx->stream, &ctx->stg.pool,
+                                   &ctx->gws, g, lambda, &dbg);
         if (e != cudaSuccess) return cuda_status(ctx, e, "reduced system");
         const int m = 6 * h.nfc;
         for (int r = 0; r < m; ++r)
@@ -1073,8 +1075,8 @@ nav_ba_status nav_ba_vjp(nav_ba_ctx* ctx, const nav_ba_problem* p, const nav_ba_
     const double t_setup = ms_since(t0);
     GridResult g;
     cudaEventRecord(ctx->ev0, ctx->stream);
-    cudaError_t e = grid_solve(h, lm_options(*o), intrinsics_of(*p), NAV_BA_FP64, ctx->stream, &ctx->stg.pool, g, -1.0,
-                               nullptr, &v);
+    cudaError_t e = grid_solve(h, lm_options(*o), intrinsics_of(*p), NAV_BA_FP64, ctx->stream, &ctx->stg.pool,
+                               &ctx->gws, g, -1.0, nullptr, &v);
     cudaEventRecord(ctx->ev1, ctx->stream);
     if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev1);
     if (e != cudaSuccess) return cuda_status(ctx, e, "grid engine (vjp)");

@@ -111,3 +111,30 @@ def test_grid_solve_forms_agree(ctx, monkeypatch, precision):
     assert a.status == abi.OK and b.status == abi.OK
     assert np.array_equal(a.cam_pose, b.cam_pose) and np.array_equal(a.points, b.points)
     assert np.array_equal(a.cost_trace, b.cost_trace, equal_nan=True)
+
+
+@pytest.mark.parametrize("precision", [abi.FP64, abi.MIXED])
+@pytest.mark.parametrize("solver", [abi.SOLVER_CHOLESKY, abi.SOLVER_PCG])
+def test_grid_workspace_reuse(product_lib, monkeypatch, solver, precision):
+    """A context keeps its grid solves' device buffers (one slab, grown at the end of a call to
+    what the call needed) and pinned read-back memory.  Solves of a small and a larger problem,
+    alternated on one context (the slab too small, then large enough, then reused), match the
+    same solves on contexts that allocate per call (NAVBA_GRID_WORKSPACE=0) bit for bit."""
+    from nav24_gb300 import Context
+
+    small = grid_problem()
+    large = Synth(4, n_cams=60, n_points=6000, seed=8).window(0)
+    o = workload_options(4, precision)
+    o.iterations = 4
+    o.solver = solver
+    o.optimize_distortion = 1 if solver == abi.SOLVER_PCG else 0
+    seq = [small, large, small, large]
+    with Context(0) as c:
+        kept = [c.solve(p, o) for p in seq]
+    monkeypatch.setenv("NAVBA_GRID_WORKSPACE", "0")
+    with Context(0) as c:
+        fresh = [c.solve(p, o) for p in seq]
+    for a, b in zip(kept, fresh):
+        assert a.status == abi.OK and b.status == abi.OK
+        assert np.array_equal(a.cam_pose, b.cam_pose) and np.array_equal(a.points, b.points)
+        assert np.array_equal(a.cost_trace, b.cost_trace, equal_nan=True)
