@@ -12,18 +12,21 @@
 //   schur_points  thread per point: chol(V + lambda I), L, t, A_e = W_e L^T with W_e recomputed (shared)
 //   schur_blocks  warp per work item (<= 256 observation pairs of one nonzero 6x6 block of S, taken in
 //                 order from a counter): S_ab = [a==b](U_a + lambda I) - sum A_i A_j^T, into a dense
-//                 FP64 S (Cholesky) or block rows of both triangles (explicit PCG); b'
+//                 FP64 S (Cholesky; the mixed form also its FP32 lower part and the upper mirror) or
+//                 block rows of both triangles (explicit PCG); b'
 //   cholesky      cooperative persistent kernel, right-looking 32x32 tiles inside the envelope of S
 //                 (tiles left of a tile row's first nonzero tile stay zero); FP32 factor + one FP64
 //                 refinement in the mixed form; leaves the diagonal tiles' inverses and contiguous
 //                 copies of the panel tiles for the solves
 //   solve         one CTA, tile by tile inside the envelope, each tile step's data copied ahead into
-//                 a shared-memory ring (cp.async)
+//                 a shared-memory ring (cp.async); the mixed form's roundings to and from FP32 at
+//                 its start and end
 //   pcg           cooperative persistent kernel per damped system, block-Jacobi preconditioner:
 //                 explicit S (two grid phases per CG iteration) or, for long pair lists, products
 //                 through the per-edge records (five phases)
-//   update        thread per point (dx_p = L^T (t - sum A^T dx_c), shared) and per camera (SE(3))
-//   cost          thread per point, per-block partial sums reduced on the host in a fixed order
+//   update        thread per point (dx_p = L^T (t - sum A^T dx_c), shared) and per camera (SE(3),
+//                 warp-sized blocks)
+//   cost          thread per edge, per-block partial sums reduced on the host in a fixed order
 // With a GridVjp, the accepted steps' states and damping are taped (or a given damping schedule
 // is replayed) and the backward pass of vjp_device.cuh runs over the taped steps, last first.
 #include <algorithm>
@@ -206,9 +209,10 @@ __global__ void k_schur_points(WinArgs<Real> A, WinDesc D, double lambda, const 
 }
 
 // Warp per work item: up to kPairChunk pairs of one nonzero block (a >= b) of S.  Output: dense
-// row-major S (m x m, lower part), or, with Sb, block rows of both triangles in Real (row-major 6x6
-// per slot; bslot[blk]: the slot of the block and of its transpose, -1 on the diagonal, whose block is
-// written whole).  Warps take the items in order from a counter (next, zero at launch), so the
+// row-major S (m x m, lower part; with S32 also mirrored into the upper part, and the lower part
+// rounded to FP32 into S32, the mixed form's factorization input), or, with Sb, block rows of both
+// triangles in Real (row-major 6x6 per slot; bslot[blk]: the slot of the block and of its
+// transpose, -1 on the diagonal, whose block is written whole).  Warps take the items in order from a counter (next, zero at launch), so the
 // records being read stay within a window of consecutive camera rows, which stays in L2; items are
 // short so that no warp lags far behind the window (a diagonal block holds all of its camera's
 // observations).  A block of several items is finished by whichever of its items ends last (count
@@ -218,7 +222,7 @@ template <class Real>
 __global__ void k_schur_blocks(WinArgs<Real> A, const int2* blocks, const int32_t* boff, const int4* items,
                                int n_items, const int2* pairs, const double* U, double lambda, double* S, int m,
                                double* bs, Real* Sb, const int2* bslot, int32_t* next, int32_t* done, Real* part,
-                               int chunk) {
+                               int chunk, float* S32 = nullptr) {
     const CC c = grid_view();
     const int slot = rs36_slot(c.lane);  // this lane's two entries of the block (slot, slot + 1)
     for (;;) {
@@ -310,6 +314,10 @@ __global__ void k_schur_blocks(WinArgs<Real> A, const int2* blocks, const int32_
                     if (bs2.y >= 0) Sb[36LL * bs2.y + q * 6 + r] = (Real)v;
                 } else {
                     S[(size_t)(6 * a + r) * m + 6 * b + q] = v;
+                    if (S32) {
+                        S32[(size_t)(6 * a + r) * m + 6 * b + q] = (float)v;
+                        if (a != b || q != r) S[(size_t)(6 * b + q) * m + 6 * a + r] = v;
+                    }
                 }
             }
         }
@@ -334,7 +342,7 @@ __global__ void k_schur_blocks(WinArgs<Real> A, const int2* blocks, const int32_
 //   update to the trailing tiles right of column K while column K is finished: the panel blocks
 //   apply it to A_KK and their own panel tiles in shared memory before factoring and solving.
 // Either way the updates reach every element column by column.  A non-positive pivot is replaced by 1 and reported through
-// ok.  Each panel tile is also stored contiguously, transposed into LT and as is into LN (32 x 32
+// fail (set to 1; zero at launch).  Each panel tile is also stored contiguously, transposed into LT and as is into LN (32 x 32
 // per entry of the panel list, in list order), and each diagonal tile's inverse into DI (L^-T and
 // L^-1, 32 x 32 each, by tile), which the solves read.  Requires 256 threads per block.  tr_ij lists each
 // column's trailing tiles by column J
@@ -509,7 +517,7 @@ __device__ void panel_solve(TileT<T>& ta, const TileT<T>& tk, const T* rv, int i
 template <class T>
 __global__ void __launch_bounds__(256) k_cholesky_coop(T* S, int m, const int32_t* tfirst, const int32_t* pan_off,
                                                        const int32_t* pan_row, const int32_t* tr_off, const int32_t* tr_skip,
-                                                       const int2* tr_ij, T* rinv, T* LT, T* LN, T* DI, int32_t* ok,
+                                                       const int2* tr_ij, T* rinv, T* LT, T* LN, T* DI, int32_t* fail,
                                                        unsigned long long* phase) {
     constexpr bool one_sync = sizeof(T) == 4;
     cg::grid_group grid = cg::this_grid();
@@ -697,7 +705,7 @@ __global__ void __launch_bounds__(256) k_cholesky_coop(T* S, int m, const int32_
         for (int k = 0; k < 5; ++k) phase[k] += tacc[k];
     if (bad) atomicOr(&sbad, 1);
     __syncthreads();
-    if (tid == 0 && sbad) ok[0] = 0;
+    if (tid == 0 && sbad) fail[0] = 1;
 }
 
 // Asynchronous global -> shared copies (cp.async, completed through commit groups).
@@ -733,11 +741,15 @@ __host__ __device__ constexpr size_t solve_slot_elems(int P) {
 //   read from global memory.  Warp 0 copies nothing: it carries the serial chain.
 // Every shared-memory read is a row of a block with lanes over its columns (conflict-free), every
 // sum runs in four partial sums (index mod 4).  Bitwise repeatable.  kXs: x is kept in dynamic
-// shared memory (padded with zeros to whole tiles) ahead of the ring.
+// shared memory (padded with zeros to whole tiles) ahead of the ring.  The mixed form's refinement
+// converts on the way: with b_in, x starts as b_in rounded to T (xg's contents are not read); with
+// x_out, x_out = x_add + x in FP64 at the end (x also stored into xg).
 template <class T, bool kXs>
 __global__ void __launch_bounds__(512) k_chol_solve(const T* __restrict__ LT, const T* __restrict__ LN,
                                                     const T* __restrict__ DI, int m, const int32_t* __restrict__ pan_off,
-                                                    const int32_t* __restrict__ pan_row, T* __restrict__ xg, int P) {
+                                                    const int32_t* __restrict__ pan_row, T* __restrict__ xg, int P,
+                                                    const double* __restrict__ b_in, const T* __restrict__ x_add,
+                                                    double* __restrict__ x_out) {
     constexpr int kW = 16;  // warps
     constexpr int kPer16 = 16 / sizeof(T);
     constexpr int kChunks = kTile * kTile / kPer16;  // 16-byte chunks per 32 x 32 block
@@ -752,7 +764,11 @@ __global__ void __launch_bounds__(512) k_chol_solve(const T* __restrict__ LT, co
     const size_t slot_elems = solve_slot_elems<T>(P);
     T* x = kXs ? xs : xg;
     if constexpr (kXs) {
-        for (int i = tid; i < nt * kTile; i += blockDim.x) x[i] = i < m ? xg[i] : T(0);
+        for (int i = tid; i < nt * kTile; i += blockDim.x) x[i] = i < m ? (b_in ? (T)b_in[i] : xg[i]) : T(0);
+    } else {
+        if (b_in) {
+            for (int i = tid; i < m; i += blockDim.x) x[i] = (T)b_in[i];
+        }
     }
     auto xrow = [&](int r) -> T { return kXs ? x[r] : x[min(r, m - 1)]; };
     const int nsteps = 2 * nt;
@@ -835,6 +851,8 @@ __global__ void __launch_bounds__(512) k_chol_solve(const T* __restrict__ LT, co
     if constexpr (kXs) {
         for (int i = tid; i < m; i += blockDim.x) xg[i] = x[i];
     }
+    if (x_out)
+        for (int i = tid; i < m; i += blockDim.x) x_out[i] = (double)x_add[i] + (double)x[i];
 }
 
 // Launches the triangular solves of a factored S: x in shared memory when it fits beside a ring
@@ -843,7 +861,8 @@ __global__ void __launch_bounds__(512) k_chol_solve(const T* __restrict__ LT, co
 // the shared-memory budget allows.
 template <class T>
 cudaError_t chol_solve(const T* LT, const T* LN, const T* DI, int m, const int32_t* pan_off, const int32_t* pan_row,
-                       T* x, int max_npan, cudaStream_t st) {
+                       T* x, int max_npan, cudaStream_t st, const double* b_in = nullptr, const T* x_add = nullptr,
+                       double* x_out = nullptr) {
     const char* gx = getenv("NAVBA_SOLVE_GLOBAL_X");
     const bool global_x = gx && gx[0] == '1';
     const size_t xs_bytes = sizeof(T) * (size_t)std::max(1, (m + kTile - 1) / kTile * kTile);
@@ -857,31 +876,15 @@ cudaError_t chol_solve(const T* LT, const T* LN, const T* DI, int m, const int32
     if (use_xs) {
         e = cudaFuncSetAttribute(k_chol_solve<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        k_chol_solve<T, true><<<1, 512, smem, st>>>(LT, LN, DI, m, pan_off, pan_row, x, P);
+        k_chol_solve<T, true><<<1, 512, smem, st>>>(LT, LN, DI, m, pan_off, pan_row, x, P, b_in, x_add, x_out);
     } else {
         e = cudaFuncSetAttribute(k_chol_solve<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        k_chol_solve<T, false><<<1, 512, smem, st>>>(LT, LN, DI, m, pan_off, pan_row, x, P);
+        k_chol_solve<T, false><<<1, 512, smem, st>>>(LT, LN, DI, m, pan_off, pan_row, x, P, b_in, x_add, x_out);
     }
     return cudaGetLastError();
 }
 
-// Mixed form: S (FP64, lower part) rounded to FP32 into S32, and both mirrored into their upper
-// parts (the refinement residual is then a plain row-major product; the factorization and the
-// solves read the lower parts only).
-__global__ void k_s_round(double* S, float* S32, int m) {
-    const size_t n = (size_t)m * m;
-    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
-        const int i = (int)(k / m), j = (int)(k % m);
-        if (j > i) continue;
-        const double v = S[k];
-        S32[k] = (float)v;
-        if (j < i) {
-            S[(size_t)j * m + i] = v;
-            S32[(size_t)j * m + i] = (float)v;
-        }
-    }
-}
 
 // r = b - S x in FP64 (warp per row of the mirrored S), rounded to FP32; x in FP32.
 __global__ void k_s_residual(const double* S, const float* x, const double* b, int m, float* r) {
@@ -896,18 +899,13 @@ __global__ void k_s_residual(const double* S, const float* x, const double* b, i
     }
 }
 
-// b (FP64) -> x (FP32); and b = x + y after the refinement.
-__global__ void k_vec_round(const double* b, float* x, int m) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) x[i] = (float)b[i];
-}
-__global__ void k_vec_sum(double* b, const float* x, const float* y, int m) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) b[i] = (double)x[i] + (double)y[i];
-}
-
-// Cameras: trial = exp(dx_a) * current for free cameras; Real / FP64 copies; scale part.
+// Cameras: trial = exp(dx_a) * current for free cameras; Real copies (and FP64 ones into camd,
+// when given); scale part.  A thread per camera: the trial's launch takes warp-sized blocks, since
+// an FP64 instruction occupies its SM partition 64 cycles per warp whatever its active lanes, and
+// a warp per SM spreads the cameras' FP64 work over as many partitions as there are warps.
 template <class Real>
 __global__ void k_update_cams(const CamState* cur, CamState* trial, Real* camr_trial, const int32_t* cam_free, int nc,
-                              const double* dc, const double* U, double lambda, double* part) {
+                              const double* dc, const double* U, double lambda, double* part, double* camd = nullptr) {
     double sc = 0.0;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < nc) {
@@ -919,6 +917,7 @@ __global__ void k_update_cams(const CamState* cur, CamState* trial, Real* camr_t
             trial[k] = cur[k];
         }
         cam_real<Real>(trial[k], camr_trial + 12 * k);
+        if (camd) cam_real<double>(trial[k], camd + 12 * k);
     }
     block_partial<false>(sc, part);
 }
@@ -2566,21 +2565,26 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     double* d_bs = dv.alloc<double>(std::max(1, mt));
     double* d_rinv = dv.alloc<double>(std::max(1, m));
     int32_t* d_ok = dv.alloc<int32_t>(1);
-    int32_t* d_next = dv.alloc<int32_t>(1);  // work counter of the item-ordered Schur kernel
+    // the item-ordered Schur kernel's work counter, the factorization's failure flag and the
+    // Schur blocks' item counts, zeroed together
+    int32_t* d_flags = dv.alloc<int32_t>(2 + g.blocks.size());
+    int32_t* d_next = d_flags;
+    int32_t* d_fail = d_flags + 1;
     const int n_sitems = (int)g.sitems.size();
     int4* d_sitems = dv.alloc<int4>(g.sitems.size());
-    int32_t* d_sdone = dv.alloc<int32_t>(g.blocks.size());
+    int32_t* d_sdone = d_flags + 2;
     Real* d_spart = dv.alloc<Real>(48LL * n_sitems);
     const int TB = 256;
     const int nsm_blocks = 152 * 4;
     const int pblocks = std::max(1, std::min(nsm_blocks, (np + TB - 1) / TB));
     const int cblocks = std::max(1, (nc + TB - 1) / TB);
+    const int ucblocks = std::max(1, (nc + 31) / 32);  // the trial's camera update: warp-sized blocks
     const int rblocks = (nfc * 27 + TB - 1) / TB;  // partials of the camera blocks' maxima
     const int npart = std::max(5 * pblocks, std::max(cblocks, pblocks + rblocks + 1));
     double* d_part = dv.alloc<double>(npart);
     // a damping trial's partial sums, read back together at its end: point blocks that failed,
     // the model decrease's camera and point terms, the trial cost
-    double* d_tpart = dv.alloc<double>(3LL * pblocks + cblocks);
+    double* d_tpart = dv.alloc<double>(3LL * pblocks + ucblocks);
     // PCG and distortion buffers
     const int n_items = (int)g.items.size();
     Real* d_kp = nk ? dv.alloc<Real>(12LL * np) : nullptr;
@@ -2727,7 +2731,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     // read-back buffers, page-locked when the workspace gives them (copies then run as the
     // stream's work; from pageable memory each copy waits for the device on its own): partial
     // sums, the linearization's maxima, a trial's partials, the shared-distortion step, flags
-    const size_t ntp = 3LL * pblocks + cblocks;
+    const size_t ntp = 3LL * pblocks + ucblocks;
     const size_t nhost = 2 * (size_t)npart + ntp + 4;
     std::vector<double> hfallback;
     double* hpart = static_cast<double*>(dv.pinned(sizeof(double) * nhost));
@@ -2839,14 +2843,16 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         for (int k = 0; k < pblocks; ++k) mxp = std::max(mxp, hlin[k]);
         for (int k = 0; nfc > 0 && k < rblocks; ++k) mxc = std::max(mxc, hlin[pblocks + k]);
     };
-    // dense reduced system S = U + lam I - sum A A^T (lower part) and b'
+    // dense reduced system S = U + lam I - sum A A^T (lower part) and b'; the mixed form's FP32
+    // copy (lower part) and the upper mirror of S with it.  The factorization's failure flag is
+    // zeroed with the Schur kernel's counters.
     auto assemble_S = [&](double lam) {
         chk(cudaMemsetAsync(d_S, 0, sizeof(double) * (size_t)m * m, st));
-        chk(cudaMemsetAsync(d_next, 0, sizeof(int32_t), st));
-        chk(cudaMemsetAsync(d_sdone, 0, sizeof(int32_t) * g.blocks.size(), st));
+        if (mixed_chol) chk(cudaMemsetAsync(d_S32, 0, sizeof(float) * (size_t)m * m, st));
+        chk(cudaMemsetAsync(d_flags, 0, sizeof(int32_t) * (2 + g.blocks.size()), st));
         k_schur_blocks<Real><<<std::max(1, std::min(nsm_blocks, (n_sitems * 32 + TB - 1) / TB)), TB, 0, st>>>(
             A, d_blocks, d_boff, d_sitems, n_sitems, d_pairs, d_U, lam, d_S, m, d_bs, (Real*)nullptr, nullptr, d_next,
-            d_sdone, d_spart, INT32_MAX);
+            d_sdone, d_spart, INT32_MAX, mixed_chol ? d_S32 : nullptr);
         chk(cudaGetLastError());
     };
     // Cholesky of S in place (cooperative, whole GPU); false if S is not positive definite
@@ -2861,9 +2867,10 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         bps = std::min(bps, bps32);
         chol_grid = std::max(1, std::min(nsm * std::max(1, std::min(bps, 2)), g.max_col_work));
     }
-    // defer: the pivot flag (d_ok) is left for the trial's read-back instead of read here
-    auto factor_S = [&](bool defer = false) -> bool {
-        chk(cudaMemcpyAsync(d_ok, hflag + 2, sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    // defer: the failure flag (d_fail) is left for the trial's read-back instead of read here;
+    // reset: zero the flag first (a factorization after another one; assemble_S zeroes it)
+    auto factor_S = [&](bool defer = false, bool reset = false) -> bool {
+        if (reset) chk(cudaMemsetAsync(d_fail, 0, sizeof(int32_t), st));
         double* Sp = d_S;
         int mm = m;
         const int32_t* tf = d_tfirst;
@@ -2876,14 +2883,14 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         double* ltp = d_LT;
         double* lnp = d_LN;
         double* dip = d_DI;
-        int32_t* okp = d_ok;
+        int32_t* okp = d_fail;
         unsigned long long* cph = d_phase;
         void* kargs[] = {&Sp, &mm, &tf, &po, &pr, &to, &tsk, &tij, &ri, &ltp, &lnp, &dip, &okp, &cph};
         chk(cudaLaunchCooperativeKernel((const void*)k_cholesky_coop<double>, dim3(chol_grid), dim3(256), kargs, 0, st));
         if (defer) return e == cudaSuccess;
-        chk(cudaMemcpyAsync(hflag, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        chk(cudaMemcpyAsync(hflag, d_fail, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
         chk(cudaStreamSynchronize(st));
-        return e == cudaSuccess && hflag[0] != 0;
+        return e == cudaSuccess && hflag[0] == 0;
     };
     // Mixed form: S x = b (x into d_bs) with the Cholesky factor of S rounded to FP32 and one FP64
     // refinement step (r = b - S x0 over the FP64 S, then the FP32 factor's solution of r added).
@@ -2910,8 +2917,6 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             chk(chol_solve(d_LT, d_LN, d_DI, m, d_pan_off, d_pan_row, d_bs, g.max_npan, st));
             return true;
         }
-        chk(cudaMemcpyAsync(d_ok, hflag + 2, sizeof(int32_t), cudaMemcpyHostToDevice, st));
-        k_s_round<<<nsm_blocks, TB, 0, st>>>(d_S, d_S32, m);
         float* Sp = d_S32;
         int mm = m;
         const int32_t* tf = d_tfirst;
@@ -2924,15 +2929,15 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         float* ltp = d_LT32;
         float* lnp = d_LN32;
         float* dip = d_DI32;
-        int32_t* okp = d_ok;
+        int32_t* okp = d_fail;
         unsigned long long* cph = d_phase;
         void* kargs[] = {&Sp, &mm, &tf, &po, &pr, &to, &tsk, &tij, &ri, &ltp, &lnp, &dip, &okp, &cph};
         chk(cudaLaunchCooperativeKernel((const void*)k_cholesky_coop<float>, dim3(chol_grid), dim3(256), kargs, 0, st));
         int32_t okh = 1;
         if (f64_useful) {
-            chk(cudaMemcpyAsync(hflag, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+            chk(cudaMemcpyAsync(hflag, d_fail, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
             chk(cudaStreamSynchronize(st));
-            okh = hflag[0];
+            okh = hflag[0] == 0;
         } else {
             deferred = true;
         }
@@ -2944,16 +2949,14 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                         f64_useful ? "FP64 factor instead" : "trial rejected");
             if (!f64_useful) return false;
             f32_fail_lambda = std::max(f32_fail_lambda, lam);
-            if (!factor_S()) return false;
+            if (!factor_S(false, true)) return false;
             chk(chol_solve(d_LT, d_LN, d_DI, m, d_pan_off, d_pan_row, d_bs, g.max_npan, st));
             return true;
         }
-        const int vb = (m + TB - 1) / TB;
-        k_vec_round<<<vb, TB, 0, st>>>(d_bs, d_x32, m);
-        chk(chol_solve(d_LT32, d_LN32, d_DI32, m, d_pan_off, d_pan_row, d_x32, g.max_npan, st));
+        // x0 = S32^-1 (float)b; y = S32^-1 (b - S x0); b <- x0 + y (the solves convert on load and store)
+        chk(chol_solve(d_LT32, d_LN32, d_DI32, m, d_pan_off, d_pan_row, d_x32, g.max_npan, st, d_bs));
         k_s_residual<<<nsm_blocks, TB, 0, st>>>(d_S, d_x32, d_bs, m, d_y32);
-        chk(chol_solve(d_LT32, d_LN32, d_DI32, m, d_pan_off, d_pan_row, d_y32, g.max_npan, st));
-        k_vec_sum<<<vb, TB, 0, st>>>(d_bs, d_x32, d_y32, m);
+        chk(chol_solve(d_LT32, d_LN32, d_DI32, m, d_pan_off, d_pan_row, d_y32, g.max_npan, st, nullptr, d_x32, d_bs));
         chk(cudaGetLastError());
         return true;
     };
@@ -3058,8 +3061,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                 chk(cudaMemcpyAsync(d_ok, hflag + 2, sizeof(int32_t), cudaMemcpyHostToDevice, st));
                 if (nfc > 0 && pcg_x) {
                     // S_ab (block rows, both triangles) and b' from the pair lists, then the factors
-                    chk(cudaMemsetAsync(d_next, 0, sizeof(int32_t), st));
-                    chk(cudaMemsetAsync(d_sdone, 0, sizeof(int32_t) * g.blocks.size(), st));
+                    chk(cudaMemsetAsync(d_flags, 0, sizeof(int32_t) * (2 + g.blocks.size()), st));
                     k_schur_blocks<Real><<<std::max(1, std::min(nsm_blocks, (n_sitems * 32 + TB - 1) / TB)), TB, 0, st>>>(
                         A, d_blocks, d_boff, d_sitems, n_sitems, d_pairs, d_U, lam_use, nullptr, 0, d_bs, d_Sb,
                         d_bslot, d_next, d_sdone, d_spart, kPairChunk);
@@ -3210,15 +3212,14 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                 if (!ok) chk(cudaMemsetAsync(d_bs, 0, sizeof(double) * m, st));
                 chk(cudaGetLastError());
             }
-            k_update_cams<Real><<<cblocks, TB, 0, st>>>(cams[cur], cams[cur ^ 1], camr[cur ^ 1], d_cam_free, nc, d_bs, d_U,
-                                                         lambda, d_tpart + pblocks);
-            k_update_points<Real><<<pblocks, TB, 0, st>>>(A, D, lambda, d_bs, cur, d_tpart + pblocks + cblocks);
+            k_update_cams<Real><<<ucblocks, 32, 0, st>>>(cams[cur], cams[cur ^ 1], camr[cur ^ 1], d_cam_free, nc, d_bs,
+                                                          d_U, lambda, d_tpart + pblocks, mixed ? d_camd : nullptr);
+            k_update_points<Real><<<pblocks, TB, 0, st>>>(A, D, lambda, d_bs, cur, d_tpart + pblocks + ucblocks);
             set_radial(A.intr, kcur[0] + dk[0], kcur[1] + dk[1]);
-            {  // the trial cost (FP64 in both forms)
+            {  // the trial cost (FP64 in both forms; the mixed form's FP64 cameras from the update)
                 const int buf = cur ^ 1;
-                double* cpart = d_tpart + 2LL * pblocks + cblocks;
+                double* cpart = d_tpart + 2LL * pblocks + ucblocks;
                 if (mixed) {
-                    k_cams_real<double><<<cblocks, TB, 0, st>>>(cams[buf], nc, d_camd);
                     k_cost<double, Real><<<pblocks, TB, 0, st>>>(A, D, d_camd, A.x[buf], cpart, d_ep[buf]);
                 } else {
                     k_cost<Real, Real><<<pblocks, TB, 0, st>>>(A, D, camr[buf], A.x[buf], cpart);
@@ -3228,15 +3229,15 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
             // the trial's one read-back
             const double* tp = hpart_trial;
             chk(cudaMemcpyAsync(hpart_trial, d_tpart, sizeof(double) * ntp, cudaMemcpyDeviceToHost, st));
-            if (okh_deferred) chk(cudaMemcpyAsync(hflag, d_ok, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+            if (okh_deferred) chk(cudaMemcpyAsync(hflag, d_fail, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
             chk(cudaStreamSynchronize(st));
             if (e != cudaSuccess) return e;
-            const int32_t okd = okh_deferred ? hflag[0] : 1;
+            const int32_t okd = okh_deferred ? (hflag[0] == 0) : 1;
             double npd = 0.0, scale_c = 0.0, scale_p = 0.0, chi_new = 0.0;
             for (int k = 0; k < pblocks; ++k) npd += tp[k];
-            for (int k = 0; k < cblocks; ++k) scale_c += tp[pblocks + k];
-            for (int k = 0; k < pblocks; ++k) scale_p += tp[pblocks + cblocks + k];
-            for (int k = 0; k < pblocks; ++k) chi_new += tp[2 * pblocks + cblocks + k];
+            for (int k = 0; k < ucblocks; ++k) scale_c += tp[pblocks + k];
+            for (int k = 0; k < pblocks; ++k) scale_p += tp[pblocks + ucblocks + k];
+            for (int k = 0; k < pblocks; ++k) chi_new += tp[2 * pblocks + ucblocks + k];
             double scale = scale_c + scale_p;
             scale += dk[0] * (lambda * dk[0] + gk[0]) + dk[1] * (lambda * dk[1] + gk[1]);
             if (npd != 0.0 || okd == 0) ok = false;
