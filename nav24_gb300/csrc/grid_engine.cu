@@ -887,12 +887,16 @@ cudaError_t chol_solve(const T* LT, const T* LN, const T* DI, int m, const int32
 
 
 // r = b - S x in FP64 (warp per row of the mirrored S), rounded to FP32; x in FP32.
-__global__ void k_s_residual(const double* S, const float* x, const double* b, int m, float* r) {
+// Row i runs over the symmetric envelope only, tiles tfirst[i / 32] .. tlast[i / 32] (whole tiles,
+// so each lane sums the same terms in the same order as over the whole row, less zeros).
+__global__ void k_s_residual(const double* S, const float* x, const double* b, int m, const int32_t* tfirst,
+                             const int32_t* tlast, float* r) {
     const CC c = grid_view();
     for (int i = c.gw; i < m; i += c.CW) {
         const double* Si = S + (size_t)i * m;
+        const int lo = tfirst[i / kTile] * kTile, hi = min(m, (tlast[i / kTile] + 1) * kTile);
         double acc = 0.0;
-        for (int j = c.lane; j < m; j += 32) acc += Si[j] * (double)x[j];
+        for (int j = lo + c.lane; j < hi; j += 32) acc += Si[j] * (double)x[j];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(kFullG, acc, o);
         if (c.lane == 0) r[i] = (float)(b[i] - acc);
@@ -2027,6 +2031,7 @@ enum GridForm {
 
 struct GridHost {
     std::vector<int32_t> cam_list, item_off, fcam, boff, tfirst;
+    std::vector<int32_t> tlast;  // per tile row I: the last tile row J with tfirst[J] <= I (S's extent)
     std::vector<int4> items;
     std::vector<int2> blocks;
     RawVec<int2> pairs;
@@ -2099,6 +2104,7 @@ void build_grid_host(const HostWindow& h, GridHost& g, int form, HostPool* pool)
     g.pairs.resize(1);
     g.pairs[0] = make_int2(0, 0);
     g.tfirst.assign(1, 0);
+    g.tlast.assign(1, 0);
     g.pan_off.assign(2, 0);
     g.tr_off.assign(2, 0);
     g.tr_skip.assign(1, 0);
@@ -2361,6 +2367,10 @@ void build_grid_host(const HostWindow& h, GridHost& g, int form, HostPool* pool)
         }
         g.tfirst[I] = first;
     }
+    // the symmetric envelope's extent: row i of the mirrored S is zero beyond tile tlast[i / 32]
+    g.tlast.assign(std::max(1, nt), 0);
+    for (int J = 0; J < nt; ++J)
+        for (int I = g.tfirst[J]; I <= J; ++I) g.tlast[I] = std::max(g.tlast[I], J);
     g.pan_off.assign(nt + 1, 0);
     g.tr_off.assign(nt + 1, 0);
     g.pan_row.clear();
@@ -2539,6 +2549,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     int32_t* d_boff = dv.alloc<int32_t>(g.boff.size());
     int2* d_pairs = dv.alloc<int2>(g.pairs.size());
     int32_t* d_tfirst = dv.alloc<int32_t>(g.tfirst.size());
+    int32_t* d_tlast = dv.alloc<int32_t>(std::max<size_t>(1, g.tlast.size()));
     int32_t* d_pan_off = dv.alloc<int32_t>(g.pan_off.size());
     int32_t* d_pan_row = dv.alloc<int32_t>(g.pan_row.size());
     int32_t* d_tr_off = dv.alloc<int32_t>(g.tr_off.size());
@@ -2680,6 +2691,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     chk(up(d_pairs, g.pairs, st));
     chk(up(d_sitems, g.sitems, st));
     chk(up(d_tfirst, g.tfirst, st));
+    chk(up(d_tlast, g.tlast, st));
     chk(up(d_pan_off, g.pan_off, st));
     chk(up(d_pan_row, g.pan_row, st));
     chk(up(d_tr_off, g.tr_off, st));
@@ -2955,7 +2967,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
         }
         // x0 = S32^-1 (float)b; y = S32^-1 (b - S x0); b <- x0 + y (the solves convert on load and store)
         chk(chol_solve(d_LT32, d_LN32, d_DI32, m, d_pan_off, d_pan_row, d_x32, g.max_npan, st, d_bs));
-        k_s_residual<<<nsm_blocks, TB, 0, st>>>(d_S, d_x32, d_bs, m, d_y32);
+        k_s_residual<<<nsm_blocks, TB, 0, st>>>(d_S, d_x32, d_bs, m, d_tfirst, d_tlast, d_y32);
         chk(chol_solve(d_LT32, d_LN32, d_DI32, m, d_pan_off, d_pan_row, d_y32, g.max_npan, st, nullptr, d_x32, d_bs));
         chk(cudaGetLastError());
         return true;
