@@ -22,7 +22,9 @@
  *    belongs to the caller's adapter (nav24_gb300/adapter/GraphOptimGpu.cpp does it).
  *
  * Threading: one context per host thread.  A context owns one CUDA stream and its device
- * buffers; every call on it is synchronous (it returns after results are on the host).
+ * buffers; every call on it is synchronous (it returns after results are on the host).  Device
+ * and page-locked buffers are kept across calls and grow to the largest call (a large-problem
+ * solve's buffers included); nav_ba_destroy frees them.
  */
 #ifndef NAV_BA_H
 #define NAV_BA_H
