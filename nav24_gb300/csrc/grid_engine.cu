@@ -74,9 +74,10 @@ __device__ __forceinline__ CC grid_view() {
     return c;
 }
 
-// Block reduction (sum or max) of one double; thread 0 writes out[blockIdx.x].
+// Block reduction (sum or max) of one double; thread 0 writes out[blockIdx.x] (out[slot] when
+// slot >= 0).
 template <bool MAX>
-__device__ void block_partial(double v, double* out) {
+__device__ void block_partial(double v, double* out, int slot = -1) {
     __shared__ double red[32];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -88,7 +89,7 @@ __device__ void block_partial(double v, double* out) {
     if (threadIdx.x == 0) {
         double r = red[0];
         for (int i = 1; i < (int)(blockDim.x >> 5); ++i) r = MAX ? fmax(r, red[i]) : r + red[i];
-        out[blockIdx.x] = r;
+        out[slot >= 0 ? slot : (int)blockIdx.x] = r;
     }
 }
 
@@ -903,27 +904,63 @@ __global__ void k_s_residual(const double* S, const float* x, const double* b, i
     }
 }
 
-// Cameras: trial = exp(dx_a) * current for free cameras; Real copies (and FP64 ones into camd,
-// when given); scale part.  A thread per camera: the trial's launch takes warp-sized blocks, since
-// an FP64 instruction occupies its SM partition 64 cycles per warp whatever its active lanes, and
-// a warp per SM spreads the cameras' FP64 work over as many partitions as there are warps.
+// Camera k: trial = exp(dx_a) * current when free; Real copy (and FP64 one into camd, when
+// given); returns its term of the step scale dx^T (lambda dx + b).
+template <class Real>
+__device__ double update_camera(int k, const CamState* cur, CamState* trial, Real* camr_trial, const int32_t* cam_free,
+                                const double* dc, const double* U, double lambda, double* camd) {
+    double sc = 0.0;
+    const int a = cam_free[k];
+    if (a >= 0) {
+        se3_left_update(dc + 6 * a, cur[k], trial[k]);
+        for (int r = 0; r < 6; ++r) sc += dc[6 * a + r] * (lambda * dc[6 * a + r] + U[28LL * a + 21 + r]);
+    } else {
+        trial[k] = cur[k];
+    }
+    cam_real<Real>(trial[k], camr_trial + 12 * k);
+    if (camd) cam_real<double>(trial[k], camd + 12 * k);
+    return sc;
+}
+
+// Cameras, a thread per camera; scale part per block.
 template <class Real>
 __global__ void k_update_cams(const CamState* cur, CamState* trial, Real* camr_trial, const int32_t* cam_free, int nc,
-                              const double* dc, const double* U, double lambda, double* part, double* camd = nullptr) {
-    double sc = 0.0;
+                              const double* dc, const double* U, double lambda, double* part) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < nc) {
-        const int a = cam_free[k];
-        if (a >= 0) {
-            se3_left_update(dc + 6 * a, cur[k], trial[k]);
-            for (int r = 0; r < 6; ++r) sc += dc[6 * a + r] * (lambda * dc[6 * a + r] + U[28LL * a + 21 + r]);
-        } else {
-            trial[k] = cur[k];
-        }
-        cam_real<Real>(trial[k], camr_trial + 12 * k);
-        if (camd) cam_real<double>(trial[k], camd + 12 * k);
-    }
+    const double sc = k < nc ? update_camera<Real>(k, cur, trial, camr_trial, cam_free, dc, U, lambda, nullptr) : 0.0;
     block_partial<false>(sc, part);
+}
+
+// A damping trial's updates in one launch.  First a block per 32 cameras whose warp 0 alone works
+// (a thread per camera, its warp's partial into part_c[g]): an FP64 instruction occupies its SM
+// partition 64 cycles per warp whatever its active lanes, so the cameras' FP64 work (SE(3)
+// exponential and products) is spread over as many SMs as there are warps of cameras; 200
+// cameras in one 256-thread block (two warps per partition) took 28 us, and a launch of their own
+// ~5 us more beside the points' launch.  Then npb blocks of points, as a launch of npb blocks of
+// k_update_points would run them (its partials into part_p).  256 threads; at most 64 registers,
+// so that four blocks fit per SM.
+template <class Real>
+__global__ void __launch_bounds__(256, 4)
+    k_update_trial(WinArgs<Real> A, WinDesc D, double lambda, const double* dc, int cur, int ncb, int npb,
+                   double* part_p, const CamState* cams_cur, CamState* cams_trial, Real* camr_trial,
+                   const int32_t* cam_free, int nc, const double* U, double* part_c, double* camd) {
+    if ((int)blockIdx.x >= ncb) {
+        const int b = blockIdx.x - ncb;  // the point block
+        CC c = grid_view();
+        c.gt = b * blockDim.x + threadIdx.x;
+        c.CT = npb * blockDim.x;
+        c.gw = b * c.nw + c.wid;
+        c.CW = npb * c.nw;
+        block_partial<false>(update_points<Real>(A, c, D, lambda, dc, cur), part_p, b);
+        return;
+    }
+    if (threadIdx.x >= 32) return;
+    const int g = blockIdx.x, k = g * 32 + threadIdx.x;
+    double sc =
+        k < nc ? update_camera<Real>(k, cams_cur, cams_trial, camr_trial, cam_free, dc, U, lambda, camd) : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sc += __shfl_down_sync(kFullG, sc, o);
+    if (threadIdx.x == 0) part_c[g] = sc;
 }
 
 template <class Real>
@@ -2589,7 +2626,7 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
     const int nsm_blocks = 152 * 4;
     const int pblocks = std::max(1, std::min(nsm_blocks, (np + TB - 1) / TB));
     const int cblocks = std::max(1, (nc + TB - 1) / TB);
-    const int ucblocks = std::max(1, (nc + 31) / 32);  // the trial's camera update: warp-sized blocks
+    const int ucblocks = std::max(1, (nc + 31) / 32);  // the trial's camera update: 32 cameras per block
     const int rblocks = (nfc * 27 + TB - 1) / TB;  // partials of the camera blocks' maxima
     const int npart = std::max(5 * pblocks, std::max(cblocks, pblocks + rblocks + 1));
     double* d_part = dv.alloc<double>(npart);
@@ -3224,9 +3261,9 @@ cudaError_t grid_solve_typed(const HostWindow& h, const LmOptions& lm, const Int
                 if (!ok) chk(cudaMemsetAsync(d_bs, 0, sizeof(double) * m, st));
                 chk(cudaGetLastError());
             }
-            k_update_cams<Real><<<ucblocks, 32, 0, st>>>(cams[cur], cams[cur ^ 1], camr[cur ^ 1], d_cam_free, nc, d_bs,
-                                                          d_U, lambda, d_tpart + pblocks, mixed ? d_camd : nullptr);
-            k_update_points<Real><<<pblocks, TB, 0, st>>>(A, D, lambda, d_bs, cur, d_tpart + pblocks + ucblocks);
+            k_update_trial<Real><<<ucblocks + pblocks, TB, 0, st>>>(
+                A, D, lambda, d_bs, cur, ucblocks, pblocks, d_tpart + pblocks + ucblocks, cams[cur], cams[cur ^ 1],
+                camr[cur ^ 1], d_cam_free, nc, d_U, d_tpart + pblocks, mixed ? d_camd : nullptr);
             set_radial(A.intr, kcur[0] + dk[0], kcur[1] + dk[1]);
             {  // the trial cost (FP64 in both forms; the mixed form's FP64 cameras from the update)
                 const int buf = cur ^ 1;
