@@ -6,8 +6,8 @@
 // Jacobian as the full edge with the point block dropped.  The LM control is the one of the other
 // engines (g2o OptimizationAlgorithmLevenberg::solve semantics) on the 6x6 normal equations:
 //   the block's threads stride over the problem's observations (structure of arrays: point [n][4],
-//   uv [n][2]); H (21 packed) and b (6) accumulate per thread in Real and are summed in FP64 (warp
-//   butterfly, then over the warps in order); thread 0 factors H + lambda I (FP64 Cholesky, in
+//   uv [n][2]); H (21 packed) and b (6) accumulate per thread in Real and are summed in FP64 (a
+//   warp reduce-scatter, then over the warps in order); thread 0 factors H + lambda I (FP64 Cholesky, in
 //   registers), applies the SE(3) update and makes the LM decisions, which the block reads from
 //   shared memory; costs are FP64 per-thread partial sums reduced the same way (fixed order:
 //   bitwise repeatable).  A single frame is one block, not one warp: its dependent FP64 chains
@@ -42,6 +42,33 @@ __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kPoseFull, v, o);
     return v;
+}
+
+// Warp reduce-scatter of N <= 32 values per lane: lane k < N returns the warp's total of value k.
+// Recursive halving over lane bits 4..0: at each level a lane keeps one half of its values (the
+// upper when its lane bit is set) and adds its partner's copy of that half, so lane k ends with
+// value k, summed over the same tree as warp_sum's butterfly (pairs across lane bit 4, then 3, ..
+// 0) and equal to it bit for bit.  31 shuffles and FP64 adds per lane for all N values, against 5
+// per value with a butterfly each: on GB300 an FP64 instruction occupies its SM partition 64
+// cycles per warp, and the 27 butterflies of H and b were half of the mixed form's FP64 work.
+template <int N>
+__device__ __forceinline__ double warp_reduce_scatter(const double (&v)[N]) {
+    static_assert(N >= 1 && N <= 32, "one value per lane at most");
+    const int lane = threadIdx.x & 31;
+    double a[32];
+#pragma unroll
+    for (int k = 0; k < 32; ++k) a[k] = k < N ? v[k] : 0.0;
+#pragma unroll
+    for (int h = 16; h >= 1; h >>= 1) {
+        const bool up = (lane & h) != 0;
+#pragma unroll
+        for (int j = 0; j < h; ++j) {
+            const double keep = up ? a[j + h] : a[j];
+            const double send = up ? a[j] : a[j + h];
+            a[j] = keep + __shfl_xor_sync(kPoseFull, send, h);
+        }
+    }
+    return a[0];
 }
 
 template <class Real>
@@ -144,10 +171,15 @@ __global__ void __launch_bounds__(kPoseThreads) pose_lm_kernel(PoseArgs A) {
     // sum over the block of N per-thread values, returned in s_tot (read after the call)
     auto block_sum = [&](auto& v) {
         constexpr int nv = (int)(sizeof(v) / sizeof(v[0]));
+        if constexpr (nv == 1) {
+            const double t = warp_sum((double)v[0]);
+            if (lane == 0) s_part[wid][0] = t;
+        } else {
+            double dv[nv];
 #pragma unroll
-        for (int k = 0; k < nv; ++k) {
-            const double t = warp_sum((double)v[k]);
-            if (lane == 0) s_part[wid][k] = t;
+            for (int k = 0; k < nv; ++k) dv[k] = (double)v[k];
+            const double t = warp_reduce_scatter<nv>(dv);
+            if (lane < nv) s_part[wid][lane] = t;
         }
         __syncthreads();
         if (tid < nv) {
